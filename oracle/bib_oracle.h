@@ -1,0 +1,101 @@
+/*
+ * bib_oracle -- CPU restatement of the reference's hot IB-LBM time step.
+ *
+ * TEST INFRASTRUCTURE ONLY.  Only tests/, __graft_entry__.smoke() and the CPU
+ * baseline legs of bench.py load this library; the product never links it.
+ *
+ * It restates, in plain C and FP64, the arithmetic of niclasberg/biblbm
+ * (Palabos + src/fsi) on the hot path, function by function, citing the
+ * reference file:line each one follows.  It is pinned against the reference's own
+ * code through the fixtures in tests/golden/ (generated by running the compiled
+ * reference, see tests/golden/make_golden.py).  Parts with no reference
+ * counterpart (TRT collision, halfway / moving-wall bounce-back, the Peskin kernel
+ * inside the IB step) are restatements of the published methods and are pinned by
+ * analytic solutions in the tests instead.
+ *
+ * Conventions: lattice fields are structure-of-arrays, component-major, x fastest:
+ * value(c, x, y, z) = a[c*n + x + nx*(y + ny*z)], n = nx*ny*nz.  Populations are
+ * stored as f-bar = f - t_i (Palabos DefaultRoundOffPolicy, roundOffPolicy.h:72-90)
+ * and represent the post-streaming state, the state Palabos holds between steps.
+ */
+#ifndef BIB_ORACLE_H
+#define BIB_ORACLE_H
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { ORC_COLLISION_BGK_GUO_VOF = 0, ORC_COLLISION_BGK = 1, ORC_COLLISION_TRT = 2 };
+enum { ORC_WALL_NONE = 0, ORC_WALL_FD_VELOCITY = 1, ORC_WALL_HALFWAY_BB = 2 };
+enum { ORC_DIRAC_ROMA = 0, ORC_DIRAC_PESKIN = 1 };
+enum {
+    ORC_MODEL_CAPSULE_NEOHOOKEAN = 0,
+    ORC_MODEL_CAPSULE_SKALAK = 1,
+    ORC_MODEL_RBC_WLCPOW = 2,
+    ORC_MODEL_SKALAK_BENDING = 3
+};
+
+/* Index of the membrane parameter vector (12 doubles). */
+enum {
+    ORC_P_G = 0, ORC_P_C, ORC_P_NU_S, ORC_P_KB, ORC_P_SHEAR_MODULUS, ORC_P_L0, ORC_P_K_AREA_GLOBAL,
+    ORC_P_K_AREA_LOCAL, ORC_P_K_VOLUME, ORC_P_VOL_DESIRED, ORC_P_K_BEND, ORC_P_THETA0, ORC_P_COUNT
+};
+
+typedef struct {
+    int64_t nx, ny, nz;
+    int32_t periodic[3];
+    int32_t collision;
+    int32_t wall_y, wall_z;     /* walls on the y / z faces when that axis is not periodic */
+    double omega, omega_inner;  /* GuoExternalForceVOFDynamics(omega1, omega2) */
+    double trt_magic;
+    double wall_u[4][3];        /* velocity of the y-, y+, z-, z+ walls */
+    int32_t envelope_swap;      /* reproduce the reference's periodic-envelope omega swap (see .c) */
+} orc_lattice;
+
+/* ---- lattice ---- */
+void orc_collide_cell(const orc_lattice* L, double* f19, const double* F3, double phase);
+void orc_collide_stream(const orc_lattice* L, double* f, double* ftmp, const double* F, const double* phase);
+void orc_apply_fd_walls(const orc_lattice* L, double* f, const double* F);
+void orc_compute_velocity(const orc_lattice* L, const double* f, const double* F, double* u);
+void orc_init_equilibrium(const orc_lattice* L, double* f, const double* rho, const double* u);
+
+/* ---- shapes and membranes ---- */
+int64_t orc_shape_connectivity(int64_t nv, const double* xyz, int64_t nt, const int64_t* tri,
+                               int64_t* links, double* link_len, int64_t* pairs, double* pair_cs,
+                               double* tri_area, double* props, int64_t* npairs);
+void orc_particle_update(int64_t nv, const double* pos, int64_t nt, const int64_t* tri, double* out5);
+void orc_inertia(const double* pos, int64_t nt, const int64_t* tri, double* out9);
+void orc_membrane_forces(int32_t model, const double* prm, int64_t nv, const double* rest, int64_t nt,
+                         const int64_t* tri, const double* tri_area, double A0, int64_t nl, const int64_t* links,
+                         const double* link_len, int64_t np, const int64_t* pairs, const double* pair_cs,
+                         const double* pos, double area, double volume, double* force);
+
+/* ---- immersed boundary ---- */
+double orc_dirac(int32_t dirac, double r);
+void orc_classify(const orc_lattice* L, int32_t dirac, int64_t n, const double* pos, int32_t* cls);
+void orc_interpolate(const orc_lattice* L, int32_t dirac, double offset, const double* u, int64_t n,
+                     const double* pos, const int32_t* cls, double* vel);
+void orc_spread(const orc_lattice* L, int32_t dirac, double offset, int64_t n, const double* pos,
+                const double* force, const int32_t* cls, double* F);
+
+/* ---- coupled system (mirrors the product's C ABI) ---- */
+typedef struct orc_sys orc_sys;
+orc_sys* orc_sys_create(const orc_lattice* L, int32_t dirac, double ib_offset);
+void orc_sys_destroy(orc_sys* s);
+double* orc_sys_f(orc_sys* s);
+double* orc_sys_force(orc_sys* s);
+double* orc_sys_phase(orc_sys* s);
+void orc_sys_set_body_force(orc_sys* s, const double* b3);
+int32_t orc_sys_add_shape(orc_sys* s, int64_t nv, const double* xyz, int64_t nt, const int64_t* tri);
+int32_t orc_sys_add_particle(orc_sys* s, int32_t shape, int32_t model, const double* prm, const double* pos);
+void orc_sys_init(orc_sys* s);
+void orc_sys_step(orc_sys* s, int64_t nsteps);
+void orc_sys_lattice_only_step(orc_sys* s, int64_t nsteps);
+void orc_sys_get_particle(orc_sys* s, int32_t pid, double* pos, double* vel, double* force, double* stats5);
+void orc_sys_velocity(orc_sys* s, double* u);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,525 @@
+// Oracle harness: runs the REFERENCE's own FP64 code (Palabos + src/fsi of
+// niclasberg/biblbm, compiled in place from the reference sources) on inputs
+// written by tests/golden/make_golden.py and dumps what it computes.
+//
+// Test infrastructure only.  Nothing here is linked into the product.
+//
+// Cases (argv[1]):
+//   lbm     collide-and-stream on a periodic box or in simple shear with the
+//           finite-difference velocity walls of progs/common/shear_flow_setup.h:51-96
+//   ibm     coupled IB-LBM steps in the order of
+//           progs/capsule_in_shear/capsule_in_shear.cpp:187-227
+//   forces  one call of a particle's compute_forces() at given vertex positions
+//   interp  Roma / Peskin interpolation and spreading through the fsi templates
+//           (ImmersedBoundaryDynamics_interpolation.hh, ImmersedBoundaryDynamics_forces.hh)
+//   shape   ParticleShape rest geometry and connectivity (ParticleShape.hh:21-212)
+//   inertia DeformableParticle3D::compute_moment_of_intertia (DeformableParticle3D.hh:173-272)
+//
+// Array conventions: lattice fields are (components, nz, ny, nx) with x fastest.
+#define FSI_PROFILE
+#include "palabos3D.h"
+#include "palabos3D.hh"
+#include "fsi/headers.h"
+#include "fsi/headers.hh"
+
+#include <string>
+#include <vector>
+#include "rec_io.h"
+
+using namespace plb;
+using namespace fsi;
+using recio::Bundle;
+using recio::shp;
+
+#define DESCRIPTOR descriptors::ForcedPhaseD3Q19Descriptor
+typedef double T;
+typedef MultiBlockLattice3D<T, DESCRIPTOR> Lattice;
+
+static const int Q = 19;
+
+// ---------------------------------------------------------------------------
+// shear flow setup, same steps as progs/common/shear_flow_setup.h:51-96
+static T shear_velocity(plint iY, plint Ny, T U) {
+    const T b = Ny - 1;
+    const T y = 2.0 * (T)iY / b - 1;
+    return U * y;
+}
+struct ShearRhoU {
+    plint ny; T U;
+    ShearRhoU(plint ny_, T U_) : ny(ny_), U(U_) {}
+    void operator()(plint, plint iY, plint, T& rho, Array<T, 3>& u) const {
+        rho = (T)1; u[0] = shear_velocity(iY, ny, U); u[1] = T(); u[2] = T();
+    }
+};
+struct ShearU {
+    plint ny; T U;
+    ShearU(plint ny_, T U_) : ny(ny_), U(U_) {}
+    void operator()(plint, plint iY, plint, Array<T, 3>& u) const {
+        u[0] = shear_velocity(iY, ny, U); u[1] = T(); u[2] = T();
+    }
+};
+static void shear_setup(Lattice& lattice, T U, OnLatticeBoundaryCondition3D<T, DESCRIPTOR>& bc) {
+    const plint nx = lattice.getNx(), ny = lattice.getNy(), nz = lattice.getNz();
+    Box3D top(0, nx - 1, ny - 1, ny - 1, 0, nz - 1);
+    Box3D bottom(0, nx - 1, 0, 0, 0, nz - 1);
+    lattice.periodicity().toggle(0, true);
+    lattice.periodicity().toggle(2, true);
+    bc.addVelocityBoundary1N(bottom, lattice);
+    bc.addVelocityBoundary1P(top, lattice);
+    initializeAtEquilibrium(lattice, lattice.getBoundingBox(), ShearRhoU(ny, U));
+    setBoundaryVelocity(lattice, lattice.getBoundingBox(), ShearU(ny, U));
+    lattice.initialize();
+}
+
+// ---------------------------------------------------------------------------
+static size_t lidx(plint x, plint y, plint z, plint nx, plint ny) { return (size_t)x + nx * ((size_t)y + ny * (size_t)z); }
+
+// With PLB_MPI_PARALLEL, MultiBlockLattice3D::get() returns a proxy cell whose
+// population writes do not reach the blocks
+// (parallelism/parallelMultiBlockLattice3D.hh:69-87), so cells are reached
+// through the single atomic block (fsi requires exactly one block per rank,
+// ImmersedBoundaryDynamics.hh:51-54).
+static plb::Cell<T, DESCRIPTOR>& cell_at(Lattice& lat, plint x, plint y, plint z) {
+    plint id = lat.getLocalInfo().getBlocks()[0];
+    SmartBulk3D bulk(lat.getMultiBlockManagement(), id);
+    return lat.getComponent(id).get(bulk.toLocalX(x), bulk.toLocalY(y), bulk.toLocalZ(z));
+}
+static Array<T, 3>& vel_at(MultiTensorField3D<T, 3>& f, plint x, plint y, plint z) {
+    plint id = f.getLocalInfo().getBlocks()[0];
+    SmartBulk3D bulk(f.getMultiBlockManagement(), id);
+    return f.getComponent(id).get(bulk.toLocalX(x), bulk.toLocalY(y), bulk.toLocalZ(z));
+}
+
+static void dump_lattice(recio::Writer& w, const std::string& tag, Lattice& lattice) {
+    const plint nx = lattice.getNx(), ny = lattice.getNy(), nz = lattice.getNz();
+    const size_t n = (size_t)nx * ny * nz;
+    std::vector<double> f(Q * n), F(3 * n);
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x) {
+                plb::Cell<T, DESCRIPTOR>& c = cell_at(lattice, x, y, z);
+                size_t k = lidx(x, y, z, nx, ny);
+                for (int i = 0; i < Q; ++i) f[i * n + k] = c[i];
+                for (int d = 0; d < 3; ++d) F[d * n + k] = c.getExternal(0)[d];
+            }
+    w.d("fbar_" + tag, shp(Q, nz, ny, nx), f);
+    w.d("force_" + tag, shp(3, nz, ny, nx), F);
+}
+
+static void dump_velocity(recio::Writer& w, const std::string& tag, Lattice& lattice) {
+    const plint nx = lattice.getNx(), ny = lattice.getNy(), nz = lattice.getNz();
+    const size_t n = (size_t)nx * ny * nz;
+    std::auto_ptr<MultiTensorField3D<T, 3> > vel = generateMultiTensorField<T, 3>(lattice.getBoundingBox());
+    computeVelocity(lattice, *vel, lattice.getBoundingBox());
+    std::vector<double> u(3 * n);
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x) {
+                Array<T, 3>& v = vel_at(*vel, x, y, z);
+                size_t k = lidx(x, y, z, nx, ny);
+                for (int d = 0; d < 3; ++d) u[d * n + k] = v[d];
+            }
+    w.d("u_" + tag, shp(3, nz, ny, nx), u);
+}
+
+static void load_lattice(const Bundle& in, Lattice& lattice, bool pops) {
+    const plint nx = lattice.getNx(), ny = lattice.getNy(), nz = lattice.getNz();
+    const size_t n = (size_t)nx * ny * nz;
+    const recio::Array* f = pops ? &recio::need(in, "fbar") : 0;
+    const recio::Array* F = recio::has(in, "force") ? &recio::need(in, "force") : 0;
+    const recio::Array* ph = recio::has(in, "phase") ? &recio::need(in, "phase") : 0;
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x) {
+                plb::Cell<T, DESCRIPTOR>& c = cell_at(lattice, x, y, z);
+                size_t k = lidx(x, y, z, nx, ny);
+                if (f) for (int i = 0; i < Q; ++i) c[i] = f->d[i * n + k];
+                if (F) for (int d = 0; d < 3; ++d) c.getExternal(0)[d] = F->d[d * n + k];
+                if (ph) c.getExternal(0)[3] = ph->d[k];
+            }
+    lattice.duplicateOverlaps(modif::staticVariables);
+}
+
+static int run_lbm(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    const T omega = recio::need(in, "omega").d[0], omega_in = recio::need(in, "omega").d[1];
+    const long long walls = recio::inum(in, "walls");
+    const long long steps = recio::inum(in, "steps");
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(omega, omega_in));
+    lattice.toggleInternalStatistics(false);
+    std::auto_ptr<OnLatticeBoundaryCondition3D<T, DESCRIPTOR> > bc(createInterpBoundaryCondition3D<T, DESCRIPTOR>());
+    if (walls == 0) {
+        lattice.periodicity().toggleAll(true);
+        lattice.initialize();  // sets up the periodic envelope exchange before the state is loaded
+        load_lattice(in, lattice, true);
+    } else {
+        shear_setup(lattice, recio::num(in, "U"), *bc);
+        load_lattice(in, lattice, false);
+    }
+    recio::Writer w(out);
+    dump_lattice(w, "0", lattice);
+    dump_velocity(w, "0", lattice);
+    for (long long it = 0; it < steps; ++it) {
+        lattice.collideAndStream();
+        if (it == 0) {
+            dump_lattice(w, "1", lattice);
+            dump_velocity(w, "1", lattice);
+        }
+    }
+    dump_lattice(w, "end", lattice);
+    dump_velocity(w, "end", lattice);
+    return 0;
+}
+
+// ---------------------------------------------------------------------------
+// Particles
+
+// Composite membrane used by the spec RBC configurations: the capsule's
+// Skalak in-plane law (DeformableCapsule.hh:68-150) plus the RBC model's global /
+// local area, volume and dihedral-bending terms (RBCParticle.hh:175-246).  The RBC
+// part is evaluated by a genuine RBCParticle with zero shear modulus, whose WLC-POW
+// link term is then identically zero (ks = kp = 0, RBCParticle.hh:27-44).
+class SkalakBendingParticle : public DeformableCapsuleParticle<T> {
+public:
+    SkalakBendingParticle(const ParticleShape<T>* s, const CapsuleParameters<T>& cp, const RBCParameters<T>& rp)
+        : DeformableCapsuleParticle<T>(s, cp), rbc_(s, rp) {}
+    virtual SkalakBendingParticle* clone() const { return new SkalakBendingParticle(*this); }
+    virtual void compute_forces() {
+        DeformableCapsuleParticle<T>::compute_forces();
+        for (plint i = 0; i < this->count_nodes(); ++i) rbc_.get_node(i).pos = this->get_node(i).pos;
+        rbc_.update();
+        rbc_.reset_forces();
+        rbc_.compute_forces();
+        for (plint i = 0; i < this->count_nodes(); ++i) this->get_node(i).force += rbc_.get_node(i).force;
+    }
+private:
+    RBCParticle<T> rbc_;
+};
+
+// DeformableCapsuleParticle has no setter for its shear law; it is serialised
+// (DeformableCapsule.hh:215-221), so select it by pack -> patch -> unpack.
+static void select_capsule_law(DeformableCapsuleParticle<T>& p, int skalak) {
+    std::vector<char> buf;
+    p.pack(buf);
+    size_t off = sizeof(plint) + sizeof(pluint) + sizeof(plint) + sizeof(bool) + (size_t)p.count_nodes() * 9 * sizeof(T);
+    int law = skalak ? 0 : 1;  // enum ShearModel {Skalak, NeoHookean}
+    std::memcpy(&buf[off], &law, sizeof(int));
+    char* it = &buf[sizeof(plint) + sizeof(pluint)];
+    p.unpack(it);
+}
+
+struct ParticleSpec {
+    long long model;  // 0 capsule NeoHookean, 1 capsule Skalak, 2 RBC (WLC-POW), 3 Skalak + bending composite
+    std::vector<double> prm;
+};
+
+static ParticleBase3D<T>* make_particle(const ParticleShape<T>* shape, const ParticleSpec& s) {
+    // prm layout: [G, C, nu_s, kb, shear_modulus, L0, k_area_global, k_area_local, k_volume, vol_desired, k_bend, theta0]
+    CapsuleParameters<T> cp;
+    cp.G = s.prm[0]; cp.C = s.prm[1]; cp.nu_s = s.prm[2]; cp.kb = s.prm[3];
+    RBCParameters<T> rp;
+    rp.shear_modulus = s.prm[4]; rp.L0 = s.prm[5]; rp.k_area_global = s.prm[6]; rp.k_area_local = s.prm[7];
+    rp.k_volume = s.prm[8]; rp.vol_desired = s.prm[9]; rp.k_bend = s.prm[10]; rp.theta0 = s.prm[11];
+    if (s.model == 0 || s.model == 1) {
+        DeformableCapsuleParticle<T>* p = new DeformableCapsuleParticle<T>(shape, cp);
+        select_capsule_law(*p, s.model == 1);
+        return p;
+    }
+    if (s.model == 2) return new RBCParticle<T>(shape, rp);
+    SkalakBendingParticle* p = new SkalakBendingParticle(shape, cp, rp);
+    select_capsule_law(*p, 1);
+    return p;
+}
+
+static void store_shape(const Bundle& in, ParticleShapeLibrary<T>& lib, const char* xyz_name) {
+    const recio::Array& xyz = recio::need(in, xyz_name);
+    const recio::Array& tri = recio::need(in, "tri");
+    const unsigned nv = (unsigned)xyz.shape[0], nt = (unsigned)tri.shape[0];
+    std::vector<Array<T, 3> > v(nv);
+    for (unsigned i = 0; i < nv; ++i) v[i] = Array<T, 3>(xyz.d[3 * i], xyz.d[3 * i + 1], xyz.d[3 * i + 2]);
+    std::vector<unsigned> idx(3 * nt);
+    for (unsigned i = 0; i < 3 * nt; ++i) idx[i] = (unsigned)tri.i[i];
+    lib.store_mesh(&v[0], &idx[0], nv, nt, "shape");
+}
+
+static void set_positions(ParticleBase3D<T>& p, const recio::Array& pos) {
+    for (plint i = 0; i < p.count_nodes(); ++i)
+        p.get_node(i).pos = Array<T, 3>(pos.d[3 * i], pos.d[3 * i + 1], pos.d[3 * i + 2]);
+    p.update();
+}
+
+static ParticleSpec read_spec(const Bundle& in) {
+    ParticleSpec s;
+    s.model = recio::inum(in, "model");
+    s.prm = recio::need(in, "params").d;
+    return s;
+}
+
+static int run_forces(const Bundle& in, const char* out) {
+    ParticleShapeLibrary<T> lib;
+    store_shape(in, lib, "rest");
+    const ParticleShape<T>* shape = lib.get_by_tag("shape");
+    ParticleBase3D<T>* p = make_particle(shape, read_spec(in));
+    set_positions(*p, recio::need(in, "pos"));
+    p->reset_forces();
+    p->compute_forces();
+    const plint nv = p->count_nodes();
+    std::vector<double> F(3 * nv);
+    for (plint i = 0; i < nv; ++i)
+        for (int d = 0; d < 3; ++d) F[3 * i + d] = p->get_node(i).force[d];
+    recio::Writer w(out);
+    w.d("force", shp(nv, 3), F);
+    w.d("area", shp(1), std::vector<double>(1, p->area()));
+    w.d("volume", shp(1), std::vector<double>(1, p->volume()));
+    std::vector<double> com(3);
+    for (int d = 0; d < 3; ++d) com[d] = p->center_of_mass()[d];
+    w.d("com", shp(3), com);
+    delete p;
+    return 0;
+}
+
+template <class Periodicity>
+static int run_ibm_impl(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    const T tau = recio::num(in, "tau");
+    const T lambda = recio::has(in, "lambda") ? recio::num(in, "lambda") : 1.0;
+    const long long walls = recio::inum(in, "walls");
+    const long long steps = recio::inum(in, "steps");
+    const T tau_inner = 0.5 + lambda * (tau - 0.5);
+    const T omega = 1. / tau, omega_inner = 1. / tau_inner;
+
+    ParticleShapeLibrary<T> lib;
+    store_shape(in, lib, "rest");
+    const ParticleShape<T>* shape = lib.get_by_tag("shape");
+    ParticleBase3D<T>* proto = make_particle(shape, read_spec(in));
+    set_positions(*proto, recio::need(in, "pos"));
+
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(omega, omega_inner));
+    lattice.toggleInternalStatistics(false);
+    Box3D domain = lattice.getBoundingBox();
+    std::auto_ptr<OnLatticeBoundaryCondition3D<T, DESCRIPTOR> > bc(createInterpBoundaryCondition3D<T, DESCRIPTOR>());
+    if (walls == 1) {
+        shear_setup(lattice, recio::num(in, "U"), *bc);
+    } else {
+        lattice.periodicity().toggleAll(true);
+        initializeAtEquilibrium(lattice, domain, (T)1, Array<T, 3>(0., 0., 0.));
+        lattice.initialize();
+    }
+    ImmersedBoundaryDynamics3D<T, DESCRIPTOR, Periodicity> fsi(lattice, lib);
+    std::auto_ptr<MultiTensorField3D<T, 3> > velocity = generateMultiTensorField<T, 3>(domain);
+    fsi.add_particle(proto);
+    fsi.init();
+
+    const plint nv = proto->count_nodes();
+    std::vector<double> pos((steps + 1) * nv * 3), vel(steps * nv * 3), frc(steps * nv * 3);
+    std::vector<double> vol(steps + 1), area(steps + 1), com((steps + 1) * 3), inertia((steps + 1) * 9);
+    std::vector<double> body(3, 0.0);
+    if (recio::has(in, "body")) body = recio::need(in, "body").d;
+
+    for (long long it = 0; it <= steps; ++it) {
+        ParticleBase3D<T>* p = 0;
+        fsi.get_particle(0, p);
+        for (plint i = 0; i < nv; ++i)
+            for (int d = 0; d < 3; ++d) pos[(it * nv + i) * 3 + d] = p->get_node(i).pos[d];
+        vol[it] = p->volume();
+        area[it] = p->area();
+        for (int d = 0; d < 3; ++d) com[it * 3 + d] = p->center_of_mass()[d];
+        Matrix<T, 3> I;
+        dynamic_cast<DeformableParticle3D<T>*>(p)->compute_moment_of_intertia(I);
+        for (int a = 0; a < 3; ++a)
+            for (int b = 0; b < 3; ++b) inertia[it * 9 + a * 3 + b] = I(a, b);
+        if (it == steps) break;
+
+        computeVelocity(lattice, *velocity, domain);
+        setExternalVector(lattice, domain, DESCRIPTOR<T>::ExternalField::forceBeginsAt, Array<T, 3>(body[0], body[1], body[2]));
+        applyProcessingFunctional(wrap_ibm_dynamics3D(fsi), domain, lattice, *velocity);
+        fsi.get_particle(0, p);
+        for (plint i = 0; i < nv; ++i)
+            for (int d = 0; d < 3; ++d) {
+                vel[(it * nv + i) * 3 + d] = p->get_node(i).vel[d];
+                frc[(it * nv + i) * 3 + d] = p->get_node(i).force[d];
+            }
+        if (it == 0) {
+            recio::Writer w0((std::string(out) + ".step0").c_str());
+            dump_lattice(w0, "spread", lattice);
+        }
+        lattice.collideAndStream();
+    }
+    recio::Writer w(out);
+    w.d("pos", shp(steps + 1, nv, 3), pos);
+    w.d("vel", shp(steps, nv, 3), vel);
+    w.d("force", shp(steps, nv, 3), frc);
+    w.d("volume", shp(steps + 1), vol);
+    w.d("area", shp(steps + 1), area);
+    w.d("com", shp(steps + 1, 3), com);
+    w.d("inertia", shp(steps + 1, 3, 3), inertia);
+    dump_lattice(w, "end", lattice);
+    dump_velocity(w, "end", lattice);
+    delete proto;
+    return 0;
+}
+
+static int run_ibm(const Bundle& in, const char* out) {
+    if (recio::inum(in, "walls") == 1) return run_ibm_impl<Periodicity3D<T, true, false, true> >(in, out);
+    return run_ibm_impl<Periodicity3D<T, true, true, true> >(in, out);
+}
+
+// ---------------------------------------------------------------------------
+// Interpolation / spreading through the fsi templates with either kernel.
+template <class Periodicity, class Dirac>
+static int run_interp_impl(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    const size_t n = (size_t)nx * ny * nz;
+    Box3D dom(0, nx - 1, 0, ny - 1, 0, nz - 1);
+    typename Periodicity::ArithmeticType arith = Periodicity::create_arithmetic(dom);
+
+    TensorField3D<T, 3> velocity(nx, ny, nz);
+    const recio::Array& u = recio::need(in, "u");
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x)
+                for (int d = 0; d < 3; ++d) velocity.get(x, y, z)[d] = u.d[d * n + lidx(x, y, z, nx, ny)];
+
+    const recio::Array& pos = recio::need(in, "pos");
+    const recio::Array& frc = recio::need(in, "nforce");
+    const plint nn = pos.shape[0];
+    std::vector<NonLocalNode<T> > nodes(nn);
+    for (plint i = 0; i < nn; ++i) {
+        nodes[i].pos = Array<T, 3>(pos.d[3 * i], pos.d[3 * i + 1], pos.d[3 * i + 2]);
+        nodes[i].force = Array<T, 3>(frc.d[3 * i], frc.d[3 * i + 1], frc.d[3 * i + 2]);
+        nodes[i].vel.resetToZero();
+    }
+    recio::Writer w(out);
+    std::vector<double> v(3 * nn);
+
+    interpolation::interpolate<T, typename Periodicity::ArithmeticType, NonLocalNode<T>, Dirac>(dom, velocity, nodes, arith);
+    for (plint i = 0; i < nn; ++i)
+        for (int d = 0; d < 3; ++d) v[3 * i + d] = nodes[i].vel[d];
+    w.d("vel_general", shp(nn, 3), v);
+
+    // The bulk fast paths skip all range checks: only nodes whose support box lies
+    // inside the field are valid for them (the IB class guarantees that through
+    // its bulk_domain, ImmersedBoundaryDynamics.hh:63-65).
+    std::vector<NonLocalNode<T> > bulk_nodes;
+    std::vector<long long> bulk_ids;
+    for (plint i = 0; i < nn; ++i) {
+        Box3D b;
+        get_dirac_compact_support_box<T, Dirac>(nodes[i].pos, b);
+        if (b.x0 >= 0 && b.x1 <= nx - 1 && b.y0 >= 0 && b.y1 <= ny - 1 && b.z0 >= 0 && b.z1 <= nz - 1) {
+            bulk_nodes.push_back(nodes[i]);
+            bulk_ids.push_back(i);
+        }
+    }
+    interpolation::interpolate_bulk<T, typename Periodicity::ArithmeticType, NonLocalNode<T>, Dirac>(dom, velocity, bulk_nodes, arith);
+    std::vector<double> vb(3 * bulk_nodes.size());
+    for (size_t i = 0; i < bulk_nodes.size(); ++i)
+        for (int d = 0; d < 3; ++d) vb[3 * i + d] = bulk_nodes[i].vel[d];
+    w.d("vel_bulk", shp((long long)bulk_nodes.size(), 3), vb);
+    w.i("bulk_ids", shp((long long)bulk_ids.size()), bulk_ids);
+
+    for (int mode = 0; mode < 2; ++mode) {
+        BlockLattice3D<T, DESCRIPTOR> lat(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(1., 1.));
+        for (plint z = 0; z < nz; ++z)
+            for (plint y = 0; y < ny; ++y)
+                for (plint x = 0; x < nx; ++x)
+                    for (int d = 0; d < 4; ++d) lat.get(x, y, z).getExternal(0)[d] = 0.;
+        if (mode == 0)
+            spreading::spread_forces<T, DESCRIPTOR, Dirac, typename Periodicity::ArithmeticType, NonLocalNode<T> >(dom, lat, nodes, arith);
+        else
+            spreading::spread_forces_bulk<T, DESCRIPTOR, Dirac, typename Periodicity::ArithmeticType, NonLocalNode<T> >(dom, lat, bulk_nodes, arith);
+        std::vector<double> F(3 * n);
+        for (plint z = 0; z < nz; ++z)
+            for (plint y = 0; y < ny; ++y)
+                for (plint x = 0; x < nx; ++x)
+                    for (int d = 0; d < 3; ++d) F[d * n + lidx(x, y, z, nx, ny)] = lat.get(x, y, z).getExternal(0)[d];
+        w.d(mode == 0 ? "spread_general" : "spread_bulk", shp(3, nz, ny, nx), F);
+    }
+    return 0;
+}
+
+template <class Periodicity>
+static int run_interp_p(const Bundle& in, const char* out) {
+    if (recio::inum(in, "dirac") == 1) return run_interp_impl<Periodicity, PeskinDirac<T, 3> >(in, out);
+    return run_interp_impl<Periodicity, RomaDirac<T, 3> >(in, out);
+}
+
+static int run_interp(const Bundle& in, const char* out) {
+    const recio::Array& per = recio::need(in, "periodic");
+    int code = (per.i[0] ? 4 : 0) | (per.i[1] ? 2 : 0) | (per.i[2] ? 1 : 0);
+    switch (code) {
+        case 7: return run_interp_p<Periodicity3D<T, true, true, true> >(in, out);
+        case 5: return run_interp_p<Periodicity3D<T, true, false, true> >(in, out);
+        case 4: return run_interp_p<Periodicity3D<T, true, false, false> >(in, out);
+        default: std::fprintf(stderr, "unsupported periodicity\n"); return 2;
+    }
+}
+
+// ---------------------------------------------------------------------------
+static int run_shape(const Bundle& in, const char* out) {
+    ParticleShapeLibrary<T> lib;
+    store_shape(in, lib, "rest");
+    const ParticleShape<T>* s = lib.get_by_tag("shape");
+    recio::Writer w(out);
+    std::vector<long long> links;
+    std::vector<double> lengths;
+    for (typename ParticleShape<T>::link_const_iterator it = s->links_begin(); it != s->links_end(); ++it) {
+        links.push_back(it->i0); links.push_back(it->i1); lengths.push_back(it->length);
+    }
+    w.i("links", shp((long long)lengths.size(), 2), links);
+    w.d("link_length", shp((long long)lengths.size()), lengths);
+    std::vector<long long> pairs;
+    std::vector<double> cs;
+    for (typename ParticleShape<T>::triangle_pair_const_iterator it = s->triangle_pairs_begin(); it != s->triangle_pairs_end(); ++it) {
+        pairs.push_back(it->i0); pairs.push_back(it->i1); pairs.push_back(it->i2); pairs.push_back(it->i3);
+        cs.push_back(it->cos_theta0); cs.push_back(it->sin_theta0);
+    }
+    w.i("pairs", shp((long long)cs.size() / 2, 4), pairs);
+    w.d("pair_cos_sin", shp((long long)cs.size() / 2, 2), cs);
+    std::vector<double> ta;
+    for (typename ParticleShape<T>::triangle_const_iterator it = s->triangles_begin(); it != s->triangles_end(); ++it) ta.push_back(it->area);
+    w.d("tri_area", shp((long long)ta.size()), ta);
+    w.d("area", shp(1), std::vector<double>(1, s->get_area()));
+    w.d("volume", shp(1), std::vector<double>(1, s->get_volume()));
+    std::vector<double> c(3);
+    for (int d = 0; d < 3; ++d) c[d] = s->get_center()[d];
+    w.d("center", shp(3), c);
+    w.d("radius", shp(1), std::vector<double>(1, s->get_radius()));
+    return 0;
+}
+
+static int run_inertia(const Bundle& in, const char* out) {
+    ParticleShapeLibrary<T> lib;
+    store_shape(in, lib, "rest");
+    DeformableCapsuleParticle<T> p(lib.get_by_tag("shape"), CapsuleParameters<T>());
+    set_positions(p, recio::need(in, "pos"));
+    Matrix<T, 3> I;
+    p.compute_moment_of_intertia(I);
+    std::vector<double> v(9);
+    for (int a = 0; a < 3; ++a)
+        for (int b = 0; b < 3; ++b) v[a * 3 + b] = I(a, b);
+    recio::Writer w(out);
+    w.d("inertia", shp(3, 3), v);
+    w.d("volume", shp(1), std::vector<double>(1, p.volume()));
+    return 0;
+}
+
+int main(int argc, char** argv) {
+    if (argc < 4) {
+        std::fprintf(stderr, "usage: ref_harness <lbm|ibm|forces|interp|shape|inertia> in.rec out.rec\n");
+        return 2;
+    }
+    plbInit(&argc, &argv);
+    Bundle in = recio::read_file(argv[2]);
+    std::string c = argv[1];
+    if (c == "lbm") return run_lbm(in, argv[3]);
+    if (c == "ibm") return run_ibm(in, argv[3]);
+    if (c == "forces") return run_forces(in, argv[3]);
+    if (c == "interp") return run_interp(in, argv[3]);
+    if (c == "shape") return run_shape(in, argv[3]);
+    if (c == "inertia") return run_inertia(in, argv[3]);
+    std::fprintf(stderr, "unknown case %s\n", argv[1]);
+    return 2;
+}

@@ -1,0 +1,302 @@
+"""ctypes front end of the CPU oracle (``oracle/_ref/libbib_oracle.so``).
+
+TEST INFRASTRUCTURE ONLY: imported by ``tests/``, ``__graft_entry__.smoke()`` and
+the CPU-baseline legs of ``bench.py``, never by the product package.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_ref", "libbib_oracle.so")
+
+COLLISION = {"bgk_guo_vof": 0, "bgk": 1, "trt": 2}
+WALL = {"none": 0, "fd_velocity": 1, "halfway_bb": 2}
+DIRAC = {"roma": 0, "peskin": 1}
+MODEL = {"capsule_neohookean": 0, "capsule_skalak": 1, "rbc_wlcpow": 2, "skalak_bending": 3}
+PARAM_KEYS = ["G", "C", "nu_s", "kb", "shear_modulus", "L0", "k_area_global", "k_area_local",
+              "k_volume", "vol_desired", "k_bend", "theta0"]
+
+
+class Lattice(C.Structure):
+    _fields_ = [
+        ("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64),
+        ("periodic", C.c_int32 * 3),
+        ("collision", C.c_int32),
+        ("wall_y", C.c_int32), ("wall_z", C.c_int32),
+        ("omega", C.c_double), ("omega_inner", C.c_double), ("trt_magic", C.c_double),
+        ("wall_u", (C.c_double * 3) * 4),
+        ("envelope_swap", C.c_int32),
+    ]
+
+
+def build():
+    """Compile the oracle library in place (plain C, seconds)."""
+    subprocess.run(["make", "-s", "-C", HERE], check=True)
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH) or os.path.getmtime(LIB_PATH) < os.path.getmtime(os.path.join(HERE, "bib_oracle.c")):
+            build()
+        L = C.CDLL(LIB_PATH)
+        dp, ip, i32p = C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int32)
+        Lp = C.POINTER(Lattice)
+        sig = {
+            "orc_collide_cell": (None, [Lp, dp, dp, C.c_double]),
+            "orc_collide_stream": (None, [Lp, dp, dp, dp, dp]),
+            "orc_apply_fd_walls": (None, [Lp, dp, dp]),
+            "orc_compute_velocity": (None, [Lp, dp, dp, dp]),
+            "orc_init_equilibrium": (None, [Lp, dp, dp, dp]),
+            "orc_shape_connectivity": (C.c_int64, [C.c_int64, dp, C.c_int64, ip, ip, dp, ip, dp, dp, dp, ip]),
+            "orc_particle_update": (None, [C.c_int64, dp, C.c_int64, ip, dp]),
+            "orc_inertia": (None, [dp, C.c_int64, ip, dp]),
+            "orc_membrane_forces": (None, [C.c_int32, dp, C.c_int64, dp, C.c_int64, ip, dp, C.c_double, C.c_int64, ip,
+                                           dp, C.c_int64, ip, dp, dp, C.c_double, C.c_double, dp]),
+            "orc_dirac": (C.c_double, [C.c_int32, C.c_double]),
+            "orc_classify": (None, [Lp, C.c_int32, C.c_int64, dp, i32p]),
+            "orc_interpolate": (None, [Lp, C.c_int32, C.c_double, dp, C.c_int64, dp, i32p, dp]),
+            "orc_spread": (None, [Lp, C.c_int32, C.c_double, C.c_int64, dp, dp, i32p, dp]),
+            "orc_sys_create": (C.c_void_p, [Lp, C.c_int32, C.c_double]),
+            "orc_sys_destroy": (None, [C.c_void_p]),
+            "orc_sys_f": (dp, [C.c_void_p]),
+            "orc_sys_force": (dp, [C.c_void_p]),
+            "orc_sys_phase": (dp, [C.c_void_p]),
+            "orc_sys_set_body_force": (None, [C.c_void_p, dp]),
+            "orc_sys_add_shape": (C.c_int32, [C.c_void_p, C.c_int64, dp, C.c_int64, ip]),
+            "orc_sys_add_particle": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dp, dp]),
+            "orc_sys_init": (None, [C.c_void_p]),
+            "orc_sys_step": (None, [C.c_void_p, C.c_int64]),
+            "orc_sys_lattice_only_step": (None, [C.c_void_p, C.c_int64]),
+            "orc_sys_get_particle": (None, [C.c_void_p, C.c_int32, dp, dp, dp, dp]),
+            "orc_sys_velocity": (None, [C.c_void_p, dp]),
+        }
+        for name, (res, args) in sig.items():
+            fn = getattr(L, name)
+            fn.restype = res
+            fn.argtypes = args
+        _lib = L
+    return _lib
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _i(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int64))
+
+
+def _i32(a):
+    return a.ctypes.data_as(C.POINTER(C.c_int32))
+
+
+def f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def i64(a):
+    return np.ascontiguousarray(a, dtype=np.int64)
+
+
+def lattice(dims, periodic=(1, 1, 1), collision="bgk_guo_vof", omega=1.0, omega_inner=None, trt_magic=0.25,
+            wall_y="none", wall_z="none", wall_u=None, envelope_swap=False) -> Lattice:
+    L = Lattice()
+    L.nx, L.ny, L.nz = (int(d) for d in dims)
+    for k in range(3):
+        L.periodic[k] = int(bool(periodic[k]))
+    L.collision = COLLISION[collision]
+    L.wall_y, L.wall_z = WALL[wall_y], WALL[wall_z]
+    L.omega = float(omega)
+    L.omega_inner = float(omega if omega_inner is None else omega_inner)
+    L.trt_magic = float(trt_magic)
+    L.envelope_swap = int(bool(envelope_swap))
+    wu = np.zeros((4, 3)) if wall_u is None else np.asarray(wall_u, dtype=np.float64).reshape(4, 3)
+    for a in range(4):
+        for b in range(3):
+            L.wall_u[a][b] = float(wu[a, b])
+    return L
+
+
+def params_vector(**kw) -> np.ndarray:
+    p = dict(G=0.0, C=1.0, nu_s=1.0, kb=0.0, shear_modulus=0.0, L0=1.0, k_area_global=0.0, k_area_local=0.0,
+             k_volume=0.0, vol_desired=1.0, k_bend=0.0, theta0=0.0)
+    p.update(kw)
+    return np.array([p[k] for k in PARAM_KEYS], dtype=np.float64)
+
+
+# ------------------------------------------------------------------ lattice ops
+def collide_stream(L, f, F=None, phase=None, steps=1):
+    f = f64(f).copy()
+    tmp = np.empty_like(f)
+    Fa = f64(F) if F is not None else None
+    ph = f64(phase) if phase is not None else None
+    for _ in range(steps):
+        lib().orc_collide_stream(C.byref(L), _d(f), _d(tmp), _d(Fa) if Fa is not None else None,
+                                 _d(ph) if ph is not None else None)
+    return f
+
+
+def apply_fd_walls(L, f, F):
+    f = f64(f).copy()
+    lib().orc_apply_fd_walls(C.byref(L), _d(f), _d(f64(F)))
+    return f
+
+
+def compute_velocity(L, f, F=None):
+    f = f64(f)
+    u = np.empty((3,) + f.shape[1:])
+    lib().orc_compute_velocity(C.byref(L), _d(f), _d(f64(F)) if F is not None else None, _d(u))
+    return u
+
+
+def init_equilibrium(L, rho, u):
+    u = f64(u)
+    f = np.empty((19,) + u.shape[1:])
+    lib().orc_init_equilibrium(C.byref(L), _d(f), _d(f64(rho)) if rho is not None else None, _d(u))
+    return f
+
+
+# ------------------------------------------------------------------ shapes / membranes
+class Shape:
+    def __init__(self, xyz, tri):
+        self.rest = f64(xyz)
+        self.tri = i64(tri)
+        nt = self.tri.shape[0]
+        links = np.zeros((3 * nt, 2), np.int64)
+        llen = np.zeros(3 * nt)
+        pairs = np.zeros((3 * nt, 4), np.int64)
+        pcs = np.zeros((3 * nt, 2))
+        tarea = np.zeros(nt)
+        props = np.zeros(5)
+        npairs = np.zeros(1, np.int64)
+        nl = lib().orc_shape_connectivity(self.rest.shape[0], _d(self.rest), nt, _i(self.tri), _i(links), _d(llen),
+                                          _i(pairs), _d(pcs), _d(tarea), _d(props), _i(npairs))
+        npr = int(npairs[0])
+        self.links, self.link_len = links[:nl].copy(), llen[:nl].copy()
+        self.pairs, self.pair_cs = pairs[:npr].copy(), pcs[:npr].copy()
+        self.tri_area = tarea
+        self.area, self.volume = float(props[0]), float(props[1])
+        self.center = props[2:5].copy()
+
+
+def particle_update(pos, tri):
+    pos, tri = f64(pos), i64(tri)
+    out = np.zeros(5)
+    lib().orc_particle_update(pos.shape[0], _d(pos), tri.shape[0], _i(tri), _d(out))
+    return out
+
+
+def inertia(pos, tri):
+    pos, tri = f64(pos), i64(tri)
+    out = np.zeros(9)
+    lib().orc_inertia(_d(pos), tri.shape[0], _i(tri), _d(out))
+    return out.reshape(3, 3)
+
+
+def membrane_forces(model, prm, shape: Shape, pos):
+    pos = f64(pos)
+    st = particle_update(pos, shape.tri)
+    out = np.zeros_like(pos)
+    lib().orc_membrane_forces(MODEL[model] if isinstance(model, str) else int(model), _d(f64(prm)), pos.shape[0],
+                              _d(shape.rest), shape.tri.shape[0], _i(shape.tri), _d(shape.tri_area), shape.area,
+                              shape.links.shape[0], _i(shape.links), _d(shape.link_len), shape.pairs.shape[0],
+                              _i(shape.pairs), _d(shape.pair_cs), _d(pos), st[0], st[1], _d(out))
+    return out
+
+
+# ------------------------------------------------------------------ immersed boundary
+def classify(L, dirac, pos):
+    pos = f64(pos)
+    cls = np.zeros(pos.shape[0], np.int32)
+    lib().orc_classify(C.byref(L), DIRAC[dirac], pos.shape[0], _d(pos), _i32(cls))
+    return cls
+
+
+def interpolate(L, dirac, u, pos, cls=None, offset=0.0):
+    pos = f64(pos)
+    cls = classify(L, dirac, pos) if cls is None else np.ascontiguousarray(cls, np.int32)
+    vel = np.zeros_like(pos)
+    lib().orc_interpolate(C.byref(L), DIRAC[dirac], float(offset), _d(f64(u)), pos.shape[0], _d(pos), _i32(cls),
+                          _d(vel))
+    return vel
+
+
+def spread(L, dirac, pos, force, cls=None, offset=0.0, F=None):
+    pos = f64(pos)
+    cls = classify(L, dirac, pos) if cls is None else np.ascontiguousarray(cls, np.int32)
+    F = np.zeros((3, L.nz, L.ny, L.nx)) if F is None else f64(F).copy()
+    lib().orc_spread(C.byref(L), DIRAC[dirac], float(offset), pos.shape[0], _d(pos), _d(f64(force)), _i32(cls),
+                     _d(F))
+    return F
+
+
+# ------------------------------------------------------------------ coupled system
+class System:
+    """Coupled IB-LBM system with the reference's step order (the oracle's mirror of the C ABI)."""
+
+    def __init__(self, L, dirac="roma", ib_offset=-1.0):
+        self.L = L
+        self.n = L.nx * L.ny * L.nz
+        self.h = lib().orc_sys_create(C.byref(L), DIRAC[dirac], float(ib_offset))
+        self.nv = []
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().orc_sys_destroy(self.h)
+            self.h = None
+
+    def _view(self, ptr, ncomp):
+        shape = (ncomp, self.L.nz, self.L.ny, self.L.nx) if ncomp > 1 else (self.L.nz, self.L.ny, self.L.nx)
+        return np.ctypeslib.as_array(ptr, shape=(ncomp * self.n,)).reshape(shape)
+
+    @property
+    def f(self):
+        return self._view(lib().orc_sys_f(self.h), 19)
+
+    @property
+    def force(self):
+        return self._view(lib().orc_sys_force(self.h), 3)
+
+    @property
+    def phase(self):
+        return self._view(lib().orc_sys_phase(self.h), 1)
+
+    def set_body_force(self, b):
+        lib().orc_sys_set_body_force(self.h, _d(f64(b)))
+
+    def add_shape(self, xyz, tri):
+        xyz, tri = f64(xyz), i64(tri)
+        self._shape_nv = getattr(self, "_shape_nv", []) + [xyz.shape[0]]
+        return lib().orc_sys_add_shape(self.h, xyz.shape[0], _d(xyz), tri.shape[0], _i(tri))
+
+    def add_particle(self, shape, model, prm, pos=None):
+        pid = lib().orc_sys_add_particle(self.h, shape, MODEL[model] if isinstance(model, str) else int(model),
+                                         _d(f64(prm)), _d(f64(pos)) if pos is not None else None)
+        self.nv.append(self._shape_nv[shape])
+        return pid
+
+    def step(self, n=1):
+        lib().orc_sys_step(self.h, int(n))
+
+    def lattice_step(self, n=1):
+        lib().orc_sys_lattice_only_step(self.h, int(n))
+
+    def particle(self, pid):
+        nv = self.nv[pid]
+        pos, vel, frc, st = np.zeros((nv, 3)), np.zeros((nv, 3)), np.zeros((nv, 3)), np.zeros(5)
+        lib().orc_sys_get_particle(self.h, pid, _d(pos), _d(vel), _d(frc), _d(st))
+        return dict(pos=pos, vel=vel, force=frc, area=st[0], volume=st[1], com=st[2:5])
+
+    def velocity(self):
+        u = np.zeros((3, self.L.nz, self.L.ny, self.L.nx))
+        lib().orc_sys_velocity(self.h, _d(u))
+        return u

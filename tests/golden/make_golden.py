@@ -1,0 +1,270 @@
+"""Generate the golden fixtures in this folder by running the REFERENCE's own code.
+
+The reference (niclasberg/biblbm: Palabos + src/fsi, FP64 C++) is compiled from
+its sources by ``make -C oracle ref`` into ``oracle/_ref/ref_harness``; this
+script writes seeded inputs, runs the harness and stores inputs and outputs as
+small ``.npz`` files.  The fixtures pin both the CPU oracle restatement and the
+CUDA path.  Run from the repository root:
+
+    make -C oracle ref REF=<path to the reference checkout>
+    python tests/golden/make_golden.py
+
+Only this script needs the reference; the tests read the committed ``.npz``.
+"""
+from __future__ import annotations
+
+import os
+import struct
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+from biblbm_gb300 import meshes  # noqa: E402
+
+HARNESS = os.path.join(ROOT, "oracle", "_ref", "ref_harness")
+
+# D3Q19 velocity set in the reference's order (src/latticeBoltzmann/nearestNeighborLattices3D.hh:165-197)
+C = np.array(
+    [[0, 0, 0], [-1, 0, 0], [0, -1, 0], [0, 0, -1], [-1, -1, 0], [-1, 1, 0], [-1, 0, -1], [-1, 0, 1],
+     [0, -1, -1], [0, -1, 1], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, -1, 0], [1, 0, 1],
+     [1, 0, -1], [0, 1, 1], [0, 1, -1]], dtype=np.int64)
+W = np.array([1 / 3] + [1 / 18] * 3 + [1 / 36] * 6 + [1 / 18] * 3 + [1 / 36] * 6)
+
+
+# ---------------------------------------------------------------- record files
+def write_rec(path, arrays: dict):
+    with open(path, "wb") as f:
+        for name, a in arrays.items():
+            a = np.asarray(a)
+            if a.dtype.kind in "iub":
+                a, dt = a.astype("<i8"), b"i"
+            else:
+                a, dt = a.astype("<f8"), b"d"
+            f.write(name.encode().ljust(32, b"\0"))
+            f.write(dt)
+            f.write(struct.pack("<i", a.ndim))
+            f.write(struct.pack("<%dq" % a.ndim, *a.shape))
+            f.write(np.ascontiguousarray(a).tobytes())
+
+
+def read_rec(path) -> dict:
+    out = {}
+    with open(path, "rb") as f:
+        while True:
+            name = f.read(32)
+            if len(name) < 32:
+                break
+            dt = f.read(1)
+            (nd,) = struct.unpack("<i", f.read(4))
+            shape = struct.unpack("<%dq" % nd, f.read(8 * nd))
+            n = int(np.prod(shape)) if nd else 1
+            a = np.frombuffer(f.read(8 * n), dtype="<f8" if dt == b"d" else "<i8").reshape(shape)
+            out[name.rstrip(b"\0").decode()] = a.copy()
+    return out
+
+
+def run(case, inputs):
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.rec"), os.path.join(d, "out.rec")
+        write_rec(fin, inputs)
+        subprocess.run([HARNESS, case, fin, fout], check=True, cwd=d,
+                       stdout=subprocess.DEVNULL)
+        out = read_rec(fout)
+        if os.path.exists(fout + ".step0"):
+            out.update(read_rec(fout + ".step0"))
+        return out
+
+
+def save(name, inputs, outputs, **extra):
+    path = os.path.join(HERE, name + ".npz")
+    payload = {"in_" + k: np.asarray(v) for k, v in inputs.items()}
+    payload.update({"out_" + k: np.asarray(v) for k, v in outputs.items()})
+    payload.update({k: np.asarray(v) for k, v in extra.items()})
+    np.savez_compressed(path, **payload)
+    print("wrote", os.path.relpath(path, ROOT), "%.1f KB" % (os.path.getsize(path) / 1024))
+
+
+# ---------------------------------------------------------------- helpers
+def equilibrium(rho, u):
+    """Palabos D3Q19 equilibrium in f-bar form (dynamicsTemplates3D.h:675-678)."""
+    rhobar = rho - 1.0
+    j = rho[None] * u
+    jsq = (j * j).sum(0)
+    inv = 1.0 / rho
+    f = np.empty((19,) + rho.shape)
+    for i in range(19):
+        cj = C[i, 0] * j[0] + C[i, 1] * j[1] + C[i, 2] * j[2]
+        f[i] = W[i] * (rhobar + 3.0 * cj + inv * (4.5 * cj * cj - 1.5 * jsq))
+    return f
+
+
+def random_state(rng, nx, ny, nz, amp_u=0.03, amp_rho=0.01, noise=2e-4):
+    shape = (nz, ny, nx)
+    rho = 1.0 + amp_rho * rng.uniform(-1, 1, shape)
+    u = amp_u * rng.uniform(-1, 1, (3,) + shape)
+    return equilibrium(rho, u) + noise * rng.uniform(-1, 1, (19,) + shape)
+
+
+def particle_params(model, **kw):
+    p = dict(G=0.0, C=1.0, nu_s=1.0, kb=0.0, shear_modulus=0.0, L0=1.0, k_area_global=0.0,
+             k_area_local=0.0, k_volume=0.0, vol_desired=1.0, k_bend=0.0, theta0=0.0)
+    p.update(kw)
+    keys = ["G", "C", "nu_s", "kb", "shear_modulus", "L0", "k_area_global", "k_area_local",
+            "k_volume", "vol_desired", "k_bend", "theta0"]
+    return np.array([p[k] for k in keys], dtype=np.float64)
+
+
+# ---------------------------------------------------------------- cases
+def case_lbm_periodic():
+    rng = np.random.default_rng(101)
+    nx, ny, nz = 9, 7, 6
+    tau, lam = 0.8, 5.0
+    omega = 1 / tau
+    omega_in = 1 / (0.5 + lam * (tau - 0.5))
+    inp = dict(dims=[nx, ny, nz], omega=[omega, omega_in], walls=0, steps=3,
+               fbar=random_state(rng, nx, ny, nz),
+               force=1e-3 * rng.uniform(-1, 1, (3, nz, ny, nx)),
+               phase=(rng.random((nz, ny, nx)) < 0.4).astype(np.float64))
+    out = run("lbm", inp)
+    save("lbm_periodic", inp, out)
+
+
+def case_lbm_shear():
+    rng = np.random.default_rng(102)
+    nx, ny, nz = 8, 9, 7
+    omega = 1 / 0.9
+    force = 2e-4 * rng.uniform(-1, 1, (3, nz, ny, nx))
+    inp = dict(dims=[nx, ny, nz], omega=[omega, omega], walls=1, U=0.01, steps=4,
+               force=force, phase=np.zeros((nz, ny, nx)))
+    out = run("lbm", inp)
+    save("lbm_shear", inp, out)
+
+
+def case_interp():
+    for dirac, dname in ((0, "roma"), (1, "peskin")):
+        for per, pname in (((1, 1, 1), "ppp"), ((1, 0, 1), "pwp"), ((1, 0, 0), "pww")):
+            rng = np.random.default_rng(200 + 10 * dirac + len(pname) + sum(per))
+            nx, ny, nz = 10, 9, 8
+            u = 0.05 * rng.uniform(-1, 1, (3, nz, ny, nx))
+            npts = 48
+            pos = rng.uniform(0, 1, (npts, 3)) * np.array([nx, ny, nz]) - 0.5
+            # a few nodes hugging the periodic seams and the non-periodic faces
+            pos[:6, 0] = [-0.45, 0.1, 0.7, nx - 1.3, nx - 0.7, nx - 0.55]
+            pos[6:12, 1] = [-0.3, 0.2, 0.9, ny - 1.9, ny - 1.2, ny - 0.6]
+            pos[12:18, 2] = [-0.2, 0.4, 1.2, nz - 1.6, nz - 1.1, nz - 0.7]
+            nforce = rng.uniform(-1, 1, (npts, 3))
+            inp = dict(dims=[nx, ny, nz], periodic=list(per), dirac=dirac, u=u, pos=pos, nforce=nforce)
+            out = run("interp", inp)
+            save("interp_%s_%s" % (dname, pname), inp, out)
+
+
+def mesh_sets():
+    ico_xyz, ico_tri = meshes.icosphere(2, 4.0)
+    ef_xyz, ef_tri = meshes.evans_fung(2, 5.0)
+    return {"ico2": (ico_xyz, ico_tri), "ef2": (ef_xyz, ef_tri)}
+
+
+def case_shape():
+    for name, (xyz, tri) in mesh_sets().items():
+        inp = dict(rest=xyz, tri=tri)
+        out = run("shape", inp)
+        save("shape_" + name, inp, out)
+
+
+def deform(rng, xyz, amp):
+    """A smooth stretch plus small noise: a prestressed, non-degenerate state."""
+    s = np.diag([1.0 + 2 * amp, 1.0 - amp, 1.0 - 0.5 * amp])
+    c = xyz.mean(0)
+    return (xyz - c) @ s.T + c + 0.02 * amp * rng.uniform(-1, 1, xyz.shape) + np.array([3.1, -2.2, 7.4])
+
+
+def case_forces():
+    sets = mesh_sets()
+    rng = np.random.default_rng(303)
+    xyz, tri = sets["ico2"]
+    ef, eft = sets["ef2"]
+    A_ef = None
+    cases = []
+    cases.append(("capsule_neohookean", xyz, tri, 0, particle_params(0, G=0.01, C=1.0)))
+    cases.append(("capsule_skalak", xyz, tri, 1, particle_params(1, G=0.02, C=1.0)))
+    shape_out = run("shape", dict(rest=ef, tri=eft))
+    A_ef, V_ef = float(shape_out["area"][0]), float(shape_out["volume"][0])
+    lmean = float(shape_out["link_length"].mean())
+    cases.append(("rbc_wlcpow", ef, eft, 2, particle_params(2, shear_modulus=0.01, L0=lmean, k_area_global=0.5,
+                                                             k_area_local=0.2, k_volume=0.7, vol_desired=V_ef,
+                                                             k_bend=0.05)))
+    cases.append(("skalak_bending", ef, eft, 3, particle_params(3, G=0.01, C=1.0, k_area_global=1.0, k_volume=1.0,
+                                                                 vol_desired=V_ef, k_bend=0.01 * 0.01 * A_ef)))
+    for name, rest, t, model, prm in cases:
+        pos = deform(rng, rest, 0.06)
+        inp = dict(rest=rest, tri=t, pos=pos, model=model, params=prm)
+        out = run("forces", inp)
+        save("forces_" + name, inp, out)
+
+
+def case_inertia():
+    rng = np.random.default_rng(404)
+    xyz, tri = meshes.evans_fung(2, 6.0)
+    pos = meshes.place(xyz, meshes.random_rotation(rng), (10.3, 12.1, 9.7))
+    inp = dict(rest=xyz, tri=tri, pos=pos)
+    out = run("inertia", inp)
+    save("inertia_ef2", inp, out)
+
+
+def case_ibm_capsule_shear():
+    n = 20
+    xyz, tri = meshes.icosphere(2, 4.0)
+    tau = 1.0
+    nu = (tau - 0.5) / 3
+    U = 0.04
+    gamma = 2 * U / (n - 1)
+    G = nu * gamma * 4.0 / 0.2
+    pos = meshes.place(xyz, None, (0.5 * (n - 1) + 0.13, 0.5 * (n - 1) - 0.21, 0.5 * (n - 1) + 0.07))
+    inp = dict(dims=[n, n, n], tau=tau, walls=1, U=U, steps=6, rest=xyz, tri=tri, pos=pos, model=1,
+               params=particle_params(1, G=G, C=1.0))
+    out = run("ibm", inp)
+    keep = {k: out[k] for k in ("pos", "vel", "force", "volume", "area", "com", "inertia")}
+    keep["u_end"] = out["u_end"]
+    keep["fbar_end_planes"] = out["fbar_end"][:, :, [0, 1, n // 2, n - 2, n - 1], :]
+    keep["fbar_end_sum"] = out["fbar_end"].sum(axis=(1, 2, 3))
+    keep["force_spread"] = out["force_spread"]
+    save("ibm_capsule_shear", inp, keep)
+
+
+def case_ibm_rbc_periodic():
+    n = 16
+    xyz, tri = meshes.evans_fung(2, 4.5)
+    shape_out = run("shape", dict(rest=xyz, tri=tri))
+    A0, V0 = float(shape_out["area"][0]), float(shape_out["volume"][0])
+    rng = np.random.default_rng(505)
+    pos = meshes.place(deform(rng, xyz, 0.05), meshes.random_rotation(rng), (n - 1.2, 6.3, 0.4))
+    G = 0.004
+    inp = dict(dims=[n, n, n], tau=1.0, walls=0, steps=5, rest=xyz, tri=tri, pos=pos, model=3,
+               params=particle_params(3, G=G, C=1.0, k_area_global=1.0, k_volume=1.0, vol_desired=V0,
+                                      k_bend=0.01 * G * A0),
+               body=[2e-5, 0.0, 0.0])
+    out = run("ibm", inp)
+    keep = {k: out[k] for k in ("pos", "vel", "force", "volume", "area", "com", "inertia")}
+    keep["u_end"] = out["u_end"]
+    keep["fbar_end_sum"] = out["fbar_end"].sum(axis=(1, 2, 3))
+    keep["fbar_end_planes"] = out["fbar_end"][:, :, [0, 5, 10], :]
+    keep["force_spread"] = out["force_spread"]
+    save("ibm_rbc_periodic", inp, keep)
+
+
+CASES = [case_lbm_periodic, case_lbm_shear, case_interp, case_shape, case_forces, case_inertia,
+         case_ibm_capsule_shear, case_ibm_rbc_periodic]
+
+if __name__ == "__main__":
+    if not os.path.exists(HARNESS):
+        sys.exit("build the reference harness first: make -C oracle ref REF=<reference checkout>")
+    sel = sys.argv[1:]
+    for fn in CASES:
+        if not sel or fn.__name__.replace("case_", "") in sel:
+            fn()
