@@ -1,0 +1,389 @@
+"""Benchmark of the coupled IB-LBM step on GB300.
+
+Workload (default): the dense red-cell suspension in a channel -- lattice 512x128x128,
+periodic x, halfway bounce-back walls on y and z, body force 1e-6, 400 Evans-Fung cells of
+642 vertices (20 % haematocrit) at seeded random non-overlapping positions and
+orientations, Skalak + dihedral bending + global area / volume penalties, D3Q19 BGK with
+Guo forcing, tau = 1.  Populations are stored as FP16 deviations f - t_i (fixed scale),
+collision runs in FP32; vertex positions and the area / volume reductions stay FP64.
+
+One step = velocity interpolation to all vertices, membrane forces, vertex motion,
+spreading, fused collide-and-stream (the reference's step order).  Populations are
+638 MB, larger than the 129 MB L2, so no flush is needed between steps.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--storage f16|f32|f64]
+    python bench.py --impl reference ...   (the CPU port of the reference's step)
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "MLUPS (coupled IB-LBM step) + membrane vertex-updates/s, FP16/FP32 storage vs FP64, 1 GB300"
+BYTES_PER_LU = {"f64": 19 * 8 * 2 + 3 * 8, "f32": 19 * 4 * 2 + 3 * 4, "f16": 19 * 2 * 2 + 3 * 4}
+
+
+def env_rank():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled every 200 ms while running."""
+
+    FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
+              "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
+              "clocks_event_reasons.sw_thermal_slowdown", "clocks_event_reasons.sw_power_cap"]
+
+    def __init__(self, device):
+        self.device, self.proc, self.lines = device, None, []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + ",".join(self.FIELDS),
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=subprocess.PIPE,
+                                         stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            p = [x.strip() for x in ln.split(",")]
+            if len(p) < 9:
+                continue
+            try:
+                sm.append(float(p[1]))
+                mx.append(float(p[2]))
+            except ValueError:
+                continue
+            for k, nm in enumerate(names):
+                if p[5 + k].lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def build_instance(bib, ctx, wl, storage):
+    nx, ny, nz = wl["dims"]
+    lat = ctx.add_domain(nx, ny, nz, storage=storage, **wl["lattice"])
+    if wl.get("initial_velocity") is not None:
+        lat.initialize_at_equilibrium(None, wl["initial_velocity"])
+    shapes = bib.ParticleShapeLibrary(ctx)
+    sid = shapes.store_mesh(wl["rest"], wl["tri"], "cell")
+    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes)
+    for pos in wl["positions"]:
+        fsi.add_particle(sid, wl["model"], wl["params"], pos)
+    return lat, fsi
+
+
+def taylor_and_volume(bib, fsi, wl):
+    pos, stats = fsi.download()
+    nv = wl["rest"].shape[0]
+    V0 = float(wl.get("V0") or stats[0, 1])
+    return pos.reshape(-1, nv, 3), stats, V0
+
+
+def cpu_sample(wl, steps):
+    """The oracle (CPU port of the reference's step) on the same instance, all host threads."""
+    from oracle import oracle as O
+
+    nx, ny, nz = wl["dims"]
+    lp = wl["lattice"]
+    L = O.lattice((nx, ny, nz), lp["periodic"], lp["collision"], lp["omega"], lp["omega"],
+                  wall_y=lp.get("wall_y", "none"), wall_z=lp.get("wall_z", "none"), wall_u=lp.get("wall_u"))
+    S = O.System(L, "roma", -1.0)
+    if wl.get("initial_velocity") is not None:
+        S.f[...] = O.init_equilibrium(L, None, wl["initial_velocity"])
+    S.set_body_force(np.asarray(lp.get("body_force", (0, 0, 0)), dtype=np.float64))
+    sid = S.add_shape(wl["rest"], wl["tri"])
+    for pos in wl["positions"]:
+        S.add_particle(sid, wl["model"], wl["params"], pos)
+    S.step(1)  # warm-up
+    t0 = time.perf_counter()
+    S.step(steps)
+    dt = time.perf_counter() - t0
+    cells = nx * ny * nz
+    nvt = wl["positions"].shape[0] * wl["positions"].shape[1]
+    return dict(mlups=cells * steps / dt / 1e6, vups=nvt * steps / dt, seconds=dt, steps=steps, threads=O.threads())
+
+
+def run_reference(args, wl):
+    rank, world, _ = env_rank()
+    if rank != 0:
+        return
+    t0 = time.perf_counter()
+    for _ in range(args.warmup):
+        pass
+    r = cpu_sample(wl, max(1, args.steps))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": r["mlups"], "unit": "MLUPS", "n_gpus": args.gpus,
+        "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": wl["name"], "cells": int(np.prod(wl["dims"])), "vertices": int(wl["positions"].size // 3)},
+        "vertex_updates_per_s": r["vups"],
+        "cpu_baseline": {"value": r["mlups"], "unit": "MLUPS", "cores": r["threads"], "kind": "port",
+                         "sample": "%d coupled steps of the full workload after 1 warm-up step" % r["steps"]},
+        "e2e": {"value": r["mlups"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "wall_s": time.perf_counter() - t0,
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=50)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="native", choices=["native", "reference"])
+    ap.add_argument("--storage", default="f16", choices=["f16", "f32", "f64"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "capsule"])
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-variants", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+
+    from biblbm_gb300 import workloads
+
+    wl = workloads.channel_suspension() if args.workload == "channel" else workloads.capsule_shear()
+    if args.impl == "reference":
+        run_reference(args, wl)
+        return
+
+    rank, world, local = env_rank()
+    dist = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    import biblbm_gb300 as bib
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    def max_over_ranks(v):
+        if dist is None:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    nx, ny, nz = wl["dims"]
+    cells = nx * ny * nz
+    nvt = int(wl["positions"].shape[0] * wl["positions"].shape[1])
+    K, W = args.steps, args.warmup
+
+    # ---------------- timed region: K coupled steps, graph replays, device events
+    ctx = bib.Context(0 if world == 1 else local)
+    lat, fsi = build_instance(bib, ctx, wl, args.storage)
+    fsi.step(W)
+    ctx.sync()
+    barrier()
+    with ClockSampler(local) as clk:
+        ms = fsi.step_timed(K)
+    barrier()
+    ms = max_over_ranks(ms)
+    mlups = cells * K * world / (ms * 1e-3) / 1e6
+    vups = nvt * K * world / (ms * 1e-3)
+    lat.check_health()
+
+    # ---------------- per-kernel device time over K more steps (events between kernels)
+    ctx.set_profiling(True)
+    fsi.step(K)
+    prof = ctx.profile()
+    ctx.set_profiling(False)
+    coll_ms = prof["collide_stream"] / K
+    bytes_lu = BYTES_PER_LU[args.storage]
+    achieved = bytes_lu * cells / (coll_ms * 1e-3) / 1e9
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except OSError:
+        pass
+    peak = float(peaks.get("hbm_gbs", 6800.0))
+    traffic = None
+    try:
+        tr = json.load(open(os.path.join(ROOT, "profiles", "collide_stream_traffic.json")))
+        if args.storage in tr.get("bytes_per_cell", {}):
+            traffic = tr["bytes_per_cell"][args.storage] * cells
+    except (OSError, ValueError):
+        pass
+
+    pos_main, stats_main, V0 = taylor_and_volume(bib, fsi, wl)
+    u_main = lat.compute_velocity() if args.storage != "f64" else None
+    steps_main = W + 2 * K
+    ctx.close()
+    del lat, fsi
+
+    # ---------------- same-GPU variants and their error against the FP64 path
+    variants = {}
+    if not args.no_variants:
+        for st in ["f64", "f32", "f16"]:
+            c2 = bib.Context(0 if world == 1 else local)
+            l2, f2 = build_instance(bib, c2, wl, st)
+            f2.step(W)
+            c2.sync()
+            kk = max(3, K // 2) if st == "f64" else K
+            t = f2.step_timed(kk)
+            f2.step(steps_main - W - kk)  # same number of steps as the main run
+            variants[st] = {"mlups": cells * kk / (t * 1e-3) / 1e6, "vertex_updates_per_s": nvt * kk / (t * 1e-3),
+                            "ms_per_step": t / kk}
+            pos_v, stats_v, _ = taylor_and_volume(bib, f2, wl)
+            variants[st]["_u"] = l2.compute_velocity()
+            variants[st]["_stats"] = stats_v
+            c2.close()
+        ref_u, ref_stats = variants["f64"]["_u"], variants["f64"]["_stats"]
+        for st in ["f32", "f16"]:
+            u = variants[st]["_u"]
+            variants[st]["velocity_rel_l2_vs_f64"] = float(np.linalg.norm(u - ref_u) / np.linalg.norm(ref_u))
+            variants[st]["volume_rel_diff_vs_f64_max"] = float(
+                np.abs(variants[st]["_stats"][:, 1] - ref_stats[:, 1]).max() / V0)
+        for st in variants:
+            variants[st]["volume_drift_max"] = float(np.abs(variants[st]["_stats"][:, 1] - V0).max() / V0)
+            variants[st].pop("_u")
+            variants[st].pop("_stats")
+        variants["f64"]["speedup_f16_over_f64"] = variants["f16"]["mlups"] / variants["f64"]["mlups"]
+
+    # ---------------- end to end through the C ABI with host buffers
+    e2e = None
+    if not args.no_e2e:
+        try:
+            import torch
+
+            def pinned(shape):
+                return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        except Exception:  # torch without CUDA pinning: pageable buffers
+            def pinned(shape):
+                return np.empty(shape, dtype=np.float64)
+        f_host = pinned((19, nz, ny, nx))
+        f_host[...] = 0.0
+        if wl.get("initial_velocity") is not None:
+            from oracle import oracle as O  # equilibrium of the initial profile, host side
+
+            lp = wl["lattice"]
+            f_host[...] = O.init_equilibrium(O.lattice(wl["dims"], lp["periodic"]), None, wl["initial_velocity"])
+        pos_host = pinned(wl["positions"].shape)
+        pos_host[...] = wl["positions"]
+        pos_out = pinned((nvt, 3))
+        stats_out = pinned((wl["positions"].shape[0], 5))
+        f_out = pinned((19, nz, ny, nx))
+        c3 = bib.Context(0 if world == 1 else local)
+        nxx = wl["dims"]
+        l3 = c3.add_domain(*nxx, storage=args.storage, **wl["lattice"])
+        shapes = bib.ParticleShapeLibrary(c3)
+        sid = shapes.store_mesh(wl["rest"], wl["tri"], "cell")
+        f3 = bib.ImmersedBoundaryDynamics3D(l3, shapes)
+        # warm the path once (graphs, kernel modules) on a throwaway step
+        l3.send(f_host)
+        for p in pos_host:
+            f3.add_particle(sid, wl["model"], wl["params"], p)
+        f3.step(W)
+        c3.sync()
+        import ctypes as C
+
+        lib, h = c3.lib, c3.h
+        barrier()
+        t0 = time.perf_counter()
+        c3.check(lib.bib_lattice_send(h, l3.h, f_host.ctypes.data, f_host.nbytes, 0))
+        for i, p in enumerate(pos_host):
+            c3.check(lib.bib_particle_set_positions(h, l3.h, i, p.ctypes.data_as(C.POINTER(C.c_double))))
+        for _ in range(K):
+            c3.check(lib.bib_step(h, l3.h, 1))
+            c3.check(lib.bib_particles_download(h, l3.h, pos_out.ctypes.data_as(C.POINTER(C.c_double)),
+                                                stats_out.ctypes.data_as(C.POINTER(C.c_double))))
+        c3.check(lib.bib_lattice_receive(h, l3.h, f_out.ctypes.data, f_out.nbytes, 0))
+        dt = time.perf_counter() - t0
+        barrier()
+        dt = max_over_ranks(dt)
+        h2d = f_host.nbytes + pos_host.nbytes
+        d2h = K * (pos_out.nbytes + stats_out.nbytes) + f_out.nbytes
+        e2e = {"value": cells * K * world / dt / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": int(h2d // K),
+               "d2h_bytes_per_step": int(d2h // K),
+               "what": "bib_lattice_send of the FP64 initial populations + vertex positions, K x (bib_step + "
+                       "bib_particles_download of all vertices and per-cell area/volume/centre), final "
+                       "bib_lattice_receive; pinned host buffers"}
+        c3.close()
+
+    # ---------------- CPU baseline (the oracle port) on a bounded sample
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        r = cpu_sample(wl, args.cpu_steps)
+        cpu = {"value": r["mlups"], "unit": "MLUPS", "cores": r["threads"], "kind": "port",
+               "sample": "%d coupled steps of the full workload (after 1 warm-up), %.1f s" % (r["steps"], r["seconds"]),
+               "vertex_updates_per_s": r["vups"]}
+
+    if rank != 0:
+        return
+    kernel = {"f64": "k_collide_stream<double>", "f32": "k_collide_stream<float>", "f16": "k_collide_stream<__half>"}
+    line = {
+        "metric": METRIC,
+        "value": mlups,
+        "unit": "MLUPS",
+        "n_gpus": world,
+        "steps": K,
+        "warmup": W,
+        "ms_per_step": ms / K,
+        "higher_is_better": True,
+        "scaling": "weak",
+        "vs_baseline": None,
+        "dtype": "f32" if args.storage != "f64" else "f64",
+        "data": "synthetic (seeded: RBC positions/orientations seed %d)" % wl["seed"],
+        "config": {"workload": wl["name"], "cells": cells, "vertices": nvt, "storage": args.storage,
+                   "collision": "BGK + Guo forcing", "walls": "halfway bounce-back y,z" if args.workload == "channel"
+                   else "finite-difference velocity walls y", "dirac": "Roma 3-point",
+                   "l2": "populations %.0f MB > 129 MB L2, no flush" % (cells * 19 * 2 * {"f16": 2, "f32": 4, "f64": 8}[args.storage] / 1e6),
+                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "vertex_updates_per_s": vups,
+        "kernel_ms_per_step": {k: v / K for k, v in prof.items()},
+        "gpu_launches": int(K * ((3 if nvt else 0) + 1 + (1 if any(wl["lattice"].get("body_force", (0, 0, 0))) else 0)
+                                 + (1 if wl["lattice"].get("wall_y") == "fd_velocity" else 0))),
+        "roofline": {"bound": "hbm", "kernel": kernel[args.storage], "achieved": achieved, "peak": peak, "unit": "GB/s",
+                     "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_cell": bytes_lu,
+                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
+        "clocks": clk.summary(),
+        "variants": variants,
+        "e2e": e2e,
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

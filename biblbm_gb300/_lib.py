@@ -1,0 +1,117 @@
+"""ctypes binding of ``lib/libbib_gb300.so`` (the C ABI in ``include/bib/bib.h``).
+
+There is no CPU fallback: if the CUDA library is missing or cannot be loaded every
+entry point raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libbib_gb300.so")
+
+P_COUNT = 12
+
+
+class LatticeParams(C.Structure):
+    _fields_ = [
+        ("periodic", C.c_int32 * 3),
+        ("collision", C.c_int32),
+        ("storage", C.c_int32),
+        ("wall_y", C.c_int32),
+        ("wall_z", C.c_int32),
+        ("use_phase", C.c_int32),
+        ("reserved", C.c_int32),
+        ("omega", C.c_double),
+        ("omega_inner", C.c_double),
+        ("trt_magic", C.c_double),
+        ("wall_u", (C.c_double * 3) * 4),
+        ("body_force", C.c_double * 3),
+        ("f16_scale", C.c_double),
+    ]
+
+
+class IbParams(C.Structure):
+    _fields_ = [("dirac", C.c_int32), ("spread_mode", C.c_int32), ("field_offset", C.c_double)]
+
+
+class Config(C.Structure):
+    _fields_ = [("device", C.c_int32), ("flags", C.c_int32)]
+
+
+# name -> (restype, argtypes)
+_dp, _ip, _i32p, _vp = C.POINTER(C.c_double), C.POINTER(C.c_int64), C.POINTER(C.c_int32), C.c_void_p
+SIGNATURES = {
+    "bib_abi_version": (C.c_int32, []),
+    "bib_status_string": (C.c_char_p, [C.c_int32]),
+    "bib_create": (C.c_int32, [C.POINTER(Config), C.POINTER(C.c_void_p)]),
+    "bib_destroy": (None, [_vp]),
+    "bib_sync": (C.c_int32, [_vp]),
+    "bib_last_error": (C.c_size_t, [_vp, C.c_char_p, C.c_size_t]),
+    "bib_set_graph_mode": (C.c_int32, [_vp, C.c_int32]),
+    "bib_set_profiling": (C.c_int32, [_vp, C.c_int32]),
+    "bib_profile_read": (C.c_int32, [_vp, _dp, C.c_int32]),
+    "bib_lattice_add_domain": (C.c_int32, [_vp, C.c_int64, C.c_int64, C.c_int64, C.POINTER(LatticeParams), _i32p]),
+    "bib_lattice_cells": (C.c_int32, [_vp, C.c_int32, _ip]),
+    "bib_lattice_send": (C.c_int32, [_vp, C.c_int32, _vp, C.c_size_t, C.c_int32]),
+    "bib_lattice_receive": (C.c_int32, [_vp, C.c_int32, _vp, C.c_size_t, C.c_int32]),
+    "bib_lattice_collide_and_stream": (C.c_int32, [_vp, C.c_int32, C.c_int64]),
+    "bib_lattice_init_equilibrium": (C.c_int32, [_vp, C.c_int32, _dp, _dp]),
+    "bib_lattice_set_force": (C.c_int32, [_vp, C.c_int32, _dp]),
+    "bib_lattice_get_force": (C.c_int32, [_vp, C.c_int32, _dp]),
+    "bib_lattice_set_phase": (C.c_int32, [_vp, C.c_int32, _dp]),
+    "bib_lattice_get_velocity": (C.c_int32, [_vp, C.c_int32, _dp]),
+    "bib_shape_store": (C.c_int32, [_vp, _dp, _ip, C.c_int64, C.c_int64, _i32p]),
+    "bib_shape_info": (C.c_int32, [_vp, C.c_int32, _dp]),
+    "bib_ib_configure": (C.c_int32, [_vp, C.c_int32, C.POINTER(IbParams)]),
+    "bib_particle_add": (C.c_int32, [_vp, C.c_int32, C.c_int32, C.c_int32, _dp, _dp, _i32p]),
+    "bib_particle_count": (C.c_int32, [_vp, C.c_int32, _i32p]),
+    "bib_particle_get": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp, _dp, _dp]),
+    "bib_particle_set_positions": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp]),
+    "bib_particle_stats": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp]),
+    "bib_particles_download": (C.c_int32, [_vp, C.c_int32, _dp, _dp]),
+    "bib_total_vertices": (C.c_int32, [_vp, C.c_int32, _ip]),
+    "bib_total_volume": (C.c_int32, [_vp, C.c_int32, _dp]),
+    "bib_ibm_step": (C.c_int32, [_vp, C.c_int32]),
+    "bib_step": (C.c_int32, [_vp, C.c_int32, C.c_int64]),
+    "bib_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),
+    "bib_check_health": (C.c_int32, [_vp, C.c_int32]),
+}
+
+_lib = None
+
+
+class BibError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__("%s (%d): %s" % (status_string(status), status, message))
+        self.status = status
+
+
+def load(path: str = LIB_PATH):
+    """Load the CUDA library; raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(
+            "biblbm_gb300 CUDA library not found at %s; build it with "
+            "`python -c 'import __graft_entry__ as g; g.build()'` or `python biblbm_gb300/build.py`" % path)
+    lib = C.CDLL(path)
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name)
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def status_string(s: int) -> str:
+    try:
+        return load().bib_status_string(s).decode()
+    except Exception:  # pragma: no cover - used while formatting another error
+        return "status"
+
+
+def exported_symbols():
+    return list(SIGNATURES)

@@ -1,0 +1,305 @@
+"""Python mirror of the reference's interface for the coupled IB-LBM step.
+
+Names follow the reference: a ``Lattice`` plays Palabos' ``MultiBlockLattice3D`` with
+its ``CoProcessor3D`` offload (``addDomain / send / receive / collideAndStream``,
+src/coProcessors/coProcessor3D.h:57-115); ``ParticleShapeLibrary.store_mesh`` is
+src/fsi/ParticleShapeFactory.h:26; ``ImmersedBoundaryDynamics3D`` exposes
+``add_particle / init / get_particle / compute_total_volume`` and the coupled step of
+progs/capsule_in_shear/capsule_in_shear.cpp:187-227.  Every call goes through the C
+ABI of ``include/bib/bib.h`` into the CUDA library; errors raise ``BibError``.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass, field
+
+import numpy as np
+
+from . import _lib
+from ._lib import BibError, IbParams, LatticeParams
+
+STORAGE = {"f64": 0, "f32": 1, "f16": 2}
+COLLISION = {"bgk_guo_vof": 0, "bgk": 1, "trt": 2}
+WALL = {"none": 0, "fd_velocity": 1, "halfway_bb": 2}
+DIRAC = {"roma": 0, "peskin": 1}
+MODEL = {"capsule_neohookean": 0, "capsule_skalak": 1, "rbc_wlcpow": 2, "skalak_bending": 3}
+LAYOUT = {"soa": 0, "palabos": 1}
+PARAM_KEYS = ["G", "C", "nu_s", "kb", "shear_modulus", "L0", "k_area_global", "k_area_local",
+              "k_volume", "vol_desired", "k_bend", "theta0"]
+Q = 19
+
+
+def _d(a):
+    return a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+@dataclass
+class CapsuleParameters:
+    """CapsuleParameters of src/fsi/DeformableCapsule.h:22-31."""
+    G: float = 0.0
+    C: float = 1.0
+    nu_s: float = 1.0
+    kb: float = 0.0
+
+
+@dataclass
+class RBCParameters:
+    """RBCParameters of src/fsi/RBCParticle.h:21-58 (the fields used by compute_forces)."""
+    shear_modulus: float = 0.0
+    L0: float = 1.0
+    k_area_global: float = 0.0
+    k_area_local: float = 0.0
+    k_volume: float = 0.0
+    vol_desired: float = 1.0
+    k_bend: float = 0.0
+    theta0: float = 0.0
+
+
+def membrane_params(capsule: CapsuleParameters | None = None, rbc: RBCParameters | None = None, **kw) -> np.ndarray:
+    """The 12-double parameter vector of the C ABI (BIB_P_*)."""
+    v = dict(zip(PARAM_KEYS, [0.0, 1.0, 1.0, 0.0, 0.0, 1.0, 0.0, 0.0, 0.0, 1.0, 0.0, 0.0]))
+    if capsule is not None:
+        v.update(G=capsule.G, C=capsule.C, nu_s=capsule.nu_s, kb=capsule.kb)
+    if rbc is not None:
+        v.update(shear_modulus=rbc.shear_modulus, L0=rbc.L0, k_area_global=rbc.k_area_global,
+                 k_area_local=rbc.k_area_local, k_volume=rbc.k_volume, vol_desired=rbc.vol_desired,
+                 k_bend=rbc.k_bend, theta0=rbc.theta0)
+    v.update(kw)
+    return np.array([v[k] for k in PARAM_KEYS], dtype=np.float64)
+
+
+class Context:
+    """A CUDA context, stream and the device objects of one user (bib_create)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = _lib.load()
+        cfg = _lib.Config(device, 0)
+        h = C.c_void_p()
+        st = self.lib.bib_create(C.byref(cfg), C.byref(h))
+        if st != 0:
+            raise BibError(st, "bib_create failed (is a CUDA GPU visible?)")
+        self.h = h
+
+    def check(self, st):
+        if st != 0:
+            buf = C.create_string_buffer(1024)
+            self.lib.bib_last_error(self.h, buf, 1024)
+            raise BibError(st, buf.value.decode())
+        return st
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bib_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def sync(self):
+        self.check(self.lib.bib_sync(self.h))
+
+    def set_graph_mode(self, on: bool):
+        self.check(self.lib.bib_set_graph_mode(self.h, int(bool(on))))
+
+    def set_profiling(self, on: bool):
+        self.check(self.lib.bib_set_profiling(self.h, int(bool(on))))
+
+    def profile(self):
+        out = np.zeros(5)
+        self.check(self.lib.bib_profile_read(self.h, _d(out), 5))
+        return dict(zip(["interpolate", "membrane", "spread", "collide_stream", "walls"], out))
+
+    def add_domain(self, nx, ny, nz, **kw) -> "Lattice":
+        return Lattice(self, nx, ny, nz, **kw)
+
+
+def lattice_params(periodic=(1, 1, 1), collision="bgk_guo_vof", storage="f64", omega=1.0, omega_inner=None,
+                   trt_magic=0.25, wall_y="none", wall_z="none", wall_u=None, body_force=(0, 0, 0), use_phase=False,
+                   f16_scale=0.0) -> LatticeParams:
+    p = LatticeParams()
+    for k in range(3):
+        p.periodic[k] = int(bool(periodic[k]))
+    p.collision = COLLISION[collision]
+    p.storage = STORAGE[storage]
+    p.wall_y, p.wall_z = WALL[wall_y], WALL[wall_z]
+    p.use_phase = int(bool(use_phase))
+    p.omega = float(omega)
+    p.omega_inner = float(omega if omega_inner is None else omega_inner)
+    p.trt_magic = float(trt_magic)
+    wu = np.zeros((4, 3)) if wall_u is None else np.asarray(wall_u, dtype=np.float64).reshape(4, 3)
+    for a in range(4):
+        for b in range(3):
+            p.wall_u[a][b] = float(wu[a, b])
+    for a in range(3):
+        p.body_force[a] = float(body_force[a])
+    p.f16_scale = float(f16_scale)
+    return p
+
+
+class Lattice:
+    """A D3Q19 lattice on the device (MultiBlockLattice3D + CoProcessor3D::addDomain)."""
+
+    def __init__(self, ctx: Context, nx, ny, nz, **kw):
+        self.ctx, self.nx, self.ny, self.nz = ctx, int(nx), int(ny), int(nz)
+        self.n = self.nx * self.ny * self.nz
+        self.params = lattice_params(**kw)
+        h = C.c_int32()
+        ctx.check(ctx.lib.bib_lattice_add_domain(ctx.h, self.nx, self.ny, self.nz, C.byref(self.params), C.byref(h)))
+        self.h = h.value
+
+    @property
+    def shape(self):
+        return (self.nz, self.ny, self.nx)
+
+    # CoProcessor3D::send / receive
+    def send(self, f, layout="soa"):
+        f = _f64(f)
+        self.ctx.check(self.ctx.lib.bib_lattice_send(self.ctx.h, self.h, f.ctypes.data, f.nbytes, LAYOUT[layout]))
+
+    def receive(self, layout="soa"):
+        out = np.empty((Q,) + self.shape) if layout == "soa" else np.empty((self.nx, self.ny, self.nz, 23))
+        self.ctx.check(self.ctx.lib.bib_lattice_receive(self.ctx.h, self.h, out.ctypes.data, out.nbytes, LAYOUT[layout]))
+        return out
+
+    def collide_and_stream(self, nsteps=1):
+        self.ctx.check(self.ctx.lib.bib_lattice_collide_and_stream(self.ctx.h, self.h, int(nsteps)))
+
+    def initialize_at_equilibrium(self, rho, u):
+        u = _f64(np.broadcast_to(u, (3,) + self.shape))
+        r = None if rho is None else _f64(np.broadcast_to(rho, self.shape))
+        self.ctx.check(self.ctx.lib.bib_lattice_init_equilibrium(self.ctx.h, self.h, _d(r) if r is not None else None,
+                                                                 _d(u)))
+
+    def set_external_force(self, F):
+        F = _f64(np.broadcast_to(F, (3,) + self.shape))
+        self.ctx.check(self.ctx.lib.bib_lattice_set_force(self.ctx.h, self.h, _d(F)))
+
+    def get_external_force(self):
+        F = np.empty((3,) + self.shape)
+        self.ctx.check(self.ctx.lib.bib_lattice_get_force(self.ctx.h, self.h, _d(F)))
+        return F
+
+    def set_phase(self, phase):
+        ph = _f64(np.broadcast_to(phase, self.shape))
+        self.ctx.check(self.ctx.lib.bib_lattice_set_phase(self.ctx.h, self.h, _d(ph)))
+
+    def compute_velocity(self):
+        u = np.empty((3,) + self.shape)
+        self.ctx.check(self.ctx.lib.bib_lattice_get_velocity(self.ctx.h, self.h, _d(u)))
+        return u
+
+    def check_health(self):
+        self.ctx.check(self.ctx.lib.bib_check_health(self.ctx.h, self.h))
+
+
+class ParticleShapeLibrary:
+    """ParticleShapeLibrary (src/fsi/ParticleShapeFactory.h:19-40): rest meshes by tag."""
+
+    def __init__(self, ctx: Context):
+        self.ctx = ctx
+        self.by_tag: dict[str, int] = {}
+        self.meshes: dict[int, tuple] = {}
+
+    def store_mesh(self, xyz, tri, tag: str) -> int:
+        xyz = _f64(xyz)
+        tri = np.ascontiguousarray(tri, dtype=np.int64)
+        sid = C.c_int32()
+        self.ctx.check(self.ctx.lib.bib_shape_store(self.ctx.h, _d(xyz), tri.ctypes.data_as(C.POINTER(C.c_int64)),
+                                                    xyz.shape[0], tri.shape[0], C.byref(sid)))
+        self.by_tag[tag] = sid.value
+        self.meshes[sid.value] = (xyz, tri)
+        return sid.value
+
+    def get_by_tag(self, tag: str) -> int:
+        return self.by_tag[tag]
+
+    def info(self, shape: int) -> dict:
+        out = np.zeros(6)
+        self.ctx.check(self.ctx.lib.bib_shape_info(self.ctx.h, int(shape), _d(out)))
+        return dict(area=out[0], volume=out[1], n_links=int(out[2]), n_pairs=int(out[3]), n_vertices=int(out[4]),
+                    n_triangles=int(out[5]))
+
+
+class ImmersedBoundaryDynamics3D:
+    """The IB module of src/fsi/ImmersedBoundaryDynamics.h:50-217 on one lattice."""
+
+    def __init__(self, lattice: Lattice, shapes: ParticleShapeLibrary, dirac="roma", field_offset=-1.0):
+        self.lattice, self.shapes, self.ctx = lattice, shapes, lattice.ctx
+        p = IbParams(DIRAC[dirac], 0, float(field_offset))
+        self.ctx.check(self.ctx.lib.bib_ib_configure(self.ctx.h, lattice.h, C.byref(p)))
+        self.nv: list[int] = []
+
+    def add_particle(self, shape: int, model: str, params, positions=None) -> int:
+        prm = _f64(params)
+        pos = None if positions is None else _f64(positions)
+        pid = C.c_int32()
+        self.ctx.check(self.ctx.lib.bib_particle_add(self.ctx.h, self.lattice.h, int(shape), MODEL[model], _d(prm),
+                                                     _d(pos) if pos is not None else None, C.byref(pid)))
+        self.nv.append(self.shapes.info(shape)["n_vertices"])
+        return pid.value
+
+    def init(self):
+        """Nothing to synchronise on one device; kept for the reference's call sequence."""
+
+    def count_particles(self) -> int:
+        return len(self.nv)
+
+    def get_particle(self, pid: int) -> dict:
+        nv = self.nv[pid]
+        pos, vel, frc = np.empty((nv, 3)), np.empty((nv, 3)), np.empty((nv, 3))
+        self.ctx.check(self.ctx.lib.bib_particle_get(self.ctx.h, self.lattice.h, pid, _d(pos), _d(vel), _d(frc)))
+        st = np.empty(14)
+        self.ctx.check(self.ctx.lib.bib_particle_stats(self.ctx.h, self.lattice.h, pid, _d(st)))
+        return dict(pos=pos, vel=vel, force=frc, area=st[0], volume=st[1], com=st[2:5], inertia=st[5:14].reshape(3, 3))
+
+    def set_positions(self, pid: int, pos):
+        pos = _f64(pos)
+        self.ctx.check(self.ctx.lib.bib_particle_set_positions(self.ctx.h, self.lattice.h, pid, _d(pos)))
+
+    def download(self):
+        nvt = C.c_int64()
+        self.ctx.check(self.ctx.lib.bib_total_vertices(self.ctx.h, self.lattice.h, C.byref(nvt)))
+        pos = np.empty((nvt.value, 3))
+        stats = np.empty((len(self.nv), 5))
+        self.ctx.check(self.ctx.lib.bib_particles_download(self.ctx.h, self.lattice.h, _d(pos), _d(stats)))
+        return pos, stats
+
+    def compute_total_volume(self) -> float:
+        v = C.c_double()
+        self.ctx.check(self.ctx.lib.bib_total_volume(self.ctx.h, self.lattice.h, C.byref(v)))
+        return v.value
+
+    def ibm_step(self):
+        self.ctx.check(self.ctx.lib.bib_ibm_step(self.ctx.h, self.lattice.h))
+
+    def step(self, nsteps=1):
+        """Coupled steps: computeVelocity, setExternalVector, IB step, collideAndStream."""
+        self.ctx.check(self.ctx.lib.bib_step(self.ctx.h, self.lattice.h, int(nsteps)))
+
+    def step_timed(self, nsteps=1) -> float:
+        """Coupled steps timed with CUDA events on the library's stream; returns milliseconds."""
+        ms = C.c_double()
+        self.ctx.check(self.ctx.lib.bib_step_timed(self.ctx.h, self.lattice.h, int(nsteps), C.byref(ms)))
+        return ms.value
+
+
+def taylor_deformation(inertia) -> float:
+    """Taylor index D = (L - B)/(L + B) of the ellipsoid with the same moment of inertia.
+
+    For an ellipsoid with semi-axes a, b, c the principal moments are
+    I1 = V(b^2+c^2)/5, ...; so a^2 ∝ (I2 + I3 - I1).  L and B are the largest and
+    smallest semi-axes.  Applied identically to the oracle's and the GPU's inertia.
+    """
+    w = np.linalg.eigvalsh(0.5 * (np.asarray(inertia) + np.asarray(inertia).T))
+    s = w.sum()
+    ax2 = np.clip(np.array([s - 2 * w[0], s - 2 * w[1], s - 2 * w[2]]), 0, None)
+    ax = np.sqrt(ax2)
+    L, B = ax.max(), ax.min()
+    return float((L - B) / (L + B))

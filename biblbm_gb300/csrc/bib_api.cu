@@ -1,0 +1,990 @@
+// Host runtime behind the C ABI (include/bib/bib.h): contexts, lattices, shapes,
+// particles, the coupled step and its CUDA-graph replay.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <memory>
+#include <new>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "bib_internal.h"
+
+using namespace bib;
+
+struct GraphEntry {
+    cudaGraphExec_t exec = nullptr;
+    int cur = 0, pcur = 0;
+};
+
+struct bib_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+    std::vector<std::unique_ptr<Lattice>> lattices;
+    std::vector<std::unique_ptr<ShapeHost>> shapes;
+    bool graph_mode = true;
+    bool profiling = false;
+    double prof[5] = {0, 0, 0, 0, 0};
+    cudaEvent_t ev[6] = {};
+    int* d_flag = nullptr;
+    std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, parity) -> two-step graph
+};
+
+namespace {
+
+bib_status fail(bib_ctx* c, bib_status s, const char* fmt, ...) {
+    char buf[512];
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(buf, sizeof(buf), fmt, ap);
+    va_end(ap);
+    if (c) c->err = buf;
+    return s;
+}
+
+#define BIB_CUDA(ctx, expr)                                                                               \
+    do {                                                                                                  \
+        cudaError_t e_ = (expr);                                                                          \
+        if (e_ != cudaSuccess) return fail(ctx, BIB_ECUDA, "%s: %s (%s:%d)", #expr, cudaGetErrorString(e_), \
+                                           __FILE__, __LINE__);                                           \
+    } while (0)
+
+#define BIB_CHECK_LAUNCH(ctx) BIB_CUDA(ctx, cudaGetLastError())
+
+Lattice* get_lattice(bib_ctx* c, int32_t h) {
+    if (!c || h < 0 || h >= (int32_t)c->lattices.size() || !c->lattices[h]) return nullptr;
+    return c->lattices[h].get();
+}
+
+size_t pop_bytes(int storage) { return storage == BIB_STORAGE_F64 ? 8 : (storage == BIB_STORAGE_F32 ? 4 : 2); }
+size_t force_bytes(int storage) { return storage == BIB_STORAGE_F64 ? 8 : 4; }
+
+// ---------------------------------------------------------------- shapes
+// ParticleShape constructor and compute_connectivity, src/fsi/ParticleShape.hh:21-212:
+// triangle rest areas (tri::normal_and_area), total area, signed volume, unique links in
+// (min, max) vertex order with their rest length, and for every link shared by two
+// triangles the adjacent pair (i0, i1, i2, i3) with (i0,i1,i2) and (i0,i2,i3) the two
+// triangles and the cosine / sine of the rest dihedral angle.
+struct V3d {
+    double x, y, z;
+};
+inline V3d sub(V3d a, V3d b) { return {a.x - b.x, a.y - b.y, a.z - b.z}; }
+inline V3d crs(V3d a, V3d b) { return {a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x}; }
+inline double dt(V3d a, V3d b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+inline double nrm(V3d a) { return std::sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+inline V3d scl(V3d a, double s) { return {a.x / s, a.y / s, a.z / s}; }
+
+bool build_shape(ShapeHost& S, const double* xyz, const int64_t* tri, int64_t nv, int64_t nt, std::string& why) {
+    S.rest.assign(xyz, xyz + 3 * nv);
+    S.tri.resize(3 * nt);
+    for (int64_t i = 0; i < 3 * nt; ++i) {
+        if (tri[i] < 0 || tri[i] >= nv) {
+            why = "triangle index out of range";
+            return false;
+        }
+        S.tri[i] = (int)tri[i];
+    }
+    auto P = [&](int i) { return V3d{xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]}; };
+    S.tri_area.resize(nt);
+    S.area = 0;
+    S.volume = 0;
+    for (int64_t t = 0; t < nt; ++t) {
+        V3d a = P(S.tri[3 * t]), b = P(S.tri[3 * t + 1]), c = P(S.tri[3 * t + 2]);
+        double ar = nrm(crs(sub(b, a), sub(c, a))) * 0.5;
+        if (!(ar > 0)) {
+            why = "degenerate triangle";
+            return false;
+        }
+        S.tri_area[t] = ar;
+        S.area += ar;
+        S.volume += dt(a, crs(b, c)) / 6.;
+    }
+    struct L {
+        int t1 = -1, t2 = -1;
+        double len = 0;
+    };
+    std::map<std::pair<int, int>, L> links;
+    for (int64_t t = 0; t < nt; ++t) {
+        int ind[4] = {S.tri[3 * t], S.tri[3 * t + 1], S.tri[3 * t + 2], S.tri[3 * t]};
+        for (int j = 0; j < 3; ++j) {
+            std::pair<int, int> key(std::min(ind[j], ind[j + 1]), std::max(ind[j], ind[j + 1]));
+            auto it = links.find(key);
+            if (it == links.end()) {
+                L l;
+                l.t1 = (int)t;
+                l.len = nrm(sub(P(key.first), P(key.second)));
+                links.emplace(key, l);
+            } else if (it->second.t1 != (int)t) {
+                it->second.t2 = (int)t;
+            }
+        }
+    }
+    S.links.clear();
+    S.link_len.clear();
+    S.pairs.clear();
+    S.pair_cs.clear();
+    for (auto& kv : links) {
+        const int i0 = kv.first.first, i1 = kv.first.second;
+        S.links.push_back(i0);
+        S.links.push_back(i1);
+        S.link_len.push_back(kv.second.len);
+        if (kv.second.t1 < 0 || kv.second.t2 < 0) continue;
+        int a[3] = {S.tri[3 * kv.second.t1], S.tri[3 * kv.second.t1 + 1], S.tri[3 * kv.second.t1 + 2]};
+        int b[3] = {S.tri[3 * kv.second.t2], S.tri[3 * kv.second.t2 + 1], S.tri[3 * kv.second.t2 + 2]};
+        for (int g = 0; g < 3 && !((a[0] == i0 && a[2] == i1) || (a[0] == i1 && a[2] == i0)); ++g) {
+            int tmp = a[0]; a[0] = a[2]; a[2] = a[1]; a[1] = tmp;
+        }
+        for (int g = 0; g < 3 && !((b[0] == i0 && b[1] == i1) || (b[0] == i1 && b[1] == i0)); ++g) {
+            int tmp = b[0]; b[0] = b[2]; b[2] = b[1]; b[1] = tmp;
+        }
+        const int q[4] = {a[0], a[1], a[2], b[2]};
+        for (int k = 0; k < 4; ++k) S.pairs.push_back(q[k]);
+        V3d p0 = P(q[0]), p1 = P(q[1]), p2 = P(q[2]), p3 = P(q[3]);
+        V3d n1 = crs(sub(p1, p0), sub(p2, p0));
+        n1 = scl(n1, nrm(n1));
+        V3d n2 = crs(sub(p2, p0), sub(p3, p0));
+        n2 = scl(n2, nrm(n2));
+        S.pair_cs.push_back(dt(n1, n2));
+        S.pair_cs.push_back((dt(sub(n1, n2), sub(p1, p3)) > 0 ? 1.0 : -1.0) * nrm(crs(n1, n2)));
+    }
+    return true;
+}
+
+template <class T>
+bib_status upload(bib_ctx* c, T** dptr, const std::vector<T>& v) {
+    *dptr = nullptr;
+    if (v.empty()) return BIB_OK;
+    BIB_CUDA(c, cudaMalloc((void**)dptr, v.size() * sizeof(T)));
+    BIB_CUDA(c, cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
+    return BIB_OK;
+}
+
+// DeformableParticle3D::update (DeformableParticle3D.hh:54-82) on the host, FP64.
+void particle_update(const ShapeHost& S, const double* pos, double* st) {
+    double area = 0, vol = 0, cx = 0, cy = 0, cz = 0;
+    const int nt = (int)S.tri_area.size();
+    for (int t = 0; t < nt; ++t) {
+        const double* a = pos + 3 * S.tri[3 * t];
+        const double* b = pos + 3 * S.tri[3 * t + 1];
+        const double* c = pos + 3 * S.tri[3 * t + 2];
+        V3d A{a[0], a[1], a[2]}, B{b[0], b[1], b[2]}, C{c[0], c[1], c[2]};
+        const double dA = nrm(crs(sub(B, A), sub(C, A))) * 0.5;
+        area += dA;
+        vol += dt(A, crs(B, C)) / 6.;
+        cx += (A.x + B.x + C.x) / 3.0 * dA;
+        cy += (A.y + B.y + C.y) / 3.0 * dA;
+        cz += (A.z + B.z + C.z) / 3.0 * dA;
+    }
+    st[0] = area;
+    st[1] = vol;
+    st[2] = cx / area;
+    st[3] = cy / area;
+    st[4] = cz / area;
+}
+
+// ParticleBase3D::map_center_of_mass_to_periodic_grid (ParticleBase.hh:111-136)
+void remap_com(const LatticeDesc& d, double* pos, int nv, double* st) {
+    const int N[3] = {d.nx, d.ny, d.nz};
+    const int per[3] = {d.px, d.py, d.pz};
+    double delta[3] = {0, 0, 0};
+    for (int a = 0; a < 3; ++a) {
+        if (!per[a]) continue;
+        const double L = (double)N[a], Linv = 1. / L;
+        const double np_ = st[2 + a] - L * std::floor((st[2 + a] - (-0.5)) * Linv);
+        delta[a] = np_ - st[2 + a];
+        st[2 + a] = np_;
+    }
+    if (delta[0] != 0 || delta[1] != 0 || delta[2] != 0)
+        for (int i = 0; i < nv; ++i)
+            for (int a = 0; a < 3; ++a) pos[3 * i + a] += delta[a];
+}
+
+// DeformableParticle3D::compute_moment_of_intertia, DeformableParticle3D.hh:173-272
+void moment_of_inertia(const ShapeHost& S, const double* pos, double* I) {
+    double in[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int nt = (int)S.tri_area.size();
+    for (int t = 0; t < nt; ++t) {
+        const double* v0 = pos + 3 * S.tri[3 * t];
+        const double* v1 = pos + 3 * S.tri[3 * t + 1];
+        const double* v2 = pos + 3 * S.tri[3 * t + 2];
+        V3d N = crs(V3d{v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]}, V3d{v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]});
+        double f1[3], f2[3], f3[3], g0[3], g1[3], g2[3];
+        for (int d = 0; d < 3; ++d) {
+            double tmp0 = v0[d] + v1[d];
+            f1[d] = tmp0 + v2[d];
+            double tmp1 = v0[d] * v0[d];
+            double tmp2 = tmp1 + v1[d] * tmp0;
+            f2[d] = tmp2 + v2[d] * f1[d];
+            f3[d] = v0[d] * tmp1 + v1[d] * tmp2 + v2[d] * f2[d];
+            g0[d] = f2[d] + v0[d] * (f1[d] + v0[d]);
+            g1[d] = f2[d] + v1[d] * (f1[d] + v1[d]);
+            g2[d] = f2[d] + v2[d] * (f1[d] + v2[d]);
+        }
+        in[0] += N.x * f1[0];
+        in[1] += N.x * f2[0];
+        in[2] += N.y * f2[1];
+        in[3] += N.z * f2[2];
+        in[4] += N.x * f3[0];
+        in[5] += N.y * f3[1];
+        in[6] += N.z * f3[2];
+        in[7] += N.x * (v0[1] * g0[0] + v1[1] * g1[0] + v2[1] * g2[0]);
+        in[8] += N.y * (v0[2] * g0[1] + v1[2] * g1[1] + v2[2] * g2[1]);
+        in[9] += N.z * (v0[0] * g0[2] + v1[0] * g1[2] + v2[0] * g2[2]);
+    }
+    in[0] *= 1.0 / 6.0;
+    for (int k = 1; k <= 3; ++k) in[k] *= 1.0 / 24.0;
+    for (int k = 4; k <= 6; ++k) in[k] *= 1.0 / 60.0;
+    for (int k = 7; k <= 9; ++k) in[k] *= 1.0 / 120.0;
+    const double vol = in[0];
+    const double c[3] = {in[1] / vol, in[2] / vol, in[3] / vol};
+    I[0] = in[5] + in[6] - vol * (c[1] * c[1] + c[2] * c[2]);
+    I[1] = -in[7] + vol * c[0] * c[1];
+    I[2] = -in[9] + vol * c[2] * c[0];
+    I[3] = I[1];
+    I[4] = in[4] + in[6] - vol * (c[2] * c[2] + c[0] * c[0]);
+    I[5] = -in[8] + vol * c[1] * c[2];
+    I[6] = I[2];
+    I[7] = I[5];
+    I[8] = in[4] + in[5] - vol * (c[0] * c[0] + c[1] * c[1]);
+}
+
+void free_particles(Lattice& L) {
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(L.pos[k]);
+        L.pos[k] = nullptr;
+    }
+    cudaFree(L.vel);
+    cudaFree(L.force);
+    cudaFree(L.stats);
+    cudaFree(L.pdev);
+    L.vel = L.force = L.stats = nullptr;
+    L.pdev = nullptr;
+}
+
+void drop_graphs(bib_ctx* c, int32_t h) {
+    for (auto it = c->graphs.begin(); it != c->graphs.end();) {
+        if (it->first.first == h) {
+            if (it->second.exec) cudaGraphExecDestroy(it->second.exec);
+            it = c->graphs.erase(it);
+        } else {
+            ++it;
+        }
+    }
+}
+
+bib_status sync_particles(bib_ctx* c, Lattice& L) {
+    if (!L.particles_dirty) return BIB_OK;
+    free_particles(L);
+    L.nvert = (int)(L.host_pos.size() / 3);
+    const int np = (int)L.parts.size();
+    if (np == 0) {
+        L.particles_dirty = false;
+        return BIB_OK;
+    }
+    const size_t vb = 3 * (size_t)L.nvert * sizeof(double);
+    for (int k = 0; k < 2; ++k) BIB_CUDA(c, cudaMalloc((void**)&L.pos[k], vb));
+    BIB_CUDA(c, cudaMalloc((void**)&L.vel, vb));
+    BIB_CUDA(c, cudaMalloc((void**)&L.force, vb));
+    BIB_CUDA(c, cudaMalloc((void**)&L.stats, STATS * np * sizeof(double)));
+    BIB_CUDA(c, cudaMemcpy(L.pos[0], L.host_pos.data(), vb, cudaMemcpyHostToDevice));
+    BIB_CUDA(c, cudaMemcpy(L.pos[1], L.host_pos.data(), vb, cudaMemcpyHostToDevice));
+    BIB_CUDA(c, cudaMemset(L.vel, 0, vb));
+    BIB_CUDA(c, cudaMemset(L.force, 0, vb));
+    BIB_CUDA(c, cudaMemcpy(L.stats, L.host_stats.data(), STATS * np * sizeof(double), cudaMemcpyHostToDevice));
+    L.pcur = 0;
+    std::vector<ParticleDev> pd(np);
+    L.max_nv = 0;
+    for (int p = 0; p < np; ++p) {
+        const ParticleHost& ph = L.parts[p];
+        const ShapeHost& S = *c->shapes[ph.shape];
+        ParticleDev& d = pd[p];
+        d.shape = ph.shape;
+        d.model = ph.model;
+        d.v0 = ph.v0;
+        d.nv = ph.nv;
+        d.nt = (int)S.tri_area.size();
+        d.nl = (int)S.link_len.size();
+        d.np = (int)S.pair_cs.size() / 2;
+        d.rest = S.dev.rest;
+        d.tri = S.dev.tri;
+        d.tri_area = S.dev.tri_area;
+        d.links = S.dev.links;
+        d.link_len = S.dev.link_len;
+        d.pairs = S.dev.pairs;
+        d.pair_cs = S.dev.pair_cs;
+        d.A0 = S.area;
+        for (int k = 0; k < BIB_P_COUNT; ++k) d.prm[k] = ph.prm[k];
+        L.max_nv = std::max(L.max_nv, ph.nv);
+    }
+    BIB_CUDA(c, cudaMalloc((void**)&L.pdev, np * sizeof(ParticleDev)));
+    BIB_CUDA(c, cudaMemcpy(L.pdev, pd.data(), np * sizeof(ParticleDev), cudaMemcpyHostToDevice));
+    L.membrane_smem = membrane_smem_bytes(L.max_nv);
+    int dev_max = 0;
+    BIB_CUDA(c, cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
+    if (L.membrane_smem + 1024 > (size_t)dev_max)
+        return fail(c, BIB_EUNSUPPORTED, "mesh with %d vertices exceeds the membrane kernel's shared memory", L.max_nv);
+    configure_membrane_kernel(L.membrane_smem);
+    BIB_CHECK_LAUNCH(c);
+    L.particles_dirty = false;
+    drop_graphs(c, L.handle);
+    return BIB_OK;
+}
+
+void record(bib_ctx* c, int idx) {
+    if (c->profiling) cudaEventRecord(c->ev[idx], c->stream);
+}
+
+// One coupled step in the driver order of progs/capsule_in_shear/capsule_in_shear.cpp:187-227:
+// velocity at the vertices from the current state (computeVelocity + interpolate), force
+// field reset to the body force (setExternalVector), membrane forces + vertex motion,
+// spreading, collide-and-stream, wall processors.
+void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
+    cudaStream_t s = c->stream;
+    const bool ib = with_ib && L.nvert > 0;
+    record(c, 0);
+    if (ib) launch_interpolate(L, s);
+    record(c, 1);
+    if (with_ib) launch_force_fill(L, s);
+    if (ib) launch_membrane(L, s);
+    record(c, 2);
+    if (ib) launch_spread(L, s);
+    record(c, 3);
+    if (with_lbm) launch_collide_stream(L, s);
+    record(c, 4);
+    if (with_lbm) launch_fd_walls(L, L.f[1 - L.cur], s);
+    record(c, 5);
+    if (with_lbm) L.cur = 1 - L.cur;
+    if (ib) L.pcur = 1 - L.pcur;
+}
+
+bib_status accumulate_profile(bib_ctx* c) {
+    if (!c->profiling) return BIB_OK;
+    BIB_CUDA(c, cudaEventSynchronize(c->ev[5]));
+    for (int k = 0; k < 5; ++k) {
+        float ms = 0;
+        BIB_CUDA(c, cudaEventElapsedTime(&ms, c->ev[k], c->ev[k + 1]));
+        c->prof[k] += ms;
+    }
+    return BIB_OK;
+}
+
+bib_status run_steps(bib_ctx* c, int32_t h, int64_t nsteps, bool with_ib, bool with_lbm) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle %d", h);
+    if (nsteps < 0) return fail(c, BIB_EINVAL, "negative step count");
+    bib_status st = sync_particles(c, *L);
+    if (st) return st;
+    const bool use_graph = c->graph_mode && !c->profiling && with_ib && with_lbm && nsteps >= 2;
+    int64_t done = 0;
+    if (use_graph) {
+        const std::pair<int, int> key(h, L->cur * 2 + L->pcur);
+        GraphEntry& ge = c->graphs[key];
+        if (!ge.exec) {
+            const int cur0 = L->cur, pcur0 = L->pcur;
+            cudaGraph_t g = nullptr;
+            BIB_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            enqueue_step(c, *L, true, true);
+            enqueue_step(c, *L, true, true);
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            L->cur = cur0;
+            L->pcur = pcur0;
+            if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&ge.exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+        }
+        for (; done + 2 <= nsteps; done += 2) BIB_CUDA(c, cudaGraphLaunch(ge.exec, c->stream));
+        // two steps leave both parities unchanged
+    }
+    for (; done < nsteps; ++done) {
+        enqueue_step(c, *L, with_ib, with_lbm);
+        BIB_CHECK_LAUNCH(c);
+        if (c->profiling) {
+            st = accumulate_profile(c);
+            if (st) return st;
+        }
+    }
+    BIB_CHECK_LAUNCH(c);
+    return BIB_OK;
+}
+
+// Make the host copies of the particle state authoritative again (before they change).
+bib_status pull_particles(bib_ctx* c, Lattice& L) {
+    if (L.particles_dirty || L.nvert == 0) return BIB_OK;
+    L.host_pos.assign(3 * (size_t)L.nvert, 0.0);
+    L.host_stats.assign(STATS * L.parts.size(), 0.0);
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    BIB_CUDA(c, cudaMemcpy(L.host_pos.data(), L.pos[L.pcur], L.host_pos.size() * 8, cudaMemcpyDeviceToHost));
+    BIB_CUDA(c, cudaMemcpy(L.host_stats.data(), L.stats, L.host_stats.size() * 8, cudaMemcpyDeviceToHost));
+    return BIB_OK;
+}
+
+bib_status device_buffer(bib_ctx* c, double** d, const double* host, size_t count) {
+    BIB_CUDA(c, cudaMalloc((void**)d, count * sizeof(double)));
+    if (host) BIB_CUDA(c, cudaMemcpyAsync(*d, host, count * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    return BIB_OK;
+}
+
+}  // namespace
+
+// =================================================================== C ABI
+extern "C" {
+
+int32_t bib_abi_version(void) { return BIB_ABI_VERSION; }
+
+const char* bib_status_string(bib_status s) {
+    switch (s) {
+        case BIB_OK: return "ok";
+        case BIB_EINVAL: return "invalid argument";
+        case BIB_ENOMEM: return "out of memory";
+        case BIB_ECUDA: return "CUDA error";
+        case BIB_ENAN: return "NaN or Inf in the state";
+        case BIB_ETIMEOUT: return "device wait timed out";
+        case BIB_ESTATE: return "invalid call order";
+        case BIB_EUNSUPPORTED: return "unsupported option";
+        default: return "unknown status";
+    }
+}
+
+bib_status bib_create(const bib_config* cfg, bib_ctx** out) {
+    if (!out) return BIB_EINVAL;
+    *out = nullptr;
+    bib_ctx* c = new (std::nothrow) bib_ctx();
+    if (!c) return BIB_ENOMEM;
+    c->device = cfg ? cfg->device : 0;
+    cudaError_t e = cudaSetDevice(c->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_flag, sizeof(int));
+    if (e != cudaSuccess) {
+        delete c;
+        return BIB_ECUDA;
+    }
+    *out = c;
+    return BIB_OK;
+}
+
+void bib_destroy(bib_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    for (auto& kv : c->graphs)
+        if (kv.second.exec) cudaGraphExecDestroy(kv.second.exec);
+    for (auto& Lp : c->lattices) {
+        if (!Lp) continue;
+        free_particles(*Lp);
+        cudaFree(Lp->f[0]);
+        cudaFree(Lp->f[1]);
+        cudaFree(Lp->F);
+        cudaFree(Lp->phase);
+    }
+    for (auto& S : c->shapes) {
+        cudaFree(S->dev.rest);
+        cudaFree(S->dev.tri);
+        cudaFree(S->dev.tri_area);
+        cudaFree(S->dev.links);
+        cudaFree(S->dev.link_len);
+        cudaFree(S->dev.pairs);
+        cudaFree(S->dev.pair_cs);
+    }
+    for (int k = 0; k < 6; ++k)
+        if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+    cudaFree(c->d_flag);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+bib_status bib_sync(bib_ctx* c) {
+    if (!c) return BIB_EINVAL;
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BIB_OK;
+}
+
+size_t bib_last_error(const bib_ctx* c, char* buf, size_t len) {
+    if (!c) return 0;
+    if (buf && len) {
+        std::strncpy(buf, c->err.c_str(), len - 1);
+        buf[len - 1] = 0;
+    }
+    return c->err.size();
+}
+
+bib_status bib_set_graph_mode(bib_ctx* c, int32_t enabled) {
+    if (!c) return BIB_EINVAL;
+    c->graph_mode = enabled != 0;
+    return BIB_OK;
+}
+
+bib_status bib_set_profiling(bib_ctx* c, int32_t enabled) {
+    if (!c) return BIB_EINVAL;
+    c->profiling = enabled != 0;
+    for (double& v : c->prof) v = 0;
+    return BIB_OK;
+}
+
+bib_status bib_profile_read(bib_ctx* c, double* out, int32_t n) {
+    if (!c || !out) return BIB_EINVAL;
+    for (int k = 0; k < n && k < 5; ++k) out[k] = c->prof[k];
+    return BIB_OK;
+}
+
+bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz, const bib_lattice_params* p,
+                                  int32_t* handle) {
+    if (!c || !p || !handle) return fail(c, BIB_EINVAL, "null argument");
+    if (nx < 3 || ny < 3 || nz < 3 || nx > 65535 || ny > 65535 || nz > 65535)
+        return fail(c, BIB_EINVAL, "lattice dimensions must be in [3, 65535]");
+    if (p->storage < BIB_STORAGE_F64 || p->storage > BIB_STORAGE_F16) return fail(c, BIB_EINVAL, "bad storage");
+    if (p->collision < 0 || p->collision > BIB_COLLISION_TRT) return fail(c, BIB_EINVAL, "bad collision");
+    if (!(p->omega > 0 && p->omega < 2)) return fail(c, BIB_EINVAL, "omega must lie in (0, 2)");
+    if (p->use_phase && !(p->omega_inner > 0 && p->omega_inner < 2)) return fail(c, BIB_EINVAL, "omega_inner must lie in (0, 2)");
+    if (p->periodic[0] == 0) return fail(c, BIB_EUNSUPPORTED, "the x axis must be periodic");
+    if (!p->periodic[1] && p->wall_y == BIB_WALL_NONE) return fail(c, BIB_EINVAL, "non-periodic y needs a wall type");
+    if (!p->periodic[2] && p->wall_z == BIB_WALL_NONE) return fail(c, BIB_EINVAL, "non-periodic z needs a wall type");
+    if (!p->periodic[2] && p->wall_z == BIB_WALL_FD_VELOCITY)
+        return fail(c, BIB_EUNSUPPORTED, "finite-difference velocity walls are implemented on y planes");
+    if (!p->periodic[1] && !p->periodic[2] && p->wall_y == BIB_WALL_FD_VELOCITY)
+        return fail(c, BIB_EUNSUPPORTED, "finite-difference y walls need a periodic z axis");
+    auto L = std::make_unique<Lattice>();
+    LatticeDesc& d = L->d;
+    d.nx = (int)nx;
+    d.ny = (int)ny;
+    d.nz = (int)nz;
+    d.n = nx * ny * nz;
+    d.stride = (d.n + 127) / 128 * 128;
+    d.px = p->periodic[0] != 0;
+    d.py = p->periodic[1] != 0;
+    d.pz = p->periodic[2] != 0;
+    d.wall_y = d.py ? BIB_WALL_NONE : p->wall_y;
+    d.wall_z = d.pz ? BIB_WALL_NONE : p->wall_z;
+    d.collision = p->collision;
+    d.use_phase = p->use_phase != 0;
+    d.omega = p->omega;
+    d.omega_inner = p->use_phase ? p->omega_inner : p->omega;
+    d.trt_magic = p->trt_magic > 0 ? p->trt_magic : 0.25;
+    // computeOmega, src/fsi/VariableViscosityDynamics.hh:131-141, for phase 0 and 1
+    d.omega_c0 = d.omega * d.omega_inner / (0.0 * d.omega + (1. - 0.0) * d.omega_inner);
+    d.omega_c1 = d.omega * d.omega_inner / (1.0 * d.omega + (1. - 1.0) * d.omega_inner);
+    std::memcpy(d.wall_u, p->wall_u, sizeof(d.wall_u));
+    std::memcpy(d.body, p->body_force, sizeof(d.body));
+    const double sc = p->f16_scale > 0 ? p->f16_scale : 8192.0;
+    d.scale = p->storage == BIB_STORAGE_F16 ? (float)sc : 1.0f;
+    d.inv_scale = 1.0f / d.scale;
+    L->storage = p->storage;
+    const size_t pb = pop_bytes(p->storage) * Q * d.stride;
+    for (int k = 0; k < 2; ++k) {
+        cudaError_t e = cudaMalloc(&L->f[k], pb);
+        if (e != cudaSuccess) {
+            cudaFree(L->f[0]);
+            return fail(c, BIB_ENOMEM, "population buffers (%zu bytes): %s", pb, cudaGetErrorString(e));
+        }
+        cudaMemsetAsync(L->f[k], 0, pb, c->stream);
+    }
+    const size_t fb = force_bytes(p->storage) * 3 * d.stride;
+    if (cudaMalloc(&L->F, fb) != cudaSuccess) {
+        cudaFree(L->f[0]);
+        cudaFree(L->f[1]);
+        return fail(c, BIB_ENOMEM, "force field (%zu bytes)", fb);
+    }
+    cudaMemsetAsync(L->F, 0, fb, c->stream);
+    if (d.use_phase) {
+        if (cudaMalloc((void**)&L->phase, d.stride) != cudaSuccess) return fail(c, BIB_ENOMEM, "phase field");
+        cudaMemsetAsync(L->phase, 0, d.stride, c->stream);
+    }
+    // external scalars start at zero, as Palabos cells do; every coupled step then
+    // resets them to the body force before spreading (setExternalVector)
+    BIB_CHECK_LAUNCH(c);
+    *handle = (int32_t)c->lattices.size();
+    L->handle = *handle;
+    c->lattices.push_back(std::move(L));
+    return BIB_OK;
+}
+
+bib_status bib_lattice_cells(bib_ctx* c, int32_t h, int64_t* n) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !n) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    *n = L->d.n;
+    return BIB_OK;
+}
+
+bib_status bib_lattice_send(bib_ctx* c, int32_t h, const void* buf, size_t bytes, int32_t layout) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !buf) return fail(c, BIB_EINVAL, "invalid lattice handle or buffer");
+    const int64_t n = L->d.n;
+    std::vector<double> soa;
+    const double* src = (const double*)buf;
+    std::vector<double> ext;
+    if (layout == BIB_LAYOUT_SOA_F64) {
+        if (bytes != (size_t)Q * n * sizeof(double)) return fail(c, BIB_EINVAL, "expected %zu bytes", (size_t)Q * n * 8);
+    } else if (layout == BIB_LAYOUT_PALABOS_F64) {
+        if (bytes != (size_t)23 * n * sizeof(double)) return fail(c, BIB_EINVAL, "expected %zu bytes", (size_t)23 * n * 8);
+        soa.resize(Q * n);
+        ext.resize(4 * n);
+        const LatticeDesc& d = L->d;
+        int64_t w = 0;
+        for (int x = 0; x < d.nx; ++x)
+            for (int y = 0; y < d.ny; ++y)
+                for (int z = 0; z < d.nz; ++z, ++w) {
+                    const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+                    for (int i = 0; i < Q; ++i) soa[i * n + k] = src[23 * w + i];
+                    for (int a = 0; a < 4; ++a) ext[a * n + k] = src[23 * w + Q + a];
+                }
+        src = soa.data();
+    } else {
+        return fail(c, BIB_EINVAL, "unknown layout %d", layout);
+    }
+    double* d = nullptr;
+    bib_status st = device_buffer(c, &d, src, Q * n);
+    if (st) return st;
+    launch_import_soa(*L, L->f[L->cur], d, c->stream);
+    BIB_CHECK_LAUNCH(c);
+    if (!ext.empty()) {
+        double* dF = nullptr;
+        st = device_buffer(c, &dF, ext.data(), 4 * n);
+        if (st) {
+            cudaFree(d);
+            return st;
+        }
+        launch_force_import(*L, dF, c->stream);
+        if (L->phase) launch_phase_import(*L, dF + 3 * n, c->stream);
+        BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+        cudaFree(dF);
+    }
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(d);
+    return BIB_OK;
+}
+
+bib_status bib_lattice_receive(bib_ctx* c, int32_t h, void* buf, size_t bytes, int32_t layout) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !buf) return fail(c, BIB_EINVAL, "invalid lattice handle or buffer");
+    const int64_t n = L->d.n;
+    const size_t want = (layout == BIB_LAYOUT_PALABOS_F64 ? 23 : Q) * n * sizeof(double);
+    if (layout != BIB_LAYOUT_SOA_F64 && layout != BIB_LAYOUT_PALABOS_F64) return fail(c, BIB_EINVAL, "unknown layout");
+    if (bytes != want) return fail(c, BIB_EINVAL, "expected %zu bytes", want);
+    double* d = nullptr;
+    bib_status st = device_buffer(c, &d, nullptr, (Q + 3) * n);
+    if (st) return st;
+    launch_export_soa(*L, L->f[L->cur], d, c->stream);
+    launch_force_export(*L, d + Q * n, c->stream);
+    BIB_CHECK_LAUNCH(c);
+    std::vector<double> host((Q + 3) * n);
+    BIB_CUDA(c, cudaMemcpyAsync(host.data(), d, host.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(d);
+    if (layout == BIB_LAYOUT_SOA_F64) {
+        std::memcpy(buf, host.data(), want);
+        return BIB_OK;
+    }
+    double* dst = (double*)buf;
+    const LatticeDesc& dd = L->d;
+    int64_t w = 0;
+    for (int x = 0; x < dd.nx; ++x)
+        for (int y = 0; y < dd.ny; ++y)
+            for (int z = 0; z < dd.nz; ++z, ++w) {
+                const int64_t k = x + (int64_t)dd.nx * (y + (int64_t)dd.ny * z);
+                for (int i = 0; i < Q; ++i) dst[23 * w + i] = host[i * n + k];
+                for (int a = 0; a < 3; ++a) dst[23 * w + Q + a] = host[(Q + a) * n + k];
+                dst[23 * w + 22] = 0.0;
+            }
+    return BIB_OK;
+}
+
+bib_status bib_lattice_collide_and_stream(bib_ctx* c, int32_t h, int64_t nsteps) {
+    return run_steps(c, h, nsteps, false, true);
+}
+
+bib_status bib_lattice_init_equilibrium(bib_ctx* c, int32_t h, const double* rho, const double* u) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !u) return fail(c, BIB_EINVAL, "invalid lattice handle or velocity");
+    const int64_t n = L->d.n;
+    double *dr = nullptr, *du = nullptr;
+    bib_status st = device_buffer(c, &du, u, 3 * n);
+    if (st) return st;
+    if (rho) {
+        st = device_buffer(c, &dr, rho, n);
+        if (st) return st;
+    }
+    launch_init_equilibrium(*L, L->f[L->cur], dr, du, c->stream);
+    launch_fd_walls(*L, L->f[L->cur], c->stream);
+    BIB_CHECK_LAUNCH(c);
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(du);
+    cudaFree(dr);
+    return BIB_OK;
+}
+
+bib_status bib_lattice_set_force(bib_ctx* c, int32_t h, const double* F) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !F) return fail(c, BIB_EINVAL, "invalid lattice handle or force");
+    double* d = nullptr;
+    bib_status st = device_buffer(c, &d, F, 3 * L->d.n);
+    if (st) return st;
+    launch_force_import(*L, d, c->stream);
+    BIB_CHECK_LAUNCH(c);
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(d);
+    return BIB_OK;
+}
+
+bib_status bib_lattice_get_force(bib_ctx* c, int32_t h, double* F) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !F) return fail(c, BIB_EINVAL, "invalid lattice handle or force");
+    double* d = nullptr;
+    bib_status st = device_buffer(c, &d, nullptr, 3 * L->d.n);
+    if (st) return st;
+    launch_force_export(*L, d, c->stream);
+    BIB_CHECK_LAUNCH(c);
+    BIB_CUDA(c, cudaMemcpyAsync(F, d, 3 * L->d.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(d);
+    return BIB_OK;
+}
+
+bib_status bib_lattice_set_phase(bib_ctx* c, int32_t h, const double* phase) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !phase) return fail(c, BIB_EINVAL, "invalid lattice handle or phase");
+    if (!L->phase) return fail(c, BIB_ESTATE, "lattice was created with use_phase = 0");
+    double* d = nullptr;
+    bib_status st = device_buffer(c, &d, phase, L->d.n);
+    if (st) return st;
+    launch_phase_import(*L, d, c->stream);
+    BIB_CHECK_LAUNCH(c);
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(d);
+    return BIB_OK;
+}
+
+bib_status bib_lattice_get_velocity(bib_ctx* c, int32_t h, double* u) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !u) return fail(c, BIB_EINVAL, "invalid lattice handle or velocity");
+    double* d = nullptr;
+    bib_status st = device_buffer(c, &d, nullptr, 3 * L->d.n);
+    if (st) return st;
+    launch_velocity(*L, d, c->stream);
+    BIB_CHECK_LAUNCH(c);
+    BIB_CUDA(c, cudaMemcpyAsync(u, d, 3 * L->d.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(d);
+    return BIB_OK;
+}
+
+bib_status bib_shape_store(bib_ctx* c, const double* xyz, const int64_t* tri, int64_t nv, int64_t nt, int32_t* shape) {
+    if (!c || !xyz || !tri || !shape) return fail(c, BIB_EINVAL, "null argument");
+    if (nv < 4 || nt < 4 || nv > (1 << 24) || nt > (1 << 25)) return fail(c, BIB_EINVAL, "bad mesh size");
+    auto S = std::make_unique<ShapeHost>();
+    std::string why;
+    if (!build_shape(*S, xyz, tri, nv, nt, why)) return fail(c, BIB_EINVAL, "invalid mesh: %s", why.c_str());
+    bib_status st;
+    if ((st = upload(c, &S->dev.rest, S->rest)) || (st = upload(c, &S->dev.tri, S->tri)) ||
+        (st = upload(c, &S->dev.tri_area, S->tri_area)) || (st = upload(c, &S->dev.links, S->links)) ||
+        (st = upload(c, &S->dev.link_len, S->link_len)) || (st = upload(c, &S->dev.pairs, S->pairs)) ||
+        (st = upload(c, &S->dev.pair_cs, S->pair_cs)))
+        return st;
+    S->dev.nv = (int)nv;
+    S->dev.nt = (int)nt;
+    S->dev.nl = (int)S->link_len.size();
+    S->dev.np = (int)S->pair_cs.size() / 2;
+    S->dev.area = S->area;
+    S->dev.volume = S->volume;
+    *shape = (int32_t)c->shapes.size();
+    c->shapes.push_back(std::move(S));
+    return BIB_OK;
+}
+
+bib_status bib_shape_info(bib_ctx* c, int32_t shape, double* out) {
+    if (!c || !out || shape < 0 || shape >= (int32_t)c->shapes.size()) return fail(c, BIB_EINVAL, "invalid shape");
+    const ShapeHost& S = *c->shapes[shape];
+    out[0] = S.area;
+    out[1] = S.volume;
+    out[2] = (double)S.link_len.size();
+    out[3] = (double)(S.pair_cs.size() / 2);
+    out[4] = (double)(S.rest.size() / 3);
+    out[5] = (double)S.tri_area.size();
+    return BIB_OK;
+}
+
+bib_status bib_ib_configure(bib_ctx* c, int32_t h, const bib_ib_params* p) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !p) return fail(c, BIB_EINVAL, "invalid lattice handle or parameters");
+    if (p->dirac != BIB_DIRAC_ROMA && p->dirac != BIB_DIRAC_PESKIN) return fail(c, BIB_EINVAL, "bad dirac");
+    if (p->spread_mode != BIB_SPREAD_ATOMIC) return fail(c, BIB_EUNSUPPORTED, "only atomic spreading is built");
+    if (p->field_offset != std::floor(p->field_offset)) return fail(c, BIB_EINVAL, "field offset must be integral");
+    L->ib.dirac = p->dirac;
+    L->ib.spread_mode = p->spread_mode;
+    L->ib.offset = p->field_offset;
+    drop_graphs(c, h);
+    return BIB_OK;
+}
+
+bib_status bib_particle_add(bib_ctx* c, int32_t h, int32_t shape, int32_t model, const double* params,
+                            const double* xyz, int32_t* pid) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !params || !pid) return fail(c, BIB_EINVAL, "invalid lattice handle or argument");
+    if (shape < 0 || shape >= (int32_t)c->shapes.size()) return fail(c, BIB_EINVAL, "invalid shape %d", shape);
+    if (model < BIB_MODEL_CAPSULE_NEOHOOKEAN || model > BIB_MODEL_SKALAK_BENDING) return fail(c, BIB_EINVAL, "bad model");
+    const ShapeHost& S = *c->shapes[shape];
+    const int nv = (int)(S.rest.size() / 3);
+    if (model == BIB_MODEL_RBC_WLCPOW || model == BIB_MODEL_SKALAK_BENDING) {
+        if (!(params[BIB_P_VOL_DESIRED] != 0)) return fail(c, BIB_EINVAL, "vol_desired must be non-zero");
+    }
+    bib_status pst = pull_particles(c, *L);
+    if (pst) return pst;
+    ParticleHost ph;
+    ph.shape = shape;
+    ph.model = model;
+    ph.v0 = (int)(L->host_pos.size() / 3);
+    ph.nv = nv;
+    ph.prm.assign(params, params + BIB_P_COUNT);
+    std::vector<double> pos(xyz ? xyz : S.rest.data(), (xyz ? xyz : S.rest.data()) + 3 * nv);
+    double st[STATS];
+    particle_update(S, pos.data(), st);
+    remap_com(L->d, pos.data(), nv, st);
+    L->host_pos.insert(L->host_pos.end(), pos.begin(), pos.end());
+    L->host_stats.insert(L->host_stats.end(), st, st + STATS);
+    L->parts.push_back(ph);
+    L->particles_dirty = true;
+    *pid = (int32_t)L->parts.size() - 1;
+    return BIB_OK;
+}
+
+bib_status bib_particle_count(bib_ctx* c, int32_t h, int32_t* n) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !n) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    *n = (int32_t)L->parts.size();
+    return BIB_OK;
+}
+
+bib_status bib_total_vertices(bib_ctx* c, int32_t h, int64_t* n) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !n) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    int64_t s = 0;
+    for (auto& p : L->parts) s += p.nv;
+    *n = s;
+    return BIB_OK;
+}
+
+bib_status bib_particle_get(bib_ctx* c, int32_t h, int32_t pid, double* pos, double* vel, double* force) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || pid < 0 || pid >= (int32_t)L->parts.size()) return fail(c, BIB_EINVAL, "invalid particle");
+    const ParticleHost& ph = L->parts[pid];
+    const size_t off = 3 * (size_t)ph.v0, cnt = 3 * (size_t)ph.nv;
+    if (L->particles_dirty) {
+        if (pos) std::memcpy(pos, L->host_pos.data() + off, cnt * 8);
+        if (vel) std::memset(vel, 0, cnt * 8);
+        if (force) std::memset(force, 0, cnt * 8);
+        return BIB_OK;
+    }
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (pos) BIB_CUDA(c, cudaMemcpy(pos, L->pos[L->pcur] + off, cnt * 8, cudaMemcpyDeviceToHost));
+    if (vel) BIB_CUDA(c, cudaMemcpy(vel, L->vel + off, cnt * 8, cudaMemcpyDeviceToHost));
+    if (force) BIB_CUDA(c, cudaMemcpy(force, L->force + off, cnt * 8, cudaMemcpyDeviceToHost));
+    return BIB_OK;
+}
+
+bib_status bib_particle_set_positions(bib_ctx* c, int32_t h, int32_t pid, const double* pos) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !pos || pid < 0 || pid >= (int32_t)L->parts.size()) return fail(c, BIB_EINVAL, "invalid particle");
+    const ParticleHost& ph = L->parts[pid];
+    bib_status pst = pull_particles(c, *L);
+    if (pst) return pst;
+    std::memcpy(L->host_pos.data() + 3 * (size_t)ph.v0, pos, 3 * (size_t)ph.nv * 8);
+    particle_update(*c->shapes[ph.shape], L->host_pos.data() + 3 * (size_t)ph.v0, L->host_stats.data() + STATS * pid);
+    L->particles_dirty = true;
+    return BIB_OK;
+}
+
+bib_status bib_particles_download(bib_ctx* c, int32_t h, double* pos, double* stats) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    if (L->particles_dirty) {
+        if (pos) std::memcpy(pos, L->host_pos.data(), L->host_pos.size() * 8);
+        if (stats) std::memcpy(stats, L->host_stats.data(), L->host_stats.size() * 8);
+        return BIB_OK;
+    }
+    if (pos && L->nvert) BIB_CUDA(c, cudaMemcpyAsync(pos, L->pos[L->pcur], 3 * (size_t)L->nvert * 8, cudaMemcpyDeviceToHost, c->stream));
+    if (stats && !L->parts.empty())
+        BIB_CUDA(c, cudaMemcpyAsync(stats, L->stats, STATS * L->parts.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BIB_OK;
+}
+
+bib_status bib_particle_stats(bib_ctx* c, int32_t h, int32_t pid, double* out) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !out || pid < 0 || pid >= (int32_t)L->parts.size()) return fail(c, BIB_EINVAL, "invalid particle");
+    const ParticleHost& ph = L->parts[pid];
+    std::vector<double> pos(3 * (size_t)ph.nv);
+    bib_status st = bib_particle_get(c, h, pid, pos.data(), nullptr, nullptr);
+    if (st) return st;
+    double s[STATS];
+    if (L->particles_dirty) {
+        std::memcpy(s, L->host_stats.data() + STATS * pid, sizeof(s));
+    } else {
+        BIB_CUDA(c, cudaMemcpy(s, L->stats + STATS * pid, sizeof(s), cudaMemcpyDeviceToHost));
+    }
+    std::memcpy(out, s, sizeof(s));
+    moment_of_inertia(*c->shapes[ph.shape], pos.data(), out + STATS);
+    return BIB_OK;
+}
+
+bib_status bib_total_volume(bib_ctx* c, int32_t h, double* v) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !v) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    std::vector<double> st(STATS * L->parts.size());
+    bib_status s = bib_particles_download(c, h, nullptr, st.data());
+    if (s) return s;
+    double tot = 0;
+    for (size_t p = 0; p < L->parts.size(); ++p) tot += st[STATS * p + 1];
+    *v = tot;
+    return BIB_OK;
+}
+
+bib_status bib_ibm_step(bib_ctx* c, int32_t h) { return run_steps(c, h, 1, true, false); }
+
+bib_status bib_step(bib_ctx* c, int32_t h, int64_t nsteps) { return run_steps(c, h, nsteps, true, true); }
+
+bib_status bib_step_timed(bib_ctx* c, int32_t h, int64_t nsteps, double* ms) {
+    if (!c || !ms) return fail(c, BIB_EINVAL, "null argument");
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle %d", h);
+    bib_status st = sync_particles(c, *L);  // uploads happen outside the timed region
+    if (st) return st;
+    cudaEvent_t a, b;
+    BIB_CUDA(c, cudaEventCreate(&a));
+    BIB_CUDA(c, cudaEventCreate(&b));
+    BIB_CUDA(c, cudaEventRecord(a, c->stream));
+    st = run_steps(c, h, nsteps, true, true);
+    BIB_CUDA(c, cudaEventRecord(b, c->stream));
+    BIB_CUDA(c, cudaEventSynchronize(b));
+    float f = 0;
+    BIB_CUDA(c, cudaEventElapsedTime(&f, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = f;
+    return st;
+}
+
+bib_status bib_check_health(bib_ctx* c, int32_t h) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    BIB_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
+    launch_nan_scan(*L, c->d_flag, c->stream);
+    BIB_CHECK_LAUNCH(c);
+    int flag = 0;
+    BIB_CUDA(c, cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (flag) return fail(c, BIB_ENAN, "populations contain NaN or Inf");
+    if (!L->particles_dirty && L->nvert) {
+        std::vector<double> pos(3 * (size_t)L->nvert);
+        BIB_CUDA(c, cudaMemcpy(pos.data(), L->pos[L->pcur], pos.size() * 8, cudaMemcpyDeviceToHost));
+        for (double v : pos)
+            if (!std::isfinite(v)) return fail(c, BIB_ENAN, "vertex positions contain NaN or Inf");
+    }
+    return BIB_OK;
+}
+
+}  // extern "C"

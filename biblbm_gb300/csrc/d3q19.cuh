@@ -1,0 +1,193 @@
+// D3Q19 lattice constants and the per-cell collision arithmetic shared by the
+// lattice and immersed-boundary kernels.
+#pragma once
+
+#include <cuda_fp16.h>
+#include <stdint.h>
+
+#include "bib_internal.h"
+
+namespace bib {
+
+// Velocity set in the reference order, src/latticeBoltzmann/nearestNeighborLattices3D.hh:165-197
+// (c[i] = -c[i+9]).
+__host__ __device__ constexpr int cx(int i) {
+    return (i == 1 || i == 4 || i == 5 || i == 6 || i == 7) ? -1 : ((i == 10 || i == 13 || i == 14 || i == 15 || i == 16) ? 1 : 0);
+}
+__host__ __device__ constexpr int cy(int i) {
+    return (i == 2 || i == 4 || i == 8 || i == 9 || i == 14) ? -1 : ((i == 5 || i == 11 || i == 13 || i == 17 || i == 18) ? 1 : 0);
+}
+__host__ __device__ constexpr int cz(int i) {
+    return (i == 3 || i == 6 || i == 8 || i == 16 || i == 18) ? -1 : ((i == 7 || i == 9 || i == 12 || i == 15 || i == 17) ? 1 : 0);
+}
+__host__ __device__ constexpr int opposite(int i) { return i == 0 ? 0 : (i < 10 ? i + 9 : i - 9); }
+
+template <class C>
+__host__ __device__ constexpr C weight(int i) {
+    return i == 0 ? C(1) / C(3) : ((cx(i) * cx(i) + cy(i) * cy(i) + cz(i) * cz(i)) == 1 ? C(1) / C(18) : C(1) / C(36));
+}
+
+// ---------------------------------------------------------------- storage
+// Populations are stored as f-bar = f - t_i; FP16 storage keeps f-bar * scale.
+template <class T>
+struct Store;
+template <>
+struct Store<double> {
+    using C = double;
+    using F = double;
+    static __device__ __forceinline__ double load(const double* p, float) { return __ldg(p); }
+    static __device__ __forceinline__ void store(double* p, double v, float) { *p = v; }
+};
+template <>
+struct Store<float> {
+    using C = float;
+    using F = float;
+    static __device__ __forceinline__ float load(const float* p, float) { return __ldg(p); }
+    static __device__ __forceinline__ void store(float* p, float v, float) { *p = v; }
+};
+template <>
+struct Store<__half> {
+    using C = float;
+    using F = float;
+    static __device__ __forceinline__ float load(const __half* p, float inv_scale) {
+        return __half2float(__ldg(p)) * inv_scale;
+    }
+    static __device__ __forceinline__ void store(__half* p, float v, float scale) { *p = __float2half_rn(v * scale); }
+};
+
+// ---------------------------------------------------------------- moments
+// get_rhoBar and get_rhoBar_j (partial sums), src/latticeBoltzmann/momentTemplates3D.h:350-423
+template <class C>
+__device__ __forceinline__ C rho_bar_seq(const C* f) {
+    return f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14] +
+           f[15] + f[16] + f[17] + f[18];
+}
+template <class C>
+__device__ __forceinline__ void rho_bar_j(const C* f, C& rb, C* j) {
+    const C sxm = f[1] + f[4] + f[5] + f[6] + f[7];
+    const C sxp = f[10] + f[13] + f[14] + f[15] + f[16];
+    const C sym = f[2] + f[4] + f[8] + f[9] + f[14];
+    const C syp = f[5] + f[11] + f[13] + f[17] + f[18];
+    const C szm = f[3] + f[6] + f[8] + f[16] + f[18];
+    const C szp = f[7] + f[9] + f[12] + f[15] + f[17];
+    const C sx0 = f[0] + f[2] + f[3] + f[8] + f[9] + f[11] + f[12] + f[17] + f[18];
+    rb = sxm + sx0 + sxp;
+    j[0] = sxp - sxm;
+    j[1] = syp - sym;
+    j[2] = szp - szm;
+}
+// ExternalForceDynamics::computeVelocity, src/basicDynamics/externalForceDynamics.hh:59-74
+template <class C>
+__device__ __forceinline__ void velocity_with_force(const C* f, const C* F, C* u) {
+    C rb, j[3];
+    rho_bar_j(f, rb, j);
+    const C inv = C(1) / (rb + C(1));
+    u[0] = j[0] * inv + F[0] / C(2);
+    u[1] = j[1] * inv + F[1] / C(2);
+    u[2] = j[2] * inv + F[2] / C(2);
+}
+
+// bgk_ma2_equilibrium, src/latticeBoltzmann/dynamicsTemplates3D.h:675-678
+template <class C>
+__device__ __forceinline__ C bgk_equilibrium(int i, C rhoBar, C invRho, const C* j, C jSqr) {
+    const C c_j = C(cx(i)) * j[0] + C(cy(i)) * j[1] + C(cz(i)) * j[2];
+    return weight<C>(i) * (rhoBar + C(3) * c_j + invRho * (C(4.5) * c_j * c_j - C(1.5) * jSqr));
+}
+
+// bgk_ma2_collision_base, src/latticeBoltzmann/dynamicsTemplates3D.h:770-838
+template <class C>
+__device__ __forceinline__ void bgk_collision(C* f, C rhoBar, const C* j, C omega, C invRho) {
+    const C omo = C(1) - omega;
+    const C t0w = weight<C>(0) * omega, t1w = weight<C>(1) * omega, t4w = weight<C>(4) * omega;
+    const C jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    const C kx = C(3) * j[0], ky = C(3) * j[1], kz = C(3) * j[2];
+    const C kxS = invRho / C(2) * kx * kx, kyS = invRho / C(2) * ky * ky, kzS = invRho / C(2) * kz * kz;
+    const C kxky = invRho * kx * ky, kxkz = invRho * kx * kz, kykz = invRho * ky * kz;
+    const C C1 = rhoBar + invRho * C(3) * jSqr;
+    C C2, C3;
+    C3 = -kxS - kyS - kzS;
+    f[0] = f[0] * omo + t0w * (C1 + C3);
+#define BIB_PAIR(a, b, tw)                      \
+    f[a] = f[a] * omo + tw * (C1 + C2 + C3); \
+    f[b] = f[b] * omo + tw * (C1 - C2 + C3);
+    C2 = -kx; C3 = -kyS - kzS; BIB_PAIR(1, 10, t1w)
+    C2 = -ky; C3 = -kxS - kzS; BIB_PAIR(2, 11, t1w)
+    C2 = -kz; C3 = -kxS - kyS; BIB_PAIR(3, 12, t1w)
+    C2 = -kx - ky; C3 = kxky - kzS; BIB_PAIR(4, 13, t4w)
+    C2 = -kx + ky; C3 = -kxky - kzS; BIB_PAIR(5, 14, t4w)
+    C2 = -kx - kz; C3 = kxkz - kyS; BIB_PAIR(6, 15, t4w)
+    C2 = -kx + kz; C3 = -kxkz - kyS; BIB_PAIR(7, 16, t4w)
+    C2 = -ky - kz; C3 = kykz - kxS; BIB_PAIR(8, 17, t4w)
+    C2 = -ky + kz; C3 = -kykz - kxS; BIB_PAIR(9, 18, t4w)
+#undef BIB_PAIR
+}
+
+// Guo forcing for D3Q19, src/fsi/VariableViscosityDynamics.hh:47-129
+template <class C>
+__device__ __forceinline__ void guo_force(C* f, const C* F, const C* u, C omega) {
+    const C mu = C(1) - omega / C(2);
+    const C o6 = C(1) / C(6), o12 = C(1) / C(12);
+    const C F0 = F[0], F1 = F[1], F2 = F[2], u0 = u[0], u1 = u[1], u2 = u[2];
+    f[0] += -mu * (F0 * u0 + F1 * u1 + F2 * u2);
+    f[1] += o6 * mu * (F0 * (C(-1) + 2 * u0) - F1 * u1 - F2 * u2);
+    f[2] += -o6 * mu * (F0 * u0 + F1 * (C(1) - 2 * u1) + F2 * u2);
+    f[3] += -o6 * mu * (F0 * u0 + F1 * u1 + F2 * (C(1) - 2 * u2));
+    f[4] += o12 * mu * (F0 * (C(-1) + 2 * u0 + 3 * u1) + F1 * (C(-1) + 2 * u1 + 3 * u0) - F2 * u2);
+    f[5] += o12 * mu * (F0 * (C(-1) + 2 * u0 - 3 * u1) + F1 * (C(1) + 2 * u1 - 3 * u0) - F2 * u2);
+    f[6] += o12 * mu * (F0 * (C(-1) + 2 * u0 + 3 * u2) - F1 * u1 + F2 * (C(-1) + 2 * u2 + 3 * u0));
+    f[7] += o12 * mu * (F0 * (C(-1) + 2 * u0 - 3 * u2) - F1 * u1 + F2 * (C(1) + 2 * u2 - 3 * u0));
+    f[8] += -o12 * mu * (F0 * u0 + F1 * (C(1) - 2 * u1 - 3 * u2) + F2 * (C(1) - 2 * u2 - 3 * u1));
+    f[9] += -o12 * mu * (F0 * u0 + F1 * (C(1) - 2 * u1 + 3 * u2) + F2 * (C(-1) - 2 * u2 + 3 * u1));
+    f[10] += o6 * mu * (F0 * (C(1) + 2 * u0) - F1 * u1 - F2 * u2);
+    f[11] += -o6 * mu * (F0 * u0 + F1 * (C(-1) - 2 * u1) + F2 * u2);
+    f[12] += -o6 * mu * (F0 * u0 + F1 * u1 + F2 * (C(-1) - 2 * u2));
+    f[13] += o12 * mu * (F0 * (C(1) + 2 * u0 + 3 * u1) + F1 * (C(1) + 2 * u1 + 3 * u0) - F2 * u2);
+    f[14] += o12 * mu * (F0 * (C(1) + 2 * u0 - 3 * u1) + F1 * (C(-1) + 2 * u1 - 3 * u0) - F2 * u2);
+    f[15] += o12 * mu * (F0 * (C(1) + 2 * u0 + 3 * u2) - F1 * u1 + F2 * (C(1) + 2 * u2 + 3 * u0));
+    f[16] += o12 * mu * (F0 * (C(1) + 2 * u0 - 3 * u2) - F1 * u1 + F2 * (C(-1) + 2 * u2 - 3 * u0));
+    f[17] += -o12 * mu * (F0 * u0 + F1 * (C(-1) - 2 * u1 - 3 * u2) + F2 * (C(-1) - 2 * u2 - 3 * u1));
+    f[18] += -o12 * mu * (F0 * u0 + F1 * (C(-1) - 2 * u1 + 3 * u2) + F2 * (C(1) - 2 * u2 + 3 * u1));
+}
+
+// Collision of one cell.  BGK_GUO_VOF follows GuoExternalForceVOFDynamics::collide
+// (src/fsi/VariableViscosityDynamics.hh:151-172); BGK follows BGKdynamics::collide
+// (src/basicDynamics/isoThermalDynamics.hh:329-340); TRT is Ginzburg's two-relaxation-
+// time split around the same equilibrium (no reference counterpart).
+template <class C, int COLL>
+__device__ __forceinline__ void collide(C* f, const C* F, C omega, C omega_minus) {
+    if (COLL == BIB_COLLISION_BGK_GUO_VOF) {
+        const C rhoBar = rho_bar_seq(f);
+        C u[3], j[3];
+        velocity_with_force(f, F, u);
+        const C rho = rhoBar + C(1);
+        j[0] = rho * u[0];
+        j[1] = rho * u[1];
+        j[2] = rho * u[2];
+        bgk_collision(f, rhoBar, j, omega, C(1) / (rhoBar + C(1)));
+        guo_force(f, F, u, omega);
+    } else if (COLL == BIB_COLLISION_BGK) {
+        C rb, j[3];
+        rho_bar_j(f, rb, j);
+        bgk_collision(f, rb, j, omega, C(1) / (rb + C(1)));
+    } else {
+        C rb, j[3];
+        rho_bar_j(f, rb, j);
+        const C invRho = C(1) / (rb + C(1));
+        const C jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+        f[0] = f[0] - omega * (f[0] - bgk_equilibrium<C>(0, rb, invRho, j, jSqr));
+#pragma unroll
+        for (int i = 1; i < 10; ++i) {
+            const C ei = bgk_equilibrium<C>(i, rb, invRho, j, jSqr);
+            const C eo = bgk_equilibrium<C>(i + 9, rb, invRho, j, jSqr);
+            const C fp = C(0.5) * (f[i] + f[i + 9]), fm = C(0.5) * (f[i] - f[i + 9]);
+            const C dp = omega * (fp - C(0.5) * (ei + eo));
+            const C dm = omega_minus * (fm - C(0.5) * (ei - eo));
+            f[i] = f[i] - dp - dm;
+            f[i + 9] = f[i + 9] - dp + dm;
+        }
+    }
+}
+
+__host__ __device__ inline int64_t wrap_index(int64_t i, int64_t n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
+
+}  // namespace bib

@@ -1,0 +1,194 @@
+/*
+ * bib.h -- C ABI of biblbm_gb300, the GB300 (sm_103a) implementation of the
+ * coupled immersed-boundary lattice-Boltzmann time step of niclasberg/biblbm.
+ *
+ * The entry points mirror the three extension points the reference exposes on
+ * this path, so that a Palabos / fsi driver (progs/ in the reference) can hand the
+ * step to the GPU:
+ *
+ *   1. Palabos' collide-and-stream offload interface CoProcessor3D<T>
+ *      (src/coProcessors/coProcessor3D.h:57-115): addDomain / send / receive /
+ *      collideAndStream  ->  bib_lattice_add_domain / _send / _receive /
+ *      _collide_and_stream.
+ *   2. The fsi data-processor functional ImmersedBoundaryWrapperFunctional3D
+ *      (src/fsi/DataProcessors.h:110-139, process() at DataProcessors.hh:94-108)
+ *      and the driver step order of progs/capsule_in_shear/capsule_in_shear.cpp:187-227
+ *      ->  bib_ibm_step / bib_step.
+ *   3. The particle model API: ParticleShapeLibrary::store_mesh
+ *      (src/fsi/ParticleShapeFactory.h:26), ImmersedBoundaryDynamics3D::add_particle /
+ *      get_particle / compute_total_volume (src/fsi/ImmersedBoundaryDynamics.h:63-113)
+ *      ->  bib_shape_store / bib_particle_add / bib_particle_get / bib_total_volume.
+ *
+ * Conventions
+ *  - Every call returns a bib_status: 0 on success, a negative code on failure.
+ *    The library never exits or traps (the reference calls exit(-1),
+ *    ImmersedBoundaryDynamics.hh:51-54).  bib_last_error() gives the message.
+ *  - The caller owns all host buffers; they are copied.  The library owns device
+ *    memory.  Handles are small non-negative integers, as CoProcessor3D::addDomain's.
+ *  - A context is not thread-safe: use it from one host thread.  Calls are ordered
+ *    on the context's CUDA stream; calls that return host data synchronise.
+ *  - Lattice fields exchanged with the host are FP64 structure-of-arrays with x
+ *    fastest: value(c, x, y, z) = a[c*n + x + nx*(y + ny*z)], n = nx*ny*nz.
+ *    Populations are f-bar = f - t_i (Palabos DefaultRoundOffPolicy,
+ *    src/latticeBoltzmann/roundOffPolicy.h:72-90) in the reference's D3Q19 order
+ *    (src/latticeBoltzmann/nearestNeighborLattices3D.hh:165-197), post-streaming,
+ *    i.e. the state Palabos holds between two time steps.
+ */
+#ifndef BIB_BIB_H
+#define BIB_BIB_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BIB_ABI_VERSION 1
+
+typedef int32_t bib_status;
+enum {
+    BIB_OK = 0,
+    BIB_EINVAL = -1,       /* bad argument, handle or size */
+    BIB_ENOMEM = -2,       /* device or host allocation failed */
+    BIB_ECUDA = -3,        /* a CUDA call failed */
+    BIB_ENAN = -4,         /* the state contains NaN / Inf */
+    BIB_ETIMEOUT = -5,     /* a bounded device wait gave up */
+    BIB_ESTATE = -6,       /* call not valid in the current state */
+    BIB_EUNSUPPORTED = -7  /* option combination not implemented */
+};
+
+/* population storage on the device */
+enum { BIB_STORAGE_F64 = 0, BIB_STORAGE_F32 = 1, BIB_STORAGE_F16 = 2 };
+/* collision operator */
+enum {
+    BIB_COLLISION_BGK_GUO_VOF = 0, /* GuoExternalForceVOFDynamics, src/fsi/VariableViscosityDynamics.hh:151-172 */
+    BIB_COLLISION_BGK = 1,         /* BGKdynamics, src/basicDynamics/isoThermalDynamics.hh:329-340 */
+    BIB_COLLISION_TRT = 2          /* two-relaxation-time (no reference counterpart) */
+};
+/* wall treatment on a non-periodic axis */
+enum {
+    BIB_WALL_NONE = 0,
+    BIB_WALL_FD_VELOCITY = 1, /* createInterpBoundaryCondition3D velocity walls (y only) */
+    BIB_WALL_HALFWAY_BB = 2   /* link-wise halfway bounce-back, optional moving wall */
+};
+enum { BIB_DIRAC_ROMA = 0, BIB_DIRAC_PESKIN = 1 };
+enum {
+    BIB_MODEL_CAPSULE_NEOHOOKEAN = 0, /* DeformableCapsuleParticle, src/fsi/DeformableCapsule.hh:60-150 */
+    BIB_MODEL_CAPSULE_SKALAK = 1,
+    BIB_MODEL_RBC_WLCPOW = 2,         /* RBCParticle, src/fsi/RBCParticle.hh:140-247 */
+    BIB_MODEL_SKALAK_BENDING = 3      /* Skalak law + the RBC area / volume / bending terms */
+};
+enum { BIB_SPREAD_ATOMIC = 0, BIB_SPREAD_DETERMINISTIC = 1 };
+enum { BIB_LAYOUT_SOA_F64 = 0, BIB_LAYOUT_PALABOS_F64 = 1 };
+
+/* membrane parameter vector, 12 doubles */
+enum {
+    BIB_P_G = 0, BIB_P_C, BIB_P_NU_S, BIB_P_KB,               /* CapsuleParameters, DeformableCapsule.h:22-31 */
+    BIB_P_SHEAR_MODULUS, BIB_P_L0, BIB_P_K_AREA_GLOBAL,       /* RBCParameters, RBCParticle.h:21-58 */
+    BIB_P_K_AREA_LOCAL, BIB_P_K_VOLUME, BIB_P_VOL_DESIRED, BIB_P_K_BEND, BIB_P_THETA0,
+    BIB_P_COUNT
+};
+
+typedef struct bib_ctx bib_ctx;
+
+typedef struct {
+    int32_t device; /* CUDA device ordinal */
+    int32_t flags;  /* reserved, 0 */
+} bib_config;
+
+typedef struct {
+    int32_t periodic[3];     /* per axis: 1 periodic, 0 walled */
+    int32_t collision;       /* BIB_COLLISION_* */
+    int32_t storage;         /* BIB_STORAGE_* */
+    int32_t wall_y, wall_z;  /* BIB_WALL_* for a non-periodic y / z axis */
+    int32_t use_phase;       /* 1: per-cell phase field enters omega (viscosity ratio != 1) */
+    int32_t reserved;
+    double omega;            /* outer-fluid relaxation frequency (omega1 of the VOF dynamics) */
+    double omega_inner;      /* inner-fluid relaxation frequency (omega2) */
+    double trt_magic;        /* TRT magic parameter Lambda */
+    double wall_u[4][3];     /* velocity of the y-, y+, z-, z+ walls */
+    double body_force[3];    /* constant body force added to the force field every step */
+    double f16_scale;        /* FP16 storage stores f-bar * scale; 0 selects the default 8192 */
+} bib_lattice_params;
+
+typedef struct {
+    int32_t dirac;        /* BIB_DIRAC_* */
+    int32_t spread_mode;  /* BIB_SPREAD_* */
+    double field_offset;  /* location of the velocity field of the reference's data processor: -1 */
+} bib_ib_params;
+
+/* ---- context (src/coProcessors/coProcessor3D.h:57-115 lifetime) ---- */
+bib_status bib_create(const bib_config* cfg, bib_ctx** out);
+void bib_destroy(bib_ctx* ctx);
+bib_status bib_sync(bib_ctx* ctx);
+size_t bib_last_error(const bib_ctx* ctx, char* buf, size_t len);
+const char* bib_status_string(bib_status s);
+int32_t bib_abi_version(void);
+
+/* ---- lattice: CoProcessor3D::addDomain / send / receive / collideAndStream ---- */
+/* CoProcessor3D::addDomain(nx, ny, nz, omega, handle), coProcessor3D.h:69-74 */
+bib_status bib_lattice_add_domain(bib_ctx* ctx, int64_t nx, int64_t ny, int64_t nz, const bib_lattice_params* p,
+                                  int32_t* handle);
+/* CoProcessor3D::send, coProcessor3D.h:75-84: whole-domain populations from the host.
+ * layout BIB_LAYOUT_SOA_F64: 19*n doubles; BIB_LAYOUT_PALABOS_F64: Palabos static-cell
+ * wire order (x-major, z fastest; 19 f-bar + 4 externals per cell, blockLattice3D.hh:671-689). */
+bib_status bib_lattice_send(bib_ctx* ctx, int32_t h, const void* buf, size_t bytes, int32_t layout);
+/* CoProcessor3D::receive, coProcessor3D.h:85-93 */
+bib_status bib_lattice_receive(bib_ctx* ctx, int32_t h, void* buf, size_t bytes, int32_t layout);
+/* CoProcessor3D::collideAndStream, coProcessor3D.h:94-97 (plus the wall processors) */
+bib_status bib_lattice_collide_and_stream(bib_ctx* ctx, int32_t h, int64_t nsteps);
+/* initializeAtEquilibrium (core/cell.hh:124-132) from rho (n, may be NULL = 1) and u (3n),
+ * then the wall processors once (MultiBlock3D::initialize) */
+bib_status bib_lattice_init_equilibrium(bib_ctx* ctx, int32_t h, const double* rho, const double* u);
+/* external force scalars (3n): setExternalVector / read back */
+bib_status bib_lattice_set_force(bib_ctx* ctx, int32_t h, const double* F);
+bib_status bib_lattice_get_force(bib_ctx* ctx, int32_t h, double* F);
+/* phase scalar (n, values 0..1), used when use_phase = 1 */
+bib_status bib_lattice_set_phase(bib_ctx* ctx, int32_t h, const double* phase);
+/* computeVelocity (dataAnalysisWrapper3D.hh:1660): u = j/rho + F/2, wall nodes give the wall velocity */
+bib_status bib_lattice_get_velocity(bib_ctx* ctx, int32_t h, double* u);
+bib_status bib_lattice_cells(bib_ctx* ctx, int32_t h, int64_t* n);
+
+/* ---- shapes: ParticleShapeLibrary::store_mesh, ParticleShapeFactory.hh:120-137 ---- */
+bib_status bib_shape_store(bib_ctx* ctx, const double* xyz, const int64_t* tri, int64_t nv, int64_t nt, int32_t* shape);
+/* out[6] = {area, volume, n_links, n_pairs, n_vertices, n_triangles} */
+bib_status bib_shape_info(bib_ctx* ctx, int32_t shape, double* out);
+
+/* ---- immersed boundary: ImmersedBoundaryDynamics3D ---- */
+bib_status bib_ib_configure(bib_ctx* ctx, int32_t h, const bib_ib_params* p);
+/* add_particle (ImmersedBoundaryDynamics.hh:500-525): xyz NULL = the rest shape */
+bib_status bib_particle_add(bib_ctx* ctx, int32_t h, int32_t shape, int32_t model, const double* params,
+                            const double* xyz, int32_t* pid);
+bib_status bib_particle_count(bib_ctx* ctx, int32_t h, int32_t* n);
+bib_status bib_particle_get(bib_ctx* ctx, int32_t h, int32_t pid, double* pos, double* vel, double* force);
+bib_status bib_particle_set_positions(bib_ctx* ctx, int32_t h, int32_t pid, const double* pos);
+/* out[14] = {area, volume, com[3], moment of inertia[9]} (DeformableParticle3D.hh:54-82, 173-272) */
+bib_status bib_particle_stats(bib_ctx* ctx, int32_t h, int32_t pid, double* out);
+/* all vertex positions (3 * total vertices) and per-particle {area, volume, com[3]} (5 per particle) */
+bib_status bib_particles_download(bib_ctx* ctx, int32_t h, double* pos, double* stats);
+bib_status bib_total_vertices(bib_ctx* ctx, int32_t h, int64_t* n);
+/* compute_total_volume, ImmersedBoundaryDynamics.hh:559-568 */
+bib_status bib_total_volume(bib_ctx* ctx, int32_t h, double* v);
+/* One IB step on the current lattice state: velocity at the vertices, forces, spreading
+ * into a force field reset to the body force, vertex motion (DataProcessors.hh:104-107). */
+bib_status bib_ibm_step(bib_ctx* ctx, int32_t h);
+
+/* ---- coupled step: computeVelocity -> setExternalVector -> IB step -> collideAndStream ---- */
+bib_status bib_step(bib_ctx* ctx, int32_t h, int64_t nsteps);
+/* bib_step bracketed by CUDA events on the context's stream; *ms = device time, synchronises */
+bib_status bib_step_timed(bib_ctx* ctx, int32_t h, int64_t nsteps, double* ms);
+/* stream the context's work into CUDA-graph replays (1) or plain launches (0) */
+bib_status bib_set_graph_mode(bib_ctx* ctx, int32_t enabled);
+/* scan populations and vertex positions for NaN / Inf: BIB_OK or BIB_ENAN */
+bib_status bib_check_health(bib_ctx* ctx, int32_t h);
+
+/* ---- timing: per-kernel-group device time (ms) of the last bib_step call when profiling is on ---- */
+bib_status bib_set_profiling(bib_ctx* ctx, int32_t enabled);
+/* out[5] = {interpolate, forces+move, spread, collide+stream, walls}; cumulative since enabled */
+bib_status bib_profile_read(bib_ctx* ctx, double* out, int32_t n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -10,6 +10,9 @@
 
 #include <float.h>
 #include <math.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
 #include <stdlib.h>
 #include <string.h>
 
@@ -282,6 +285,9 @@ void orc_collide_stream(const orc_lattice* L, double* f, double* ftmp, const dou
     init_weights();
     const int64_t nx = L->nx, ny = L->ny, nz = L->nz, n = nx * ny * nz;
     memcpy(ftmp, f, sizeof(double) * Q * n);
+    /* cells are independent and every (population, destination) pair is written once:
+     * the z slabs run in parallel without changing any result */
+#pragma omp parallel for schedule(static) if (n > 262144)
     for (int64_t z = 0; z < nz; ++z)
         for (int64_t y = 0; y < ny; ++y)
             for (int64_t x = 0; x < nx; ++x) {
@@ -341,6 +347,7 @@ void orc_collide_stream(const orc_lattice* L, double* f, double* ftmp, const dou
 void orc_compute_velocity(const orc_lattice* L, const double* f, const double* F, double* u) {
     init_weights();
     const int64_t nx = L->nx, ny = L->ny, nz = L->nz, n = nx * ny * nz;
+#pragma omp parallel for schedule(static) if (n > 262144)
     for (int64_t z = 0; z < nz; ++z)
         for (int64_t y = 0; y < ny; ++y)
             for (int64_t x = 0; x < nx; ++x) {
@@ -936,6 +943,14 @@ void orc_spread(const orc_lattice* L, int32_t dirac, double offset, int64_t n, c
     }
 }
 
+int32_t orc_threads(void) {
+#ifdef _OPENMP
+    return (int32_t)omp_get_max_threads();
+#else
+    return 1;
+#endif
+}
+
 /* ------------------------------------------------------------------ coupled system */
 typedef struct {
     int64_t nv, nt, nl, np;
@@ -1088,8 +1103,12 @@ static void sys_step(orc_sys* s) {
     const orc_lattice* L = &s->L;
     const int64_t n = L->nx * L->ny * L->nz;
     orc_compute_velocity(L, s->f, s->F, s->u);
-    for (int d = 0; d < 3; ++d)
-        for (int64_t k = 0; k < n; ++k) s->F[d * n + k] = s->body[d];
+    for (int d = 0; d < 3; ++d) {
+        const double b = s->body[d];
+        double* Fd = s->F + d * n;
+#pragma omp parallel for schedule(static) if (n > 262144)
+        for (int64_t k = 0; k < n; ++k) Fd[k] = b;
+    }
     if (s->nparts > 0) {
         double* pos;
         int64_t nvt;

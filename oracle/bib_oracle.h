@@ -79,6 +79,9 @@ void orc_interpolate(const orc_lattice* L, int32_t dirac, double offset, const d
 void orc_spread(const orc_lattice* L, int32_t dirac, double offset, int64_t n, const double* pos,
                 const double* force, const int32_t* cls, double* F);
 
+/* number of OpenMP threads the lattice loops use (1 without OpenMP) */
+int32_t orc_threads(void);
+
 /* ---- coupled system (mirrors the product's C ABI) ---- */
 typedef struct orc_sys orc_sys;
 orc_sys* orc_sys_create(const orc_lattice* L, int32_t dirac, double ib_offset);

@@ -62,6 +62,7 @@ def lib():
             "orc_membrane_forces": (None, [C.c_int32, dp, C.c_int64, dp, C.c_int64, ip, dp, C.c_double, C.c_int64, ip,
                                            dp, C.c_int64, ip, dp, dp, C.c_double, C.c_double, dp]),
             "orc_dirac": (C.c_double, [C.c_int32, C.c_double]),
+            "orc_threads": (C.c_int32, []),
             "orc_classify": (None, [Lp, C.c_int32, C.c_int64, dp, i32p]),
             "orc_interpolate": (None, [Lp, C.c_int32, C.c_double, dp, C.c_int64, dp, i32p, dp]),
             "orc_spread": (None, [Lp, C.c_int32, C.c_double, C.c_int64, dp, dp, i32p, dp]),
@@ -131,6 +132,10 @@ def params_vector(**kw) -> np.ndarray:
              k_volume=0.0, vol_desired=1.0, k_bend=0.0, theta0=0.0)
     p.update(kw)
     return np.array([p[k] for k in PARAM_KEYS], dtype=np.float64)
+
+
+def threads() -> int:
+    return int(lib().orc_threads())
 
 
 # ------------------------------------------------------------------ lattice ops

@@ -1,0 +1,251 @@
+"""CUDA path (through the C ABI) against the reference fixtures and the CPU oracle.
+
+Tolerances: the FP64 path is compared with the reference / oracle to 1e-13 absolute on
+populations (|f-bar| <= ~1e-2) and 1e-12 relative on vertex data.  It is not bit-exact:
+nvcc contracts multiply-adds into FMAs, and spreading uses atomics whose summation order
+varies from run to run.
+"""
+import numpy as np
+import pytest
+
+from oracle import oracle as O
+from tests.conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+bib = pytest.importorskip("biblbm_gb300")
+from biblbm_gb300 import meshes  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def ctx():
+    c = bib.Context(0)
+    yield c
+    c.close()
+
+
+def rel(a, b):
+    return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
+
+
+def shear_state(L, U):
+    nx, ny, nz = L.nx, L.ny, L.nz
+    y = np.arange(ny)
+    u = np.zeros((3, nz, ny, nx))
+    u[0] = (U * (2.0 * y / (ny - 1) - 1))[None, :, None]
+    return u
+
+
+# ---------------------------------------------------------------- lattice
+def test_periodic_collide_stream_matches_oracle(ctx):
+    d = golden("lbm_periodic")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    om = d["in_omega"]
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=om[0], omega_inner=om[1], use_phase=True)
+    lat.send(d["in_fbar"])
+    lat.set_external_force(d["in_force"])
+    lat.set_phase(d["in_phase"])
+    assert np.abs(lat.compute_velocity() - d["out_u_0"]).max() < 1e-15
+    lat.collide_and_stream(1)
+    f1 = lat.receive()
+    L = O.lattice((nx, ny, nz), (1, 1, 1), "bgk_guo_vof", om[0], om[1])
+    ref1 = O.collide_stream(L, d["in_fbar"], d["in_force"], d["in_phase"], 1)
+    assert np.abs(f1 - ref1).max() < 1e-15
+    # populations that did not cross a periodic face equal the reference's own output
+    assert np.abs(f1[0] - d["out_fbar_1"][0]).max() < 1e-15
+    lat.collide_and_stream(2)
+    ref3 = O.collide_stream(L, d["in_fbar"], d["in_force"], d["in_phase"], 3)
+    assert np.abs(lat.receive() - ref3).max() < 1e-14
+
+
+def test_shear_walls_match_reference(ctx):
+    d = golden("lbm_shear")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    om = d["in_omega"]
+    U = float(d["in_U"])
+    wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 1), omega=om[0], wall_y="fd_velocity", wall_u=wall_u)
+    L = O.lattice((nx, ny, nz), (1, 0, 1), "bgk_guo_vof", om[0], om[1], wall_y="fd_velocity", wall_u=wall_u)
+    lat.initialize_at_equilibrium(None, shear_state(L, U))
+    assert np.abs(lat.receive() - d["out_fbar_0"]).max() < 1e-16
+    lat.set_external_force(d["in_force"])
+    lat.collide_and_stream(1)
+    assert np.abs(lat.receive() - d["out_fbar_1"]).max() < 1e-15
+    assert np.abs(lat.compute_velocity() - d["out_u_1"]).max() < 1e-15
+    lat.collide_and_stream(int(d["in_steps"]) - 1)
+    assert np.abs(lat.receive() - d["out_fbar_end"]).max() < 1e-15
+    assert np.abs(lat.compute_velocity() - d["out_u_end"]).max() < 1e-15
+
+
+def test_palabos_layout_round_trip(ctx):
+    d = golden("lbm_periodic")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=1.2)
+    wire = np.zeros((nx, ny, nz, 23))
+    wire[..., :19] = np.transpose(d["in_fbar"], (3, 2, 1, 0))
+    wire[..., 19:22] = np.transpose(d["in_force"], (3, 2, 1, 0))
+    lat.send(wire, layout="palabos")
+    assert np.array_equal(lat.receive(), d["in_fbar"])
+    assert np.array_equal(lat.get_external_force(), d["in_force"])
+    back = lat.receive(layout="palabos")
+    assert np.array_equal(back[..., :22], wire[..., :22])
+
+
+# ---------------------------------------------------------------- membranes
+@pytest.mark.parametrize("model", ["capsule_neohookean", "capsule_skalak", "rbc_wlcpow", "skalak_bending"])
+def test_membrane_forces_match_reference(ctx, model):
+    d = golden("forces_" + model)
+    n = 40
+    lat = ctx.add_domain(n, n, n, periodic=(1, 1, 1), omega=1.0)
+    shapes = bib.ParticleShapeLibrary(ctx)
+    sid = shapes.store_mesh(d["in_rest"], d["in_tri"], "m")
+    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes)
+    pos = d["in_pos"] + np.array([15.0, 18.0, 12.0])  # inside the box, away from the faces
+    pid = fsi.add_particle(sid, model, d["in_params"], pos)
+    p0 = fsi.get_particle(pid)
+    assert abs(p0["area"] - d["out_area"][0]) < 1e-12 * d["out_area"][0]
+    assert abs(p0["volume"] - d["out_volume"][0]) < 1e-10 * d["out_volume"][0]
+    fsi.ibm_step()  # forces are evaluated at the current positions, before the move
+    p = fsi.get_particle(pid)
+    assert rel(p["force"], d["out_force"]) < 1e-11
+
+
+# ---------------------------------------------------------------- coupled steps
+def run_coupled_gpu(ctx, d, storage="f64", graph=True):
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    om = 1.0 / float(d["in_tau"])
+    walls = int(d["in_walls"])
+    body = d["in_body"] if "in_body" in d.files else np.zeros(3)
+    if walls == 1:
+        U = float(d["in_U"])
+        wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
+        lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 1), omega=om, wall_y="fd_velocity", wall_u=wall_u,
+                             storage=storage, body_force=body)
+        L = O.lattice((nx, ny, nz), (1, 0, 1), "bgk_guo_vof", om, om, wall_y="fd_velocity", wall_u=wall_u)
+        lat.initialize_at_equilibrium(None, shear_state(L, U))
+    else:
+        lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=om, storage=storage, body_force=body)
+        lat.initialize_at_equilibrium(None, np.zeros((3, nz, ny, nx)))
+    shapes = bib.ParticleShapeLibrary(ctx)
+    sid = shapes.store_mesh(d["in_rest"], d["in_tri"], "p")
+    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes)
+    model = {0: "capsule_neohookean", 1: "capsule_skalak", 2: "rbc_wlcpow", 3: "skalak_bending"}[int(d["in_model"])]
+    pid = fsi.add_particle(sid, model, d["in_params"], d["in_pos"])
+    ctx.set_graph_mode(graph)
+    return lat, fsi, pid
+
+
+@pytest.mark.parametrize("name", ["ibm_capsule_shear", "ibm_rbc_periodic"])
+def test_coupled_steps_match_reference(ctx, name):
+    d = golden(name)
+    lat, fsi, pid = run_coupled_gpu(ctx, d, graph=False)
+    steps = int(d["in_steps"])
+    fscale = np.abs(d["out_force"]).max()  # the first steps start stress-free (forces ~1e-17)
+    for it in range(steps):
+        p = fsi.get_particle(pid)
+        assert rel(p["pos"], d["out_pos"][it]) < 1e-13
+        fsi.step(1)
+        p = fsi.get_particle(pid)
+        assert rel(p["vel"], d["out_vel"][it]) < 1e-11, it
+        assert np.abs(p["force"] - d["out_force"][it]).max() < 1e-10 * fscale, it
+        assert abs(p["volume"] - d["out_volume"][it + 1]) < 1e-11 * d["out_volume"][it + 1]
+        if it == 0:
+            assert np.abs(lat.get_external_force() - d["out_force_spread"]).max() < 1e-15
+    assert np.abs(lat.compute_velocity() - d["out_u_end"]).max() < 1e-14
+    assert rel(fsi.get_particle(pid)["inertia"], d["out_inertia"][-1]) < 1e-12
+
+
+def test_graph_replay_equals_plain_launches(ctx):
+    d = golden("ibm_capsule_shear")
+    lat_a, fsi_a, pa = run_coupled_gpu(ctx, d, graph=False)
+    fsi_a.step(6)
+    lat_b, fsi_b, pb = run_coupled_gpu(ctx, d, graph=True)
+    fsi_b.step(6)
+    ctx.set_graph_mode(True)
+    assert rel(fsi_b.get_particle(pb)["pos"], fsi_a.get_particle(pa)["pos"]) < 1e-14
+    assert np.abs(lat_b.receive() - lat_a.receive()).max() < 1e-15
+
+
+def oracle_capsule_system(n, U, xyz, tri, pos, prm, dirac="roma", steps=0):
+    om = 1.0
+    wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
+    L = O.lattice((n, n, n), (1, 0, 1), "bgk_guo_vof", om, om, wall_y="fd_velocity", wall_u=wall_u)
+    S = O.System(L, dirac, -1.0)
+    S.f[...] = O.apply_fd_walls(L, O.init_equilibrium(L, None, shear_state(L, U)), np.zeros((3, n, n, n)))
+    pid = S.add_particle(S.add_shape(xyz, tri), "capsule_skalak", prm, pos)
+    S.step(steps)
+    return S, pid
+
+
+@pytest.mark.parametrize("dirac", ["roma", "peskin"])
+def test_capsule_in_shear_against_oracle(ctx, dirac):
+    n, U = 20, 0.03
+    xyz, tri = meshes.icosphere(2, 4.0)
+    pos = meshes.place(xyz, None, (9.4, 9.2, 9.6))
+    prm = bib.membrane_params(G=0.002, C=1.0)
+    S, opid = oracle_capsule_system(n, U, xyz, tri, pos, prm, dirac, steps=20)
+    wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
+    lat = ctx.add_domain(n, n, n, periodic=(1, 0, 1), omega=1.0, wall_y="fd_velocity", wall_u=wall_u)
+    lat.initialize_at_equilibrium(None, shear_state(S.L, U))
+    shapes = bib.ParticleShapeLibrary(ctx)
+    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes, dirac=dirac)
+    pid = fsi.add_particle(shapes.store_mesh(xyz, tri, "c"), "capsule_skalak", prm, pos)
+    fsi.step(20)
+    g, r = fsi.get_particle(pid), S.particle(opid)
+    assert rel(g["pos"], r["pos"]) < 1e-13
+    assert rel(g["force"], r["force"]) < 1e-8
+    assert np.abs(lat.receive() - S.f).max() < 1e-13
+
+
+# ---------------------------------------------------------------- reduced precision
+@pytest.mark.parametrize("storage,tol_pos,tol_u", [("f32", 2e-5, 2e-4), ("f16", 2e-3, 2e-2)])
+def test_reduced_precision_capsule(ctx, storage, tol_pos, tol_u):
+    """FP32 / FP16 deviation storage against the FP64 oracle on the same inputs.
+
+    Bounds: vertex displacement error relative to the displacement itself, and the
+    velocity field relative L2 error, after 40 steps.
+    """
+    n, U = 20, 0.03
+    xyz, tri = meshes.icosphere(2, 4.0)
+    pos = meshes.place(xyz, None, (9.4, 9.2, 9.6))
+    prm = bib.membrane_params(G=0.002, C=1.0)
+    S, opid = oracle_capsule_system(n, U, xyz, tri, pos, prm, steps=40)
+    wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
+    lat = ctx.add_domain(n, n, n, periodic=(1, 0, 1), omega=1.0, wall_y="fd_velocity", wall_u=wall_u, storage=storage)
+    lat.initialize_at_equilibrium(None, shear_state(S.L, U))
+    shapes = bib.ParticleShapeLibrary(ctx)
+    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes)
+    pid = fsi.add_particle(shapes.store_mesh(xyz, tri, "c"), "capsule_skalak", prm, pos)
+    fsi.step(40)
+    g, r = fsi.get_particle(pid), S.particle(opid)
+    disp = np.abs(r["pos"] - pos).max()
+    assert np.abs(g["pos"] - r["pos"]).max() < tol_pos * max(disp, 1e-3) + 1e-6
+    u_ref = S.velocity()
+    err = np.linalg.norm(lat.compute_velocity() - u_ref) / np.linalg.norm(u_ref)
+    assert err < tol_u
+    assert abs(g["volume"] - r["volume"]) / r["volume"] < 1e-4
+
+
+# ---------------------------------------------------------------- errors
+def test_invalid_arguments_are_reported(ctx):
+    with pytest.raises(bib.BibError) as e:
+        ctx.add_domain(2, 8, 8, periodic=(1, 1, 1), omega=1.0)
+    assert e.value.status == -1
+    with pytest.raises(bib.BibError):
+        ctx.add_domain(8, 8, 8, periodic=(1, 1, 1), omega=2.5)
+    lat = ctx.add_domain(8, 8, 8, periodic=(1, 1, 1), omega=1.0)
+    with pytest.raises(bib.BibError):
+        lat.send(np.zeros(10))
+    shapes = bib.ParticleShapeLibrary(ctx)
+    with pytest.raises(bib.BibError):
+        shapes.store_mesh(np.zeros((4, 3)), np.array([[0, 1, 9], [0, 1, 2], [1, 2, 3], [0, 2, 3]]), "bad")
+
+
+def test_nan_is_detected(ctx):
+    lat = ctx.add_domain(8, 8, 8, periodic=(1, 1, 1), omega=1.0)
+    f = np.zeros((19, 8, 8, 8))
+    f[3, 2, 2, 2] = np.nan
+    lat.send(f)
+    with pytest.raises(bib.BibError) as e:
+        lat.check_health()
+    assert e.value.status == -4
