@@ -30,7 +30,9 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MLUPS (coupled IB-LBM step) + membrane vertex-updates/s, FP16/FP32 storage vs FP64, 1 GB300"
-BYTES_PER_LU = {"f64": 19 * 8 * 2 + 3 * 8, "f32": 19 * 4 * 2 + 3 * 4, "f16": 19 * 2 * 2 + 3 * 4}
+# algorithmic bytes per lattice update of the coupled collide-and-stream kernel: populations
+# read + written, spread force read, previous force read + reset, velocity field written
+BYTES_PER_LU = {"f64": 19 * 8 * 2 + 4 * 3 * 8, "f32": 19 * 4 * 2 + 4 * 3 * 4, "f16": 19 * 2 * 2 + 4 * 3 * 4}
 
 
 def env_rank():
@@ -170,6 +172,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--ncu", action="store_true",
+                    help="profiling run: build the instance, run --warmup plain (non-graph) steps, print nothing")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
 
@@ -207,6 +211,15 @@ def main():
     cells = nx * ny * nz
     nvt = int(wl["positions"].shape[0] * wl["positions"].shape[1])
     K, W = args.steps, args.warmup
+
+    if args.ncu:
+        ctx = bib.Context(local)
+        lat, fsi = build_instance(bib, ctx, wl, args.storage)
+        ctx.set_graph_mode(False)
+        fsi.step(W)
+        ctx.sync()
+        ctx.close()
+        return
 
     # ---------------- timed region: K coupled steps, graph replays, device events
     ctx = bib.Context(0 if world == 1 else local)
@@ -266,6 +279,8 @@ def main():
             pos_v, stats_v, _ = taylor_and_volume(bib, f2, wl)
             variants[st]["_u"] = l2.compute_velocity()
             variants[st]["_stats"] = stats_v
+            I = bib.api.moments_of_inertia(pos_v, wl["tri"])
+            variants[st]["_D"] = np.array([bib.taylor_deformation(Ik) for Ik in I])
             c2.close()
         ref_u, ref_stats = variants["f64"]["_u"], variants["f64"]["_stats"]
         for st in ["f32", "f16"]:
@@ -273,10 +288,15 @@ def main():
             variants[st]["velocity_rel_l2_vs_f64"] = float(np.linalg.norm(u - ref_u) / np.linalg.norm(ref_u))
             variants[st]["volume_rel_diff_vs_f64_max"] = float(
                 np.abs(variants[st]["_stats"][:, 1] - ref_stats[:, 1]).max() / V0)
+            dD = np.abs(variants[st]["_D"] - variants["f64"]["_D"])
+            variants[st]["taylor_D_abs_diff_vs_f64"] = {"max": float(dD.max()), "mean": float(dD.mean())}
         for st in variants:
             variants[st]["volume_drift_max"] = float(np.abs(variants[st]["_stats"][:, 1] - V0).max() / V0)
+            variants[st]["taylor_D_mean"] = float(variants[st]["_D"].mean())
             variants[st].pop("_u")
             variants[st].pop("_stats")
+            variants[st].pop("_D")
+        variants["steps_compared"] = steps_main
         variants["f64"]["speedup_f16_over_f64"] = variants["f16"]["mlups"] / variants["f64"]["mlups"]
 
     # ---------------- end to end through the C ABI with host buffers

@@ -23,7 +23,8 @@ COLLISION = {"bgk_guo_vof": 0, "bgk": 1, "trt": 2}
 WALL = {"none": 0, "fd_velocity": 1, "halfway_bb": 2}
 DIRAC = {"roma": 0, "peskin": 1}
 MODEL = {"capsule_neohookean": 0, "capsule_skalak": 1, "rbc_wlcpow": 2, "skalak_bending": 3}
-LAYOUT = {"soa": 0, "palabos": 1}
+LAYOUT = {"soa": 0, "palabos": 1, "coprocessor": 2}
+SPREAD = {"atomic": 0, "deterministic": 1}
 PARAM_KEYS = ["G", "C", "nu_s", "kb", "shear_modulus", "L0", "k_area_global", "k_area_local",
               "k_volume", "vol_desired", "k_bend", "theta0"]
 Q = 19
@@ -114,7 +115,7 @@ class Context:
     def profile(self):
         out = np.zeros(5)
         self.check(self.lib.bib_profile_read(self.h, _d(out), 5))
-        return dict(zip(["interpolate", "membrane", "spread", "collide_stream", "walls"], out))
+        return dict(zip(["membrane", "spread", "collide_stream", "walls", "interpolate_update"], out))
 
     def add_domain(self, nx, ny, nz, **kw) -> "Lattice":
         return Lattice(self, nx, ny, nz, **kw)
@@ -164,7 +165,10 @@ class Lattice:
         self.ctx.check(self.ctx.lib.bib_lattice_send(self.ctx.h, self.h, f.ctypes.data, f.nbytes, LAYOUT[layout]))
 
     def receive(self, layout="soa"):
-        out = np.empty((Q,) + self.shape) if layout == "soa" else np.empty((self.nx, self.ny, self.nz, 23))
+        if layout == "soa":
+            out = np.empty((Q,) + self.shape)
+        else:
+            out = np.empty((self.nx, self.ny, self.nz, 23 if layout == "palabos" else Q))
         self.ctx.check(self.ctx.lib.bib_lattice_receive(self.ctx.h, self.h, out.ctypes.data, out.nbytes, LAYOUT[layout]))
         return out
 
@@ -230,9 +234,10 @@ class ParticleShapeLibrary:
 class ImmersedBoundaryDynamics3D:
     """The IB module of src/fsi/ImmersedBoundaryDynamics.h:50-217 on one lattice."""
 
-    def __init__(self, lattice: Lattice, shapes: ParticleShapeLibrary, dirac="roma", field_offset=-1.0):
+    def __init__(self, lattice: Lattice, shapes: ParticleShapeLibrary, dirac="roma", field_offset=-1.0,
+                 spread="atomic"):
         self.lattice, self.shapes, self.ctx = lattice, shapes, lattice.ctx
-        p = IbParams(DIRAC[dirac], 0, float(field_offset))
+        p = IbParams(DIRAC[dirac], SPREAD[spread], float(field_offset))
         self.ctx.check(self.ctx.lib.bib_ib_configure(self.ctx.h, lattice.h, C.byref(p)))
         self.nv: list[int] = []
 
@@ -288,6 +293,48 @@ class ImmersedBoundaryDynamics3D:
         ms = C.c_double()
         self.ctx.check(self.ctx.lib.bib_step_timed(self.ctx.h, self.lattice.h, int(nsteps), C.byref(ms)))
         return ms.value
+
+
+def moments_of_inertia(pos, tri) -> np.ndarray:
+    """Moment-of-inertia tensors of closed meshes, vectorised over particles.
+
+    ``pos`` is (n_particles, n_vertices, 3), ``tri`` (n_triangles, 3); the integrals are
+    those of DeformableParticle3D::compute_moment_of_intertia (DeformableParticle3D.hh:173-272).
+    Host-side post-processing of downloaded vertex positions.
+    """
+    pos = np.asarray(pos, dtype=np.float64)
+    tri = np.asarray(tri)
+    v0, v1, v2 = pos[:, tri[:, 0]], pos[:, tri[:, 1]], pos[:, tri[:, 2]]
+    N = np.cross(v1 - v0, v2 - v0)
+    tmp0 = v0 + v1
+    f1 = tmp0 + v2
+    tmp1 = v0 * v0
+    tmp2 = tmp1 + v1 * tmp0
+    f2 = tmp2 + v2 * f1
+    f3 = v0 * tmp1 + v1 * tmp2 + v2 * f2
+    g0 = f2 + v0 * (f1 + v0)
+    g1 = f2 + v1 * (f1 + v1)
+    g2 = f2 + v2 * (f1 + v2)
+    i0 = (N[..., 0] * f1[..., 0]).sum(-1) / 6.0
+    i1 = (N[..., 0] * f2[..., 0]).sum(-1) / 24.0
+    i2 = (N[..., 1] * f2[..., 1]).sum(-1) / 24.0
+    i3 = (N[..., 2] * f2[..., 2]).sum(-1) / 24.0
+    i4 = (N[..., 0] * f3[..., 0]).sum(-1) / 60.0
+    i5 = (N[..., 1] * f3[..., 1]).sum(-1) / 60.0
+    i6 = (N[..., 2] * f3[..., 2]).sum(-1) / 60.0
+    i7 = (N[..., 0] * (v0[..., 1] * g0[..., 0] + v1[..., 1] * g1[..., 0] + v2[..., 1] * g2[..., 0])).sum(-1) / 120.0
+    i8 = (N[..., 1] * (v0[..., 2] * g0[..., 1] + v1[..., 2] * g1[..., 1] + v2[..., 2] * g2[..., 1])).sum(-1) / 120.0
+    i9 = (N[..., 2] * (v0[..., 0] * g0[..., 2] + v1[..., 0] * g1[..., 2] + v2[..., 0] * g2[..., 2])).sum(-1) / 120.0
+    vol = i0
+    c = np.stack([i1 / vol, i2 / vol, i3 / vol], -1)
+    I = np.empty(pos.shape[:1] + (3, 3))
+    I[:, 0, 0] = i5 + i6 - vol * (c[:, 1] ** 2 + c[:, 2] ** 2)
+    I[:, 0, 1] = I[:, 1, 0] = -i7 + vol * c[:, 0] * c[:, 1]
+    I[:, 0, 2] = I[:, 2, 0] = -i9 + vol * c[:, 2] * c[:, 0]
+    I[:, 1, 1] = i4 + i6 - vol * (c[:, 2] ** 2 + c[:, 0] ** 2)
+    I[:, 1, 2] = I[:, 2, 1] = -i8 + vol * c[:, 1] * c[:, 2]
+    I[:, 2, 2] = i4 + i5 - vol * (c[:, 0] ** 2 + c[:, 1] ** 2)
+    return I
 
 
 def taylor_deformation(inertia) -> float:

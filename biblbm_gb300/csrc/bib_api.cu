@@ -29,7 +29,7 @@ struct bib_ctx {
     std::vector<std::unique_ptr<ShapeHost>> shapes;
     bool graph_mode = true;
     bool profiling = false;
-    double prof[5] = {0, 0, 0, 0, 0};
+    double prof[5] = {0, 0, 0, 0, 0};  // membrane, spread, collide+stream, walls, interpolate+update
     cudaEvent_t ev[6] = {};
     int* d_flag = nullptr;
     std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, parity) -> two-step graph
@@ -152,6 +152,22 @@ bool build_shape(ShapeHost& S, const double* xyz, const int64_t* tri, int64_t nv
         S.pair_cs.push_back(dt(n1, n2));
         S.pair_cs.push_back((dt(sub(n1, n2), sub(p1, p3)) > 0 ? 1.0 : -1.0) * nrm(crs(n1, n2)));
     }
+    // per-vertex incidence lists for the deterministic force gather: links, then triangles,
+    // then pairs, each in element order (the order of the reference's element loops)
+    std::vector<std::vector<int>> incv(nv);
+    const int nl = (int)S.link_len.size(), np = (int)S.pair_cs.size() / 2;
+    for (int l = 0; l < nl; ++l)
+        for (int k = 0; k < 2; ++k) incv[S.links[2 * l + k]].push_back((0 << 29) | l);
+    for (int t = 0; t < (int)nt; ++t)
+        for (int k = 0; k < 3; ++k) incv[S.tri[3 * t + k]].push_back((1 << 29) | t);
+    for (int q = 0; q < np; ++q)
+        for (int k = 0; k < 4; ++k) incv[S.pairs[4 * q + k]].push_back((2 << 29) | q);
+    S.inc_off.assign(1, 0);
+    S.inc.clear();
+    for (int64_t v = 0; v < nv; ++v) {
+        S.inc.insert(S.inc.end(), incv[v].begin(), incv[v].end());
+        S.inc_off.push_back((int)S.inc.size());
+    }
     return true;
 }
 
@@ -262,8 +278,18 @@ void free_particles(Lattice& L) {
     cudaFree(L.force);
     cudaFree(L.stats);
     cudaFree(L.pdev);
+    cudaFree(L.vert_particle);
     L.vel = L.force = L.stats = nullptr;
     L.pdev = nullptr;
+    L.vert_particle = nullptr;
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(L.sort_keys[k]);
+        cudaFree(L.sort_ids[k]);
+        L.sort_keys[k] = L.sort_ids[k] = nullptr;
+    }
+    cudaFree(L.sort_temp);
+    L.sort_temp = nullptr;
+    L.sort_temp_bytes = 0;
 }
 
 void drop_graphs(bib_ctx* c, int32_t h) {
@@ -317,9 +343,29 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
         d.link_len = S.dev.link_len;
         d.pairs = S.dev.pairs;
         d.pair_cs = S.dev.pair_cs;
+        d.inc_off = S.dev.inc_off;
+        d.inc = S.dev.inc;
         d.A0 = S.area;
         for (int k = 0; k < BIB_P_COUNT; ++k) d.prm[k] = ph.prm[k];
         L.max_nv = std::max(L.max_nv, ph.nv);
+    }
+    if (L.ib.spread_mode == BIB_SPREAD_DETERMINISTIC) {
+        const int sup = L.ib.dirac == BIB_DIRAC_PESKIN ? 4 : 3;
+        const int64_t ne = (int64_t)L.nvert * sup * sup * sup;
+        if (ne >= (int64_t)1 << 31) return fail(c, BIB_EUNSUPPORTED, "too many spreading entries for the sort");
+        for (int k = 0; k < 2; ++k) {
+            BIB_CUDA(c, cudaMalloc((void**)&L.sort_keys[k], ne * sizeof(uint32_t)));
+            BIB_CUDA(c, cudaMalloc((void**)&L.sort_ids[k], ne * sizeof(uint32_t)));
+        }
+        L.sort_temp_bytes = spread_sort_temp_bytes(ne);
+        BIB_CUDA(c, cudaMalloc(&L.sort_temp, L.sort_temp_bytes));
+    }
+    {
+        std::vector<int> vp(L.nvert);
+        for (int p = 0; p < np; ++p)
+            for (int v = 0; v < L.parts[p].nv; ++v) vp[L.parts[p].v0 + v] = p;
+        BIB_CUDA(c, cudaMalloc((void**)&L.vert_particle, L.nvert * sizeof(int)));
+        BIB_CUDA(c, cudaMemcpy(L.vert_particle, vp.data(), L.nvert * sizeof(int), cudaMemcpyHostToDevice));
     }
     BIB_CUDA(c, cudaMalloc((void**)&L.pdev, np * sizeof(ParticleDev)));
     BIB_CUDA(c, cudaMemcpy(L.pdev, pd.data(), np * sizeof(ParticleDev), cudaMemcpyHostToDevice));
@@ -339,27 +385,71 @@ void record(bib_ctx* c, int idx) {
     if (c->profiling) cudaEventRecord(c->ev[idx], c->stream);
 }
 
-// One coupled step in the driver order of progs/capsule_in_shear/capsule_in_shear.cpp:187-227:
-// velocity at the vertices from the current state (computeVelocity + interpolate), force
-// field reset to the body force (setExternalVector), membrane forces + vertex motion,
-// spreading, collide-and-stream, wall processors.
+// One coupled step.  The reference's driver order (progs/capsule_in_shear/capsule_in_shear.cpp:
+// 187-227) is computeVelocity -> setExternalVector -> [interpolate, compute + spread forces,
+// move] -> collideAndStream -> wall processors.  Forces at X_n do not depend on the velocity,
+// so the same arithmetic is issued as: membrane forces at X_n -> spreading into the force
+// buffer that the previous step reset to the body force -> collide-and-stream, which also
+// emits the velocity field of the pre-collision state with the previous force -> wall
+// reconstruction -> interpolation of that velocity to X_n and the move -> area / volume /
+// centre of the new positions.
 void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
     cudaStream_t s = c->stream;
     const bool ib = with_ib && L.nvert > 0;
+    if (with_ib && with_lbm) {
+        if (!L.target_clean) launch_force_fill(L, 1 - L.fe, s);
+        record(c, 0);
+        if (ib) launch_membrane_forces(L, s);
+        record(c, 1);
+        if (ib) launch_spread(L, 1 - L.fe, s);
+        record(c, 2);
+        launch_collide_stream(L, true, s);  // u of this state, collision with F[1-fe], F[fe] := body
+        record(c, 3);
+        L.cur = 1 - L.cur;
+        L.fe = 1 - L.fe;
+        L.target_clean = true;
+        launch_fd_walls(L, L.cur, L.fe, s);
+        record(c, 4);
+        if (ib) {
+            launch_interpolate_move(L, s);
+            launch_particle_update(L, s);
+            L.pcur = 1 - L.pcur;
+        }
+        record(c, 5);
+        return;
+    }
+    if (with_ib) {
+        // the IB data processor alone: velocity of the current state, force field reset to
+        // the body force, forces, spreading, move (DataProcessors.hh:104-107)
+        record(c, 0);
+        launch_velocity_field(L, s);
+        launch_force_fill(L, L.fe, s);
+        L.target_clean = false;
+        if (ib) launch_membrane_forces(L, s);
+        record(c, 1);
+        if (ib) launch_spread(L, L.fe, s);
+        record(c, 2);
+        record(c, 3);
+        record(c, 4);
+        if (ib) {
+            launch_interpolate_move(L, s);
+            launch_particle_update(L, s);
+            L.pcur = 1 - L.pcur;
+        }
+        record(c, 5);
+        return;
+    }
+    // collide-and-stream alone (CoProcessor3D::collideAndStream): collision with the current
+    // external force, which stays as it is
     record(c, 0);
-    if (ib) launch_interpolate(L, s);
     record(c, 1);
-    if (with_ib) launch_force_fill(L, s);
-    if (ib) launch_membrane(L, s);
     record(c, 2);
-    if (ib) launch_spread(L, s);
+    launch_collide_stream(L, false, s);
     record(c, 3);
-    if (with_lbm) launch_collide_stream(L, s);
+    L.cur = 1 - L.cur;
+    launch_fd_walls(L, L.cur, L.fe, s);
     record(c, 4);
-    if (with_lbm) launch_fd_walls(L, L.f[1 - L.cur], s);
     record(c, 5);
-    if (with_lbm) L.cur = 1 - L.cur;
-    if (ib) L.pcur = 1 - L.pcur;
 }
 
 bib_status accumulate_profile(bib_ctx* c) {
@@ -382,10 +472,16 @@ bib_status run_steps(bib_ctx* c, int32_t h, int64_t nsteps, bool with_ib, bool w
     const bool use_graph = c->graph_mode && !c->profiling && with_ib && with_lbm && nsteps >= 2;
     int64_t done = 0;
     if (use_graph) {
-        const std::pair<int, int> key(h, L->cur * 2 + L->pcur);
+        if (!L->target_clean) {  // the graph assumes a clean spreading target on entry
+            enqueue_step(c, *L, true, true);
+            BIB_CHECK_LAUNCH(c);
+            ++done;
+        }
+        const std::pair<int, int> key(h, L->cur * 4 + L->pcur * 2 + L->fe);
         GraphEntry& ge = c->graphs[key];
         if (!ge.exec) {
-            const int cur0 = L->cur, pcur0 = L->pcur;
+            const int cur0 = L->cur, pcur0 = L->pcur, fe0 = L->fe;
+            const bool clean0 = L->target_clean;
             cudaGraph_t g = nullptr;
             BIB_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
             enqueue_step(c, *L, true, true);
@@ -393,13 +489,15 @@ bib_status run_steps(bib_ctx* c, int32_t h, int64_t nsteps, bool with_ib, bool w
             cudaError_t e = cudaStreamEndCapture(c->stream, &g);
             L->cur = cur0;
             L->pcur = pcur0;
+            L->fe = fe0;
+            L->target_clean = clean0;
             if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
             e = cudaGraphInstantiate(&ge.exec, g, 0);
             cudaGraphDestroy(g);
             if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
         }
         for (; done + 2 <= nsteps; done += 2) BIB_CUDA(c, cudaGraphLaunch(ge.exec, c->stream));
-        // two steps leave both parities unchanged
+        // two steps leave every parity unchanged
     }
     for (; done < nsteps; ++done) {
         enqueue_step(c, *L, with_ib, with_lbm);
@@ -480,7 +578,10 @@ void bib_destroy(bib_ctx* c) {
         free_particles(*Lp);
         cudaFree(Lp->f[0]);
         cudaFree(Lp->f[1]);
-        cudaFree(Lp->F);
+        cudaFree(Lp->F[0]);
+        cudaFree(Lp->F[1]);
+        cudaFree(Lp->u);
+        cudaFree(Lp->wall);
         cudaFree(Lp->phase);
     }
     for (auto& S : c->shapes) {
@@ -491,6 +592,8 @@ void bib_destroy(bib_ctx* c) {
         cudaFree(S->dev.link_len);
         cudaFree(S->dev.pairs);
         cudaFree(S->dev.pair_cs);
+        cudaFree(S->dev.inc_off);
+        cudaFree(S->dev.inc);
     }
     for (int k = 0; k < 6; ++k)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
@@ -555,7 +658,10 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
     d.ny = (int)ny;
     d.nz = (int)nz;
     d.n = nx * ny * nz;
-    d.stride = (d.n + 127) / 128 * 128;
+    // population / field arrays: 128-cell aligned, and offset by 384 cells so that the 19 + 12
+    // concurrently streamed arrays do not start at a power-of-two distance from each other
+    // (identical DRAM channel / bank interleaving for every stream)
+    d.stride = (d.n + 127) / 128 * 128 + 384;
     d.px = p->periodic[0] != 0;
     d.py = p->periodic[1] != 0;
     d.pz = p->periodic[2] != 0;
@@ -567,6 +673,9 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
     d.omega_inner = p->use_phase ? p->omega_inner : p->omega;
     d.trt_magic = p->trt_magic > 0 ? p->trt_magic : 0.25;
     // computeOmega, src/fsi/VariableViscosityDynamics.hh:131-141, for phase 0 and 1
+    d.inv_n[0] = 1. / (double)d.nx;
+    d.inv_n[1] = 1. / (double)d.ny;
+    d.inv_n[2] = 1. / (double)d.nz;
     d.omega_c0 = d.omega * d.omega_inner / (0.0 * d.omega + (1. - 0.0) * d.omega_inner);
     d.omega_c1 = d.omega * d.omega_inner / (1.0 * d.omega + (1. - 1.0) * d.omega_inner);
     std::memcpy(d.wall_u, p->wall_u, sizeof(d.wall_u));
@@ -575,26 +684,26 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
     d.scale = p->storage == BIB_STORAGE_F16 ? (float)sc : 1.0f;
     d.inv_scale = 1.0f / d.scale;
     L->storage = p->storage;
+    d.fd_walls = (!d.py && d.wall_y == BIB_WALL_FD_VELOCITY) ? 1 : 0;
     const size_t pb = pop_bytes(p->storage) * Q * d.stride;
-    for (int k = 0; k < 2; ++k) {
-        cudaError_t e = cudaMalloc(&L->f[k], pb);
-        if (e != cudaSuccess) {
-            cudaFree(L->f[0]);
-            return fail(c, BIB_ENOMEM, "population buffers (%zu bytes): %s", pb, cudaGetErrorString(e));
-        }
-        cudaMemsetAsync(L->f[k], 0, pb, c->stream);
-    }
     const size_t fb = force_bytes(p->storage) * 3 * d.stride;
-    if (cudaMalloc(&L->F, fb) != cudaSuccess) {
-        cudaFree(L->f[0]);
-        cudaFree(L->f[1]);
-        return fail(c, BIB_ENOMEM, "force field (%zu bytes)", fb);
+    const size_t wb = d.fd_walls ? pop_bytes(p->storage) * Q * 2 * (size_t)d.nx * d.nz : 0;
+    void** bufs[6] = {&L->f[0], &L->f[1], &L->F[0], &L->F[1], &L->u, &L->wall};
+    const size_t sizes[6] = {pb, pb, fb, fb, fb, wb};
+    for (int k = 0; k < 6; ++k) {
+        if (!sizes[k]) continue;
+        cudaError_t e = cudaMalloc(bufs[k], sizes[k]);
+        if (e != cudaSuccess) {
+            for (int j = 0; j < k; ++j) cudaFree(*bufs[j]);
+            return fail(c, BIB_ENOMEM, "lattice buffer of %zu bytes: %s", sizes[k], cudaGetErrorString(e));
+        }
+        cudaMemsetAsync(*bufs[k], 0, sizes[k], c->stream);
     }
-    cudaMemsetAsync(L->F, 0, fb, c->stream);
     if (d.use_phase) {
         if (cudaMalloc((void**)&L->phase, d.stride) != cudaSuccess) return fail(c, BIB_ENOMEM, "phase field");
         cudaMemsetAsync(L->phase, 0, d.stride, c->stream);
     }
+    L->target_clean = false;
     // external scalars start at zero, as Palabos cells do; every coupled step then
     // resets them to the body force before spreading (setExternalVector)
     BIB_CHECK_LAUNCH(c);
@@ -620,18 +729,20 @@ bib_status bib_lattice_send(bib_ctx* c, int32_t h, const void* buf, size_t bytes
     std::vector<double> ext;
     if (layout == BIB_LAYOUT_SOA_F64) {
         if (bytes != (size_t)Q * n * sizeof(double)) return fail(c, BIB_EINVAL, "expected %zu bytes", (size_t)Q * n * 8);
-    } else if (layout == BIB_LAYOUT_PALABOS_F64) {
-        if (bytes != (size_t)23 * n * sizeof(double)) return fail(c, BIB_EINVAL, "expected %zu bytes", (size_t)23 * n * 8);
+    } else if (layout == BIB_LAYOUT_PALABOS_F64 || layout == BIB_LAYOUT_COPROCESSOR_F64) {
+        const int per = layout == BIB_LAYOUT_PALABOS_F64 ? 23 : Q;
+        if (bytes != (size_t)per * n * sizeof(double)) return fail(c, BIB_EINVAL, "expected %zu bytes", (size_t)per * n * 8);
         soa.resize(Q * n);
-        ext.resize(4 * n);
+        if (per == 23) ext.resize(4 * n);
         const LatticeDesc& d = L->d;
         int64_t w = 0;
         for (int x = 0; x < d.nx; ++x)
             for (int y = 0; y < d.ny; ++y)
                 for (int z = 0; z < d.nz; ++z, ++w) {
                     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
-                    for (int i = 0; i < Q; ++i) soa[i * n + k] = src[23 * w + i];
-                    for (int a = 0; a < 4; ++a) ext[a * n + k] = src[23 * w + Q + a];
+                    for (int i = 0; i < Q; ++i) soa[i * n + k] = src[per * w + i];
+                    if (per == 23)
+                        for (int a = 0; a < 4; ++a) ext[a * n + k] = src[per * w + Q + a];
                 }
         src = soa.data();
     } else {
@@ -640,7 +751,7 @@ bib_status bib_lattice_send(bib_ctx* c, int32_t h, const void* buf, size_t bytes
     double* d = nullptr;
     bib_status st = device_buffer(c, &d, src, Q * n);
     if (st) return st;
-    launch_import_soa(*L, L->f[L->cur], d, c->stream);
+    launch_import_soa(*L, d, c->stream);
     BIB_CHECK_LAUNCH(c);
     if (!ext.empty()) {
         double* dF = nullptr;
@@ -649,7 +760,8 @@ bib_status bib_lattice_send(bib_ctx* c, int32_t h, const void* buf, size_t bytes
             cudaFree(d);
             return st;
         }
-        launch_force_import(*L, dF, c->stream);
+        launch_force_import(*L, L->fe, dF, c->stream);
+        L->target_clean = false;
         if (L->phase) launch_phase_import(*L, dF + 3 * n, c->stream);
         BIB_CUDA(c, cudaStreamSynchronize(c->stream));
         cudaFree(dF);
@@ -663,14 +775,16 @@ bib_status bib_lattice_receive(bib_ctx* c, int32_t h, void* buf, size_t bytes, i
     Lattice* L = get_lattice(c, h);
     if (!L || !buf) return fail(c, BIB_EINVAL, "invalid lattice handle or buffer");
     const int64_t n = L->d.n;
-    const size_t want = (layout == BIB_LAYOUT_PALABOS_F64 ? 23 : Q) * n * sizeof(double);
-    if (layout != BIB_LAYOUT_SOA_F64 && layout != BIB_LAYOUT_PALABOS_F64) return fail(c, BIB_EINVAL, "unknown layout");
+    const int per = layout == BIB_LAYOUT_PALABOS_F64 ? 23 : Q;
+    const size_t want = (size_t)per * n * sizeof(double);
+    if (layout != BIB_LAYOUT_SOA_F64 && layout != BIB_LAYOUT_PALABOS_F64 && layout != BIB_LAYOUT_COPROCESSOR_F64)
+        return fail(c, BIB_EINVAL, "unknown layout");
     if (bytes != want) return fail(c, BIB_EINVAL, "expected %zu bytes", want);
     double* d = nullptr;
     bib_status st = device_buffer(c, &d, nullptr, (Q + 3) * n);
     if (st) return st;
-    launch_export_soa(*L, L->f[L->cur], d, c->stream);
-    launch_force_export(*L, d + Q * n, c->stream);
+    launch_export_soa(*L, d, c->stream);
+    launch_force_export(*L, L->fe, d + Q * n, c->stream);
     BIB_CHECK_LAUNCH(c);
     std::vector<double> host((Q + 3) * n);
     BIB_CUDA(c, cudaMemcpyAsync(host.data(), d, host.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
@@ -687,9 +801,11 @@ bib_status bib_lattice_receive(bib_ctx* c, int32_t h, void* buf, size_t bytes, i
         for (int y = 0; y < dd.ny; ++y)
             for (int z = 0; z < dd.nz; ++z, ++w) {
                 const int64_t k = x + (int64_t)dd.nx * (y + (int64_t)dd.ny * z);
-                for (int i = 0; i < Q; ++i) dst[23 * w + i] = host[i * n + k];
-                for (int a = 0; a < 3; ++a) dst[23 * w + Q + a] = host[(Q + a) * n + k];
-                dst[23 * w + 22] = 0.0;
+                for (int i = 0; i < Q; ++i) dst[per * w + i] = host[i * n + k];
+                if (per == 23) {
+                    for (int a = 0; a < 3; ++a) dst[per * w + Q + a] = host[(Q + a) * n + k];
+                    dst[per * w + 22] = 0.0;
+                }
             }
     return BIB_OK;
 }
@@ -709,8 +825,8 @@ bib_status bib_lattice_init_equilibrium(bib_ctx* c, int32_t h, const double* rho
         st = device_buffer(c, &dr, rho, n);
         if (st) return st;
     }
-    launch_init_equilibrium(*L, L->f[L->cur], dr, du, c->stream);
-    launch_fd_walls(*L, L->f[L->cur], c->stream);
+    launch_init_equilibrium(*L, dr, du, c->stream);
+    launch_fd_walls(*L, L->cur, L->fe, c->stream);
     BIB_CHECK_LAUNCH(c);
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(du);
@@ -724,7 +840,8 @@ bib_status bib_lattice_set_force(bib_ctx* c, int32_t h, const double* F) {
     double* d = nullptr;
     bib_status st = device_buffer(c, &d, F, 3 * L->d.n);
     if (st) return st;
-    launch_force_import(*L, d, c->stream);
+    launch_force_import(*L, L->fe, d, c->stream);
+    L->target_clean = false;
     BIB_CHECK_LAUNCH(c);
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(d);
@@ -737,7 +854,7 @@ bib_status bib_lattice_get_force(bib_ctx* c, int32_t h, double* F) {
     double* d = nullptr;
     bib_status st = device_buffer(c, &d, nullptr, 3 * L->d.n);
     if (st) return st;
-    launch_force_export(*L, d, c->stream);
+    launch_force_export(*L, L->fe, d, c->stream);
     BIB_CHECK_LAUNCH(c);
     BIB_CUDA(c, cudaMemcpyAsync(F, d, 3 * L->d.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -765,7 +882,7 @@ bib_status bib_lattice_get_velocity(bib_ctx* c, int32_t h, double* u) {
     double* d = nullptr;
     bib_status st = device_buffer(c, &d, nullptr, 3 * L->d.n);
     if (st) return st;
-    launch_velocity(*L, d, c->stream);
+    launch_velocity_export(*L, d, c->stream);
     BIB_CHECK_LAUNCH(c);
     BIB_CUDA(c, cudaMemcpyAsync(u, d, 3 * L->d.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -783,7 +900,8 @@ bib_status bib_shape_store(bib_ctx* c, const double* xyz, const int64_t* tri, in
     if ((st = upload(c, &S->dev.rest, S->rest)) || (st = upload(c, &S->dev.tri, S->tri)) ||
         (st = upload(c, &S->dev.tri_area, S->tri_area)) || (st = upload(c, &S->dev.links, S->links)) ||
         (st = upload(c, &S->dev.link_len, S->link_len)) || (st = upload(c, &S->dev.pairs, S->pairs)) ||
-        (st = upload(c, &S->dev.pair_cs, S->pair_cs)))
+        (st = upload(c, &S->dev.pair_cs, S->pair_cs)) || (st = upload(c, &S->dev.inc_off, S->inc_off)) ||
+        (st = upload(c, &S->dev.inc, S->inc)))
         return st;
     S->dev.nv = (int)nv;
     S->dev.nt = (int)nt;
@@ -812,11 +930,17 @@ bib_status bib_ib_configure(bib_ctx* c, int32_t h, const bib_ib_params* p) {
     Lattice* L = get_lattice(c, h);
     if (!L || !p) return fail(c, BIB_EINVAL, "invalid lattice handle or parameters");
     if (p->dirac != BIB_DIRAC_ROMA && p->dirac != BIB_DIRAC_PESKIN) return fail(c, BIB_EINVAL, "bad dirac");
-    if (p->spread_mode != BIB_SPREAD_ATOMIC) return fail(c, BIB_EUNSUPPORTED, "only atomic spreading is built");
+    if (p->spread_mode != BIB_SPREAD_ATOMIC && p->spread_mode != BIB_SPREAD_DETERMINISTIC)
+        return fail(c, BIB_EINVAL, "bad spread mode");
+    if (L->d.n >= (int64_t)0xffffffff) return fail(c, BIB_EUNSUPPORTED, "lattice too large for 32-bit cell keys");
     if (p->field_offset != std::floor(p->field_offset)) return fail(c, BIB_EINVAL, "field offset must be integral");
     L->ib.dirac = p->dirac;
     L->ib.spread_mode = p->spread_mode;
     L->ib.offset = p->field_offset;
+    // the spreading buffers depend on the mode: re-upload the particles on the next step
+    bib_status pst = pull_particles(c, *L);
+    if (pst) return pst;
+    if (!L->parts.empty()) L->particles_dirty = true;
     drop_graphs(c, h);
     return BIB_OK;
 }

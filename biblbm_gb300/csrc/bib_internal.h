@@ -18,13 +18,15 @@ constexpr int Q = 19;
 struct LatticeDesc {
     int nx, ny, nz;
     int64_t n;        // nx*ny*nz
-    int64_t stride;   // distance between two population arrays (>= n, padded)
+    int64_t stride;   // distance between two population arrays (>= n, padded to 128)
     int px, py, pz;   // periodic flags
     int wall_y, wall_z;
+    int fd_walls;     // finite-difference velocity walls on the y = 0 and y = ny-1 planes
     int collision;
     int use_phase;
     double omega, omega_inner, trt_magic;
     double omega_c0, omega_c1;  // omega for phase 0 and 1: w0*w1/(c*w0 + (1-c)*w1)
+    double inv_n[3];            // 1/nx, 1/ny, 1/nz (Arithmetic1D's Linv, Periodicity.h:73-78)
     double wall_u[4][3];
     double body[3];
     float scale, inv_scale;     // FP16 storage scale
@@ -47,6 +49,8 @@ struct ShapeDev {
     double* link_len;     // nl
     int* pairs;           // 4*np
     double* pair_cs;      // 2*np
+    int* inc_off;         // nv+1: per-vertex incidence lists (links, triangles, pairs)
+    int* inc;             // (type << 29) | element id
 };
 
 // One particle as the device kernels see it.
@@ -61,16 +65,18 @@ struct ParticleDev {
     const double* link_len;
     const int* pairs;
     const double* pair_cs;
+    const int* inc_off;
+    const int* inc;
     double A0;
     double prm[BIB_P_COUNT];
 };
 
-// Per-particle state written by the membrane kernel: {area, volume, com[3]}.
+// Per-particle state kept on the device: {area, volume, com[3]}.
 constexpr int STATS = 5;
 
 struct ShapeHost {
     std::vector<double> rest, tri_area, link_len, pair_cs;
-    std::vector<int> tri, links, pairs;
+    std::vector<int> tri, links, pairs, inc_off, inc;
     double area = 0, volume = 0;
     ShapeDev dev{};
 };
@@ -81,13 +87,30 @@ struct ParticleHost {
     std::vector<double> prm;
 };
 
+// Device state of one lattice.
+//
+// Populations use a pull scheme: buffer f[cur] holds the post-collision populations of
+// the previous step, f*(x), so the post-streaming state the reference keeps between
+// steps is f_i(x) = f*_i(x - c_i) (with bounce-back / wall rules at the faces).  The
+// collide-and-stream kernel gathers f_i(x), emits the velocity field
+// u = j/rho + F_prev/2 the reference's computeVelocity would produce for this state,
+// collides with the force spread in this step and writes f*(x) into f[1-cur].  Nodes on
+// finite-difference velocity walls read their populations from wall[] instead, which the
+// wall kernel fills after every collide-and-stream.
+//
+// Forces are double-buffered: F[fe] holds the external force of the current state (the
+// reference's Cell externals), F[1-fe] is the target of the spreading of the next step.
 struct Lattice {
     LatticeDesc d{};
     IbDesc ib{0, 0, -1.0};
     int storage = BIB_STORAGE_F64;
-    void* f[2] = {nullptr, nullptr};  // population buffers, swapped every step
+    void* f[2] = {nullptr, nullptr};
     int cur = 0;
-    void* F = nullptr;                // force field (double for F64 storage, float otherwise)
+    void* wall = nullptr;             // 2 sides x nx x nz x 19 populations of FD wall nodes
+    void* F[2] = {nullptr, nullptr};  // force fields (double for F64 storage, float otherwise)
+    int fe = 0;
+    bool target_clean = false;        // F[1-fe] holds the body force, ready to receive spreading
+    void* u = nullptr;                // velocity field (double for F64 storage, float otherwise)
     uint8_t* phase = nullptr;
     // immersed boundary
     std::vector<ParticleHost> parts;
@@ -98,33 +121,43 @@ struct Lattice {
     double* force = nullptr;
     double* stats = nullptr;              // STATS per particle
     ParticleDev* pdev = nullptr;
-    int* vert_particle = nullptr;         // vertex -> particle
+    int* vert_particle = nullptr;         // global vertex -> particle
     int max_nv = 0;
     bool particles_dirty = true;  // host copies below are authoritative until uploaded
     std::vector<double> host_pos;    // concatenated vertex positions
     std::vector<double> host_stats;  // STATS per particle
     size_t membrane_smem = 0;
+    // deterministic spreading: (target cell, entry) pairs and their radix-sorted copies
+    uint32_t* sort_keys[2] = {nullptr, nullptr};
+    uint32_t* sort_ids[2] = {nullptr, nullptr};
+    void* sort_temp = nullptr;
+    size_t sort_temp_bytes = 0;
     int handle = -1;
 };
 
 // ---- kernel launchers (lattice_kernels.cu) ----
-void launch_collide_stream(const Lattice& L, cudaStream_t s);
-void launch_fd_walls(const Lattice& L, void* f, cudaStream_t s);
-void launch_velocity(const Lattice& L, double* u, cudaStream_t s);
-void launch_init_equilibrium(const Lattice& L, void* f, const double* rho, const double* u, cudaStream_t s);
-void launch_import_soa(const Lattice& L, void* f, const double* src, cudaStream_t s);
-void launch_export_soa(const Lattice& L, const void* f, double* dst, cudaStream_t s);
-void launch_force_import(const Lattice& L, const double* src, cudaStream_t s);
-void launch_force_export(const Lattice& L, double* dst, cudaStream_t s);
+// coupled = true: velocity output, collision with the spread force F[1-fe], F[fe] reset
+// to the body force afterwards.  coupled = false: collision with F[fe], no side outputs.
+void launch_collide_stream(const Lattice& L, bool coupled, cudaStream_t s);
+void launch_fd_walls(const Lattice& L, int buf, int fbuf, cudaStream_t s);
+void launch_velocity_field(const Lattice& L, cudaStream_t s);  // u from the current state and F[fe]
+void launch_velocity_export(const Lattice& L, double* u, cudaStream_t s);
+void launch_init_equilibrium(const Lattice& L, const double* rho, const double* u, cudaStream_t s);
+void launch_import_soa(const Lattice& L, const double* src, cudaStream_t s);
+void launch_export_soa(const Lattice& L, double* dst, cudaStream_t s);
+void launch_force_import(const Lattice& L, int buf, const double* src, cudaStream_t s);
+void launch_force_export(const Lattice& L, int buf, double* dst, cudaStream_t s);
+void launch_force_fill(const Lattice& L, int buf, cudaStream_t s);
 void launch_phase_import(const Lattice& L, const double* src, cudaStream_t s);
-void launch_force_fill(const Lattice& L, cudaStream_t s);
 void launch_nan_scan(const Lattice& L, int* flag, cudaStream_t s);
 
 // ---- kernel launchers (ib_kernels.cu) ----
-void launch_interpolate(const Lattice& L, cudaStream_t s);
-void launch_membrane(const Lattice& L, cudaStream_t s);
-void launch_spread(const Lattice& L, cudaStream_t s);
+void launch_membrane_forces(const Lattice& L, cudaStream_t s);
+void launch_spread(const Lattice& L, int fbuf, cudaStream_t s);
+void launch_interpolate_move(const Lattice& L, cudaStream_t s);  // vel and pos[1-pcur] = pos + vel
+void launch_particle_update(const Lattice& L, cudaStream_t s);   // area/volume/COM of pos[1-pcur] + remap
 size_t membrane_smem_bytes(int max_nv);
+size_t spread_sort_temp_bytes(int64_t nentries);
 void configure_membrane_kernel(size_t smem);
 
 }  // namespace bib

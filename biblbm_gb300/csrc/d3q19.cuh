@@ -188,6 +188,70 @@ __device__ __forceinline__ void collide(C* f, const C* F, C omega, C omega_minus
     }
 }
 
+// Compact BGK + Guo collision for the reduced-precision paths.  Algebraically the same
+// operator as collide<C, BGK_GUO_VOF> (the Guo term of VariableViscosityDynamics.hh:47-129
+// is t_i (1 - w/2) [3 (c_i - u).F + 9 (c_i.u)(c_i.F)]), evaluated per opposite pair
+// (i, i+9) from its symmetric and antisymmetric parts.  The populations may carry a common
+// scale S (FP16 storage keeps f-bar * S): moments are unscaled once, post-collision values
+// are produced in scaled units.  With `u_prev` non-null the velocity j/rho + F_prev/2 of the
+// incoming state is returned as well (the reference's computeVelocity).
+template <int COLL>
+__device__ __forceinline__ void collide_compact(float* f, const float* F, float omega, float S, float invS,
+                                                const float* Fprev, float* u_prev) {
+    const float sxm = f[1] + f[4] + f[5] + f[6] + f[7];
+    const float sxp = f[10] + f[13] + f[14] + f[15] + f[16];
+    const float sym = f[2] + f[4] + f[8] + f[9] + f[14];
+    const float syp = f[5] + f[11] + f[13] + f[17] + f[18];
+    const float szm = f[3] + f[6] + f[8] + f[16] + f[18];
+    const float szp = f[7] + f[9] + f[12] + f[15] + f[17];
+    const float sx0 = f[0] + f[2] + f[3] + f[8] + f[9] + f[11] + f[12] + f[17] + f[18];
+    const float rb = (sxm + sx0 + sxp) * invS;
+    const float j0 = (sxp - sxm) * invS, j1 = (syp - sym) * invS, j2 = (szp - szm) * invS;
+    const float invRho = 1.0f / (rb + 1.0f);
+    if (u_prev) {
+        u_prev[0] = j0 * invRho + 0.5f * Fprev[0];
+        u_prev[1] = j1 * invRho + 0.5f * Fprev[1];
+        u_prev[2] = j2 * invRho + 0.5f * Fprev[2];
+    }
+    const float omo = 1.0f - omega;
+    if (COLL == BIB_COLLISION_BGK) {
+        // BGKdynamics: equilibrium of j, no forcing
+        const float jsq = j0 * j0 + j1 * j1 + j2 * j2;
+        const float base = rb - 1.5f * invRho * jsq;
+        const float h = 4.5f * invRho;
+        f[0] = omo * f[0] + S * omega * weight<float>(0) * base;
+#pragma unroll
+        for (int i = 1; i < 10; ++i) {
+            const float cj = float(cx(i)) * j0 + float(cy(i)) * j1 + float(cz(i)) * j2;
+            const float tw = S * omega * weight<float>(i);
+            const float P = tw * fmaf(h * cj, cj, base), M = tw * 3.0f * cj;
+            f[i] = omo * f[i] + P + M;
+            f[i + 9] = omo * f[i + 9] + P - M;
+        }
+        return;
+    }
+    const float u0 = j0 * invRho + 0.5f * F[0], u1 = j1 * invRho + 0.5f * F[1], u2 = j2 * invRho + 0.5f * F[2];
+    const float rho = rb + 1.0f;
+    const float J0 = rho * u0, J1 = rho * u1, J2 = rho * u2;
+    const float jsq = J0 * J0 + J1 * J1 + J2 * J2;
+    const float base = rb - 1.5f * invRho * jsq;
+    const float h = 4.5f * invRho;
+    const float mu = 1.0f - 0.5f * omega;
+    const float uF = u0 * F[0] + u1 * F[1] + u2 * F[2];
+    f[0] = omo * f[0] + S * weight<float>(0) * (omega * base - 3.0f * mu * uF);
+#pragma unroll
+    for (int i = 1; i < 10; ++i) {
+        const float cj = float(cx(i)) * J0 + float(cy(i)) * J1 + float(cz(i)) * J2;
+        const float cu = float(cx(i)) * u0 + float(cy(i)) * u1 + float(cz(i)) * u2;
+        const float cF = float(cx(i)) * F[0] + float(cy(i)) * F[1] + float(cz(i)) * F[2];
+        const float tw = S * weight<float>(i);
+        const float P = tw * (omega * fmaf(h * cj, cj, base) + mu * (9.0f * cu * cF - 3.0f * uF));
+        const float M = tw * 3.0f * (omega * cj + mu * cF);
+        f[i] = omo * f[i] + P + M;
+        f[i + 9] = omo * f[i + 9] + P - M;
+    }
+}
+
 __host__ __device__ inline int64_t wrap_index(int64_t i, int64_t n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
 }  // namespace bib

@@ -7,6 +7,8 @@
 // buffers swapped every step), velocities and forces (FP64).
 #include <cfloat>
 
+#include <cub/device/device_radix_sort.cuh>
+
 #include "d3q19.cuh"
 
 namespace bib {
@@ -29,11 +31,10 @@ __device__ __forceinline__ double half_support(int dirac) { return dirac == BIB_
 __device__ __forceinline__ int support(int dirac) { return dirac == BIB_DIRAC_PESKIN ? 4 : 3; }
 
 // Arithmetic1D::min_mod_diff (periodic) / plain difference, src/fsi/Periodicity.h:26-34, 93-96
-__device__ __forceinline__ double axis_dist(int periodic, int N, double a, double b) {
+__device__ __forceinline__ double axis_dist(int periodic, int N, double Linv, double a, double b) {
     const double x = a - b;
     if (!periodic) return x;
-    const double L = (double)N, Linv = 1.0 / L;
-    return x - floor(x * Linv + 0.5) * L;
+    return x - floor(x * Linv + 0.5) * (double)N;
 }
 
 // Node classification of a single-block domain (ImmersedBoundaryDynamics.hh:46-66, 351-363):
@@ -48,8 +49,8 @@ __device__ int classify(const LatticeDesc& d, int dirac, const double* p) {
         const double top = (double)(N[a] - 1);
         const double elo = 0.0 - h, ehi = top + h;
         const double blo = 0.0 - shrink, bhi = top + shrink;
-        in_env = in_env && fabs(axis_dist(per[a], N[a], 0.5 * (elo + ehi), p[a])) < 0.5 * (ehi - elo);
-        in_bulk = in_bulk && fabs(axis_dist(per[a], N[a], 0.5 * (blo + bhi), p[a])) < 0.5 * (bhi - blo);
+        in_env = in_env && fabs(axis_dist(per[a], N[a], d.inv_n[a], 0.5 * (elo + ehi), p[a])) < 0.5 * (ehi - elo);
+        in_bulk = in_bulk && fabs(axis_dist(per[a], N[a], d.inv_n[a], 0.5 * (blo + bhi), p[a])) < 0.5 * (bhi - blo);
     }
     return !in_env ? 0 : (in_bulk ? 1 : 2);
 }
@@ -69,31 +70,16 @@ __device__ __forceinline__ int remap_global(int periodic, int N, int64_t i_local
 }
 
 // ---------------------------------------------------------------- interpolation
-template <class T>
-__device__ __forceinline__ void node_velocity(const LatticeDesc& d, const T* __restrict__ f,
-                                              const typename Store<T>::F* __restrict__ F, int x, int y, int z,
-                                              typename Store<T>::C* u) {
-    using C = typename Store<T>::C;
-    if (!d.py && d.wall_y == BIB_WALL_FD_VELOCITY && (y == 0 || y == d.ny - 1)) {
-        const int side = y == 0 ? 0 : 1;
-        u[0] = (C)d.wall_u[side][0];
-        u[1] = (C)d.wall_u[side][1];
-        u[2] = (C)d.wall_u[side][2];
-        return;
-    }
-    const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
-    C fc[Q];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) fc[i] = Store<T>::load(f + i * d.stride + k, d.inv_scale);
-    C Fc[3] = {(C)F[k], (C)F[d.stride + k], (C)F[2 * d.stride + k]};
-    velocity_with_force(fc, Fc, u);
-}
-
-template <class T>
-__global__ void __launch_bounds__(128) k_interpolate(LatticeDesc d, IbDesc ib, int nvert, const double* __restrict__ pos,
-                                                      const T* __restrict__ f, const typename Store<T>::F* __restrict__ F,
-                                                      double* __restrict__ vel) {
-    using C = typename Store<T>::C;
+// Interpolation of the velocity field (written by the collide-and-stream kernel or the
+// velocity kernel) to every vertex, followed by the explicit Euler move
+// X_{n+1} = X_n + U_n (DeformableParticle3D::move_vertices, DeformableParticle3D.hh:26-51).
+// Classes and index arithmetic follow interpolate_impl with the Bulk / General
+// interpolators, ImmersedBoundaryDynamics_interpolation.hh:13-153.
+template <class UT>
+__global__ void __launch_bounds__(128) k_interpolate_move(LatticeDesc d, IbDesc ib, int nvert, const double* __restrict__ pos,
+                                                           double* __restrict__ pos_next, const UT* __restrict__ u,
+                                                           double* __restrict__ vel) {
+    using C = UT;
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvert) return;
     const double p[3] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
@@ -125,11 +111,10 @@ __global__ void __launch_bounds__(128) k_interpolate(LatticeDesc d, IbDesc ib, i
                 for (int c = 0; c < s; ++c) {
                     if (gz[c] < 0) continue;
                     const C wt = wxy * w[2][c];
-                    C u[3];
-                    node_velocity<T>(d, f, F, gx[a], gy[b], gz[c], u);
-                    acc[0] += wt * u[0];
-                    acc[1] += wt * u[1];
-                    acc[2] += wt * u[2];
+                    const int64_t k = gx[a] + (int64_t)d.nx * (gy[b] + (int64_t)d.ny * gz[c]);
+                    acc[0] += wt * __ldg(u + k);
+                    acc[1] += wt * __ldg(u + d.stride + k);
+                    acc[2] += wt * __ldg(u + 2 * d.stride + k);
                 }
             }
         }
@@ -140,6 +125,9 @@ __global__ void __launch_bounds__(128) k_interpolate(LatticeDesc d, IbDesc ib, i
     vel[3 * v] = out[0];
     vel[3 * v + 1] = out[1];
     vel[3 * v + 2] = out[2];
+    pos_next[3 * v] = p[0] + out[0];
+    pos_next[3 * v + 1] = p[1] + out[1];
+    pos_next[3 * v + 2] = p[2] + out[2];
 }
 
 // ---------------------------------------------------------------- spreading
@@ -184,6 +172,73 @@ __global__ void __launch_bounds__(128) k_spread(LatticeDesc d, IbDesc ib, int nv
     }
 }
 
+// Deterministic spreading.  Every (vertex, stencil node) pair becomes an entry keyed by its
+// target cell; a stable radix sort groups the entries of a cell in vertex order, and one
+// thread per cell sums its contributions in that order onto the body force already in F.
+// The result does not depend on scheduling (the atomic path does, in its last bits).
+// Entries that spread nowhere carry the key n (one past the last cell), so the sort needs
+// only ceil(log2(n + 1)) key bits.
+__host__ __device__ inline int key_bits(int64_t n) {
+    int b = 1;
+    while (((int64_t)1 << b) <= n) ++b;
+    return b;
+}
+
+__global__ void __launch_bounds__(128) k_spread_keys(LatticeDesc d, IbDesc ib, int nvert, const double* __restrict__ pos,
+                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nvert) return;
+    const int s = support(ib.dirac), s3 = s * s * s;
+    const double p[3] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
+    const bool inside = classify(d, ib.dirac, p) != 0;
+    const int off = (int)ib.offset;
+    const double h = half_support(ib.dirac);
+    int64_t lo[3];
+    for (int a = 0; a < 3; ++a) lo[a] = (int64_t)ceil(p[a] - ib.offset - h);
+    for (int m = 0; m < s3; ++m) {
+        const int a = m / (s * s), b = (m / s) % s, c = m % s;
+        const int gx = remap_global(d.px, d.nx, lo[0] + a, off);
+        const int gy = remap_global(d.py, d.ny, lo[1] + b, off);
+        const int gz = remap_global(d.pz, d.nz, lo[2] + c, off);
+        const bool ok = inside && gx >= 0 && gy >= 0 && gz >= 0;
+        keys[(int64_t)v * s3 + m] = ok ? (uint32_t)(gx + (int64_t)d.nx * (gy + (int64_t)d.ny * gz)) : (uint32_t)d.n;
+        ids[(int64_t)v * s3 + m] = (uint32_t)((int64_t)v * s3 + m);
+    }
+}
+
+template <class FT>
+__global__ void __launch_bounds__(128) k_spread_reduce(LatticeDesc d, IbDesc ib, int64_t nentries,
+                                                        const uint32_t* __restrict__ keys, const uint32_t* __restrict__ ids,
+                                                        const double* __restrict__ pos, const double* __restrict__ force,
+                                                        FT* __restrict__ F) {
+    const int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (p >= nentries) return;
+    const uint32_t key = keys[p];
+    if (key == (uint32_t)d.n || (p > 0 && keys[p - 1] == key)) return;  // not the head of a cell's run
+    const int s = support(ib.dirac), s3 = s * s * s;
+    const double h = half_support(ib.dirac);
+    FT acc[3] = {F[key], F[d.stride + key], F[2 * d.stride + key]};
+    for (int64_t q = p; q < nentries && keys[q] == key; ++q) {
+        const uint32_t e = ids[q];
+        const int v = (int)(e / s3), m = (int)(e % s3);
+        const int a = m / (s * s), b = (m / s) % s, c = m % s;
+        const double pr[3] = {pos[3 * v] - ib.offset, pos[3 * v + 1] - ib.offset, pos[3 * v + 2] - ib.offset};
+        FT w[3];
+        const int sel[3] = {a, b, c};
+        for (int ax = 0; ax < 3; ++ax) {
+            const int64_t lo = (int64_t)ceil(pr[ax] - h);
+            w[ax] = dirac_eval<FT>(ib.dirac, (FT)((double)(lo + sel[ax]) - pr[ax]));
+        }
+        const FT wt = (w[0] * w[1]) * w[2];
+        acc[0] += wt * (FT)force[3 * v];
+        acc[1] += wt * (FT)force[3 * v + 1];
+        acc[2] += wt * (FT)force[3 * v + 2];
+    }
+    F[key] = acc[0];
+    F[d.stride + key] = acc[1];
+    F[2 * d.stride + key] = acc[2];
+}
+
 // ---------------------------------------------------------------- membrane mechanics
 template <class M>
 struct V3 {
@@ -208,27 +263,51 @@ __device__ __forceinline__ V3<M> cross3(V3<M> a, V3<M> b) {
     return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
 }
 
+// Element force consumers: AtomicSink accumulates every corner force into shared memory
+// (order of summation left to the hardware); GatherSink keeps the contributions to one
+// vertex, in the order the elements are visited (deterministic).
 template <class M>
-__device__ __forceinline__ void acc_force(M* sf, int v, V3<M> f) {
-    atomicAdd(sf + 3 * v, f.x);
-    atomicAdd(sf + 3 * v + 1, f.y);
-    atomicAdd(sf + 3 * v + 2, f.z);
-}
+struct AtomicSink {
+    M* sf;
+    __device__ __forceinline__ void operator()(int v, V3<M> f) const {
+        atomicAdd(sf + 3 * v, f.x);
+        atomicAdd(sf + 3 * v + 1, f.y);
+        atomicAdd(sf + 3 * v + 2, f.z);
+    }
+};
+template <class M>
+struct GatherSink {
+    int target;
+    V3<M> acc;
+    __device__ __forceinline__ void operator()(int v, V3<M> f) {
+        if (v == target) acc = acc + f;
+    }
+};
 
-// Vertex position relative to the particle's centre (exact FP64 subtraction, then
-// rounding to M), so FP32 element arithmetic works on O(radius) numbers.
+// Vertex positions as the element kernels see them.  GlobalPos reads the FP64 positions
+// (relative to c, exact FP64 subtraction, then rounding to M); SharedPos reads a copy of
+// the particle's relative positions staged in shared memory.
 template <class M>
-__device__ __forceinline__ V3<M> relpos(const double* pos, int v, const double* c) {
-    return mk3<M>((M)(pos[3 * v] - c[0]), (M)(pos[3 * v + 1] - c[1]), (M)(pos[3 * v + 2] - c[2]));
-}
+struct GlobalPos {
+    const double* pos;  // particle's first vertex
+    double c[3];
+    __device__ __forceinline__ V3<M> operator()(int v) const {
+        return mk3<M>((M)(pos[3 * v] - c[0]), (M)(pos[3 * v + 1] - c[1]), (M)(pos[3 * v + 2] - c[2]));
+    }
+};
+template <class M>
+struct SharedPos {
+    const M* sp;
+    __device__ __forceinline__ V3<M> operator()(int v) const { return mk3<M>(sp[3 * v], sp[3 * v + 1], sp[3 * v + 2]); }
+};
 
 // DeformableCapsuleParticle::compute_forces for one triangle, src/fsi/DeformableCapsule.hh:68-148
 // (with the reference's c = l' sin(phi) / (l' sin(phi0)), line 96).
-template <class M>
-__device__ void capsule_triangle(const ParticleDev& P, int t, const double* pos, const double* c0, int skalak, M* sf) {
+template <class M, class PS, class Sink>
+__device__ void capsule_triangle(const ParticleDev& P, int t, const PS& ps, int skalak, Sink& sk) {
     const int i0 = P.tri[3 * t], i1 = P.tri[3 * t + 1], i2 = P.tri[3 * t + 2];
     const int id[3] = {i0, i1, i2};
-    const V3<M> p0 = relpos<M>(pos, P.v0 + i0, c0), p1 = relpos<M>(pos, P.v0 + i1, c0), p2 = relpos<M>(pos, P.v0 + i2, c0);
+    const V3<M> p0 = ps(i0), p1 = ps(i1), p2 = ps(i2);
     const V3<M> e0 = p1 - p0, e1 = p2 - p0;
     const V3<M> e0_0 = mk3<M>((M)(P.rest[3 * i1] - P.rest[3 * i0]), (M)(P.rest[3 * i1 + 1] - P.rest[3 * i0 + 1]),
                               (M)(P.rest[3 * i1 + 2] - P.rest[3 * i0 + 2]));
@@ -270,14 +349,14 @@ __device__ void capsule_triangle(const ParticleDev& P, int t, const double* pos,
         V3<M> fv;
         if (skalak) fv = pref * ((I1 + M(1)) * gI1 + (Cc * I2 - M(1)) * gI2);
         else fv = pref * (gI1 - (M(1) / ((M(1) + I2) * (M(1) + I2))) * gI2);
-        acc_force(sf, id[i], fv);
+        sk(id[i], fv);
     }
 }
 
 // RBCParticle link term (WLC + POW), src/fsi/RBCParticle.hh:148-169 with
 // RBCParameters::in_plane_ks_kp (RBCParticle.hh:27-44), m = 2, x0 = 1/2.2.
-template <class M>
-__device__ void rbc_link(const ParticleDev& P, int l, const double* pos, const double* c0, M* sf) {
+template <class M, class PS, class Sink>
+__device__ void rbc_link(const ParticleDev& P, int l, const PS& ps, Sink& sk) {
     const double x0 = 1. / 2.2;
     const double ks_c1 = 0.25 * (6. * x0 + (3 * x0 * x0 - 2 * x0 * x0 * x0) / ((1 - x0) * (1 - x0)));
     const double ks_c2 = x0 / (2. * (1 - x0) * (1 - x0) * (1 - x0)) + 0.25 * (1. - 1. / ((1 - x0) * (1 - x0)));
@@ -287,24 +366,23 @@ __device__ void rbc_link(const ParticleDev& P, int l, const double* pos, const d
     const double den = ks_c1 * kp_c2 - ks_c2 * kp_c1;
     const M ks = (M)(-kp_c1 * G_lhs / den), kp = (M)(ks_c1 * G_lhs / den);
     const int a = P.links[2 * l], b = P.links[2 * l + 1];
-    const V3<M> dv = relpos<M>(pos, P.v0 + a, c0) - relpos<M>(pos, P.v0 + b, c0);
+    const V3<M> dv = ps(a) - ps(b);
     const M L = norm3(dv);
     const M x = L / (M)(l0 * 2.2);
     const M df = M(-0.25) * ks * (M(6) * x + (M(3) * x * x - M(2) * x * x * x) / ((M(1) - x) * (M(1) - x))) + kp / (L * L);
     const V3<M> fv = (df / L) * dv;
-    acc_force(sf, a, fv);
-    acc_force(sf, b, M(-1) * fv);
+    sk(a, fv);
+    sk(b, M(-1) * fv);
 }
 
 // RBCParticle triangle terms: global + local area and volume penalties,
 // src/fsi/RBCParticle.hh:175-213 with tri::triangle_area_and_gradient and
 // tri::grad_signed_volume (TriangleUtils.h:58-120).  The volume gradient is
 // translation invariant on a closed surface, so it is taken relative to the centre.
-template <class M>
-__device__ void rbc_triangle(const ParticleDev& P, int t, const double* pos, const double* c0, double area, double volume,
-                             M* sf) {
+template <class M, class PS, class Sink>
+__device__ void rbc_triangle(const ParticleDev& P, int t, const PS& ps, double area, double volume, Sink& sk) {
     const int i0 = P.tri[3 * t], i1 = P.tri[3 * t + 1], i2 = P.tri[3 * t + 2];
-    const V3<M> v0 = relpos<M>(pos, P.v0 + i0, c0), v1 = relpos<M>(pos, P.v0 + i1, c0), v2 = relpos<M>(pos, P.v0 + i2, c0);
+    const V3<M> v0 = ps(i0), v1 = ps(i1), v2 = ps(i2);
     const M v01v11 = v0.y - v1.y, v02v22 = v0.z - v2.z, v02v12 = v0.z - v1.z;
     const M v01v21 = v0.y - v2.y, v00v20 = v0.x - v2.x, v00v10 = v0.x - v1.x;
     const M a = v01v11 * v02v22 - v02v12 * v01v21;
@@ -322,22 +400,21 @@ __device__ void rbc_triangle(const ParticleDev& P, int t, const double* pos, con
     const double A0 = P.A0;
     M df_area = (M)(P.prm[BIB_P_K_AREA_GLOBAL] * (A0 - area) / A0);
     df_area += (M)P.prm[BIB_P_K_AREA_LOCAL] * ((M)P.tri_area[t] - la) / (M)P.tri_area[t];
-    acc_force(sf, i0, df_area * g0);
-    acc_force(sf, i1, df_area * g1);
-    acc_force(sf, i2, df_area * g2);
+    sk(i0, df_area * g0);
+    sk(i1, df_area * g1);
+    sk(i2, df_area * g2);
     const M df_vol = (M)(P.prm[BIB_P_K_VOLUME] * (P.prm[BIB_P_VOL_DESIRED] - volume) / P.prm[BIB_P_VOL_DESIRED]);
-    acc_force(sf, i0, (df_vol / M(6)) * cross3(v1, v2));
-    acc_force(sf, i1, (df_vol / M(6)) * cross3(v2, v0));
-    acc_force(sf, i2, (df_vol / M(6)) * cross3(v0, v1));
+    sk(i0, (df_vol / M(6)) * cross3(v1, v2));
+    sk(i1, (df_vol / M(6)) * cross3(v2, v0));
+    sk(i2, (df_vol / M(6)) * cross3(v0, v1));
 }
 
 // Dihedral bending of one adjacent-triangle pair, src/fsi/RBCParticle.hh:217-246 with
 // tri::grad_angle_between_pair (TriangleUtils.h:139-164).
-template <class M>
-__device__ void rbc_pair(const ParticleDev& P, int p, const double* pos, const double* c0, M* sf) {
+template <class M, class PS, class Sink>
+__device__ void rbc_pair(const ParticleDev& P, int p, const PS& ps, Sink& sk) {
     const int* q = P.pairs + 4 * p;
-    const V3<M> v0 = relpos<M>(pos, P.v0 + q[0], c0), v1 = relpos<M>(pos, P.v0 + q[1], c0);
-    const V3<M> v2 = relpos<M>(pos, P.v0 + q[2], c0), v3 = relpos<M>(pos, P.v0 + q[3], c0);
+    const V3<M> v0 = ps(q[0]), v1 = ps(q[1]), v2 = ps(q[2]), v3 = ps(q[3]);
     const V3<M> e0 = v1 - v0, e1 = v2 - v0, e2 = v3 - v0;
     const M e1n = norm3(e1);
     const V3<M> e1u = e1 / e1n;
@@ -347,10 +424,10 @@ __device__ void rbc_pair(const ParticleDev& P, int p, const double* pos, const d
     const M cos_t = dot3(n1u, n2u);
     const M sin_t = (dot3(n1 - n2, v1 - v3) > M(0) ? M(1) : M(-1)) * norm3(cross3(n1u, n2u));
     const M pref = (M)P.prm[BIB_P_K_BEND] * (-(M)P.pair_cs[2 * p] * sin_t + (M)P.pair_cs[2 * p + 1] * cos_t);
-    acc_force(sf, q[0], pref * ((dot3(e1u, e1 - e2) / n2n) * n2u + (dot3(e1u, e1 - e0) / n1n) * n1u));
-    acc_force(sf, q[1], pref * ((-e1n / n1n) * n1u));
-    acc_force(sf, q[2], pref * ((dot3(e1u, e2) / n2n) * n2u + (dot3(e1u, e0) / n1n) * n1u));
-    acc_force(sf, q[3], pref * ((-e1n / n2n) * n2u));
+    sk(q[0], pref * ((dot3(e1u, e1 - e2) / n2n) * n2u + (dot3(e1u, e1 - e0) / n1n) * n1u));
+    sk(q[1], pref * ((-e1n / n1n) * n1u));
+    sk(q[2], pref * ((dot3(e1u, e2) / n2n) * n2u + (dot3(e1u, e0) / n1n) * n1u));
+    sk(q[3], pref * ((-e1n / n2n) * n2u));
 }
 
 template <class T>
@@ -368,47 +445,104 @@ __device__ __forceinline__ T block_sum(T v, T* red) {
     return r;  // valid in thread 0
 }
 
-// One CTA per particle: forces at X_n (ParticleBase3D::reset_forces + compute_forces),
-// X_{n+1} = X_n + U_n (DeformableParticle3D::move_vertices, DeformableParticle3D.hh:26-51),
-// area / volume / area-weighted centre (update(), :54-82) and the periodic centre-of-mass
-// remap (ParticleBase3D::map_center_of_mass_to_periodic_grid, ParticleBase.hh:111-136).
+// One CTA per particle: vertex forces at X_n (ParticleBase3D::reset_forces +
+// compute_forces), accumulated in shared memory.
 template <class M>
-__global__ void __launch_bounds__(256) k_membrane(LatticeDesc d, const ParticleDev* __restrict__ parts,
-                                                   const double* __restrict__ pos, double* __restrict__ pos_next,
-                                                   const double* __restrict__ vel, double* __restrict__ force,
-                                                   double* __restrict__ stats) {
+__global__ void __launch_bounds__(256) k_membrane(const ParticleDev* __restrict__ parts, const double* __restrict__ pos,
+                                                   double* __restrict__ force, const double* __restrict__ stats) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     M* sf = reinterpret_cast<M*>(smem_raw);
+    const ParticleDev& P = parts[blockIdx.x];
+    const double* st = stats + STATS * blockIdx.x;
+    const double area = st[0], volume = st[1];
+    for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sf[i] = M(0);
+    // FP64 element arithmetic uses absolute positions as the reference does; reduced
+    // precision stages the positions relative to the centre of mass in shared memory
+    // (exact FP64 subtraction, then rounding) so the element loops read them from there.
+    const bool rel = sizeof(M) < sizeof(double);
+    M* sp = sf + 3 * P.nv;
+    if (rel) {
+        const double* pp = pos + 3LL * P.v0;
+        for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sp[i] = (M)(pp[i] - st[2 + i % 3]);
+    }
+    __syncthreads();
+    AtomicSink<M> sk{sf};
+    const int skalak = P.model != BIB_MODEL_CAPSULE_NEOHOOKEAN;
+    const bool capsule = P.model == BIB_MODEL_CAPSULE_NEOHOOKEAN || P.model == BIB_MODEL_CAPSULE_SKALAK ||
+                         P.model == BIB_MODEL_SKALAK_BENDING;
+    const bool rbc_terms = P.model == BIB_MODEL_RBC_WLCPOW || P.model == BIB_MODEL_SKALAK_BENDING;
+    auto run = [&](const auto& ps) {
+        if (capsule)
+            for (int t = threadIdx.x; t < P.nt; t += blockDim.x) capsule_triangle<M>(P, t, ps, skalak, sk);
+        if (P.model == BIB_MODEL_RBC_WLCPOW)
+            for (int l = threadIdx.x; l < P.nl; l += blockDim.x) rbc_link<M>(P, l, ps, sk);
+        if (rbc_terms) {
+            for (int t = threadIdx.x; t < P.nt; t += blockDim.x) rbc_triangle<M>(P, t, ps, area, volume, sk);
+            for (int p = threadIdx.x; p < P.np; p += blockDim.x) rbc_pair<M>(P, p, ps, sk);
+        }
+    };
+    if (rel) run(SharedPos<M>{sp});
+    else run(GlobalPos<M>{pos + 3LL * P.v0, {0.0, 0.0, 0.0}});
+    __syncthreads();
+    for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) force[3LL * P.v0 + i] = (double)sf[i];
+}
+
+// Deterministic membrane forces: one thread per vertex sums the contributions of its
+// incident links, triangles and adjacent-triangle pairs, visited in the order of the
+// reference's element loops (RBCParticle.hh:148-246: links, then triangles with the area
+// term before the volume term, then pairs).  Each incident element is evaluated once per
+// corner, so the element arithmetic is repeated 2-4 times; no atomics, bit-reproducible.
+// The Skalak + bending composite sums the capsule part and the RBC part separately, as
+// the reference does when both particle classes act on the same vertices.
+constexpr int INC_LINK = 0, INC_TRI = 1, INC_PAIR = 2;
+
+template <class M>
+__global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* __restrict__ vert_particle,
+                                                          const ParticleDev* __restrict__ parts,
+                                                          const double* __restrict__ pos, double* __restrict__ force,
+                                                          const double* __restrict__ stats) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nvert) return;
+    const int pid = vert_particle[g];
+    const ParticleDev& P = parts[pid];
+    const int lv = g - P.v0;
+    const double* st = stats + STATS * pid;
+    const double area = st[0], volume = st[1];
+    const bool rel = sizeof(M) < sizeof(double);
+    const GlobalPos<M> ps{pos + 3LL * P.v0, {rel ? st[2] : 0.0, rel ? st[3] : 0.0, rel ? st[4] : 0.0}};
+    const bool capsule = P.model == BIB_MODEL_CAPSULE_NEOHOOKEAN || P.model == BIB_MODEL_CAPSULE_SKALAK ||
+                         P.model == BIB_MODEL_SKALAK_BENDING;
+    const bool rbc_terms = P.model == BIB_MODEL_RBC_WLCPOW || P.model == BIB_MODEL_SKALAK_BENDING;
+    const int skalak = P.model != BIB_MODEL_CAPSULE_NEOHOOKEAN;
+    GatherSink<M> cap{lv, mk3<M>(0, 0, 0)}, rbc{lv, mk3<M>(0, 0, 0)};
+    for (int e = P.inc_off[lv]; e < P.inc_off[lv + 1]; ++e) {
+        const int code = P.inc[e];
+        const int type = code >> 29, id = code & ((1 << 29) - 1);
+        if (type == INC_LINK) {
+            if (P.model == BIB_MODEL_RBC_WLCPOW) rbc_link<M>(P, id, ps, rbc);
+        } else if (type == INC_TRI) {
+            if (capsule) capsule_triangle<M>(P, id, ps, skalak, cap);
+            if (rbc_terms) rbc_triangle<M>(P, id, ps, area, volume, rbc);
+        } else if (rbc_terms) {
+            rbc_pair<M>(P, id, ps, rbc);
+        }
+    }
+    V3<M> f = P.model == BIB_MODEL_SKALAK_BENDING ? cap.acc + rbc.acc : (capsule ? cap.acc : rbc.acc);
+    force[3LL * g] = (double)f.x;
+    force[3LL * g + 1] = (double)f.y;
+    force[3LL * g + 2] = (double)f.z;
+}
+
+// One CTA per particle: area, signed volume and area-weighted centroid of X_{n+1}
+// (DeformableParticle3D::update, DeformableParticle3D.hh:54-82), then the periodic
+// centre-of-mass remap (ParticleBase3D::map_center_of_mass_to_periodic_grid,
+// ParticleBase.hh:111-136), FP64.
+__global__ void __launch_bounds__(256) k_particle_update(LatticeDesc d, const ParticleDev* __restrict__ parts,
+                                                          double* __restrict__ pos_next, double* __restrict__ stats) {
     __shared__ double red[32];
-    __shared__ double com_new[3];
+    __shared__ double delta[3];
     const ParticleDev& P = parts[blockIdx.x];
     double* st = stats + STATS * blockIdx.x;
-    const double area = st[0], volume = st[1];
-    // FP64 element arithmetic uses absolute positions as the reference does; reduced
-    // precision works relative to the centre of mass.
-    const bool rel = sizeof(M) < sizeof(double);
-    const double c0[3] = {rel ? st[2] : 0.0, rel ? st[3] : 0.0, rel ? st[4] : 0.0};
-    for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sf[i] = M(0);
-    __syncthreads();
-    if (P.model == BIB_MODEL_CAPSULE_NEOHOOKEAN || P.model == BIB_MODEL_CAPSULE_SKALAK || P.model == BIB_MODEL_SKALAK_BENDING) {
-        const int skalak = P.model != BIB_MODEL_CAPSULE_NEOHOOKEAN;
-        for (int t = threadIdx.x; t < P.nt; t += blockDim.x) capsule_triangle<M>(P, t, pos, c0, skalak, sf);
-    }
-    if (P.model == BIB_MODEL_RBC_WLCPOW) {
-        for (int l = threadIdx.x; l < P.nl; l += blockDim.x) rbc_link<M>(P, l, pos, c0, sf);
-    }
-    if (P.model == BIB_MODEL_RBC_WLCPOW || P.model == BIB_MODEL_SKALAK_BENDING) {
-        for (int t = threadIdx.x; t < P.nt; t += blockDim.x) rbc_triangle<M>(P, t, pos, c0, area, volume, sf);
-        for (int p = threadIdx.x; p < P.np; p += blockDim.x) rbc_pair<M>(P, p, pos, c0, sf);
-    }
-    __syncthreads();
-    for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) {
-        const int64_t g = 3LL * P.v0 + i;
-        force[g] = (double)sf[i];
-        pos_next[g] = pos[g] + vel[g];
-    }
-    __syncthreads();
-    // update(): area, signed volume and area-weighted centroid of X_{n+1}
     double sa = 0, sv = 0, scx = 0, scy = 0, scz = 0;
     for (int t = threadIdx.x; t < P.nt; t += blockDim.x) {
         const double* a = pos_next + 3LL * (P.v0 + P.tri[3 * t]);
@@ -417,8 +551,10 @@ __global__ void __launch_bounds__(256) k_membrane(LatticeDesc d, const ParticleD
         const V3<double> A = mk3(a[0], a[1], a[2]), B = mk3(b[0], b[1], b[2]), Cv = mk3(c[0], c[1], c[2]);
         const double dA = norm3(cross3(B - A, Cv - A)) * 0.5;
         sa += dA;
-        sv += dot3(A, cross3(B, Cv)) / 6.;
-        const V3<double> cen = (A + B + Cv) / 3.0;
+        // multiplications by 1/6 and 1/3 instead of the reference's divisions (FP64 division
+        // is a long instruction sequence on this part); differences are within one ulp per term
+        sv += dot3(A, cross3(B, Cv)) * (1.0 / 6.0);
+        const V3<double> cen = (1.0 / 3.0) * (A + B + Cv);
         scx += cen.x * dA;
         scy += cen.y * dA;
         scz += cen.z * dA;
@@ -433,17 +569,14 @@ __global__ void __launch_bounds__(256) k_membrane(LatticeDesc d, const ParticleD
     __syncthreads();
     scz = block_sum(scz, red);
     if (threadIdx.x == 0) {
-        double com[3] = {scx / sa, scy / sa, scz / sa};
+        const double com[3] = {scx / sa, scy / sa, scz / sa};
         const int N[3] = {d.nx, d.ny, d.nz};
         const int per[3] = {d.px, d.py, d.pz};
         double np_[3];
         for (int a = 0; a < 3; ++a) {
             np_[a] = com[a];
-            if (per[a]) {
-                const double L = (double)N[a], Linv = 1. / L;
-                np_[a] = com[a] - L * floor((com[a] - (-0.5)) * Linv);
-            }
-            com_new[a] = np_[a] - com[a];  // delta
+            if (per[a]) np_[a] = com[a] - (double)N[a] * floor((com[a] - (-0.5)) * d.inv_n[a]);
+            delta[a] = np_[a] - com[a];
         }
         st[0] = sa;
         st[1] = sv;
@@ -452,12 +585,12 @@ __global__ void __launch_bounds__(256) k_membrane(LatticeDesc d, const ParticleD
         st[4] = np_[2];
     }
     __syncthreads();
-    if (com_new[0] != 0.0 || com_new[1] != 0.0 || com_new[2] != 0.0) {
+    if (delta[0] != 0.0 || delta[1] != 0.0 || delta[2] != 0.0) {
         for (int i = threadIdx.x; i < P.nv; i += blockDim.x) {
             const int64_t g = 3LL * (P.v0 + i);
-            pos_next[g] += com_new[0];
-            pos_next[g + 1] += com_new[1];
-            pos_next[g + 2] += com_new[2];
+            pos_next[g] += delta[0];
+            pos_next[g + 1] += delta[1];
+            pos_next[g + 2] += delta[2];
         }
     }
 }
@@ -466,38 +599,70 @@ __global__ void __launch_bounds__(256) k_membrane(LatticeDesc d, const ParticleD
 
 size_t membrane_smem_bytes(int max_nv) { return (size_t)3 * max_nv * sizeof(double); }
 
+size_t spread_sort_temp_bytes(int64_t nentries) {
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs((void*)nullptr, bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (uint32_t*)nullptr, (int)nentries, 0, 32);  // upper bound over the key widths
+    return bytes;
+}
+
 void configure_membrane_kernel(size_t smem) {
     cudaFuncSetAttribute(k_membrane<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_membrane<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
 }
 
-void launch_interpolate(const Lattice& L, cudaStream_t s) {
+void launch_interpolate_move(const Lattice& L, cudaStream_t s) {
     if (L.nvert == 0) return;
     const unsigned g = (L.nvert + 127) / 128;
-    const double* pos = L.pos[L.pcur];
     if (L.storage == BIB_STORAGE_F64)
-        k_interpolate<double><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, (const double*)L.f[L.cur], (const double*)L.F, L.vel);
-    else if (L.storage == BIB_STORAGE_F32)
-        k_interpolate<float><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, (const float*)L.f[L.cur], (const float*)L.F, L.vel);
+        k_interpolate_move<double><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, L.pos[L.pcur], L.pos[1 - L.pcur], (const double*)L.u, L.vel);
     else
-        k_interpolate<__half><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, (const __half*)L.f[L.cur], (const float*)L.F, L.vel);
+        k_interpolate_move<float><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, L.pos[L.pcur], L.pos[1 - L.pcur], (const float*)L.u, L.vel);
 }
 
-void launch_membrane(const Lattice& L, cudaStream_t s) {
+void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
     const int np = (int)L.parts.size();
     if (np == 0) return;
+    if (L.ib.spread_mode == BIB_SPREAD_DETERMINISTIC) {
+        const unsigned g = (L.nvert + 127) / 128;
+        if (L.storage == BIB_STORAGE_F64)
+            k_membrane_gather<double><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats);
+        else
+            k_membrane_gather<float><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats);
+        return;
+    }
     if (L.storage == BIB_STORAGE_F64)
-        k_membrane<double><<<np, 256, L.membrane_smem, s>>>(L.d, L.pdev, L.pos[L.pcur], L.pos[1 - L.pcur], L.vel, L.force, L.stats);
+        k_membrane<double><<<np, 256, L.membrane_smem, s>>>(L.pdev, L.pos[L.pcur], L.force, L.stats);
     else
-        k_membrane<float><<<np, 256, L.membrane_smem / 2, s>>>(L.d, L.pdev, L.pos[L.pcur], L.pos[1 - L.pcur], L.vel, L.force, L.stats);
+        k_membrane<float><<<np, 256, L.membrane_smem, s>>>(L.pdev, L.pos[L.pcur], L.force, L.stats);  // forces + staged positions
 }
 
-void launch_spread(const Lattice& L, cudaStream_t s) {
+void launch_particle_update(const Lattice& L, cudaStream_t s) {
+    const int np = (int)L.parts.size();
+    if (np == 0) return;
+    k_particle_update<<<np, 256, 0, s>>>(L.d, L.pdev, L.pos[1 - L.pcur], L.stats);
+}
+
+void launch_spread(const Lattice& L, int fbuf, cudaStream_t s) {
     if (L.nvert == 0) return;
     const unsigned g = (L.nvert + 127) / 128;
     const double* pos = L.pos[L.pcur];
-    if (L.storage == BIB_STORAGE_F64) k_spread<double><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, (double*)L.F);
-    else k_spread<float><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, (float*)L.F);
+    if (L.ib.spread_mode == BIB_SPREAD_DETERMINISTIC) {
+        const int sup = L.ib.dirac == BIB_DIRAC_PESKIN ? 4 : 3;
+        const int64_t ne = (int64_t)L.nvert * sup * sup * sup;
+        k_spread_keys<<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.sort_keys[0], L.sort_ids[0]);
+        size_t tb = L.sort_temp_bytes;
+        cub::DeviceRadixSort::SortPairs(L.sort_temp, tb, L.sort_keys[0], L.sort_keys[1], L.sort_ids[0], L.sort_ids[1],
+                                        (int)ne, 0, key_bits(L.d.n), s);
+        const unsigned ge = (unsigned)((ne + 127) / 128);
+        if (L.storage == BIB_STORAGE_F64)
+            k_spread_reduce<double><<<ge, 128, 0, s>>>(L.d, L.ib, ne, L.sort_keys[1], L.sort_ids[1], pos, L.force, (double*)L.F[fbuf]);
+        else
+            k_spread_reduce<float><<<ge, 128, 0, s>>>(L.d, L.ib, ne, L.sort_keys[1], L.sort_ids[1], pos, L.force, (float*)L.F[fbuf]);
+        return;
+    }
+    if (L.storage == BIB_STORAGE_F64) k_spread<double><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, (double*)L.F[fbuf]);
+    else k_spread<float><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, (float*)L.F[fbuf]);
 }
 
 }  // namespace bib

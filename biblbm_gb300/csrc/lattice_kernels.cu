@@ -1,12 +1,13 @@
-// Lattice kernels: fused collide-and-stream, finite-difference velocity walls,
-// velocity field, equilibrium initialisation and host-format conversion.
+// Lattice kernels: fused pull collide-and-stream (+ velocity field), finite-difference
+// velocity walls, state import / export and equilibrium initialisation.
 //
 // Data layout in HBM: one array per population (structure of arrays), x fastest,
-// cell k = x + nx*(y + ny*z), population i at f[i*stride + k].  The stored state is
-// post-streaming (Palabos semantics), so streaming is a push: a cell reads its own 19
-// populations (coalesced), collides in registers and writes each population into the
-// neighbour it moves to (x-shifted writes stay coalesced at sector level).
-#include <cstdio>
+// cell k = x + nx*(y + ny*z), population i at f[i*stride + k].  The buffers hold
+// post-collision populations f*(x); the post-streaming state (the reference's state
+// between steps) is gathered: f_i(x) = f*_i(x - c_i), periodic by index wrap, halfway
+// bounce-back f_i(x) = f*_opp(i)(x) + 6 t_i (c_i . u_wall) where x - c_i lies behind a
+// wall, and the nodes of finite-difference velocity walls read a separate wall buffer.
+#include <algorithm>
 
 #include "d3q19.cuh"
 
@@ -14,25 +15,110 @@ namespace bib {
 
 namespace {
 
+__device__ __forceinline__ bool fd_wall_node(const LatticeDesc& d, int y) { return d.fd_walls && (y == 0 || y == d.ny - 1); }
+
+__device__ __forceinline__ int64_t wall_index(const LatticeDesc& d, int side, int x, int z) {
+    return ((int64_t)side * d.nz + z) * d.nx + x;
+}
+__device__ __forceinline__ int64_t wall_stride(const LatticeDesc& d) { return 2LL * d.nz * d.nx; }
+
+// Source cell of population i arriving at (x, y, z).  Returns the cell index, or -1 if
+// the source lies behind a wall; `face` then tells which wall (0 y-, 1 y+, 2 z-, 3 z+).
+__device__ __forceinline__ int64_t source_cell(const LatticeDesc& d, int i, int x, int y, int z, int& face) {
+    int xs = x - cx(i), ys = y - cy(i), zs = z - cz(i);
+    face = -1;
+    xs = (int)wrap_index(xs, d.nx);
+    if (d.py) ys = (int)wrap_index(ys, d.ny);
+    else if (ys < 0 || ys >= d.ny) face = ys < 0 ? 0 : 1;
+    if (d.pz) zs = (int)wrap_index(zs, d.nz);
+    else if (face < 0 && (zs < 0 || zs >= d.nz)) face = zs < 0 ? 2 : 3;
+    if (face >= 0) return -1;
+    return xs + (int64_t)d.nx * (ys + (int64_t)d.ny * zs);
+}
+
+template <class C>
+__device__ __forceinline__ C moving_wall_term(const LatticeDesc& d, int i, int face) {
+    const C cu = C(cx(i)) * (C)d.wall_u[face][0] + C(cy(i)) * (C)d.wall_u[face][1] + C(cz(i)) * (C)d.wall_u[face][2];
+    return C(6) * weight<C>(i) * cu;
+}
+
+// Post-streaming populations of one cell.
 template <class T>
+__device__ __forceinline__ void gather(const LatticeDesc& d, const T* __restrict__ f, const T* __restrict__ wall, int x,
+                                       int y, int z, int64_t k, typename Store<T>::C* out) {
+    using C = typename Store<T>::C;
+    if (fd_wall_node(d, y)) {
+        const int64_t wk = wall_index(d, y == 0 ? 0 : 1, x, z), ws = wall_stride(d);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) out[i] = Store<T>::load(wall + i * ws + wk, d.inv_scale);
+        return;
+    }
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        int face;
+        const int64_t s = source_cell(d, i, x, y, z, face);
+        if (s >= 0) out[i] = Store<T>::load(f + i * d.stride + s, d.inv_scale);
+        else out[i] = Store<T>::load(f + opposite(i) * d.stride + k, d.inv_scale) + moving_wall_term<C>(d, i, face);
+    }
+}
+
+// Inverse of gather for a single population: where the value f_i(x) of a post-streaming
+// state has to be stored so that the next gather returns it.
+template <class T>
+__device__ __forceinline__ void scatter_canonical(const LatticeDesc& d, T* __restrict__ f, T* __restrict__ wall, int i, int x,
+                                                  int y, int z, int64_t k, double v) {
+    using C = typename Store<T>::C;
+    if (fd_wall_node(d, y)) {
+        Store<T>::store(wall + i * wall_stride(d) + wall_index(d, y == 0 ? 0 : 1, x, z), (C)v, d.scale);
+        return;
+    }
+    int face;
+    const int64_t s = source_cell(d, i, x, y, z, face);
+    if (s >= 0) Store<T>::store(f + i * d.stride + s, (C)v, d.scale);
+    else Store<T>::store(f + opposite(i) * d.stride + k, (C)v - moving_wall_term<C>(d, i, face), d.scale);
+}
+
+template <class T, bool COUPLED>
 __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* __restrict__ fin, T* __restrict__ fout,
-                                                         const typename Store<T>::F* __restrict__ F,
+                                                         const T* __restrict__ wall,
+                                                         const typename Store<T>::F* __restrict__ Fcol,
+                                                         typename Store<T>::F* __restrict__ Fprev,
+                                                         typename Store<T>::F* __restrict__ u_out,
                                                          const uint8_t* __restrict__ phase, int coll) {
     using C = typename Store<T>::C;
+    using FT = typename Store<T>::F;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= d.nx) return;
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
     C f[Q];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) f[i] = Store<T>::load(fin + i * d.stride + k, d.inv_scale);
-    C Fc[3];
-    Fc[0] = (C)__ldg(F + k);
-    Fc[1] = (C)__ldg(F + d.stride + k);
-    Fc[2] = (C)__ldg(F + 2 * d.stride + k);
-    C omega = (C)d.omega_c0;
-    if (d.use_phase && phase[k]) omega = (C)d.omega_c1;
+    gather<T>(d, fin, wall, x, y, z, k, f);
+    if (COUPLED) {
+        // computeVelocity of the current state (externalForceDynamics.hh:59-74; the wall
+        // nodes give their imposed velocity, boundaryDynamics.hh:316-322), with the force of
+        // the previous collision; that force buffer is then reset to the body force so the
+        // next step can spread into it (setExternalVector).
+        C u[3];
+        if (fd_wall_node(d, y)) {
+            const int side = y == 0 ? 0 : 1;
+            u[0] = (C)d.wall_u[side][0];
+            u[1] = (C)d.wall_u[side][1];
+            u[2] = (C)d.wall_u[side][2];
+        } else {
+            C Fp[3] = {(C)Fprev[k], (C)Fprev[d.stride + k], (C)Fprev[2 * d.stride + k]};
+            velocity_with_force(f, Fp, u);
+        }
+        u_out[k] = (FT)u[0];
+        u_out[d.stride + k] = (FT)u[1];
+        u_out[2 * d.stride + k] = (FT)u[2];
+        Fprev[k] = (FT)d.body[0];
+        Fprev[d.stride + k] = (FT)d.body[1];
+        Fprev[2 * d.stride + k] = (FT)d.body[2];
+    }
+    C Fc[3] = {(C)__ldg(Fcol + k), (C)__ldg(Fcol + d.stride + k), (C)__ldg(Fcol + 2 * d.stride + k)};
     if (coll == BIB_COLLISION_BGK_GUO_VOF) {
+        C omega = (C)d.omega_c0;
+        if (d.use_phase && phase[k]) omega = (C)d.omega_c1;
         collide<C, BIB_COLLISION_BGK_GUO_VOF>(f, Fc, omega, C(0));
     } else if (coll == BIB_COLLISION_BGK) {
         collide<C, BIB_COLLISION_BGK>(f, Fc, (C)d.omega, C(0));
@@ -42,39 +128,236 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
         collide<C, BIB_COLLISION_TRT>(f, Fc, om, omm);
     }
 #pragma unroll
-    for (int i = 0; i < Q; ++i) {
-        int xd = x + cx(i), yd = y + cy(i), zd = z + cz(i);
-        int face = -1;
-        if (d.px) xd = (int)wrap_index(xd, d.nx);
-        else if (xd < 0 || xd >= d.nx) face = 4;
-        if (d.py) yd = (int)wrap_index(yd, d.ny);
-        else if (yd < 0 || yd >= d.ny) face = yd < 0 ? 0 : 1;
-        if (d.pz) zd = (int)wrap_index(zd, d.nz);
-        else if (face < 0 && (zd < 0 || zd >= d.nz)) face = zd < 0 ? 2 : 3;
-        if (face < 0) {
-            const int64_t kd = xd + (int64_t)d.nx * (yd + (int64_t)d.ny * zd);
-            Store<T>::store(fout + i * d.stride + kd, f[i], d.scale);
-        } else {
-            // The population leaves the domain.  Halfway bounce-back returns it reversed
-            // to its own node with the moving-wall term -6 t_i (c_i . u_w) (rho_w = 1).
-            // FD velocity walls drop it: the wall processor rebuilds the wall node.
-            const int wall = face <= 1 ? d.wall_y : (face <= 3 ? d.wall_z : BIB_WALL_NONE);
-            if (wall == BIB_WALL_HALFWAY_BB) {
-                const C cu = C(cx(i)) * (C)d.wall_u[face][0] + C(cy(i)) * (C)d.wall_u[face][1] + C(cz(i)) * (C)d.wall_u[face][2];
-                Store<T>::store(fout + opposite(i) * d.stride + k, f[i] - C(6) * weight<C>(i) * cu, d.scale);
+    for (int i = 0; i < Q; ++i) Store<T>::store(fout + i * d.stride + k, f[i], d.scale);
+}
+
+// ---------------------------------------------------------------------------------------
+// Row-vectorised pull collide-and-stream (nx even).  A warp covers 64 consecutive cells of
+// one x-row, two per thread: every population is read as an aligned pair (half2 / float2 /
+// double2) from its source row, and the +-1 shift along x of the populations with
+// c_x != 0 is done with one warp shuffle (the lanes at the warp's ends fetch the missing
+// neighbour with a scalar load, wrapping periodically at the row ends).  The nine source
+// rows (y - c_y, z - c_z) are resolved once per thread.
+template <class T>
+struct Pair;
+template <>
+struct Pair<__half> {
+    static __device__ __forceinline__ void load(const __half* p, float inv, float& a, float& b) {
+        const float2 v = __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+        a = v.x * inv;
+        b = v.y * inv;
+    }
+    static __device__ __forceinline__ void store(__half* p, float a, float b, float s) {
+        *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a * s, b * s);
+    }
+    // scaled values as stored (f-bar * S)
+    static __device__ __forceinline__ void load_raw(const __half* p, float& a, float& b) {
+        const float2 v = __half22float2(__ldg(reinterpret_cast<const __half2*>(p)));
+        a = v.x;
+        b = v.y;
+    }
+    static __device__ __forceinline__ void store_raw(__half* p, float a, float b) {
+        *reinterpret_cast<__half2*>(p) = __floats2half2_rn(a, b);
+    }
+    static __device__ __forceinline__ float load1_raw(const __half* p) { return __half2float(__ldg(p)); }
+};
+template <>
+struct Pair<float> {
+    static __device__ __forceinline__ void load(const float* p, float, float& a, float& b) {
+        const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+        a = v.x;
+        b = v.y;
+    }
+    static __device__ __forceinline__ void store(float* p, float a, float b, float) {
+        *reinterpret_cast<float2*>(p) = make_float2(a, b);
+    }
+    static __device__ __forceinline__ void load_raw(const float* p, float& a, float& b) { load(p, 1.0f, a, b); }
+    static __device__ __forceinline__ void store_raw(float* p, float a, float b) { store(p, a, b, 1.0f); }
+    static __device__ __forceinline__ float load1_raw(const float* p) { return __ldg(p); }
+};
+template <>
+struct Pair<double> {
+    static __device__ __forceinline__ void load(const double* p, float, double& a, double& b) {
+        const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+        a = v.x;
+        b = v.y;
+    }
+    static __device__ __forceinline__ void store(double* p, double a, double b, float) {
+        *reinterpret_cast<double2*>(p) = make_double2(a, b);
+    }
+};
+
+template <class FT>
+__device__ __forceinline__ void load2(const FT* p, FT& a, FT& b);
+template <>
+__device__ __forceinline__ void load2<float>(const float* p, float& a, float& b) {
+    const float2 v = __ldg(reinterpret_cast<const float2*>(p));
+    a = v.x;
+    b = v.y;
+}
+template <>
+__device__ __forceinline__ void load2<double>(const double* p, double& a, double& b) {
+    const double2 v = __ldg(reinterpret_cast<const double2*>(p));
+    a = v.x;
+    b = v.y;
+}
+template <class FT>
+__device__ __forceinline__ void store2(FT* p, FT a, FT b);
+template <>
+__device__ __forceinline__ void store2<float>(float* p, float a, float b) {
+    *reinterpret_cast<float2*>(p) = make_float2(a, b);
+}
+template <>
+__device__ __forceinline__ void store2<double>(double* p, double a, double b) {
+    *reinterpret_cast<double2*>(p) = make_double2(a, b);
+}
+
+template <class T, bool COUPLED>
+__global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, const T* __restrict__ fin, T* __restrict__ fout,
+                                                              const T* __restrict__ wall,
+                                                              const typename Store<T>::F* __restrict__ Fcol,
+                                                              typename Store<T>::F* __restrict__ Fprev,
+                                                              typename Store<T>::F* __restrict__ u_out,
+                                                              const uint8_t* __restrict__ phase, int coll) {
+    using C = typename Store<T>::C;
+    using FT = typename Store<T>::F;
+    const unsigned FULL = 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int tx = blockIdx.x * blockDim.x + threadIdx.x;
+    const int row = blockIdx.y * blockDim.y + threadIdx.y;
+    if (row >= d.ny * d.nz) return;  // uniform per warp: a warp never spans two rows
+    const int y = row % d.ny, z = row / d.ny;
+    const int x0 = 2 * tx;
+    const bool active = x0 < d.nx;
+    const int64_t k0 = (int64_t)row * d.nx + x0;
+    const bool wallrow = fd_wall_node(d, y);
+    // ---- phase 1: issue every load of the cell pair before any shuffle or arithmetic, so
+    // that all of them are in flight together (the shuffles would otherwise serialise them)
+    C pa[Q], pb[Q], edge[Q];
+    FT fpa[3], fpb[3], fca[3], fcb[3];
+    int sface[3][3];
+    if (wallrow) {
+        const int64_t ws = wall_stride(d), wk = wall_index(d, y == 0 ? 0 : 1, active ? x0 : 0, z);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            pa[i] = pb[i] = edge[i] = C(0);
+            if (active) Pair<T>::load(wall + i * ws + wk, d.inv_scale, pa[i], pb[i]);
+        }
+    } else {
+        int64_t srow[3][3];
+#pragma unroll
+        for (int a = 0; a < 3; ++a)
+#pragma unroll
+            for (int b = 0; b < 3; ++b) {
+                int ys = y - (a - 1), zs = z - (b - 1), face = -1;
+                if (d.py) ys = (int)wrap_index(ys, d.ny);
+                else if (ys < 0 || ys >= d.ny) face = ys < 0 ? 0 : 1;
+                if (d.pz) zs = (int)wrap_index(zs, d.nz);
+                else if (face < 0 && (zs < 0 || zs >= d.nz)) face = zs < 0 ? 2 : 3;
+                sface[a][b] = face;
+                srow[a][b] = face >= 0 ? -1 : ((int64_t)ys + (int64_t)d.ny * zs) * d.nx;
+            }
+        const int xl = x0 == 0 ? d.nx - 1 : x0 - 1;            // left neighbour of the pair
+        const int xr = x0 + 2 >= d.nx ? x0 + 2 - d.nx : x0 + 2; // right neighbour of the pair
+        const bool need_l = active && lane == 0;
+        const bool need_r = active && (lane == 31 || x0 + 2 >= d.nx);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const int a = cy(i) + 1, b = cz(i) + 1;
+            pa[i] = pb[i] = edge[i] = C(0);
+            if (srow[a][b] < 0) {
+                // halfway bounce-back: the own node's opposite population, no shift in x
+                if (active) Pair<T>::load(fin + opposite(i) * d.stride + k0, d.inv_scale, pa[i], pb[i]);
+                continue;
+            }
+            const T* src = fin + i * d.stride + srow[a][b];
+            if (active) Pair<T>::load(src + x0, d.inv_scale, pa[i], pb[i]);
+            if (cx(i) == 1 && need_l) edge[i] = Store<T>::load(src + xl, d.inv_scale);
+            if (cx(i) == -1 && need_r) edge[i] = Store<T>::load(src + xr, d.inv_scale);
+        }
+    }
+    if (active) {
+        for (int c = 0; c < 3; ++c) load2<FT>(Fcol + c * d.stride + k0, fca[c], fcb[c]);
+        if (COUPLED && !wallrow)
+            for (int c = 0; c < 3; ++c) load2<FT>(Fprev + c * d.stride + k0, fpa[c], fpb[c]);
+    }
+    // ---- phase 2: assemble the gathered populations (x shifts through the warp)
+    C f0[Q], f1[Q];
+    if (wallrow) {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            f0[i] = pa[i];
+            f1[i] = pb[i];
+        }
+    } else {
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            const int a = cy(i) + 1, b = cz(i) + 1;
+            if (sface[a][b] >= 0) {
+                const C mw = moving_wall_term<C>(d, i, sface[a][b]);
+                f0[i] = pa[i] + mw;
+                f1[i] = pb[i] + mw;
+            } else if (cx(i) == 0) {
+                f0[i] = pa[i];
+                f1[i] = pb[i];
+            } else if (cx(i) == 1) {  // src[x0 - 1], src[x0]
+                const C left = __shfl_up_sync(FULL, pb[i], 1);
+                f0[i] = lane == 0 ? edge[i] : left;
+                f1[i] = pa[i];
+            } else {  // src[x0 + 1], src[x0 + 2]
+                const C right = __shfl_down_sync(FULL, pa[i], 1);
+                f0[i] = pb[i];
+                f1[i] = (lane == 31 || x0 + 2 >= d.nx) ? edge[i] : right;
             }
         }
     }
+    if (!active) return;
+    if (COUPLED) {
+        C u0[3], u1[3];
+        if (wallrow) {
+            const int side = y == 0 ? 0 : 1;
+            for (int c = 0; c < 3; ++c) u0[c] = u1[c] = (C)d.wall_u[side][c];
+        } else {
+            C Fa[3] = {(C)fpa[0], (C)fpa[1], (C)fpa[2]}, Fb[3] = {(C)fpb[0], (C)fpb[1], (C)fpb[2]};
+            velocity_with_force(f0, Fa, u0);
+            velocity_with_force(f1, Fb, u1);
+        }
+        for (int c = 0; c < 3; ++c) {
+            store2<FT>(u_out + c * d.stride + k0, (FT)u0[c], (FT)u1[c]);
+            store2<FT>(Fprev + c * d.stride + k0, (FT)d.body[c], (FT)d.body[c]);
+        }
+    }
+    C Fa[3] = {(C)fca[0], (C)fca[1], (C)fca[2]}, Fb[3] = {(C)fcb[0], (C)fcb[1], (C)fcb[2]};
+    if (coll == BIB_COLLISION_BGK_GUO_VOF) {
+        C om0 = (C)d.omega_c0, om1 = (C)d.omega_c0;
+        if (d.use_phase) {
+            if (phase[k0]) om0 = (C)d.omega_c1;
+            if (phase[k0 + 1]) om1 = (C)d.omega_c1;
+        }
+        collide<C, BIB_COLLISION_BGK_GUO_VOF>(f0, Fa, om0, C(0));
+        collide<C, BIB_COLLISION_BGK_GUO_VOF>(f1, Fb, om1, C(0));
+    } else if (coll == BIB_COLLISION_BGK) {
+        collide<C, BIB_COLLISION_BGK>(f0, Fa, (C)d.omega, C(0));
+        collide<C, BIB_COLLISION_BGK>(f1, Fb, (C)d.omega, C(0));
+    } else {
+        const C om = (C)d.omega;
+        const C omm = C(1) / ((C)d.trt_magic / (C(1) / om - C(0.5)) + C(0.5));
+        collide<C, BIB_COLLISION_TRT>(f0, Fa, om, omm);
+        collide<C, BIB_COLLISION_TRT>(f1, Fb, om, omm);
+    }
+#pragma unroll
+    for (int i = 0; i < Q; ++i) Pair<T>::store(fout + i * d.stride + k0, f0[i], f1[i], d.scale);
 }
 
-// PlaneFdBoundaryFunctional3D::processCell on the y walls,
+// PlaneFdBoundaryFunctional3D::processCell on the y walls after collide-and-stream,
 // src/boundaryCondition/finiteDifferenceBoundaryProcessor3D.hh:68-115: density from the
 // known populations (VelocityDirichletBoundaryDynamics::computeRhoBar,
 // boundaryDynamics.hh:631-663), one-sided normal velocity derivative
 // (finiteDifference3D.h:67-82; tangential derivatives vanish for a uniform wall
-// velocity), regularised reconstruction of all 19 populations.
+// velocity), regularised reconstruction of all 19 populations into the wall buffer.
 template <class T>
-__global__ void k_fd_walls(LatticeDesc d, T* __restrict__ f, const typename Store<T>::F* __restrict__ F) {
+__global__ void k_fd_walls(LatticeDesc d, const T* __restrict__ f, T* __restrict__ wall,
+                           const typename Store<T>::F* __restrict__ F) {
     using C = typename Store<T>::C;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int z = blockIdx.y;
@@ -83,13 +366,16 @@ __global__ void k_fd_walls(LatticeDesc d, T* __restrict__ f, const typename Stor
     const int y = side == 0 ? 0 : d.ny - 1;
     const int orientation = side == 0 ? -1 : 1;
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
-    const int64_t k1 = x + (int64_t)d.nx * (y - orientation + (int64_t)d.ny * z);
+    const int y1 = y - orientation;
+    const int64_t k1 = x + (int64_t)d.nx * (y1 + (int64_t)d.ny * z);
     C fc[Q], f1[Q];
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
-        fc[i] = Store<T>::load(f + i * d.stride + k, d.inv_scale);
-        f1[i] = Store<T>::load(f + i * d.stride + k1, d.inv_scale);
+        int face;
+        const int64_t s = source_cell(d, i, x, y, z, face);
+        fc[i] = s >= 0 ? Store<T>::load(f + i * d.stride + s, d.inv_scale) : C(0);  // unknown ones are not used
     }
+    gather<T>(d, f, wall, x, y1, z, k1, f1);
     const C Fy = (C)F[d.stride + k];
     C F1[3] = {(C)F[k1], (C)F[d.stride + k1], (C)F[2 * d.stride + k1]};
     const C uw[3] = {(C)d.wall_u[side][0], (C)d.wall_u[side][1], (C)d.wall_u[side][2]};
@@ -117,6 +403,7 @@ __global__ void k_fd_walls(LatticeDesc d, T* __restrict__ f, const typename Stor
     const C jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
     const C rhoBar = rho - C(1);
     const C invRho = C(1) / (rhoBar + C(1));
+    const int64_t wk = wall_index(d, side, x, z), ws = wall_stride(d);
 #pragma unroll
     for (int i = 0; i < Q; ++i) {
         // fromPiToFneq, src/latticeBoltzmann/offEquilibriumTemplates.h:91-115
@@ -130,63 +417,70 @@ __global__ void k_fd_walls(LatticeDesc d, T* __restrict__ f, const typename Stor
         fneq += pi[4] * C(2) * c1 * c2;
         fneq += pi[5] * (c2 * c2 - cs2);
         fneq *= weight<C>(i) * C(3) * C(3) / C(2);
-        Store<T>::store(f + i * d.stride + k, bgk_equilibrium<C>(i, rhoBar, invRho, j, jSqr) + fneq, d.scale);
+        Store<T>::store(wall + i * ws + wk, bgk_equilibrium<C>(i, rhoBar, invRho, j, jSqr) + fneq, d.scale);
     }
 }
 
-__device__ __forceinline__ bool is_fd_wall(const LatticeDesc& d, int y, int z) {
-    (void)z;
-    return !d.py && d.wall_y == BIB_WALL_FD_VELOCITY && (y == 0 || y == d.ny - 1);
-}
-
-template <class T>
-__global__ void k_velocity(LatticeDesc d, const T* __restrict__ f, const typename Store<T>::F* __restrict__ F,
-                           double* __restrict__ u) {
+// computeVelocity of the current state with the current external force F (wall nodes
+// give the wall velocity); OT = double for the host export, the compute type otherwise.
+template <class T, class OT>
+__global__ void k_velocity(LatticeDesc d, const T* __restrict__ f, const T* __restrict__ wall,
+                           const typename Store<T>::F* __restrict__ F, OT* __restrict__ u, int64_t ustride) {
     using C = typename Store<T>::C;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= d.nx) return;
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
-    if (is_fd_wall(d, y, z)) {
+    C uc[3];
+    if (fd_wall_node(d, y)) {
         const int side = y == 0 ? 0 : 1;
-        for (int a = 0; a < 3; ++a) u[a * d.n + k] = d.wall_u[side][a];
-        return;
+        for (int a = 0; a < 3; ++a) uc[a] = (C)d.wall_u[side][a];
+    } else {
+        C fc[Q];
+        gather<T>(d, f, wall, x, y, z, k, fc);
+        C Fc[3] = {(C)F[k], (C)F[d.stride + k], (C)F[2 * d.stride + k]};
+        velocity_with_force(fc, Fc, uc);
     }
-    C fc[Q], Fc[3], uc[3];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) fc[i] = Store<T>::load(f + i * d.stride + k, d.inv_scale);
-    for (int a = 0; a < 3; ++a) Fc[a] = (C)F[a * d.stride + k];
-    velocity_with_force(fc, Fc, uc);
-    for (int a = 0; a < 3; ++a) u[a * d.n + k] = (double)uc[a];
+    for (int a = 0; a < 3; ++a) u[a * ustride + k] = (OT)uc[a];
 }
 
 // iniCellAtEquilibrium, src/core/cell.hh:124-132
 template <class T>
-__global__ void k_init_eq(LatticeDesc d, T* __restrict__ f, const double* __restrict__ rho, const double* __restrict__ u) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= d.n) return;
+__global__ void k_init_eq(LatticeDesc d, T* __restrict__ f, T* __restrict__ wall, const double* __restrict__ rho,
+                          const double* __restrict__ u) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= d.nx) return;
+    const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
     const double r = rho ? rho[k] : 1.0;
     double j[3] = {u[k] * r, u[d.n + k] * r, u[2 * d.n + k] * r};
     const double jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
     const double rhoBar = r - 1.0;
     const double invRho = 1.0 / (rhoBar + 1.0);
 #pragma unroll
-    for (int i = 0; i < Q; ++i)
-        Store<T>::store(f + i * d.stride + k, (typename Store<T>::C)bgk_equilibrium<double>(i, rhoBar, invRho, j, jSqr), d.scale);
+    for (int i = 0; i < Q; ++i) scatter_canonical<T>(d, f, wall, i, x, y, z, k, bgk_equilibrium<double>(i, rhoBar, invRho, j, jSqr));
 }
 
 template <class T>
-__global__ void k_import(LatticeDesc d, T* __restrict__ f, const double* __restrict__ src) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= d.n) return;
-    for (int i = 0; i < Q; ++i) Store<T>::store(f + i * d.stride + k, (typename Store<T>::C)src[i * d.n + k], d.scale);
+__global__ void k_import(LatticeDesc d, T* __restrict__ f, T* __restrict__ wall, const double* __restrict__ src) {
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= d.nx) return;
+    const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+#pragma unroll
+    for (int i = 0; i < Q; ++i) scatter_canonical<T>(d, f, wall, i, x, y, z, k, src[i * d.n + k]);
 }
 
 template <class T>
-__global__ void k_export(LatticeDesc d, const T* __restrict__ f, double* __restrict__ dst) {
-    const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
-    if (k >= d.n) return;
-    for (int i = 0; i < Q; ++i) dst[i * d.n + k] = (double)Store<T>::load(f + i * d.stride + k, d.inv_scale);
+__global__ void k_export(LatticeDesc d, const T* __restrict__ f, const T* __restrict__ wall, double* __restrict__ dst) {
+    using C = typename Store<T>::C;
+    const int x = blockIdx.x * blockDim.x + threadIdx.x;
+    const int y = blockIdx.y, z = blockIdx.z;
+    if (x >= d.nx) return;
+    const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+    C fc[Q];
+    gather<T>(d, f, wall, x, y, z, k, fc);
+    for (int i = 0; i < Q; ++i) dst[i * d.n + k] = (double)fc[i];
 }
 
 template <class FT>
@@ -230,97 +524,149 @@ __global__ void k_nan_scan(LatticeDesc d, const T* __restrict__ f, int* flag) {
     if (bad) atomicOr(flag, 1);
 }
 
-inline dim3 row_grid(const LatticeDesc& d, int bx) { return dim3((d.nx + bx - 1) / bx, d.ny, d.nz); }
 inline int row_block(const LatticeDesc& d) { return d.nx >= 256 ? 256 : (d.nx >= 128 ? 128 : (d.nx >= 64 ? 64 : 32)); }
+inline dim3 row_grid(const LatticeDesc& d, int bx) { return dim3((d.nx + bx - 1) / bx, d.ny, d.nz); }
 inline unsigned lin_grid(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
 template <class T>
-void collide_stream_t(const Lattice& L, cudaStream_t s) {
-    const int bx = row_block(L.d);
+void collide_stream_t(const Lattice& L, bool coupled, cudaStream_t s) {
     using FT = typename Store<T>::F;
-    k_collide_stream<T><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (T*)L.f[1 - L.cur], (const FT*)L.F,
-                                                           L.phase, L.d.collision);
+    if (L.d.nx % 2 == 0) {
+        const int pairs = L.d.nx / 2;
+        const int bx = std::min(256, (pairs + 31) / 32 * 32);
+        const int by = std::max(1, 256 / bx);
+        const int rows = L.d.ny * L.d.nz;
+        dim3 grid((pairs + bx - 1) / bx, (rows + by - 1) / by);
+        dim3 block(bx, by);
+        const T* fin = (const T*)L.f[L.cur];
+        T* fout = (T*)L.f[1 - L.cur];
+        if (coupled)
+            k_collide_stream_rows<T, true><<<grid, block, 0, s>>>(L.d, fin, fout, (const T*)L.wall, (const FT*)L.F[1 - L.fe],
+                                                                  (FT*)L.F[L.fe], (FT*)L.u, L.phase, L.d.collision);
+        else
+            k_collide_stream_rows<T, false><<<grid, block, 0, s>>>(L.d, fin, fout, (const T*)L.wall, (const FT*)L.F[L.fe],
+                                                                   nullptr, nullptr, L.phase, L.d.collision);
+        return;
+    }
+    const int bx = row_block(L.d);
+    const T* fin = (const T*)L.f[L.cur];
+    T* fout = (T*)L.f[1 - L.cur];
+    const T* wall = (const T*)L.wall;
+    if (coupled) {
+        k_collide_stream<T, true><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, fin, fout, wall, (const FT*)L.F[1 - L.fe],
+                                                                    (FT*)L.F[L.fe], (FT*)L.u, L.phase, L.d.collision);
+    } else {
+        k_collide_stream<T, false><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, fin, fout, wall, (const FT*)L.F[L.fe], nullptr,
+                                                                     nullptr, L.phase, L.d.collision);
+    }
+}
+
+template <class T>
+void fd_walls_t(const Lattice& L, int buf, int fbuf, cudaStream_t s) {
+    using FT = typename Store<T>::F;
+    const int bx = row_block(L.d);
+    dim3 g((L.d.nx + bx - 1) / bx, L.d.nz, 2);
+    k_fd_walls<T><<<g, bx, 0, s>>>(L.d, (const T*)L.f[buf], (T*)L.wall, (const FT*)L.F[fbuf]);
+}
+
+#define BIB_DISPATCH(storage, FN, ...)                          \
+    do {                                                       \
+        if ((storage) == BIB_STORAGE_F64) FN<double>(__VA_ARGS__); \
+        else if ((storage) == BIB_STORAGE_F32) FN<float>(__VA_ARGS__); \
+        else FN<__half>(__VA_ARGS__);                          \
+    } while (0)
+
+template <class T>
+void velocity_field_t(const Lattice& L, cudaStream_t s) {
+    using FT = typename Store<T>::F;
+    const int bx = row_block(L.d);
+    k_velocity<T, FT><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall, (const FT*)L.F[L.fe],
+                                                        (FT*)L.u, L.d.stride);
+}
+
+template <class T>
+void velocity_export_t(const Lattice& L, double* u, cudaStream_t s) {
+    using FT = typename Store<T>::F;
+    const int bx = row_block(L.d);
+    k_velocity<T, double><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall,
+                                                            (const FT*)L.F[L.fe], u, L.d.n);
+}
+
+template <class T>
+void init_eq_t(const Lattice& L, const double* rho, const double* u, cudaStream_t s) {
+    const int bx = row_block(L.d);
+    k_init_eq<T><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (T*)L.f[L.cur], (T*)L.wall, rho, u);
+}
+
+template <class T>
+void import_t(const Lattice& L, const double* src, cudaStream_t s) {
+    const int bx = row_block(L.d);
+    k_import<T><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (T*)L.f[L.cur], (T*)L.wall, src);
+}
+
+template <class T>
+void export_t(const Lattice& L, double* dst, cudaStream_t s) {
+    const int bx = row_block(L.d);
+    k_export<T><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall, dst);
+}
+
+template <class T>
+void nan_scan_t(const Lattice& L, int* flag, cudaStream_t s) {
+    k_nan_scan<T><<<lin_grid(L.d.n, 256), 256, 0, s>>>(L.d, (const T*)L.f[L.cur], flag);
 }
 
 }  // namespace
 
-void launch_collide_stream(const Lattice& L, cudaStream_t s) {
-    if (L.storage == BIB_STORAGE_F64) collide_stream_t<double>(L, s);
-    else if (L.storage == BIB_STORAGE_F32) collide_stream_t<float>(L, s);
-    else collide_stream_t<__half>(L, s);
+void launch_collide_stream(const Lattice& L, bool coupled, cudaStream_t s) {
+    BIB_DISPATCH(L.storage, collide_stream_t, L, coupled, s);
 }
 
-void launch_fd_walls(const Lattice& L, void* f, cudaStream_t s) {
-    if (L.d.py || L.d.wall_y != BIB_WALL_FD_VELOCITY) return;
-    const int bx = row_block(L.d);
-    dim3 g((L.d.nx + bx - 1) / bx, L.d.nz, 2);
-    if (L.storage == BIB_STORAGE_F64) k_fd_walls<double><<<g, bx, 0, s>>>(L.d, (double*)f, (const double*)L.F);
-    else if (L.storage == BIB_STORAGE_F32) k_fd_walls<float><<<g, bx, 0, s>>>(L.d, (float*)f, (const float*)L.F);
-    else k_fd_walls<__half><<<g, bx, 0, s>>>(L.d, (__half*)f, (const float*)L.F);
+void launch_fd_walls(const Lattice& L, int buf, int fbuf, cudaStream_t s) {
+    if (!L.d.fd_walls) return;
+    BIB_DISPATCH(L.storage, fd_walls_t, L, buf, fbuf, s);
 }
 
-void launch_velocity(const Lattice& L, double* u, cudaStream_t s) {
-    const int bx = row_block(L.d);
-    const void* f = L.f[L.cur];
-    if (L.storage == BIB_STORAGE_F64) k_velocity<double><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const double*)f, (const double*)L.F, u);
-    else if (L.storage == BIB_STORAGE_F32) k_velocity<float><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const float*)f, (const float*)L.F, u);
-    else k_velocity<__half><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const __half*)f, (const float*)L.F, u);
+void launch_velocity_field(const Lattice& L, cudaStream_t s) { BIB_DISPATCH(L.storage, velocity_field_t, L, s); }
+
+void launch_velocity_export(const Lattice& L, double* u, cudaStream_t s) {
+    BIB_DISPATCH(L.storage, velocity_export_t, L, u, s);
 }
 
-void launch_init_equilibrium(const Lattice& L, void* f, const double* rho, const double* u, cudaStream_t s) {
+void launch_init_equilibrium(const Lattice& L, const double* rho, const double* u, cudaStream_t s) {
+    BIB_DISPATCH(L.storage, init_eq_t, L, rho, u, s);
+}
+
+void launch_import_soa(const Lattice& L, const double* src, cudaStream_t s) { BIB_DISPATCH(L.storage, import_t, L, src, s); }
+
+void launch_export_soa(const Lattice& L, double* dst, cudaStream_t s) { BIB_DISPATCH(L.storage, export_t, L, dst, s); }
+
+void launch_force_import(const Lattice& L, int buf, const double* src, cudaStream_t s) {
     const unsigned g = lin_grid(L.d.n, 256);
-    if (L.storage == BIB_STORAGE_F64) k_init_eq<double><<<g, 256, 0, s>>>(L.d, (double*)f, rho, u);
-    else if (L.storage == BIB_STORAGE_F32) k_init_eq<float><<<g, 256, 0, s>>>(L.d, (float*)f, rho, u);
-    else k_init_eq<__half><<<g, 256, 0, s>>>(L.d, (__half*)f, rho, u);
+    if (L.storage == BIB_STORAGE_F64) k_force_import<double><<<g, 256, 0, s>>>(L.d, (double*)L.F[buf], src);
+    else k_force_import<float><<<g, 256, 0, s>>>(L.d, (float*)L.F[buf], src);
 }
 
-void launch_import_soa(const Lattice& L, void* f, const double* src, cudaStream_t s) {
+void launch_force_export(const Lattice& L, int buf, double* dst, cudaStream_t s) {
     const unsigned g = lin_grid(L.d.n, 256);
-    if (L.storage == BIB_STORAGE_F64) k_import<double><<<g, 256, 0, s>>>(L.d, (double*)f, src);
-    else if (L.storage == BIB_STORAGE_F32) k_import<float><<<g, 256, 0, s>>>(L.d, (float*)f, src);
-    else k_import<__half><<<g, 256, 0, s>>>(L.d, (__half*)f, src);
+    if (L.storage == BIB_STORAGE_F64) k_force_export<double><<<g, 256, 0, s>>>(L.d, (const double*)L.F[buf], dst);
+    else k_force_export<float><<<g, 256, 0, s>>>(L.d, (const float*)L.F[buf], dst);
 }
 
-void launch_export_soa(const Lattice& L, const void* f, double* dst, cudaStream_t s) {
-    const unsigned g = lin_grid(L.d.n, 256);
-    if (L.storage == BIB_STORAGE_F64) k_export<double><<<g, 256, 0, s>>>(L.d, (const double*)f, dst);
-    else if (L.storage == BIB_STORAGE_F32) k_export<float><<<g, 256, 0, s>>>(L.d, (const float*)f, dst);
-    else k_export<__half><<<g, 256, 0, s>>>(L.d, (const __half*)f, dst);
-}
-
-void launch_force_import(const Lattice& L, const double* src, cudaStream_t s) {
-    const unsigned g = lin_grid(L.d.n, 256);
-    if (L.storage == BIB_STORAGE_F64) k_force_import<double><<<g, 256, 0, s>>>(L.d, (double*)L.F, src);
-    else k_force_import<float><<<g, 256, 0, s>>>(L.d, (float*)L.F, src);
-}
-
-void launch_force_export(const Lattice& L, double* dst, cudaStream_t s) {
-    const unsigned g = lin_grid(L.d.n, 256);
-    if (L.storage == BIB_STORAGE_F64) k_force_export<double><<<g, 256, 0, s>>>(L.d, (const double*)L.F, dst);
-    else k_force_export<float><<<g, 256, 0, s>>>(L.d, (const float*)L.F, dst);
-}
-
-void launch_force_fill(const Lattice& L, cudaStream_t s) {
+void launch_force_fill(const Lattice& L, int buf, cudaStream_t s) {
     const size_t fsz = L.storage == BIB_STORAGE_F64 ? sizeof(double) : sizeof(float);
     if (L.d.body[0] == 0.0 && L.d.body[1] == 0.0 && L.d.body[2] == 0.0) {
-        cudaMemsetAsync(L.F, 0, 3 * L.d.stride * fsz, s);
+        cudaMemsetAsync(L.F[buf], 0, 3 * L.d.stride * fsz, s);
         return;
     }
     const unsigned g = lin_grid(L.d.stride, 256);
-    if (L.storage == BIB_STORAGE_F64) k_force_fill<double><<<g, 256, 0, s>>>(L.d, (double*)L.F);
-    else k_force_fill<float><<<g, 256, 0, s>>>(L.d, (float*)L.F);
+    if (L.storage == BIB_STORAGE_F64) k_force_fill<double><<<g, 256, 0, s>>>(L.d, (double*)L.F[buf]);
+    else k_force_fill<float><<<g, 256, 0, s>>>(L.d, (float*)L.F[buf]);
 }
 
 void launch_phase_import(const Lattice& L, const double* src, cudaStream_t s) {
     k_phase_import<<<lin_grid(L.d.n, 256), 256, 0, s>>>(L.d, L.phase, src);
 }
 
-void launch_nan_scan(const Lattice& L, int* flag, cudaStream_t s) {
-    const unsigned g = lin_grid(L.d.n, 256);
-    const void* f = L.f[L.cur];
-    if (L.storage == BIB_STORAGE_F64) k_nan_scan<double><<<g, 256, 0, s>>>(L.d, (const double*)f, flag);
-    else if (L.storage == BIB_STORAGE_F32) k_nan_scan<float><<<g, 256, 0, s>>>(L.d, (const float*)f, flag);
-    else k_nan_scan<__half><<<g, 256, 0, s>>>(L.d, (const __half*)f, flag);
-}
+void launch_nan_scan(const Lattice& L, int* flag, cudaStream_t s) { BIB_DISPATCH(L.storage, nan_scan_t, L, flag, s); }
 
 }  // namespace bib

@@ -58,11 +58,15 @@ def _place_cells(rng, dims, rest, n_cells, margin, max_tries=20000):
             if v[:, 1].min() < lo[1] or v[:, 1].max() > hi[1] or v[:, 2].min() < lo[2] or v[:, 2].max() > hi[2]:
                 continue
             ok = True
-            for cj, Rj, vj in zip(centers, rots, verts):
+            near = []
+            if centers:
+                dc = c - np.asarray(centers)
+                dc[:, 0] -= nx * np.round(dc[:, 0] / nx)
+                near = np.nonzero(np.einsum("ij,ij->i", dc, dc) < (2.0 * R * 1.04) ** 2)[0]
+            for j in near:
+                cj, Rj, vj = centers[j], rots[j], verts[j]
                 d = c - cj
                 d[0] -= nx * np.round(d[0] / nx)
-                if np.dot(d, d) >= (2.0 * R * 1.04) ** 2:
-                    continue
                 shift = np.array([c[0] - cj[0] - d[0], 0.0, 0.0])
                 p = ((v - shift - cj) @ Rj) / scale
                 if (np.einsum("ij,ij->i", p, p) < 1.0).any():

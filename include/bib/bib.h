@@ -80,7 +80,13 @@ enum {
     BIB_MODEL_SKALAK_BENDING = 3      /* Skalak law + the RBC area / volume / bending terms */
 };
 enum { BIB_SPREAD_ATOMIC = 0, BIB_SPREAD_DETERMINISTIC = 1 };
-enum { BIB_LAYOUT_SOA_F64 = 0, BIB_LAYOUT_PALABOS_F64 = 1 };
+/* host layouts of bib_lattice_send / _receive:
+ *  SOA_F64         19 arrays of n doubles, x fastest (this library's order)
+ *  PALABOS_F64     Palabos static-cell wire order: x-major, z fastest, 23 doubles per cell
+ *                  (19 f-bar + 4 external scalars), blockLattice3D.hh:671-689
+ *  COPROCESSOR_F64 CoProcessor3D::send order: x-major, z fastest, 19 f-bar per cell
+ *                  (coProcessor3D.h:80-91) */
+enum { BIB_LAYOUT_SOA_F64 = 0, BIB_LAYOUT_PALABOS_F64 = 1, BIB_LAYOUT_COPROCESSOR_F64 = 2 };
 
 /* membrane parameter vector, 12 doubles */
 enum {
@@ -130,9 +136,8 @@ int32_t bib_abi_version(void);
 /* CoProcessor3D::addDomain(nx, ny, nz, omega, handle), coProcessor3D.h:69-74 */
 bib_status bib_lattice_add_domain(bib_ctx* ctx, int64_t nx, int64_t ny, int64_t nz, const bib_lattice_params* p,
                                   int32_t* handle);
-/* CoProcessor3D::send, coProcessor3D.h:75-84: whole-domain populations from the host.
- * layout BIB_LAYOUT_SOA_F64: 19*n doubles; BIB_LAYOUT_PALABOS_F64: Palabos static-cell
- * wire order (x-major, z fastest; 19 f-bar + 4 externals per cell, blockLattice3D.hh:671-689). */
+/* CoProcessor3D::send, coProcessor3D.h:75-91: whole-domain populations from the host in one of
+ * the BIB_LAYOUT_* orders (the PALABOS layout also sets the force and phase scalars). */
 bib_status bib_lattice_send(bib_ctx* ctx, int32_t h, const void* buf, size_t bytes, int32_t layout);
 /* CoProcessor3D::receive, coProcessor3D.h:85-93 */
 bib_status bib_lattice_receive(bib_ctx* ctx, int32_t h, void* buf, size_t bytes, int32_t layout);
@@ -185,7 +190,8 @@ bib_status bib_check_health(bib_ctx* ctx, int32_t h);
 
 /* ---- timing: per-kernel-group device time (ms) of the last bib_step call when profiling is on ---- */
 bib_status bib_set_profiling(bib_ctx* ctx, int32_t enabled);
-/* out[5] = {interpolate, forces+move, spread, collide+stream, walls}; cumulative since enabled */
+/* out[5] = {membrane forces, spreading, collide+stream, walls, interpolation+move+update};
+ * cumulative device milliseconds since profiling was enabled */
 bib_status bib_profile_read(bib_ctx* ctx, double* out, int32_t n);
 
 #ifdef __cplusplus

@@ -91,15 +91,57 @@ def test_palabos_layout_round_trip(ctx):
     assert np.array_equal(back[..., :22], wire[..., :22])
 
 
+@pytest.mark.parametrize("nx", [12, 11])  # even nx: row-vectorised kernel, odd nx: per-cell kernel
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_channel_bounce_back_against_oracle(ctx, nx, storage):
+    """Halfway bounce-back on y and z with moving walls, body force, random state."""
+    rng = np.random.default_rng(7)
+    ny, nz = 7, 6
+    wall_u = [[0.01, 0, 0.002], [-0.005, 0, 0], [0, 0.003, 0], [0.004, -0.002, 0]]
+    f0 = 1e-3 * rng.uniform(-1, 1, (19, nz, ny, nx))
+    F = 1e-4 * rng.uniform(-1, 1, (3, nz, ny, nx))
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 0), omega=1.3, wall_y="halfway_bb", wall_z="halfway_bb",
+                         wall_u=wall_u, storage=storage)
+    lat.send(f0)
+    lat.set_external_force(F)
+    lat.collide_and_stream(5)
+    L = O.lattice((nx, ny, nz), (1, 0, 0), "bgk_guo_vof", 1.3, 1.3, wall_y="halfway_bb", wall_z="halfway_bb",
+                  wall_u=wall_u)
+    ref = O.collide_stream(L, f0, F, None, 5)
+    tol = 1e-15 if storage == "f64" else 2e-8
+    assert np.abs(lat.receive() - ref).max() < tol
+    assert np.abs(lat.compute_velocity() - O.compute_velocity(L, ref, F)).max() < 50 * tol
+
+
+@pytest.mark.parametrize("storage,tol", [("f64", 1e-14), ("f32", 5e-6), ("f16", 2e-3)])
+def test_taylor_green_trt(ctx, storage, tol):
+    """TRT (magic 1/4) Taylor-Green decay: against the FP64 oracle and the analytic rate."""
+    from tests.test_oracle_analytic import tgv_state
+
+    n, u0, tau, steps = 32, 0.02, 0.8, 200
+    L = O.lattice((n, n, 4), (1, 1, 1), "trt", 1 / tau, trt_magic=0.25)
+    f0, k = tgv_state(n, u0, L)
+    lat = ctx.add_domain(n, n, 4, periodic=(1, 1, 1), collision="trt", omega=1 / tau, trt_magic=0.25, storage=storage)
+    lat.send(f0)
+    lat.collide_and_stream(steps)
+    ref = O.collide_stream(L, f0, None, None, steps)
+    u_gpu, u_ref = lat.compute_velocity(), O.compute_velocity(L, ref)
+    assert np.abs(u_gpu - u_ref).max() < tol * u0
+    nu = (tau - 0.5) / 3
+    expect = np.exp(-2 * nu * k * k * steps)
+    assert abs(np.abs(u_gpu[0]).max() / u0 - expect) / expect < 1.5e-2
+
+
 # ---------------------------------------------------------------- membranes
+@pytest.mark.parametrize("mode", ["atomic", "deterministic"])
 @pytest.mark.parametrize("model", ["capsule_neohookean", "capsule_skalak", "rbc_wlcpow", "skalak_bending"])
-def test_membrane_forces_match_reference(ctx, model):
+def test_membrane_forces_match_reference(ctx, model, mode):
     d = golden("forces_" + model)
     n = 40
     lat = ctx.add_domain(n, n, n, periodic=(1, 1, 1), omega=1.0)
     shapes = bib.ParticleShapeLibrary(ctx)
     sid = shapes.store_mesh(d["in_rest"], d["in_tri"], "m")
-    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes)
+    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes, spread=mode)
     pos = d["in_pos"] + np.array([15.0, 18.0, 12.0])  # inside the box, away from the faces
     pid = fsi.add_particle(sid, model, d["in_params"], pos)
     p0 = fsi.get_particle(pid)
@@ -111,7 +153,7 @@ def test_membrane_forces_match_reference(ctx, model):
 
 
 # ---------------------------------------------------------------- coupled steps
-def run_coupled_gpu(ctx, d, storage="f64", graph=True):
+def run_coupled_gpu(ctx, d, storage="f64", graph=True, spread="atomic"):
     nx, ny, nz = (int(v) for v in d["in_dims"])
     om = 1.0 / float(d["in_tau"])
     walls = int(d["in_walls"])
@@ -128,7 +170,7 @@ def run_coupled_gpu(ctx, d, storage="f64", graph=True):
         lat.initialize_at_equilibrium(None, np.zeros((3, nz, ny, nx)))
     shapes = bib.ParticleShapeLibrary(ctx)
     sid = shapes.store_mesh(d["in_rest"], d["in_tri"], "p")
-    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes)
+    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes, spread=spread)
     model = {0: "capsule_neohookean", 1: "capsule_skalak", 2: "rbc_wlcpow", 3: "skalak_bending"}[int(d["in_model"])]
     pid = fsi.add_particle(sid, model, d["in_params"], d["in_pos"])
     ctx.set_graph_mode(graph)
@@ -195,6 +237,23 @@ def test_capsule_in_shear_against_oracle(ctx, dirac):
     assert rel(g["pos"], r["pos"]) < 1e-13
     assert rel(g["force"], r["force"]) < 1e-8
     assert np.abs(lat.receive() - S.f).max() < 1e-13
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_deterministic_spreading(ctx, storage):
+    """Vertex-sorted spreading: identical bits on every run, equal to the atomic path to
+    rounding, and to the oracle."""
+    d = golden("ibm_rbc_periodic")
+    runs = []
+    for mode in ["deterministic", "deterministic", "atomic"]:
+        lat, fsi, pid = run_coupled_gpu(ctx, d, storage=storage, graph=True, spread=mode)
+        fsi.step(7)
+        runs.append((lat.receive(), fsi.get_particle(pid)["pos"], lat.get_external_force()))
+    assert np.array_equal(runs[0][0], runs[1][0]) and np.array_equal(runs[0][1], runs[1][1])
+    assert np.array_equal(runs[0][2], runs[1][2])
+    tol = 1e-15 if storage == "f64" else 1e-8
+    assert np.abs(runs[0][0] - runs[2][0]).max() < tol
+    assert rel(runs[0][1], runs[2][1]) < (1e-14 if storage == "f64" else 1e-7)
 
 
 # ---------------------------------------------------------------- reduced precision
