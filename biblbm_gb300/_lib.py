@@ -36,6 +36,10 @@ class IbParams(C.Structure):
     _fields_ = [("dirac", C.c_int32), ("spread_mode", C.c_int32), ("field_offset", C.c_double)]
 
 
+class Tuning(C.Structure):
+    _fields_ = [("collide_kernel", C.c_int32), ("tile_cells", C.c_int32), ("reserved", C.c_int32 * 6)]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_int32)]
 
@@ -77,6 +81,7 @@ SIGNATURES = {
     "bib_step": (C.c_int32, [_vp, C.c_int32, C.c_int64]),
     "bib_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),
     "bib_check_health": (C.c_int32, [_vp, C.c_int32]),
+    "bib_lattice_set_tuning": (C.c_int32, [_vp, C.c_int32, C.POINTER(Tuning)]),
 }
 
 _lib = None

@@ -16,7 +16,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import BibError, IbParams, LatticeParams
+from ._lib import BibError, IbParams, LatticeParams, Tuning
 
 STORAGE = {"f64": 0, "f32": 1, "f16": 2}
 COLLISION = {"bgk_guo_vof": 0, "bgk": 1, "trt": 2}
@@ -25,6 +25,7 @@ DIRAC = {"roma": 0, "peskin": 1}
 MODEL = {"capsule_neohookean": 0, "capsule_skalak": 1, "rbc_wlcpow": 2, "skalak_bending": 3}
 LAYOUT = {"soa": 0, "palabos": 1, "coprocessor": 2}
 SPREAD = {"atomic": 0, "deterministic": 1}
+KERNEL = {"auto": 0, "rows": 1, "staged": 2}
 PARAM_KEYS = ["G", "C", "nu_s", "kb", "shear_modulus", "L0", "k_area_global", "k_area_local",
               "k_volume", "vol_desired", "k_bend", "theta0"]
 Q = 19
@@ -201,6 +202,13 @@ class Lattice:
 
     def check_health(self):
         self.ctx.check(self.ctx.lib.bib_check_health(self.ctx.h, self.h))
+
+    def set_tuning(self, kernel="auto", tile_cells=0):
+        """Collide-and-stream kernel ("auto", "rows" or "staged") and staged tile size in cells."""
+        t = Tuning()
+        t.collide_kernel = KERNEL[kernel]
+        t.tile_cells = int(tile_cells)
+        self.ctx.check(self.ctx.lib.bib_lattice_set_tuning(self.ctx.h, self.h, C.byref(t)))
 
 
 class ParticleShapeLibrary:

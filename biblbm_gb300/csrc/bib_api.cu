@@ -558,7 +558,9 @@ bib_status bib_create(const bib_config* cfg, bib_ctx** out) {
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_flag, sizeof(int));
+    // d_flag[0]: NaN scan result, d_flag[1]: set by a bounded device wait that gave up
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_flag, 2 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_flag, 0, 2 * sizeof(int));
     if (e != cudaSuccess) {
         delete c;
         return BIB_ECUDA;
@@ -620,6 +622,23 @@ size_t bib_last_error(const bib_ctx* c, char* buf, size_t len) {
 bib_status bib_set_graph_mode(bib_ctx* c, int32_t enabled) {
     if (!c) return BIB_EINVAL;
     c->graph_mode = enabled != 0;
+    return BIB_OK;
+}
+
+bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !t) return fail(c, BIB_EINVAL, "invalid lattice handle or tuning");
+    if (t->collide_kernel < BIB_KERNEL_AUTO || t->collide_kernel > BIB_KERNEL_STAGED || t->tile_cells < 0)
+        return fail(c, BIB_EINVAL, "invalid tuning values");
+    Lattice probe = {};
+    probe.d = L->d;
+    probe.storage = L->storage;
+    probe.tile_cells = t->tile_cells;
+    if (t->collide_kernel == BIB_KERNEL_STAGED && !collide_staged_fits(probe))
+        return fail(c, BIB_EUNSUPPORTED, "the staged collide-and-stream kernel does not fit this lattice / tile size");
+    drop_graphs(c, h);
+    L->collide_kernel = t->collide_kernel;
+    L->tile_cells = t->tile_cells;
     return BIB_OK;
 }
 
@@ -709,6 +728,7 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
     BIB_CHECK_LAUNCH(c);
     *handle = (int32_t)c->lattices.size();
     L->handle = *handle;
+    L->wait_err = c->d_flag + 1;
     c->lattices.push_back(std::move(L));
     return BIB_OK;
 }
@@ -1098,10 +1118,14 @@ bib_status bib_check_health(bib_ctx* c, int32_t h) {
     BIB_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
     launch_nan_scan(*L, c->d_flag, c->stream);
     BIB_CHECK_LAUNCH(c);
-    int flag = 0;
-    BIB_CUDA(c, cudaMemcpyAsync(&flag, c->d_flag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    int flag[2] = {0, 0};
+    BIB_CUDA(c, cudaMemcpyAsync(flag, c->d_flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
-    if (flag) return fail(c, BIB_ENAN, "populations contain NaN or Inf");
+    if (flag[1]) {
+        BIB_CUDA(c, cudaMemsetAsync(c->d_flag + 1, 0, sizeof(int), c->stream));
+        return fail(c, BIB_ETIMEOUT, "a bounded device wait gave up; the results of that step are invalid");
+    }
+    if (flag[0]) return fail(c, BIB_ENAN, "populations contain NaN or Inf");
     if (!L->particles_dirty && L->nvert) {
         std::vector<double> pos(3 * (size_t)L->nvert);
         BIB_CUDA(c, cudaMemcpy(pos.data(), L->pos[L->pcur], pos.size() * 8, cudaMemcpyDeviceToHost));

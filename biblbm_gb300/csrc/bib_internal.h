@@ -132,6 +132,10 @@ struct Lattice {
     uint32_t* sort_ids[2] = {nullptr, nullptr};
     void* sort_temp = nullptr;
     size_t sort_temp_bytes = 0;
+    // collide-and-stream kernel selection (BIB_KERNEL_*) and staged tile size (0 = default)
+    int collide_kernel = BIB_KERNEL_AUTO;
+    int tile_cells = 0;
+    int* wait_err = nullptr;  // device word set by a bounded device wait that gave up
     int handle = -1;
 };
 
@@ -139,6 +143,9 @@ struct Lattice {
 // coupled = true: velocity output, collision with the spread force F[1-fe], F[fe] reset
 // to the body force afterwards.  coupled = false: collision with F[fe], no side outputs.
 void launch_collide_stream(const Lattice& L, bool coupled, cudaStream_t s);
+// shared-memory staged variant (collide_staged.cu); false if the lattice shape does not fit it
+bool launch_collide_stream_staged(const Lattice& L, bool coupled, cudaStream_t s);
+bool collide_staged_fits(const Lattice& L);  // both step kinds fit the staged kernel
 void launch_fd_walls(const Lattice& L, int buf, int fbuf, cudaStream_t s);
 void launch_velocity_field(const Lattice& L, cudaStream_t s);  // u from the current state and F[fe]
 void launch_velocity_export(const Lattice& L, double* u, cudaStream_t s);

@@ -86,6 +86,9 @@ enum { BIB_SPREAD_ATOMIC = 0, BIB_SPREAD_DETERMINISTIC = 1 };
  *                  (19 f-bar + 4 external scalars), blockLattice3D.hh:671-689
  *  COPROCESSOR_F64 CoProcessor3D::send order: x-major, z fastest, 19 f-bar per cell
  *                  (coProcessor3D.h:80-91) */
+/* collide-and-stream kernel choice (no reference counterpart: a GPU tuning knob) */
+enum { BIB_KERNEL_AUTO = 0, BIB_KERNEL_ROWS = 1, BIB_KERNEL_STAGED = 2 };
+
 enum { BIB_LAYOUT_SOA_F64 = 0, BIB_LAYOUT_PALABOS_F64 = 1, BIB_LAYOUT_COPROCESSOR_F64 = 2 };
 
 /* membrane parameter vector, 12 doubles */
@@ -123,6 +126,12 @@ typedef struct {
     int32_t spread_mode;  /* BIB_SPREAD_* */
     double field_offset;  /* location of the velocity field of the reference's data processor: -1 */
 } bib_ib_params;
+
+typedef struct {
+    int32_t collide_kernel; /* BIB_KERNEL_*: AUTO takes the shared-memory staged kernel where the x-row fits */
+    int32_t tile_cells;     /* staged kernel: cells per tile (whole x-rows); 0 = 512 (256 for FP64) */
+    int32_t reserved[6];
+} bib_tuning;
 
 /* ---- context (src/coProcessors/coProcessor3D.h:57-115 lifetime) ---- */
 bib_status bib_create(const bib_config* cfg, bib_ctx** out);
@@ -185,8 +194,12 @@ bib_status bib_step(bib_ctx* ctx, int32_t h, int64_t nsteps);
 bib_status bib_step_timed(bib_ctx* ctx, int32_t h, int64_t nsteps, double* ms);
 /* stream the context's work into CUDA-graph replays (1) or plain launches (0) */
 bib_status bib_set_graph_mode(bib_ctx* ctx, int32_t enabled);
-/* scan populations and vertex positions for NaN / Inf: BIB_OK or BIB_ENAN */
+/* scan populations and vertex positions for NaN / Inf: BIB_OK or BIB_ENAN; BIB_ETIMEOUT if a
+ * bounded device wait of an earlier step gave up (the flag is cleared by the call) */
 bib_status bib_check_health(bib_ctx* ctx, int32_t h);
+/* kernel selection and tile size of the collide-and-stream step (no reference counterpart);
+ * BIB_EUNSUPPORTED if BIB_KERNEL_STAGED is forced on a lattice whose x-rows do not fit it */
+bib_status bib_lattice_set_tuning(bib_ctx* ctx, int32_t h, const bib_tuning* t);
 
 /* ---- timing: per-kernel-group device time (ms) of the last bib_step call when profiling is on ---- */
 bib_status bib_set_profiling(bib_ctx* ctx, int32_t enabled);

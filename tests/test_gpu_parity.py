@@ -28,6 +28,11 @@ def rel(a, b):
     return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
 
 
+# collide-and-stream kernels: shared-memory staged (default where the x-row fits) and
+# row-vectorised; odd nx runs the per-cell kernel
+KERNELS = ["staged", "rows"]
+
+
 def shear_state(L, U):
     nx, ny, nz = L.nx, L.ny, L.nz
     y = np.arange(ny)
@@ -58,13 +63,15 @@ def test_periodic_collide_stream_matches_oracle(ctx):
     assert np.abs(lat.receive() - ref3).max() < 1e-14
 
 
-def test_shear_walls_match_reference(ctx):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_shear_walls_match_reference(ctx, kernel):
     d = golden("lbm_shear")
     nx, ny, nz = (int(v) for v in d["in_dims"])
     om = d["in_omega"]
     U = float(d["in_U"])
     wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
     lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 1), omega=om[0], wall_y="fd_velocity", wall_u=wall_u)
+    lat.set_tuning(kernel)
     L = O.lattice((nx, ny, nz), (1, 0, 1), "bgk_guo_vof", om[0], om[1], wall_y="fd_velocity", wall_u=wall_u)
     lat.initialize_at_equilibrium(None, shear_state(L, U))
     assert np.abs(lat.receive() - d["out_fbar_0"]).max() < 1e-16
@@ -91,9 +98,9 @@ def test_palabos_layout_round_trip(ctx):
     assert np.array_equal(back[..., :22], wire[..., :22])
 
 
-@pytest.mark.parametrize("nx", [12, 11])  # even nx: row-vectorised kernel, odd nx: per-cell kernel
-@pytest.mark.parametrize("storage", ["f64", "f32"])
-def test_channel_bounce_back_against_oracle(ctx, nx, storage):
+@pytest.mark.parametrize("nx,kernel", [(16, "staged"), (16, "rows"), (11, "auto")])
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16"])
+def test_channel_bounce_back_against_oracle(ctx, nx, kernel, storage):
     """Halfway bounce-back on y and z with moving walls, body force, random state."""
     rng = np.random.default_rng(7)
     ny, nz = 7, 6
@@ -102,19 +109,22 @@ def test_channel_bounce_back_against_oracle(ctx, nx, storage):
     F = 1e-4 * rng.uniform(-1, 1, (3, nz, ny, nx))
     lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 0), omega=1.3, wall_y="halfway_bb", wall_z="halfway_bb",
                          wall_u=wall_u, storage=storage)
+    if kernel != "auto":
+        lat.set_tuning(kernel)
     lat.send(f0)
     lat.set_external_force(F)
     lat.collide_and_stream(5)
     L = O.lattice((nx, ny, nz), (1, 0, 0), "bgk_guo_vof", 1.3, 1.3, wall_y="halfway_bb", wall_z="halfway_bb",
                   wall_u=wall_u)
     ref = O.collide_stream(L, f0, F, None, 5)
-    tol = 1e-15 if storage == "f64" else 2e-8
+    tol = {"f64": 1e-15, "f32": 2e-8, "f16": 1e-5}[storage]
     assert np.abs(lat.receive() - ref).max() < tol
     assert np.abs(lat.compute_velocity() - O.compute_velocity(L, ref, F)).max() < 50 * tol
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
 @pytest.mark.parametrize("storage,tol", [("f64", 1e-14), ("f32", 5e-6), ("f16", 2e-3)])
-def test_taylor_green_trt(ctx, storage, tol):
+def test_taylor_green_trt(ctx, storage, tol, kernel):
     """TRT (magic 1/4) Taylor-Green decay: against the FP64 oracle and the analytic rate."""
     from tests.test_oracle_analytic import tgv_state
 
@@ -122,6 +132,7 @@ def test_taylor_green_trt(ctx, storage, tol):
     L = O.lattice((n, n, 4), (1, 1, 1), "trt", 1 / tau, trt_magic=0.25)
     f0, k = tgv_state(n, u0, L)
     lat = ctx.add_domain(n, n, 4, periodic=(1, 1, 1), collision="trt", omega=1 / tau, trt_magic=0.25, storage=storage)
+    lat.set_tuning(kernel)
     lat.send(f0)
     lat.collide_and_stream(steps)
     ref = O.collide_stream(L, f0, None, None, steps)
@@ -153,7 +164,7 @@ def test_membrane_forces_match_reference(ctx, model, mode):
 
 
 # ---------------------------------------------------------------- coupled steps
-def run_coupled_gpu(ctx, d, storage="f64", graph=True, spread="atomic"):
+def run_coupled_gpu(ctx, d, storage="f64", graph=True, spread="atomic", kernel="auto"):
     nx, ny, nz = (int(v) for v in d["in_dims"])
     om = 1.0 / float(d["in_tau"])
     walls = int(d["in_walls"])
@@ -168,6 +179,7 @@ def run_coupled_gpu(ctx, d, storage="f64", graph=True, spread="atomic"):
     else:
         lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=om, storage=storage, body_force=body)
         lat.initialize_at_equilibrium(None, np.zeros((3, nz, ny, nx)))
+    lat.set_tuning(kernel)
     shapes = bib.ParticleShapeLibrary(ctx)
     sid = shapes.store_mesh(d["in_rest"], d["in_tri"], "p")
     fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes, spread=spread)
@@ -178,9 +190,10 @@ def run_coupled_gpu(ctx, d, storage="f64", graph=True, spread="atomic"):
 
 
 @pytest.mark.parametrize("name", ["ibm_capsule_shear", "ibm_rbc_periodic"])
-def test_coupled_steps_match_reference(ctx, name):
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_coupled_steps_match_reference(ctx, name, kernel):
     d = golden(name)
-    lat, fsi, pid = run_coupled_gpu(ctx, d, graph=False)
+    lat, fsi, pid = run_coupled_gpu(ctx, d, graph=False, kernel=kernel)
     steps = int(d["in_steps"])
     fscale = np.abs(d["out_force"]).max()  # the first steps start stress-free (forces ~1e-17)
     for it in range(steps):
@@ -195,6 +208,64 @@ def test_coupled_steps_match_reference(ctx, name):
             assert np.abs(lat.get_external_force() - d["out_force_spread"]).max() < 1e-15
     assert np.abs(lat.compute_velocity() - d["out_u_end"]).max() < 1e-14
     assert rel(fsi.get_particle(pid)["inertia"], d["out_inertia"][-1]) < 1e-12
+
+
+def random_channel(nx, ny, nz, seed=11):
+    rng = np.random.default_rng(seed)
+    f0 = 1e-3 * rng.uniform(-1, 1, (19, nz, ny, nx))
+    F = 1e-4 * rng.uniform(-1, 1, (3, nz, ny, nx))
+    phase = (rng.uniform(size=(nz, ny, nx)) < 0.3).astype(np.float64)
+    return f0, F, phase
+
+
+@pytest.mark.parametrize("storage,tol", [("f64", 1e-15), ("f32", 2e-8), ("f16", 1e-5)])
+def test_staged_pipeline_many_tiles(ctx, storage, tol):
+    """Thousands of one-row tiles per launch: every CTA runs the double-buffered pipeline
+    through many tiles.  Periodic y, moving halfway walls on z, phase field, body force."""
+    nx, ny, nz = 32, 64, 48
+    f0, F, phase = random_channel(nx, ny, nz)
+    wall_u = [[0, 0, 0], [0, 0, 0], [0.003, 0, 0.001], [-0.002, 0.001, 0]]
+    kw = dict(periodic=(1, 1, 0), omega=1.3, omega_inner=0.9, use_phase=True, wall_z="halfway_bb", wall_u=wall_u)
+    lat = ctx.add_domain(nx, ny, nz, storage=storage, **kw)
+    lat.set_tuning("staged", tile_cells=nx)
+    lat.send(f0)
+    lat.set_external_force(F)
+    lat.set_phase(phase)
+    lat.collide_and_stream(3)
+    L = O.lattice((nx, ny, nz), (1, 1, 0), "bgk_guo_vof", 1.3, 0.9, wall_z="halfway_bb", wall_u=wall_u)
+    ref = O.collide_stream(L, f0, F, phase, 3)
+    assert np.abs(lat.receive() - ref).max() < tol
+    lat.check_health()
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32", "f16"])
+@pytest.mark.parametrize("tile_cells", [32, 160, 0])
+def test_staged_coupled_step_equals_rows_kernel(ctx, storage, tile_cells):
+    """Coupled lattice step (velocity output, force reset, body force) of the staged kernel
+    against the row-vectorised kernel, on 1-, 5- and 16-row tiles."""
+    nx, ny, nz = 32, 80, 24
+    f0, F, phase = random_channel(nx, ny, nz, seed=5)
+    out = {}
+    for kernel in ("rows", "staged"):
+        lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 0), omega=1.1, wall_y="halfway_bb", wall_z="halfway_bb",
+                             storage=storage, body_force=(1e-5, -2e-6, 0))
+        lat.set_tuning(kernel, tile_cells=tile_cells)
+        lat.send(f0)
+        lat.set_external_force(F)
+        fsi = bib.ImmersedBoundaryDynamics3D(lat, bib.ParticleShapeLibrary(ctx))
+        fsi.step(4)
+        out[kernel] = (lat.receive(), lat.compute_velocity(), lat.get_external_force())
+    tol = {"f64": 1e-16, "f32": 2e-9, "f16": 5e-6}[storage]
+    for a, b in zip(out["rows"], out["staged"]):
+        assert np.abs(a - b).max() < tol
+
+
+def test_staged_kernel_rejects_misfit_rows(ctx):
+    lat = ctx.add_domain(12, 8, 8, periodic=(1, 1, 1), omega=1.0, storage="f16")  # 24-byte rows
+    with pytest.raises(bib.BibError):
+        lat.set_tuning("staged")
+    lat.set_tuning("auto")
+    lat.collide_and_stream(1)
 
 
 def test_graph_replay_equals_plain_launches(ctx):
