@@ -82,6 +82,7 @@ SIGNATURES = {
     "bib_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),
     "bib_check_health": (C.c_int32, [_vp, C.c_int32]),
     "bib_lattice_set_tuning": (C.c_int32, [_vp, C.c_int32, C.POINTER(Tuning)]),
+    "bib_spread_forces_noalloc": (C.c_int32, [_vp, C.c_int32, _vp, _vp, C.c_int64, _vp]),
 }
 
 _lib = None

@@ -625,6 +625,16 @@ bib_status bib_set_graph_mode(bib_ctx* c, int32_t enabled) {
     return BIB_OK;
 }
 
+bib_status bib_spread_forces_noalloc(bib_ctx* c, int32_t h, const double* pos, const double* force, int64_t nvert,
+                                     void* field) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    std::string msg;
+    const bib_status st = spread_noalloc(*L, c->device, c->stream, pos, force, nvert, field, msg);
+    if (st != BIB_OK) return fail(c, st, "%s", msg.c_str());
+    return BIB_OK;
+}
+
 bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     Lattice* L = get_lattice(c, h);
     if (!L || !t) return fail(c, BIB_EINVAL, "invalid lattice handle or tuning");

@@ -166,5 +166,17 @@ void launch_particle_update(const Lattice& L, cudaStream_t s);   // area/volume/
 size_t membrane_smem_bytes(int max_nv);
 size_t spread_sort_temp_bytes(int64_t nentries);
 void configure_membrane_kernel(size_t smem);
+// Deterministic spreading into a field of stride d.stride with caller-provided scratch:
+// (cell, entry) keys and entry ids, two buffers each of nvert * support^3 words, and the
+// radix sort's temporary storage (spread_sort_temp_bytes_pingpong bytes).
+size_t spread_sort_temp_bytes_pingpong(int64_t nentries, int end_bit);
+cudaError_t launch_spread_sorted(const LatticeDesc& d, const IbDesc& ib, bool f64_field, int nvert, const double* pos,
+                                 const double* force, void* field, uint32_t* keys0, uint32_t* keys1, uint32_t* ids0,
+                                 uint32_t* ids1, void* temp, size_t temp_bytes, cudaStream_t s);
+int spread_key_bits(int64_t n);
+
+// ---- spreading without device allocation (noalloc.cu) ----
+bib_status spread_noalloc(const Lattice& L, int device, cudaStream_t s, const double* pos, const double* force,
+                          int64_t nvert, void* field, std::string& msg);
 
 }  // namespace bib

@@ -606,6 +606,33 @@ size_t spread_sort_temp_bytes(int64_t nentries) {
     return bytes;
 }
 
+int spread_key_bits(int64_t n) { return key_bits(n); }
+
+size_t spread_sort_temp_bytes_pingpong(int64_t nentries, int end_bit) {
+    size_t bytes = 0;
+    cub::DoubleBuffer<uint32_t> k(nullptr, nullptr), v(nullptr, nullptr);
+    if (cub::DeviceRadixSort::SortPairs(nullptr, bytes, k, v, (int)nentries, 0, end_bit) != cudaSuccess) return SIZE_MAX;
+    return bytes;
+}
+
+cudaError_t launch_spread_sorted(const LatticeDesc& d, const IbDesc& ib, bool f64_field, int nvert, const double* pos,
+                                 const double* force, void* field, uint32_t* keys0, uint32_t* keys1, uint32_t* ids0,
+                                 uint32_t* ids1, void* temp, size_t temp_bytes, cudaStream_t s) {
+    const int sup = ib.dirac == BIB_DIRAC_PESKIN ? 4 : 3;
+    const int64_t ne = (int64_t)nvert * sup * sup * sup;
+    k_spread_keys<<<(nvert + 127) / 128, 128, 0, s>>>(d, ib, nvert, pos, keys0, ids0);
+    cub::DoubleBuffer<uint32_t> k(keys0, keys1), v(ids0, ids1);
+    size_t tb = temp_bytes;
+    cudaError_t e = cub::DeviceRadixSort::SortPairs(temp, tb, k, v, (int)ne, 0, key_bits(d.n), s);
+    if (e != cudaSuccess) return e;
+    const unsigned ge = (unsigned)((ne + 127) / 128);
+    if (f64_field)
+        k_spread_reduce<double><<<ge, 128, 0, s>>>(d, ib, ne, k.Current(), v.Current(), pos, force, (double*)field);
+    else
+        k_spread_reduce<float><<<ge, 128, 0, s>>>(d, ib, ne, k.Current(), v.Current(), pos, force, (float*)field);
+    return cudaGetLastError();
+}
+
 void configure_membrane_kernel(size_t smem) {
     cudaFuncSetAttribute(k_membrane<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_membrane<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);

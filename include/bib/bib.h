@@ -201,6 +201,25 @@ bib_status bib_check_health(bib_ctx* ctx, int32_t h);
  * BIB_EUNSUPPORTED if BIB_KERNEL_STAGED is forced on a lattice whose x-rows do not fit it */
 bib_status bib_lattice_set_tuning(bib_ctx* ctx, int32_t h, const bib_tuning* t);
 
+/* ---- deterministic force spreading that allocates no device memory (no counterpart in the reference) ----
+ * For callers that cannot let the library allocate device memory: a host whose pool allocator already
+ * holds the GPU's free memory (a cudaMalloc by the library would fail or fragment it), or a stepping loop
+ * that cannot take the device-wide synchronisation of cudaMalloc / cudaFree.
+ * Adds the delta-weighted forces of nvert vertices into `field`, in the order of BIB_SPREAD_DETERMINISTIC,
+ * with the geometry, periodicity, delta kernel and field offset of lattice h.  pos and force are device
+ * arrays of nvert x 3 doubles; field is a device array of 3 x nz x ny x nx values (x fastest), double for a
+ * BIB_STORAGE_F64 lattice and float otherwise.  The sort scratch is one static device array of the library
+ * (BIB_SPREAD_NOALLOC_SCRATCH_BYTES); nvert x support^3 (support 3 for Roma, 4 for Peskin) above
+ * BIB_SPREAD_NOALLOC_MAX_ENTRIES is rejected with BIB_EINVAL before any work is queued.
+ * The first call on a device resolves the array's device address (a set-up step): make it before any
+ * stream capture.  Every call uses the same array, so calls that overlap in time on one device (from two
+ * contexts, two threads, or streams not ordered with each other) race on it.  The work is queued on the
+ * context's stream; the call returns without synchronising. */
+#define BIB_SPREAD_NOALLOC_MAX_ENTRIES (1 << 20)
+#define BIB_SPREAD_NOALLOC_SCRATCH_BYTES (17u << 20)
+bib_status bib_spread_forces_noalloc(bib_ctx* ctx, int32_t h, const double* pos, const double* force, int64_t nvert,
+                                     void* field);
+
 /* ---- timing: per-kernel-group device time (ms) of the last bib_step call when profiling is on ---- */
 bib_status bib_set_profiling(bib_ctx* ctx, int32_t enabled);
 /* out[5] = {membrane forces, spreading, collide+stream, walls, interpolation+move+update};
