@@ -37,7 +37,8 @@ class IbParams(C.Structure):
 
 
 class Tuning(C.Structure):
-    _fields_ = [("collide_kernel", C.c_int32), ("tile_cells", C.c_int32), ("reserved", C.c_int32 * 6)]
+    _fields_ = [("collide_kernel", C.c_int32), ("tile_cells", C.c_int32), ("stages", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
 
 
 class Config(C.Structure):

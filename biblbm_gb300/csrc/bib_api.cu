@@ -638,17 +638,20 @@ bib_status bib_spread_forces_noalloc(bib_ctx* c, int32_t h, const double* pos, c
 bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     Lattice* L = get_lattice(c, h);
     if (!L || !t) return fail(c, BIB_EINVAL, "invalid lattice handle or tuning");
-    if (t->collide_kernel < BIB_KERNEL_AUTO || t->collide_kernel > BIB_KERNEL_STAGED || t->tile_cells < 0)
+    if (t->collide_kernel < BIB_KERNEL_AUTO || t->collide_kernel > BIB_KERNEL_STAGED || t->tile_cells < 0 ||
+        t->stages < 0 || t->stages == 1 || t->stages > 4)
         return fail(c, BIB_EINVAL, "invalid tuning values");
     Lattice probe = {};
     probe.d = L->d;
     probe.storage = L->storage;
     probe.tile_cells = t->tile_cells;
+    probe.stages = t->stages;
     if (t->collide_kernel == BIB_KERNEL_STAGED && !collide_staged_fits(probe))
         return fail(c, BIB_EUNSUPPORTED, "the staged collide-and-stream kernel does not fit this lattice / tile size");
     drop_graphs(c, h);
     L->collide_kernel = t->collide_kernel;
     L->tile_cells = t->tile_cells;
+    L->stages = t->stages;
     return BIB_OK;
 }
 

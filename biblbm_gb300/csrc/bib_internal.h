@@ -132,9 +132,10 @@ struct Lattice {
     uint32_t* sort_ids[2] = {nullptr, nullptr};
     void* sort_temp = nullptr;
     size_t sort_temp_bytes = 0;
-    // collide-and-stream kernel selection (BIB_KERNEL_*) and staged tile size (0 = default)
+    // collide-and-stream kernel selection (BIB_KERNEL_*), staged tile size (0 = default)
     int collide_kernel = BIB_KERNEL_AUTO;
     int tile_cells = 0;
+    int stages = 0;           // staged kernel pipeline depth (0 = automatic)
     int* wait_err = nullptr;  // device word set by a bounded device wait that gave up
     int handle = -1;
 };

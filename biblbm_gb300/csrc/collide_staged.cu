@@ -24,8 +24,6 @@ namespace bib {
 
 namespace {
 
-constexpr int kStagedThreads = 256;
-
 __device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
 
 __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
@@ -34,6 +32,9 @@ __device__ __forceinline__ void mbar_init(uint64_t* bar, unsigned count) {
 __device__ __forceinline__ void mbar_init_fence() { asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory"); }
 __device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* bar, unsigned bytes) {
     asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)), "r"(bytes) : "memory");
+}
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+    asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_addr(bar)) : "memory");
 }
 __device__ __forceinline__ bool mbar_try_wait(uint64_t* bar, unsigned parity) {
     uint32_t done;
@@ -135,40 +136,90 @@ __device__ __forceinline__ void staged_collide(C* f, const C* F, C om, C omm, C 
     }
 }
 
-struct StagedGeom {
-    int R;            // rows per tile (divides ny)
-    int Ct;           // cells per tile, R * nx
-    int tiles_y;      // ny / R
-    int64_t ntiles;   // tiles_y * nz
-    unsigned pop_bytes, f_bytes;     // one population / force component of one tile
-    unsigned off_fcol, off_fprev;    // byte offsets inside a stage
-    unsigned stage_bytes, tx_bytes;  // stage size (padded) and bytes copied per tile
+// Tile pitch in cells: the shared-memory row of one population holds up to TILE cells, so
+// every staged address is a per-thread base plus a compile-time offset.
+template <class T>
+struct TileOf {
+    static constexpr int value = sizeof(T) == 8 ? 256 : 512;
 };
 
-// Issue the copies of one tile into one stage (executed by warp 0).
-template <class T, class FT, bool COUPLED, bool NEED_FCOL>
-__device__ __forceinline__ void issue_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, unsigned char* stage,
-                                           uint64_t* bar, const T* fin, const T* wall, const FT* Fcol, const FT* Fprev,
-                                           int lane) {
-    const int z = (int)(tile / g.tiles_y);
-    const int y0 = (int)(tile - (int64_t)z * g.tiles_y) * g.R;
+// Stage layout (compile-time): 19 population rows, the collision force (BGK + Guo) and,
+// for the coupled step, the previous force, each TILE cells long.
+template <class T, bool COUPLED, int COLL>
+struct StageLayout {
+    using FT = typename Store<T>::F;
+    static constexpr int TILE = TileOf<T>::value;
+    static constexpr int CONSUMERS = TILE / 32;  // consumer warps: one cell per thread and tile
+    static constexpr int THREADS = 32 * (CONSUMERS + 1);
+    static constexpr bool NEED_FCOL = COLL == BIB_COLLISION_BGK_GUO_VOF;
+    static constexpr unsigned POP = TILE * sizeof(T);
+    static constexpr unsigned FRC = TILE * sizeof(FT);
+    static constexpr unsigned OFF_FCOL = Q * POP;
+    static constexpr unsigned OFF_FPREV = OFF_FCOL + (NEED_FCOL ? 3 * FRC : 0);
+    static constexpr unsigned BYTES = ((OFF_FPREV + (COUPLED ? 3 * FRC : 0)) + 127) / 128 * 128;
+};
+
+constexpr int kMaxStages = 8;
+
+struct StagedGeom {
+    int R;            // rows per tile (divides ny)
+    int Ct;           // cells per tile, R * nx <= TILE
+    int tiles_y;      // ny / R
+    int nstages;      // pipeline depth (2..kMaxStages)
+    int64_t ntiles;   // tiles_y * nz
+    unsigned tx_bytes;  // bytes copied in per tile
+};
+
+// Per-launch constants in the compute type, so that no double -> float conversion (FP64
+// pipe) happens per cell.
+template <class C>
+struct CollideParams {
+    C om0, om1;      // relaxation frequency of phase 0 / 1 (BGK + Guo) or the omega of BGK / TRT
+    C omm;           // TRT: omega of the antisymmetric part
+    C S, invS;       // storage scale (FP16) and its inverse, 1 otherwise
+    C body[3];       // body force, the reset value of the previous force field
+    C wall_u[2][3];  // velocity of the finite-difference wall rows y = 0, ny - 1
+    C mw[4][Q];      // moving-wall bounce-back term per wall face and population, storage units
+};
+
+struct TileRef {
+    int z, y0;
+    int64_t row0;  // first cell of the tile
+};
+__device__ __forceinline__ TileRef tile_ref(const LatticeDesc& d, const StagedGeom& g, int64_t tile) {
+    TileRef t;
+    t.z = (int)(tile / g.tiles_y);
+    t.y0 = (int)(tile - (int64_t)t.z * g.tiles_y) * g.R;
+    t.row0 = ((int64_t)t.y0 + (int64_t)d.ny * t.z) * d.nx;
+    return t;
+}
+
+// Copies of one tile into one stage, by the producer warp: lane i < 19 moves population i,
+// lanes 19..21 the collision force, lanes 22..24 the previous force.
+template <class T, bool COUPLED, int COLL>
+__device__ __forceinline__ void load_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, unsigned char* stage,
+                                          uint64_t* bar, const T* fin, const T* wall, const typename Store<T>::F* Fcol,
+                                          const typename Store<T>::F* Fprev, int lane) {
+    using L = StageLayout<T, COUPLED, COLL>;
+    using FT = typename Store<T>::F;
+    const TileRef t = tile_ref(d, g, tile);
     if (lane == 0) mbar_arrive_expect_tx(bar, g.tx_bytes);
     __syncwarp();
     const unsigned rowb = (unsigned)d.nx * sizeof(T);
     if (lane < Q) {
         const int i = lane;
-        unsigned char* dst = stage + (size_t)i * g.pop_bytes;
+        unsigned char* dst = stage + i * L::POP;
         const unsigned char* run = nullptr;
         unsigned run_len = 0, run_at = 0;
         for (int r = 0; r < g.R; ++r) {
-            const int y = y0 + r;
+            const int y = t.y0 + r;
             const T* src;
             if (fd_wall_node(d, y)) {
-                src = wall + i * wall_stride(d) + wall_index(d, y == 0 ? 0 : 1, 0, z);
+                src = wall + i * wall_stride(d) + wall_index(d, y == 0 ? 0 : 1, 0, t.z);
             } else {
                 int64_t srow;
-                const int face = source_row(d, i, y, z, srow);
-                src = face >= 0 ? fin + opposite(i) * d.stride + ((int64_t)y + (int64_t)d.ny * z) * d.nx
+                const int face = source_row(d, i, y, t.z, srow);
+                src = face >= 0 ? fin + opposite(i) * d.stride + ((int64_t)y + (int64_t)d.ny * t.z) * d.nx
                                 : fin + i * d.stride + srow * d.nx;
             }
             const unsigned char* s = reinterpret_cast<const unsigned char*>(src);
@@ -183,131 +234,160 @@ __device__ __forceinline__ void issue_tile(const LatticeDesc& d, const StagedGeo
         }
         bulk_copy_g2s(dst + run_at, run, run_len, bar);
     } else {
-        const int64_t row0 = ((int64_t)y0 + (int64_t)d.ny * z) * d.nx;
-        if (NEED_FCOL && lane < Q + 3) {
+        const unsigned fb = (unsigned)(g.Ct * sizeof(FT));
+        if (L::NEED_FCOL && lane < Q + 3) {
             const int c = lane - Q;
-            bulk_copy_g2s(stage + g.off_fcol + c * g.f_bytes, Fcol + c * d.stride + row0, g.f_bytes, bar);
+            bulk_copy_g2s(stage + L::OFF_FCOL + c * L::FRC, Fcol + c * d.stride + t.row0, fb, bar);
         } else if (COUPLED && lane >= Q + 3 && lane < Q + 6) {
             const int c = lane - Q - 3;
-            bulk_copy_g2s(stage + g.off_fprev + c * g.f_bytes, Fprev + c * d.stride + row0, g.f_bytes, bar);
+            bulk_copy_g2s(stage + L::OFF_FPREV + c * L::FRC, Fprev + c * d.stride + t.row0, fb, bar);
         }
     }
+    __syncwarp();
+}
+
+// Warp-specialised persistent kernel: warp 0 produces, warps 1..CONSUMERS collide.  Stage
+// s is handed over through two mbarriers: full[s] completes when the tile's bytes have
+// landed, empty[s] when every consumer warp is done reading it.  Consumers never wait for
+// each other, and the producer refills a stage as soon as it is released, so up to NS - 1
+// tiles of loads are in flight per CTA.  Results go straight from registers to HBM.
+// Resident CTAs per SM the kernel is built for: FP16 needs two (32 consumer warps) to hide
+// the latency of its arithmetic; FP32 and FP64 run one CTA with a deeper pipeline.
+template <class T>
+constexpr int staged_ctas_per_sm() {
+    return sizeof(T) == 2 ? 2 : 1;
 }
 
 template <class T, bool COUPLED, int COLL>
-__global__ void __launch_bounds__(kStagedThreads, sizeof(T) == 8 ? 1 : 3) k_collide_stream_staged(
-    LatticeDesc d, StagedGeom g, const T* __restrict__ fin, T* __restrict__ fout, const T* __restrict__ wall,
-    const typename Store<T>::F* __restrict__ Fcol, typename Store<T>::F* __restrict__ Fprev,
-    typename Store<T>::F* __restrict__ u_out, const uint8_t* __restrict__ phase, int* __restrict__ wait_err) {
+__global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged_ctas_per_sm<T>())
+    k_collide_stream_staged(
+    LatticeDesc d, StagedGeom g, CollideParams<typename Store<T>::C> cp, const T* __restrict__ fin,
+    T* __restrict__ fout, const T* __restrict__ wall, const typename Store<T>::F* __restrict__ Fcol,
+    typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
+    const uint8_t* __restrict__ phase, int* __restrict__ wait_err) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
-    constexpr bool NEED_FCOL = COLL == BIB_COLLISION_BGK_GUO_VOF;
+    using L = StageLayout<T, COUPLED, COLL>;
+    constexpr int TILE = L::TILE;
     extern __shared__ __align__(128) unsigned char smem[];
-    __shared__ int s_ok;
-    uint64_t* bar = reinterpret_cast<uint64_t*>(smem);
-    unsigned char* stages = smem + 128;
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+    uint64_t* empty = full + kMaxStages;
+    unsigned char* stages = smem + 256;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    int64_t tile = blockIdx.x;
-    if (tile >= g.ntiles) return;
+    const int NS = g.nstages;
+    if ((int64_t)blockIdx.x >= g.ntiles) return;
     if (tid == 0) {
-        mbar_init(&bar[0], 1);
-        mbar_init(&bar[1], 1);
+        for (int k = 0; k < NS; ++k) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], L::CONSUMERS);
+        }
         mbar_init_fence();
     }
     __syncthreads();
-    if (warp == 0)
-        issue_tile<T, FT, COUPLED, NEED_FCOL>(d, g, tile, stages, &bar[0], fin, wall, Fcol, Fprev, lane);
 
-    const C S = sizeof(T) == 2 ? (C)d.scale : C(1);
-    const C invS = sizeof(T) == 2 ? (C)d.inv_scale : C(1);
-    C omm = C(0);
-    if (COLL == BIB_COLLISION_TRT) {
-        const C om = (C)d.omega;
-        omm = C(1) / ((C)d.trt_magic / (C(1) / om - C(0.5)) + C(0.5));
-    }
-    for (int it = 0; tile < g.ntiles; ++it, tile += gridDim.x) {
-        const int s = it & 1;
-        const int64_t next = tile + gridDim.x;
-        if (warp == 0 && next < g.ntiles)
-            issue_tile<T, FT, COUPLED, NEED_FCOL>(d, g, next, stages + (s ^ 1) * g.stage_bytes, &bar[s ^ 1], fin, wall,
-                                                  Fcol, Fprev, lane);
-        if (tid == 0) {
-            const bool ok = mbar_wait_bounded(&bar[s], (unsigned)(it >> 1) & 1u);
-            if (!ok) {
-                atomicExch(wait_err, 1);
-                // let the copies of the prefetched tile land before the CTA leaves
-                if (next < g.ntiles) mbar_wait_bounded(&bar[s ^ 1], (unsigned)((it + 1) >> 1) & 1u);
+    if (warp == 0) {
+        // ---- producer
+        int it = 0;
+        for (int64_t tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x, ++it) {
+            const int s = it % NS, use = it / NS;
+            if (use > 0) {
+                // every lane observes the release, so every lane's copies are ordered after it
+                const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&empty[s], (unsigned)(use - 1) & 1u));
+                if (!ok) {
+                    if (lane == 0) atomicExch(wait_err, 1);
+                    break;
+                }
             }
-            s_ok = ok;
+            load_tile<T, COUPLED, COLL>(d, g, tile, stages + s * L::BYTES, &full[s], fin, wall, Fcol, Fprev, lane);
         }
-        __syncthreads();
-        if (!s_ok) return;  // uniform: every thread of the CTA leaves
+        // a copy may still be landing only if the consumers gave up; wait for it so that
+        // no bulk copy writes into the shared memory of a retired CTA
+        if (lane == 0) {
+            const int issued = it;
+            for (int k = issued > NS ? issued - NS : 0; k < issued; ++k)
+                mbar_wait_bounded(&full[k % NS], (unsigned)(k / NS) & 1u);
+        }
+        return;
+    }
 
-        const unsigned char* st = stages + s * g.stage_bytes;
+    // ---- consumers: thread `ct` owns cell ct of every tile
+    const int ct = tid - 32;
+    const bool active = ct < g.Ct;
+    const int r = ct / d.nx, x = ct - r * d.nx;
+    const int o0 = ct;
+    const int ol = r * d.nx + (x == 0 ? d.nx - 1 : x - 1);
+    const int orr = r * d.nx + (x == d.nx - 1 ? 0 : x + 1);
+    int it = 0;
+    for (int64_t tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x, ++it) {
+        const int s = it % NS;
+        // every lane waits, so that the landed bytes are visible to every lane
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (unsigned)(it / NS) & 1u));
+        if (!ok) {
+            if (lane == 0) atomicExch(wait_err, 1);
+            return;
+        }
+        const unsigned char* st = stages + s * L::BYTES;
         const T* P = reinterpret_cast<const T*>(st);
-        const FT* SFc = reinterpret_cast<const FT*>(st + g.off_fcol);
-        const FT* SFp = reinterpret_cast<const FT*>(st + g.off_fprev);
-        const int z = (int)(tile / g.tiles_y);
-        const int y0 = (int)(tile - (int64_t)z * g.tiles_y) * g.R;
-        for (int c = tid; c < g.Ct; c += kStagedThreads) {
-            const int r = c / d.nx;
-            const int x = c - r * d.nx;
-            const int y = y0 + r;
-            const int rb = r * d.nx;
-            const int xl = x == 0 ? d.nx - 1 : x - 1;
-            const int xr = x == d.nx - 1 ? 0 : x + 1;
-            C f[Q];
-            const bool fd = fd_wall_node(d, y);
-            if (!row_special(d, y, z)) {
+        const FT* SFc = reinterpret_cast<const FT*>(st + L::OFF_FCOL);
+        const FT* SFp = reinterpret_cast<const FT*>(st + L::OFF_FPREV);
+        const TileRef t = tile_ref(d, g, tile);
+        C f[Q], u[3], F[3] = {C(0), C(0), C(0)}, Fp[3];
+        const int y = t.y0 + r;
+        const bool fd = fd_wall_node(d, y);
+        C om = cp.om0;
+        if (active) {
+            if (!row_special(d, y, t.z)) {
 #pragma unroll
-                for (int i = 0; i < Q; ++i)
-                    f[i] = Staged<T>::one(P + i * g.Ct + rb + (cx(i) == 0 ? x : (cx(i) == 1 ? xl : xr)));
+                for (int i = 0; i < Q; ++i) f[i] = Staged<T>::one(P + i * TILE + (cx(i) == 0 ? o0 : (cx(i) == 1 ? ol : orr)));
             } else {
 #pragma unroll
                 for (int i = 0; i < Q; ++i) {
                     int face = -1;
                     if (!fd) {
                         int64_t srow;
-                        face = source_row(d, i, y, z, srow);
+                        face = source_row(d, i, y, t.z, srow);
                     }
                     const bool shift = !fd && face < 0;
-                    f[i] = Staged<T>::one(P + i * g.Ct + rb + (!shift || cx(i) == 0 ? x : (cx(i) == 1 ? xl : xr)));
-                    if (face >= 0) f[i] += moving_wall_term<C>(d, i, face) * S;
+                    f[i] = Staged<T>::one(P + i * TILE + (!shift || cx(i) == 0 ? o0 : (cx(i) == 1 ? ol : orr)));
+                    if (face >= 0) f[i] += cp.mw[face][i];
                 }
             }
-            const int64_t k = ((int64_t)y + (int64_t)d.ny * z) * d.nx + x;
-            C F[3] = {C(0), C(0), C(0)};
-            if (NEED_FCOL) {
+            if (L::NEED_FCOL) {
 #pragma unroll
-                for (int q = 0; q < 3; ++q) F[q] = (C)SFc[q * g.Ct + c];
-            }
-            C om = (C)d.omega;
-            if (COLL == BIB_COLLISION_BGK_GUO_VOF) {
-                om = (C)d.omega_c0;
-                if (d.use_phase && phase[k]) om = (C)d.omega_c1;
+                for (int q = 0; q < 3; ++q) F[q] = (C)SFc[q * TILE + o0];
             }
             if (COUPLED) {
-                C Fp[3], u[3];
 #pragma unroll
-                for (int q = 0; q < 3; ++q) Fp[q] = (C)SFp[q * g.Ct + c];
-                staged_collide<C, COLL>(f, F, om, omm, S, invS, Fp, fd ? nullptr : u);
-                if (fd) {
-                    const int side = y == 0 ? 0 : 1;
+                for (int q = 0; q < 3; ++q) Fp[q] = (C)SFp[q * TILE + o0];
+            }
+        }
+        // the stage has been read into registers: hand it back to the producer
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&empty[s]);
+        if (!active) continue;
+        const int64_t k = t.row0 + o0;
+        if (COLL == BIB_COLLISION_BGK_GUO_VOF && d.use_phase && phase[k]) om = cp.om1;
+        if (COUPLED) {
+            staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, Fp, fd ? nullptr : u);
+            if (fd) {
+                const int side = y == 0 ? 0 : 1;
 #pragma unroll
-                    for (int q = 0; q < 3; ++q) u[q] = (C)d.wall_u[side][q];
-                }
-#pragma unroll
-                for (int q = 0; q < 3; ++q) {
-                    u_out[q * d.stride + k] = (FT)u[q];
-                    Fprev[q * d.stride + k] = (FT)d.body[q];
-                }
-            } else {
-                staged_collide<C, COLL>(f, F, om, omm, S, invS, nullptr, nullptr);
+                for (int q = 0; q < 3; ++q) u[q] = cp.wall_u[side][q];
             }
 #pragma unroll
-            for (int i = 0; i < Q; ++i) Staged<T>::put(fout + i * d.stride + k, f[i]);
+            for (int q = 0; q < 3; ++q) {
+                u_out[q * d.stride + k] = (FT)u[q];
+                Fprev[q * d.stride + k] = (FT)cp.body[q];
+            }
+        } else {
+            staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, nullptr, nullptr);
         }
-        __syncthreads();  // the stage is refilled in the next-but-one iteration
+        T* o = fout + k;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            Staged<T>::put(o, f[i]);
+            o += d.stride;
+        }
     }
 }
 
@@ -319,43 +399,69 @@ int staged_rows(const LatticeDesc& d, int target) {
     return R;
 }
 
-
-template <class T>
-size_t staged_geom(const LatticeDesc& d, int target, bool coupled, bool need_fcol, StagedGeom& g) {
-    using FT = typename Store<T>::F;
-    g = StagedGeom{};
-    g.R = staged_rows(d, target);
-    g.Ct = g.R * d.nx;
-    g.tiles_y = d.ny / g.R;
-    g.ntiles = (int64_t)g.tiles_y * d.nz;
-    g.pop_bytes = (unsigned)(g.Ct * sizeof(T));
-    g.f_bytes = (unsigned)(g.Ct * sizeof(FT));
-    g.off_fcol = Q * g.pop_bytes;
-    g.off_fprev = g.off_fcol + (need_fcol ? 3 * g.f_bytes : 0);
-    g.tx_bytes = g.off_fprev + (coupled ? 3 * g.f_bytes : 0);
-    g.stage_bytes = (g.tx_bytes + 127) / 128 * 128;
-    return 128 + 2 * (size_t)g.stage_bytes;
-}
-
-bool smem_fits(size_t smem) {
+int optin_smem() {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    return smem + 1024 <= (size_t)optin;
+    return optin;
 }
 
-int default_tile_cells(const Lattice& L) {
-    return L.tile_cells > 0 ? L.tile_cells : (L.storage == BIB_STORAGE_F64 ? 256 : 512);
+template <class T, bool COUPLED, int COLL>
+size_t staged_smem(int nstages) {
+    return 256 + (size_t)nstages * StageLayout<T, COUPLED, COLL>::BYTES;
+}
+
+// Pipeline depth: the tuning value, else as many stages as fit the resident CTAs of an SM
+// (228 KB of shared memory per SM, 1 KB of it reserved per CTA).
+template <class T, bool COUPLED, int COLL>
+int staged_stages(const Lattice& L) {
+    if (L.stages >= 2) return L.stages;
+    const size_t limit = std::min<size_t>((size_t)optin_smem(), 228 * 1024 / staged_ctas_per_sm<T>()) - 1024;
+    int best = 2;
+    for (int ns = 2; ns <= kMaxStages; ++ns)
+        if (staged_smem<T, COUPLED, COLL>(ns) <= limit) best = ns;
+    return best;
+}
+
+template <class C>
+CollideParams<C> collide_params(const LatticeDesc& d, int storage) {
+    CollideParams<C> cp{};
+    const bool phase_omega = d.collision == BIB_COLLISION_BGK_GUO_VOF;
+    cp.om0 = (C)(phase_omega ? d.omega_c0 : d.omega);
+    cp.om1 = (C)(phase_omega ? d.omega_c1 : d.omega);
+    cp.omm = (C)(1.0 / (d.trt_magic / (1.0 / d.omega - 0.5) + 0.5));
+    const double S = storage == BIB_STORAGE_F16 ? (double)d.scale : 1.0;
+    cp.S = (C)S;
+    cp.invS = (C)(storage == BIB_STORAGE_F16 ? (double)d.inv_scale : 1.0);
+    for (int q = 0; q < 3; ++q) {
+        cp.body[q] = (C)d.body[q];
+        cp.wall_u[0][q] = (C)d.wall_u[0][q];
+        cp.wall_u[1][q] = (C)d.wall_u[1][q];
+    }
+    for (int face = 0; face < 4; ++face)
+        for (int i = 0; i < Q; ++i) {
+            const double cu = cx(i) * d.wall_u[face][0] + cy(i) * d.wall_u[face][1] + cz(i) * d.wall_u[face][2];
+            cp.mw[face][i] = (C)((C)(6.0 * weight<double>(i) * cu) * (C)S);
+        }
+    return cp;
 }
 
 template <class T, bool COUPLED, int COLL>
 bool staged_inst(const Lattice& L, int target, cudaStream_t s) {
     using FT = typename Store<T>::F;
-    constexpr bool NEED_FCOL = COLL == BIB_COLLISION_BGK_GUO_VOF;
+    using C = typename Store<T>::C;
+    using LY = StageLayout<T, COUPLED, COLL>;
     const LatticeDesc& d = L.d;
-    StagedGeom g;
-    const size_t smem = staged_geom<T>(d, target, COUPLED, NEED_FCOL, g);
-    if (!smem_fits(smem)) return false;
+    StagedGeom g{};
+    g.R = staged_rows(d, std::min(target, LY::TILE));
+    g.Ct = g.R * d.nx;
+    if (g.Ct > LY::TILE) return false;
+    g.tiles_y = d.ny / g.R;
+    g.ntiles = (int64_t)g.tiles_y * d.nz;
+    g.nstages = staged_stages<T, COUPLED, COLL>(L);
+    g.tx_bytes = (unsigned)(Q * g.Ct * sizeof(T) + ((LY::NEED_FCOL ? 3 : 0) + (COUPLED ? 3 : 0)) * g.Ct * sizeof(FT));
+    const size_t smem = staged_smem<T, COUPLED, COLL>(g.nstages);
+    if (smem + 1024 > (size_t)optin_smem()) return false;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
@@ -376,7 +482,7 @@ bool staged_inst(const Lattice& L, int target, cudaStream_t s) {
             lim = smem;
         }
         int& r = resident[((int64_t)dev << 32) | (int64_t)smem];
-        if (r == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, kStagedThreads, smem) != cudaSuccess ||
+        if (r == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, LY::THREADS, smem) != cudaSuccess ||
                        r < 1)) {
             r = 0;
             return false;
@@ -388,8 +494,9 @@ bool staged_inst(const Lattice& L, int target, cudaStream_t s) {
     T* fout = (T*)L.f[1 - L.cur];
     const FT* Fcol = (const FT*)(COUPLED ? L.F[1 - L.fe] : L.F[L.fe]);
     FT* Fprev = COUPLED ? (FT*)L.F[L.fe] : nullptr;
-    kern<<<(unsigned)grid, kStagedThreads, smem, s>>>(d, g, fin, fout, (const T*)L.wall, Fcol, Fprev,
-                                                       COUPLED ? (FT*)L.u : nullptr, L.phase, L.wait_err);
+    kern<<<(unsigned)grid, LY::THREADS, smem, s>>>(d, g, collide_params<C>(d, L.storage), fin, fout,
+                                                       (const T*)L.wall, Fcol, Fprev, COUPLED ? (FT*)L.u : nullptr,
+                                                       L.phase, L.wait_err);
     return true;
 }
 
@@ -404,7 +511,11 @@ bool staged_coll(const Lattice& L, int target, cudaStream_t s) {
 
 template <class T>
 bool shape_ok(const Lattice& L) {
-    return L.d.nx % 2 == 0 && (L.d.nx * sizeof(T)) % 16 == 0;
+    return L.d.nx % 2 == 0 && (L.d.nx * sizeof(T)) % 16 == 0 && L.d.nx <= TileOf<T>::value;
+}
+
+int default_tile_cells(const Lattice& L) {
+    return L.tile_cells > 0 ? L.tile_cells : (L.storage == BIB_STORAGE_F64 ? 256 : 512);
 }
 
 template <class T>
@@ -417,8 +528,8 @@ bool staged_t(const Lattice& L, bool coupled, cudaStream_t s) {
 template <class T>
 bool fits_t(const Lattice& L) {
     if (!shape_ok<T>(L)) return false;
-    StagedGeom g;
-    return smem_fits(staged_geom<T>(L.d, default_tile_cells(L), true, true, g));  // the largest stage
+    const int ns = L.stages >= 2 ? L.stages : 2;
+    return ns <= kMaxStages && staged_smem<T, true, BIB_COLLISION_BGK_GUO_VOF>(ns) + 1024 <= (size_t)optin_smem();
 }
 
 }  // namespace

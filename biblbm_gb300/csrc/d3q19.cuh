@@ -189,12 +189,29 @@ __device__ __forceinline__ void collide(C* f, const C* F, C omega, C omega_minus
 }
 
 // Compact BGK + Guo collision for the reduced-precision paths.  Algebraically the same
-// operator as collide<C, BGK_GUO_VOF> (the Guo term of VariableViscosityDynamics.hh:47-129
-// is t_i (1 - w/2) [3 (c_i - u).F + 9 (c_i.u)(c_i.F)]), evaluated per opposite pair
-// (i, i+9) from its symmetric and antisymmetric parts.  The populations may carry a common
-// scale S (FP16 storage keeps f-bar * S): moments are unscaled once, post-collision values
-// are produced in scaled units.  With `u_prev` non-null the velocity j/rho + F_prev/2 of the
-// incoming state is returned as well (the reference's computeVelocity).
+// operator as collide<C, BGK_GUO_VOF>: with u = j/rho + F/2, rho = rhoBar + 1, the BGK
+// equilibrium of J = rho u plus the Guo term of VariableViscosityDynamics.hh:47-129,
+// t_i (1 - w/2) [3 (c_i - u).F + 9 (c_i.u)(c_i.F)], collapse to
+//     f_i' = (1 - w) f_i + t_i [A + c_i.H + (c_i.u)(c_i.G)]
+//     A = w rhoBar - 1.5 w rho u.u - 3 mu u.F,  H = 3 w rho u + 3 mu F,  G = 4.5 w rho u + 9 mu F,
+// mu = 1 - w/2, evaluated once per opposite pair (i, i+9) (c_{i+9} = -c_i).  BGK without
+// forcing is the same with F = 0 and u = j/rho.  The populations may carry a common scale S
+// (FP16 storage keeps f-bar * S): moments are unscaled once, post-collision values come out
+// in scaled units.  With `u_prev` non-null the velocity j/rho + F_prev/2 of the incoming
+// state is returned as well (the reference's computeVelocity).
+// c_i . (a, b, c) with the zero components left out: multiplications by 0 are not removed
+// by the compiler under IEEE semantics (0 * inf is NaN), so they are not written.
+__device__ __forceinline__ float cdot(int i, float a, float b, float c) {
+    const float xa = cx(i) > 0 ? a : -a, yb = cy(i) > 0 ? b : -b, zc = cz(i) > 0 ? c : -c;
+    if (cx(i) != 0) {
+        if (cy(i) != 0) return xa + yb;
+        if (cz(i) != 0) return xa + zc;
+        return xa;
+    }
+    if (cy(i) != 0) return cz(i) != 0 ? yb + zc : yb;
+    return cz(i) != 0 ? zc : 0.0f;
+}
+
 template <int COLL>
 __device__ __forceinline__ void collide_compact(float* f, const float* F, float omega, float S, float invS,
                                                 const float* Fprev, float* u_prev) {
@@ -209,46 +226,29 @@ __device__ __forceinline__ void collide_compact(float* f, const float* F, float 
     const float j0 = (sxp - sxm) * invS, j1 = (syp - sym) * invS, j2 = (szp - szm) * invS;
     const float invRho = 1.0f / (rb + 1.0f);
     if (u_prev) {
-        u_prev[0] = j0 * invRho + 0.5f * Fprev[0];
-        u_prev[1] = j1 * invRho + 0.5f * Fprev[1];
-        u_prev[2] = j2 * invRho + 0.5f * Fprev[2];
+        u_prev[0] = fmaf(j0, invRho, 0.5f * Fprev[0]);
+        u_prev[1] = fmaf(j1, invRho, 0.5f * Fprev[1]);
+        u_prev[2] = fmaf(j2, invRho, 0.5f * Fprev[2]);
     }
-    const float omo = 1.0f - omega;
-    if (COLL == BIB_COLLISION_BGK) {
-        // BGKdynamics: equilibrium of j, no forcing
-        const float jsq = j0 * j0 + j1 * j1 + j2 * j2;
-        const float base = rb - 1.5f * invRho * jsq;
-        const float h = 4.5f * invRho;
-        f[0] = omo * f[0] + S * omega * weight<float>(0) * base;
-#pragma unroll
-        for (int i = 1; i < 10; ++i) {
-            const float cj = float(cx(i)) * j0 + float(cy(i)) * j1 + float(cz(i)) * j2;
-            const float tw = S * omega * weight<float>(i);
-            const float P = tw * fmaf(h * cj, cj, base), M = tw * 3.0f * cj;
-            f[i] = omo * f[i] + P + M;
-            f[i + 9] = omo * f[i + 9] + P - M;
-        }
-        return;
-    }
-    const float u0 = j0 * invRho + 0.5f * F[0], u1 = j1 * invRho + 0.5f * F[1], u2 = j2 * invRho + 0.5f * F[2];
+    const bool forced = COLL == BIB_COLLISION_BGK_GUO_VOF;
+    const float F0 = forced ? F[0] : 0.0f, F1 = forced ? F[1] : 0.0f, F2 = forced ? F[2] : 0.0f;
+    const float u0 = fmaf(j0, invRho, 0.5f * F0), u1 = fmaf(j1, invRho, 0.5f * F1), u2 = fmaf(j2, invRho, 0.5f * F2);
     const float rho = rb + 1.0f;
-    const float J0 = rho * u0, J1 = rho * u1, J2 = rho * u2;
-    const float jsq = J0 * J0 + J1 * J1 + J2 * J2;
-    const float base = rb - 1.5f * invRho * jsq;
-    const float h = 4.5f * invRho;
     const float mu = 1.0f - 0.5f * omega;
-    const float uF = u0 * F[0] + u1 * F[1] + u2 * F[2];
-    f[0] = omo * f[0] + S * weight<float>(0) * (omega * base - 3.0f * mu * uF);
+    const float wr = omega * rho;
+    const float A = omega * rb - 1.5f * wr * (u0 * u0 + u1 * u1 + u2 * u2) - 3.0f * mu * (u0 * F0 + u1 * F1 + u2 * F2);
+    const float h3 = 3.0f * wr, m3 = 3.0f * mu, g45 = 4.5f * wr, m9 = 9.0f * mu;
+    const float H0 = fmaf(h3, u0, m3 * F0), H1 = fmaf(h3, u1, m3 * F1), H2 = fmaf(h3, u2, m3 * F2);
+    const float G0 = fmaf(g45, u0, m9 * F0), G1 = fmaf(g45, u1, m9 * F1), G2 = fmaf(g45, u2, m9 * F2);
+    const float omo = 1.0f - omega;
+    f[0] = fmaf(omo, f[0], (S * weight<float>(0)) * A);
 #pragma unroll
     for (int i = 1; i < 10; ++i) {
-        const float cj = float(cx(i)) * J0 + float(cy(i)) * J1 + float(cz(i)) * J2;
-        const float cu = float(cx(i)) * u0 + float(cy(i)) * u1 + float(cz(i)) * u2;
-        const float cF = float(cx(i)) * F[0] + float(cy(i)) * F[1] + float(cz(i)) * F[2];
+        const float cu = cdot(i, u0, u1, u2), cG = cdot(i, G0, G1, G2), cH = cdot(i, H0, H1, H2);
         const float tw = S * weight<float>(i);
-        const float P = tw * (omega * fmaf(h * cj, cj, base) + mu * (9.0f * cu * cF - 3.0f * uF));
-        const float M = tw * 3.0f * (omega * cj + mu * cF);
-        f[i] = omo * f[i] + P + M;
-        f[i + 9] = omo * f[i + 9] + P - M;
+        const float P = tw * fmaf(cu, cG, A), M = tw * cH;
+        f[i] = fmaf(omo, f[i], P + M);
+        f[i + 9] = fmaf(omo, f[i + 9], P - M);
     }
 }
 

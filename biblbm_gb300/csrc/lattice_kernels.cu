@@ -122,8 +122,9 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
     using FT = typename Store<T>::F;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
-    const int tx = blockIdx.x * blockDim.x + threadIdx.x;
-    const int row = blockIdx.y * blockDim.y + threadIdx.y;
+    // grid.x runs over blocks of rows (ny * nz can exceed the 65535 limit of grid.y)
+    const int tx = blockIdx.y * blockDim.x + threadIdx.x;
+    const int row = blockIdx.x * blockDim.y + threadIdx.y;
     if (row >= d.ny * d.nz) return;  // uniform per warp: a warp never spans two rows
     const int y = row % d.ny, z = row / d.ny;
     const int x0 = 2 * tx;
@@ -436,7 +437,7 @@ void collide_stream_t(const Lattice& L, bool coupled, cudaStream_t s) {
         const int bx = std::min(256, (pairs + 31) / 32 * 32);
         const int by = std::max(1, 256 / bx);
         const int rows = L.d.ny * L.d.nz;
-        dim3 grid((pairs + bx - 1) / bx, (rows + by - 1) / by);
+        dim3 grid((rows + by - 1) / by, (pairs + bx - 1) / bx);
         dim3 block(bx, by);
         const T* fin = (const T*)L.f[L.cur];
         T* fout = (T*)L.f[1 - L.cur];

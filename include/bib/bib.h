@@ -130,7 +130,8 @@ typedef struct {
 typedef struct {
     int32_t collide_kernel; /* BIB_KERNEL_*: AUTO takes the shared-memory staged kernel where the x-row fits */
     int32_t tile_cells;     /* staged kernel: cells per tile (whole x-rows); 0 = 512 (256 for FP64) */
-    int32_t reserved[6];
+    int32_t stages;         /* staged kernel: pipeline depth 2..4; 0 = the deepest that keeps the CTAs resident */
+    int32_t reserved[5];
 } bib_tuning;
 
 /* ---- context (src/coProcessors/coProcessor3D.h:57-115 lifetime) ---- */
