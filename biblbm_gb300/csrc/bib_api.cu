@@ -152,6 +152,20 @@ bool build_shape(ShapeHost& S, const double* xyz, const int64_t* tri, int64_t nv
         S.pair_cs.push_back(dt(n1, n2));
         S.pair_cs.push_back((dt(sub(n1, n2), sub(p1, p3)) > 0 ? 1.0 : -1.0) * nrm(crs(n1, n2)));
     }
+    // FP32 copies of the rest-state constants for the reduced-precision element kernels
+    S.tri_rest_f.resize(4 * nt);
+    S.tri_area_f.resize(nt);
+    for (int64_t t = 0; t < nt; ++t) {
+        const V3d a = P(S.tri[3 * t]), b = P(S.tri[3 * t + 1]), c = P(S.tri[3 * t + 2]);
+        const V3d e0 = sub(b, a), e1 = sub(c, a);
+        const double l0 = nrm(e0), l0p = nrm(e1);
+        S.tri_rest_f[4 * t] = (float)l0;
+        S.tri_rest_f[4 * t + 1] = (float)l0p;
+        S.tri_rest_f[4 * t + 2] = (float)(dt(e0, e1) / (l0 * l0p));
+        S.tri_rest_f[4 * t + 3] = (float)(nrm(crs(e0, e1)) / (l0 * l0p));
+        S.tri_area_f[t] = (float)S.tri_area[t];
+    }
+    S.pair_cs_f.assign(S.pair_cs.begin(), S.pair_cs.end());
     // per-vertex incidence lists for the deterministic force gather: links, then triangles,
     // then pairs, each in element order (the order of the reference's element loops)
     std::vector<std::vector<int>> incv(nv);
@@ -345,6 +359,9 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
         d.pair_cs = S.dev.pair_cs;
         d.inc_off = S.dev.inc_off;
         d.inc = S.dev.inc;
+        d.tri_rest_f = S.dev.tri_rest_f;
+        d.tri_area_f = S.dev.tri_area_f;
+        d.pair_cs_f = S.dev.pair_cs_f;
         d.A0 = S.area;
         for (int k = 0; k < BIB_P_COUNT; ++k) d.prm[k] = ph.prm[k];
         L.max_nv = std::max(L.max_nv, ph.nv);
@@ -596,6 +613,9 @@ void bib_destroy(bib_ctx* c) {
         cudaFree(S->dev.pair_cs);
         cudaFree(S->dev.inc_off);
         cudaFree(S->dev.inc);
+        cudaFree(S->dev.tri_rest_f);
+        cudaFree(S->dev.tri_area_f);
+        cudaFree(S->dev.pair_cs_f);
     }
     for (int k = 0; k < 6; ++k)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
@@ -934,7 +954,8 @@ bib_status bib_shape_store(bib_ctx* c, const double* xyz, const int64_t* tri, in
         (st = upload(c, &S->dev.tri_area, S->tri_area)) || (st = upload(c, &S->dev.links, S->links)) ||
         (st = upload(c, &S->dev.link_len, S->link_len)) || (st = upload(c, &S->dev.pairs, S->pairs)) ||
         (st = upload(c, &S->dev.pair_cs, S->pair_cs)) || (st = upload(c, &S->dev.inc_off, S->inc_off)) ||
-        (st = upload(c, &S->dev.inc, S->inc)))
+        (st = upload(c, &S->dev.inc, S->inc)) || (st = upload(c, &S->dev.tri_rest_f, S->tri_rest_f)) ||
+        (st = upload(c, &S->dev.tri_area_f, S->tri_area_f)) || (st = upload(c, &S->dev.pair_cs_f, S->pair_cs_f)))
         return st;
     S->dev.nv = (int)nv;
     S->dev.nt = (int)nt;

@@ -51,6 +51,10 @@ struct ShapeDev {
     double* pair_cs;      // 2*np
     int* inc_off;         // nv+1: per-vertex incidence lists (links, triangles, pairs)
     int* inc;             // (type << 29) | element id
+    // FP32 copies for the reduced-precision element kernels
+    float* tri_rest_f;    // 4*nt: rest l0, l0', cos(phi0), sin(phi0) of each triangle
+    float* tri_area_f;    // nt
+    float* pair_cs_f;     // 2*np
 };
 
 // One particle as the device kernels see it.
@@ -67,6 +71,9 @@ struct ParticleDev {
     const double* pair_cs;
     const int* inc_off;
     const int* inc;
+    const float* tri_rest_f;
+    const float* tri_area_f;
+    const float* pair_cs_f;
     double A0;
     double prm[BIB_P_COUNT];
 };
@@ -77,6 +84,7 @@ constexpr int STATS = 5;
 struct ShapeHost {
     std::vector<double> rest, tri_area, link_len, pair_cs;
     std::vector<int> tri, links, pairs, inc_off, inc;
+    std::vector<float> tri_rest_f, tri_area_f, pair_cs_f;
     double area = 0, volume = 0;
     ShapeDev dev{};
 };

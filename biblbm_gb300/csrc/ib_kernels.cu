@@ -30,29 +30,36 @@ __device__ __forceinline__ W dirac_eval(int dirac, W x) {
 __device__ __forceinline__ double half_support(int dirac) { return dirac == BIB_DIRAC_PESKIN ? 2.0 : 1.5; }
 __device__ __forceinline__ int support(int dirac) { return dirac == BIB_DIRAC_PESKIN ? 4 : 3; }
 
-// Arithmetic1D::min_mod_diff (periodic) / plain difference, src/fsi/Periodicity.h:26-34, 93-96
-__device__ __forceinline__ double axis_dist(int periodic, int N, double Linv, double a, double b) {
-    const double x = a - b;
-    if (!periodic) return x;
-    return x - floor(x * Linv + 0.5) * (double)N;
-}
-
-// Node classification of a single-block domain (ImmersedBoundaryDynamics.hh:46-66, 351-363):
-// 1 bulk (support inside the domain), 2 envelope (general path), 0 outside.
-__device__ int classify(const LatticeDesc& d, int dirac, const double* p) {
+// Node classes of a single-block domain (ImmersedBoundaryDynamics.hh:46-66, 351-363): a
+// vertex is in the envelope when, on every axis, the min-mod distance from the domain
+// centre (N - 1)/2 is below the half width (N - 1)/2 + h (the bulk / envelope split only
+// selects between two interpolators with the same result here).  On a periodic axis the
+// min-mod distance is at most N/2 < (N - 1)/2 + h, so only walled axes can put a vertex
+// outside.  Non-finite positions are outside.
+__device__ __forceinline__ bool inside_envelope(const LatticeDesc& d, int dirac, const double* p) {
     const double h = half_support(dirac);
     const int N[3] = {d.nx, d.ny, d.nz};
     const int per[3] = {d.px, d.py, d.pz};
-    const double shrink = 0.5 - h - DBL_EPSILON;
-    bool in_env = true, in_bulk = true;
+    bool in = true;
     for (int a = 0; a < 3; ++a) {
-        const double top = (double)(N[a] - 1);
-        const double elo = 0.0 - h, ehi = top + h;
-        const double blo = 0.0 - shrink, bhi = top + shrink;
-        in_env = in_env && fabs(axis_dist(per[a], N[a], d.inv_n[a], 0.5 * (elo + ehi), p[a])) < 0.5 * (ehi - elo);
-        in_bulk = in_bulk && fabs(axis_dist(per[a], N[a], d.inv_n[a], 0.5 * (blo + bhi), p[a])) < 0.5 * (bhi - blo);
+        if (per[a]) {
+            in = in && isfinite(p[a]);
+        } else {
+            const double top = (double)(N[a] - 1);
+            const double elo = 0.0 - h, ehi = top + h;
+            in = in && fabs(0.5 * (elo + ehi) - p[a]) < 0.5 * (ehi - elo);
+        }
     }
-    return !in_env ? 0 : (in_bulk ? 1 : 2);
+    return in;
+}
+
+// Positive remainder of x modulo N; the division is only taken more than a period away.
+__device__ __forceinline__ int pmod(int64_t x, int N) {
+    if (x >= 0 && x < N) return (int)x;
+    if (x < 0 && x >= -(int64_t)N) return (int)(x + N);
+    if (x >= N && x < 2LL * N) return (int)(x - N);
+    const int64_t r = x % N;
+    return (int)(r < 0 ? r + N : r);
 }
 
 // Arithmetic1D::remap_int(i, offset) with i0 = 0, Periodicity.h:106-110; returns a global
@@ -60,13 +67,70 @@ __device__ int classify(const LatticeDesc& d, int dirac, const double* p) {
 __device__ __forceinline__ int remap_global(int periodic, int N, int64_t i_local, int off) {
     int64_t g;
     if (periodic) {
-        int64_t val = ((i_local + off + 100LL * N) % N) - off;
+        int val = pmod(i_local + off, N) - off;
         if (val < 0) val += N;
-        g = val + off;
+        g = (int64_t)val + off;
     } else {
         g = i_local + off;
     }
     return (g < 0 || g >= N) ? -1 : (int)g;
+}
+
+// Delta weight of support node lo + m on one axis, phi(lo + m - x) with lo = ceil(x - h).
+// FP32 weights take the FP64 offset lo - x and add m in FP32.
+template <class W>
+__device__ __forceinline__ W axis_weight(int dirac, int64_t lo, double x, int m) {
+    if (sizeof(W) == sizeof(double)) return dirac_eval<W>(dirac, (W)((double)(lo + m) - x));
+    return dirac_eval<W>(dirac, (W)((double)lo - x) + (W)m);
+}
+template <class W, int S>
+__device__ __forceinline__ int64_t axis_weights(double x, W* w) {
+    constexpr int dirac = S == 4 ? BIB_DIRAC_PESKIN : BIB_DIRAC_ROMA;
+    const int64_t lo = (int64_t)ceil(x - half_support(dirac));
+#pragma unroll
+    for (int m = 0; m < S; ++m) w[m] = axis_weight<W>(dirac, lo, x, m);
+    return lo;
+}
+
+// Windows of up to four consecutive cells of one x-row of one field component, moved as
+// one or two aligned float4 accesses (the field rows start 16-byte aligned: the component
+// stride is a multiple of 128 cells).  Slots outside the window read / add zero.
+__device__ __forceinline__ float window_select(const float* x, int j, int o, int s) {
+    float r = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+        if (m < s && j - o == m) r = x[m];
+    return r;
+}
+__device__ __forceinline__ void red_window(float* row, int64_t k0, const float* v, int s) {
+    const int64_t kq = k0 & ~(int64_t)3;
+    const int o = (int)(k0 - kq);
+    float4* q = reinterpret_cast<float4*>(row + kq);
+    atomicAdd(q, make_float4(window_select(v, 0, o, s), window_select(v, 1, o, s), window_select(v, 2, o, s),
+                             window_select(v, 3, o, s)));
+    if (o + s > 4)
+        atomicAdd(q + 1, make_float4(window_select(v, 4, o, s), window_select(v, 5, o, s), window_select(v, 6, o, s),
+                                     window_select(v, 7, o, s)));
+}
+// sum_m w[m] * row[k0 + m]
+__device__ __forceinline__ float dot_window(const float* row, int64_t k0, const float* w, int s) {
+    const int64_t kq = k0 & ~(int64_t)3;
+    const int o = (int)(k0 - kq);
+    const float4* q = reinterpret_cast<const float4*>(row + kq);
+    const float4 a = __ldg(q);
+    const float4 b = o + s > 4 ? __ldg(q + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float x[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+    float acc = 0.0f;
+#pragma unroll
+    for (int m = 0; m < 4; ++m)
+        if (m < s) {
+            float xm = 0.0f;
+#pragma unroll
+            for (int j = 0; j < 8; ++j)
+                if (j == o + m) xm = x[j];
+            acc += w[m] * xm;
+        }
+    return acc;
 }
 
 // ---------------------------------------------------------------- interpolation
@@ -75,46 +139,71 @@ __device__ __forceinline__ int remap_global(int periodic, int N, int64_t i_local
 // X_{n+1} = X_n + U_n (DeformableParticle3D::move_vertices, DeformableParticle3D.hh:26-51).
 // Classes and index arithmetic follow interpolate_impl with the Bulk / General
 // interpolators, ImmersedBoundaryDynamics_interpolation.hh:13-153.
-template <class UT>
+template <class UT, int S>
 __global__ void __launch_bounds__(128) k_interpolate_move(LatticeDesc d, IbDesc ib, int nvert, const double* __restrict__ pos,
                                                            double* __restrict__ pos_next, const UT* __restrict__ u,
                                                            double* __restrict__ vel) {
     using C = UT;
+    static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvert) return;
     const double p[3] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
     double out[3] = {0.0, 0.0, 0.0};
-    const int cls = classify(d, ib.dirac, p);
-    if (cls != 0) {
+    if (inside_envelope(d, ib.dirac, p)) {
         const int off = (int)ib.offset;
-        const double pr[3] = {p[0] - ib.offset, p[1] - ib.offset, p[2] - ib.offset};
-        const double h = half_support(ib.dirac);
-        const int s = support(ib.dirac);
+        constexpr int s = S;
         int64_t lo[3];
         C w[3][4];
-        for (int a = 0; a < 3; ++a) {
-            lo[a] = (int64_t)ceil(pr[a] - h);
-            for (int m = 0; m < s; ++m) w[a][m] = dirac_eval<C>(ib.dirac, (C)((double)(lo[a] + m) - pr[a]));
-        }
+        for (int a = 0; a < 3; ++a) lo[a] = axis_weights<C, S>(p[a] - ib.offset, w[a]);
         int gx[4], gy[4], gz[4];
+#pragma unroll
         for (int m = 0; m < s; ++m) {
             gx[m] = remap_global(d.px, d.nx, lo[0] + m, off);
             gy[m] = remap_global(d.py, d.ny, lo[1] + m, off);
             gz[m] = remap_global(d.pz, d.nz, lo[2] + m, off);
         }
+        int64_t yo[4], zo[4];  // row offsets of the support nodes
+#pragma unroll
+        for (int m = 0; m < s; ++m) {
+            yo[m] = (int64_t)gy[m] * d.nx;
+            zo[m] = (int64_t)gz[m] * d.ny * d.nx;
+        }
         C acc[3] = {C(0), C(0), C(0)};
-        for (int a = 0; a < s; ++a) {
-            if (gx[a] < 0) continue;
+        if (sizeof(UT) == sizeof(float) && gx[s - 1] == gx[0] + s - 1) {
+            // FP32 field and no periodic wrap along x inside the support: each (y, z) row is
+            // one window of s consecutive cells, read with aligned vector loads
+            const float* uf = reinterpret_cast<const float*>(u);
+#pragma unroll
             for (int b = 0; b < s; ++b) {
                 if (gy[b] < 0) continue;
-                const C wxy = w[0][a] * w[1][b];
+#pragma unroll
                 for (int c = 0; c < s; ++c) {
                     if (gz[c] < 0) continue;
-                    const C wt = wxy * w[2][c];
-                    const int64_t k = gx[a] + (int64_t)d.nx * (gy[b] + (int64_t)d.ny * gz[c]);
-                    acc[0] += wt * __ldg(u + k);
-                    acc[1] += wt * __ldg(u + d.stride + k);
-                    acc[2] += wt * __ldg(u + 2 * d.stride + k);
+                    const float wyz = (float)(w[1][b] * w[2][c]);
+                    const int64_t k0 = gx[0] + yo[b] + zo[c];
+                    float wx[4];
+                    for (int m = 0; m < 4; ++m) wx[m] = m < s ? (float)w[0][m] * wyz : 0.0f;
+                    for (int q = 0; q < 3; ++q) acc[q] += (C)dot_window(uf + q * d.stride, k0, wx, s);
+                }
+            }
+        } else {
+#pragma unroll
+            for (int a = 0; a < s; ++a) {
+                if (gx[a] < 0) continue;
+#pragma unroll
+                for (int b = 0; b < s; ++b) {
+                    if (gy[b] < 0) continue;
+                    const C wxy = w[0][a] * w[1][b];
+                    const UT* col = u + gx[a] + yo[b];
+#pragma unroll
+                    for (int c = 0; c < s; ++c) {
+                        if (gz[c] < 0) continue;
+                        const C wt = wxy * w[2][c];
+                        const UT* q = col + zo[c];
+                        acc[0] += wt * __ldg(q);
+                        acc[1] += wt * __ldg(q + d.stride);
+                        acc[2] += wt * __ldg(q + 2 * d.stride);
+                    }
                 }
             }
         }
@@ -131,42 +220,71 @@ __global__ void __launch_bounds__(128) k_interpolate_move(LatticeDesc d, IbDesc 
 }
 
 // ---------------------------------------------------------------- spreading
-template <class FT>
+template <class FT, int S>
 __global__ void __launch_bounds__(128) k_spread(LatticeDesc d, IbDesc ib, int nvert, const double* __restrict__ pos,
                                                  const double* __restrict__ force, FT* __restrict__ F) {
+    static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvert) return;
     const double p[3] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
-    if (classify(d, ib.dirac, p) == 0) return;
+    if (!inside_envelope(d, ib.dirac, p)) return;
     const int off = (int)ib.offset;
-    const double pr[3] = {p[0] - ib.offset, p[1] - ib.offset, p[2] - ib.offset};
-    const double h = half_support(ib.dirac);
-    const int s = support(ib.dirac);
+    constexpr int s = S;
     int64_t lo[3];
     FT w[3][4];
-    for (int a = 0; a < 3; ++a) {
-        lo[a] = (int64_t)ceil(pr[a] - h);
-        for (int m = 0; m < s; ++m) w[a][m] = dirac_eval<FT>(ib.dirac, (FT)((double)(lo[a] + m) - pr[a]));
-    }
+    for (int a = 0; a < 3; ++a) lo[a] = axis_weights<FT, S>(p[a] - ib.offset, w[a]);
     int gx[4], gy[4], gz[4];
+#pragma unroll
     for (int m = 0; m < s; ++m) {
         gx[m] = remap_global(d.px, d.nx, lo[0] + m, off);
         gy[m] = remap_global(d.py, d.ny, lo[1] + m, off);
         gz[m] = remap_global(d.pz, d.nz, lo[2] + m, off);
     }
+    int64_t yo[4], zo[4];
+#pragma unroll
+    for (int m = 0; m < s; ++m) {
+        yo[m] = (int64_t)gy[m] * d.nx;
+        zo[m] = (int64_t)gz[m] * d.ny * d.nx;
+    }
     const FT fv[3] = {(FT)force[3 * v], (FT)force[3 * v + 1], (FT)force[3 * v + 2]};
+    if (sizeof(FT) == sizeof(float) && gx[s - 1] == gx[0] + s - 1) {
+        // FP32 field and no periodic wrap along x inside the support: each (y, z) row of
+        // each component receives one window of s values through one or two float4 atomics
+        float* Ff = reinterpret_cast<float*>(F);
+#pragma unroll
+        for (int b = 0; b < s; ++b) {
+            if (gy[b] < 0) continue;
+#pragma unroll
+            for (int c = 0; c < s; ++c) {
+                if (gz[c] < 0) continue;
+                const FT wyz = w[1][b] * w[2][c];
+                const int64_t k0 = gx[0] + yo[b] + zo[c];
+#pragma unroll
+                for (int q = 0; q < 3; ++q) {
+                    float vals[4];
+                    for (int m = 0; m < 4; ++m) vals[m] = m < s ? (float)((w[0][m] * wyz) * fv[q]) : 0.0f;
+                    red_window(Ff + q * d.stride, k0, vals, s);
+                }
+            }
+        }
+        return;
+    }
+#pragma unroll
     for (int a = 0; a < s; ++a) {
         if (gx[a] < 0) continue;
+#pragma unroll
         for (int b = 0; b < s; ++b) {
             if (gy[b] < 0) continue;
             const FT wxy = w[0][a] * w[1][b];
+            FT* col = F + gx[a] + yo[b];
+#pragma unroll
             for (int c = 0; c < s; ++c) {
                 if (gz[c] < 0) continue;
                 const FT wt = wxy * w[2][c];
-                const int64_t k = gx[a] + (int64_t)d.nx * (gy[b] + (int64_t)d.ny * gz[c]);
-                atomicAdd(F + k, wt * fv[0]);
-                atomicAdd(F + d.stride + k, wt * fv[1]);
-                atomicAdd(F + 2 * d.stride + k, wt * fv[2]);
+                FT* q = col + zo[c];
+                atomicAdd(q, wt * fv[0]);
+                atomicAdd(q + d.stride, wt * fv[1]);
+                atomicAdd(q + 2 * d.stride, wt * fv[2]);
             }
         }
     }
@@ -190,7 +308,7 @@ __global__ void __launch_bounds__(128) k_spread_keys(LatticeDesc d, IbDesc ib, i
     if (v >= nvert) return;
     const int s = support(ib.dirac), s3 = s * s * s;
     const double p[3] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
-    const bool inside = classify(d, ib.dirac, p) != 0;
+    const bool inside = inside_envelope(d, ib.dirac, p);
     const int off = (int)ib.offset;
     const double h = half_support(ib.dirac);
     int64_t lo[3];
@@ -227,7 +345,7 @@ __global__ void __launch_bounds__(128) k_spread_reduce(LatticeDesc d, IbDesc ib,
         const int sel[3] = {a, b, c};
         for (int ax = 0; ax < 3; ++ax) {
             const int64_t lo = (int64_t)ceil(pr[ax] - h);
-            w[ax] = dirac_eval<FT>(ib.dirac, (FT)((double)(lo + sel[ax]) - pr[ax]));
+            w[ax] = axis_weight<FT>(ib.dirac, lo, pr[ax], sel[ax]);
         }
         const FT wt = (w[0] * w[1]) * w[2];
         acc[0] += wt * (FT)force[3 * v];
@@ -301,24 +419,115 @@ struct SharedPos {
     __device__ __forceinline__ V3<M> operator()(int v) const { return mk3<M>(sp[3 * v], sp[3 * v + 1], sp[3 * v + 2]); }
 };
 
+// Per-particle constants of the element kernels, evaluated once per thread in the
+// element precision M (the FP64 expressions are the reference's, so M = double gives the
+// same values as evaluating them per element).
+template <class M>
+struct MemCoef {
+    M G, C;            // capsule shear modulus and area-dilation ratio
+    M kb;              // bending modulus
+    M k_area_local;
+    M df_area_global;  // k_area_global (A0 - A) / A0
+    M df_vol6;         // k_volume (V_desired - V) / V_desired / 6
+};
+template <class M>
+__device__ __forceinline__ MemCoef<M> mem_coef(const ParticleDev& P, double area, double volume) {
+    MemCoef<M> k;
+    k.G = (M)P.prm[BIB_P_G];
+    k.C = (M)P.prm[BIB_P_C];
+    k.kb = (M)P.prm[BIB_P_K_BEND];
+    k.k_area_local = (M)P.prm[BIB_P_K_AREA_LOCAL];
+    k.df_area_global = (M)(P.prm[BIB_P_K_AREA_GLOBAL] * (P.A0 - area) / P.A0);
+    k.df_vol6 = (M)(P.prm[BIB_P_K_VOLUME] * (P.prm[BIB_P_VOL_DESIRED] - volume) / P.prm[BIB_P_VOL_DESIRED]) / M(6);
+    return k;
+}
+template <class M>
+__device__ __forceinline__ M tri_area_of(const ParticleDev& P, int t) {
+    return sizeof(M) == sizeof(double) ? (M)P.tri_area[t] : (M)P.tri_area_f[t];
+}
+template <class M>
+__device__ __forceinline__ M pair_c(const ParticleDev& P, int p, int k) {
+    return sizeof(M) == sizeof(double) ? (M)P.pair_cs[2 * p + k] : (M)P.pair_cs_f[2 * p + k];
+}
+
 // DeformableCapsuleParticle::compute_forces for one triangle, src/fsi/DeformableCapsule.hh:68-148
-// (with the reference's c = l' sin(phi) / (l' sin(phi0)), line 96).
+// (with the reference's c = l' sin(phi) / (l' sin(phi0)), line 96).  The rest-state lengths
+// and angle come from the FP64 rest mesh (M = double) or its FP32 copies.
 template <class M, class PS, class Sink>
-__device__ void capsule_triangle(const ParticleDev& P, int t, const PS& ps, int skalak, Sink& sk) {
+__device__ void capsule_triangle(const ParticleDev& P, int t, const PS& ps, int skalak, const MemCoef<M>& k,
+                                 Sink& sk) {
     const int i0 = P.tri[3 * t], i1 = P.tri[3 * t + 1], i2 = P.tri[3 * t + 2];
     const int id[3] = {i0, i1, i2};
     const V3<M> p0 = ps(i0), p1 = ps(i1), p2 = ps(i2);
     const V3<M> e0 = p1 - p0, e1 = p2 - p0;
-    const V3<M> e0_0 = mk3<M>((M)(P.rest[3 * i1] - P.rest[3 * i0]), (M)(P.rest[3 * i1 + 1] - P.rest[3 * i0 + 1]),
-                              (M)(P.rest[3 * i1 + 2] - P.rest[3 * i0 + 2]));
-    const V3<M> e1_0 = mk3<M>((M)(P.rest[3 * i2] - P.rest[3 * i0]), (M)(P.rest[3 * i2 + 1] - P.rest[3 * i0 + 1]),
-                              (M)(P.rest[3 * i2 + 2] - P.rest[3 * i0 + 2]));
-    const M l = norm3(e0), lp = norm3(e1), l0 = norm3(e0_0), l0p = norm3(e1_0);
+    M l0, l0p, sin_phi_0, cos_phi_0;
+    if (sizeof(M) == sizeof(double)) {
+        const V3<M> e0_0 = mk3<M>((M)(P.rest[3 * i1] - P.rest[3 * i0]), (M)(P.rest[3 * i1 + 1] - P.rest[3 * i0 + 1]),
+                                  (M)(P.rest[3 * i1 + 2] - P.rest[3 * i0 + 2]));
+        const V3<M> e1_0 = mk3<M>((M)(P.rest[3 * i2] - P.rest[3 * i0]), (M)(P.rest[3 * i2 + 1] - P.rest[3 * i0 + 1]),
+                                  (M)(P.rest[3 * i2 + 2] - P.rest[3 * i0 + 2]));
+        l0 = norm3(e0_0);
+        l0p = norm3(e1_0);
+        sin_phi_0 = norm3(cross3(e0_0, e1_0)) / (l0 * l0p);
+        cos_phi_0 = dot3(e0_0, e1_0) / (l0 * l0p);
+    } else {
+        const float4 r = reinterpret_cast<const float4*>(P.tri_rest_f)[t];
+        l0 = (M)r.x;
+        l0p = (M)r.y;
+        cos_phi_0 = (M)r.z;
+        sin_phi_0 = (M)r.w;
+    }
+    if constexpr (sizeof(M) == sizeof(float)) {
+        // The same forces with the corner-independent scalars gathered: every gradient of
+        // D11, D22, D12 (hence of I1, I2) is a combination of the corner gradients of
+        // l, l' and cos(phi) (gl, glp, gc below), so f_i = pref (Cl gl_i + Cp glp_i + Cq gc_i);
+        // reciprocals are taken once.
+        const M l = norm3(e0), lp = norm3(e1);
+        const M e0e1 = dot3(e0, e1), cr = norm3(cross3(e0, e1));
+        const M rl = M(1) / l, rlp = M(1) / lp, rl0 = M(1) / l0, rl0p = M(1) / l0p, rs0 = M(1) / sin_phi_0;
+        const M rllp = rl * rlp;
+        const M sin_phi = cr * rllp, cos_phi = e0e1 * rllp;
+        const M a = l * rl0;
+        const M b = (lp * cos_phi * rl0p - l * cos_phi_0 * rl0) * rs0;
+        const M c = sin_phi * rs0;
+        const M D11 = (a * a - M(1)) * M(0.5);
+        const M D22 = (b * b + c * c - M(1)) * M(0.5);
+        const M D12 = a * b * M(0.5);
+        const M I1 = M(2) * (D11 + D22);
+        const M I2 = I1 + M(4) * (D11 * D22 - D12 * D12);
+        M w1, w2;
+        if (skalak) {
+            w1 = I1 + M(1);
+            w2 = k.C * I2 - M(1);
+        } else {
+            const M q = M(1) + I2;
+            w1 = M(1);
+            w2 = -M(1) / (q * q);
+        }
+        const M A11 = l * rl0 * rl0, s2 = rs0 * rs0;
+        const M k22p = s2 * (lp * rl0p * rl0p - l * cos_phi * cos_phi_0 * rl0 * rl0p);
+        const M k22l = s2 * (l * cos_phi_0 * cos_phi_0 * rl0 * rl0 - lp * cos_phi * cos_phi_0 * rl0p * rl0);
+        const M k22c = -s2 * l * lp * cos_phi_0 * rl0 * rl0p;
+        const M k12 = M(0.5) * rl0p * rs0;
+        const M k12l = k12 * (lp * cos_phi * rl0p - M(2) * l * cos_phi_0 * rl0);
+        const M k12p = k12 * l * cos_phi * rl0p, k12c = k12 * l * lp * rl0p;
+        const M al = M(2) + M(4) * D22, be = M(2) + M(4) * D11, ga = M(8) * D12;
+        const M Cl = M(2) * w1 * (A11 + k22l) + w2 * (al * A11 + be * k22l - ga * k12l);
+        const M Cp = M(2) * w1 * k22p + w2 * (be * k22p - ga * k12p);
+        const M Cq = M(2) * w1 * k22c + w2 * (be * k22c - ga * k12c);
+        const M t3 = e0e1 * rl * rl * rllp, t4 = e0e1 * rllp * rlp * rlp;
+        const M pref = -k.G * M(0.5) * tri_area_of<M>(P, t);
+        const V3<M> gl1 = rl * e0, glp2 = rlp * e1;
+        const V3<M> gc0 = (t3 - rllp) * e0 + (t4 - rllp) * e1, gc1 = rllp * e1 - t3 * e0, gc2 = rllp * e0 - t4 * e1;
+        sk(i0, pref * (M(-1) * (Cl * gl1 + Cp * glp2) + Cq * gc0));
+        sk(i1, pref * (Cl * gl1 + Cq * gc1));
+        sk(i2, pref * (Cp * glp2 + Cq * gc2));
+        return;
+    }
+    const M l = norm3(e0), lp = norm3(e1);
     const M e0e1 = dot3(e0, e1);
     const M sin_phi = norm3(cross3(e0, e1)) / (l * lp);
     const M cos_phi = e0e1 / (l * lp);
-    const M sin_phi_0 = norm3(cross3(e0_0, e1_0)) / (l0 * l0p);
-    const M cos_phi_0 = dot3(e0_0, e1_0) / (l0 * l0p);
     const M a = l / l0;
     const M b = (lp * cos_phi / l0p - l * cos_phi_0 / l0) / sin_phi_0;
     const M c = lp * sin_phi / (lp * sin_phi_0);
@@ -334,8 +543,8 @@ __device__ void capsule_triangle(const ParticleDev& P, int t, const PS& ps, int 
                          (M(1) / (l * lp)) * e1 - (e0e1 / (l * l * l * lp)) * e0,
                          (M(1) / (l * lp)) * e0 - (e0e1 / (l * lp * lp * lp)) * e1};
     const M s0sq = sin_phi_0 * sin_phi_0;
-    const M G = (M)P.prm[BIB_P_G], Cc = (M)P.prm[BIB_P_C];
-    const M pref = -G / M(2) * (M)P.tri_area[t];
+    const M G = k.G, Cc = k.C;
+    const M pref = -G / M(2) * tri_area_of<M>(P, t);
     for (int i = 0; i < 3; ++i) {
         const V3<M> gD11 = (l / (l0 * l0)) * gl[i];
         const V3<M> gD22 = (M(1) / s0sq) * ((lp / (l0p * l0p) - l * cos_phi * cos_phi_0 / (l0 * l0p)) * glp[i] +
@@ -380,7 +589,7 @@ __device__ void rbc_link(const ParticleDev& P, int l, const PS& ps, Sink& sk) {
 // tri::grad_signed_volume (TriangleUtils.h:58-120).  The volume gradient is
 // translation invariant on a closed surface, so it is taken relative to the centre.
 template <class M, class PS, class Sink>
-__device__ void rbc_triangle(const ParticleDev& P, int t, const PS& ps, double area, double volume, Sink& sk) {
+__device__ void rbc_triangle(const ParticleDev& P, int t, const PS& ps, const MemCoef<M>& k, Sink& sk) {
     const int i0 = P.tri[3 * t], i1 = P.tri[3 * t + 1], i2 = P.tri[3 * t + 2];
     const V3<M> v0 = ps(i0), v1 = ps(i1), v2 = ps(i2);
     const M v01v11 = v0.y - v1.y, v02v22 = v0.z - v2.z, v02v12 = v0.z - v1.z;
@@ -396,23 +605,22 @@ __device__ void rbc_triangle(const ParticleDev& P, int t, const PS& ps, double a
                             (a * v01v21 + b * (v2.x - v0.x)) * denom);
     const V3<M> g2 = mk3<M>((b * (v1.z - v0.z) + c * v01v11) * denom, (a * v02v12 + c * (v1.x - v0.x)) * denom,
                             (a * (v1.y - v0.y) + b * v00v10) * denom);
-    // penalty differences in FP64
-    const double A0 = P.A0;
-    M df_area = (M)(P.prm[BIB_P_K_AREA_GLOBAL] * (A0 - area) / A0);
-    df_area += (M)P.prm[BIB_P_K_AREA_LOCAL] * ((M)P.tri_area[t] - la) / (M)P.tri_area[t];
+    // the global penalty differences are evaluated once per particle, in FP64
+    const M a0t = tri_area_of<M>(P, t);
+    M df_area = k.df_area_global;
+    df_area += k.k_area_local * (a0t - la) / a0t;
     sk(i0, df_area * g0);
     sk(i1, df_area * g1);
     sk(i2, df_area * g2);
-    const M df_vol = (M)(P.prm[BIB_P_K_VOLUME] * (P.prm[BIB_P_VOL_DESIRED] - volume) / P.prm[BIB_P_VOL_DESIRED]);
-    sk(i0, (df_vol / M(6)) * cross3(v1, v2));
-    sk(i1, (df_vol / M(6)) * cross3(v2, v0));
-    sk(i2, (df_vol / M(6)) * cross3(v0, v1));
+    sk(i0, k.df_vol6 * cross3(v1, v2));
+    sk(i1, k.df_vol6 * cross3(v2, v0));
+    sk(i2, k.df_vol6 * cross3(v0, v1));
 }
 
 // Dihedral bending of one adjacent-triangle pair, src/fsi/RBCParticle.hh:217-246 with
 // tri::grad_angle_between_pair (TriangleUtils.h:139-164).
 template <class M, class PS, class Sink>
-__device__ void rbc_pair(const ParticleDev& P, int p, const PS& ps, Sink& sk) {
+__device__ void rbc_pair(const ParticleDev& P, int p, const PS& ps, const MemCoef<M>& k, Sink& sk) {
     const int* q = P.pairs + 4 * p;
     const V3<M> v0 = ps(q[0]), v1 = ps(q[1]), v2 = ps(q[2]), v3 = ps(q[3]);
     const V3<M> e0 = v1 - v0, e1 = v2 - v0, e2 = v3 - v0;
@@ -423,12 +631,24 @@ __device__ void rbc_pair(const ParticleDev& P, int p, const PS& ps, Sink& sk) {
     const V3<M> n1u = n1 / n1n, n2u = n2 / n2n;
     const M cos_t = dot3(n1u, n2u);
     const M sin_t = (dot3(n1 - n2, v1 - v3) > M(0) ? M(1) : M(-1)) * norm3(cross3(n1u, n2u));
-    const M pref = (M)P.prm[BIB_P_K_BEND] * (-(M)P.pair_cs[2 * p] * sin_t + (M)P.pair_cs[2 * p + 1] * cos_t);
+    const M pref = k.kb * (-pair_c<M>(P, p, 0) * sin_t + pair_c<M>(P, p, 1) * cos_t);
     sk(q[0], pref * ((dot3(e1u, e1 - e2) / n2n) * n2u + (dot3(e1u, e1 - e0) / n1n) * n1u));
     sk(q[1], pref * ((-e1n / n1n) * n1u));
     sk(q[2], pref * ((dot3(e1u, e2) / n2n) * n2u + (dot3(e1u, e0) / n1n) * n1u));
     sk(q[3], pref * ((-e1n / n2n) * n2u));
 }
+
+// Forces on the three corners of one triangle, summed in registers and handed on once.
+template <class M>
+struct CornerSink {
+    int id[3];
+    V3<M> f[3];
+    __device__ __forceinline__ void operator()(int v, V3<M> g) {
+        if (v == id[0]) f[0] = f[0] + g;
+        else if (v == id[1]) f[1] = f[1] + g;
+        else f[2] = f[2] + g;
+    }
+};
 
 template <class T>
 __device__ __forceinline__ T block_sum(T v, T* red) {
@@ -471,15 +691,22 @@ __global__ void __launch_bounds__(256) k_membrane(const ParticleDev* __restrict_
     const bool capsule = P.model == BIB_MODEL_CAPSULE_NEOHOOKEAN || P.model == BIB_MODEL_CAPSULE_SKALAK ||
                          P.model == BIB_MODEL_SKALAK_BENDING;
     const bool rbc_terms = P.model == BIB_MODEL_RBC_WLCPOW || P.model == BIB_MODEL_SKALAK_BENDING;
+    const MemCoef<M> k = mem_coef<M>(P, area, volume);
     auto run = [&](const auto& ps) {
-        if (capsule)
-            for (int t = threadIdx.x; t < P.nt; t += blockDim.x) capsule_triangle<M>(P, t, ps, skalak, sk);
+        // triangle terms (capsule law and RBC area / volume penalties) of one triangle are
+        // summed per corner before they reach the shared accumulators
+        if (capsule || rbc_terms)
+            for (int t = threadIdx.x; t < P.nt; t += blockDim.x) {
+                const V3<M> z = mk3<M>(0, 0, 0);
+                CornerSink<M> cs{{P.tri[3 * t], P.tri[3 * t + 1], P.tri[3 * t + 2]}, {z, z, z}};
+                if (capsule) capsule_triangle<M>(P, t, ps, skalak, k, cs);
+                if (rbc_terms) rbc_triangle<M>(P, t, ps, k, cs);
+                for (int c = 0; c < 3; ++c) sk(cs.id[c], cs.f[c]);
+            }
         if (P.model == BIB_MODEL_RBC_WLCPOW)
             for (int l = threadIdx.x; l < P.nl; l += blockDim.x) rbc_link<M>(P, l, ps, sk);
-        if (rbc_terms) {
-            for (int t = threadIdx.x; t < P.nt; t += blockDim.x) rbc_triangle<M>(P, t, ps, area, volume, sk);
-            for (int p = threadIdx.x; p < P.np; p += blockDim.x) rbc_pair<M>(P, p, ps, sk);
-        }
+        if (rbc_terms)
+            for (int p = threadIdx.x; p < P.np; p += blockDim.x) rbc_pair<M>(P, p, ps, k, sk);
     };
     if (rel) run(SharedPos<M>{sp});
     else run(GlobalPos<M>{pos + 3LL * P.v0, {0.0, 0.0, 0.0}});
@@ -514,6 +741,7 @@ __global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* _
                          P.model == BIB_MODEL_SKALAK_BENDING;
     const bool rbc_terms = P.model == BIB_MODEL_RBC_WLCPOW || P.model == BIB_MODEL_SKALAK_BENDING;
     const int skalak = P.model != BIB_MODEL_CAPSULE_NEOHOOKEAN;
+    const MemCoef<M> k = mem_coef<M>(P, area, volume);
     GatherSink<M> cap{lv, mk3<M>(0, 0, 0)}, rbc{lv, mk3<M>(0, 0, 0)};
     for (int e = P.inc_off[lv]; e < P.inc_off[lv + 1]; ++e) {
         const int code = P.inc[e];
@@ -521,10 +749,10 @@ __global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* _
         if (type == INC_LINK) {
             if (P.model == BIB_MODEL_RBC_WLCPOW) rbc_link<M>(P, id, ps, rbc);
         } else if (type == INC_TRI) {
-            if (capsule) capsule_triangle<M>(P, id, ps, skalak, cap);
-            if (rbc_terms) rbc_triangle<M>(P, id, ps, area, volume, rbc);
-        } else if (rbc_terms) {
-            rbc_pair<M>(P, id, ps, rbc);
+            if (capsule) capsule_triangle<M>(P, id, ps, skalak, k, cap);
+            if (rbc_terms) rbc_triangle<M>(P, id, ps, k, rbc);
+        } else if (type == INC_PAIR && rbc_terms) {
+            rbc_pair<M>(P, id, ps, k, rbc);
         }
     }
     V3<M> f = P.model == BIB_MODEL_SKALAK_BENDING ? cap.acc + rbc.acc : (capsule ? cap.acc : rbc.acc);
@@ -536,29 +764,45 @@ __global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* _
 // One CTA per particle: area, signed volume and area-weighted centroid of X_{n+1}
 // (DeformableParticle3D::update, DeformableParticle3D.hh:54-82), then the periodic
 // centre-of-mass remap (ParticleBase3D::map_center_of_mass_to_periodic_grid,
-// ParticleBase.hh:111-136), FP64.
+// ParticleBase.hh:111-136).  M = double follows the reference with absolute positions.
+// M = float (reduced-precision lattices) evaluates each triangle in FP32 on positions
+// relative to the previous centre of mass (exact FP64 subtraction, then rounding) and
+// accumulates in FP64; the signed volume of the closed surface does not depend on the
+// origin.
+template <class M>
 __global__ void __launch_bounds__(256) k_particle_update(LatticeDesc d, const ParticleDev* __restrict__ parts,
                                                           double* __restrict__ pos_next, double* __restrict__ stats) {
     __shared__ double red[32];
     __shared__ double delta[3];
+    extern __shared__ __align__(16) float sp[];  // M = float: relative vertex positions
     const ParticleDev& P = parts[blockIdx.x];
     double* st = stats + STATS * blockIdx.x;
-    double sa = 0, sv = 0, scx = 0, scy = 0, scz = 0;
+    const bool rel = sizeof(M) < sizeof(double);
+    const double c0 = rel ? st[2] : 0.0, c1 = rel ? st[3] : 0.0, c2 = rel ? st[4] : 0.0;
+    const double* pv = pos_next + 3LL * P.v0;
+    if (rel) {  // one FP64 subtraction and rounding per vertex coordinate
+        for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sp[i] = (float)(pv[i] - (i % 3 == 0 ? c0 : (i % 3 == 1 ? c1 : c2)));
+        __syncthreads();
+    }
+    auto vert = [&](int i) {
+        return rel ? mk3<M>((M)sp[3 * i], (M)sp[3 * i + 1], (M)sp[3 * i + 2])
+                   : mk3<M>((M)(pv[3 * i] - c0), (M)(pv[3 * i + 1] - c1), (M)(pv[3 * i + 2] - c2));
+    };
+    // per-thread partial sums in M (a few triangles each), block sums in FP64
+    M ta = 0, tv = 0, tcx = 0, tcy = 0, tcz = 0;
     for (int t = threadIdx.x; t < P.nt; t += blockDim.x) {
-        const double* a = pos_next + 3LL * (P.v0 + P.tri[3 * t]);
-        const double* b = pos_next + 3LL * (P.v0 + P.tri[3 * t + 1]);
-        const double* c = pos_next + 3LL * (P.v0 + P.tri[3 * t + 2]);
-        const V3<double> A = mk3(a[0], a[1], a[2]), B = mk3(b[0], b[1], b[2]), Cv = mk3(c[0], c[1], c[2]);
-        const double dA = norm3(cross3(B - A, Cv - A)) * 0.5;
-        sa += dA;
+        const V3<M> A = vert(P.tri[3 * t]), B = vert(P.tri[3 * t + 1]), Cv = vert(P.tri[3 * t + 2]);
+        const M dA = norm3(cross3(B - A, Cv - A)) * M(0.5);
+        ta += dA;
         // multiplications by 1/6 and 1/3 instead of the reference's divisions (FP64 division
         // is a long instruction sequence on this part); differences are within one ulp per term
-        sv += dot3(A, cross3(B, Cv)) * (1.0 / 6.0);
-        const V3<double> cen = (1.0 / 3.0) * (A + B + Cv);
-        scx += cen.x * dA;
-        scy += cen.y * dA;
-        scz += cen.z * dA;
+        tv += dot3(A, cross3(B, Cv)) * (M(1) / M(6));
+        const V3<M> cen = (M(1) / M(3)) * (A + B + Cv);
+        tcx += cen.x * dA;
+        tcy += cen.y * dA;
+        tcz += cen.z * dA;
     }
+    double sa = (double)ta, sv = (double)tv, scx = (double)tcx, scy = (double)tcy, scz = (double)tcz;
     sa = block_sum(sa, red);
     __syncthreads();
     sv = block_sum(sv, red);
@@ -569,7 +813,7 @@ __global__ void __launch_bounds__(256) k_particle_update(LatticeDesc d, const Pa
     __syncthreads();
     scz = block_sum(scz, red);
     if (threadIdx.x == 0) {
-        const double com[3] = {scx / sa, scy / sa, scz / sa};
+        const double com[3] = {c0 + scx / sa, c1 + scy / sa, c2 + scz / sa};
         const int N[3] = {d.nx, d.ny, d.nz};
         const int per[3] = {d.px, d.py, d.pz};
         double np_[3];
@@ -636,15 +880,23 @@ cudaError_t launch_spread_sorted(const LatticeDesc& d, const IbDesc& ib, bool f6
 void configure_membrane_kernel(size_t smem) {
     cudaFuncSetAttribute(k_membrane<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     cudaFuncSetAttribute(k_membrane<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // 3 floats per vertex, at most half of the membrane kernel's 3 doubles per vertex
+    cudaFuncSetAttribute(k_particle_update<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2));
 }
 
 void launch_interpolate_move(const Lattice& L, cudaStream_t s) {
     if (L.nvert == 0) return;
     const unsigned g = (L.nvert + 127) / 128;
-    if (L.storage == BIB_STORAGE_F64)
-        k_interpolate_move<double><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, L.pos[L.pcur], L.pos[1 - L.pcur], (const double*)L.u, L.vel);
-    else
-        k_interpolate_move<float><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, L.pos[L.pcur], L.pos[1 - L.pcur], (const float*)L.u, L.vel);
+    const bool peskin = L.ib.dirac == BIB_DIRAC_PESKIN;
+    const double* p0 = L.pos[L.pcur];
+    double* p1 = L.pos[1 - L.pcur];
+    if (L.storage == BIB_STORAGE_F64) {
+        if (peskin) k_interpolate_move<double, 4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, p0, p1, (const double*)L.u, L.vel);
+        else k_interpolate_move<double, 3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, p0, p1, (const double*)L.u, L.vel);
+    } else {
+        if (peskin) k_interpolate_move<float, 4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, p0, p1, (const float*)L.u, L.vel);
+        else k_interpolate_move<float, 3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, p0, p1, (const float*)L.u, L.vel);
+    }
 }
 
 void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
@@ -667,7 +919,10 @@ void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
 void launch_particle_update(const Lattice& L, cudaStream_t s) {
     const int np = (int)L.parts.size();
     if (np == 0) return;
-    k_particle_update<<<np, 256, 0, s>>>(L.d, L.pdev, L.pos[1 - L.pcur], L.stats);
+    if (L.storage == BIB_STORAGE_F64)
+        k_particle_update<double><<<np, 256, 0, s>>>(L.d, L.pdev, L.pos[1 - L.pcur], L.stats);
+    else
+        k_particle_update<float><<<np, 256, 3 * sizeof(float) * L.max_nv, s>>>(L.d, L.pdev, L.pos[1 - L.pcur], L.stats);
 }
 
 void launch_spread(const Lattice& L, int fbuf, cudaStream_t s) {
@@ -688,8 +943,16 @@ void launch_spread(const Lattice& L, int fbuf, cudaStream_t s) {
             k_spread_reduce<float><<<ge, 128, 0, s>>>(L.d, L.ib, ne, L.sort_keys[1], L.sort_ids[1], pos, L.force, (float*)L.F[fbuf]);
         return;
     }
-    if (L.storage == BIB_STORAGE_F64) k_spread<double><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, (double*)L.F[fbuf]);
-    else k_spread<float><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, (float*)L.F[fbuf]);
+    const bool peskin = L.ib.dirac == BIB_DIRAC_PESKIN;
+    if (L.storage == BIB_STORAGE_F64) {
+        double* F = (double*)L.F[fbuf];
+        if (peskin) k_spread<double, 4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, F);
+        else k_spread<double, 3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, F);
+    } else {
+        float* F = (float*)L.F[fbuf];
+        if (peskin) k_spread<float, 4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, F);
+        else k_spread<float, 3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, F);
+    }
 }
 
 }  // namespace bib
