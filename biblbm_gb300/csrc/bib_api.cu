@@ -33,6 +33,8 @@ struct bib_ctx {
     cudaEvent_t ev[6] = {};
     int* d_flag = nullptr;
     std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, parity) -> two-step graph
+    double* stage = nullptr;  // device staging area of the host <-> device population transfers
+    size_t stage_count = 0;   // its size in doubles
 };
 
 namespace {
@@ -539,6 +541,62 @@ bib_status pull_particles(bib_ctx* c, Lattice& L) {
     return BIB_OK;
 }
 
+// Population transfers stream whole z-planes through a staging area of about 32 MB (at
+// least one plane of all 19 populations), allocated once per context.
+constexpr size_t kStageTarget = (size_t)4 << 20;  // doubles
+
+bib_status plane_chunk(bib_ctx* c, const Lattice& L, int* planes) {
+    const size_t plane = (size_t)Q * L.d.nx * L.d.ny;
+    const size_t want = std::max(plane, kStageTarget / plane * plane);
+    if (c->stage_count < want) {
+        cudaFree(c->stage);
+        c->stage = nullptr;
+        c->stage_count = 0;
+        BIB_CUDA(c, cudaMalloc((void**)&c->stage, want * sizeof(double)));
+        c->stage_count = want;
+    }
+    *planes = (int)std::min<size_t>(c->stage_count / plane, (size_t)L.d.nz);
+    return BIB_OK;
+}
+
+// Host SoA populations (19 arrays of n doubles) -> lattice state, chunk by chunk: 19 copies
+// into the staging area, then the import of those planes, in stream order.
+bib_status import_populations(bib_ctx* c, Lattice& L, const double* src) {
+    int P = 0;
+    bib_status st = plane_chunk(c, L, &P);
+    if (st) return st;
+    const int64_t n = L.d.n, plane = (int64_t)L.d.nx * L.d.ny;
+    for (int z0 = 0; z0 < L.d.nz; z0 += P) {
+        const int nzc = std::min(P, L.d.nz - z0);
+        const int64_t cc = plane * nzc;
+        for (int i = 0; i < Q; ++i)
+            BIB_CUDA(c, cudaMemcpyAsync(c->stage + i * cc, src + i * n + z0 * plane, cc * sizeof(double),
+                                        cudaMemcpyHostToDevice, c->stream));
+        launch_import_planes(L, c->stage, z0, nzc, cc, c->stream);
+        BIB_CHECK_LAUNCH(c);
+    }
+    return BIB_OK;
+}
+
+// Lattice state -> host SoA populations, chunk by chunk.
+bib_status export_populations(bib_ctx* c, Lattice& L, double* dst) {
+    int P = 0;
+    bib_status st = plane_chunk(c, L, &P);
+    if (st) return st;
+    const int64_t n = L.d.n, plane = (int64_t)L.d.nx * L.d.ny;
+    for (int z0 = 0; z0 < L.d.nz; z0 += P) {
+        const int nzc = std::min(P, L.d.nz - z0);
+        const int64_t cc = plane * nzc;
+        launch_export_planes(L, c->stage, z0, nzc, cc, c->stream);
+        BIB_CHECK_LAUNCH(c);
+        for (int i = 0; i < Q; ++i)
+            BIB_CUDA(c, cudaMemcpyAsync(dst + i * n + z0 * plane, c->stage + i * cc, cc * sizeof(double),
+                                        cudaMemcpyDeviceToHost, c->stream));
+    }
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BIB_OK;
+}
+
 bib_status device_buffer(bib_ctx* c, double** d, const double* host, size_t count) {
     BIB_CUDA(c, cudaMalloc((void**)d, count * sizeof(double)));
     if (host) BIB_CUDA(c, cudaMemcpyAsync(*d, host, count * sizeof(double), cudaMemcpyHostToDevice, c->stream));
@@ -620,6 +678,7 @@ void bib_destroy(bib_ctx* c) {
     for (int k = 0; k < 6; ++k)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
     cudaFree(c->d_flag);
+    cudaFree(c->stage);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -801,18 +860,12 @@ bib_status bib_lattice_send(bib_ctx* c, int32_t h, const void* buf, size_t bytes
     } else {
         return fail(c, BIB_EINVAL, "unknown layout %d", layout);
     }
-    double* d = nullptr;
-    bib_status st = device_buffer(c, &d, src, Q * n);
+    bib_status st = import_populations(c, *L, src);
     if (st) return st;
-    launch_import_soa(*L, d, c->stream);
-    BIB_CHECK_LAUNCH(c);
     if (!ext.empty()) {
         double* dF = nullptr;
         st = device_buffer(c, &dF, ext.data(), 4 * n);
-        if (st) {
-            cudaFree(d);
-            return st;
-        }
+        if (st) return st;
         launch_force_import(*L, L->fe, dF, c->stream);
         L->target_clean = false;
         if (L->phase) launch_phase_import(*L, dF + 3 * n, c->stream);
@@ -820,7 +873,6 @@ bib_status bib_lattice_send(bib_ctx* c, int32_t h, const void* buf, size_t bytes
         cudaFree(dF);
     }
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
-    cudaFree(d);
     return BIB_OK;
 }
 
@@ -833,20 +885,18 @@ bib_status bib_lattice_receive(bib_ctx* c, int32_t h, void* buf, size_t bytes, i
     if (layout != BIB_LAYOUT_SOA_F64 && layout != BIB_LAYOUT_PALABOS_F64 && layout != BIB_LAYOUT_COPROCESSOR_F64)
         return fail(c, BIB_EINVAL, "unknown layout");
     if (bytes != want) return fail(c, BIB_EINVAL, "expected %zu bytes", want);
-    double* d = nullptr;
-    bib_status st = device_buffer(c, &d, nullptr, (Q + 3) * n);
-    if (st) return st;
-    launch_export_soa(*L, d, c->stream);
-    launch_force_export(*L, L->fe, d + Q * n, c->stream);
-    BIB_CHECK_LAUNCH(c);
+    if (layout == BIB_LAYOUT_SOA_F64) return export_populations(c, *L, (double*)buf);
     std::vector<double> host((Q + 3) * n);
-    BIB_CUDA(c, cudaMemcpyAsync(host.data(), d, host.size() * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    bib_status st = export_populations(c, *L, host.data());
+    if (st) return st;
+    double* d = nullptr;
+    st = device_buffer(c, &d, nullptr, 3 * n);
+    if (st) return st;
+    launch_force_export(*L, L->fe, d, c->stream);
+    BIB_CHECK_LAUNCH(c);
+    BIB_CUDA(c, cudaMemcpyAsync(host.data() + Q * n, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(d);
-    if (layout == BIB_LAYOUT_SOA_F64) {
-        std::memcpy(buf, host.data(), want);
-        return BIB_OK;
-    }
     double* dst = (double*)buf;
     const LatticeDesc& dd = L->d;
     int64_t w = 0;

@@ -159,8 +159,9 @@ void launch_fd_walls(const Lattice& L, int buf, int fbuf, cudaStream_t s);
 void launch_velocity_field(const Lattice& L, cudaStream_t s);  // u from the current state and F[fe]
 void launch_velocity_export(const Lattice& L, double* u, cudaStream_t s);
 void launch_init_equilibrium(const Lattice& L, const double* rho, const double* u, cudaStream_t s);
-void launch_import_soa(const Lattice& L, const double* src, cudaStream_t s);
-void launch_export_soa(const Lattice& L, double* dst, cudaStream_t s);
+// populations of planes z0 .. z0 + nzc - 1 from / to FP64 SoA slices of `pitch` cells
+void launch_import_planes(const Lattice& L, const double* src, int z0, int nzc, int64_t pitch, cudaStream_t s);
+void launch_export_planes(const Lattice& L, double* dst, int z0, int nzc, int64_t pitch, cudaStream_t s);
 void launch_force_import(const Lattice& L, int buf, const double* src, cudaStream_t s);
 void launch_force_export(const Lattice& L, int buf, double* dst, cudaStream_t s);
 void launch_force_fill(const Lattice& L, int buf, cudaStream_t s);

@@ -361,26 +361,32 @@ __global__ void k_init_eq(LatticeDesc d, T* __restrict__ f, T* __restrict__ wall
     for (int i = 0; i < Q; ++i) scatter_canonical<T>(d, f, wall, i, x, y, z, k, bgk_equilibrium<double>(i, rhoBar, invRho, j, jSqr));
 }
 
+// Import / export of the planes z0 .. z0 + gridDim.z - 1 from / to a buffer holding, per
+// population, `pitch` cells that start with the first cell of plane z0.
 template <class T>
-__global__ void k_import(LatticeDesc d, T* __restrict__ f, T* __restrict__ wall, const double* __restrict__ src) {
+__global__ void k_import(LatticeDesc d, T* __restrict__ f, T* __restrict__ wall, const double* __restrict__ src, int z0,
+                         int64_t pitch) {
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
+    const int y = blockIdx.y, z = z0 + (int)blockIdx.z;
     if (x >= d.nx) return;
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+    const int64_t j = k - (int64_t)z0 * d.nx * d.ny;
 #pragma unroll
-    for (int i = 0; i < Q; ++i) scatter_canonical<T>(d, f, wall, i, x, y, z, k, src[i * d.n + k]);
+    for (int i = 0; i < Q; ++i) scatter_canonical<T>(d, f, wall, i, x, y, z, k, src[i * pitch + j]);
 }
 
 template <class T>
-__global__ void k_export(LatticeDesc d, const T* __restrict__ f, const T* __restrict__ wall, double* __restrict__ dst) {
+__global__ void k_export(LatticeDesc d, const T* __restrict__ f, const T* __restrict__ wall, double* __restrict__ dst,
+                         int z0, int64_t pitch) {
     using C = typename Store<T>::C;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int y = blockIdx.y, z = blockIdx.z;
+    const int y = blockIdx.y, z = z0 + (int)blockIdx.z;
     if (x >= d.nx) return;
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+    const int64_t j = k - (int64_t)z0 * d.nx * d.ny;
     C fc[Q];
     gather<T>(d, f, wall, x, y, z, k, fc);
-    for (int i = 0; i < Q; ++i) dst[i * d.n + k] = (double)fc[i];
+    for (int i = 0; i < Q; ++i) dst[i * pitch + j] = (double)fc[i];
 }
 
 template <class FT>
@@ -500,15 +506,17 @@ void init_eq_t(const Lattice& L, const double* rho, const double* u, cudaStream_
 }
 
 template <class T>
-void import_t(const Lattice& L, const double* src, cudaStream_t s) {
+void import_t(const Lattice& L, const double* src, int z0, int nzc, int64_t pitch, cudaStream_t s) {
     const int bx = row_block(L.d);
-    k_import<T><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (T*)L.f[L.cur], (T*)L.wall, src);
+    dim3 g((L.d.nx + bx - 1) / bx, L.d.ny, nzc);
+    k_import<T><<<g, bx, 0, s>>>(L.d, (T*)L.f[L.cur], (T*)L.wall, src, z0, pitch);
 }
 
 template <class T>
-void export_t(const Lattice& L, double* dst, cudaStream_t s) {
+void export_t(const Lattice& L, double* dst, int z0, int nzc, int64_t pitch, cudaStream_t s) {
     const int bx = row_block(L.d);
-    k_export<T><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall, dst);
+    dim3 g((L.d.nx + bx - 1) / bx, L.d.ny, nzc);
+    k_export<T><<<g, bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall, dst, z0, pitch);
 }
 
 template <class T>
@@ -537,9 +545,13 @@ void launch_init_equilibrium(const Lattice& L, const double* rho, const double* 
     BIB_DISPATCH(L.storage, init_eq_t, L, rho, u, s);
 }
 
-void launch_import_soa(const Lattice& L, const double* src, cudaStream_t s) { BIB_DISPATCH(L.storage, import_t, L, src, s); }
+void launch_import_planes(const Lattice& L, const double* src, int z0, int nzc, int64_t pitch, cudaStream_t s) {
+    BIB_DISPATCH(L.storage, import_t, L, src, z0, nzc, pitch, s);
+}
 
-void launch_export_soa(const Lattice& L, double* dst, cudaStream_t s) { BIB_DISPATCH(L.storage, export_t, L, dst, s); }
+void launch_export_planes(const Lattice& L, double* dst, int z0, int nzc, int64_t pitch, cudaStream_t s) {
+    BIB_DISPATCH(L.storage, export_t, L, dst, z0, nzc, pitch, s);
+}
 
 void launch_force_import(const Lattice& L, int buf, const double* src, cudaStream_t s) {
     const unsigned g = lin_grid(L.d.n, 256);
