@@ -41,6 +41,11 @@ class Tuning(C.Structure):
                 ("reserved", C.c_int32 * 5)]
 
 
+class BatchTuning(C.Structure):
+    _fields_ = [("tile_cells", C.c_int32), ("stages", C.c_int32), ("membrane_block", C.c_int32),
+                ("reserved", C.c_int32 * 5)]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_int32)]
 
@@ -84,6 +89,12 @@ SIGNATURES = {
     "bib_check_health": (C.c_int32, [_vp, C.c_int32]),
     "bib_lattice_set_tuning": (C.c_int32, [_vp, C.c_int32, C.POINTER(Tuning)]),
     "bib_spread_forces_noalloc": (C.c_int32, [_vp, C.c_int32, _vp, _vp, C.c_int64, _vp]),
+    "bib_batch_create": (C.c_int32, [_vp, _i32p, C.c_int32, _i32p]),
+    "bib_batch_destroy": (C.c_int32, [_vp, C.c_int32]),
+    "bib_batch_step": (C.c_int32, [_vp, C.c_int32, C.c_int64]),
+    "bib_batch_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),
+    "bib_batch_set_tuning": (C.c_int32, [_vp, C.c_int32, C.POINTER(BatchTuning)]),
+    "bib_batch_autotune": (C.c_int32, [_vp, C.c_int32, C.c_int32, C.POINTER(BatchTuning)]),
 }
 
 _lib = None

@@ -16,7 +16,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import BibError, IbParams, LatticeParams, Tuning
+from ._lib import BatchTuning, BibError, IbParams, LatticeParams, Tuning
 
 STORAGE = {"f64": 0, "f32": 1, "f16": 2}
 COLLISION = {"bgk_guo_vof": 0, "bgk": 1, "trt": 2}
@@ -360,3 +360,41 @@ def taylor_deformation(inertia) -> float:
     ax = np.sqrt(ax2)
     L, B = ax.max(), ax.min()
     return float((L - B) / (L + B))
+
+
+class Batch:
+    """Lattices (each with its ImmersedBoundaryDynamics3D) stepped in lockstep: one launch per kernel
+    for all of them, replayed as CUDA graphs.  A batch step is a coupled step of every lattice."""
+
+    def __init__(self, ctx: Context, lattices):
+        self.ctx = ctx
+        self.lattices = list(lattices)
+        hs = (C.c_int32 * len(self.lattices))(*[lat.h for lat in self.lattices])
+        b = C.c_int32()
+        ctx.check(ctx.lib.bib_batch_create(ctx.h, hs, len(self.lattices), C.byref(b)))
+        self.h = b.value
+
+    def step(self, nsteps=1):
+        self.ctx.check(self.ctx.lib.bib_batch_step(self.ctx.h, self.h, int(nsteps)))
+
+    def step_timed(self, nsteps=1) -> float:
+        ms = C.c_double()
+        self.ctx.check(self.ctx.lib.bib_batch_step_timed(self.ctx.h, self.h, int(nsteps), C.byref(ms)))
+        return ms.value
+
+    def set_tuning(self, tile_cells=0, stages=0, membrane_block=0):
+        t = BatchTuning()
+        t.tile_cells, t.stages, t.membrane_block = int(tile_cells), int(stages), int(membrane_block)
+        self.ctx.check(self.ctx.lib.bib_batch_set_tuning(self.ctx.h, self.h, C.byref(t)))
+
+    def autotune(self, steps=5) -> dict:
+        """Times the candidate schedules over `steps` real steps each (the batch advances) and
+        keeps the fastest; returns it."""
+        t = BatchTuning()
+        self.ctx.check(self.ctx.lib.bib_batch_autotune(self.ctx.h, self.h, int(steps), C.byref(t)))
+        return {"tile_cells": t.tile_cells, "stages": t.stages, "membrane_block": t.membrane_block}
+
+    def close(self):
+        if self.h is not None:
+            self.ctx.check(self.ctx.lib.bib_batch_destroy(self.ctx.h, self.h))
+            self.h = None

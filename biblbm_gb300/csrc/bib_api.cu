@@ -5,6 +5,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
 #include <map>
 #include <memory>
 #include <new>
@@ -21,6 +22,8 @@ struct GraphEntry {
     int cur = 0, pcur = 0;
 };
 
+struct Batch;
+
 struct bib_ctx {
     int device = 0;
     cudaStream_t stream = nullptr;
@@ -35,6 +38,8 @@ struct bib_ctx {
     std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, parity) -> two-step graph
     double* stage = nullptr;  // device staging area of the host <-> device population transfers
     size_t stage_count = 0;   // its size in doubles
+    std::vector<std::unique_ptr<Batch>> batches;
+    ~bib_ctx();
 };
 
 namespace {
@@ -321,6 +326,7 @@ void drop_graphs(bib_ctx* c, int32_t h) {
 
 bib_status sync_particles(bib_ctx* c, Lattice& L) {
     if (!L.particles_dirty) return BIB_OK;
+    ++L.version;
     free_particles(L);
     L.nvert = (int)(L.host_pos.size() / 3);
     const int np = (int)L.parts.size();
@@ -364,6 +370,8 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
         d.tri_rest_f = S.dev.tri_rest_f;
         d.tri_area_f = S.dev.tri_area_f;
         d.pair_cs_f = S.dev.pair_cs_f;
+        d.inst = 0;
+        d.lpid = p;
         d.A0 = S.area;
         for (int k = 0; k < BIB_P_COUNT; ++k) d.prm[k] = ph.prm[k];
         L.max_nv = std::max(L.max_nv, ph.nv);
@@ -388,6 +396,7 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
     }
     BIB_CUDA(c, cudaMalloc((void**)&L.pdev, np * sizeof(ParticleDev)));
     BIB_CUDA(c, cudaMemcpy(L.pdev, pd.data(), np * sizeof(ParticleDev), cudaMemcpyHostToDevice));
+    L.pdev_host = pd;
     L.membrane_smem = membrane_smem_bytes(L.max_nv);
     int dev_max = 0;
     BIB_CUDA(c, cudaDeviceGetAttribute(&dev_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, c->device));
@@ -605,6 +614,270 @@ bib_status device_buffer(bib_ctx* c, double** d, const double* host, size_t coun
 
 }  // namespace
 
+// =================================================================== batches
+// A batch steps several lattices in lockstep with one launch per kernel for all of them.
+// Its device tables hold, for each of the two step parities, one IbView and one CollideView
+// per lattice; the lattices' own parities (cur, fe, pcur) advance together.
+struct Batch {
+    std::vector<int32_t> handles;
+    int storage = 0, collision = 0, dirac = 0;
+    IbView* views[2] = {nullptr, nullptr};
+    CollideView* cviews[2] = {nullptr, nullptr};
+    ParticleDev* parts = nullptr;
+    int* vinst = nullptr;
+    int nparts = 0, nvert = 0, max_nv = 0;
+    size_t membrane_smem = 0;
+    int64_t ntiles = 0;
+    int any_fd = 0, nx_max = 0, nz_max = 0;
+    int tile_cells = 0, stages = 0, membrane_block = 256;
+    int phase = 0;                      // parity of the next step relative to the tables
+    std::vector<uint64_t> versions;     // lattice versions the tables were built for
+    std::vector<int> state0;            // per lattice: cur*4 + pcur*2 + fe at phase 0
+    bool built = false;
+    GraphEntry graph[2];
+    void free_tables() {
+        for (int p = 0; p < 2; ++p) {
+            cudaFree(views[p]);
+            cudaFree(cviews[p]);
+            views[p] = nullptr;
+            cviews[p] = nullptr;
+            if (graph[p].exec) cudaGraphExecDestroy(graph[p].exec);
+            graph[p].exec = nullptr;
+        }
+        cudaFree(parts);
+        cudaFree(vinst);
+        parts = nullptr;
+        vinst = nullptr;
+        built = false;
+    }
+    ~Batch() { free_tables(); }
+};
+
+bib_ctx::~bib_ctx() = default;
+
+namespace {
+
+Batch* get_batch(bib_ctx* c, int32_t b) {
+    if (!c || b < 0 || b >= (int32_t)c->batches.size()) return nullptr;
+    return c->batches[b].get();
+}
+
+int lattice_state(const Lattice& L) { return L.cur * 4 + L.pcur * 2 + L.fe; }
+
+// (Re)build the device tables from the lattices' current state, which becomes phase 0.
+bib_status build_batch(bib_ctx* c, Batch& B) {
+    B.free_tables();
+    const int n = (int)B.handles.size();
+    std::vector<IbView> iv[2];
+    std::vector<CollideView> cv[2];
+    std::vector<ParticleDev> parts;
+    std::vector<int> vinst;
+    B.versions.assign(n, 0);
+    B.state0.assign(n, 0);
+    B.max_nv = 0;
+    B.ntiles = 0;
+    B.any_fd = 0;
+    B.nx_max = B.nz_max = 0;
+    int vbase = 0;
+    for (int i = 0; i < n; ++i) {
+        Lattice& L = *get_lattice(c, B.handles[i]);
+        bib_status st = sync_particles(c, L);
+        if (st) return st;
+        B.versions[i] = L.version;
+        B.state0[i] = lattice_state(L);
+        for (int p = 0; p < 2; ++p) {
+            // phase p: every parity of the lattice flipped p times
+            const int cur = L.cur ^ p, fe = L.fe ^ p, pcur = L.nvert ? (L.pcur ^ p) : L.pcur;
+            IbView v{};
+            v.d = L.d;
+            v.ib = L.ib;
+            v.pos = L.pos[pcur];
+            v.pos_next = L.pos[1 - pcur];
+            v.u = L.u;
+            v.vel = L.vel;
+            v.force = L.force;
+            v.F = L.F[1 - fe];
+            v.stats = L.stats;
+            v.vbase = vbase;
+            v.nvert = L.nvert;
+            iv[p].push_back(v);
+            CollideView w{};
+            if (!staged_collide_view(L, B.tile_cells, w))
+                return fail(c, BIB_EUNSUPPORTED, "lattice %d does not fit the staged collide-and-stream kernel", B.handles[i]);
+            w.fin = L.f[cur];
+            w.fout = L.f[1 - cur];
+            w.wall = L.wall;
+            w.Fcol = L.F[1 - fe];
+            w.Fprev = L.F[fe];
+            w.u = L.u;
+            w.phase = L.phase;
+            w.tile0 = B.ntiles;
+            cv[p].push_back(w);
+        }
+        B.ntiles += cv[0].back().ntiles;
+        B.any_fd |= L.d.fd_walls;
+        B.nx_max = std::max(B.nx_max, L.d.nx);
+        B.nz_max = std::max(B.nz_max, L.d.nz);
+        for (size_t k = 0; k < L.pdev_host.size(); ++k) {
+            ParticleDev d = L.pdev_host[k];
+            d.inst = i;
+            parts.push_back(d);
+        }
+        for (int v = 0; v < L.nvert; ++v) vinst.push_back(i);
+        vbase += L.nvert;
+        B.max_nv = std::max(B.max_nv, L.max_nv);
+    }
+    B.nparts = (int)parts.size();
+    B.nvert = vbase;
+    B.membrane_smem = membrane_smem_bytes(B.max_nv);
+    configure_membrane_kernel(B.membrane_smem);
+    bib_status st;
+    for (int p = 0; p < 2; ++p)
+        if ((st = upload(c, &B.views[p], iv[p])) || (st = upload(c, &B.cviews[p], cv[p]))) return st;
+    if ((st = upload(c, &B.parts, parts)) || (st = upload(c, &B.vinst, vinst))) return st;
+    B.phase = 0;
+    B.built = true;
+    return BIB_OK;
+}
+
+// Bring the tables up to date with the lattices; returns the phase of the next step.
+bib_status prepare_batch(bib_ctx* c, Batch& B) {
+    bool rebuild = !B.built;
+    const int n = (int)B.handles.size();
+    for (int i = 0; i < n && !rebuild; ++i) {
+        Lattice* L = get_lattice(c, B.handles[i]);
+        if (!L) return fail(c, BIB_EINVAL, "a lattice of the batch has been destroyed");
+        if (L->particles_dirty || L->version != B.versions[i]) rebuild = true;
+    }
+    if (!rebuild) {  // every lattice must sit at the batch's phase
+        for (int i = 0; i < n && !rebuild; ++i) {
+            const Lattice& L = *get_lattice(c, B.handles[i]);
+            const int s0 = B.state0[i];
+            const int want = B.phase ? (s0 ^ (L.nvert ? 7 : 5)) : s0;
+            if (lattice_state(L) != want) rebuild = true;
+        }
+    }
+    if (rebuild) {
+        bib_status st = build_batch(c, B);
+        if (st) return st;
+    }
+    // the coupled step expects every spreading target already reset to the body force
+    for (int i = 0; i < n; ++i) {
+        Lattice& L = *get_lattice(c, B.handles[i]);
+        if (!L.target_clean) {
+            launch_force_fill(L, 1 - L.fe, c->stream);
+            L.target_clean = true;
+        }
+    }
+    BIB_CHECK_LAUNCH(c);
+    return BIB_OK;
+}
+
+BatchLaunch batch_launch(bib_ctx* c, const Batch& B, int phase) {
+    BatchLaunch bl;
+    bl.n = (int)B.handles.size();
+    bl.storage = B.storage;
+    bl.collision = B.collision;
+    bl.dirac = B.dirac;
+    bl.views = B.views[phase];
+    bl.cviews = B.cviews[phase];
+    bl.wviews = B.cviews[phase ^ 1];
+    bl.parts = B.parts;
+    bl.nparts = B.nparts;
+    bl.vinst = B.vinst;
+    bl.nvert = B.nvert;
+    bl.max_nv = B.max_nv;
+    bl.membrane_smem = B.membrane_smem;
+    bl.ntiles = B.ntiles;
+    bl.stages = B.stages;
+    bl.any_fd = B.any_fd;
+    bl.nx_max = B.nx_max;
+    bl.nz_max = B.nz_max;
+    bl.wait_err = c->d_flag + 1;
+    return bl;
+}
+
+// One coupled step of every lattice of the batch (the order of enqueue_step).
+bib_status enqueue_batch_step(bib_ctx* c, Batch& B) {
+    const BatchLaunch bl = batch_launch(c, B, B.phase);
+    launch_membrane_batch(bl, B.membrane_block, c->stream);
+    launch_spread_batch(bl, c->stream);
+    if (!launch_collide_batch(bl, c->stream))
+        return fail(c, BIB_EUNSUPPORTED, "batched collide-and-stream could not be launched (shared memory)");
+    launch_fd_walls_batch(bl, c->stream);
+    launch_interpolate_batch(bl, c->stream);
+    launch_update_batch(bl, c->stream);
+    for (int32_t h : B.handles) {
+        Lattice& L = *get_lattice(c, h);
+        L.cur ^= 1;
+        L.fe ^= 1;
+        if (L.nvert) L.pcur ^= 1;
+        L.target_clean = true;
+    }
+    B.phase ^= 1;
+    return BIB_OK;
+}
+
+bib_status run_batch(bib_ctx* c, Batch& B, int64_t nsteps) {
+    bib_status st = prepare_batch(c, B);
+    if (st) return st;
+    int64_t done = 0;
+    if (c->graph_mode && nsteps >= 2) {
+        GraphEntry& ge = B.graph[B.phase];
+        if (!ge.exec) {
+            std::vector<int> saved;
+            for (int32_t h : B.handles) saved.push_back(lattice_state(*get_lattice(c, h)));
+            const int phase0 = B.phase;
+            cudaGraph_t g = nullptr;
+            BIB_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            bib_status s1 = enqueue_batch_step(c, B);
+            bib_status s2 = s1 ? s1 : enqueue_batch_step(c, B);
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            for (size_t i = 0; i < B.handles.size(); ++i) {  // two steps: every parity back where it was
+                Lattice& L = *get_lattice(c, B.handles[i]);
+                L.cur = saved[i] >> 2;
+                L.pcur = (saved[i] >> 1) & 1;
+                L.fe = saved[i] & 1;
+            }
+            B.phase = phase0;
+            if (s2) {
+                if (g) cudaGraphDestroy(g);
+                return s2;
+            }
+            if (e != cudaSuccess) return fail(c, BIB_ECUDA, "batch graph capture failed: %s", cudaGetErrorString(e));
+            e = cudaGraphInstantiate(&ge.exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) return fail(c, BIB_ECUDA, "batch graph instantiation failed: %s", cudaGetErrorString(e));
+        }
+        for (; done + 2 <= nsteps; done += 2) BIB_CUDA(c, cudaGraphLaunch(ge.exec, c->stream));
+    }
+    for (; done < nsteps; ++done) {
+        st = enqueue_batch_step(c, B);
+        if (st) return st;
+        BIB_CHECK_LAUNCH(c);
+    }
+    BIB_CHECK_LAUNCH(c);
+    return BIB_OK;
+}
+
+bib_status timed(bib_ctx* c, const std::function<bib_status()>& fn, double* ms) {
+    cudaEvent_t a, b;
+    BIB_CUDA(c, cudaEventCreate(&a));
+    BIB_CUDA(c, cudaEventCreate(&b));
+    BIB_CUDA(c, cudaEventRecord(a, c->stream));
+    bib_status st = fn();
+    BIB_CUDA(c, cudaEventRecord(b, c->stream));
+    BIB_CUDA(c, cudaEventSynchronize(b));
+    float f = 0;
+    BIB_CUDA(c, cudaEventElapsedTime(&f, a, b));
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    *ms = f;
+    return st;
+}
+
+}  // namespace
+
 // =================================================================== C ABI
 extern "C" {
 
@@ -701,6 +974,134 @@ size_t bib_last_error(const bib_ctx* c, char* buf, size_t len) {
 bib_status bib_set_graph_mode(bib_ctx* c, int32_t enabled) {
     if (!c) return BIB_EINVAL;
     c->graph_mode = enabled != 0;
+    return BIB_OK;
+}
+
+bib_status bib_batch_create(bib_ctx* c, const int32_t* handles, int32_t n, int32_t* batch) {
+    if (!c || !handles || n <= 0 || !batch) return fail(c, BIB_EINVAL, "null argument or empty batch");
+    auto B = std::make_unique<Batch>();
+    for (int32_t i = 0; i < n; ++i) {
+        Lattice* L = get_lattice(c, handles[i]);
+        if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle %d", handles[i]);
+        for (int32_t j = 0; j < i; ++j)
+            if (handles[j] == handles[i]) return fail(c, BIB_EINVAL, "lattice %d appears twice", handles[i]);
+        if (i == 0) {
+            B->storage = L->storage;
+            B->collision = L->d.collision;
+            B->dirac = L->ib.dirac;
+        } else if (L->storage != B->storage || L->d.collision != B->collision || L->ib.dirac != B->dirac) {
+            return fail(c, BIB_EINVAL, "the lattices of a batch share storage, collision and delta kernel");
+        }
+        if (L->ib.spread_mode != BIB_SPREAD_ATOMIC)
+            return fail(c, BIB_EUNSUPPORTED, "batched steps spread with atomics (lattice %d is deterministic)", handles[i]);
+        CollideView probe{};
+        if (!staged_collide_view(*L, 0, probe))
+            return fail(c, BIB_EUNSUPPORTED, "lattice %d does not fit the staged collide-and-stream kernel", handles[i]);
+        B->handles.push_back(handles[i]);
+    }
+    *batch = (int32_t)c->batches.size();
+    c->batches.push_back(std::move(B));
+    return BIB_OK;
+}
+
+bib_status bib_batch_destroy(bib_ctx* c, int32_t b) {
+    Batch* B = get_batch(c, b);
+    if (!B) return fail(c, BIB_EINVAL, "invalid batch handle");
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->batches[b].reset();
+    return BIB_OK;
+}
+
+bib_status bib_batch_step(bib_ctx* c, int32_t b, int64_t nsteps) {
+    Batch* B = get_batch(c, b);
+    if (!B) return fail(c, BIB_EINVAL, "invalid batch handle");
+    if (nsteps < 0) return fail(c, BIB_EINVAL, "negative step count");
+    return run_batch(c, *B, nsteps);
+}
+
+bib_status bib_batch_step_timed(bib_ctx* c, int32_t b, int64_t nsteps, double* ms) {
+    Batch* B = get_batch(c, b);
+    if (!B || !ms) return fail(c, BIB_EINVAL, "invalid batch handle or null argument");
+    if (nsteps < 0) return fail(c, BIB_EINVAL, "negative step count");
+    bib_status st = prepare_batch(c, *B);  // uploads happen outside the timed region
+    if (st) return st;
+    return timed(c, [&] { return run_batch(c, *B, nsteps); }, ms);
+}
+
+bib_status bib_batch_set_tuning(bib_ctx* c, int32_t b, const bib_batch_tuning* t) {
+    Batch* B = get_batch(c, b);
+    if (!B || !t) return fail(c, BIB_EINVAL, "invalid batch handle or tuning");
+    if (t->tile_cells < 0 || t->stages < 0 || t->stages == 1 || t->stages > 4 ||
+        (t->membrane_block != 0 && t->membrane_block != 64 && t->membrane_block != 128 && t->membrane_block != 256))
+        return fail(c, BIB_EINVAL, "invalid batch tuning values");
+    if (!collide_batch_fits(B->storage, B->collision, t->stages))
+        return fail(c, BIB_EUNSUPPORTED, "%d stages do not fit the shared memory of a CTA", t->stages);
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    B->tile_cells = t->tile_cells;
+    B->stages = t->stages;
+    B->membrane_block = t->membrane_block ? t->membrane_block : 256;
+    B->free_tables();  // tile geometry and graphs depend on the tuning
+    return BIB_OK;
+}
+
+bib_status bib_batch_autotune(bib_ctx* c, int32_t b, int32_t steps, bib_batch_tuning* chosen) {
+    Batch* B = get_batch(c, b);
+    if (!B || steps <= 0) return fail(c, BIB_EINVAL, "invalid batch handle or step count");
+    // Every candidate runs `steps` real coupled steps (plain launches); the tile size, the
+    // stage count and the membrane block size change the schedule, not the arithmetic.
+    const int graph = c->graph_mode;
+    c->graph_mode = false;
+    bib_batch_tuning best{};
+    double best_ms = 1e300;
+    const int tiles[2] = {0, 256};
+    for (int ti = 0; ti < 2; ++ti)
+        for (int ns = 2; ns <= 4; ++ns) {
+            bib_batch_tuning t{};
+            t.tile_cells = tiles[ti];
+            t.stages = ns;
+            t.membrane_block = B->membrane_block;
+            if (!collide_batch_fits(B->storage, B->collision, ns)) continue;
+            bib_status st = bib_batch_set_tuning(c, b, &t);
+            if (st) {
+                c->graph_mode = graph;
+                return st;
+            }
+            double ms = 0;
+            st = bib_batch_step(c, b, 1);  // builds the tables outside the timed steps
+            if (!st) st = bib_batch_step_timed(c, b, steps, &ms);
+            if (st) {
+                c->graph_mode = graph;
+                return st;
+            }
+            if (ms < best_ms) {
+                best_ms = ms;
+                best = t;
+            }
+        }
+    double best_mb = 1e300;
+    int best_block = 256;
+    const int blocks[3] = {64, 128, 256};
+    for (int k = 0; k < 3; ++k) {
+        bib_batch_tuning t = best;
+        t.membrane_block = blocks[k];
+        bib_status st = bib_batch_set_tuning(c, b, &t);
+        double ms = 0;
+        if (!st) st = bib_batch_step(c, b, 1);
+        if (!st) st = bib_batch_step_timed(c, b, steps, &ms);
+        if (st) {
+            c->graph_mode = graph;
+            return st;
+        }
+        if (ms < best_mb) {
+            best_mb = ms;
+            best_block = blocks[k];
+        }
+    }
+    best.membrane_block = best_block;
+    c->graph_mode = graph;
+    bib_status st = bib_batch_set_tuning(c, b, &best);
+    if (st) return st;
+    if (chosen) *chosen = best;
     return BIB_OK;
 }
 

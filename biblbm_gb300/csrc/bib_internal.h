@@ -74,12 +74,60 @@ struct ParticleDev {
     const float* tri_rest_f;
     const float* tri_area_f;
     const float* pair_cs_f;
+    int inst;             // lattice of the particle within a batch (0 for a single lattice)
+    int lpid;             // particle index within its lattice
     double A0;
     double prm[BIB_P_COUNT];
 };
 
 // Per-particle state kept on the device: {area, volume, com[3]}.
 constexpr int STATS = 5;
+
+// What the immersed-boundary kernels need of one lattice for one step (buffer parities
+// resolved).  A single lattice passes one view by value; a batch passes a device table of
+// views, indexed per vertex (through the vertex -> lattice map) or per particle (inst).
+struct IbView {
+    LatticeDesc d;
+    IbDesc ib;
+    const double* pos;   // X_n
+    double* pos_next;    // X_{n+1}
+    const void* u;       // velocity field (FP64 for FP64 storage, FP32 otherwise)
+    double* vel;
+    double* force;       // vertex forces
+    void* F;             // spreading target (field type as u)
+    double* stats;       // STATS per particle
+    int vbase;           // batch numbering of the lattice's first vertex
+    int nvert;
+};
+
+// Per-launch constants of the collision in the compute type C.
+template <class C>
+struct CollideParams {
+    C om0, om1;      // relaxation frequency of phase 0 / 1 (BGK + Guo) or the omega of BGK / TRT
+    C omm;           // TRT: omega of the antisymmetric part
+    C S, invS;       // storage scale (FP16) and its inverse, 1 otherwise
+    C body[3];       // body force, the reset value of the previous force field
+    C wall_u[2][3];  // velocity of the finite-difference wall rows y = 0, ny - 1
+    C mw[4][19];     // moving-wall bounce-back term per wall face and population, storage units
+};
+
+// One lattice of a batched collide-and-stream step (buffer parities resolved): the staged
+// kernel maps its global tile index to (lattice, local tile) through tile0.
+struct CollideView {
+    LatticeDesc d;
+    const void* fin;
+    void* fout;
+    const void* wall;
+    const void* Fcol;       // spread force of this step
+    void* Fprev;            // force of the incoming state (reset to the body force)
+    void* u;                // velocity output
+    const uint8_t* phase;
+    int64_t tile0;          // first global tile of this lattice
+    int64_t ntiles;
+    int R, Ct, tiles_y;     // rows per tile, cells per tile, tiles per z-plane
+    unsigned tx_bytes;      // bytes copied in per tile
+    alignas(16) unsigned char cp[sizeof(CollideParams<double>)];  // CollideParams<compute type>
+};
 
 struct ShapeHost {
     std::vector<double> rest, tri_area, link_len, pair_cs;
@@ -129,6 +177,7 @@ struct Lattice {
     double* force = nullptr;
     double* stats = nullptr;              // STATS per particle
     ParticleDev* pdev = nullptr;
+    std::vector<ParticleDev> pdev_host;  // host copy of pdev (batch tables are built from it)
     int* vert_particle = nullptr;         // global vertex -> particle
     int max_nv = 0;
     bool particles_dirty = true;  // host copies below are authoritative until uploaded
@@ -145,6 +194,7 @@ struct Lattice {
     int tile_cells = 0;
     int stages = 0;           // staged kernel pipeline depth (0 = automatic)
     int* wait_err = nullptr;  // device word set by a bounded device wait that gave up
+    uint64_t version = 0;     // bumped whenever the particle buffers are (re)allocated
     int handle = -1;
 };
 
@@ -184,6 +234,39 @@ cudaError_t launch_spread_sorted(const LatticeDesc& d, const IbDesc& ib, bool f6
                                  const double* force, void* field, uint32_t* keys0, uint32_t* keys1, uint32_t* ids0,
                                  uint32_t* ids1, void* temp, size_t temp_bytes, cudaStream_t s);
 int spread_key_bits(int64_t n);
+
+// ---- batched steps: one launch per kernel for all lattices of a batch ----
+// Device tables of one step parity (the lattices of a batch advance in lockstep).
+struct BatchLaunch {
+    int n = 0;                          // lattices
+    int storage = 0, collision = 0, dirac = 0;
+    const IbView* views = nullptr;      // n views of this step (spreading target = F[1-fe])
+    const CollideView* cviews = nullptr;  // n collide views of this step
+    const CollideView* wviews = nullptr;  // n collide views of the next state (finite-difference walls)
+    const ParticleDev* parts = nullptr; // all particles, ParticleDev::inst = lattice
+    int nparts = 0;
+    const int* vinst = nullptr;         // batch vertex -> lattice
+    int nvert = 0;
+    int max_nv = 0;
+    size_t membrane_smem = 0;
+    int64_t ntiles = 0;                 // staged tiles over all lattices
+    int stages = 0;                     // staged pipeline depth (0 = automatic)
+    int any_fd = 0;                     // some lattice has finite-difference walls
+    int nx_max = 0, nz_max = 0;
+    int* wait_err = nullptr;            // device word of the bounded waits
+};
+IbView single_view(const Lattice& L, int fbuf);  // parities of L; fbuf < 0: no spreading target
+void launch_membrane_batch(const BatchLaunch& B, int block, cudaStream_t s);
+void launch_spread_batch(const BatchLaunch& B, cudaStream_t s);
+void launch_interpolate_batch(const BatchLaunch& B, cudaStream_t s);
+void launch_update_batch(const BatchLaunch& B, cudaStream_t s);
+// staged collide-and-stream over the tiles of all lattices (coupled step); false if a lattice
+// does not fit the staged kernel
+bool launch_collide_batch(const BatchLaunch& B, cudaStream_t s);
+bool collide_batch_fits(int storage, int collision, int stages);  // shared memory of that many stages
+void launch_fd_walls_batch(const BatchLaunch& B, cudaStream_t s);
+// fills the tile geometry and collision constants of a collide view; false if L does not fit
+bool staged_collide_view(const Lattice& L, int tile_cells, CollideView& v);
 
 // ---- spreading without device allocation (noalloc.cu) ----
 bib_status spread_noalloc(const Lattice& L, int device, cudaStream_t s, const double* pos, const double* force,

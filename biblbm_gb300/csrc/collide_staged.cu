@@ -15,6 +15,7 @@
 // and written once, the spread force read, and (coupled step) the previous force read,
 // reset to the body force and the velocity field written.
 #include <algorithm>
+#include <cstring>
 #include <mutex>
 #include <unordered_map>
 
@@ -170,18 +171,6 @@ struct StagedGeom {
     unsigned tx_bytes;  // bytes copied in per tile
 };
 
-// Per-launch constants in the compute type, so that no double -> float conversion (FP64
-// pipe) happens per cell.
-template <class C>
-struct CollideParams {
-    C om0, om1;      // relaxation frequency of phase 0 / 1 (BGK + Guo) or the omega of BGK / TRT
-    C omm;           // TRT: omega of the antisymmetric part
-    C S, invS;       // storage scale (FP16) and its inverse, 1 otherwise
-    C body[3];       // body force, the reset value of the previous force field
-    C wall_u[2][3];  // velocity of the finite-difference wall rows y = 0, ny - 1
-    C mw[4][Q];      // moving-wall bounce-back term per wall face and population, storage units
-};
-
 struct TileRef {
     int z, y0;
     int64_t row0;  // first cell of the tile
@@ -244,6 +233,98 @@ __device__ __forceinline__ void load_tile(const LatticeDesc& d, const StagedGeom
         }
     }
     __syncwarp();
+}
+
+// Consumer side of one tile: read this thread's cell from the stage, release the stage,
+// collide and store.  `cell` is the thread's cell of the tile and its x-neighbours.
+struct TileCell {
+    bool active;
+    int r, o0, ol, orr;
+};
+__device__ __forceinline__ TileCell tile_cell(const LatticeDesc& d, int Ct, int ct) {
+    TileCell c;
+    c.active = ct < Ct;
+    c.r = ct / d.nx;
+    const int x = ct - c.r * d.nx;
+    c.o0 = ct;
+    c.ol = c.r * d.nx + (x == 0 ? d.nx - 1 : x - 1);
+    c.orr = c.r * d.nx + (x == d.nx - 1 ? 0 : x + 1);
+    return c;
+}
+
+template <class T, bool COUPLED, int COLL>
+__device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, const unsigned char* st,
+                                             const CollideParams<typename Store<T>::C>& cp, T* __restrict__ fout,
+                                             typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
+                                             const uint8_t* __restrict__ phase, const TileCell& cell, uint64_t* empty_s,
+                                             int lane) {
+    using C = typename Store<T>::C;
+    using FT = typename Store<T>::F;
+    using L = StageLayout<T, COUPLED, COLL>;
+    constexpr int TILE = L::TILE;
+    const int r = cell.r, o0 = cell.o0, ol = cell.ol, orr = cell.orr;
+    const bool active = cell.active;
+    const T* P = reinterpret_cast<const T*>(st);
+    const FT* SFc = reinterpret_cast<const FT*>(st + L::OFF_FCOL);
+    const FT* SFp = reinterpret_cast<const FT*>(st + L::OFF_FPREV);
+    const TileRef t = tile_ref(d, g, tile);
+    C f[Q], u[3], F[3] = {C(0), C(0), C(0)}, Fp[3];
+    const int y = t.y0 + r;
+    const bool fd = fd_wall_node(d, y);
+    C om = cp.om0;
+    if (active) {
+        if (!row_special(d, y, t.z)) {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) f[i] = Staged<T>::one(P + i * TILE + (cx(i) == 0 ? o0 : (cx(i) == 1 ? ol : orr)));
+        } else {
+#pragma unroll
+            for (int i = 0; i < Q; ++i) {
+                int face = -1;
+                if (!fd) {
+                    int64_t srow;
+                    face = source_row(d, i, y, t.z, srow);
+                }
+                const bool shift = !fd && face < 0;
+                f[i] = Staged<T>::one(P + i * TILE + (!shift || cx(i) == 0 ? o0 : (cx(i) == 1 ? ol : orr)));
+                if (face >= 0) f[i] += cp.mw[face][i];
+            }
+        }
+        if (L::NEED_FCOL) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) F[q] = (C)SFc[q * TILE + o0];
+        }
+        if (COUPLED) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) Fp[q] = (C)SFp[q * TILE + o0];
+        }
+    }
+    // the stage has been read into registers: hand it back to the producer
+    __syncwarp();
+    if (lane == 0) mbar_arrive(empty_s);
+    if (!active) return;
+    const int64_t k = t.row0 + o0;
+    if (COLL == BIB_COLLISION_BGK_GUO_VOF && d.use_phase && phase[k]) om = cp.om1;
+    if (COUPLED) {
+        staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, Fp, fd ? nullptr : u);
+        if (fd) {
+            const int side = y == 0 ? 0 : 1;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) u[q] = cp.wall_u[side][q];
+        }
+#pragma unroll
+        for (int q = 0; q < 3; ++q) {
+            u_out[q * d.stride + k] = (FT)u[q];
+            Fprev[q * d.stride + k] = (FT)cp.body[q];
+        }
+    } else {
+        staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, nullptr, nullptr);
+    }
+    T* o = fout + k;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        Staged<T>::put(o, f[i]);
+        o += d.stride;
+    }
 }
 
 // Warp-specialised persistent kernel: warp 0 produces, warps 1..CONSUMERS collide.  Stage
@@ -311,12 +392,7 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
     }
 
     // ---- consumers: thread `ct` owns cell ct of every tile
-    const int ct = tid - 32;
-    const bool active = ct < g.Ct;
-    const int r = ct / d.nx, x = ct - r * d.nx;
-    const int o0 = ct;
-    const int ol = r * d.nx + (x == 0 ? d.nx - 1 : x - 1);
-    const int orr = r * d.nx + (x == d.nx - 1 ? 0 : x + 1);
+    const TileCell cell = tile_cell(d, g.Ct, tid - 32);
     int it = 0;
     for (int64_t tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x, ++it) {
         const int s = it % NS;
@@ -326,68 +402,96 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
             if (lane == 0) atomicExch(wait_err, 1);
             return;
         }
-        const unsigned char* st = stages + s * L::BYTES;
-        const T* P = reinterpret_cast<const T*>(st);
-        const FT* SFc = reinterpret_cast<const FT*>(st + L::OFF_FCOL);
-        const FT* SFp = reinterpret_cast<const FT*>(st + L::OFF_FPREV);
-        const TileRef t = tile_ref(d, g, tile);
-        C f[Q], u[3], F[3] = {C(0), C(0), C(0)}, Fp[3];
-        const int y = t.y0 + r;
-        const bool fd = fd_wall_node(d, y);
-        C om = cp.om0;
-        if (active) {
-            if (!row_special(d, y, t.z)) {
-#pragma unroll
-                for (int i = 0; i < Q; ++i) f[i] = Staged<T>::one(P + i * TILE + (cx(i) == 0 ? o0 : (cx(i) == 1 ? ol : orr)));
-            } else {
-#pragma unroll
-                for (int i = 0; i < Q; ++i) {
-                    int face = -1;
-                    if (!fd) {
-                        int64_t srow;
-                        face = source_row(d, i, y, t.z, srow);
-                    }
-                    const bool shift = !fd && face < 0;
-                    f[i] = Staged<T>::one(P + i * TILE + (!shift || cx(i) == 0 ? o0 : (cx(i) == 1 ? ol : orr)));
-                    if (face >= 0) f[i] += cp.mw[face][i];
+        consume_tile<T, COUPLED, COLL>(d, g, tile, stages + s * L::BYTES, cp, fout, Fprev, u_out, phase, cell, &empty[s],
+                                        lane);
+    }
+}
+
+// Batched variant: the global tile index runs over the tiles of all lattices of a batch
+// (CollideView::tile0 is the first tile of each); producer and consumers look the lattice
+// of each tile up in the view table (coupled step only).
+__device__ __forceinline__ int find_view(const CollideView* __restrict__ views, int n, int64_t tile) {
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (views[mid].tile0 <= tile) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+__device__ __forceinline__ StagedGeom view_geom(const CollideView& v, int ns) {
+    StagedGeom g;
+    g.R = v.R;
+    g.Ct = v.Ct;
+    g.tiles_y = v.tiles_y;
+    g.nstages = ns;
+    g.ntiles = v.ntiles;
+    g.tx_bytes = v.tx_bytes;
+    return g;
+}
+
+template <class T, int COLL>
+__global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ctas_per_sm<T>())
+    k_collide_stream_staged_batch(const CollideView* __restrict__ views, int nviews, int64_t ntiles, int NS,
+                                  int* __restrict__ wait_err) {
+    using C = typename Store<T>::C;
+    using FT = typename Store<T>::F;
+    using L = StageLayout<T, true, COLL>;
+    extern __shared__ __align__(128) unsigned char smem[];
+    uint64_t* full = reinterpret_cast<uint64_t*>(smem);
+    uint64_t* empty = full + kMaxStages;
+    unsigned char* stages = smem + 256;
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    if ((int64_t)blockIdx.x >= ntiles) return;
+    if (tid == 0) {
+        for (int k = 0; k < NS; ++k) {
+            mbar_init(&full[k], 1);
+            mbar_init(&empty[k], L::CONSUMERS);
+        }
+        mbar_init_fence();
+    }
+    __syncthreads();
+    if (warp == 0) {
+        int it = 0;
+        for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+            const int s = it % NS, use = it / NS;
+            if (use > 0) {
+                const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&empty[s], (unsigned)(use - 1) & 1u));
+                if (!ok) {
+                    if (lane == 0) atomicExch(wait_err, 1);
+                    break;
                 }
             }
-            if (L::NEED_FCOL) {
-#pragma unroll
-                for (int q = 0; q < 3; ++q) F[q] = (C)SFc[q * TILE + o0];
-            }
-            if (COUPLED) {
-#pragma unroll
-                for (int q = 0; q < 3; ++q) Fp[q] = (C)SFp[q * TILE + o0];
-            }
+            const CollideView& V = views[find_view(views, nviews, tile)];
+            load_tile<T, true, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES, &full[s],
+                                     static_cast<const T*>(V.fin), static_cast<const T*>(V.wall),
+                                     static_cast<const FT*>(V.Fcol), static_cast<const FT*>(V.Fprev), lane);
         }
-        // the stage has been read into registers: hand it back to the producer
-        __syncwarp();
-        if (lane == 0) mbar_arrive(&empty[s]);
-        if (!active) continue;
-        const int64_t k = t.row0 + o0;
-        if (COLL == BIB_COLLISION_BGK_GUO_VOF && d.use_phase && phase[k]) om = cp.om1;
-        if (COUPLED) {
-            staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, Fp, fd ? nullptr : u);
-            if (fd) {
-                const int side = y == 0 ? 0 : 1;
-#pragma unroll
-                for (int q = 0; q < 3; ++q) u[q] = cp.wall_u[side][q];
-            }
-#pragma unroll
-            for (int q = 0; q < 3; ++q) {
-                u_out[q * d.stride + k] = (FT)u[q];
-                Fprev[q * d.stride + k] = (FT)cp.body[q];
-            }
-        } else {
-            staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, nullptr, nullptr);
+        if (lane == 0) {
+            const int issued = it;
+            for (int k = issued > NS ? issued - NS : 0; k < issued; ++k)
+                mbar_wait_bounded(&full[k % NS], (unsigned)(k / NS) & 1u);
         }
-        T* o = fout + k;
-#pragma unroll
-        for (int i = 0; i < Q; ++i) {
-            Staged<T>::put(o, f[i]);
-            o += d.stride;
+        return;
+    }
+    int it = 0, cur_view = -1;
+    TileCell cell{};
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
+        const int s = it % NS;
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (unsigned)(it / NS) & 1u));
+        if (!ok) {
+            if (lane == 0) atomicExch(wait_err, 1);
+            return;
         }
+        const int vi = find_view(views, nviews, tile);
+        const CollideView& V = views[vi];
+        if (vi != cur_view) {  // the cell of this thread depends on the lattice's row length
+            cell = tile_cell(V.d, V.Ct, tid - 32);
+            cur_view = vi;
+        }
+        consume_tile<T, true, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES,
+                                    *reinterpret_cast<const CollideParams<C>*>(V.cp), static_cast<T*>(V.fout),
+                                    static_cast<FT*>(V.Fprev), static_cast<FT*>(V.u), V.phase, cell, &empty[s], lane);
     }
 }
 
@@ -532,7 +636,100 @@ bool fits_t(const Lattice& L) {
     return ns <= kMaxStages && staged_smem<T, true, BIB_COLLISION_BGK_GUO_VOF>(ns) + 1024 <= (size_t)optin_smem();
 }
 
+template <class T, int COLL>
+bool batch_inst(const BatchLaunch& B, cudaStream_t s) {
+    using LY = StageLayout<T, true, COLL>;
+    const int ns = B.stages >= 2 ? B.stages : staged_stages<T, true, COLL>(Lattice{});
+    const size_t smem = staged_smem<T, true, COLL>(ns);
+    if (smem + 1024 > (size_t)optin_smem()) return false;
+    int dev = 0, sms = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    auto kern = k_collide_stream_staged_batch<T, COLL>;
+    static std::mutex mu;
+    static std::unordered_map<int, size_t> allowed;
+    static std::unordered_map<int64_t, int> resident;
+    int nb = 0;
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        size_t& lim = allowed[dev];
+        if (smem > lim) {
+            if (cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem) != cudaSuccess)
+                return false;
+            lim = smem;
+        }
+        int& r = resident[((int64_t)dev << 32) | (int64_t)smem];
+        if (r == 0 && (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&r, kern, LY::THREADS, smem) != cudaSuccess ||
+                       r < 1)) {
+            r = 0;
+            return false;
+        }
+        nb = r;
+    }
+    const int64_t grid = std::min<int64_t>(B.ntiles, (int64_t)nb * sms);
+    kern<<<(unsigned)grid, LY::THREADS, smem, s>>>(B.cviews, B.n, B.ntiles, ns, B.wait_err);
+    return true;
+}
+
+template <class T>
+bool batch_t(const BatchLaunch& B, cudaStream_t s) {
+    switch (B.collision) {
+        case BIB_COLLISION_BGK_GUO_VOF: return batch_inst<T, BIB_COLLISION_BGK_GUO_VOF>(B, s);
+        case BIB_COLLISION_BGK: return batch_inst<T, BIB_COLLISION_BGK>(B, s);
+        default: return batch_inst<T, BIB_COLLISION_TRT>(B, s);
+    }
+}
+
+template <class T>
+bool view_t(const Lattice& L, int tile_cells, CollideView& v) {
+    using FT = typename Store<T>::F;
+    using C = typename Store<T>::C;
+    if (!shape_ok<T>(L)) return false;
+    const LatticeDesc& d = L.d;
+    const int target = std::min(tile_cells > 0 ? tile_cells : (sizeof(T) == 8 ? 256 : 512), TileOf<T>::value);
+    v.d = d;
+    v.R = staged_rows(d, target);
+    v.Ct = v.R * d.nx;
+    if (v.Ct > TileOf<T>::value) return false;
+    v.tiles_y = d.ny / v.R;
+    v.ntiles = (int64_t)v.tiles_y * d.nz;
+    const bool need_fcol = d.collision == BIB_COLLISION_BGK_GUO_VOF;
+    v.tx_bytes = (unsigned)(Q * v.Ct * sizeof(T) + ((need_fcol ? 3 : 0) + 3) * v.Ct * sizeof(FT));
+    const CollideParams<C> cp = collide_params<C>(d, L.storage);
+    static_assert(sizeof(CollideParams<C>) <= sizeof(v.cp), "collision constants fit the view");
+    std::memcpy(v.cp, &cp, sizeof(cp));
+    return true;
+}
+
 }  // namespace
+
+bool staged_collide_view(const Lattice& L, int tile_cells, CollideView& v) {
+    if (L.storage == BIB_STORAGE_F64) return view_t<double>(L, tile_cells, v);
+    if (L.storage == BIB_STORAGE_F32) return view_t<float>(L, tile_cells, v);
+    return view_t<__half>(L, tile_cells, v);
+}
+
+bool collide_batch_fits(int storage, int collision, int stages) {
+    auto fits = [&](auto tag) {
+        using T = decltype(tag);
+        const int ns = stages >= 2 ? stages : 2;
+        size_t smem = 0;
+        if (collision == BIB_COLLISION_BGK_GUO_VOF) smem = staged_smem<T, true, BIB_COLLISION_BGK_GUO_VOF>(ns);
+        else if (collision == BIB_COLLISION_BGK) smem = staged_smem<T, true, BIB_COLLISION_BGK>(ns);
+        else smem = staged_smem<T, true, BIB_COLLISION_TRT>(ns);
+        return ns <= 4 && smem + 1024 <= (size_t)optin_smem();
+    };
+    if (storage == BIB_STORAGE_F64) return fits(double{});
+    if (storage == BIB_STORAGE_F32) return fits(float{});
+    return fits(__half{});
+}
+
+bool launch_collide_batch(const BatchLaunch& B, cudaStream_t s) {
+    if (B.n == 0 || B.ntiles == 0) return true;
+    if (B.storage == BIB_STORAGE_F64) return batch_t<double>(B, s);
+    if (B.storage == BIB_STORAGE_F32) return batch_t<float>(B, s);
+    return batch_t<__half>(B, s);
+}
 
 bool collide_staged_fits(const Lattice& L) {
     if (L.storage == BIB_STORAGE_F64) return fits_t<double>(L);

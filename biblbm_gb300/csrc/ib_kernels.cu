@@ -139,14 +139,23 @@ __device__ __forceinline__ float dot_window(const float* row, int64_t k0, const 
 // X_{n+1} = X_n + U_n (DeformableParticle3D::move_vertices, DeformableParticle3D.hh:26-51).
 // Classes and index arithmetic follow interpolate_impl with the Bulk / General
 // interpolators, ImmersedBoundaryDynamics_interpolation.hh:13-153.
-template <class UT, int S>
-__global__ void __launch_bounds__(128) k_interpolate_move(LatticeDesc d, IbDesc ib, int nvert, const double* __restrict__ pos,
-                                                           double* __restrict__ pos_next, const UT* __restrict__ u,
-                                                           double* __restrict__ vel) {
+// One thread per vertex.  BATCH: the vertex numbering runs over the lattices of a batch and
+// each thread looks its lattice's view up through vinst; otherwise v1 is the lattice.
+template <class UT, int S, bool BATCH>
+__global__ void __launch_bounds__(128) k_interpolate_move(IbView v1, const IbView* __restrict__ views,
+                                                           const int* __restrict__ vinst, int nvert) {
     using C = UT;
     static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nvert) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nvert) return;
+    const IbView& V = BATCH ? views[vinst[g]] : v1;
+    const LatticeDesc& d = V.d;
+    const IbDesc& ib = V.ib;
+    const int v = BATCH ? g - V.vbase : g;
+    const double* __restrict__ pos = V.pos;
+    double* __restrict__ pos_next = V.pos_next;
+    const UT* __restrict__ u = static_cast<const UT*>(V.u);
+    double* __restrict__ vel = V.vel;
     const double p[3] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
     double out[3] = {0.0, 0.0, 0.0};
     if (inside_envelope(d, ib.dirac, p)) {
@@ -220,12 +229,19 @@ __global__ void __launch_bounds__(128) k_interpolate_move(LatticeDesc d, IbDesc 
 }
 
 // ---------------------------------------------------------------- spreading
-template <class FT, int S>
-__global__ void __launch_bounds__(128) k_spread(LatticeDesc d, IbDesc ib, int nvert, const double* __restrict__ pos,
-                                                 const double* __restrict__ force, FT* __restrict__ F) {
+template <class FT, int S, bool BATCH>
+__global__ void __launch_bounds__(128) k_spread(IbView v1, const IbView* __restrict__ views, const int* __restrict__ vinst,
+                                                 int nvert) {
     static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
-    const int v = blockIdx.x * blockDim.x + threadIdx.x;
-    if (v >= nvert) return;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nvert) return;
+    const IbView& V = BATCH ? views[vinst[g]] : v1;
+    const LatticeDesc& d = V.d;
+    const IbDesc& ib = V.ib;
+    const int v = BATCH ? g - V.vbase : g;
+    const double* __restrict__ pos = V.pos;
+    const double* __restrict__ force = V.force;
+    FT* __restrict__ F = static_cast<FT*>(V.F);
     const double p[3] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
     if (!inside_envelope(d, ib.dirac, p)) return;
     const int off = (int)ib.offset;
@@ -667,13 +683,16 @@ __device__ __forceinline__ T block_sum(T v, T* red) {
 
 // One CTA per particle: vertex forces at X_n (ParticleBase3D::reset_forces +
 // compute_forces), accumulated in shared memory.
-template <class M>
-__global__ void __launch_bounds__(256) k_membrane(const ParticleDev* __restrict__ parts, const double* __restrict__ pos,
-                                                   double* __restrict__ force, const double* __restrict__ stats) {
+template <class M, bool BATCH>
+__global__ void __launch_bounds__(256) k_membrane(const ParticleDev* __restrict__ parts, IbView v1,
+                                                   const IbView* __restrict__ views) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     M* sf = reinterpret_cast<M*>(smem_raw);
     const ParticleDev& P = parts[blockIdx.x];
-    const double* st = stats + STATS * blockIdx.x;
+    const IbView& V = BATCH ? views[P.inst] : v1;
+    const double* __restrict__ pos = V.pos;
+    double* __restrict__ force = V.force;
+    const double* st = V.stats + STATS * P.lpid;
     const double area = st[0], volume = st[1];
     for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sf[i] = M(0);
     // FP64 element arithmetic uses absolute positions as the reference does; reduced
@@ -769,14 +788,17 @@ __global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* _
 // relative to the previous centre of mass (exact FP64 subtraction, then rounding) and
 // accumulates in FP64; the signed volume of the closed surface does not depend on the
 // origin.
-template <class M>
-__global__ void __launch_bounds__(256) k_particle_update(LatticeDesc d, const ParticleDev* __restrict__ parts,
-                                                          double* __restrict__ pos_next, double* __restrict__ stats) {
+template <class M, bool BATCH>
+__global__ void __launch_bounds__(256) k_particle_update(const ParticleDev* __restrict__ parts, IbView v1,
+                                                          const IbView* __restrict__ views) {
     __shared__ double red[32];
     __shared__ double delta[3];
     extern __shared__ __align__(16) float sp[];  // M = float: relative vertex positions
     const ParticleDev& P = parts[blockIdx.x];
-    double* st = stats + STATS * blockIdx.x;
+    const IbView& V = BATCH ? views[P.inst] : v1;
+    const LatticeDesc& d = V.d;
+    double* __restrict__ pos_next = V.pos_next;
+    double* st = V.stats + STATS * P.lpid;
     const bool rel = sizeof(M) < sizeof(double);
     const double c0 = rel ? st[2] : 0.0, c1 = rel ? st[3] : 0.0, c2 = rel ? st[4] : 0.0;
     const double* pv = pos_next + 3LL * P.v0;
@@ -878,25 +900,84 @@ cudaError_t launch_spread_sorted(const LatticeDesc& d, const IbDesc& ib, bool f6
 }
 
 void configure_membrane_kernel(size_t smem) {
-    cudaFuncSetAttribute(k_membrane<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    cudaFuncSetAttribute(k_membrane<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    // the limit is per kernel function: only ever raise it, other lattices may need more
+    static size_t configured = 0;
+    if (smem <= configured) return;
+    configured = smem;
+    cudaFuncSetAttribute(k_membrane<double, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_membrane<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_membrane<double, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    cudaFuncSetAttribute(k_membrane<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     // 3 floats per vertex, at most half of the membrane kernel's 3 doubles per vertex
-    cudaFuncSetAttribute(k_particle_update<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2));
+    cudaFuncSetAttribute(k_particle_update<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2));
+    cudaFuncSetAttribute(k_particle_update<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2));
 }
+
+IbView single_view(const Lattice& L, int fbuf) {
+    IbView v{};
+    v.d = L.d;
+    v.ib = L.ib;
+    v.pos = L.pos[L.pcur];
+    v.pos_next = L.pos[1 - L.pcur];
+    v.u = L.u;
+    v.vel = L.vel;
+    v.force = L.force;
+    v.F = fbuf >= 0 ? L.F[fbuf] : nullptr;
+    v.stats = L.stats;
+    v.vbase = 0;
+    v.nvert = L.nvert;
+    return v;
+}
+
+namespace {
+
+template <bool BATCH>
+void interpolate_any(int storage, int dirac, const IbView& v1, const IbView* views, const int* vinst, int nvert,
+                     cudaStream_t s) {
+    const unsigned g = (nvert + 127) / 128;
+    const bool peskin = dirac == BIB_DIRAC_PESKIN;
+    if (storage == BIB_STORAGE_F64) {
+        if (peskin) k_interpolate_move<double, 4, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+        else k_interpolate_move<double, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+    } else {
+        if (peskin) k_interpolate_move<float, 4, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+        else k_interpolate_move<float, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+    }
+}
+
+template <bool BATCH>
+void spread_any(int storage, int dirac, const IbView& v1, const IbView* views, const int* vinst, int nvert,
+                cudaStream_t s) {
+    const unsigned g = (nvert + 127) / 128;
+    const bool peskin = dirac == BIB_DIRAC_PESKIN;
+    if (storage == BIB_STORAGE_F64) {
+        if (peskin) k_spread<double, 4, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+        else k_spread<double, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+    } else {
+        if (peskin) k_spread<float, 4, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+        else k_spread<float, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+    }
+}
+
+template <bool BATCH>
+void membrane_any(int storage, const ParticleDev* parts, int np, const IbView& v1, const IbView* views, size_t smem,
+                  int block, cudaStream_t s) {
+    if (storage == BIB_STORAGE_F64) k_membrane<double, BATCH><<<np, block, smem, s>>>(parts, v1, views);
+    else k_membrane<float, BATCH><<<np, block, smem, s>>>(parts, v1, views);
+}
+
+template <bool BATCH>
+void update_any(int storage, const ParticleDev* parts, int np, const IbView& v1, const IbView* views, int max_nv,
+                cudaStream_t s) {
+    if (storage == BIB_STORAGE_F64) k_particle_update<double, BATCH><<<np, 256, 0, s>>>(parts, v1, views);
+    else k_particle_update<float, BATCH><<<np, 256, 3 * sizeof(float) * max_nv, s>>>(parts, v1, views);
+}
+
+}  // namespace
 
 void launch_interpolate_move(const Lattice& L, cudaStream_t s) {
     if (L.nvert == 0) return;
-    const unsigned g = (L.nvert + 127) / 128;
-    const bool peskin = L.ib.dirac == BIB_DIRAC_PESKIN;
-    const double* p0 = L.pos[L.pcur];
-    double* p1 = L.pos[1 - L.pcur];
-    if (L.storage == BIB_STORAGE_F64) {
-        if (peskin) k_interpolate_move<double, 4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, p0, p1, (const double*)L.u, L.vel);
-        else k_interpolate_move<double, 3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, p0, p1, (const double*)L.u, L.vel);
-    } else {
-        if (peskin) k_interpolate_move<float, 4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, p0, p1, (const float*)L.u, L.vel);
-        else k_interpolate_move<float, 3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, p0, p1, (const float*)L.u, L.vel);
-    }
+    interpolate_any<false>(L.storage, L.ib.dirac, single_view(L, -1), nullptr, nullptr, L.nvert, s);
 }
 
 void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
@@ -910,19 +991,30 @@ void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
             k_membrane_gather<float><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats);
         return;
     }
-    if (L.storage == BIB_STORAGE_F64)
-        k_membrane<double><<<np, 256, L.membrane_smem, s>>>(L.pdev, L.pos[L.pcur], L.force, L.stats);
-    else
-        k_membrane<float><<<np, 256, L.membrane_smem, s>>>(L.pdev, L.pos[L.pcur], L.force, L.stats);  // forces + staged positions
+    membrane_any<false>(L.storage, L.pdev, np, single_view(L, -1), nullptr, L.membrane_smem, 256, s);
 }
 
 void launch_particle_update(const Lattice& L, cudaStream_t s) {
     const int np = (int)L.parts.size();
     if (np == 0) return;
-    if (L.storage == BIB_STORAGE_F64)
-        k_particle_update<double><<<np, 256, 0, s>>>(L.d, L.pdev, L.pos[1 - L.pcur], L.stats);
-    else
-        k_particle_update<float><<<np, 256, 3 * sizeof(float) * L.max_nv, s>>>(L.d, L.pdev, L.pos[1 - L.pcur], L.stats);
+    update_any<false>(L.storage, L.pdev, np, single_view(L, -1), nullptr, L.max_nv, s);
+}
+
+void launch_membrane_batch(const BatchLaunch& B, int block, cudaStream_t s) {
+    if (B.nparts == 0) return;
+    membrane_any<true>(B.storage, B.parts, B.nparts, IbView{}, B.views, B.membrane_smem, block, s);
+}
+void launch_spread_batch(const BatchLaunch& B, cudaStream_t s) {
+    if (B.nvert == 0) return;
+    spread_any<true>(B.storage, B.dirac, IbView{}, B.views, B.vinst, B.nvert, s);
+}
+void launch_interpolate_batch(const BatchLaunch& B, cudaStream_t s) {
+    if (B.nvert == 0) return;
+    interpolate_any<true>(B.storage, B.dirac, IbView{}, B.views, B.vinst, B.nvert, s);
+}
+void launch_update_batch(const BatchLaunch& B, cudaStream_t s) {
+    if (B.nparts == 0) return;
+    update_any<true>(B.storage, B.parts, B.nparts, IbView{}, B.views, B.max_nv, s);
 }
 
 void launch_spread(const Lattice& L, int fbuf, cudaStream_t s) {
@@ -943,16 +1035,7 @@ void launch_spread(const Lattice& L, int fbuf, cudaStream_t s) {
             k_spread_reduce<float><<<ge, 128, 0, s>>>(L.d, L.ib, ne, L.sort_keys[1], L.sort_ids[1], pos, L.force, (float*)L.F[fbuf]);
         return;
     }
-    const bool peskin = L.ib.dirac == BIB_DIRAC_PESKIN;
-    if (L.storage == BIB_STORAGE_F64) {
-        double* F = (double*)L.F[fbuf];
-        if (peskin) k_spread<double, 4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, F);
-        else k_spread<double, 3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, F);
-    } else {
-        float* F = (float*)L.F[fbuf];
-        if (peskin) k_spread<float, 4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, F);
-        else k_spread<float, 3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.force, F);
-    }
+    spread_any<false>(L.storage, L.ib.dirac, single_view(L, fbuf), nullptr, nullptr, L.nvert, s);
 }
 
 }  // namespace bib

@@ -256,13 +256,31 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
 // (finiteDifference3D.h:67-82; tangential derivatives vanish for a uniform wall
 // velocity), regularised reconstruction of all 19 populations into the wall buffer.
 template <class T>
+__device__ __forceinline__ void fd_wall_cell(const LatticeDesc& d, const T* __restrict__ f, T* __restrict__ wall,
+                                             const typename Store<T>::F* __restrict__ F, int x, int z, int side);
+
+template <class T>
 __global__ void k_fd_walls(LatticeDesc d, const T* __restrict__ f, T* __restrict__ wall,
                            const typename Store<T>::F* __restrict__ F) {
-    using C = typename Store<T>::C;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
-    const int z = blockIdx.y;
-    const int side = blockIdx.z;
     if (x >= d.nx) return;
+    fd_wall_cell<T>(d, f, wall, F, x, blockIdx.y, blockIdx.z);
+}
+
+// Batched: grid.z = 2 sides x lattices; each lattice's view of the state after the swap.
+template <class T>
+__global__ void k_fd_walls_batch(const CollideView* __restrict__ views) {
+    const CollideView& V = views[blockIdx.z >> 1];
+    const int x = blockIdx.x * blockDim.x + threadIdx.x, z = blockIdx.y;
+    if (!V.d.fd_walls || x >= V.d.nx || z >= V.d.nz) return;
+    fd_wall_cell<T>(V.d, static_cast<const T*>(V.fin), static_cast<T*>(const_cast<void*>(V.wall)),
+                    static_cast<const typename Store<T>::F*>(V.Fprev), x, z, blockIdx.z & 1);
+}
+
+template <class T>
+__device__ __forceinline__ void fd_wall_cell(const LatticeDesc& d, const T* __restrict__ f, T* __restrict__ wall,
+                                             const typename Store<T>::F* __restrict__ F, int x, int z, int side) {
+    using C = typename Store<T>::C;
     const int y = side == 0 ? 0 : d.ny - 1;
     const int orientation = side == 0 ? -1 : 1;
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
@@ -469,6 +487,13 @@ void collide_stream_t(const Lattice& L, bool coupled, cudaStream_t s) {
 }
 
 template <class T>
+void fd_walls_batch_t(const BatchLaunch& B, cudaStream_t s) {
+    const int bx = B.nx_max >= 128 ? 128 : 64;
+    dim3 g((B.nx_max + bx - 1) / bx, B.nz_max, 2 * B.n);
+    k_fd_walls_batch<T><<<g, bx, 0, s>>>(B.wviews);
+}
+
+template <class T>
 void fd_walls_t(const Lattice& L, int buf, int fbuf, cudaStream_t s) {
     using FT = typename Store<T>::F;
     const int bx = row_block(L.d);
@@ -528,6 +553,11 @@ void nan_scan_t(const Lattice& L, int* flag, cudaStream_t s) {
 
 void launch_collide_stream(const Lattice& L, bool coupled, cudaStream_t s) {
     BIB_DISPATCH(L.storage, collide_stream_t, L, coupled, s);
+}
+
+void launch_fd_walls_batch(const BatchLaunch& B, cudaStream_t s) {
+    if (!B.any_fd || B.n == 0) return;
+    BIB_DISPATCH(B.storage, fd_walls_batch_t, B, s);
 }
 
 void launch_fd_walls(const Lattice& L, int buf, int fbuf, cudaStream_t s) {

@@ -202,6 +202,25 @@ bib_status bib_check_health(bib_ctx* ctx, int32_t h);
  * BIB_EUNSUPPORTED if BIB_KERNEL_STAGED is forced on a lattice whose x-rows do not fit it */
 bib_status bib_lattice_set_tuning(bib_ctx* ctx, int32_t h, const bib_tuning* t);
 
+/* ---- batches: several independent lattices stepped in lockstep, one launch per kernel for all of them,
+ * replayed as CUDA graphs (no reference counterpart; the reference runs one domain per process).  The
+ * lattices share storage, collision and delta kernel, spread with atomics and fit the staged
+ * collide-and-stream kernel.  A batch step is a bib_step of every lattice. ---- */
+typedef struct {
+    int32_t tile_cells;     /* staged collide-and-stream tile (cells, whole x-rows); 0 = default */
+    int32_t stages;         /* its pipeline depth 2..4; 0 = automatic */
+    int32_t membrane_block; /* threads per particle of the membrane kernel: 64, 128 or 256 (0 = 256) */
+    int32_t reserved[5];
+} bib_batch_tuning;
+bib_status bib_batch_create(bib_ctx* ctx, const int32_t* handles, int32_t n, int32_t* batch);
+bib_status bib_batch_destroy(bib_ctx* ctx, int32_t batch);
+bib_status bib_batch_step(bib_ctx* ctx, int32_t batch, int64_t nsteps);
+bib_status bib_batch_step_timed(bib_ctx* ctx, int32_t batch, int64_t nsteps, double* ms);
+bib_status bib_batch_set_tuning(bib_ctx* ctx, int32_t batch, const bib_batch_tuning* t);
+/* Autotuner: times every tile size x stage count, then every membrane block size, each over `steps`
+ * real coupled steps (the batch advances by those steps), and keeps the fastest; *chosen may be NULL. */
+bib_status bib_batch_autotune(bib_ctx* ctx, int32_t batch, int32_t steps, bib_batch_tuning* chosen);
+
 /* ---- deterministic force spreading that allocates no device memory (no counterpart in the reference) ----
  * For callers that cannot let the library allocate device memory: a host whose pool allocator already
  * holds the GPU's free memory (a cudaMalloc by the library would fail or fragment it), or a stepping loop
