@@ -160,6 +160,106 @@ def run_reference(args, wl):
     print(json.dumps(line), flush=True)
 
 
+def run_batch(args):
+    """64 independent capsule-in-shear instances (cubic edges 32..96, radius edge/6, 162 / 642
+    vertices, Ca log-uniform in [0.01, 1], seed 4), FP32 storage, stepped as one batch after the
+    autotuner picked its schedule; the same instances stepped one lattice at a time for
+    comparison."""
+    import biblbm_gb300 as bib
+    from biblbm_gb300 import workloads
+
+    wl = workloads.batched_capsules()
+    K, W = args.steps, args.warmup
+    storage = "f32" if args.storage == "f16" else args.storage
+    ctx = bib.Context(0)
+    built = [build_instance(bib, ctx, w, storage) for w in wl["instances"]]
+    batch = bib.Batch(ctx, [b[0] for b in built])
+    chosen = batch.autotune(steps=3)
+    batch.step(W)
+    ctx.sync()
+    with ClockSampler(0) as clk:
+        ms = batch.step_timed(K)
+    cells, verts = wl["cells"], wl["vertices"]
+    mlups = cells * K / (ms * 1e-3) / 1e6
+    # one lattice at a time (each with its own two-step graphs), same number of steps
+    k2 = max(2, K // 10)
+    ms_solo = sum(f.step_timed(k2) for _, f in built) / k2 * K
+    launches = K * 6
+    line = {
+        "metric": METRIC, "value": mlups, "unit": "MLUPS", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": ms / K, "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded instance sizes, meshes and capillary numbers, seed 4)",
+        "config": {"workload": wl["name"], "instances": len(wl["instances"]), "cells": cells, "vertices": verts,
+                   "storage": storage, "l2": "64 lattices, 17.7 M cells: populations 1.1 GB > L2", "parallelism": "1 GPU"},
+        "vertex_updates_per_s": verts * K / (ms * 1e-3),
+        "autotuned": chosen,
+        "one_lattice_at_a_time": {"mlups": cells * K / (ms_solo * 1e-3) / 1e6, "ms_per_step": ms_solo / K},
+        "gpu_launches": launches,
+        "roofline": {"bound": "hbm", "kernel": "whole batched step (6 launches)", "achieved":
+                     200 * cells / (ms / K * 1e-3) / 1e9, "peak": float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs", 6800.0)) if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")) else 6800.0,
+                     "unit": "GB/s", "traffic": None},
+        "clocks": clk.summary(),
+        "e2e": None,
+        "cpu_baseline": None,
+    }
+    line["roofline"]["frac"] = line["roofline"]["achieved"] / line["roofline"]["peak"]
+    print(json.dumps(line))
+
+
+def run_tgv(args):
+    """Lattice-only TRT (magic 1/4) Taylor-Green vortex in periodic cubes of 128, 256 and 384,
+    u0 = 0.02: MLUPS and the relative error of the decay against exp(-2 nu k^2 t) after the
+    timed steps, for the chosen storage (all three with --storage all is not offered: run
+    three times)."""
+    import biblbm_gb300 as bib
+
+    K, W = args.steps, args.warmup
+    ctx = bib.Context(0)
+    res = {}
+    peak = 6800.0
+    if os.path.exists(os.path.join(ROOT, "MEASURED_PEAKS.json")):
+        peak = float(json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("hbm_gbs", peak))
+    bytes_lu = {"f64": 2 * 19 * 8 + 3 * 8, "f32": 2 * 19 * 4 + 3 * 4, "f16": 2 * 19 * 2 + 3 * 4}[args.storage]
+    for n in (128, 256, 384):
+        tau, u0 = 0.8, 0.02
+        lat = ctx.add_domain(n, n, n, periodic=(1, 1, 1), collision="trt", omega=1 / tau, trt_magic=0.25,
+                             storage=args.storage)
+        k = 2 * np.pi / n
+        x = np.arange(n)
+        X, Y = np.meshgrid(x, x, indexing="xy")
+        u = np.zeros((3, n, n, n))
+        u[0] = (u0 * np.sin(k * X) * np.cos(k * Y))[None]
+        u[1] = (-u0 * np.cos(k * X) * np.sin(k * Y))[None]
+        rho = np.broadcast_to((1.0 + 0.75 * u0 * u0 * (np.cos(2 * k * X) + np.cos(2 * k * Y)))[None], (n, n, n))
+        lat.initialize_at_equilibrium(np.ascontiguousarray(rho), u)
+        lat.collide_and_stream(W)
+        ctx.sync()
+        t0 = time.perf_counter()
+        lat.collide_and_stream(K)
+        ctx.sync()
+        dt = time.perf_counter() - t0
+        ux = lat.compute_velocity()[0]
+        nu = (tau - 0.5) / 3
+        expect = u0 * np.exp(-2 * nu * k * k * (W + K))
+        res[str(n)] = {"mlups": n ** 3 * K / dt / 1e6, "achieved_gbs": bytes_lu * n ** 3 * K / dt / 1e9,
+                       "decay_rel_error": float(abs(np.abs(ux).max() - expect) / expect)}
+        ctx.sync()
+        del lat
+    best = res["384"]
+    line = {
+        "metric": METRIC, "value": best["mlups"], "unit": "MLUPS", "n_gpus": 1, "steps": K, "warmup": W,
+        "ms_per_step": 384 ** 3 / best["mlups"] / 1e3, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": args.storage, "data": "synthetic (Taylor-Green vortex, u0 = 0.02)",
+        "config": {"workload": "tgv_trt_sweep", "edges": [128, 256, 384], "storage": args.storage,
+                   "l2": "populations > L2 from 128^3 on", "parallelism": "1 GPU"},
+        "sweep": res,
+        "roofline": {"bound": "hbm", "kernel": "collide-and-stream (lattice-only)", "achieved": best["achieved_gbs"],
+                     "peak": peak, "unit": "GB/s", "frac": best["achieved_gbs"] / peak, "traffic": None},
+        "gpu_launches": K, "e2e": None, "cpu_baseline": None,
+    }
+    print(json.dumps(line))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -167,7 +267,10 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--storage", default="f16", choices=["f16", "f32", "f64"])
-    ap.add_argument("--workload", default="channel", choices=["channel", "capsule"])
+    ap.add_argument("--workload", default="channel", choices=["channel", "capsule", "rbc", "batch", "tgv"],
+                    help="channel: 400 RBCs in 512x128x128 (the headline); capsule: one capsule in shear, 64^3; "
+                         "rbc: one RBC in shear, 128x64x64; batch: 64 capsule instances stepped as one batch; "
+                         "tgv: TRT Taylor-Green bandwidth sweep, 128^3 / 256^3 / 384^3")
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
@@ -179,7 +282,11 @@ def main():
 
     from biblbm_gb300 import workloads
 
-    wl = workloads.channel_suspension() if args.workload == "channel" else workloads.capsule_shear()
+    if args.workload in ("batch", "tgv") and args.impl == "native":
+        return run_batch(args) if args.workload == "batch" else run_tgv(args)
+    wl = {"channel": workloads.channel_suspension, "capsule": workloads.capsule_shear, "rbc": workloads.rbc_shear,
+          "batch": lambda: workloads.batched_capsules()["instances"][0],
+          "tgv": workloads.capsule_shear}[args.workload]()
     if args.impl == "reference":
         run_reference(args, wl)
         return

@@ -10,6 +10,9 @@ bounce-back walls on y and z, periodic x, body force 1e-6, 400 Evans-Fung cells 
 vertices at 20 % haematocrit, random non-overlapping positions and orientations).
 ``capsule_shear``: one spherical capsule in simple shear between finite-difference
 velocity walls (progs/capsule_in_shear/capsule_in_shear.cpp).
+``batched_capsules``: independent capsule-in-shear instances of uneven sizes (cubic edges
+drawn from {32, 48, 64, 80, 96}, radius edge/6, 162- or 642-vertex meshes, capillary number
+log-uniform in [0.01, 1]), stepped together as one batch.
 """
 from __future__ import annotations
 
@@ -128,4 +131,44 @@ def capsule_shear(n=64, level=3, radius=10.0, U=0.01, tau=1.0, Ca=0.1, seed=1):
                      wall_u=[[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]),
         rest=rest, tri=tri, positions=pos[None], model="capsule_skalak", params=params_vector(G=G, C=1.0),
         radius=radius, initial_velocity=u0, seed=seed,
+    )
+
+
+def batched_capsules(n_inst=64, seed=4, edges=(32, 48, 64, 80, 96), U=0.01, tau=1.0):
+    rng = np.random.default_rng(seed)
+    inst = []
+    for _ in range(n_inst):
+        n = int(rng.choice(edges))
+        level = 2 if rng.uniform() < 0.5 else 3  # 162 or 642 vertices
+        Ca = float(np.exp(rng.uniform(np.log(0.01), np.log(1.0))))
+        inst.append(capsule_shear(n=n, level=level, radius=n / 6.0, U=U, tau=tau, Ca=Ca, seed=seed))
+    cells = sum(w["dims"][0] ** 3 for w in inst)
+    verts = sum(w["rest"].shape[0] for w in inst)
+    return dict(name="batched_capsules_%d" % n_inst, instances=inst, cells=cells, vertices=verts, seed=seed)
+
+
+def rbc_shear(nx=128, ny=64, nz=64, level=4, radius=8.0, U=0.01, tau=1.0, Ca=0.1, seed=2):
+    """One Evans-Fung red cell (major radius 8, 2562 vertices) in simple shear between
+    finite-difference velocity walls, Skalak + bending (kb = 0.01 G A0) + global area and
+    volume penalties, random orientation."""
+    rng = np.random.default_rng(seed)
+    rest, tri = meshes.evans_fung(level, radius)
+    rest = rest - rest.mean(axis=0)
+    A0, V0 = mesh_area_volume(rest, tri)
+    nu = (tau - 0.5) / 3.0
+    gamma = 2.0 * U / (ny - 1)
+    G = nu * gamma * radius / Ca
+    c = np.array([0.5 * (nx - 1), 0.5 * (ny - 1), 0.5 * (nz - 1)])
+    pos = rest @ meshes.random_rotation(rng).T + c
+    y = np.arange(ny)
+    u0 = np.zeros((3, nz, ny, nx))
+    u0[0] = (U * (2.0 * y / (ny - 1) - 1))[None, :, None]
+    prm = params_vector(G=G, C=1.0, k_area_global=1.0, k_volume=1.0, vol_desired=V0, k_bend=0.01 * G * A0)
+    return dict(
+        name="rbc_shear_%dx%dx%d_%dv" % (nx, ny, nz, rest.shape[0]),
+        dims=(nx, ny, nz),
+        lattice=dict(periodic=(1, 0, 1), collision="bgk_guo_vof", omega=1.0 / tau, wall_y="fd_velocity",
+                     wall_u=[[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]),
+        rest=rest, tri=tri, positions=pos[None], model="skalak_bending", params=prm, radius=radius, A0=A0, V0=V0,
+        initial_velocity=u0, seed=seed,
     )
