@@ -174,6 +174,12 @@ def run_batch(args):
     ctx = bib.Context(0)
     built = [build_instance(bib, ctx, w, storage) for w in wl["instances"]]
     batch = bib.Batch(ctx, [b[0] for b in built])
+    if args.ncu:  # profiling run: default schedule, plain launches
+        ctx.set_graph_mode(False)
+        batch.step(W)
+        ctx.sync()
+        ctx.close()
+        return
     chosen = batch.autotune(steps=3)
     batch.step(W)
     ctx.sync()

@@ -116,12 +116,15 @@ struct Staged<double> {
     static __device__ __forceinline__ void put(double* p, double a) { *p = a; }
 };
 
-// Collision of one cell in storage units.  FP32 compute with BGK(+Guo) uses the compact
-// pairwise form; TRT and FP64 unscale, run the generic operator and rescale.  With u
+// Collision of one cell in storage units.  FP32 compute uses the compact pairwise forms
+// (BGK + Guo, BGK, TRT); FP64 runs the generic operator of the reference's order.  With u
 // non-null the velocity j/rho + Fp/2 of the incoming state is returned.
 template <class C, int COLL>
 __device__ __forceinline__ void staged_collide(C* f, const C* F, C om, C omm, C S, C invS, const C* Fp, C* u) {
-    if constexpr (sizeof(C) == 4 && COLL != BIB_COLLISION_TRT) {
+    if constexpr (sizeof(C) == 4 && COLL == BIB_COLLISION_TRT) {
+        const C Fm[3] = {omm, C(0), C(0)};  // the TRT branch takes omega_minus in F[0]
+        collide_compact<COLL>(f, Fm, om, S, invS, Fp, u);
+    } else if constexpr (sizeof(C) == 4) {
         collide_compact<COLL>(f, F, om, S, invS, Fp, u);
     } else {
         if (sizeof(C) == 4) {
@@ -183,12 +186,29 @@ __device__ __forceinline__ TileRef tile_ref(const LatticeDesc& d, const StagedGe
     return t;
 }
 
+// Lattice vector of the population a producer lane moves, resolved once per kernel (the
+// lane index is not a compile-time constant, so cx(i) etc. would be evaluated per row).
+struct PopLane {
+    int cy, cz, opp;
+};
+__device__ __forceinline__ PopLane pop_lane(int lane) {
+    PopLane p{0, 0, 0};
+#pragma unroll
+    for (int i = 0; i < Q; ++i)
+        if (lane == i) {
+            p.cy = cy(i);
+            p.cz = cz(i);
+            p.opp = opposite(i);
+        }
+    return p;
+}
+
 // Copies of one tile into one stage, by the producer warp: lane i < 19 moves population i,
 // lanes 19..21 the collision force, lanes 22..24 the previous force.
 template <class T, bool COUPLED, int COLL>
 __device__ __forceinline__ void load_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, unsigned char* stage,
                                           uint64_t* bar, const T* fin, const T* wall, const typename Store<T>::F* Fcol,
-                                          const typename Store<T>::F* Fprev, int lane) {
+                                          const typename Store<T>::F* Fprev, int lane, const PopLane& pl) {
     using L = StageLayout<T, COUPLED, COLL>;
     using FT = typename Store<T>::F;
     const TileRef t = tile_ref(d, g, tile);
@@ -198,30 +218,44 @@ __device__ __forceinline__ void load_tile(const LatticeDesc& d, const StagedGeom
     if (lane < Q) {
         const int i = lane;
         unsigned char* dst = stage + i * L::POP;
-        const unsigned char* run = nullptr;
-        unsigned run_len = 0, run_at = 0;
-        for (int r = 0; r < g.R; ++r) {
-            const int y = t.y0 + r;
-            const T* src;
-            if (fd_wall_node(d, y)) {
-                src = wall + i * wall_stride(d) + wall_index(d, y == 0 ? 0 : 1, 0, t.z);
-            } else {
-                int64_t srow;
-                const int face = source_row(d, i, y, t.z, srow);
-                src = face >= 0 ? fin + opposite(i) * d.stride + ((int64_t)y + (int64_t)d.ny * t.z) * d.nx
-                                : fin + i * d.stride + srow * d.nx;
+        // source plane of this population (periodic wrap or a z wall behind it)
+        int zs = t.z - pl.cz;
+        bool zface = false;
+        if (d.pz) zs = zs < 0 ? zs + d.nz : (zs >= d.nz ? zs - d.nz : zs);
+        else zface = zs < 0 || zs >= d.nz;
+        const int ya = t.y0 - pl.cy, yb = t.y0 + g.R - 1 - pl.cy;  // source rows of the tile's first / last row
+        const bool fd_rows = d.fd_walls && (t.y0 == 0 || t.y0 + g.R == d.ny);
+        if (!zface && !fd_rows && ya >= 0 && yb < d.ny) {
+            // every row of the tile streams from the neighbouring rows of one plane: one run
+            bulk_copy_g2s(dst, fin + i * d.stride + ((int64_t)ya + (int64_t)d.ny * zs) * d.nx, g.R * rowb, bar);
+        } else {
+            const unsigned char* run = nullptr;
+            unsigned run_len = 0, run_at = 0;
+            for (int r = 0; r < g.R; ++r) {
+                const int y = t.y0 + r;
+                const T* src;
+                if (fd_wall_node(d, y)) {
+                    src = wall + i * wall_stride(d) + wall_index(d, y == 0 ? 0 : 1, 0, t.z);
+                } else {
+                    int ys = y - pl.cy;
+                    bool face = zface;
+                    if (d.py) ys = ys < 0 ? ys + d.ny : (ys >= d.ny ? ys - d.ny : ys);
+                    else face = face || ys < 0 || ys >= d.ny;
+                    src = face ? fin + pl.opp * d.stride + ((int64_t)y + (int64_t)d.ny * t.z) * d.nx
+                               : fin + i * d.stride + ((int64_t)ys + (int64_t)d.ny * zs) * d.nx;
+                }
+                const unsigned char* s = reinterpret_cast<const unsigned char*>(src);
+                if (run_len && s == run + run_len) {
+                    run_len += rowb;
+                } else {
+                    if (run_len) bulk_copy_g2s(dst + run_at, run, run_len, bar);
+                    run = s;
+                    run_len = rowb;
+                    run_at = (unsigned)r * rowb;
+                }
             }
-            const unsigned char* s = reinterpret_cast<const unsigned char*>(src);
-            if (run_len && s == run + run_len) {
-                run_len += rowb;
-            } else {
-                if (run_len) bulk_copy_g2s(dst + run_at, run, run_len, bar);
-                run = s;
-                run_len = rowb;
-                run_at = (unsigned)r * rowb;
-            }
+            bulk_copy_g2s(dst + run_at, run, run_len, bar);
         }
-        bulk_copy_g2s(dst + run_at, run, run_len, bar);
     } else {
         const unsigned fb = (unsigned)(g.Ct * sizeof(FT));
         if (L::NEED_FCOL && lane < Q + 3) {
@@ -368,6 +402,7 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
 
     if (warp == 0) {
         // ---- producer
+        const PopLane pl = pop_lane(lane);
         int it = 0;
         for (int64_t tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x, ++it) {
             const int s = it % NS, use = it / NS;
@@ -379,7 +414,7 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
                     break;
                 }
             }
-            load_tile<T, COUPLED, COLL>(d, g, tile, stages + s * L::BYTES, &full[s], fin, wall, Fcol, Fprev, lane);
+            load_tile<T, COUPLED, COLL>(d, g, tile, stages + s * L::BYTES, &full[s], fin, wall, Fcol, Fprev, lane, pl);
         }
         // a copy may still be landing only if the consumers gave up; wait for it so that
         // no bulk copy writes into the shared memory of a retired CTA
@@ -452,6 +487,7 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
     }
     __syncthreads();
     if (warp == 0) {
+        const PopLane pl = pop_lane(lane);
         int it = 0;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
             const int s = it % NS, use = it / NS;
@@ -465,7 +501,7 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
             const CollideView& V = views[find_view(views, nviews, tile)];
             load_tile<T, true, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES, &full[s],
                                      static_cast<const T*>(V.fin), static_cast<const T*>(V.wall),
-                                     static_cast<const FT*>(V.Fcol), static_cast<const FT*>(V.Fprev), lane);
+                                     static_cast<const FT*>(V.Fcol), static_cast<const FT*>(V.Fprev), lane, pl);
         }
         if (lane == 0) {
             const int issued = it;

@@ -230,6 +230,26 @@ __device__ __forceinline__ void collide_compact(float* f, const float* F, float 
         u_prev[1] = fmaf(j1, invRho, 0.5f * Fprev[1]);
         u_prev[2] = fmaf(j2, invRho, 0.5f * Fprev[2]);
     }
+    if (COLL == BIB_COLLISION_TRT) {
+        // Two relaxation times around the BGK equilibrium of j: the symmetric part of each
+        // pair (i, i+9) relaxes with omega, the antisymmetric part with omega_minus (passed
+        // in F[0]); feq+ = t_i (rhoBar + 4.5 (c.j)^2 / rho - 1.5 j.j / rho), feq- = 3 t_i c.j.
+        const float omm = F[0];
+        const float base = rb - 1.5f * invRho * (j0 * j0 + j1 * j1 + j2 * j2);
+        const float h = 4.5f * invRho;
+        f[0] = fmaf(-omega, f[0] - (S * weight<float>(0)) * base, f[0]);
+#pragma unroll
+        for (int i = 1; i < 10; ++i) {
+            const float cj = cdot(i, j0, j1, j2);
+            const float tw = S * weight<float>(i);
+            const float ep = tw * fmaf(h * cj, cj, base), em = tw * 3.0f * cj;
+            const float dp = omega * (0.5f * (f[i] + f[i + 9]) - ep);
+            const float dm = omm * (0.5f * (f[i] - f[i + 9]) - em);
+            f[i] = f[i] - dp - dm;
+            f[i + 9] = f[i + 9] - dp + dm;
+        }
+        return;
+    }
     const bool forced = COLL == BIB_COLLISION_BGK_GUO_VOF;
     const float F0 = forced ? F[0] : 0.0f, F1 = forced ? F[1] : 0.0f, F2 = forced ? F[2] : 0.0f;
     const float u0 = fmaf(j0, invRho, 0.5f * F0), u1 = fmaf(j1, invRho, 0.5f * F1), u2 = fmaf(j2, invRho, 0.5f * F2);
