@@ -91,7 +91,7 @@ struct IbView {
     IbDesc ib;
     const double* pos;   // X_n
     double* pos_next;    // X_{n+1}
-    const void* u;       // velocity field (FP64 for FP64 storage, FP32 otherwise)
+    const void* u;       // velocity field, 4 values per cell (FP64 for FP64 storage, FP32 otherwise)
     double* vel;
     double* force;       // vertex forces
     void* F;             // spreading target (field type as u)
@@ -166,7 +166,7 @@ struct Lattice {
     void* F[2] = {nullptr, nullptr};  // force fields (double for F64 storage, float otherwise)
     int fe = 0;
     bool target_clean = false;        // F[1-fe] holds the body force, ready to receive spreading
-    void* u = nullptr;                // velocity field (double for F64 storage, float otherwise)
+    void* u = nullptr;                // velocity field, (ux, uy, uz, 0) per cell (double for F64 storage, float otherwise)
     uint8_t* phase = nullptr;
     // immersed boundary
     std::vector<ParticleHost> parts;

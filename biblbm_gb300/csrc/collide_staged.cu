@@ -345,11 +345,9 @@ __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedG
 #pragma unroll
             for (int q = 0; q < 3; ++q) u[q] = cp.wall_u[side][q];
         }
+        store_u<FT>(u_out, k, (FT)u[0], (FT)u[1], (FT)u[2]);
 #pragma unroll
-        for (int q = 0; q < 3; ++q) {
-            u_out[q * d.stride + k] = (FT)u[q];
-            Fprev[q * d.stride + k] = (FT)cp.body[q];
-        }
+        for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
     } else {
         staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, nullptr, nullptr);
     }

@@ -92,9 +92,9 @@ __device__ __forceinline__ int64_t axis_weights(double x, W* w) {
     return lo;
 }
 
-// Windows of up to four consecutive cells of one x-row of one field component, moved as
-// one or two aligned float4 accesses (the field rows start 16-byte aligned: the component
-// stride is a multiple of 128 cells).  Slots outside the window read / add zero.
+// Windows of up to four consecutive cells of one x-row of one force component, added with
+// one or two aligned float4 atomics (the field rows start 16-byte aligned: the component
+// stride is a multiple of 128 cells).  Slots outside the window add zero.
 __device__ __forceinline__ float window_select(const float* x, int j, int o, int s) {
     float r = 0.0f;
 #pragma unroll
@@ -112,25 +112,19 @@ __device__ __forceinline__ void red_window(float* row, int64_t k0, const float* 
         atomicAdd(q + 1, make_float4(window_select(v, 4, o, s), window_select(v, 5, o, s), window_select(v, 6, o, s),
                                      window_select(v, 7, o, s)));
 }
-// sum_m w[m] * row[k0 + m]
-__device__ __forceinline__ float dot_window(const float* row, int64_t k0, const float* w, int s) {
-    const int64_t kq = k0 & ~(int64_t)3;
-    const int o = (int)(k0 - kq);
-    const float4* q = reinterpret_cast<const float4*>(row + kq);
-    const float4 a = __ldg(q);
-    const float4 b = o + s > 4 ? __ldg(q + 1) : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float x[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
-    float acc = 0.0f;
-#pragma unroll
-    for (int m = 0; m < 4; ++m)
-        if (m < s) {
-            float xm = 0.0f;
-#pragma unroll
-            for (int j = 0; j < 8; ++j)
-                if (j == o + m) xm = x[j];
-            acc += w[m] * xm;
-        }
-    return acc;
+// One cell of the velocity field ((ux, uy, uz, 0) per cell), one or two vector loads.
+template <class C>
+struct U3 {
+    C x, y, z;
+};
+__device__ __forceinline__ U3<float> load_u(const float* u, int64_t k) {
+    const float4 v = __ldg(reinterpret_cast<const float4*>(u) + k);
+    return U3<float>{v.x, v.y, v.z};
+}
+__device__ __forceinline__ U3<double> load_u(const double* u, int64_t k) {
+    const double2* q = reinterpret_cast<const double2*>(u) + 2 * k;
+    const double2 a = __ldg(q), b = __ldg(q + 1);
+    return U3<double>{a.x, a.y, b.x};
 }
 
 // ---------------------------------------------------------------- interpolation
@@ -178,41 +172,22 @@ __global__ void __launch_bounds__(128) k_interpolate_move(IbView v1, const IbVie
             zo[m] = (int64_t)gz[m] * d.ny * d.nx;
         }
         C acc[3] = {C(0), C(0), C(0)};
-        if (sizeof(UT) == sizeof(float) && gx[s - 1] == gx[0] + s - 1) {
-            // FP32 field and no periodic wrap along x inside the support: each (y, z) row is
-            // one window of s consecutive cells, read with aligned vector loads
-            const float* uf = reinterpret_cast<const float*>(u);
+#pragma unroll
+        for (int a = 0; a < s; ++a) {
+            if (gx[a] < 0) continue;
 #pragma unroll
             for (int b = 0; b < s; ++b) {
                 if (gy[b] < 0) continue;
+                const C wxy = w[0][a] * w[1][b];
+                const int64_t col = gx[a] + yo[b];
 #pragma unroll
                 for (int c = 0; c < s; ++c) {
                     if (gz[c] < 0) continue;
-                    const float wyz = (float)(w[1][b] * w[2][c]);
-                    const int64_t k0 = gx[0] + yo[b] + zo[c];
-                    float wx[4];
-                    for (int m = 0; m < 4; ++m) wx[m] = m < s ? (float)w[0][m] * wyz : 0.0f;
-                    for (int q = 0; q < 3; ++q) acc[q] += (C)dot_window(uf + q * d.stride, k0, wx, s);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int a = 0; a < s; ++a) {
-                if (gx[a] < 0) continue;
-#pragma unroll
-                for (int b = 0; b < s; ++b) {
-                    if (gy[b] < 0) continue;
-                    const C wxy = w[0][a] * w[1][b];
-                    const UT* col = u + gx[a] + yo[b];
-#pragma unroll
-                    for (int c = 0; c < s; ++c) {
-                        if (gz[c] < 0) continue;
-                        const C wt = wxy * w[2][c];
-                        const UT* q = col + zo[c];
-                        acc[0] += wt * __ldg(q);
-                        acc[1] += wt * __ldg(q + d.stride);
-                        acc[2] += wt * __ldg(q + 2 * d.stride);
-                    }
+                    const C wt = wxy * w[2][c];
+                    const U3<C> uc = load_u(u, col + zo[c]);
+                    acc[0] += wt * uc.x;
+                    acc[1] += wt * uc.y;
+                    acc[2] += wt * uc.z;
                 }
             }
         }

@@ -34,6 +34,21 @@ __device__ __forceinline__ C moving_wall_term(const LatticeDesc& d, int i, int f
 }
 
 
+// The velocity field is stored as four values per cell (ux, uy, uz, 0): one aligned vector
+// access per cell for the interpolation's 27 / 64-node gathers.
+template <class FT>
+__device__ __forceinline__ void store_u(FT* u, int64_t k, FT a, FT b, FT c);
+template <>
+__device__ __forceinline__ void store_u<float>(float* u, int64_t k, float a, float b, float c) {
+    reinterpret_cast<float4*>(u)[k] = make_float4(a, b, c, 0.0f);
+}
+template <>
+__device__ __forceinline__ void store_u<double>(double* u, int64_t k, double a, double b, double c) {
+    double2* q = reinterpret_cast<double2*>(u) + 2 * k;
+    q[0] = make_double2(a, b);
+    q[1] = make_double2(c, 0.0);
+}
+
 // Row (y, z) lies next to a wall or is a finite-difference wall row: its gather needs the
 // per-population face tests; every other row streams from its 18 neighbours unchanged.
 __device__ __forceinline__ bool row_special(const LatticeDesc& d, int y, int z) {

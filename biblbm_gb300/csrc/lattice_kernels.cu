@@ -81,9 +81,7 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
             C Fp[3] = {(C)Fprev[k], (C)Fprev[d.stride + k], (C)Fprev[2 * d.stride + k]};
             velocity_with_force(f, Fp, u);
         }
-        u_out[k] = (FT)u[0];
-        u_out[d.stride + k] = (FT)u[1];
-        u_out[2 * d.stride + k] = (FT)u[2];
+        store_u<FT>(u_out, k, (FT)u[0], (FT)u[1], (FT)u[2]);
         Fprev[k] = (FT)d.body[0];
         Fprev[d.stride + k] = (FT)d.body[1];
         Fprev[2 * d.stride + k] = (FT)d.body[2];
@@ -222,8 +220,9 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
             velocity_with_force(f0, Fa, u0);
             velocity_with_force(f1, Fb, u1);
         }
+        store_u<FT>(u_out, k0, (FT)u0[0], (FT)u0[1], (FT)u0[2]);
+        store_u<FT>(u_out, k0 + 1, (FT)u1[0], (FT)u1[1], (FT)u1[2]);
         for (int c = 0; c < 3; ++c) {
-            store2<FT>(u_out + c * d.stride + k0, (FT)u0[c], (FT)u1[c]);
             store2<FT>(Fprev + c * d.stride + k0, (FT)d.body[c], (FT)d.body[c]);
         }
     }
@@ -343,7 +342,8 @@ __device__ __forceinline__ void fd_wall_cell(const LatticeDesc& d, const T* __re
 // give the wall velocity); OT = double for the host export, the compute type otherwise.
 template <class T, class OT>
 __global__ void k_velocity(LatticeDesc d, const T* __restrict__ f, const T* __restrict__ wall,
-                           const typename Store<T>::F* __restrict__ F, OT* __restrict__ u, int64_t ustride) {
+                           const typename Store<T>::F* __restrict__ F, OT* __restrict__ u, int64_t cstride,
+                           int64_t kstride) {
     using C = typename Store<T>::C;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
@@ -359,7 +359,8 @@ __global__ void k_velocity(LatticeDesc d, const T* __restrict__ f, const T* __re
         C Fc[3] = {(C)F[k], (C)F[d.stride + k], (C)F[2 * d.stride + k]};
         velocity_with_force(fc, Fc, uc);
     }
-    for (int a = 0; a < 3; ++a) u[a * ustride + k] = (OT)uc[a];
+    for (int a = 0; a < 3; ++a) u[a * cstride + k * kstride] = (OT)uc[a];
+    if (kstride == 4) u[k * 4 + 3] = OT(0);
 }
 
 // iniCellAtEquilibrium, src/core/cell.hh:124-132
@@ -513,7 +514,7 @@ void velocity_field_t(const Lattice& L, cudaStream_t s) {
     using FT = typename Store<T>::F;
     const int bx = row_block(L.d);
     k_velocity<T, FT><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall, (const FT*)L.F[L.fe],
-                                                        (FT*)L.u, L.d.stride);
+                                                        (FT*)L.u, 1, 4);
 }
 
 template <class T>
@@ -521,7 +522,7 @@ void velocity_export_t(const Lattice& L, double* u, cudaStream_t s) {
     using FT = typename Store<T>::F;
     const int bx = row_block(L.d);
     k_velocity<T, double><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall,
-                                                            (const FT*)L.F[L.fe], u, L.d.n);
+                                                            (const FT*)L.F[L.fe], u, L.d.n, 1);
 }
 
 template <class T>
