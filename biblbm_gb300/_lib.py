@@ -38,7 +38,7 @@ class IbParams(C.Structure):
 
 class Tuning(C.Structure):
     _fields_ = [("collide_kernel", C.c_int32), ("tile_cells", C.c_int32), ("stages", C.c_int32),
-                ("reserved", C.c_int32 * 5)]
+                ("membrane_block", C.c_int32), ("reserved", C.c_int32 * 4)]
 
 
 class BatchTuning(C.Structure):

@@ -203,13 +203,14 @@ class Lattice:
     def check_health(self):
         self.ctx.check(self.ctx.lib.bib_check_health(self.ctx.h, self.h))
 
-    def set_tuning(self, kernel="auto", tile_cells=0, stages=0):
-        """Collide-and-stream kernel ("auto", "rows" or "staged"), staged tile size in cells and
-        pipeline depth (0: automatic)."""
+    def set_tuning(self, kernel="auto", tile_cells=0, stages=0, membrane_block=0):
+        """Collide-and-stream kernel ("auto", "rows" or "staged"), staged tile size in cells,
+        pipeline depth and membrane-kernel block size (0: automatic / default)."""
         t = Tuning()
         t.collide_kernel = KERNEL[kernel]
         t.tile_cells = int(tile_cells)
         t.stages = int(stages)
+        t.membrane_block = int(membrane_block)
         self.ctx.check(self.ctx.lib.bib_lattice_set_tuning(self.ctx.h, self.h, C.byref(t)))
 
 

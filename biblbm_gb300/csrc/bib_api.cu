@@ -1032,7 +1032,8 @@ bib_status bib_batch_set_tuning(bib_ctx* c, int32_t b, const bib_batch_tuning* t
     Batch* B = get_batch(c, b);
     if (!B || !t) return fail(c, BIB_EINVAL, "invalid batch handle or tuning");
     if (t->tile_cells < 0 || t->stages < 0 || t->stages == 1 || t->stages > 4 ||
-        (t->membrane_block != 0 && t->membrane_block != 64 && t->membrane_block != 128 && t->membrane_block != 256))
+        (t->membrane_block != 0 && t->membrane_block != 64 && t->membrane_block != 128 && t->membrane_block != 256 &&
+         t->membrane_block != 512))
         return fail(c, BIB_EINVAL, "invalid batch tuning values");
     if (!collide_batch_fits(B->storage, B->collision, t->stages))
         return fail(c, BIB_EUNSUPPORTED, "%d stages do not fit the shared memory of a CTA", t->stages);
@@ -1080,8 +1081,8 @@ bib_status bib_batch_autotune(bib_ctx* c, int32_t b, int32_t steps, bib_batch_tu
         }
     double best_mb = 1e300;
     int best_block = 256;
-    const int blocks[3] = {64, 128, 256};
-    for (int k = 0; k < 3; ++k) {
+    const int blocks[4] = {64, 128, 256, 512};
+    for (int k = 0; k < 4; ++k) {
         bib_batch_tuning t = best;
         t.membrane_block = blocks[k];
         bib_status st = bib_batch_set_tuning(c, b, &t);
@@ -1118,8 +1119,10 @@ bib_status bib_spread_forces_noalloc(bib_ctx* c, int32_t h, const double* pos, c
 bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     Lattice* L = get_lattice(c, h);
     if (!L || !t) return fail(c, BIB_EINVAL, "invalid lattice handle or tuning");
+    const int mb = t->membrane_block;
     if (t->collide_kernel < BIB_KERNEL_AUTO || t->collide_kernel > BIB_KERNEL_STAGED || t->tile_cells < 0 ||
-        t->stages < 0 || t->stages == 1 || t->stages > 4)
+        t->stages < 0 || t->stages == 1 || t->stages > 4 ||
+        (mb != 0 && mb != 64 && mb != 128 && mb != 256 && mb != 512))
         return fail(c, BIB_EINVAL, "invalid tuning values");
     Lattice probe = {};
     probe.d = L->d;
@@ -1132,6 +1135,7 @@ bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     L->collide_kernel = t->collide_kernel;
     L->tile_cells = t->tile_cells;
     L->stages = t->stages;
+    L->membrane_block = mb ? mb : 256;
     return BIB_OK;
 }
 

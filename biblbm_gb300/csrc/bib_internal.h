@@ -193,6 +193,7 @@ struct Lattice {
     int collide_kernel = BIB_KERNEL_AUTO;
     int tile_cells = 0;
     int stages = 0;           // staged kernel pipeline depth (0 = automatic)
+    int membrane_block = 256; // threads per particle of the membrane kernel
     int* wait_err = nullptr;  // device word set by a bounded device wait that gave up
     uint64_t version = 0;     // bumped whenever the particle buffers are (re)allocated
     int handle = -1;

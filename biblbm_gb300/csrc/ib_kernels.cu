@@ -659,7 +659,7 @@ __device__ __forceinline__ T block_sum(T v, T* red) {
 // One CTA per particle: vertex forces at X_n (ParticleBase3D::reset_forces +
 // compute_forces), accumulated in shared memory.
 template <class M, bool BATCH>
-__global__ void __launch_bounds__(256) k_membrane(const ParticleDev* __restrict__ parts, IbView v1,
+__global__ void __launch_bounds__(512) k_membrane(const ParticleDev* __restrict__ parts, IbView v1,
                                                    const IbView* __restrict__ views) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     M* sf = reinterpret_cast<M*>(smem_raw);
@@ -966,7 +966,7 @@ void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
             k_membrane_gather<float><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats);
         return;
     }
-    membrane_any<false>(L.storage, L.pdev, np, single_view(L, -1), nullptr, L.membrane_smem, 256, s);
+    membrane_any<false>(L.storage, L.pdev, np, single_view(L, -1), nullptr, L.membrane_smem, L.membrane_block, s);
 }
 
 void launch_particle_update(const Lattice& L, cudaStream_t s) {

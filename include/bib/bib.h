@@ -131,7 +131,8 @@ typedef struct {
     int32_t collide_kernel; /* BIB_KERNEL_*: AUTO takes the shared-memory staged kernel where the x-row fits */
     int32_t tile_cells;     /* staged kernel: cells per tile (whole x-rows); 0 = 512 (256 for FP64) */
     int32_t stages;         /* staged kernel: pipeline depth 2..4; 0 = the deepest that keeps the CTAs resident */
-    int32_t reserved[5];
+    int32_t membrane_block; /* threads per particle of the membrane kernel: 64 .. 512 (power of two), 0 = 256 */
+    int32_t reserved[4];
 } bib_tuning;
 
 /* ---- context (src/coProcessors/coProcessor3D.h:57-115 lifetime) ---- */
@@ -209,7 +210,7 @@ bib_status bib_lattice_set_tuning(bib_ctx* ctx, int32_t h, const bib_tuning* t);
 typedef struct {
     int32_t tile_cells;     /* staged collide-and-stream tile (cells, whole x-rows); 0 = default */
     int32_t stages;         /* its pipeline depth 2..4; 0 = automatic */
-    int32_t membrane_block; /* threads per particle of the membrane kernel: 64, 128 or 256 (0 = 256) */
+    int32_t membrane_block; /* threads per particle of the membrane kernel: 64, 128, 256 or 512 (0 = 256) */
     int32_t reserved[5];
 } bib_batch_tuning;
 bib_status bib_batch_create(bib_ctx* ctx, const int32_t* handles, int32_t n, int32_t* batch);

@@ -95,9 +95,9 @@ def test_batch_autotune_keeps_the_physics(ctx):
     grouped = make_set(ctx, "f32")
     batch = bib.Batch(ctx, [g[0] for g in grouped])
     chosen = batch.autotune(steps=2)
-    assert chosen["stages"] in (2, 3, 4) and chosen["membrane_block"] in (64, 128, 256)
-    # 6 tile x stage candidates + 3 block sizes, each one untimed + 2 timed steps
-    steps = (6 + 3) * 3
+    assert chosen["stages"] in (2, 3, 4) and chosen["membrane_block"] in (64, 128, 256, 512)
+    # 6 tile x stage candidates + 4 block sizes, each one untimed + 2 timed steps
+    steps = (6 + 4) * 3
     batch.step(4)
     for lat, fsi, pid in solo:
         fsi.step(steps + 4)
