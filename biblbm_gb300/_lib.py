@@ -88,6 +88,7 @@ SIGNATURES = {
     "bib_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),
     "bib_check_health": (C.c_int32, [_vp, C.c_int32]),
     "bib_lattice_set_tuning": (C.c_int32, [_vp, C.c_int32, C.POINTER(Tuning)]),
+    "bib_lattice_set_cell_types": (C.c_int32, [_vp, C.c_int32, _vp]),
     "bib_spread_forces_noalloc": (C.c_int32, [_vp, C.c_int32, _vp, _vp, C.c_int64, _vp]),
     "bib_batch_create": (C.c_int32, [_vp, _i32p, C.c_int32, _i32p]),
     "bib_batch_destroy": (C.c_int32, [_vp, C.c_int32]),

@@ -203,6 +203,14 @@ class Lattice:
     def check_health(self):
         self.ctx.check(self.ctx.lib.bib_check_health(self.ctx.h, self.h))
 
+    def set_cell_types(self, types):
+        """defineDynamics per cell: 0 the lattice's dynamics, 1 BounceBack, 2 NoDynamics; None resets."""
+        if types is None:
+            self.ctx.check(self.ctx.lib.bib_lattice_set_cell_types(self.ctx.h, self.h, None))
+            return
+        t = np.ascontiguousarray(np.broadcast_to(types, self.shape), dtype=np.uint8)
+        self.ctx.check(self.ctx.lib.bib_lattice_set_cell_types(self.ctx.h, self.h, t.ctypes.data))
+
     def set_tuning(self, kernel="auto", tile_cells=0, stages=0, membrane_block=0):
         """Collide-and-stream kernel ("auto", "rows" or "staged"), staged tile size in cells,
         pipeline depth and membrane-kernel block size (0: automatic / default)."""

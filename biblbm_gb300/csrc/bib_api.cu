@@ -711,6 +711,7 @@ bib_status build_batch(bib_ctx* c, Batch& B) {
             w.Fprev = L.F[fe];
             w.u = L.u;
             w.phase = L.phase;
+            w.celltype = L.celltype;
             w.tile0 = B.ntiles;
             cv[p].push_back(w);
         }
@@ -933,6 +934,7 @@ void bib_destroy(bib_ctx* c) {
         cudaFree(Lp->u);
         cudaFree(Lp->wall);
         cudaFree(Lp->phase);
+        cudaFree(Lp->celltype);
     }
     for (auto& S : c->shapes) {
         cudaFree(S->dev.rest);
@@ -1113,6 +1115,27 @@ bib_status bib_spread_forces_noalloc(bib_ctx* c, int32_t h, const double* pos, c
     std::string msg;
     const bib_status st = spread_noalloc(*L, c->device, c->stream, pos, force, nvert, field, msg);
     if (st != BIB_OK) return fail(c, st, "%s", msg.c_str());
+    return BIB_OK;
+}
+
+bib_status bib_lattice_set_cell_types(bib_ctx* c, int32_t h, const uint8_t* types) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (!types) {
+        cudaFree(L->celltype);
+        L->celltype = nullptr;
+        L->d.has_types = 0;
+    } else {
+        for (int64_t k = 0; k < L->d.n; ++k)
+            if (types[k] > BIB_CELL_NO_DYNAMICS) return fail(c, BIB_EINVAL, "cell type %d at cell %lld", (int)types[k], (long long)k);
+        if (!L->celltype) BIB_CUDA(c, cudaMalloc((void**)&L->celltype, L->d.n));
+        BIB_CUDA(c, cudaMemcpy(L->celltype, types, L->d.n, cudaMemcpyHostToDevice));
+        L->d.has_types = 1;
+    }
+    drop_graphs(c, h);
+    for (auto& B : c->batches)  // batch tables hold the lattice description
+        if (B) B->free_tables();
     return BIB_OK;
 }
 

@@ -24,6 +24,7 @@ struct LatticeDesc {
     int fd_walls;     // finite-difference velocity walls on the y = 0 and y = ny-1 planes
     int collision;
     int use_phase;
+    int has_types;    // per-cell dynamics (celltype) present
     double omega, omega_inner, trt_magic;
     double omega_c0, omega_c1;  // omega for phase 0 and 1: w0*w1/(c*w0 + (1-c)*w1)
     double inv_n[3];            // 1/nx, 1/ny, 1/nz (Arithmetic1D's Linv, Periodicity.h:73-78)
@@ -122,6 +123,7 @@ struct CollideView {
     void* Fprev;            // force of the incoming state (reset to the body force)
     void* u;                // velocity output
     const uint8_t* phase;
+    const uint8_t* celltype;
     int64_t tile0;          // first global tile of this lattice
     int64_t ntiles;
     int R, Ct, tiles_y;     // rows per tile, cells per tile, tiles per z-plane
@@ -168,6 +170,7 @@ struct Lattice {
     bool target_clean = false;        // F[1-fe] holds the body force, ready to receive spreading
     void* u = nullptr;                // velocity field, (ux, uy, uz, 0) per cell (double for F64 storage, float otherwise)
     uint8_t* phase = nullptr;
+    uint8_t* celltype = nullptr;      // BIB_CELL_* per cell, or nullptr: every cell has the lattice's dynamics
     // immersed boundary
     std::vector<ParticleHost> parts;
     int nvert = 0;

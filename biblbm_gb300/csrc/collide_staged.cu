@@ -290,8 +290,8 @@ template <class T, bool COUPLED, int COLL>
 __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, const unsigned char* st,
                                              const CollideParams<typename Store<T>::C>& cp, T* __restrict__ fout,
                                              typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
-                                             const uint8_t* __restrict__ phase, const TileCell& cell, uint64_t* empty_s,
-                                             int lane) {
+                                             const uint8_t* __restrict__ phase, const uint8_t* __restrict__ celltype,
+                                             const TileCell& cell, uint64_t* empty_s, int lane) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
     using L = StageLayout<T, COUPLED, COLL>;
@@ -337,6 +337,22 @@ __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedG
     if (lane == 0) mbar_arrive(empty_s);
     if (!active) return;
     const int64_t k = t.row0 + o0;
+    const int ctype = d.has_types ? celltype[k] : BIB_CELL_FLUID;
+    if (ctype != BIB_CELL_FLUID) {  // BounceBack / NoDynamics node: no collision, zero velocity
+        if (COUPLED) {
+            store_u<FT>(u_out, k, FT(0), FT(0), FT(0));
+#pragma unroll
+            for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
+        }
+        if (ctype == BIB_CELL_BOUNCE_BACK) bounce_back_cell(f);
+        T* o = fout + k;
+#pragma unroll
+        for (int i = 0; i < Q; ++i) {
+            Staged<T>::put(o, f[i]);
+            o += d.stride;
+        }
+        return;
+    }
     if (COLL == BIB_COLLISION_BGK_GUO_VOF && d.use_phase && phase[k]) om = cp.om1;
     if (COUPLED) {
         staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, Fp, fd ? nullptr : u);
@@ -377,7 +393,7 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
     LatticeDesc d, StagedGeom g, CollideParams<typename Store<T>::C> cp, const T* __restrict__ fin,
     T* __restrict__ fout, const T* __restrict__ wall, const typename Store<T>::F* __restrict__ Fcol,
     typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
-    const uint8_t* __restrict__ phase, int* __restrict__ wait_err) {
+    const uint8_t* __restrict__ phase, const uint8_t* __restrict__ celltype, int* __restrict__ wait_err) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
     using L = StageLayout<T, COUPLED, COLL>;
@@ -435,8 +451,8 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
             if (lane == 0) atomicExch(wait_err, 1);
             return;
         }
-        consume_tile<T, COUPLED, COLL>(d, g, tile, stages + s * L::BYTES, cp, fout, Fprev, u_out, phase, cell, &empty[s],
-                                        lane);
+        consume_tile<T, COUPLED, COLL>(d, g, tile, stages + s * L::BYTES, cp, fout, Fprev, u_out, phase, celltype, cell,
+                                        &empty[s], lane);
     }
 }
 
@@ -525,7 +541,8 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
         }
         consume_tile<T, true, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES,
                                     *reinterpret_cast<const CollideParams<C>*>(V.cp), static_cast<T*>(V.fout),
-                                    static_cast<FT*>(V.Fprev), static_cast<FT*>(V.u), V.phase, cell, &empty[s], lane);
+                                    static_cast<FT*>(V.Fprev), static_cast<FT*>(V.u), V.phase, V.celltype, cell,
+                                    &empty[s], lane);
     }
 }
 
@@ -634,7 +651,7 @@ bool staged_inst(const Lattice& L, int target, cudaStream_t s) {
     FT* Fprev = COUPLED ? (FT*)L.F[L.fe] : nullptr;
     kern<<<(unsigned)grid, LY::THREADS, smem, s>>>(d, g, collide_params<C>(d, L.storage), fin, fout,
                                                        (const T*)L.wall, Fcol, Fprev, COUPLED ? (FT*)L.u : nullptr,
-                                                       L.phase, L.wait_err);
+                                                       L.phase, L.celltype, L.wait_err);
     return true;
 }
 

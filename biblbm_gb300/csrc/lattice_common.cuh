@@ -49,6 +49,17 @@ __device__ __forceinline__ void store_u<double>(double* u, int64_t k, double a, 
     q[1] = make_double2(c, 0.0);
 }
 
+// BounceBack::collide (core/dynamics.hh:763-770): each population swaps with its opposite.
+template <class C>
+__device__ __forceinline__ void bounce_back_cell(C* f) {
+#pragma unroll
+    for (int i = 1; i <= 9; ++i) {
+        const C t = f[i];
+        f[i] = f[i + 9];
+        f[i + 9] = t;
+    }
+}
+
 // Row (y, z) lies next to a wall or is a finite-difference wall row: its gather needs the
 // per-population face tests; every other row streams from its 18 neighbours unchanged.
 __device__ __forceinline__ bool row_special(const LatticeDesc& d, int y, int z) {

@@ -57,7 +57,8 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
                                                          const typename Store<T>::F* __restrict__ Fcol,
                                                          typename Store<T>::F* __restrict__ Fprev,
                                                          typename Store<T>::F* __restrict__ u_out,
-                                                         const uint8_t* __restrict__ phase, int coll) {
+                                                         const uint8_t* __restrict__ phase,
+                                                         const uint8_t* __restrict__ celltype, int coll) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
@@ -66,6 +67,17 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
     C f[Q];
     gather<T>(d, fin, wall, x, y, z, k, f);
+    const int ctype = d.has_types ? celltype[k] : BIB_CELL_FLUID;
+    if (ctype != BIB_CELL_FLUID) {  // BounceBack / NoDynamics node: no collision, zero velocity
+        if (COUPLED) {
+            store_u<FT>(u_out, k, FT(0), FT(0), FT(0));
+            for (int c = 0; c < 3; ++c) Fprev[c * d.stride + k] = (FT)d.body[c];
+        }
+        if (ctype == BIB_CELL_BOUNCE_BACK) bounce_back_cell(f);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) Store<T>::store(fout + i * d.stride + k, f[i], d.scale);
+        return;
+    }
     if (COUPLED) {
         // computeVelocity of the current state (externalForceDynamics.hh:59-74; the wall
         // nodes give their imposed velocity, boundaryDynamics.hh:316-322), with the force of
@@ -115,7 +127,8 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
                                                               const typename Store<T>::F* __restrict__ Fcol,
                                                               typename Store<T>::F* __restrict__ Fprev,
                                                               typename Store<T>::F* __restrict__ u_out,
-                                                              const uint8_t* __restrict__ phase, int coll) {
+                                                              const uint8_t* __restrict__ phase,
+                                                              const uint8_t* __restrict__ celltype, int coll) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
     const unsigned FULL = 0xffffffffu;
@@ -210,6 +223,11 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
         }
     }
     if (!active) return;
+    int ct0 = BIB_CELL_FLUID, ct1 = BIB_CELL_FLUID;
+    if (d.has_types) {
+        ct0 = celltype[k0];
+        ct1 = celltype[k0 + 1];
+    }
     if (COUPLED) {
         C u0[3], u1[3];
         if (wallrow) {
@@ -220,6 +238,8 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
             velocity_with_force(f0, Fa, u0);
             velocity_with_force(f1, Fb, u1);
         }
+        if (ct0 != BIB_CELL_FLUID) u0[0] = u0[1] = u0[2] = C(0);
+        if (ct1 != BIB_CELL_FLUID) u1[0] = u1[1] = u1[2] = C(0);
         store_u<FT>(u_out, k0, (FT)u0[0], (FT)u0[1], (FT)u0[2]);
         store_u<FT>(u_out, k0 + 1, (FT)u1[0], (FT)u1[1], (FT)u1[2]);
         for (int c = 0; c < 3; ++c) {
@@ -227,23 +247,26 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
         }
     }
     C Fa[3] = {(C)fca[0], (C)fca[1], (C)fca[2]}, Fb[3] = {(C)fcb[0], (C)fcb[1], (C)fcb[2]};
+    C om0 = (C)d.omega, om1 = (C)d.omega, omm = C(0);
     if (coll == BIB_COLLISION_BGK_GUO_VOF) {
-        C om0 = (C)d.omega_c0, om1 = (C)d.omega_c0;
+        om0 = om1 = (C)d.omega_c0;
         if (d.use_phase) {
             if (phase[k0]) om0 = (C)d.omega_c1;
             if (phase[k0 + 1]) om1 = (C)d.omega_c1;
         }
-        collide<C, BIB_COLLISION_BGK_GUO_VOF>(f0, Fa, om0, C(0));
-        collide<C, BIB_COLLISION_BGK_GUO_VOF>(f1, Fb, om1, C(0));
-    } else if (coll == BIB_COLLISION_BGK) {
-        collide<C, BIB_COLLISION_BGK>(f0, Fa, (C)d.omega, C(0));
-        collide<C, BIB_COLLISION_BGK>(f1, Fb, (C)d.omega, C(0));
-    } else {
-        const C om = (C)d.omega;
-        const C omm = C(1) / ((C)d.trt_magic / (C(1) / om - C(0.5)) + C(0.5));
-        collide<C, BIB_COLLISION_TRT>(f0, Fa, om, omm);
-        collide<C, BIB_COLLISION_TRT>(f1, Fb, om, omm);
+    } else if (coll == BIB_COLLISION_TRT) {
+        omm = C(1) / ((C)d.trt_magic / (C(1) / om0 - C(0.5)) + C(0.5));
     }
+    auto collide_one = [&](C* f, const C* Fx, C om) {
+        if (coll == BIB_COLLISION_BGK_GUO_VOF) collide<C, BIB_COLLISION_BGK_GUO_VOF>(f, Fx, om, C(0));
+        else if (coll == BIB_COLLISION_BGK) collide<C, BIB_COLLISION_BGK>(f, Fx, om, C(0));
+        else collide<C, BIB_COLLISION_TRT>(f, Fx, om, omm);
+    };
+    // BounceBack nodes swap their incoming populations, NoDynamics nodes keep them
+    if (ct0 == BIB_CELL_FLUID) collide_one(f0, Fa, om0);
+    else if (ct0 == BIB_CELL_BOUNCE_BACK) bounce_back_cell(f0);
+    if (ct1 == BIB_CELL_FLUID) collide_one(f1, Fb, om1);
+    else if (ct1 == BIB_CELL_BOUNCE_BACK) bounce_back_cell(f1);
 #pragma unroll
     for (int i = 0; i < Q; ++i) Pair<T>::store(fout + i * d.stride + k0, f0[i], f1[i], d.scale);
 }
@@ -343,14 +366,16 @@ __device__ __forceinline__ void fd_wall_cell(const LatticeDesc& d, const T* __re
 template <class T, class OT>
 __global__ void k_velocity(LatticeDesc d, const T* __restrict__ f, const T* __restrict__ wall,
                            const typename Store<T>::F* __restrict__ F, OT* __restrict__ u, int64_t cstride,
-                           int64_t kstride) {
+                           int64_t kstride, const uint8_t* __restrict__ celltype) {
     using C = typename Store<T>::C;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= d.nx) return;
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
     C uc[3];
-    if (fd_wall_node(d, y)) {
+    if (d.has_types && celltype[k] != BIB_CELL_FLUID) {  // BounceBack / NoDynamics: zero velocity
+        uc[0] = uc[1] = uc[2] = C(0);
+    } else if (fd_wall_node(d, y)) {
         const int side = y == 0 ? 0 : 1;
         for (int a = 0; a < 3; ++a) uc[a] = (C)d.wall_u[side][a];
     } else {
@@ -468,10 +493,10 @@ void collide_stream_t(const Lattice& L, bool coupled, cudaStream_t s) {
         T* fout = (T*)L.f[1 - L.cur];
         if (coupled)
             k_collide_stream_rows<T, true><<<grid, block, 0, s>>>(L.d, fin, fout, (const T*)L.wall, (const FT*)L.F[1 - L.fe],
-                                                                  (FT*)L.F[L.fe], (FT*)L.u, L.phase, L.d.collision);
+                                                                  (FT*)L.F[L.fe], (FT*)L.u, L.phase, L.celltype, L.d.collision);
         else
             k_collide_stream_rows<T, false><<<grid, block, 0, s>>>(L.d, fin, fout, (const T*)L.wall, (const FT*)L.F[L.fe],
-                                                                   nullptr, nullptr, L.phase, L.d.collision);
+                                                                   nullptr, nullptr, L.phase, L.celltype, L.d.collision);
         return;
     }
     const int bx = row_block(L.d);
@@ -480,10 +505,10 @@ void collide_stream_t(const Lattice& L, bool coupled, cudaStream_t s) {
     const T* wall = (const T*)L.wall;
     if (coupled) {
         k_collide_stream<T, true><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, fin, fout, wall, (const FT*)L.F[1 - L.fe],
-                                                                    (FT*)L.F[L.fe], (FT*)L.u, L.phase, L.d.collision);
+                                                                    (FT*)L.F[L.fe], (FT*)L.u, L.phase, L.celltype, L.d.collision);
     } else {
         k_collide_stream<T, false><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, fin, fout, wall, (const FT*)L.F[L.fe], nullptr,
-                                                                     nullptr, L.phase, L.d.collision);
+                                                                     nullptr, L.phase, L.celltype, L.d.collision);
     }
 }
 
@@ -514,7 +539,7 @@ void velocity_field_t(const Lattice& L, cudaStream_t s) {
     using FT = typename Store<T>::F;
     const int bx = row_block(L.d);
     k_velocity<T, FT><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall, (const FT*)L.F[L.fe],
-                                                        (FT*)L.u, 1, 4);
+                                                        (FT*)L.u, 1, 4, L.celltype);
 }
 
 template <class T>
@@ -522,7 +547,7 @@ void velocity_export_t(const Lattice& L, double* u, cudaStream_t s) {
     using FT = typename Store<T>::F;
     const int bx = row_block(L.d);
     k_velocity<T, double><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall,
-                                                            (const FT*)L.F[L.fe], u, L.d.n, 1);
+                                                            (const FT*)L.F[L.fe], u, L.d.n, 1, L.celltype);
 }
 
 template <class T>

@@ -86,6 +86,9 @@ enum { BIB_SPREAD_ATOMIC = 0, BIB_SPREAD_DETERMINISTIC = 1 };
  *                  (19 f-bar + 4 external scalars), blockLattice3D.hh:671-689
  *  COPROCESSOR_F64 CoProcessor3D::send order: x-major, z fastest, 19 f-bar per cell
  *                  (coProcessor3D.h:80-91) */
+/* per-cell dynamics, defineDynamics(lattice, domain, new BounceBack / NoDynamics), core/dynamics.h:559-600 */
+enum { BIB_CELL_FLUID = 0, BIB_CELL_BOUNCE_BACK = 1, BIB_CELL_NO_DYNAMICS = 2 };
+
 /* collide-and-stream kernel choice (no reference counterpart: a GPU tuning knob) */
 enum { BIB_KERNEL_AUTO = 0, BIB_KERNEL_ROWS = 1, BIB_KERNEL_STAGED = 2 };
 
@@ -147,6 +150,11 @@ int32_t bib_abi_version(void);
 /* CoProcessor3D::addDomain(nx, ny, nz, omega, handle), coProcessor3D.h:69-74 */
 bib_status bib_lattice_add_domain(bib_ctx* ctx, int64_t nx, int64_t ny, int64_t nz, const bib_lattice_params* p,
                                   int32_t* handle);
+/* defineDynamics with BounceBack / NoDynamics per cell (rbc_in_pipe.cpp:307-310): types is nz x ny x nx
+ * BIB_CELL_* values (x fastest); BounceBack nodes swap each population with its opposite instead of
+ * colliding, NoDynamics nodes keep theirs; both report zero velocity.  NULL restores the lattice's
+ * dynamics everywhere. */
+bib_status bib_lattice_set_cell_types(bib_ctx* ctx, int32_t h, const uint8_t* types);
 /* CoProcessor3D::send, coProcessor3D.h:75-91: whole-domain populations from the host in one of
  * the BIB_LAYOUT_* orders (the PALABOS layout also sets the force and phase scalars). */
 bib_status bib_lattice_send(bib_ctx* ctx, int32_t h, const void* buf, size_t bytes, int32_t layout);

@@ -305,14 +305,29 @@ void orc_collide_stream(const orc_lattice* L, double* f, double* ftmp, const dou
                 double fsw[Q];
                 const int edge = (L->periodic[0] && (x == 0 || x == nx - 1)) || (L->periodic[1] && (y == 0 || y == ny - 1)) ||
                                  (L->periodic[2] && (z == 0 || z == nz - 1));
-                if (L->envelope_swap && edge) {
-                    orc_lattice Ls = *L;
-                    Ls.omega = L->omega_inner;
-                    Ls.omega_inner = L->omega;
+                const int ct = L->celltype ? L->celltype[k] : ORC_CELL_FLUID;
+                if (ct == ORC_CELL_BOUNCE_BACK) {
+                    /* BounceBack::collide swaps each population with its opposite,
+                     * core/dynamics.hh:763-770 */
+                    for (int i = 1; i <= Q / 2; ++i) {
+                        const double t = fc[i];
+                        fc[i] = fc[i + Q / 2];
+                        fc[i + Q / 2] = t;
+                    }
                     for (int i = 0; i < Q; ++i) fsw[i] = fc[i];
-                    orc_collide_cell(&Ls, fsw, Fc, phase ? phase[k] : 0.0);
+                } else if (ct == ORC_CELL_NO_DYNAMICS) {
+                    /* NoDynamics::collide leaves the populations unchanged */
+                    for (int i = 0; i < Q; ++i) fsw[i] = fc[i];
+                } else {
+                    if (L->envelope_swap && edge) {
+                        orc_lattice Ls = *L;
+                        Ls.omega = L->omega_inner;
+                        Ls.omega_inner = L->omega;
+                        for (int i = 0; i < Q; ++i) fsw[i] = fc[i];
+                        orc_collide_cell(&Ls, fsw, Fc, phase ? phase[k] : 0.0);
+                    }
+                    orc_collide_cell(L, fc, Fc, phase ? phase[k] : 0.0);
                 }
-                orc_collide_cell(L, fc, Fc, phase ? phase[k] : 0.0);
                 for (int i = 0; i < Q; ++i) {
                     int64_t xd = x + CX[i], yd = y + CY[i], zd = z + CZ[i];
                     const int crosses = (L->periodic[0] && (xd < 0 || xd >= nx)) || (L->periodic[1] && (yd < 0 || yd >= ny)) ||
@@ -353,7 +368,10 @@ void orc_compute_velocity(const orc_lattice* L, const double* f, const double* F
             for (int64_t x = 0; x < nx; ++x) {
                 const int64_t k = cell_index(L, x, y, z);
                 double uc[3];
-                if (is_fd_wall(L, y, z)) {
+                if (L->celltype && L->celltype[k] != ORC_CELL_FLUID) {
+                    /* BounceBack / NoDynamics::computeVelocity yield 0, core/dynamics.hh:796-801 */
+                    uc[0] = uc[1] = uc[2] = 0.0;
+                } else if (is_fd_wall(L, y, z)) {
                     /* StoreVelocityDynamics::computeVelocity returns the imposed velocity,
                      * boundaryCondition/boundaryDynamics.hh:316-322 */
                     const double* uw = fd_wall_velocity(L, y, z);

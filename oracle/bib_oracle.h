@@ -51,7 +51,10 @@ typedef struct {
     double trt_magic;
     double wall_u[4][3];        /* velocity of the y-, y+, z-, z+ walls */
     int32_t envelope_swap;      /* reproduce the reference's periodic-envelope omega swap (see .c) */
+    const uint8_t* celltype;    /* NULL or per cell: 0 the lattice's dynamics, 1 BounceBack, 2 NoDynamics */
 } orc_lattice;
+
+enum { ORC_CELL_FLUID = 0, ORC_CELL_BOUNCE_BACK = 1, ORC_CELL_NO_DYNAMICS = 2 };
 
 /* ---- lattice ---- */
 void orc_collide_cell(const orc_lattice* L, double* f19, const double* F3, double phase);

@@ -149,6 +149,18 @@ static int run_lbm(const Bundle& in, const char* out) {
     Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(omega, omega_in));
     lattice.toggleInternalStatistics(false);
     std::auto_ptr<OnLatticeBoundaryCondition3D<T, DESCRIPTOR> > bc(createInterpBoundaryCondition3D<T, DESCRIPTOR>());
+    if (recio::has(in, "celltype")) {
+        // per-cell dynamics as a driver sets them with defineDynamics (rbc_in_pipe.cpp:307-310):
+        // 1 BounceBack, 2 NoDynamics
+        const recio::Array& ct = recio::need(in, "celltype");
+        for (plint z = 0; z < nz; ++z)
+            for (plint y = 0; y < ny; ++y)
+                for (plint x = 0; x < nx; ++x) {
+                    const long long t = ct.i[lidx(x, y, z, nx, ny)];
+                    if (t == 1) defineDynamics(lattice, Box3D(x, x, y, y, z, z), new BounceBack<T, DESCRIPTOR>());
+                    else if (t == 2) defineDynamics(lattice, Box3D(x, x, y, y, z, z), new NoDynamics<T, DESCRIPTOR>());
+                }
+    }
     if (walls == 0) {
         lattice.periodicity().toggleAll(true);
         lattice.initialize();  // sets up the periodic envelope exchange before the state is loaded

@@ -31,6 +31,7 @@ class Lattice(C.Structure):
         ("omega", C.c_double), ("omega_inner", C.c_double), ("trt_magic", C.c_double),
         ("wall_u", (C.c_double * 3) * 4),
         ("envelope_swap", C.c_int32),
+        ("celltype", C.c_void_p),
     ]
 
 
@@ -108,9 +109,17 @@ def i64(a):
     return np.ascontiguousarray(a, dtype=np.int64)
 
 
+_celltypes_alive = []  # the oracle keeps a pointer to the cell-type array of a lattice
+
+
 def lattice(dims, periodic=(1, 1, 1), collision="bgk_guo_vof", omega=1.0, omega_inner=None, trt_magic=0.25,
-            wall_y="none", wall_z="none", wall_u=None, envelope_swap=False) -> Lattice:
+            wall_y="none", wall_z="none", wall_u=None, envelope_swap=False, celltype=None) -> Lattice:
+    """celltype: None or a (nz, ny, nx) array, 0 the lattice's dynamics, 1 BounceBack, 2 NoDynamics."""
     L = Lattice()
+    if celltype is not None:
+        ct = np.ascontiguousarray(celltype, dtype=np.uint8)
+        _celltypes_alive.append(ct)
+        L.celltype = ct.ctypes.data
     L.nx, L.ny, L.nz = (int(d) for d in dims)
     for k in range(3):
         L.periodic[k] = int(bool(periodic[k]))

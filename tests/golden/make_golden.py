@@ -146,6 +146,24 @@ def case_lbm_shear():
     save("lbm_shear", inp, out)
 
 
+def case_lbm_bounceback():
+    """Per-cell BounceBack and NoDynamics nodes (defineDynamics) in a periodic box, lambda = 1."""
+    rng = np.random.default_rng(103)
+    nx, ny, nz = 10, 8, 6
+    omega = 1 / 0.85
+    ct = np.zeros((nz, ny, nx), dtype=np.int64)
+    ct[1:4, 2:5, 3:6] = 1          # a solid block
+    ct[2, 0:3, 0] = 1              # solid cells on the periodic seam
+    ct[:, :, 8] = 2                # a NoDynamics slab
+    ct[4, 5, 8] = 1
+    inp = dict(dims=[nx, ny, nz], omega=[omega, omega], walls=0, steps=4,
+               fbar=random_state(rng, nx, ny, nz),
+               force=1e-3 * rng.uniform(-1, 1, (3, nz, ny, nx)),
+               phase=np.zeros((nz, ny, nx)), celltype=ct)
+    out = run("lbm", inp)
+    save("lbm_bounceback", inp, out)
+
+
 def case_interp():
     for dirac, dname in ((0, "roma"), (1, "peskin")):
         for per, pname in (((1, 1, 1), "ppp"), ((1, 0, 1), "pwp"), ((1, 0, 0), "pww")):
@@ -258,7 +276,7 @@ def case_ibm_rbc_periodic():
     save("ibm_rbc_periodic", inp, keep)
 
 
-CASES = [case_lbm_periodic, case_lbm_shear, case_interp, case_shape, case_forces, case_inertia,
+CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
          case_ibm_capsule_shear, case_ibm_rbc_periodic]
 
 if __name__ == "__main__":

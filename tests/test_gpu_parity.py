@@ -210,6 +210,58 @@ def test_coupled_steps_match_reference(ctx, name, kernel):
     assert rel(fsi.get_particle(pid)["inertia"], d["out_inertia"][-1]) < 1e-12
 
 
+# 10-cell rows: 80 bytes in FP64 fit the staged tile, 40 bytes in FP32 do not
+@pytest.mark.parametrize("kernel,storage,tol", [("staged", "f64", 1e-15), ("rows", "f64", 1e-15), ("rows", "f32", 1e-7)])
+def test_bounce_back_nodes_match_reference(ctx, kernel, storage, tol):
+    """BounceBack / NoDynamics nodes set per cell, against the reference's own run."""
+    d = golden("lbm_bounceback")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    om = d["in_omega"]
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=om[0], omega_inner=om[1], storage=storage)
+    lat.set_tuning(kernel)
+    lat.set_cell_types(d["in_celltype"])
+    lat.send(d["in_fbar"])
+    lat.set_external_force(d["in_force"])
+    lat.collide_and_stream(1)
+    assert np.abs(lat.receive() - d["out_fbar_1"]).max() < tol
+    lat.collide_and_stream(int(d["in_steps"]) - 1)
+    assert np.abs(lat.receive() - d["out_fbar_end"]).max() < tol
+    assert np.abs(lat.compute_velocity() - d["out_u_end"]).max() < 50 * tol
+
+
+def test_bounce_back_nodes_odd_rows_and_coupled_steps(ctx):
+    """Odd nx (per-cell kernel) against the oracle; coupled steps of the staged and the
+    row-vectorised kernels against each other, with solid and NoDynamics cells."""
+    rng = np.random.default_rng(23)
+    nx, ny, nz = 11, 9, 6
+    f0 = 1e-3 * rng.uniform(-1, 1, (19, nz, ny, nx))
+    F = 1e-4 * rng.uniform(-1, 1, (3, nz, ny, nx))
+    ct = (rng.uniform(size=(nz, ny, nx)) < 0.2).astype(np.uint8) + (rng.uniform(size=(nz, ny, nx)) < 0.05)
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 1), omega=1.2, wall_y="halfway_bb")
+    lat.set_cell_types(ct)
+    lat.send(f0)
+    lat.set_external_force(F)
+    lat.collide_and_stream(3)
+    L = O.lattice((nx, ny, nz), (1, 0, 1), "bgk_guo_vof", 1.2, 1.2, wall_y="halfway_bb", celltype=ct)
+    ref = O.collide_stream(L, f0, F, None, 3)
+    assert np.abs(lat.receive() - ref).max() < 1e-15
+    assert np.abs(lat.compute_velocity() - O.compute_velocity(L, ref, F)).max() < 1e-14
+    nx = 16
+    f0 = 1e-3 * rng.uniform(-1, 1, (19, nz, ny, nx))
+    ct = (rng.uniform(size=(nz, ny, nx)) < 0.2).astype(np.uint8) + (rng.uniform(size=(nz, ny, nx)) < 0.05)
+    out = {}
+    for kernel in ("rows", "staged"):
+        lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 1), omega=1.2, wall_y="halfway_bb", body_force=(1e-5, 0, 0))
+        lat.set_tuning(kernel)
+        lat.set_cell_types(ct)
+        lat.send(f0)
+        fsi = bib.ImmersedBoundaryDynamics3D(lat, bib.ParticleShapeLibrary(ctx))
+        fsi.step(4)
+        out[kernel] = (lat.receive(), lat.compute_velocity())
+    for a, b in zip(out["rows"], out["staged"]):
+        assert np.abs(a - b).max() < 1e-16
+
+
 def random_channel(nx, ny, nz, seed=11):
     rng = np.random.default_rng(seed)
     f0 = 1e-3 * rng.uniform(-1, 1, (19, nz, ny, nx))

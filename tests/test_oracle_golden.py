@@ -50,6 +50,20 @@ def test_periodic_collide_stream(swap):
         assert np.abs(f1 - d["out_fbar_1"])[0].max() == 0.0
 
 
+def test_bounce_back_and_no_dynamics_nodes():
+    """BounceBack (core/dynamics.hh:763-770) and NoDynamics nodes set per cell with
+    defineDynamics; velocity 0 on them (dynamics.hh:796-801)."""
+    d = golden("lbm_bounceback")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    om = d["in_omega"]
+    L = O.lattice((nx, ny, nz), (1, 1, 1), "bgk_guo_vof", om[0], om[1], celltype=d["in_celltype"])
+    f1 = O.collide_stream(L, d["in_fbar"], d["in_force"], d["in_phase"], 1)
+    assert np.array_equal(f1, d["out_fbar_1"])
+    f_end = O.collide_stream(L, d["in_fbar"], d["in_force"], d["in_phase"], int(d["in_steps"]))
+    assert np.array_equal(f_end, d["out_fbar_end"])
+    assert np.array_equal(O.compute_velocity(L, f_end, d["in_force"]), d["out_u_end"])
+
+
 def test_shear_fd_walls():
     d = golden("lbm_shear")
     L = shear_lattice(d)
