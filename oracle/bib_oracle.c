@@ -182,6 +182,116 @@ void orc_collide_cell(const orc_lattice* L, double* f, const double* F, double p
     }
 }
 
+/* ------------------------------------------------------------------ voxelization */
+/* RayTracer::tri_ray_intersect (fsi/RayTracer.hh:80-108) for the ray from (px, py, 0) along +z,
+ * Moller-Trumbore with Palabos' crossProduct / dot (geometricOperationTemplates.h:460-480). */
+static int tri_ray_z(const double* v0, const double* v1, const double* v2, double px, double py, double* dist) {
+    const double e1[3] = {v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]};
+    const double e2[3] = {v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]};
+    const double dir[3] = {0.0, 0.0, 1.0};
+    const double q[3] = {dir[1] * e2[2] - dir[2] * e2[1], dir[2] * e2[0] - dir[0] * e2[2], dir[0] * e2[1] - dir[1] * e2[0]};
+    double a = 0.0;
+    for (int d = 0; d < 3; ++d) a += e1[d] * q[d];
+    if (fabs(a) < DBL_EPSILON) return 0;
+    const double f = 1 / a;
+    const double sv[3] = {px - v0[0], py - v0[1], 0.0 - v0[2]};
+    double sq = 0.0;
+    for (int d = 0; d < 3; ++d) sq += sv[d] * q[d];
+    const double u = f * sq;
+    if (u < 0.0) return 0;
+    const double r[3] = {sv[1] * e1[2] - sv[2] * e1[1], sv[2] * e1[0] - sv[0] * e1[2], sv[0] * e1[1] - sv[1] * e1[0]};
+    double dr = 0.0;
+    for (int d = 0; d < 3; ++d) dr += dir[d] * r[d];
+    const double v = f * dr;
+    if (v < 0.0 || u + v > 1.0) return 0;
+    double er = 0.0;
+    for (int d = 0; d < 3; ++d) er += e2[d] * r[d];
+    *dist = f * er;
+    return 1;
+}
+
+static int cmp_double(const void* a, const void* b) {
+    const double x = *(const double*)a, y = *(const double*)b;
+    return x < y ? -1 : (x > y ? 1 : 0);
+}
+
+/* ImmersedBoundaryDynamics3D::voxelize + apply_voxelization
+ * (fsi/ImmersedBoundaryDynamics_voxelization.hh:17-30, 121-161): every triangle casts z-rays
+ * through the integer (x, y) points of its xy bounding box (RayTracer::find_intersections_z,
+ * RayTracer.hh:18-40); the intersection heights go into the ZBuffer column of (x, y) (periodic
+ * index and height wrap, ZBuffer.h put / Periodicity.h:83-93, heights in [-1/2, nz - 1/2)); each
+ * column is sorted and filled from below by parity, [ceil(z_prev), floor(z)] getting the current
+ * inside flag; above the last intersection the fill only happens when ceil(z_last) < nz - 1. */
+void orc_voxelize(const orc_lattice* L, int64_t nvt, const double* pos, int64_t ntt, const int64_t* tri, double* phase) {
+    (void)nvt;
+    const int64_t nx = L->nx, ny = L->ny, nz = L->nz, ncol = nx * ny;
+    int64_t* count = (int64_t*)calloc((size_t)ncol + 1, sizeof(int64_t));
+    /* two passes over the triangles: count, then fill */
+    double* zs = NULL;
+    int64_t* fillp = NULL;
+    for (int pass = 0; pass < 2; ++pass) {
+        for (int64_t t = 0; t < ntt; ++t) {
+            const double* v0 = pos + 3 * tri[3 * t];
+            const double* v1 = pos + 3 * tri[3 * t + 1];
+            const double* v2 = pos + 3 * tri[3 * t + 2];
+            const int64_t i0 = (int64_t)ceil(fmin(v0[0], fmin(v1[0], v2[0])));
+            const int64_t i1 = (int64_t)floor(fmax(v0[0], fmax(v1[0], v2[0])));
+            const int64_t j0 = (int64_t)ceil(fmin(v0[1], fmin(v1[1], v2[1])));
+            const int64_t j1 = (int64_t)floor(fmax(v0[1], fmax(v1[1], v2[1])));
+            for (int64_t i = i0; i <= i1; ++i)
+                for (int64_t j = j0; j <= j1; ++j) {
+                    double dist;
+                    if (!tri_ray_z(v0, v1, v2, (double)i, (double)j, &dist)) continue;
+                    int64_t cx = i, cy = j;
+                    if (L->periodic[0]) cx = ((cx % nx) + nx) % nx;
+                    else if (cx < 0 || cx >= nx) continue;
+                    if (L->periodic[1]) cy = ((cy % ny) + ny) % ny;
+                    else if (cy < 0 || cy >= ny) continue;
+                    /* Arithmetic1D::remap_pos with the periodic interval [-1/2, nz - 1/2),
+                     * Periodicity.h:83-87 (x0 = -0.5, as for the centre-of-mass remap) */
+                    if (L->periodic[2]) dist = dist - (double)nz * floor((dist - (-0.5)) * (1.0 / (double)nz));
+                    const int64_t c = cx * ny + cy;
+                    if (pass == 0) count[c + 1]++;
+                    else zs[fillp[c]++] = dist;
+                }
+        }
+        if (pass == 0) {
+            for (int64_t c = 0; c < ncol; ++c) count[c + 1] += count[c];
+            zs = (double*)malloc(sizeof(double) * (size_t)(count[ncol] > 0 ? count[ncol] : 1));
+            fillp = (int64_t*)malloc(sizeof(int64_t) * (size_t)ncol);
+            for (int64_t c = 0; c < ncol; ++c) fillp[c] = count[c];
+        }
+    }
+    for (int64_t cx = 0; cx < nx; ++cx)
+        for (int64_t cy = 0; cy < ny; ++cy) {
+            const int64_t c = cx * ny + cy;
+            double* col = zs + count[c];
+            const int64_t m = count[c + 1] - count[c];
+            qsort(col, (size_t)m, sizeof(double), cmp_double);
+            int inside = 0;
+            double z_last = -10000;
+            for (int64_t e = 0; e <= m; ++e) {
+                int64_t lo, hi;
+                if (e < m) {
+                    lo = (int64_t)ceil(z_last); if (lo < 0) lo = 0;
+                    hi = (int64_t)floor(col[e]); if (hi > nz - 1) hi = nz - 1;
+                } else {
+                    if (!(ceil(z_last) < (double)(nz - 1))) break;
+                    lo = (int64_t)ceil(z_last); if (lo < 0) lo = 0;
+                    hi = nz - 1;
+                }
+                for (int64_t z = lo; z <= hi; ++z) phase[cell_index(L, cx, cy, z)] = inside ? 1.0 : 0.0;
+                if (e < m) {
+                    z_last = col[e];
+                    inside = !inside;
+                }
+            }
+        }
+    free(count);
+    free(zs);
+    free(fillp);
+}
+
 /* ------------------------------------------------------------------ walls */
 static int is_fd_wall(const orc_lattice* L, int64_t y, int64_t z) {
     if (!L->periodic[1] && L->wall_y == ORC_WALL_FD_VELOCITY && (y == 0 || y == L->ny - 1)) return 1;
@@ -996,6 +1106,7 @@ struct orc_sys {
     int32_t nparts;
     int32_t* cls;
     int64_t ncls;
+    int32_t voxelize;
 };
 
 orc_sys* orc_sys_create(const orc_lattice* L, int32_t dirac, double ib_offset) {
@@ -1099,7 +1210,32 @@ int32_t orc_sys_add_particle(orc_sys* s, int32_t shape, int32_t model, const dou
     return s->nparts++;
 }
 
-void orc_sys_init(orc_sys* s) { (void)s; }
+static void gather_vertices(orc_sys* s, double** pos, int64_t* ntot);
+
+/* all particles' triangles with global vertex indices, then the voxelization */
+static void sys_voxelize(orc_sys* s) {
+    if (!s->voxelize || s->nparts == 0) return;
+    double* pos;
+    int64_t nvt, ntt = 0;
+    gather_vertices(s, &pos, &nvt);
+    for (int32_t i = 0; i < s->nparts; ++i) ntt += s->shapes[s->parts[i].shape].nt;
+    int64_t* tri = (int64_t*)malloc(sizeof(int64_t) * 3 * (size_t)(ntt > 0 ? ntt : 1));
+    int64_t t = 0, vo = 0;
+    for (int32_t i = 0; i < s->nparts; ++i) {
+        const orc_shape* sh = &s->shapes[s->parts[i].shape];
+        for (int64_t k = 0; k < sh->nt; ++k, ++t)
+            for (int c = 0; c < 3; ++c) tri[3 * t + c] = vo + sh->tri[3 * k + c];
+        vo += sh->nv;
+    }
+    orc_voxelize(&s->L, nvt, pos, ntt, tri, s->phase);
+    free(pos);
+    free(tri);
+}
+
+void orc_sys_set_voxelize(orc_sys* s, int32_t on) { s->voxelize = on; }
+
+/* ImmersedBoundaryDynamics3D::init voxelizes the initial positions (ImmersedBoundaryDynamics.hh:404-412) */
+void orc_sys_init(orc_sys* s) { sys_voxelize(s); }
 
 static void gather_vertices(orc_sys* s, double** pos, int64_t* ntot) {
     int64_t n = 0;
@@ -1156,6 +1292,8 @@ static void sys_step(orc_sys* s) {
             remap_com(s, p);
         }
         free(pos); free(cls); free(vel); free(frc);
+        /* move_vertices_and_revoxelize, ImmersedBoundaryDynamics.hh:461-483 */
+        sys_voxelize(s);
     }
     orc_collide_stream(L, s->f, s->ftmp, s->F, s->phase);
 }

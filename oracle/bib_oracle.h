@@ -56,6 +56,11 @@ typedef struct {
 
 enum { ORC_CELL_FLUID = 0, ORC_CELL_BOUNCE_BACK = 1, ORC_CELL_NO_DYNAMICS = 2 };
 
+/* ---- voxelization: phase 1 inside the closed membranes, 0 outside ---- */
+/* pos: nvt x 3 vertex positions of all particles; tri: ntt x 3 global vertex indices; phase: n cells,
+ * updated in place (cells the reference's fill does not reach keep their value). */
+void orc_voxelize(const orc_lattice* L, int64_t nvt, const double* pos, int64_t ntt, const int64_t* tri, double* phase);
+
 /* ---- lattice ---- */
 void orc_collide_cell(const orc_lattice* L, double* f19, const double* F3, double phase);
 void orc_collide_stream(const orc_lattice* L, double* f, double* ftmp, const double* F, const double* phase);
@@ -97,6 +102,7 @@ int32_t orc_sys_add_shape(orc_sys* s, int64_t nv, const double* xyz, int64_t nt,
 int32_t orc_sys_add_particle(orc_sys* s, int32_t shape, int32_t model, const double* prm, const double* pos);
 void orc_sys_init(orc_sys* s);
 void orc_sys_step(orc_sys* s, int64_t nsteps);
+void orc_sys_set_voxelize(orc_sys* s, int32_t on);  /* revoxelize after every move (and at init) */
 void orc_sys_lattice_only_step(orc_sys* s, int64_t nsteps);
 void orc_sys_get_particle(orc_sys* s, int32_t pid, double* pos, double* vel, double* force, double* stats5);
 void orc_sys_velocity(orc_sys* s, double* u);

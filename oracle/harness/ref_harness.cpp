@@ -122,6 +122,16 @@ static void dump_velocity(recio::Writer& w, const std::string& tag, Lattice& lat
     w.d("u_" + tag, shp(3, nz, ny, nx), u);
 }
 
+// the phase external (the voxelization's output), ImmersedBoundaryDynamics_voxelization.hh:106-115
+static void dump_phase(recio::Writer& w, const std::string& tag, Lattice& lattice) {
+    const plint nx = lattice.getNx(), ny = lattice.getNy(), nz = lattice.getNz();
+    std::vector<double> ph((size_t)nx * ny * nz);
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x) ph[lidx(x, y, z, nx, ny)] = cell_at(lattice, x, y, z).getExternal(0)[3];
+    w.d("phase_" + tag, shp(nz, ny, nx), ph);
+}
+
 static void load_lattice(const Bundle& in, Lattice& lattice, bool pops) {
     const plint nx = lattice.getNx(), ny = lattice.getNy(), nz = lattice.getNz();
     const size_t n = (size_t)nx * ny * nz;
@@ -323,6 +333,14 @@ static int run_ibm_impl(const Bundle& in, const char* out) {
     std::auto_ptr<MultiTensorField3D<T, 3> > velocity = generateMultiTensorField<T, 3>(domain);
     fsi.add_particle(proto);
     fsi.init();
+    std::vector<double> phase0;
+    {
+        const size_t n = (size_t)nx * ny * nz;
+        phase0.resize(n);
+        for (plint z = 0; z < nz; ++z)
+            for (plint y = 0; y < ny; ++y)
+                for (plint x = 0; x < nx; ++x) phase0[lidx(x, y, z, nx, ny)] = cell_at(lattice, x, y, z).getExternal(0)[3];
+    }
 
     const plint nv = proto->count_nodes();
     std::vector<double> pos((steps + 1) * nv * 3), vel(steps * nv * 3), frc(steps * nv * 3);
@@ -369,6 +387,8 @@ static int run_ibm_impl(const Bundle& in, const char* out) {
     w.d("inertia", shp(steps + 1, 3, 3), inertia);
     dump_lattice(w, "end", lattice);
     dump_velocity(w, "end", lattice);
+    w.d("phase_0", shp(nz, ny, nx), phase0);
+    dump_phase(w, "end", lattice);
     delete proto;
     return 0;
 }

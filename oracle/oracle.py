@@ -76,6 +76,8 @@ def lib():
             "orc_sys_add_shape": (C.c_int32, [C.c_void_p, C.c_int64, dp, C.c_int64, ip]),
             "orc_sys_add_particle": (C.c_int32, [C.c_void_p, C.c_int32, C.c_int32, dp, dp]),
             "orc_sys_init": (None, [C.c_void_p]),
+            "orc_sys_set_voxelize": (None, [C.c_void_p, C.c_int32]),
+            "orc_voxelize": (None, [C.c_void_p, C.c_int64, C.c_void_p, C.c_int64, C.c_void_p, C.c_void_p]),
             "orc_sys_step": (None, [C.c_void_p, C.c_int64]),
             "orc_sys_lattice_only_step": (None, [C.c_void_p, C.c_int64]),
             "orc_sys_get_particle": (None, [C.c_void_p, C.c_int32, dp, dp, dp, dp]),
@@ -298,6 +300,14 @@ class System:
         self.nv.append(self._shape_nv[shape])
         return pid
 
+    def set_voxelize(self, on=True):
+        """Revoxelize the membranes into the phase field after every move (and at init)."""
+        lib().orc_sys_set_voxelize(self.h, int(bool(on)))
+
+    def init(self):
+        """ImmersedBoundaryDynamics3D::init: voxelize the initial positions (when enabled)."""
+        lib().orc_sys_init(self.h)
+
     def step(self, n=1):
         lib().orc_sys_step(self.h, int(n))
 
@@ -314,3 +324,12 @@ class System:
         u = np.zeros((3, self.L.nz, self.L.ny, self.L.nx))
         lib().orc_sys_velocity(self.h, _d(u))
         return u
+
+
+def voxelize(L, pos, tri, phase=None):
+    """Phase field (nz, ny, nx) of closed meshes: pos (nvt, 3), tri (ntt, 3) global vertex indices;
+    `phase` is updated in place (cells the fill does not reach keep their value)."""
+    pos, tri = f64(pos), i64(tri)
+    ph = np.zeros((L.nz, L.ny, L.nx)) if phase is None else phase
+    lib().orc_voxelize(C.byref(L), pos.shape[0], _d(pos), tri.shape[0], _i(tri), _d(ph))
+    return ph

@@ -252,6 +252,7 @@ def case_ibm_capsule_shear():
     keep["fbar_end_planes"] = out["fbar_end"][:, :, [0, 1, n // 2, n - 2, n - 1], :]
     keep["fbar_end_sum"] = out["fbar_end"].sum(axis=(1, 2, 3))
     keep["force_spread"] = out["force_spread"]
+    keep["phase_0"], keep["phase_end"] = out["phase_0"], out["phase_end"]
     save("ibm_capsule_shear", inp, keep)
 
 
@@ -273,11 +274,31 @@ def case_ibm_rbc_periodic():
     keep["fbar_end_sum"] = out["fbar_end"].sum(axis=(1, 2, 3))
     keep["fbar_end_planes"] = out["fbar_end"][:, :, [0, 5, 10], :]
     keep["force_spread"] = out["force_spread"]
+    keep["phase_0"], keep["phase_end"] = out["phase_0"], out["phase_end"]
     save("ibm_rbc_periodic", inp, keep)
 
 
+def case_ibm_capsule_lambda():
+    """Viscosity ratio 5 inside a capsule in shear: the voxelized phase enters omega."""
+    n = 20
+    xyz, tri = meshes.icosphere(2, 4.5)
+    tau, U = 0.9, 0.04
+    nu = (tau - 0.5) / 3
+    G = nu * (2 * U / (n - 1)) * 4.5 / 0.3
+    pos = meshes.place(xyz, None, (0.5 * (n - 1) + 0.31, 0.5 * (n - 1) - 0.17, 0.5 * (n - 1) + 0.23))
+    inp = dict(dims=[n, n, n], tau=tau, lam=5.0, walls=1, U=U, steps=6, rest=xyz, tri=tri, pos=pos, model=1,
+               params=particle_params(1, G=G, C=1.0))
+    inp["lambda"] = inp.pop("lam")
+    out = run("ibm", inp)
+    keep = {k: out[k] for k in ("pos", "vel", "force", "volume", "area", "com")}
+    keep["u_end"] = out["u_end"]
+    keep["fbar_end"] = out["fbar_end"]
+    keep["phase_0"], keep["phase_end"] = out["phase_0"], out["phase_end"]
+    save("ibm_capsule_lambda", inp, keep)
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
-         case_ibm_capsule_shear, case_ibm_rbc_periodic]
+         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
