@@ -71,6 +71,7 @@ SIGNATURES = {
     "bib_lattice_set_force": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_lattice_get_force": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_lattice_set_phase": (C.c_int32, [_vp, C.c_int32, _dp]),
+    "bib_lattice_get_phase": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_lattice_get_velocity": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_shape_store": (C.c_int32, [_vp, _dp, _ip, C.c_int64, C.c_int64, _i32p]),
     "bib_shape_info": (C.c_int32, [_vp, C.c_int32, _dp]),

@@ -195,6 +195,11 @@ class Lattice:
         ph = _f64(np.broadcast_to(phase, self.shape))
         self.ctx.check(self.ctx.lib.bib_lattice_set_phase(self.ctx.h, self.h, _d(ph)))
 
+    def get_phase(self):
+        ph = np.empty(self.shape)
+        self.ctx.check(self.ctx.lib.bib_lattice_get_phase(self.ctx.h, self.h, _d(ph)))
+        return ph
+
     def compute_velocity(self):
         u = np.empty((3,) + self.shape)
         self.ctx.check(self.ctx.lib.bib_lattice_get_velocity(self.ctx.h, self.h, _d(u)))

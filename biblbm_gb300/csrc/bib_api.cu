@@ -311,6 +311,10 @@ void free_particles(Lattice& L) {
     cudaFree(L.sort_temp);
     L.sort_temp = nullptr;
     L.sort_temp_bytes = 0;
+    cudaFree(L.vox_count);
+    cudaFree(L.vox_z);
+    L.vox_count = nullptr;
+    L.vox_z = nullptr;
 }
 
 void drop_graphs(bib_ctx* c, int32_t h) {
@@ -403,6 +407,15 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
     if (L.membrane_smem + 1024 > (size_t)dev_max)
         return fail(c, BIB_EUNSUPPORTED, "mesh with %d vertices exceeds the membrane kernel's shared memory", L.max_nv);
     configure_membrane_kernel(L.membrane_smem);
+    if (L.phase) {
+        // the reference voxelizes the membranes into the phase field when the immersed-boundary
+        // functional first runs (ImmersedBoundaryDynamics.hh:404-412) and after every move
+        const int64_t ncol = (int64_t)L.d.nx * L.d.ny;
+        BIB_CUDA(c, cudaMalloc((void**)&L.vox_count, ncol * sizeof(int)));
+        BIB_CUDA(c, cudaMemset(L.vox_count, 0, ncol * sizeof(int)));
+        BIB_CUDA(c, cudaMalloc((void**)&L.vox_z, ncol * kVoxelCap * sizeof(double)));
+        launch_voxelize(L, L.pos[L.pcur], c->stream);
+    }
     BIB_CHECK_LAUNCH(c);
     L.particles_dirty = false;
     drop_graphs(c, L.handle);
@@ -421,9 +434,36 @@ void record(bib_ctx* c, int idx) {
 // emits the velocity field of the pre-collision state with the previous force -> wall
 // reconstruction -> interpolation of that velocity to X_n and the move -> area / volume /
 // centre of the new positions.
+//
+// With a phase field and particles the collision needs the phase of the moved membranes
+// (move_vertices_and_revoxelize, ImmersedBoundaryDynamics.hh:461-483, runs before
+// collideAndStream), so the move comes first: velocity field of the current state ->
+// interpolation and move -> area / volume / centre -> voxelization -> collide-and-stream.
 void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
     cudaStream_t s = c->stream;
     const bool ib = with_ib && L.nvert > 0;
+    if (with_ib && with_lbm && ib && L.phase) {
+        if (!L.target_clean) launch_force_fill(L, 1 - L.fe, s);
+        record(c, 0);
+        launch_membrane_forces(L, s);
+        record(c, 1);
+        launch_spread(L, 1 - L.fe, s);
+        record(c, 2);
+        launch_velocity_field(L, s);
+        launch_interpolate_move(L, s);
+        launch_particle_update(L, s);
+        L.pcur = 1 - L.pcur;
+        launch_voxelize(L, L.pos[L.pcur], s);
+        launch_collide_stream(L, true, s);
+        record(c, 3);
+        L.cur = 1 - L.cur;
+        L.fe = 1 - L.fe;
+        L.target_clean = true;
+        launch_fd_walls(L, L.cur, L.fe, s);
+        record(c, 4);
+        record(c, 5);
+        return;
+    }
     if (with_ib && with_lbm) {
         if (!L.target_clean) launch_force_fill(L, 1 - L.fe, s);
         record(c, 0);
@@ -463,6 +503,7 @@ void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
             launch_interpolate_move(L, s);
             launch_particle_update(L, s);
             L.pcur = 1 - L.pcur;
+            launch_voxelize(L, L.pos[L.pcur], s);
         }
         record(c, 5);
         return;
@@ -683,6 +724,9 @@ bib_status build_batch(bib_ctx* c, Batch& B) {
         Lattice& L = *get_lattice(c, B.handles[i]);
         bib_status st = sync_particles(c, L);
         if (st) return st;
+        if (L.phase && L.nvert)
+            return fail(c, BIB_EUNSUPPORTED, "batched steps do not voxelize membranes into a phase field (lattice %d)",
+                        B.handles[i]);
         B.versions[i] = L.version;
         B.state0[i] = lattice_state(L);
         for (int p = 0; p < 2; ++p) {
@@ -894,6 +938,7 @@ const char* bib_status_string(bib_status s) {
         case BIB_ETIMEOUT: return "device wait timed out";
         case BIB_ESTATE: return "invalid call order";
         case BIB_EUNSUPPORTED: return "unsupported option";
+        case BIB_EOVERFLOW: return "device buffer overflow";
         default: return "unknown status";
     }
 }
@@ -907,9 +952,10 @@ bib_status bib_create(const bib_config* cfg, bib_ctx** out) {
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
-    // d_flag[0]: NaN scan result, d_flag[1]: set by a bounded device wait that gave up
-    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_flag, 2 * sizeof(int));
-    if (e == cudaSuccess) e = cudaMemset(c->d_flag, 0, 2 * sizeof(int));
+    // d_flag[0]: NaN scan result, d_flag[1]: set by a bounded device wait that gave up,
+    // d_flag[2]: set by a voxelization whose column held more crossings than it can store
+    if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_flag, 3 * sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(c->d_flag, 0, 3 * sizeof(int));
     if (e != cudaSuccess) {
         delete c;
         return BIB_ECUDA;
@@ -1250,6 +1296,7 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
     *handle = (int32_t)c->lattices.size();
     L->handle = *handle;
     L->wait_err = c->d_flag + 1;
+    L->vox_err = c->d_flag + 2;
     c->lattices.push_back(std::move(L));
     return BIB_OK;
 }
@@ -1391,6 +1438,17 @@ bib_status bib_lattice_get_force(bib_ctx* c, int32_t h, double* F) {
     BIB_CUDA(c, cudaMemcpyAsync(F, d, 3 * L->d.n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(d);
+    return BIB_OK;
+}
+
+bib_status bib_lattice_get_phase(bib_ctx* c, int32_t h, double* phase) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !phase) return fail(c, BIB_EINVAL, "invalid lattice handle or phase");
+    if (!L->phase) return fail(c, BIB_ESTATE, "lattice was created with use_phase = 0");
+    std::vector<uint8_t> h8((size_t)L->d.n);
+    BIB_CUDA(c, cudaMemcpyAsync(h8.data(), L->phase, h8.size(), cudaMemcpyDeviceToHost, c->stream));
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (size_t k = 0; k < h8.size(); ++k) phase[k] = h8[k] ? 1.0 : 0.0;
     return BIB_OK;
 }
 
@@ -1631,12 +1689,17 @@ bib_status bib_check_health(bib_ctx* c, int32_t h) {
     BIB_CUDA(c, cudaMemsetAsync(c->d_flag, 0, sizeof(int), c->stream));
     launch_nan_scan(*L, c->d_flag, c->stream);
     BIB_CHECK_LAUNCH(c);
-    int flag[2] = {0, 0};
-    BIB_CUDA(c, cudaMemcpyAsync(flag, c->d_flag, 2 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    int flag[3] = {0, 0, 0};
+    BIB_CUDA(c, cudaMemcpyAsync(flag, c->d_flag, 3 * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     if (flag[1]) {
         BIB_CUDA(c, cudaMemsetAsync(c->d_flag + 1, 0, sizeof(int), c->stream));
         return fail(c, BIB_ETIMEOUT, "a bounded device wait gave up; the results of that step are invalid");
+    }
+    if (flag[2]) {
+        BIB_CUDA(c, cudaMemsetAsync(c->d_flag + 2, 0, sizeof(int), c->stream));
+        return fail(c, BIB_EOVERFLOW, "voxelization: a lattice column was crossed by more than %d membrane triangles, or "
+                    "a triangle was wider than the lattice; the phase field of that step is incomplete", kVoxelCap);
     }
     if (flag[0]) return fail(c, BIB_ENAN, "populations contain NaN or Inf");
     if (!L->particles_dirty && L->nvert) {

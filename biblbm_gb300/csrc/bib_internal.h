@@ -198,6 +198,10 @@ struct Lattice {
     int stages = 0;           // staged kernel pipeline depth (0 = automatic)
     int membrane_block = 256; // threads per particle of the membrane kernel
     int* wait_err = nullptr;  // device word set by a bounded device wait that gave up
+    // voxelization of the membranes into the phase field (lattices with a phase field and particles)
+    int* vox_count = nullptr;  // crossings per (x, y) column, zero between launches
+    double* vox_z = nullptr;   // kVoxelCap heights per column, slot-major
+    int* vox_err = nullptr;    // device word set when a column held more than kVoxelCap crossings
     uint64_t version = 0;     // bumped whenever the particle buffers are (re)allocated
     int handle = -1;
 };
@@ -227,6 +231,8 @@ void launch_membrane_forces(const Lattice& L, cudaStream_t s);
 void launch_spread(const Lattice& L, int fbuf, cudaStream_t s);
 void launch_interpolate_move(const Lattice& L, cudaStream_t s);  // vel and pos[1-pcur] = pos + vel
 void launch_particle_update(const Lattice& L, cudaStream_t s);   // area/volume/COM of pos[1-pcur] + remap
+constexpr int kVoxelCap = 64;  // membrane crossings one (x, y) column can hold
+void launch_voxelize(const Lattice& L, const double* pos, cudaStream_t s);  // phase field of the membranes at pos
 size_t membrane_smem_bytes(int max_nv);
 size_t spread_sort_temp_bytes(int64_t nentries);
 void configure_membrane_kernel(size_t smem);

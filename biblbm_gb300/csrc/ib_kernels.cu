@@ -836,6 +836,128 @@ __global__ void __launch_bounds__(256) k_particle_update(const ParticleDev* __re
     }
 }
 
+// ---------------------------------------------------------------- voxelization
+// RayTracer::tri_ray_intersect (fsi/RayTracer.hh:80-108) for the ray from (px, py, 0) along
+// +z, in the reference's operation order and without fused multiply-adds, so the
+// intersection heights (and therefore the phase field) are the reference's to the bit.
+__device__ __forceinline__ double dot_nofma(const double* a, const double* b) {
+    double r = 0.0;
+#pragma unroll
+    for (int d = 0; d < 3; ++d) r = __dadd_rn(r, __dmul_rn(a[d], b[d]));
+    return r;
+}
+__device__ __forceinline__ void cross_nofma(const double* a, const double* b, double* c) {
+    c[0] = __dsub_rn(__dmul_rn(a[1], b[2]), __dmul_rn(a[2], b[1]));
+    c[1] = __dsub_rn(__dmul_rn(a[2], b[0]), __dmul_rn(a[0], b[2]));
+    c[2] = __dsub_rn(__dmul_rn(a[0], b[1]), __dmul_rn(a[1], b[0]));
+}
+__device__ __forceinline__ bool tri_ray_z(const double* v0, const double* v1, const double* v2, double px, double py,
+                                          double& dist) {
+    const double e1[3] = {__dsub_rn(v1[0], v0[0]), __dsub_rn(v1[1], v0[1]), __dsub_rn(v1[2], v0[2])};
+    const double e2[3] = {__dsub_rn(v2[0], v0[0]), __dsub_rn(v2[1], v0[1]), __dsub_rn(v2[2], v0[2])};
+    const double dir[3] = {0.0, 0.0, 1.0};
+    double q[3];
+    cross_nofma(dir, e2, q);
+    const double a = dot_nofma(e1, q);
+    if (fabs(a) < DBL_EPSILON) return false;
+    const double f = __drcp_rn(a);
+    const double sv[3] = {__dsub_rn(px, v0[0]), __dsub_rn(py, v0[1]), __dsub_rn(0.0, v0[2])};
+    const double u = __dmul_rn(f, dot_nofma(sv, q));
+    if (u < 0.0) return false;
+    double r[3];
+    cross_nofma(sv, e1, r);
+    const double v = __dmul_rn(f, dot_nofma(dir, r));
+    if (v < 0.0 || __dadd_rn(u, v) > 1.0) return false;
+    dist = __dmul_rn(f, dot_nofma(e2, r));
+    return true;
+}
+
+// One CTA per particle, one thread per triangle: z-rays through the integer (x, y) points of
+// the triangle's xy box (RayTracer::find_intersections_z, RayTracer.hh:18-40); each hit goes
+// to its (periodically wrapped) column, height wrapped into [-1/2, nz - 1/2) (ZBuffer::put,
+// Arithmetic1D::remap_pos).  Columns are numbered x fastest.
+__global__ void __launch_bounds__(128) k_voxel_rays(LatticeDesc d, const ParticleDev* __restrict__ parts,
+                                                     const double* __restrict__ pos, int* __restrict__ count,
+                                                     double* __restrict__ zbuf, int cap, int* __restrict__ overflow) {
+    const ParticleDev& P = parts[blockIdx.x];
+    const double* pv = pos + 3LL * P.v0;
+    const int64_t ncol = (int64_t)d.nx * d.ny;
+    for (int t = threadIdx.x; t < P.nt; t += blockDim.x) {
+        const double* v0 = pv + 3 * P.tri[3 * t];
+        const double* v1 = pv + 3 * P.tri[3 * t + 1];
+        const double* v2 = pv + 3 * P.tri[3 * t + 2];
+        double x0 = fmin(v0[0], fmin(v1[0], v2[0])), x1 = fmax(v0[0], fmax(v1[0], v2[0]));
+        double y0 = fmin(v0[1], fmin(v1[1], v2[1])), y1 = fmax(v0[1], fmax(v1[1], v2[1]));
+        // a triangle wider than the lattice (or not finite) only arises from a diverged
+        // membrane: flag it instead of casting rays through a runaway box
+        if (!(x1 - x0 < (double)d.nx && y1 - y0 < (double)d.ny)) {
+            atomicExch(overflow, 1);
+            continue;
+        }
+        if (!d.px) x0 = fmax(x0, -1.0), x1 = fmin(x1, (double)d.nx);  // rays outside a walled axis are dropped
+        if (!d.py) y0 = fmax(y0, -1.0), y1 = fmin(y1, (double)d.ny);
+        const int64_t i0 = (int64_t)ceil(x0), i1 = (int64_t)floor(x1);
+        const int64_t j0 = (int64_t)ceil(y0), j1 = (int64_t)floor(y1);
+        for (int64_t i = i0; i <= i1; ++i)
+            for (int64_t j = j0; j <= j1; ++j) {
+                double z;
+                if (!tri_ray_z(v0, v1, v2, (double)i, (double)j, z)) continue;
+                int64_t cx = i, cy = j;
+                if (d.px) cx = pmod(cx, d.nx);
+                else if (cx < 0 || cx >= d.nx) continue;
+                if (d.py) cy = pmod(cy, d.ny);
+                else if (cy < 0 || cy >= d.ny) continue;
+                if (d.pz) z = __dsub_rn(z, __dmul_rn((double)d.nz, floor(__dmul_rn(__dsub_rn(z, -0.5), d.inv_n[2]))));
+                const int64_t c = cx + (int64_t)d.nx * cy;
+                const int slot = atomicAdd(count + c, 1);
+                if (slot < cap) zbuf[slot * ncol + c] = z;
+                else atomicExch(overflow, 1);
+            }
+    }
+}
+
+// One thread per column: sort its heights and fill the column from below by parity
+// (apply_voxelization, ImmersedBoundaryDynamics_voxelization.hh:121-161); resets the count.
+// Heights of column c sit at zbuf[slot * ncol + c], so a warp reads slot e of 32 columns at once.
+__global__ void __launch_bounds__(128) k_voxel_fill(LatticeDesc d, int* __restrict__ count, double* __restrict__ zbuf,
+                                                     int cap, uint8_t* __restrict__ phase) {
+    const int64_t ncol = (int64_t)d.nx * d.ny;
+    const int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (c >= ncol) return;
+    const int m = min(count[c], cap);
+    count[c] = 0;
+    double* zl = zbuf + c;
+    for (int e = 1; e < m; ++e) {  // insertion sort, ascending, in place
+        const double z = zl[e * ncol];
+        int p = e;
+        while (p > 0 && zl[(p - 1) * ncol] > z) {
+            zl[p * ncol] = zl[(p - 1) * ncol];
+            --p;
+        }
+        zl[p * ncol] = z;
+    }
+    const int64_t plane = ncol;
+    uint8_t inside = 0;
+    double z_last = -10000.0;
+    for (int e = 0; e <= m; ++e) {
+        const double ze = e < m ? zl[e * ncol] : 0.0;
+        int64_t lo, hi;
+        if (e < m) {
+            lo = max((int64_t)ceil(z_last), (int64_t)0);
+            hi = min((int64_t)floor(ze), (int64_t)d.nz - 1);
+        } else {
+            if (!(ceil(z_last) < (double)(d.nz - 1))) break;
+            lo = max((int64_t)ceil(z_last), (int64_t)0);
+            hi = d.nz - 1;
+        }
+        for (int64_t z = lo; z <= hi; ++z) phase[c + plane * z] = inside;
+        if (e < m) {
+            z_last = ze;
+            inside ^= 1;
+        }
+    }
+}
+
 }  // namespace
 
 size_t membrane_smem_bytes(int max_nv) { return (size_t)3 * max_nv * sizeof(double); }
@@ -1011,6 +1133,17 @@ void launch_spread(const Lattice& L, int fbuf, cudaStream_t s) {
         return;
     }
     spread_any<false>(L.storage, L.ib.dirac, single_view(L, fbuf), nullptr, nullptr, L.nvert, s);
+}
+
+// Phase field of the membranes at pos (the positions of the current step's end): z-rays of
+// every triangle, then the per-column parity fill.  count must be zero on entry (it is left
+// zero); a column with more than cap crossings, or a triangle wider than the lattice, sets
+// *overflow (the column keeps its first cap crossings, the triangle casts no rays).
+void launch_voxelize(const Lattice& L, const double* pos, cudaStream_t s) {
+    if (!L.phase || L.parts.empty()) return;
+    k_voxel_rays<<<(int)L.parts.size(), 128, 0, s>>>(L.d, L.pdev, pos, L.vox_count, L.vox_z, kVoxelCap, L.vox_err);
+    const int64_t ncol = (int64_t)L.d.nx * L.d.ny;
+    k_voxel_fill<<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(L.d, L.vox_count, L.vox_z, kVoxelCap, L.phase);
 }
 
 }  // namespace bib

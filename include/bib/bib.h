@@ -55,7 +55,8 @@ enum {
     BIB_ENAN = -4,         /* the state contains NaN / Inf */
     BIB_ETIMEOUT = -5,     /* a bounded device wait gave up */
     BIB_ESTATE = -6,       /* call not valid in the current state */
-    BIB_EUNSUPPORTED = -7  /* option combination not implemented */
+    BIB_EUNSUPPORTED = -7, /* option combination not implemented */
+    BIB_EOVERFLOW = -8     /* a fixed-capacity device buffer overflowed (see bib_check_health) */
 };
 
 /* population storage on the device */
@@ -168,8 +169,11 @@ bib_status bib_lattice_init_equilibrium(bib_ctx* ctx, int32_t h, const double* r
 /* external force scalars (3n): setExternalVector / read back */
 bib_status bib_lattice_set_force(bib_ctx* ctx, int32_t h, const double* F);
 bib_status bib_lattice_get_force(bib_ctx* ctx, int32_t h, double* F);
-/* phase scalar (n, values 0..1), used when use_phase = 1 */
+/* phase scalar (n, values 0..1), used when use_phase = 1.  With particles the lattice keeps it
+ * up to date itself: the membranes are voxelized into it when the particles are first stepped
+ * and after every move (ImmersedBoundaryDynamics_voxelization.hh:17-30, 121-161) */
 bib_status bib_lattice_set_phase(bib_ctx* ctx, int32_t h, const double* phase);
+bib_status bib_lattice_get_phase(bib_ctx* ctx, int32_t h, double* phase);
 /* computeVelocity (dataAnalysisWrapper3D.hh:1660): u = j/rho + F/2, wall nodes give the wall velocity */
 bib_status bib_lattice_get_velocity(bib_ctx* ctx, int32_t h, double* u);
 bib_status bib_lattice_cells(bib_ctx* ctx, int32_t h, int64_t* n);
@@ -205,7 +209,9 @@ bib_status bib_step_timed(bib_ctx* ctx, int32_t h, int64_t nsteps, double* ms);
 /* stream the context's work into CUDA-graph replays (1) or plain launches (0) */
 bib_status bib_set_graph_mode(bib_ctx* ctx, int32_t enabled);
 /* scan populations and vertex positions for NaN / Inf: BIB_OK or BIB_ENAN; BIB_ETIMEOUT if a
- * bounded device wait of an earlier step gave up (the flag is cleared by the call) */
+ * bounded device wait of an earlier step gave up, BIB_EOVERFLOW if an earlier voxelization met a
+ * lattice column crossed by more than 64 membrane triangles or a triangle wider than the lattice
+ * (each flag is cleared by the call) */
 bib_status bib_check_health(bib_ctx* ctx, int32_t h);
 /* kernel selection and tile size of the collide-and-stream step (no reference counterpart);
  * BIB_EUNSUPPORTED if BIB_KERNEL_STAGED is forced on a lattice whose x-rows do not fit it */

@@ -164,20 +164,27 @@ def test_membrane_forces_match_reference(ctx, model, mode):
 
 
 # ---------------------------------------------------------------- coupled steps
-def run_coupled_gpu(ctx, d, storage="f64", graph=True, spread="atomic", kernel="auto"):
+def run_coupled_gpu(ctx, d, storage="f64", graph=True, spread="atomic", kernel="auto", use_phase=False):
+    """The fixture's coupled case on the GPU; use_phase (implied by a viscosity ratio in the
+    fixture) gives the lattice a phase field that the membranes are voxelized into."""
     nx, ny, nz = (int(v) for v in d["in_dims"])
-    om = 1.0 / float(d["in_tau"])
+    tau = float(d["in_tau"])
+    om = 1.0 / tau
+    lam = float(d["in_lambda"]) if "in_lambda" in d.files else 1.0
+    phase_kw = {}
+    if use_phase or lam != 1.0:
+        phase_kw = dict(use_phase=True, omega_inner=1.0 / (0.5 + lam * (tau - 0.5)))
     walls = int(d["in_walls"])
     body = d["in_body"] if "in_body" in d.files else np.zeros(3)
     if walls == 1:
         U = float(d["in_U"])
         wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
         lat = ctx.add_domain(nx, ny, nz, periodic=(1, 0, 1), omega=om, wall_y="fd_velocity", wall_u=wall_u,
-                             storage=storage, body_force=body)
+                             storage=storage, body_force=body, **phase_kw)
         L = O.lattice((nx, ny, nz), (1, 0, 1), "bgk_guo_vof", om, om, wall_y="fd_velocity", wall_u=wall_u)
         lat.initialize_at_equilibrium(None, shear_state(L, U))
     else:
-        lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=om, storage=storage, body_force=body)
+        lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=om, storage=storage, body_force=body, **phase_kw)
         lat.initialize_at_equilibrium(None, np.zeros((3, nz, ny, nx)))
     lat.set_tuning(kernel)
     shapes = bib.ParticleShapeLibrary(ctx)
@@ -208,6 +215,71 @@ def test_coupled_steps_match_reference(ctx, name, kernel):
             assert np.abs(lat.get_external_force() - d["out_force_spread"]).max() < 1e-15
     assert np.abs(lat.compute_velocity() - d["out_u_end"]).max() < 1e-14
     assert rel(fsi.get_particle(pid)["inertia"], d["out_inertia"][-1]) < 1e-12
+
+
+@pytest.mark.parametrize("name", ["ibm_capsule_shear", "ibm_rbc_periodic"])
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_voxelized_phase_matches_reference(ctx, name, kernel):
+    """Viscosity ratio 1 with a phase field: the step that voxelizes the moved membranes
+    before the collision follows the reference's trajectory, and the phase field of the
+    final positions is the reference's, cell for cell."""
+    d = golden(name)
+    lat, fsi, pid = run_coupled_gpu(ctx, d, graph=False, kernel=kernel, use_phase=True)
+    steps = int(d["in_steps"])
+    fscale = np.abs(d["out_force"]).max()
+    for it in range(steps):
+        fsi.step(1)
+        p = fsi.get_particle(pid)
+        assert rel(p["pos"], d["out_pos"][it + 1]) < 1e-13, it
+        assert rel(p["vel"], d["out_vel"][it]) < 1e-11, it
+        assert np.abs(p["force"] - d["out_force"][it]).max() < 1e-10 * fscale, it
+    assert np.abs(lat.compute_velocity() - d["out_u_end"]).max() < 1e-14
+    ph = lat.get_phase()
+    assert ph.sum() > 0
+    assert np.array_equal(ph, d["out_phase_end"])
+
+
+def oracle_lambda_system(d):
+    """The oracle on the fixture's inputs with the reference's intended dynamics (no omega
+    swap on the periodic envelope), voxelizing after every move."""
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    tau, lam, U = float(d["in_tau"]), float(d["in_lambda"]), float(d["in_U"])
+    om, om_in = 1 / tau, 1 / (0.5 + lam * (tau - 0.5))
+    wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
+    L = O.lattice((nx, ny, nz), (1, 0, 1), "bgk_guo_vof", om, om_in, wall_y="fd_velocity", wall_u=wall_u,
+                  envelope_swap=False)
+    S = O.System(L, "roma", -1.0)
+    S.f[...] = O.apply_fd_walls(L, O.init_equilibrium(L, None, shear_state(L, U)), np.zeros((3, nz, ny, nx)))
+    S.set_voxelize(True)
+    pid = S.add_particle(S.add_shape(d["in_rest"], d["in_tri"]), int(d["in_model"]), d["in_params"], d["in_pos"])
+    S.init()
+    return S, pid
+
+
+@pytest.mark.parametrize("kernel,graph", [("staged", False), ("rows", False), ("staged", True)])
+def test_viscosity_ratio_capsule_against_oracle(ctx, kernel, graph):
+    """Viscosity ratio 5: the voxelized phase selects omega in every collision.  Positions,
+    forces and the phase field follow the oracle step by step, the populations at the end."""
+    d = golden("ibm_capsule_lambda")
+    S, opid = oracle_lambda_system(d)
+    lat, fsi, pid = run_coupled_gpu(ctx, d, graph=graph, kernel=kernel)
+    steps = int(d["in_steps"])
+    if graph:  # graph replay: compare at the end only
+        S.step(steps)
+        fsi.step(steps)
+    for it in range(0 if graph else steps):
+        S.step(1)
+        fsi.step(1)
+        g, r = fsi.get_particle(pid), S.particle(opid)
+        assert rel(g["pos"], r["pos"]) < 1e-13, it
+        assert rel(g["vel"], r["vel"]) < 1e-11, it
+        assert np.array_equal(lat.get_phase(), S.phase), it
+    g, r = fsi.get_particle(pid), S.particle(opid)
+    assert rel(g["pos"], r["pos"]) < 1e-13
+    assert np.array_equal(lat.get_phase(), S.phase)
+    assert lat.get_phase().sum() > 0
+    assert np.abs(lat.receive() - S.f).max() < 1e-13
+    assert np.abs(lat.compute_velocity() - S.velocity()).max() < 1e-14
 
 
 # 10-cell rows: 80 bytes in FP64 fit the staged tile, 40 bytes in FP32 do not
