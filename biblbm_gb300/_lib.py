@@ -85,6 +85,11 @@ SIGNATURES = {
     "bib_total_vertices": (C.c_int32, [_vp, C.c_int32, _ip]),
     "bib_total_volume": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_ibm_step": (C.c_int32, [_vp, C.c_int32]),
+    "bib_ibm_init": (C.c_int32, [_vp, C.c_int32]),
+    "bib_particle_info": (C.c_int32, [_vp, C.c_int32, C.c_int32, _i32p]),
+    "bib_lattice_iteration": (C.c_int32, [_vp, C.c_int32, _ip]),
+    "bib_checkpoint_save": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),
+    "bib_checkpoint_load": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),
     "bib_step": (C.c_int32, [_vp, C.c_int32, C.c_int64]),
     "bib_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),
     "bib_check_health": (C.c_int32, [_vp, C.c_int32]),

@@ -11,6 +11,7 @@ ABI of ``include/bib/bib.h`` into the CUDA library; errors raise ``BibError``.
 from __future__ import annotations
 
 import ctypes as C
+import os
 from dataclasses import dataclass, field
 
 import numpy as np
@@ -208,6 +209,18 @@ class Lattice:
     def check_health(self):
         self.ctx.check(self.ctx.lib.bib_check_health(self.ctx.h, self.h))
 
+    def save_checkpoint(self, path):
+        """Populations, forces, phase, cell types, particles and the iteration counter."""
+        self.ctx.check(self.ctx.lib.bib_checkpoint_save(self.ctx.h, self.h, os.fsencode(path)))
+
+    def load_checkpoint(self, path):
+        self.ctx.check(self.ctx.lib.bib_checkpoint_load(self.ctx.h, self.h, os.fsencode(path)))
+
+    def iteration(self) -> int:
+        it = C.c_int64()
+        self.ctx.check(self.ctx.lib.bib_lattice_iteration(self.ctx.h, self.h, C.byref(it)))
+        return it.value
+
     def set_cell_types(self, types):
         """defineDynamics per cell: 0 the lattice's dynamics, 1 BounceBack, 2 NoDynamics; None resets."""
         if types is None:
@@ -275,7 +288,29 @@ class ImmersedBoundaryDynamics3D:
         return pid.value
 
     def init(self):
-        """Nothing to synchronise on one device; kept for the reference's call sequence."""
+        """ImmersedBoundaryDynamics3D::init: upload the particles and voxelize them into the
+        phase field (the first step does this by itself)."""
+        self.ctx.check(self.ctx.lib.bib_ibm_init(self.ctx.h, self.lattice.h))
+
+    def save_checkpoint(self, path):
+        """Lattice, particles and iteration counter in one file (bib_checkpoint_save)."""
+        self.ctx.check(self.ctx.lib.bib_checkpoint_save(self.ctx.h, self.lattice.h, os.fsencode(path)))
+
+    def load_checkpoint(self, path):
+        """Restore a checkpoint into this lattice; its particles replace the current ones.  The
+        shapes must be stored in the same order as in the run that saved it."""
+        self.ctx.check(self.ctx.lib.bib_checkpoint_load(self.ctx.h, self.lattice.h, os.fsencode(path)))
+        n = C.c_int32()
+        self.ctx.check(self.ctx.lib.bib_particle_count(self.ctx.h, self.lattice.h, C.byref(n)))
+        info = np.zeros(3, dtype=np.int32)
+        self.nv = []
+        for pid in range(n.value):
+            self.ctx.check(self.ctx.lib.bib_particle_info(self.ctx.h, self.lattice.h, pid,
+                                                          info.ctypes.data_as(C.POINTER(C.c_int32))))
+            self.nv.append(int(info[2]))
+
+    def iteration(self) -> int:
+        return self.lattice.iteration()
 
     def count_particles(self) -> int:
         return len(self.nv)

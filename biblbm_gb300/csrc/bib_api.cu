@@ -577,6 +577,7 @@ bib_status run_steps(bib_ctx* c, int32_t h, int64_t nsteps, bool with_ib, bool w
         }
     }
     BIB_CHECK_LAUNCH(c);
+    L->iteration += (uint64_t)nsteps;
     return BIB_OK;
 }
 
@@ -902,6 +903,7 @@ bib_status run_batch(bib_ctx* c, Batch& B, int64_t nsteps) {
         BIB_CHECK_LAUNCH(c);
     }
     BIB_CHECK_LAUNCH(c);
+    for (int32_t h : B.handles) get_lattice(c, h)->iteration += (uint64_t)nsteps;
     return BIB_OK;
 }
 
@@ -1574,6 +1576,15 @@ bib_status bib_particle_count(bib_ctx* c, int32_t h, int32_t* n) {
     return BIB_OK;
 }
 
+bib_status bib_particle_info(bib_ctx* c, int32_t h, int32_t pid, int32_t* out) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !out || pid < 0 || pid >= (int32_t)L->parts.size()) return fail(c, BIB_EINVAL, "invalid particle");
+    out[0] = L->parts[pid].shape;
+    out[1] = L->parts[pid].model;
+    out[2] = L->parts[pid].nv;
+    return BIB_OK;
+}
+
 bib_status bib_total_vertices(bib_ctx* c, int32_t h, int64_t* n) {
     Lattice* L = get_lattice(c, h);
     if (!L || !n) return fail(c, BIB_EINVAL, "invalid lattice handle");
@@ -1708,6 +1719,309 @@ bib_status bib_check_health(bib_ctx* c, int32_t h) {
         for (double v : pos)
             if (!std::isfinite(v)) return fail(c, BIB_ENAN, "vertex positions contain NaN or Inf");
     }
+    return BIB_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------- checkpoints
+// One file per lattice: the reference's lattice checkpoint (parallelIO::save,
+// io/multiBlockWriter3D.cpp:201), its particle checkpoint (save_checkpoint,
+// ImmersedBoundaryDynamics_io.hh:17-72, one pack per particle) and its iteration counter
+// (Time::write_checkpoint, Time.h:20-27) in one versioned binary.  The device buffers are
+// written in their own storage type, so a run resumed from a checkpoint continues bit for
+// bit (with deterministic spreading).  Layout, all little-endian:
+//   CkptHeader | f[cur] (19 x stride) | wall buffer (FD walls) | F[0] | F[1] (3 x stride each)
+//   | phase (stride bytes, use_phase) | cell types (n bytes, when set)
+//   | per particle: CkptParticle + BIB_P_COUNT doubles | positions, velocities, forces (3 x nvert
+//   each) | STATS doubles per particle | 64-bit checksum of everything before it.
+namespace {
+
+constexpr char kCkptMagic[8] = {'B', 'I', 'B', 'C', 'K', 'P', 'T', '1'};
+constexpr uint32_t kCkptVersion = 1;
+
+struct CkptHeader {
+    char magic[8];
+    uint32_t version, header_bytes;
+    int32_t nx, ny, nz, storage, collision, use_phase, has_types, fd_walls;
+    int32_t px, py, pz, wall_y, wall_z;
+    int32_t cur, fe, target_clean, nparts, p_count;
+    int64_t stride, nvert;
+    uint64_t iteration;
+    double omega, omega_inner, trt_magic, scale;
+    double body[3], wall_u[4][3];
+};
+
+struct CkptParticle {
+    int32_t shape, model, nv, nt;
+};
+
+// 64-bit multiply-xorshift hash over the byte stream, 8 bytes at a time
+struct Checksum {
+    uint64_t h = 0x9e3779b97f4a7c15ull;
+    uint64_t carry = 0;
+    int nc = 0;
+    void word(uint64_t w) {
+        h ^= w;
+        h *= 0xbf58476d1ce4e5b9ull;
+        h ^= h >> 31;
+    }
+    void add(const void* p, size_t n) {
+        const unsigned char* b = static_cast<const unsigned char*>(p);
+        size_t i = 0;
+        while (nc && i < n) {
+            carry |= (uint64_t)b[i++] << (8 * nc);
+            if (++nc == 8) word(carry), carry = 0, nc = 0;
+        }
+        for (; i + 8 <= n; i += 8) {
+            uint64_t w;
+            std::memcpy(&w, b + i, 8);
+            word(w);
+        }
+        for (; i < n; ++i) {
+            carry |= (uint64_t)b[i] << (8 * nc);
+            ++nc;
+        }
+    }
+    uint64_t value() const {
+        Checksum t = *this;
+        if (t.nc) t.word(t.carry ^ ((uint64_t)t.nc << 56));
+        return t.h;
+    }
+};
+
+struct CkptFile {
+    FILE* f = nullptr;
+    Checksum sum;
+    ~CkptFile() {
+        if (f) fclose(f);
+    }
+    bool put(const void* p, size_t n) {
+        sum.add(p, n);
+        return fwrite(p, 1, n, f) == n;
+    }
+    bool get(void* p, size_t n) {
+        if (fread(p, 1, n, f) != n) return false;
+        sum.add(p, n);
+        return true;
+    }
+};
+
+constexpr size_t kCkptChunk = (size_t)64 << 20;
+
+bib_status ckpt_put_device(bib_ctx* c, CkptFile& F, const void* dev, size_t bytes, std::vector<unsigned char>& buf) {
+    for (size_t o = 0; o < bytes; o += kCkptChunk) {
+        const size_t n = std::min(kCkptChunk, bytes - o);
+        buf.resize(n);
+        BIB_CUDA(c, cudaMemcpy(buf.data(), static_cast<const unsigned char*>(dev) + o, n, cudaMemcpyDeviceToHost));
+        if (!F.put(buf.data(), n)) return fail(c, BIB_EINVAL, "checkpoint write failed");
+    }
+    return BIB_OK;
+}
+
+bib_status ckpt_get_device(bib_ctx* c, CkptFile& F, void* dev, size_t bytes, std::vector<unsigned char>& buf) {
+    for (size_t o = 0; o < bytes; o += kCkptChunk) {
+        const size_t n = std::min(kCkptChunk, bytes - o);
+        buf.resize(n);
+        if (!F.get(buf.data(), n)) return fail(c, BIB_EINVAL, "checkpoint file is truncated");
+        BIB_CUDA(c, cudaMemcpy(static_cast<unsigned char*>(dev) + o, buf.data(), n, cudaMemcpyHostToDevice));
+    }
+    return BIB_OK;
+}
+
+size_t wall_bytes(const Lattice& L) {
+    return L.d.fd_walls ? pop_bytes(L.storage) * Q * 2 * (size_t)L.d.nx * L.d.nz : 0;
+}
+
+CkptHeader ckpt_header(const Lattice& L) {
+    CkptHeader h;
+    std::memset(&h, 0, sizeof(h));
+    std::memcpy(h.magic, kCkptMagic, 8);
+    h.version = kCkptVersion;
+    h.header_bytes = sizeof(CkptHeader);
+    h.nx = L.d.nx, h.ny = L.d.ny, h.nz = L.d.nz;
+    h.storage = L.storage, h.collision = L.d.collision, h.use_phase = L.d.use_phase;
+    h.has_types = L.celltype != nullptr, h.fd_walls = L.d.fd_walls;
+    h.px = L.d.px, h.py = L.d.py, h.pz = L.d.pz, h.wall_y = L.d.wall_y, h.wall_z = L.d.wall_z;
+    h.cur = L.cur, h.fe = L.fe, h.target_clean = L.target_clean;
+    h.nparts = (int32_t)L.parts.size(), h.p_count = BIB_P_COUNT;
+    h.stride = L.d.stride;
+    h.nvert = L.nvert;
+    h.iteration = L.iteration;
+    h.omega = L.d.omega, h.omega_inner = L.d.omega_inner, h.trt_magic = L.d.trt_magic, h.scale = L.d.scale;
+    std::memcpy(h.body, L.d.body, sizeof(h.body));
+    std::memcpy(h.wall_u, L.d.wall_u, sizeof(h.wall_u));
+    return h;
+}
+
+}  // namespace
+
+extern "C" {
+
+bib_status bib_lattice_iteration(bib_ctx* c, int32_t h, int64_t* it) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !it) return fail(c, BIB_EINVAL, "invalid lattice handle or argument");
+    *it = (int64_t)L->iteration;
+    return BIB_OK;
+}
+
+bib_status bib_ibm_init(bib_ctx* c, int32_t h) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    bib_status st = sync_particles(c, *L);
+    if (st) return st;
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BIB_OK;
+}
+
+bib_status bib_checkpoint_save(bib_ctx* c, int32_t h, const char* path) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !path) return fail(c, BIB_EINVAL, "invalid lattice handle or path");
+    bib_status st = sync_particles(c, *L);
+    if (st) return st;
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    CkptFile F;
+    F.f = fopen(path, "wb");
+    if (!F.f) return fail(c, BIB_EINVAL, "cannot open %s for writing", path);
+    const CkptHeader hd = ckpt_header(*L);
+    if (!F.put(&hd, sizeof(hd))) return fail(c, BIB_EINVAL, "checkpoint write failed");
+    std::vector<unsigned char> buf;
+    const size_t pb = pop_bytes(L->storage) * Q * (size_t)L->d.stride;
+    const size_t fb = force_bytes(L->storage) * 3 * (size_t)L->d.stride;
+    if ((st = ckpt_put_device(c, F, L->f[L->cur], pb, buf))) return st;
+    if (L->d.fd_walls && (st = ckpt_put_device(c, F, L->wall, wall_bytes(*L), buf))) return st;
+    for (int k = 0; k < 2; ++k)
+        if ((st = ckpt_put_device(c, F, L->F[k], fb, buf))) return st;
+    if (L->phase && (st = ckpt_put_device(c, F, L->phase, (size_t)L->d.stride, buf))) return st;
+    if (L->celltype && (st = ckpt_put_device(c, F, L->celltype, (size_t)L->d.n, buf))) return st;
+    for (const ParticleHost& ph : L->parts) {
+        const ShapeHost& S = *c->shapes[ph.shape];
+        const CkptParticle cp{ph.shape, ph.model, ph.nv, (int32_t)S.tri_area.size()};
+        if (!F.put(&cp, sizeof(cp)) || !F.put(ph.prm.data(), BIB_P_COUNT * sizeof(double)))
+            return fail(c, BIB_EINVAL, "checkpoint write failed");
+    }
+    if (L->nvert) {
+        const size_t vb = 3 * (size_t)L->nvert * sizeof(double);
+        if ((st = ckpt_put_device(c, F, L->pos[L->pcur], vb, buf))) return st;
+        if ((st = ckpt_put_device(c, F, L->vel, vb, buf))) return st;
+        if ((st = ckpt_put_device(c, F, L->force, vb, buf))) return st;
+        if ((st = ckpt_put_device(c, F, L->stats, STATS * L->parts.size() * sizeof(double), buf))) return st;
+    }
+    const uint64_t sum = F.sum.value();
+    if (fwrite(&sum, 1, sizeof(sum), F.f) != sizeof(sum) || fflush(F.f) != 0)
+        return fail(c, BIB_EINVAL, "checkpoint write failed");
+    return BIB_OK;
+}
+
+bib_status bib_checkpoint_load(bib_ctx* c, int32_t h, const char* path) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !path) return fail(c, BIB_EINVAL, "invalid lattice handle or path");
+    CkptFile F;
+    F.f = fopen(path, "rb");
+    if (!F.f) return fail(c, BIB_EINVAL, "cannot open %s for reading", path);
+    CkptHeader hd;
+    if (!F.get(&hd, sizeof(hd))) return fail(c, BIB_EINVAL, "checkpoint file is truncated");
+    if (std::memcmp(hd.magic, kCkptMagic, 8) != 0) return fail(c, BIB_EINVAL, "%s is not a biblbm_gb300 checkpoint", path);
+    if (hd.version != kCkptVersion || hd.header_bytes != sizeof(CkptHeader) || hd.p_count != BIB_P_COUNT)
+        return fail(c, BIB_EUNSUPPORTED, "checkpoint format version %u is not supported", hd.version);
+    // the lattice must be configured as the one that was saved
+    const CkptHeader me = ckpt_header(*L);
+    const bool same = hd.nx == me.nx && hd.ny == me.ny && hd.nz == me.nz && hd.storage == me.storage &&
+                      hd.collision == me.collision && hd.use_phase == me.use_phase && hd.fd_walls == me.fd_walls &&
+                      hd.px == me.px && hd.py == me.py && hd.pz == me.pz && hd.wall_y == me.wall_y &&
+                      hd.wall_z == me.wall_z && hd.stride == me.stride && hd.omega == me.omega &&
+                      hd.omega_inner == me.omega_inner && hd.trt_magic == me.trt_magic && hd.scale == me.scale &&
+                      std::memcmp(hd.body, me.body, sizeof(hd.body)) == 0 &&
+                      std::memcmp(hd.wall_u, me.wall_u, sizeof(hd.wall_u)) == 0;
+    if (!same) return fail(c, BIB_EINVAL, "checkpoint was written by a lattice of another configuration");
+    if (hd.nparts < 0 || hd.nvert < 0 || hd.nvert > (int64_t)1 << 31 || hd.cur < 0 || hd.cur > 1 || hd.fe < 0 || hd.fe > 1)
+        return fail(c, BIB_EINVAL, "corrupt checkpoint header");
+    // read everything host-side first (particles) and validate it before touching the lattice
+    std::vector<unsigned char> buf;
+    const size_t pb = pop_bytes(L->storage) * Q * (size_t)L->d.stride;
+    const size_t fb = force_bytes(L->storage) * 3 * (size_t)L->d.stride;
+    const long body_at = ftell(F.f);
+    size_t skip = pb + wall_bytes(*L) + 2 * fb + (hd.use_phase ? (size_t)hd.stride : 0) + (hd.has_types ? (size_t)L->d.n : 0);
+    // pass 1: checksum of the whole file and the particle records
+    {
+        std::vector<unsigned char> tmp;
+        for (size_t o = 0; o < skip; o += kCkptChunk) {
+            const size_t n = std::min(kCkptChunk, skip - o);
+            tmp.resize(n);
+            if (!F.get(tmp.data(), n)) return fail(c, BIB_EINVAL, "checkpoint file is truncated");
+        }
+    }
+    std::vector<ParticleHost> parts(hd.nparts);
+    int64_t vtot = 0;
+    for (int32_t p = 0; p < hd.nparts; ++p) {
+        CkptParticle cp;
+        ParticleHost& ph = parts[p];
+        ph.prm.resize(BIB_P_COUNT);
+        if (!F.get(&cp, sizeof(cp)) || !F.get(ph.prm.data(), BIB_P_COUNT * sizeof(double)))
+            return fail(c, BIB_EINVAL, "checkpoint file is truncated");
+        if (cp.shape < 0 || cp.shape >= (int32_t)c->shapes.size())
+            return fail(c, BIB_EINVAL, "checkpoint particle %d uses shape %d, which this context does not hold", p, cp.shape);
+        const ShapeHost& S = *c->shapes[cp.shape];
+        if ((int32_t)(S.rest.size() / 3) != cp.nv || (int32_t)S.tri_area.size() != cp.nt)
+            return fail(c, BIB_EINVAL, "shape %d of this context does not match the checkpoint's (%d vertices, %d triangles)",
+                        cp.shape, cp.nv, cp.nt);
+        if (cp.model < BIB_MODEL_CAPSULE_NEOHOOKEAN || cp.model > BIB_MODEL_SKALAK_BENDING)
+            return fail(c, BIB_EINVAL, "corrupt checkpoint particle record");
+        ph.shape = cp.shape, ph.model = cp.model, ph.nv = cp.nv, ph.v0 = (int)vtot;
+        vtot += cp.nv;
+    }
+    if (vtot != hd.nvert) return fail(c, BIB_EINVAL, "corrupt checkpoint: vertex count");
+    const size_t vb = 3 * (size_t)vtot * sizeof(double);
+    std::vector<double> pos(3 * vtot), vel(3 * vtot), frc(3 * vtot), stats(STATS * (size_t)hd.nparts);
+    if (vtot && (!F.get(pos.data(), vb) || !F.get(vel.data(), vb) || !F.get(frc.data(), vb) ||
+                 !F.get(stats.data(), stats.size() * sizeof(double))))
+        return fail(c, BIB_EINVAL, "checkpoint file is truncated");
+    uint64_t sum = 0;
+    if (fread(&sum, 1, sizeof(sum), F.f) != sizeof(sum) || sum != F.sum.value())
+        return fail(c, BIB_EINVAL, "checkpoint checksum mismatch");
+    // pass 2: the lattice buffers straight into device memory
+    if (fseek(F.f, body_at, SEEK_SET) != 0) return fail(c, BIB_EINVAL, "checkpoint seek failed");
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    bib_status st;
+    if ((st = ckpt_get_device(c, F, L->f[hd.cur], pb, buf))) return st;
+    if (L->d.fd_walls && (st = ckpt_get_device(c, F, L->wall, wall_bytes(*L), buf))) return st;
+    for (int k = 0; k < 2; ++k)
+        if ((st = ckpt_get_device(c, F, L->F[k], fb, buf))) return st;
+    if (L->phase && (st = ckpt_get_device(c, F, L->phase, (size_t)L->d.stride, buf))) return st;
+    if (hd.has_types) {
+        std::vector<uint8_t> types((size_t)L->d.n);
+        if (!F.get(types.data(), types.size())) return fail(c, BIB_EINVAL, "checkpoint file is truncated");
+        for (uint8_t t : types)
+            if (t > BIB_CELL_NO_DYNAMICS) return fail(c, BIB_EINVAL, "corrupt checkpoint: cell type %d", (int)t);
+        if (!L->celltype) BIB_CUDA(c, cudaMalloc((void**)&L->celltype, (size_t)L->d.n));
+        BIB_CUDA(c, cudaMemcpy(L->celltype, types.data(), types.size(), cudaMemcpyHostToDevice));
+        L->d.has_types = 1;
+    } else if (L->celltype) {
+        cudaFree(L->celltype);
+        L->celltype = nullptr;
+        L->d.has_types = 0;
+    }
+    for (auto& B : c->batches)  // batch tables hold the lattice description and the particle set
+        if (B) B->free_tables();
+    L->cur = hd.cur;
+    L->fe = hd.fe;
+    L->target_clean = hd.target_clean != 0;
+    L->iteration = hd.iteration;
+    // particles: replace the lattice's set, upload, then restore velocities, forces and the
+    // per-particle area / volume / centre exactly as saved
+    L->parts = std::move(parts);
+    L->host_pos = std::move(pos);
+    L->host_stats = stats;
+    L->particles_dirty = true;
+    free_particles(*L);
+    L->nvert = 0;
+    if ((st = sync_particles(c, *L))) return st;
+    if (L->nvert) {
+        BIB_CUDA(c, cudaMemcpy(L->vel, vel.data(), vb, cudaMemcpyHostToDevice));
+        BIB_CUDA(c, cudaMemcpy(L->force, frc.data(), vb, cudaMemcpyHostToDevice));
+    }
+    drop_graphs(c, h);
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     return BIB_OK;
 }
 

@@ -203,6 +203,7 @@ struct Lattice {
     double* vox_z = nullptr;   // kVoxelCap heights per column, slot-major
     int* vox_err = nullptr;    // device word set when a column held more than kVoxelCap crossings
     uint64_t version = 0;     // bumped whenever the particle buffers are (re)allocated
+    uint64_t iteration = 0;   // steps taken (coupled, IB-only and collide-and-stream), kept in checkpoints
     int handle = -1;
 };
 

@@ -189,6 +189,8 @@ bib_status bib_ib_configure(bib_ctx* ctx, int32_t h, const bib_ib_params* p);
 bib_status bib_particle_add(bib_ctx* ctx, int32_t h, int32_t shape, int32_t model, const double* params,
                             const double* xyz, int32_t* pid);
 bib_status bib_particle_count(bib_ctx* ctx, int32_t h, int32_t* n);
+/* shape id, membrane model and vertex count of particle pid: out[0..2] */
+bib_status bib_particle_info(bib_ctx* ctx, int32_t h, int32_t pid, int32_t* out);
 bib_status bib_particle_get(bib_ctx* ctx, int32_t h, int32_t pid, double* pos, double* vel, double* force);
 bib_status bib_particle_set_positions(bib_ctx* ctx, int32_t h, int32_t pid, const double* pos);
 /* out[14] = {area, volume, com[3], moment of inertia[9]} (DeformableParticle3D.hh:54-82, 173-272) */
@@ -198,9 +200,27 @@ bib_status bib_particles_download(bib_ctx* ctx, int32_t h, double* pos, double* 
 bib_status bib_total_vertices(bib_ctx* ctx, int32_t h, int64_t* n);
 /* compute_total_volume, ImmersedBoundaryDynamics.hh:559-568 */
 bib_status bib_total_volume(bib_ctx* ctx, int32_t h, double* v);
+/* ImmersedBoundaryDynamics3D::init (ImmersedBoundaryDynamics.hh:404-412): upload the particles
+ * and, on a lattice with a phase field, voxelize them into it.  The first step does this by
+ * itself; the call makes the moment explicit (and synchronises). */
+bib_status bib_ibm_init(bib_ctx* ctx, int32_t h);
 /* One IB step on the current lattice state: velocity at the vertices, forces, spreading
  * into a force field reset to the body force, vertex motion (DataProcessors.hh:104-107). */
 bib_status bib_ibm_step(bib_ctx* ctx, int32_t h);
+/* steps taken by the lattice (bib_step, bib_ibm_step, collide-and-stream, batch steps); the
+ * counterpart of the reference's Time (Time.h:20-35), kept in checkpoints */
+bib_status bib_lattice_iteration(bib_ctx* ctx, int32_t h, int64_t* iteration);
+
+/* ---- checkpoints: parallelIO::save / load of the lattice (io/multiBlockWriter3D.cpp:201,
+ * io/multiBlockReader3D.cpp:261), save_checkpoint / load_checkpoint of the particles
+ * (ImmersedBoundaryDynamics_io.hh:17-158) and the iteration counter, in one versioned binary file
+ * per lattice.  Device buffers are stored in their own storage type: a resumed run continues
+ * bit for bit (with deterministic spreading).  Load needs a lattice created with the same
+ * parameters and a context holding the same shapes under the same ids; it replaces the lattice's
+ * particles.  Errors (BIB_EINVAL) leave the lattice unchanged, except a file that changes while it
+ * is being read. ---- */
+bib_status bib_checkpoint_save(bib_ctx* ctx, int32_t h, const char* path);
+bib_status bib_checkpoint_load(bib_ctx* ctx, int32_t h, const char* path);
 
 /* ---- coupled step: computeVelocity -> setExternalVector -> IB step -> collideAndStream ---- */
 bib_status bib_step(bib_ctx* ctx, int32_t h, int64_t nsteps);
