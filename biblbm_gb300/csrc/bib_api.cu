@@ -173,6 +173,9 @@ bool build_shape(ShapeHost& S, const double* xyz, const int64_t* tri, int64_t nv
         S.tri_area_f[t] = (float)S.tri_area[t];
     }
     S.pair_cs_f.assign(S.pair_cs.begin(), S.pair_cs.end());
+    S.tri4.assign(4 * nt, 0);
+    for (int64_t t = 0; t < nt; ++t)
+        for (int k = 0; k < 3; ++k) S.tri4[4 * t + k] = S.tri[3 * t + k];
     // per-vertex incidence lists for the deterministic force gather: links, then triangles,
     // then pairs, each in element order (the order of the reference's element loops)
     std::vector<std::vector<int>> incv(nv);
@@ -372,6 +375,7 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
         d.inc_off = S.dev.inc_off;
         d.inc = S.dev.inc;
         d.tri_rest_f = S.dev.tri_rest_f;
+        d.tri4 = S.dev.tri4;
         d.tri_area_f = S.dev.tri_area_f;
         d.pair_cs_f = S.dev.pair_cs_f;
         d.inst = 0;
@@ -995,6 +999,7 @@ void bib_destroy(bib_ctx* c) {
         cudaFree(S->dev.inc_off);
         cudaFree(S->dev.inc);
         cudaFree(S->dev.tri_rest_f);
+        cudaFree(S->dev.tri4);
         cudaFree(S->dev.tri_area_f);
         cudaFree(S->dev.pair_cs_f);
     }
@@ -1494,7 +1499,8 @@ bib_status bib_shape_store(bib_ctx* c, const double* xyz, const int64_t* tri, in
         (st = upload(c, &S->dev.link_len, S->link_len)) || (st = upload(c, &S->dev.pairs, S->pairs)) ||
         (st = upload(c, &S->dev.pair_cs, S->pair_cs)) || (st = upload(c, &S->dev.inc_off, S->inc_off)) ||
         (st = upload(c, &S->dev.inc, S->inc)) || (st = upload(c, &S->dev.tri_rest_f, S->tri_rest_f)) ||
-        (st = upload(c, &S->dev.tri_area_f, S->tri_area_f)) || (st = upload(c, &S->dev.pair_cs_f, S->pair_cs_f)))
+        (st = upload(c, &S->dev.tri_area_f, S->tri_area_f)) || (st = upload(c, &S->dev.pair_cs_f, S->pair_cs_f)) ||
+        (st = upload(c, &S->dev.tri4, S->tri4)))
         return st;
     S->dev.nv = (int)nv;
     S->dev.nt = (int)nt;

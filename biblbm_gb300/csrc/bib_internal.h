@@ -45,6 +45,7 @@ struct ShapeDev {
     double area, volume;  // rest area A0 and volume V0
     double* rest;         // 3*nv
     int* tri;             // 3*nt
+    int* tri4;            // 4*nt: the corners of each triangle and a pad, for 16-byte loads
     double* tri_area;     // nt
     int* links;           // 2*nl
     double* link_len;     // nl
@@ -65,6 +66,7 @@ struct ParticleDev {
     int nt, nl, np;
     const double* rest;
     const int* tri;
+    const int* tri4;
     const double* tri_area;
     const int* links;
     const double* link_len;
@@ -133,7 +135,7 @@ struct CollideView {
 
 struct ShapeHost {
     std::vector<double> rest, tri_area, link_len, pair_cs;
-    std::vector<int> tri, links, pairs, inc_off, inc;
+    std::vector<int> tri, tri4, links, pairs, inc_off, inc;
     std::vector<float> tri_rest_f, tri_area_f, pair_cs_f;
     double area = 0, volume = 0;
     ShapeDev dev{};

@@ -15,16 +15,34 @@ namespace bib {
 
 namespace {
 
+// Reduced-precision arithmetic: the FP32 element and weight evaluations use the hardware's
+// approximate square root, reciprocal and division (a few ulp); FP64 keeps the IEEE
+// operations of the reference's expressions.
+__device__ __forceinline__ float fast_sqrt(float x) {
+    float r;
+    asm("sqrt.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ double fast_sqrt(double x) { return sqrt(x); }
+__device__ __forceinline__ float fast_rcp(float x) {
+    float r;
+    asm("rcp.approx.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ double fast_rcp(double x) { return 1.0 / x; }
+__device__ __forceinline__ float fast_div(float a, float b) { return __fdividef(a, b); }
+__device__ __forceinline__ double fast_div(double a, double b) { return a / b; }
+
 // ---------------------------------------------------------------- delta kernels
 // RomaDirac<T,3>::eval and PeskinDirac<T,3>::eval(x), src/fsi/Dirac.h:27-31, 78-83
 template <class W>
 __device__ __forceinline__ W dirac_eval(int dirac, W x) {
     const W dx = fabs(x);
     if (dirac == BIB_DIRAC_PESKIN)
-        return W(0.125) * (dx <= W(1) ? (W(3) - W(2) * dx + sqrt(W(1) + W(4) * dx * (W(1) - dx)))
-                                      : (W(5) - W(2) * dx - sqrt(W(-7) + W(4) * dx * (W(3) - dx))));
-    return (W(1) / W(6)) * (dx > W(0.5) ? (W(5) - W(3) * dx - sqrt(W(-3) * (W(1) - dx) * (W(1) - dx) + W(1)))
-                                        : W(2) * (W(1) + sqrt(W(1) - W(3) * dx * dx)));
+        return W(0.125) * (dx <= W(1) ? (W(3) - W(2) * dx + fast_sqrt(W(1) + W(4) * dx * (W(1) - dx)))
+                                      : (W(5) - W(2) * dx - fast_sqrt(W(-7) + W(4) * dx * (W(3) - dx))));
+    return (W(1) / W(6)) * (dx > W(0.5) ? (W(5) - W(3) * dx - fast_sqrt(W(-3) * (W(1) - dx) * (W(1) - dx) + W(1)))
+                                        : W(2) * (W(1) + fast_sqrt(W(1) - W(3) * dx * dx)));
 }
 
 __device__ __forceinline__ double half_support(int dirac) { return dirac == BIB_DIRAC_PESKIN ? 2.0 : 1.5; }
@@ -135,17 +153,12 @@ __device__ __forceinline__ U3<double> load_u(const double* u, int64_t k) {
 // interpolators, ImmersedBoundaryDynamics_interpolation.hh:13-153.
 // One thread per vertex.  BATCH: the vertex numbering runs over the lattices of a batch and
 // each thread looks its lattice's view up through vinst; otherwise v1 is the lattice.
-template <class UT, int S, bool BATCH>
-__global__ void __launch_bounds__(128) k_interpolate_move(IbView v1, const IbView* __restrict__ views,
-                                                           const int* __restrict__ vinst, int nvert) {
+template <class UT, int S>
+__device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) {
     using C = UT;
     static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
-    const int g = blockIdx.x * blockDim.x + threadIdx.x;
-    if (g >= nvert) return;
-    const IbView& V = BATCH ? views[vinst[g]] : v1;
     const LatticeDesc& d = V.d;
     const IbDesc& ib = V.ib;
-    const int v = BATCH ? g - V.vbase : g;
     const double* __restrict__ pos = V.pos;
     double* __restrict__ pos_next = V.pos_next;
     const UT* __restrict__ u = static_cast<const UT*>(V.u);
@@ -203,17 +216,21 @@ __global__ void __launch_bounds__(128) k_interpolate_move(IbView v1, const IbVie
     pos_next[3 * v + 2] = p[2] + out[2];
 }
 
-// ---------------------------------------------------------------- spreading
-template <class FT, int S, bool BATCH>
-__global__ void __launch_bounds__(128) k_spread(IbView v1, const IbView* __restrict__ views, const int* __restrict__ vinst,
-                                                 int nvert) {
-    static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
+template <class UT, int S, bool BATCH>
+__global__ void __launch_bounds__(128) k_interpolate_move(IbView v1, const IbView* __restrict__ views,
+                                                           const int* __restrict__ vinst, int nvert) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nvert) return;
     const IbView& V = BATCH ? views[vinst[g]] : v1;
+    interpolate_move_vertex<UT, S>(V, BATCH ? g - V.vbase : g);
+}
+
+// ---------------------------------------------------------------- spreading
+template <class FT, int S>
+__device__ __forceinline__ void spread_vertex(const IbView& V, int v) {
+    static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
     const LatticeDesc& d = V.d;
     const IbDesc& ib = V.ib;
-    const int v = BATCH ? g - V.vbase : g;
     const double* __restrict__ pos = V.pos;
     const double* __restrict__ force = V.force;
     FT* __restrict__ F = static_cast<FT*>(V.F);
@@ -279,6 +296,15 @@ __global__ void __launch_bounds__(128) k_spread(IbView v1, const IbView* __restr
             }
         }
     }
+}
+
+template <class FT, int S, bool BATCH>
+__global__ void __launch_bounds__(128) k_spread(IbView v1, const IbView* __restrict__ views, const int* __restrict__ vinst,
+                                                 int nvert) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= nvert) return;
+    const IbView& V = BATCH ? views[vinst[g]] : v1;
+    spread_vertex<FT, S>(V, BATCH ? g - V.vbase : g);
 }
 
 // Deterministic spreading.  Every (vertex, stencil node) pair becomes an entry keyed by its
@@ -366,7 +392,13 @@ __device__ __forceinline__ V3<M> operator/(V3<M> a, M s) { return mk3(a.x / s, a
 template <class M>
 __device__ __forceinline__ M dot3(V3<M> a, V3<M> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
 template <class M>
-__device__ __forceinline__ M norm3(V3<M> a) { return sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+__device__ __forceinline__ M norm3(V3<M> a) { return fast_sqrt(a.x * a.x + a.y * a.y + a.z * a.z); }
+// a / s: one approximate reciprocal in FP32, the three IEEE divisions in FP64
+template <class M>
+__device__ __forceinline__ V3<M> div3(V3<M> a, M s) {
+    if constexpr (sizeof(M) == sizeof(float)) return fast_rcp(s) * a;
+    else return a / s;
+}
 template <class M>
 __device__ __forceinline__ V3<M> cross3(V3<M> a, V3<M> b) {
     return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
@@ -445,9 +477,9 @@ __device__ __forceinline__ M pair_c(const ParticleDev& P, int p, int k) {
 // (with the reference's c = l' sin(phi) / (l' sin(phi0)), line 96).  The rest-state lengths
 // and angle come from the FP64 rest mesh (M = double) or its FP32 copies.
 template <class M, class PS, class Sink>
-__device__ void capsule_triangle(const ParticleDev& P, int t, const PS& ps, int skalak, const MemCoef<M>& k,
+__device__ void capsule_triangle(const ParticleDev& P, int t, int4 ti, const PS& ps, int skalak, const MemCoef<M>& k,
                                  Sink& sk) {
-    const int i0 = P.tri[3 * t], i1 = P.tri[3 * t + 1], i2 = P.tri[3 * t + 2];
+    const int i0 = ti.x, i1 = ti.y, i2 = ti.z;
     const int id[3] = {i0, i1, i2};
     const V3<M> p0 = ps(i0), p1 = ps(i1), p2 = ps(i2);
     const V3<M> e0 = p1 - p0, e1 = p2 - p0;
@@ -475,7 +507,7 @@ __device__ void capsule_triangle(const ParticleDev& P, int t, const PS& ps, int 
         // reciprocals are taken once.
         const M l = norm3(e0), lp = norm3(e1);
         const M e0e1 = dot3(e0, e1), cr = norm3(cross3(e0, e1));
-        const M rl = M(1) / l, rlp = M(1) / lp, rl0 = M(1) / l0, rl0p = M(1) / l0p, rs0 = M(1) / sin_phi_0;
+        const M rl = fast_rcp(l), rlp = fast_rcp(lp), rl0 = fast_rcp(l0), rl0p = fast_rcp(l0p), rs0 = fast_rcp(sin_phi_0);
         const M rllp = rl * rlp;
         const M sin_phi = cr * rllp, cos_phi = e0e1 * rllp;
         const M a = l * rl0;
@@ -493,7 +525,7 @@ __device__ void capsule_triangle(const ParticleDev& P, int t, const PS& ps, int 
         } else {
             const M q = M(1) + I2;
             w1 = M(1);
-            w2 = -M(1) / (q * q);
+            w2 = -fast_rcp(q * q);
         }
         const M A11 = l * rl0 * rl0, s2 = rs0 * rs0;
         const M k22p = s2 * (lp * rl0p * rl0p - l * cos_phi * cos_phi_0 * rl0 * rl0p);
@@ -580,16 +612,16 @@ __device__ void rbc_link(const ParticleDev& P, int l, const PS& ps, Sink& sk) {
 // tri::grad_signed_volume (TriangleUtils.h:58-120).  The volume gradient is
 // translation invariant on a closed surface, so it is taken relative to the centre.
 template <class M, class PS, class Sink>
-__device__ void rbc_triangle(const ParticleDev& P, int t, const PS& ps, const MemCoef<M>& k, Sink& sk) {
-    const int i0 = P.tri[3 * t], i1 = P.tri[3 * t + 1], i2 = P.tri[3 * t + 2];
+__device__ void rbc_triangle(const ParticleDev& P, int t, int4 ti, const PS& ps, const MemCoef<M>& k, Sink& sk) {
+    const int i0 = ti.x, i1 = ti.y, i2 = ti.z;
     const V3<M> v0 = ps(i0), v1 = ps(i1), v2 = ps(i2);
     const M v01v11 = v0.y - v1.y, v02v22 = v0.z - v2.z, v02v12 = v0.z - v1.z;
     const M v01v21 = v0.y - v2.y, v00v20 = v0.x - v2.x, v00v10 = v0.x - v1.x;
     const M a = v01v11 * v02v22 - v02v12 * v01v21;
     const M b = v02v12 * v00v20 - v00v10 * v02v22;
     const M c = v00v10 * v01v21 - v01v11 * v00v20;
-    const M la = M(0.5) * sqrt(a * a + b * b + c * c);
-    const M denom = M(1) / (M(4) * la);
+    const M la = M(0.5) * fast_sqrt(a * a + b * b + c * c);
+    const M denom = fast_div(M(1), M(4) * la);
     const V3<M> g0 = mk3<M>((b * (v2.z - v1.z) + c * (v1.y - v2.y)) * denom, (a * (v1.z - v2.z) + c * (v2.x - v1.x)) * denom,
                             (a * (v2.y - v1.y) + b * (v1.x - v2.x)) * denom);
     const V3<M> g1 = mk3<M>((b * v02v22 + c * (v2.y - v0.y)) * denom, (a * (v2.z - v0.z) + c * v00v20) * denom,
@@ -599,7 +631,7 @@ __device__ void rbc_triangle(const ParticleDev& P, int t, const PS& ps, const Me
     // the global penalty differences are evaluated once per particle, in FP64
     const M a0t = tri_area_of<M>(P, t);
     M df_area = k.df_area_global;
-    df_area += k.k_area_local * (a0t - la) / a0t;
+    df_area += fast_div(k.k_area_local * (a0t - la), a0t);
     sk(i0, df_area * g0);
     sk(i1, df_area * g1);
     sk(i2, df_area * g2);
@@ -612,21 +644,29 @@ __device__ void rbc_triangle(const ParticleDev& P, int t, const PS& ps, const Me
 // tri::grad_angle_between_pair (TriangleUtils.h:139-164).
 template <class M, class PS, class Sink>
 __device__ void rbc_pair(const ParticleDev& P, int p, const PS& ps, const MemCoef<M>& k, Sink& sk) {
-    const int* q = P.pairs + 4 * p;
+    const int4 qq = __ldg(reinterpret_cast<const int4*>(P.pairs) + p);
+    const int q[4] = {qq.x, qq.y, qq.z, qq.w};
     const V3<M> v0 = ps(q[0]), v1 = ps(q[1]), v2 = ps(q[2]), v3 = ps(q[3]);
     const V3<M> e0 = v1 - v0, e1 = v2 - v0, e2 = v3 - v0;
     const M e1n = norm3(e1);
-    const V3<M> e1u = e1 / e1n;
+    const V3<M> e1u = div3(e1, e1n);
     const V3<M> n1 = cross3(e0, e1), n2 = cross3(e1, e2);
     const M n1n = norm3(n1), n2n = norm3(n2);
-    const V3<M> n1u = n1 / n1n, n2u = n2 / n2n;
+    const V3<M> n1u = div3(n1, n1n), n2u = div3(n2, n2n);
     const M cos_t = dot3(n1u, n2u);
     const M sin_t = (dot3(n1 - n2, v1 - v3) > M(0) ? M(1) : M(-1)) * norm3(cross3(n1u, n2u));
-    const M pref = k.kb * (-pair_c<M>(P, p, 0) * sin_t + pair_c<M>(P, p, 1) * cos_t);
-    sk(q[0], pref * ((dot3(e1u, e1 - e2) / n2n) * n2u + (dot3(e1u, e1 - e0) / n1n) * n1u));
-    sk(q[1], pref * ((-e1n / n1n) * n1u));
-    sk(q[2], pref * ((dot3(e1u, e2) / n2n) * n2u + (dot3(e1u, e0) / n1n) * n1u));
-    sk(q[3], pref * ((-e1n / n2n) * n2u));
+    M c0, c1;
+    if constexpr (sizeof(M) == sizeof(float)) {
+        const float2 cs = __ldg(reinterpret_cast<const float2*>(P.pair_cs_f) + p);
+        c0 = cs.x, c1 = cs.y;
+    } else {
+        c0 = pair_c<M>(P, p, 0), c1 = pair_c<M>(P, p, 1);
+    }
+    const M pref = k.kb * (-c0 * sin_t + c1 * cos_t);
+    sk(q[0], pref * (fast_div(dot3(e1u, e1 - e2), n2n) * n2u + fast_div(dot3(e1u, e1 - e0), n1n) * n1u));
+    sk(q[1], pref * (fast_div(-e1n, n1n) * n1u));
+    sk(q[2], pref * (fast_div(dot3(e1u, e2), n2n) * n2u + fast_div(dot3(e1u, e0), n1n) * n1u));
+    sk(q[3], pref * (fast_div(-e1n, n2n) * n2u));
 }
 
 // Forces on the three corners of one triangle, summed in registers and handed on once.
@@ -641,30 +681,11 @@ struct CornerSink {
     }
 };
 
-template <class T>
-__device__ __forceinline__ T block_sum(T v, T* red) {
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    __syncthreads();
-    if (lane == 0) red[warp] = v;
-    __syncthreads();
-    T r = T(0);
-    if (threadIdx.x < 32) {
-        r = threadIdx.x < (blockDim.x >> 5) ? red[threadIdx.x] : T(0);
-        for (int o = 16; o > 0; o >>= 1) r += __shfl_down_sync(0xffffffffu, r, o);
-    }
-    return r;  // valid in thread 0
-}
-
 // One CTA per particle: vertex forces at X_n (ParticleBase3D::reset_forces +
 // compute_forces), accumulated in shared memory.
-template <class M, bool BATCH>
-__global__ void __launch_bounds__(512) k_membrane(const ParticleDev* __restrict__ parts, IbView v1,
-                                                   const IbView* __restrict__ views) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
+template <class M>
+__device__ __forceinline__ void membrane_block(const ParticleDev& P, const IbView& V, unsigned char* smem_raw) {
     M* sf = reinterpret_cast<M*>(smem_raw);
-    const ParticleDev& P = parts[blockIdx.x];
-    const IbView& V = BATCH ? views[P.inst] : v1;
     const double* __restrict__ pos = V.pos;
     double* __restrict__ force = V.force;
     const double* st = V.stats + STATS * P.lpid;
@@ -677,24 +698,33 @@ __global__ void __launch_bounds__(512) k_membrane(const ParticleDev* __restrict_
     M* sp = sf + 3 * P.nv;
     if (rel) {
         const double* pp = pos + 3LL * P.v0;
-        for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sp[i] = (M)(pp[i] - st[2 + i % 3]);
+        const double c[3] = {st[2], st[3], st[4]};
+        for (int i = threadIdx.x; i < P.nv; i += blockDim.x) {
+            sp[3 * i] = (M)(pp[3 * i] - c[0]);
+            sp[3 * i + 1] = (M)(pp[3 * i + 1] - c[1]);
+            sp[3 * i + 2] = (M)(pp[3 * i + 2] - c[2]);
+        }
     }
+    // the per-particle constants (FP64 divisions) once per CTA
+    __shared__ MemCoef<M> kc;
+    if (threadIdx.x == 0) kc = mem_coef<M>(P, area, volume);
     __syncthreads();
     AtomicSink<M> sk{sf};
     const int skalak = P.model != BIB_MODEL_CAPSULE_NEOHOOKEAN;
     const bool capsule = P.model == BIB_MODEL_CAPSULE_NEOHOOKEAN || P.model == BIB_MODEL_CAPSULE_SKALAK ||
                          P.model == BIB_MODEL_SKALAK_BENDING;
     const bool rbc_terms = P.model == BIB_MODEL_RBC_WLCPOW || P.model == BIB_MODEL_SKALAK_BENDING;
-    const MemCoef<M> k = mem_coef<M>(P, area, volume);
+    const MemCoef<M> k = kc;
     auto run = [&](const auto& ps) {
         // triangle terms (capsule law and RBC area / volume penalties) of one triangle are
         // summed per corner before they reach the shared accumulators
         if (capsule || rbc_terms)
             for (int t = threadIdx.x; t < P.nt; t += blockDim.x) {
                 const V3<M> z = mk3<M>(0, 0, 0);
-                CornerSink<M> cs{{P.tri[3 * t], P.tri[3 * t + 1], P.tri[3 * t + 2]}, {z, z, z}};
-                if (capsule) capsule_triangle<M>(P, t, ps, skalak, k, cs);
-                if (rbc_terms) rbc_triangle<M>(P, t, ps, k, cs);
+                const int4 ti = __ldg(reinterpret_cast<const int4*>(P.tri4) + t);
+                CornerSink<M> cs{{ti.x, ti.y, ti.z}, {z, z, z}};
+                if (capsule) capsule_triangle<M>(P, t, ti, ps, skalak, k, cs);
+                if (rbc_terms) rbc_triangle<M>(P, t, ti, ps, k, cs);
                 for (int c = 0; c < 3; ++c) sk(cs.id[c], cs.f[c]);
             }
         if (P.model == BIB_MODEL_RBC_WLCPOW)
@@ -706,6 +736,14 @@ __global__ void __launch_bounds__(512) k_membrane(const ParticleDev* __restrict_
     else run(GlobalPos<M>{pos + 3LL * P.v0, {0.0, 0.0, 0.0}});
     __syncthreads();
     for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) force[3LL * P.v0 + i] = (double)sf[i];
+}
+
+template <class M, bool BATCH>
+__global__ void __launch_bounds__(512) k_membrane(const ParticleDev* __restrict__ parts, IbView v1,
+                                                   const IbView* __restrict__ views) {
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    const ParticleDev& P = parts[blockIdx.x];
+    membrane_block<M>(P, BATCH ? views[P.inst] : v1, smem_raw);
 }
 
 // Deterministic membrane forces: one thread per vertex sums the contributions of its
@@ -743,8 +781,9 @@ __global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* _
         if (type == INC_LINK) {
             if (P.model == BIB_MODEL_RBC_WLCPOW) rbc_link<M>(P, id, ps, rbc);
         } else if (type == INC_TRI) {
-            if (capsule) capsule_triangle<M>(P, id, ps, skalak, k, cap);
-            if (rbc_terms) rbc_triangle<M>(P, id, ps, k, rbc);
+            const int4 ti = __ldg(reinterpret_cast<const int4*>(P.tri4) + id);
+            if (capsule) capsule_triangle<M>(P, id, ti, ps, skalak, k, cap);
+            if (rbc_terms) rbc_triangle<M>(P, id, ti, ps, k, rbc);
         } else if (type == INC_PAIR && rbc_terms) {
             rbc_pair<M>(P, id, ps, k, rbc);
         }
@@ -763,22 +802,39 @@ __global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* _
 // relative to the previous centre of mass (exact FP64 subtraction, then rounding) and
 // accumulates in FP64; the signed volume of the closed surface does not depend on the
 // origin.
-template <class M, bool BATCH>
-__global__ void __launch_bounds__(256) k_particle_update(const ParticleDev* __restrict__ parts, IbView v1,
-                                                          const IbView* __restrict__ views) {
-    __shared__ double red[32];
-    __shared__ double delta[3];
-    extern __shared__ __align__(16) float sp[];  // M = float: relative vertex positions
-    const ParticleDev& P = parts[blockIdx.x];
-    const IbView& V = BATCH ? views[P.inst] : v1;
+// Sums of five per-thread values over the block into out[0..4] (shared): the partials go
+// to red (5 x blockDim.x doubles), then one warp per quantity adds them up.
+__device__ __forceinline__ void block_sum5(const double v[5], double* red, double* out) {
+    const int n = blockDim.x, t = threadIdx.x;
+#pragma unroll
+    for (int k = 0; k < 5; ++k) red[k * n + t] = v[k];
+    __syncthreads();
+    const int lane = t & 31, nw = n >> 5;
+    for (int q = t >> 5; q < 5; q += nw) {
+        double s = 0.0;
+        for (int i = lane; i < n; i += 32) s += red[q * n + i];
+        for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+        if (lane == 0) out[q] = s;
+    }
+    __syncthreads();
+}
+
+template <class M>
+__device__ __forceinline__ void update_block(const ParticleDev& P, const IbView& V, float* sp, double* red,
+                                             double* delta) {
+    __shared__ double sum[5];
     const LatticeDesc& d = V.d;
-    double* __restrict__ pos_next = V.pos_next;
+    double* pos_next = V.pos_next;
     double* st = V.stats + STATS * P.lpid;
     const bool rel = sizeof(M) < sizeof(double);
     const double c0 = rel ? st[2] : 0.0, c1 = rel ? st[3] : 0.0, c2 = rel ? st[4] : 0.0;
     const double* pv = pos_next + 3LL * P.v0;
     if (rel) {  // one FP64 subtraction and rounding per vertex coordinate
-        for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sp[i] = (float)(pv[i] - (i % 3 == 0 ? c0 : (i % 3 == 1 ? c1 : c2)));
+        for (int i = threadIdx.x; i < P.nv; i += blockDim.x) {
+            sp[3 * i] = (float)(pv[3 * i] - c0);
+            sp[3 * i + 1] = (float)(pv[3 * i + 1] - c1);
+            sp[3 * i + 2] = (float)(pv[3 * i + 2] - c2);
+        }
         __syncthreads();
     }
     auto vert = [&](int i) {
@@ -788,7 +844,8 @@ __global__ void __launch_bounds__(256) k_particle_update(const ParticleDev* __re
     // per-thread partial sums in M (a few triangles each), block sums in FP64
     M ta = 0, tv = 0, tcx = 0, tcy = 0, tcz = 0;
     for (int t = threadIdx.x; t < P.nt; t += blockDim.x) {
-        const V3<M> A = vert(P.tri[3 * t]), B = vert(P.tri[3 * t + 1]), Cv = vert(P.tri[3 * t + 2]);
+        const int4 ti = __ldg(reinterpret_cast<const int4*>(P.tri4) + t);
+        const V3<M> A = vert(ti.x), B = vert(ti.y), Cv = vert(ti.z);
         const M dA = norm3(cross3(B - A, Cv - A)) * M(0.5);
         ta += dA;
         // multiplications by 1/6 and 1/3 instead of the reference's divisions (FP64 division
@@ -799,18 +856,11 @@ __global__ void __launch_bounds__(256) k_particle_update(const ParticleDev* __re
         tcy += cen.y * dA;
         tcz += cen.z * dA;
     }
-    double sa = (double)ta, sv = (double)tv, scx = (double)tcx, scy = (double)tcy, scz = (double)tcz;
-    sa = block_sum(sa, red);
-    __syncthreads();
-    sv = block_sum(sv, red);
-    __syncthreads();
-    scx = block_sum(scx, red);
-    __syncthreads();
-    scy = block_sum(scy, red);
-    __syncthreads();
-    scz = block_sum(scz, red);
+    const double part[5] = {(double)ta, (double)tv, (double)tcx, (double)tcy, (double)tcz};
+    block_sum5(part, red, sum);
     if (threadIdx.x == 0) {
-        const double com[3] = {c0 + scx / sa, c1 + scy / sa, c2 + scz / sa};
+        const double sa = sum[0], sv = sum[1];
+        const double com[3] = {c0 + sum[2] / sa, c1 + sum[3] / sa, c2 + sum[4] / sa};
         const int N[3] = {d.nx, d.ny, d.nz};
         const int per[3] = {d.px, d.py, d.pz};
         double np_[3];
@@ -834,6 +884,16 @@ __global__ void __launch_bounds__(256) k_particle_update(const ParticleDev* __re
             pos_next[g + 2] += delta[2];
         }
     }
+}
+
+template <class M, bool BATCH>
+__global__ void __launch_bounds__(256) k_particle_update(const ParticleDev* __restrict__ parts, IbView v1,
+                                                          const IbView* __restrict__ views) {
+    __shared__ double red[5 * 256];
+    __shared__ double delta[3];
+    extern __shared__ __align__(16) float sp[];  // M = float: relative vertex positions
+    const ParticleDev& P = parts[blockIdx.x];
+    update_block<M>(P, BATCH ? views[P.inst] : v1, sp, red, delta);
 }
 
 // ---------------------------------------------------------------- voxelization
