@@ -863,11 +863,12 @@ static void rbc_forces(const double* prm, int64_t nt, const int64_t* tri, const 
     }
 }
 
-void orc_membrane_forces(int32_t model, const double* prm, int64_t nv, const double* rest, int64_t nt,
-                         const int64_t* tri, const double* tri_area, double A0, int64_t nl, const int64_t* links,
-                         const double* link_len, int64_t np, const int64_t* pairs, const double* pair_cs,
-                         const double* pos, double area, double volume, double* force) {
-    memset(force, 0, sizeof(double) * 3 * nv);
+/* The element forces added onto `force` (which holds, e.g., the wall-interaction forces the
+ * decorators applied first, ImmersedBoundaryDynamics_forces.hh:293-296). */
+static void membrane_forces_acc(int32_t model, const double* prm, int64_t nv, const double* rest, int64_t nt,
+                                const int64_t* tri, const double* tri_area, double A0, int64_t nl, const int64_t* links,
+                                const double* link_len, int64_t np, const int64_t* pairs, const double* pair_cs,
+                                const double* pos, double area, double volume, double* force) {
     if (model == ORC_MODEL_CAPSULE_NEOHOOKEAN || model == ORC_MODEL_CAPSULE_SKALAK) {
         capsule_forces(model == ORC_MODEL_CAPSULE_SKALAK, prm[ORC_P_G], prm[ORC_P_C], rest, nt, tri, tri_area, pos, force);
     } else if (model == ORC_MODEL_RBC_WLCPOW) {
@@ -885,6 +886,183 @@ void orc_membrane_forces(int32_t model, const double* prm, int64_t nv, const dou
         for (int64_t i = 0; i < 3 * nv; ++i) force[i] += extra[i];
         free(extra);
     }
+}
+
+void orc_membrane_forces(int32_t model, const double* prm, int64_t nv, const double* rest, int64_t nt,
+                         const int64_t* tri, const double* tri_area, double A0, int64_t nl, const int64_t* links,
+                         const double* link_len, int64_t np, const int64_t* pairs, const double* pair_cs,
+                         const double* pos, double area, double volume, double* force) {
+    memset(force, 0, sizeof(double) * 3 * nv);
+    membrane_forces_acc(model, prm, nv, rest, nt, tri, tri_area, A0, nl, links, link_len, np, pairs, pair_cs, pos,
+                        area, volume, force);
+}
+
+/* ------------------------------------------------------------------ interaction forces */
+/* MorsePotential::eval and SpringPotential::operator() (fsi/Potentials.h:29-71): the force
+ * magnitude at distance d, positive = repulsive; both are cut off at r0 (get_cutoff_distance). */
+double orc_potential_eval(const orc_potential* p, double d) {
+    if (p->kind == ORC_POTENTIAL_MORSE) {
+        if (d < 0) d = 0.0;
+        const double x = exp(p->beta * (p->r0 - d));
+        return 2 * p->beta * p->strength * x * (x - 1);
+    }
+    if (p->kind == ORC_POTENTIAL_SPRING) return (p->r0 - d) * p->strength;
+    return 0.0;
+}
+
+/* WallInteraction::apply_force (ForceDecorator.hh:25-32) with ParallelPlatesBoundary(lo, hi) on
+ * `axis` (Boundary.h:305-365, plates normal to y there): distance to the nearer plate, outward
+ * normal; force -= phi(dist) * normal for dist <= cutoff. */
+void orc_wall_forces(const orc_potential* p, int32_t axis, double lo, double hi, int64_t nv, const double* pos,
+                     double* force) {
+    for (int64_t i = 0; i < nv; ++i) {
+        const double r = pos[3 * i + axis];
+        const int lower = r < 0.5 * (lo + hi);
+        const double dist = lower ? r - lo : hi - r;
+        if (dist <= p->r0) {
+            const double f = orc_potential_eval(p, dist);
+            double n[3] = {0.0, 0.0, 0.0};
+            n[axis] = lower ? -1.0 : 1.0;
+            for (int d = 0; d < 3; ++d) force[3 * i + d] -= f * n[d];
+        }
+    }
+}
+
+/* Arithmetic1D::min_mod_diff (Periodicity.h:27-35, 96-99) on periodic axes, x - y otherwise */
+static double axis_diff(const orc_lattice* L, int a, double x, double y) {
+    const int64_t N = a == 0 ? L->nx : (a == 1 ? L->ny : L->nz);
+    const double d = x - y;
+    if (!L->periodic[a]) return d;
+    const double Ld = (double)N, Linv = 1.0 / Ld;
+    return d - floor(d * Linv + 0.5) * Ld;
+}
+
+/* CollisionHandler::handle_collision (CollisionForces.h:187-199) */
+static void pp_pair(const orc_lattice* L, const orc_potential* p, double c2, const double* xa, const double* xb,
+                    double* fa, double* fb) {
+    const double dr[3] = {axis_diff(L, 0, xb[0], xa[0]), axis_diff(L, 1, xb[1], xa[1]), axis_diff(L, 2, xb[2], xa[2])};
+    const double dsq = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+    if (dsq <= c2) {
+        const double dist = sqrt(dsq);
+        const double s = -orc_potential_eval(p, dist) / dist;
+        for (int d = 0; d < 3; ++d) {
+            const double df = s * dr[d];
+            fa[d] += df;
+            fb[d] -= df;
+        }
+    }
+}
+
+/* Particle-particle forces as the reference evaluates them
+ * (compute_particle_particle_interaction_impl, ImmersedBoundaryDynamics_forces.hh:330-375, with
+ * CollisionHandler::compute_collision_forces, CollisionForces.h:63-164, and Grid, Grid.hh):
+ * nodes inside the lattice box enlarged by 1/2 + cutoff go into a grid of ~unit cells over the
+ * box in particle / vertex order; every bulk cell pairs its nodes among themselves and with the
+ * nodes of 7 neighbour cells (+y, +y+z, +z, +x, +x+y, +x+y+z, +x+z), then the first and last
+ * bulk layers of each periodic axis are paired.  Pairs whose cells sit at other offsets (e.g.
+ * +x-y) are not examined: orc_pp_forces below takes every pair within the cutoff. */
+void orc_pp_forces_grid(const orc_lattice* L, const orc_potential* p, int64_t nv, const double* pos,
+                        const int32_t* owner, double* force) {
+    const int64_t N[3] = {L->nx, L->ny, L->nz};
+    const double cut = p->r0, c2 = cut * cut;
+    double b0[3], b1[3], cs[3], g0[3];
+    int64_t nc[3];
+    for (int a = 0; a < 3; ++a) {
+        b0[a] = 0 - 0.5;
+        b1[a] = (double)(N[a] - 1) + 0.5 - DBL_EPSILON;
+        nc[a] = (int64_t)floor((b1[a] - b0[a]) / 1.0);
+        cs[a] = (b1[a] - b0[a]) / (double)nc[a];
+        nc[a] += 2;
+        g0[a] = b0[a] - cs[a];
+    }
+    const int64_t ncell = nc[0] * nc[1] * nc[2];
+    int64_t* count = (int64_t*)calloc((size_t)ncell + 1, sizeof(int64_t));
+    int64_t* cell_of = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nv > 0 ? nv : 1));
+    for (int64_t i = 0; i < nv; ++i) {
+        const double* x = pos + 3 * i;
+        int in = 1;
+        for (int a = 0; a < 3; ++a) in = in && x[a] > b0[a] - cut && x[a] < b1[a] + cut;
+        cell_of[i] = -1;
+        if (!in) continue;
+        int64_t ci[3];
+        for (int a = 0; a < 3; ++a) ci[a] = (int64_t)floor((x[a] - g0[a]) / cs[a]);
+        cell_of[i] = ci[2] + nc[2] * (ci[1] + nc[1] * ci[0]);
+        count[cell_of[i] + 1]++;
+    }
+    for (int64_t c = 0; c < ncell; ++c) count[c + 1] += count[c];
+    int64_t* fill = (int64_t*)malloc(sizeof(int64_t) * (size_t)ncell);
+    int64_t* node = (int64_t*)malloc(sizeof(int64_t) * (size_t)(count[ncell] > 0 ? count[ncell] : 1));
+    for (int64_t c = 0; c < ncell; ++c) fill[c] = count[c];
+    for (int64_t i = 0; i < nv; ++i)
+        if (cell_of[i] >= 0) node[fill[cell_of[i]]++] = i;
+#define CELL(i, j, k) ((k) + nc[2] * ((j) + nc[1] * (i)))
+#define PAIR(u, v)                                                                                     \
+    do {                                                                                               \
+        const int64_t a_ = (u), b_ = (v);                                                              \
+        if (owner[a_] != owner[b_]) pp_pair(L, p, c2, pos + 3 * a_, pos + 3 * b_, force + 3 * a_, force + 3 * b_); \
+    } while (0)
+    for (int64_t i = 1; i <= nc[0] - 2; ++i)
+        for (int64_t j = 1; j <= nc[1] - 2; ++j)
+            for (int64_t k = 1; k <= nc[2] - 2; ++k) {
+                const int64_t c = CELL(i, j, k);
+                const int64_t nb[7] = {CELL(i, j + 1, k), CELL(i, j + 1, k + 1), CELL(i, j, k + 1), CELL(i + 1, j, k),
+                                       CELL(i + 1, j + 1, k), CELL(i + 1, j + 1, k + 1), CELL(i + 1, j, k + 1)};
+                for (int64_t l = count[c]; l < count[c + 1]; ++l) {
+                    for (int64_t m = l + 1; m < count[c + 1]; ++m) PAIR(node[l], node[m]);
+                    for (int n = 0; n < 7; ++n)
+                        for (int64_t m = count[nb[n]]; m < count[nb[n] + 1]; ++m) PAIR(node[l], node[m]);
+                }
+            }
+    /* collide_all_in_cells of the first and last bulk layers of periodic axes (CollisionForces.h:119-163) */
+    const int64_t x0 = 1, x1 = nc[0] - 2, y0 = 1, y1 = nc[1] - 2, z0 = 1, z1 = nc[2] - 2;
+#define ALL(ca, cb)                                                                 \
+    do {                                                                            \
+        const int64_t p_ = (ca), q_ = (cb);                                         \
+        for (int64_t l = count[p_]; l < count[p_ + 1]; ++l)                         \
+            for (int64_t m = count[q_]; m < count[q_ + 1]; ++m) PAIR(node[l], node[m]); \
+    } while (0)
+    if (L->periodic[0])
+        for (int64_t j = y0; j <= y1; ++j)
+            for (int64_t k = z0; k <= z1; ++k) ALL(CELL(x0, j, k), CELL(x1, j, k));
+    if (L->periodic[1])
+        for (int64_t i = x0; i <= x1; ++i)
+            for (int64_t k = z0; k <= z1; ++k) ALL(CELL(i, y0, k), CELL(i, y1, k));
+    if (L->periodic[2])
+        for (int64_t i = x0; i <= x1; ++i)
+            for (int64_t j = y0; j <= y1; ++j) ALL(CELL(i, j, z0), CELL(i, j, z1));
+    if (L->periodic[0] && L->periodic[1])
+        for (int64_t k = z0; k <= z1; ++k) ALL(CELL(x0, y0, k), CELL(x1, y1, k));
+    if (L->periodic[0] && L->periodic[2])
+        for (int64_t j = y0; j <= y1; ++j) ALL(CELL(x0, j, z0), CELL(x1, j, z1));
+    if (L->periodic[1] && L->periodic[2])
+        for (int64_t i = x0; i <= x1; ++i) ALL(CELL(i, y0, z0), CELL(i, y1, z1));
+    if (L->periodic[0] && L->periodic[1] && L->periodic[2]) ALL(CELL(x0, y0, z0), CELL(x1, y1, z1));
+#undef ALL
+#undef PAIR
+#undef CELL
+    free(count);
+    free(cell_of);
+    free(fill);
+    free(node);
+}
+
+/* Every pair of vertices of different particles within the cutoff (minimum image on periodic
+ * axes), each vertex summing its own terms: for vertex i, the partners j in increasing index
+ * order.  This is the interaction the grid search above approximates. */
+void orc_pp_forces(const orc_lattice* L, const orc_potential* p, int64_t nv, const double* pos, const int32_t* owner,
+                   double* force) {
+    const double c2 = p->r0 * p->r0;
+    double* acc = (double*)calloc((size_t)(3 * (nv > 0 ? nv : 1)), sizeof(double));
+#pragma omp parallel for schedule(dynamic, 64) if (nv > 4096)
+    for (int64_t i = 0; i < nv; ++i) {
+        double dummy[3];
+        for (int64_t j = 0; j < nv; ++j) {
+            if (owner[j] == owner[i]) continue;
+            pp_pair(L, p, c2, pos + 3 * i, pos + 3 * j, acc + 3 * i, dummy);
+        }
+    }
+    for (int64_t i = 0; i < 3 * nv; ++i) force[i] += acc[i];
+    free(acc);
 }
 
 /* ------------------------------------------------------------------ immersed boundary */
@@ -1107,6 +1285,14 @@ struct orc_sys {
     int32_t* cls;
     int64_t ncls;
     int32_t voxelize;
+    /* force decorators (wall interactions) and particle-particle interactions */
+    int32_t nwalls;
+    orc_potential wall_pot[8];
+    int32_t wall_axis[8];
+    double wall_lo[8], wall_hi[8];
+    int32_t npp;
+    orc_potential pp_pot[8];
+    int32_t pp_grid;  /* 1: the reference's grid search, 0: every pair within the cutoff */
 };
 
 orc_sys* orc_sys_create(const orc_lattice* L, int32_t dirac, double ib_offset) {
@@ -1234,6 +1420,22 @@ static void sys_voxelize(orc_sys* s) {
 
 void orc_sys_set_voxelize(orc_sys* s, int32_t on) { s->voxelize = on; }
 
+int32_t orc_sys_add_wall_interaction(orc_sys* s, const orc_potential* p, int32_t axis, double lo, double hi) {
+    if (s->nwalls >= 8 || axis < 0 || axis > 2) return -1;
+    s->wall_pot[s->nwalls] = *p;
+    s->wall_axis[s->nwalls] = axis;
+    s->wall_lo[s->nwalls] = lo;
+    s->wall_hi[s->nwalls] = hi;
+    return s->nwalls++;
+}
+
+int32_t orc_sys_add_pp_interaction(orc_sys* s, const orc_potential* p, int32_t grid) {
+    if (s->npp >= 8) return -1;
+    s->pp_pot[s->npp] = *p;
+    s->pp_grid = grid;
+    return s->npp++;
+}
+
 /* ImmersedBoundaryDynamics3D::init voxelizes the initial positions (ImmersedBoundaryDynamics.hh:404-412) */
 void orc_sys_init(orc_sys* s) { sys_voxelize(s); }
 
@@ -1276,12 +1478,34 @@ static void sys_step(orc_sys* s) {
         for (int32_t i = 0; i < s->nparts; ++i) {
             orc_particle* p = &s->parts[i];
             const orc_shape* sh = &s->shapes[p->shape];
-            orc_membrane_forces(p->model, p->prm, sh->nv, sh->rest, sh->nt, sh->tri, sh->tri_area, sh->area, sh->nl,
+            /* ImmersedBoundaryDynamics3D::compute_forces (ImmersedBoundaryDynamics_forces.hh:287-302):
+             * zero, the force decorators, then the particle's own forces */
+            memset(p->force, 0, sizeof(double) * 3 * sh->nv);
+            for (int32_t w = 0; w < s->nwalls; ++w)
+                orc_wall_forces(&s->wall_pot[w], s->wall_axis[w], s->wall_lo[w], s->wall_hi[w], sh->nv, p->pos, p->force);
+            membrane_forces_acc(p->model, p->prm, sh->nv, sh->rest, sh->nt, sh->tri, sh->tri_area, sh->area, sh->nl,
                                 sh->links, sh->link_len, sh->np, sh->pairs, sh->pair_cs, p->pos, p->area, p->volume,
                                 p->force);
             memcpy(p->vel, vel + 3 * o, sizeof(double) * 3 * sh->nv);
             memcpy(frc + 3 * o, p->force, sizeof(double) * 3 * sh->nv);
             o += sh->nv;
+        }
+        if (s->npp > 0) {  /* then the particle-particle interactions over all vertices */
+            int32_t* owner = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nvt > 0 ? nvt : 1));
+            int64_t q = 0;
+            for (int32_t i = 0; i < s->nparts; ++i)
+                for (int64_t k = 0; k < s->shapes[s->parts[i].shape].nv; ++k) owner[q++] = i;
+            for (int32_t k = 0; k < s->npp; ++k) {
+                if (s->pp_grid) orc_pp_forces_grid(L, &s->pp_pot[k], nvt, pos, owner, frc);
+                else orc_pp_forces(L, &s->pp_pot[k], nvt, pos, owner, frc);
+            }
+            q = 0;
+            for (int32_t i = 0; i < s->nparts; ++i) {
+                const int64_t nvi = s->shapes[s->parts[i].shape].nv;
+                memcpy(s->parts[i].force, frc + 3 * q, sizeof(double) * 3 * nvi);
+                q += nvi;
+            }
+            free(owner);
         }
         orc_spread(L, s->dirac, s->offset, nvt, pos, frc, cls, s->F);
         for (int32_t i = 0; i < s->nparts; ++i) {

@@ -91,6 +91,20 @@ void orc_spread(const orc_lattice* L, int32_t dirac, double offset, int64_t n, c
 int32_t orc_threads(void);
 
 /* ---- coupled system (mirrors the product's C ABI) ---- */
+/* interaction potentials (fsi/Potentials.h): kind, cutoff r0 (Morse r_min / spring min_dist), Morse beta, strength */
+enum { ORC_POTENTIAL_NONE = 0, ORC_POTENTIAL_MORSE = 1, ORC_POTENTIAL_SPRING = 2 };
+typedef struct {
+    int32_t kind;
+    double r0, beta, strength;
+} orc_potential;
+double orc_potential_eval(const orc_potential* p, double d);
+void orc_wall_forces(const orc_potential* p, int32_t axis, double lo, double hi, int64_t nv, const double* pos,
+                     double* force);
+void orc_pp_forces_grid(const orc_lattice* L, const orc_potential* p, int64_t nv, const double* pos,
+                        const int32_t* owner, double* force);
+void orc_pp_forces(const orc_lattice* L, const orc_potential* p, int64_t nv, const double* pos, const int32_t* owner,
+                   double* force);
+
 typedef struct orc_sys orc_sys;
 orc_sys* orc_sys_create(const orc_lattice* L, int32_t dirac, double ib_offset);
 void orc_sys_destroy(orc_sys* s);
@@ -103,6 +117,10 @@ int32_t orc_sys_add_particle(orc_sys* s, int32_t shape, int32_t model, const dou
 void orc_sys_init(orc_sys* s);
 void orc_sys_step(orc_sys* s, int64_t nsteps);
 void orc_sys_set_voxelize(orc_sys* s, int32_t on);  /* revoxelize after every move (and at init) */
+/* add_force_decorator(WallInteraction(ParallelPlatesBoundary(lo, hi) normal to `axis`, p)) */
+int32_t orc_sys_add_wall_interaction(orc_sys* s, const orc_potential* p, int32_t axis, double lo, double hi);
+/* add_pp_force(PPPotentialForce(p)); grid = 1 evaluates it with the reference's grid search */
+int32_t orc_sys_add_pp_interaction(orc_sys* s, const orc_potential* p, int32_t grid);
 void orc_sys_lattice_only_step(orc_sys* s, int64_t nsteps);
 void orc_sys_get_particle(orc_sys* s, int32_t pid, double* pos, double* vel, double* force, double* stats5);
 void orc_sys_velocity(orc_sys* s, double* u);

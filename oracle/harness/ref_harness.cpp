@@ -14,6 +14,9 @@
 //           (ImmersedBoundaryDynamics_interpolation.hh, ImmersedBoundaryDynamics_forces.hh)
 //   shape   ParticleShape rest geometry and connectivity (ParticleShape.hh:21-212)
 //   inertia DeformableParticle3D::compute_moment_of_intertia (DeformableParticle3D.hh:173-272)
+//   interact the vertex forces of one IB step with a particle-particle interaction
+//           (add_pp_force, CollisionForces.h) and a wall interaction decorator
+//           (add_force_decorator, ForceDecorator.hh) on parallel plates (Boundary.h:305-365)
 //
 // Array conventions: lattice fields are (components, nz, ny, nx) with x fastest.
 #define FSI_PROFILE
@@ -538,6 +541,70 @@ static int run_inertia(const Bundle& in, const char* out) {
     return 0;
 }
 
+// Potentials of kind 1 (Morse: r_min, beta, strength) or 2 (spring: min_dist, _, strength),
+// Potentials.h
+template <class PP, class WP>
+static int run_interact_impl(const Bundle& in, const char* out, const PP& ppot, const WP& wpot) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    ParticleShapeLibrary<T> lib;
+    store_shape(in, lib, "rest");
+    const ParticleShape<T>* shape = lib.get_by_tag("shape");
+    const ParticleSpec spec = read_spec(in);
+    ParticleBase3D<T>* pa = make_particle(shape, spec);
+    ParticleBase3D<T>* pb = make_particle(shape, spec);
+    set_positions(*pa, recio::need(in, "pos_a"));
+    set_positions(*pb, recio::need(in, "pos_b"));
+
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(1.0, 1.0));
+    lattice.toggleInternalStatistics(false);
+    Box3D domain = lattice.getBoundingBox();
+    lattice.periodicity().toggleAll(true);
+    initializeAtEquilibrium(lattice, domain, (T)1, Array<T, 3>(0., 0., 0.));
+    lattice.initialize();
+    ImmersedBoundaryDynamics3D<T, DESCRIPTOR, Periodicity3D<T, true, true, true> > fsi(lattice, lib);
+    const std::vector<double> wy = recio::need(in, "wall_y").d;
+    ParallelPlatesBoundary<T> plates(wy[0], wy[1]);
+    WallInteraction<T, WP> wall(plates, wpot);
+    PPPotentialForce<T, PP> pp(ppot);
+    fsi.add_force_decorator(&wall);
+    fsi.add_pp_force(&pp);
+    std::auto_ptr<MultiTensorField3D<T, 3> > velocity = generateMultiTensorField<T, 3>(domain);
+    fsi.add_particle(pa);
+    fsi.add_particle(pb);
+    fsi.init();
+    computeVelocity(lattice, *velocity, domain);
+    setExternalVector(lattice, domain, DESCRIPTOR<T>::ExternalField::forceBeginsAt, Array<T, 3>(0., 0., 0.));
+    applyProcessingFunctional(wrap_ibm_dynamics3D(fsi), domain, lattice, *velocity);
+    recio::Writer w(out);
+    const char* names[2] = {"force_a", "force_b"};
+    for (plint id = 0; id < 2; ++id) {
+        ParticleBase3D<T>* p = 0;
+        fsi.get_particle(id, p);
+        const plint nv = p->count_nodes();
+        std::vector<double> F(3 * nv);
+        for (plint i = 0; i < nv; ++i)
+            for (int d = 0; d < 3; ++d) F[3 * i + d] = p->get_node(i).force[d];
+        w.d(names[id], shp(nv, 3), F);
+    }
+    delete pa;
+    delete pb;
+    return 0;
+}
+
+static int run_interact(const Bundle& in, const char* out) {
+    const long long ppk = recio::inum(in, "pp_kind"), wk = recio::inum(in, "wall_kind");
+    const std::vector<double> a = recio::need(in, "pp_params").d, b = recio::need(in, "wall_params").d;
+    const MorsePotential<T> ma(a[0], a[1], a[2]), mb(b[0], b[1], b[2]);
+    const SpringPotential<T> sa(a[0], a[2]), sb(b[0], b[2]);
+    if (ppk == 1 && wk == 1) return run_interact_impl(in, out, ma, mb);
+    if (ppk == 1 && wk == 2) return run_interact_impl(in, out, ma, sb);
+    if (ppk == 2 && wk == 1) return run_interact_impl(in, out, sa, mb);
+    if (ppk == 2 && wk == 2) return run_interact_impl(in, out, sa, sb);
+    std::fprintf(stderr, "unknown potential kinds %lld %lld\n", ppk, wk);
+    return 2;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) {
         std::fprintf(stderr, "usage: ref_harness <lbm|ibm|forces|interp|shape|inertia> in.rec out.rec\n");
@@ -552,6 +619,7 @@ int main(int argc, char** argv) {
     if (c == "interp") return run_interp(in, argv[3]);
     if (c == "shape") return run_shape(in, argv[3]);
     if (c == "inertia") return run_inertia(in, argv[3]);
+    if (c == "interact") return run_interact(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

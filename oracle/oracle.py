@@ -18,6 +18,7 @@ COLLISION = {"bgk_guo_vof": 0, "bgk": 1, "trt": 2}
 WALL = {"none": 0, "fd_velocity": 1, "halfway_bb": 2}
 DIRAC = {"roma": 0, "peskin": 1}
 MODEL = {"capsule_neohookean": 0, "capsule_skalak": 1, "rbc_wlcpow": 2, "skalak_bending": 3}
+POTENTIAL = {"none": 0, "morse": 1, "spring": 2}
 PARAM_KEYS = ["G", "C", "nu_s", "kb", "shear_modulus", "L0", "k_area_global", "k_area_local",
               "k_volume", "vol_desired", "k_bend", "theta0"]
 
@@ -33,6 +34,15 @@ class Lattice(C.Structure):
         ("envelope_swap", C.c_int32),
         ("celltype", C.c_void_p),
     ]
+
+
+class Potential(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("r0", C.c_double), ("beta", C.c_double), ("strength", C.c_double)]
+
+
+def potential(kind, r0, beta=0.0, strength=0.0) -> Potential:
+    """MorsePotential(r_min = r0, beta, strength) or SpringPotential(min_dist = r0, strength)."""
+    return Potential(POTENTIAL[kind] if isinstance(kind, str) else int(kind), float(r0), float(beta), float(strength))
 
 
 def build():
@@ -81,6 +91,13 @@ def lib():
             "orc_sys_step": (None, [C.c_void_p, C.c_int64]),
             "orc_sys_lattice_only_step": (None, [C.c_void_p, C.c_int64]),
             "orc_sys_get_particle": (None, [C.c_void_p, C.c_int32, dp, dp, dp, dp]),
+            "orc_potential_eval": (C.c_double, [C.POINTER(Potential), C.c_double]),
+            "orc_wall_forces": (None, [C.POINTER(Potential), C.c_int32, C.c_double, C.c_double, C.c_int64, dp, dp]),
+            "orc_pp_forces_grid": (None, [Lp, C.POINTER(Potential), C.c_int64, dp, i32p, dp]),
+            "orc_pp_forces": (None, [Lp, C.POINTER(Potential), C.c_int64, dp, i32p, dp]),
+            "orc_sys_add_wall_interaction": (C.c_int32, [C.c_void_p, C.POINTER(Potential), C.c_int32, C.c_double,
+                                                         C.c_double]),
+            "orc_sys_add_pp_interaction": (C.c_int32, [C.c_void_p, C.POINTER(Potential), C.c_int32]),
             "orc_sys_velocity": (None, [C.c_void_p, dp]),
         }
         for name, (res, args) in sig.items():
@@ -304,6 +321,14 @@ class System:
         """Revoxelize the membranes into the phase field after every move (and at init)."""
         lib().orc_sys_set_voxelize(self.h, int(bool(on)))
 
+    def add_wall_interaction(self, pot: Potential, axis: int, lo: float, hi: float):
+        """add_force_decorator(WallInteraction(ParallelPlatesBoundary(lo, hi) normal to axis, pot))."""
+        assert lib().orc_sys_add_wall_interaction(self.h, C.byref(pot), int(axis), float(lo), float(hi)) >= 0
+
+    def add_pp_interaction(self, pot: Potential, grid: bool = False):
+        """add_pp_force(PPPotentialForce(pot)); grid=True searches pairs as the reference does."""
+        assert lib().orc_sys_add_pp_interaction(self.h, C.byref(pot), int(bool(grid))) >= 0
+
     def init(self):
         """ImmersedBoundaryDynamics3D::init: voxelize the initial positions (when enabled)."""
         lib().orc_sys_init(self.h)
@@ -333,3 +358,20 @@ def voxelize(L, pos, tri, phase=None):
     ph = np.zeros((L.nz, L.ny, L.nx)) if phase is None else phase
     lib().orc_voxelize(C.byref(L), pos.shape[0], _d(pos), tri.shape[0], _i(tri), _d(ph))
     return ph
+
+
+def wall_forces(pot: Potential, axis, lo, hi, pos, force=None):
+    pos = f64(pos)
+    out = np.zeros_like(pos) if force is None else f64(force).copy()
+    lib().orc_wall_forces(C.byref(pot), int(axis), float(lo), float(hi), pos.shape[0], _d(pos), _d(out))
+    return out
+
+
+def pp_forces(L, pot: Potential, pos, owner, force=None, grid=False):
+    """Particle-particle forces on the concatenated vertices (owner = particle of each vertex)."""
+    pos = f64(pos)
+    own = np.ascontiguousarray(owner, dtype=np.int32)
+    out = np.zeros_like(pos) if force is None else f64(force).copy()
+    fn = lib().orc_pp_forces_grid if grid else lib().orc_pp_forces
+    fn(C.byref(L), C.byref(pot), pos.shape[0], _d(pos), _i32(own), _d(out))
+    return out

@@ -297,8 +297,50 @@ def case_ibm_capsule_lambda():
     save("ibm_capsule_lambda", inp, keep)
 
 
+def interact_geometry(n=24, radius=3.0, cut_pp=0.6, cut_wall=0.5):
+    """Two capsules almost touching along x and a pair of y plates just outside them, placed so
+    that every vertex pair within the cutoff lies in cells the reference's grid search pairs
+    (checked with the oracle: the grid search and the all-pairs search give the same forces)."""
+    from oracle import oracle as O
+
+    xyz, tri = meshes.icosphere(2, radius)
+    L = O.lattice((n, n, n), (1, 1, 1))
+    pot = O.potential("spring", cut_pp, 0.0, 1.0)
+    a = xyz + np.array([8.3, 10.2, 11.6])
+    owner = np.repeat([0, 1], xyz.shape[0])
+    gap_x = a[:, 0].max() - a[:, 0].min()
+    for dy in np.linspace(-0.45, 0.45, 19):
+        for dz in np.linspace(-0.45, 0.45, 19):
+            for d in (0.25, 0.3, 0.35):
+                b = xyz + np.array([8.3 + gap_x + d, 10.2 + dy, 11.6 + dz])
+                pos = np.concatenate([a, b])
+                f_all = O.pp_forces(L, pot, pos, owner)
+                f_grid = O.pp_forces(L, pot, pos, owner, grid=True)
+                n_pairs = int((np.abs(f_all).sum(axis=1) > 0).sum())
+                if n_pairs >= 6 and np.abs(f_all - f_grid).max() <= 1e-15 * np.abs(f_all).max():
+                    lo = a[:, 1].min() - 0.6 * cut_wall
+                    hi = max(a[:, 1].max(), b[:, 1].max()) + 0.8 * cut_wall
+                    return xyz, tri, a, b, (lo, hi)
+    raise RuntimeError("no configuration where the grid search finds every pair")
+
+
+def case_interact():
+    """Particle-particle (PPPotentialForce) and wall (WallInteraction on parallel y plates)
+    forces of one IB step on a lattice at rest: Morse pairs + spring walls, and the reverse."""
+    n = 24
+    xyz, tri, a, b, wy = interact_geometry(n)
+    prm = particle_params(1, G=1e-3, C=1.0)
+    for name, ppk, ppq, wk, wq in (("interact_morse_spring", 1, [0.6, 3.0, 2e-3], 2, [0.5, 0.0, 1e-2]),
+                                   ("interact_spring_morse", 2, [0.6, 0.0, 5e-3], 1, [0.5, 2.0, 1e-3])):
+        inp = dict(dims=[n, n, n], rest=xyz, tri=tri, pos_a=a, pos_b=b, model=1, params=prm, pp_kind=ppk,
+                   pp_params=ppq, wall_kind=wk, wall_params=wq, wall_y=list(wy))
+        out = run("interact", inp)
+        assert np.abs(out["force_a"]).max() > 1e-4 and np.abs(out["force_b"]).max() > 1e-4
+        save(name, inp, {"force_a": out["force_a"], "force_b": out["force_b"]})
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
-         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda]
+         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):

@@ -173,3 +173,51 @@ def test_coupled_rbc_periodic_body_force():
 def test_coupled_capsule_viscosity_ratio():
     """lambda = 5: the voxelized phase enters omega every step."""
     run_coupled(golden("ibm_capsule_lambda"))
+
+
+def interact_system(d, grid):
+    n = int(d["in_dims"][0])
+    L = O.lattice((n, n, n), (1, 1, 1), "bgk_guo_vof", 1.0, 1.0)
+    S = O.System(L, "roma", -1.0)
+    sid = S.add_shape(d["in_rest"], d["in_tri"])
+    pa = S.add_particle(sid, int(d["in_model"]), d["in_params"], d["in_pos_a"])
+    pb = S.add_particle(sid, int(d["in_model"]), d["in_params"], d["in_pos_b"])
+    wq, pq = d["in_wall_params"], d["in_pp_params"]
+    lo, hi = d["in_wall_y"]
+    S.add_wall_interaction(O.potential(int(d["in_wall_kind"]), wq[0], wq[1], wq[2]), 1, lo, hi)
+    S.add_pp_interaction(O.potential(int(d["in_pp_kind"]), pq[0], pq[1], pq[2]), grid=grid)
+    S.init()
+    S.step(1)
+    return S.particle(pa)["force"], S.particle(pb)["force"]
+
+
+@pytest.mark.parametrize("name", ["interact_morse_spring", "interact_spring_morse"])
+def test_interaction_forces(name):
+    """Wall decorator + particle-particle forces of one IB step: the reference's grid search
+    bit for bit, and the all-pairs search (what the CUDA path evaluates) to the summation
+    order on a configuration where the grid finds every pair."""
+    d = golden(name)
+    fa, fb = interact_system(d, grid=True)
+    assert np.array_equal(fa, d["out_force_a"]) and np.array_equal(fb, d["out_force_b"])
+    # both particles feel the pair force, particle a also the lower plate
+    near = np.abs(d["out_force_a"][:, 0]) > 0
+    assert near.any() and (np.abs(d["out_force_b"][:, 0]) > 0).any()
+    assert (d["out_force_a"][:, 1] > 1e-6).any()
+    ga, gb = interact_system(d, grid=False)
+    scale = max(np.abs(d["out_force_a"]).max(), np.abs(d["out_force_b"]).max())
+    assert np.abs(ga - d["out_force_a"]).max() <= 1e-15 * scale
+    assert np.abs(gb - d["out_force_b"]).max() <= 1e-15 * scale
+
+
+def test_grid_search_misses_diagonal_pairs():
+    """The reference's grid pairs a cell with 7 of its 13 forward neighbours: two vertices in
+    cells offset by (+1, -1, 0) do not interact there; the all-pairs search finds them."""
+    L = O.lattice((16, 16, 16), (1, 1, 1))
+    pot = O.potential("spring", 0.8, 0.0, 1.0)
+    pos = np.array([[7.45, 8.55, 8.0], [7.55, 8.45, 8.0]])  # grid cells (x 8, y 10) and (x 9, y 9)
+    owner = np.array([0, 1])
+    assert np.abs(O.pp_forces(L, pot, pos, owner, grid=True)).max() == 0.0
+    f = O.pp_forces(L, pot, pos, owner)
+    d = np.linalg.norm(pos[1] - pos[0])
+    expect = -(0.8 - d) / d * (pos[1] - pos[0])
+    assert np.allclose(f[0], expect, rtol=1e-14) and np.array_equal(f[1], -f[0])
