@@ -46,6 +46,11 @@ class BatchTuning(C.Structure):
                 ("reserved", C.c_int32 * 5)]
 
 
+class Potential(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("r0", C.c_double), ("beta", C.c_double),
+                ("strength", C.c_double)]
+
+
 class Config(C.Structure):
     _fields_ = [("device", C.c_int32), ("flags", C.c_int32)]
 
@@ -86,6 +91,9 @@ SIGNATURES = {
     "bib_total_volume": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_ibm_step": (C.c_int32, [_vp, C.c_int32]),
     "bib_ibm_init": (C.c_int32, [_vp, C.c_int32]),
+    "bib_add_wall_interaction": (C.c_int32, [_vp, C.c_int32, C.c_int32, C.c_double, C.c_double, C.POINTER(Potential)]),
+    "bib_add_pp_interaction": (C.c_int32, [_vp, C.c_int32, C.POINTER(Potential)]),
+    "bib_clear_interactions": (C.c_int32, [_vp, C.c_int32]),
     "bib_particle_info": (C.c_int32, [_vp, C.c_int32, C.c_int32, _i32p]),
     "bib_lattice_iteration": (C.c_int32, [_vp, C.c_int32, _ip]),
     "bib_checkpoint_save": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),

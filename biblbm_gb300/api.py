@@ -17,7 +17,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import BatchTuning, BibError, IbParams, LatticeParams, Tuning
+from ._lib import BatchTuning, BibError, IbParams, LatticeParams, Potential, Tuning
 
 STORAGE = {"f64": 0, "f32": 1, "f16": 2}
 COLLISION = {"bgk_guo_vof": 0, "bgk": 1, "trt": 2}
@@ -268,6 +268,16 @@ class ParticleShapeLibrary:
                     n_triangles=int(out[5]))
 
 
+def MorsePotential(r_min, beta, strength) -> Potential:
+    """fsi/Potentials.h MorsePotential: 2 beta strength x (x - 1), x = exp(beta (r_min - d)), d <= r_min."""
+    return Potential(1, 0, float(r_min), float(beta), float(strength))
+
+
+def SpringPotential(min_dist, strength) -> Potential:
+    """fsi/Potentials.h SpringPotential: (min_dist - d) strength, d <= min_dist."""
+    return Potential(2, 0, float(min_dist), 0.0, float(strength))
+
+
 class ImmersedBoundaryDynamics3D:
     """The IB module of src/fsi/ImmersedBoundaryDynamics.h:50-217 on one lattice."""
 
@@ -286,6 +296,19 @@ class ImmersedBoundaryDynamics3D:
                                                      _d(pos) if pos is not None else None, C.byref(pid)))
         self.nv.append(self.shapes.info(shape)["n_vertices"])
         return pid.value
+
+    def add_wall_interaction(self, potential: Potential, axis: int, lo: float, hi: float):
+        """add_force_decorator(WallInteraction(ParallelPlatesBoundary(lo, hi), potential)); the
+        plates are normal to `axis` (1 = y as in the reference, 2 = z)."""
+        self.ctx.check(self.ctx.lib.bib_add_wall_interaction(self.ctx.h, self.lattice.h, int(axis), float(lo),
+                                                             float(hi), C.byref(potential)))
+
+    def add_pp_force(self, potential: Potential):
+        """add_pp_force(PPPotentialForce(potential)): repulsion between vertices of different particles."""
+        self.ctx.check(self.ctx.lib.bib_add_pp_interaction(self.ctx.h, self.lattice.h, C.byref(potential)))
+
+    def clear_interactions(self):
+        self.ctx.check(self.ctx.lib.bib_clear_interactions(self.ctx.h, self.lattice.h))
 
     def init(self):
         """ImmersedBoundaryDynamics3D::init: upload the particles and voxelize them into the

@@ -314,6 +314,14 @@ void free_particles(Lattice& L) {
     cudaFree(L.sort_temp);
     L.sort_temp = nullptr;
     L.sort_temp_bytes = 0;
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(L.pgrid.keys[k]);
+        cudaFree(L.pgrid.ids[k]);
+    }
+    cudaFree(L.pgrid.start);
+    cudaFree(L.pgrid.end);
+    cudaFree(L.pgrid.temp);
+    L.pgrid = PairGrid{};
     cudaFree(L.vox_count);
     cudaFree(L.vox_z);
     L.vox_count = nullptr;
@@ -411,6 +419,30 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
     if (L.membrane_smem + 1024 > (size_t)dev_max)
         return fail(c, BIB_EUNSUPPORTED, "mesh with %d vertices exceeds the membrane kernel's shared memory", L.max_nv);
     configure_membrane_kernel(L.membrane_smem);
+    if (L.inter.npp > 0) {
+        // pair search: cells of at least the cutoff, hashed into >= 2 buckets per vertex
+        PairGrid& G = L.pgrid;
+        const int N[3] = {L.d.nx, L.d.ny, L.d.nz};
+        for (int a = 0; a < 3; ++a) {
+            G.nc[a] = std::max(1, (int)std::floor((double)N[a] / L.inter.pp_cut));
+            G.cs[a] = (double)N[a] / (double)G.nc[a];
+        }
+        G.table = 1024;
+        while (G.table < 2u * (unsigned)L.nvert && G.table < (1u << 24)) G.table <<= 1;
+        G.bits = 0;
+        while ((1u << G.bits) < G.table) ++G.bits;
+        for (int k = 0; k < 2; ++k) {
+            BIB_CUDA(c, cudaMalloc((void**)&G.keys[k], L.nvert * sizeof(uint32_t)));
+            BIB_CUDA(c, cudaMalloc((void**)&G.ids[k], L.nvert * sizeof(uint32_t)));
+        }
+        BIB_CUDA(c, cudaMemset(G.keys[1], 0, L.nvert * sizeof(uint32_t)));
+        BIB_CUDA(c, cudaMalloc((void**)&G.start, G.table * sizeof(int)));
+        BIB_CUDA(c, cudaMalloc((void**)&G.end, G.table * sizeof(int)));
+        BIB_CUDA(c, cudaMemset(G.start, 0, G.table * sizeof(int)));
+        BIB_CUDA(c, cudaMemset(G.end, 0, G.table * sizeof(int)));
+        G.temp_bytes = pp_sort_temp_bytes(L.nvert, G.bits);
+        BIB_CUDA(c, cudaMalloc(&G.temp, std::max<size_t>(G.temp_bytes, 16)));
+    }
     if (L.phase) {
         // the reference voxelizes the membranes into the phase field when the immersed-boundary
         // functional first runs (ImmersedBoundaryDynamics.hh:404-412) and after every move
@@ -450,6 +482,7 @@ void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
         if (!L.target_clean) launch_force_fill(L, 1 - L.fe, s);
         record(c, 0);
         launch_membrane_forces(L, s);
+        launch_pp_forces(L, s);
         record(c, 1);
         launch_spread(L, 1 - L.fe, s);
         record(c, 2);
@@ -472,6 +505,7 @@ void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
         if (!L.target_clean) launch_force_fill(L, 1 - L.fe, s);
         record(c, 0);
         if (ib) launch_membrane_forces(L, s);
+        if (ib) launch_pp_forces(L, s);
         record(c, 1);
         if (ib) launch_spread(L, 1 - L.fe, s);
         record(c, 2);
@@ -498,6 +532,7 @@ void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
         launch_force_fill(L, L.fe, s);
         L.target_clean = false;
         if (ib) launch_membrane_forces(L, s);
+        if (ib) launch_pp_forces(L, s);
         record(c, 1);
         if (ib) launch_spread(L, L.fe, s);
         record(c, 2);
@@ -731,6 +766,9 @@ bib_status build_batch(bib_ctx* c, Batch& B) {
         if (st) return st;
         if (L.phase && L.nvert)
             return fail(c, BIB_EUNSUPPORTED, "batched steps do not voxelize membranes into a phase field (lattice %d)",
+                        B.handles[i]);
+        if (L.inter.npp > 0)
+            return fail(c, BIB_EUNSUPPORTED, "batched steps do not evaluate particle-particle interactions (lattice %d)",
                         B.handles[i]);
         B.versions[i] = L.version;
         B.state0[i] = lattice_state(L);
@@ -1541,6 +1579,65 @@ bib_status bib_ib_configure(bib_ctx* c, int32_t h, const bib_ib_params* p) {
     if (pst) return pst;
     if (!L->parts.empty()) L->particles_dirty = true;
     drop_graphs(c, h);
+    return BIB_OK;
+}
+
+static bib_status check_potential(bib_ctx* c, const bib_potential* p) {
+    if (!p) return fail(c, BIB_EINVAL, "null potential");
+    if (p->kind != BIB_POTENTIAL_MORSE && p->kind != BIB_POTENTIAL_SPRING) return fail(c, BIB_EINVAL, "bad potential kind");
+    if (!(p->r0 > 0 && std::isfinite(p->r0)) || !std::isfinite(p->strength) || !std::isfinite(p->beta))
+        return fail(c, BIB_EINVAL, "potential parameters must be finite, with a positive cutoff");
+    return BIB_OK;
+}
+
+// Interaction changes alter kernel arguments captured in graphs and batch tables
+static void interactions_changed(bib_ctx* c, int32_t h) {
+    drop_graphs(c, h);
+    for (auto& B : c->batches)
+        if (B) B->free_tables();
+}
+
+bib_status bib_add_wall_interaction(bib_ctx* c, int32_t h, int32_t axis, double lo, double hi, const bib_potential* p) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    bib_status st = check_potential(c, p);
+    if (st) return st;
+    if (axis < 0 || axis > 2 || !(lo < hi)) return fail(c, BIB_EINVAL, "wall interaction needs axis 0..2 and lo < hi");
+    if (L->inter.nwall >= BIB_MAX_WALL_INTERACTIONS) return fail(c, BIB_EINVAL, "too many wall interactions");
+    const int w = L->inter.nwall++;
+    L->inter.wall_axis[w] = axis;
+    L->inter.wall_lo[w] = lo;
+    L->inter.wall_hi[w] = hi;
+    L->inter.wall[w] = PotentialDev{p->kind, p->r0, p->beta, p->strength};
+    interactions_changed(c, h);
+    return BIB_OK;
+}
+
+bib_status bib_add_pp_interaction(bib_ctx* c, int32_t h, const bib_potential* p) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    bib_status st = check_potential(c, p);
+    if (st) return st;
+    if (L->inter.npp >= BIB_MAX_PP_INTERACTIONS) return fail(c, BIB_EINVAL, "too many particle-particle interactions");
+    // the reference limits the cutoff to the delta kernel's half support - 1/2
+    // (ImmersedBoundaryDynamics_forces.hh:346-349)
+    const double limit = (L->ib.dirac == BIB_DIRAC_PESKIN ? 2.0 : 1.5) - 0.5;
+    if (p->r0 > limit) return fail(c, BIB_EINVAL, "interaction cutoff %g exceeds %g", p->r0, limit);
+    L->inter.pp[L->inter.npp++] = PotentialDev{p->kind, p->r0, p->beta, p->strength};
+    L->inter.pp_cut = std::max(L->inter.pp_cut, p->r0);
+    // the pair search buffers are sized with the particles: re-upload them on the next step
+    st = pull_particles(c, *L);
+    if (st) return st;
+    if (!L->parts.empty()) L->particles_dirty = true;
+    interactions_changed(c, h);
+    return BIB_OK;
+}
+
+bib_status bib_clear_interactions(bib_ctx* c, int32_t h) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    L->inter = Interactions{};
+    interactions_changed(c, h);
     return BIB_OK;
 }
 

@@ -86,6 +86,36 @@ struct ParticleDev {
 // Per-particle state kept on the device: {area, volume, com[3]}.
 constexpr int STATS = 5;
 
+// Interaction potentials and the wall / particle-particle interactions of a lattice.
+struct PotentialDev {
+    int kind;  // BIB_POTENTIAL_*
+    double r0, beta, strength;
+};
+struct Interactions {
+    int nwall = 0;
+    int wall_axis[BIB_MAX_WALL_INTERACTIONS] = {};
+    double wall_lo[BIB_MAX_WALL_INTERACTIONS] = {}, wall_hi[BIB_MAX_WALL_INTERACTIONS] = {};
+    PotentialDev wall[BIB_MAX_WALL_INTERACTIONS] = {};
+    int npp = 0;
+    PotentialDev pp[BIB_MAX_PP_INTERACTIONS] = {};
+    double pp_cut = 0.0;  // largest particle-particle cutoff
+};
+
+// Hashed cell list of the pair search: cells of at least the cutoff (nc per axis, size cs),
+// hashed into `table` buckets; vertices sorted by bucket, [start, end) per bucket.
+struct PairGrid {
+    int nc[3] = {1, 1, 1};
+    double cs[3] = {1.0, 1.0, 1.0};
+    unsigned table = 0;  // power of two
+    int bits = 0;
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* ids[2] = {nullptr, nullptr};
+    int* start = nullptr;
+    int* end = nullptr;
+    void* temp = nullptr;
+    size_t temp_bytes = 0;
+};
+
 // What the immersed-boundary kernels need of one lattice for one step (buffer parities
 // resolved).  A single lattice passes one view by value; a batch passes a device table of
 // views, indexed per vertex (through the vertex -> lattice map) or per particle (inst).
@@ -101,6 +131,7 @@ struct IbView {
     double* stats;       // STATS per particle
     int vbase;           // batch numbering of the lattice's first vertex
     int nvert;
+    Interactions inter;  // wall interactions are applied by the membrane kernel
 };
 
 // Per-launch constants of the collision in the compute type C.
@@ -184,6 +215,8 @@ struct Lattice {
     ParticleDev* pdev = nullptr;
     std::vector<ParticleDev> pdev_host;  // host copy of pdev (batch tables are built from it)
     int* vert_particle = nullptr;         // global vertex -> particle
+    Interactions inter;                   // wall and particle-particle interactions
+    PairGrid pgrid;                       // pair search of the particle-particle interactions
     int max_nv = 0;
     bool particles_dirty = true;  // host copies below are authoritative until uploaded
     std::vector<double> host_pos;    // concatenated vertex positions
@@ -234,6 +267,9 @@ void launch_membrane_forces(const Lattice& L, cudaStream_t s);
 void launch_spread(const Lattice& L, int fbuf, cudaStream_t s);
 void launch_interpolate_move(const Lattice& L, cudaStream_t s);  // vel and pos[1-pcur] = pos + vel
 void launch_particle_update(const Lattice& L, cudaStream_t s);   // area/volume/COM of pos[1-pcur] + remap
+// particle-particle interaction forces at pos[pcur] added to the vertex forces (no-op without)
+void launch_pp_forces(const Lattice& L, cudaStream_t s);
+size_t pp_sort_temp_bytes(int nvert, int bits);
 constexpr int kVoxelCap = 64;  // membrane crossings one (x, y) column can hold
 void launch_voxelize(const Lattice& L, const double* pos, cudaStream_t s);  // phase field of the membranes at pos
 size_t membrane_smem_bytes(int max_nv);

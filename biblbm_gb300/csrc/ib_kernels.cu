@@ -374,6 +374,35 @@ __global__ void __launch_bounds__(128) k_spread_reduce(LatticeDesc d, IbDesc ib,
     F[2 * d.stride + key] = acc[2];
 }
 
+// ---------------------------------------------------------------- interaction forces
+// MorsePotential::eval / SpringPotential::operator() (fsi/Potentials.h:29-71), FP64
+__device__ __forceinline__ double potential_eval(const PotentialDev& p, double d) {
+    if (p.kind == BIB_POTENTIAL_MORSE) {
+        if (d < 0) d = 0.0;
+        const double x = exp(p.beta * (p.r0 - d));
+        return 2 * p.beta * p.strength * x * (x - 1);
+    }
+    if (p.kind == BIB_POTENTIAL_SPRING) return (p.r0 - d) * p.strength;
+    return 0.0;
+}
+
+// Sum of the wall-interaction decorators on a vertex at p (WallInteraction::apply_force,
+// ForceDecorator.hh:25-32, with ParallelPlatesBoundary, Boundary.h:305-365): for the nearer
+// plate at distance dist <= r0, force -= phi(dist) * outward normal.
+__device__ __forceinline__ void wall_force(const Interactions& I, const double* p, double* f) {
+    f[0] = f[1] = f[2] = 0.0;
+    for (int w = 0; w < I.nwall; ++w) {
+        const int a = I.wall_axis[w];
+        const double r = p[a], lo = I.wall_lo[w], hi = I.wall_hi[w];
+        const bool lower = r < 0.5 * (lo + hi);
+        const double dist = lower ? r - lo : hi - r;
+        if (dist <= I.wall[w].r0) {
+            const double phi = potential_eval(I.wall[w], dist);
+            f[a] -= lower ? -phi : phi;
+        }
+    }
+}
+
 // ---------------------------------------------------------------- membrane mechanics
 template <class M>
 struct V3 {
@@ -690,7 +719,18 @@ __device__ __forceinline__ void membrane_block(const ParticleDev& P, const IbVie
     double* __restrict__ force = V.force;
     const double* st = V.stats + STATS * P.lpid;
     const double area = st[0], volume = st[1];
-    for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sf[i] = M(0);
+    // the force decorators come first (ImmersedBoundaryDynamics_forces.hh:293-296)
+    if (V.inter.nwall > 0) {
+        for (int i = threadIdx.x; i < P.nv; i += blockDim.x) {
+            double fw[3];
+            wall_force(V.inter, pos + 3LL * (P.v0 + i), fw);
+            sf[3 * i] = (M)fw[0];
+            sf[3 * i + 1] = (M)fw[1];
+            sf[3 * i + 2] = (M)fw[2];
+        }
+    } else {
+        for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) sf[i] = M(0);
+    }
     // FP64 element arithmetic uses absolute positions as the reference does; reduced
     // precision stages the positions relative to the centre of mass in shared memory
     // (exact FP64 subtraction, then rounding) so the element loops read them from there.
@@ -759,7 +799,7 @@ template <class M>
 __global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* __restrict__ vert_particle,
                                                           const ParticleDev* __restrict__ parts,
                                                           const double* __restrict__ pos, double* __restrict__ force,
-                                                          const double* __restrict__ stats) {
+                                                          const double* __restrict__ stats, Interactions inter) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nvert) return;
     const int pid = vert_particle[g];
@@ -789,9 +829,11 @@ __global__ void __launch_bounds__(128) k_membrane_gather(int nvert, const int* _
         }
     }
     V3<M> f = P.model == BIB_MODEL_SKALAK_BENDING ? cap.acc + rbc.acc : (capsule ? cap.acc : rbc.acc);
-    force[3LL * g] = (double)f.x;
-    force[3LL * g + 1] = (double)f.y;
-    force[3LL * g + 2] = (double)f.z;
+    double fw[3] = {0.0, 0.0, 0.0};
+    if (inter.nwall > 0) wall_force(inter, pos + 3LL * g, fw);
+    force[3LL * g] = fw[0] + (double)f.x;
+    force[3LL * g + 1] = fw[1] + (double)f.y;
+    force[3LL * g + 2] = fw[2] + (double)f.z;
 }
 
 // One CTA per particle: area, signed volume and area-weighted centroid of X_{n+1}
@@ -1018,6 +1060,117 @@ __global__ void __launch_bounds__(128) k_voxel_fill(LatticeDesc d, int* __restri
     }
 }
 
+// ---------------------------------------------------------------- particle-particle interactions
+// Pair search on a hashed cell list: cells of at least the largest cutoff, each vertex keyed
+// by the hash of its cell, vertices sorted by key (stable: vertex order within a bucket).
+struct PairCells {
+    int nc[3];
+    double cs[3];
+    unsigned mask;
+};
+
+__device__ __forceinline__ int pair_cell(const LatticeDesc& d, const PairCells& g, int a, double x) {
+    const int N = a == 0 ? d.nx : (a == 1 ? d.ny : d.nz);
+    const int per = a == 0 ? d.px : (a == 1 ? d.py : d.pz);
+    if (per) x -= (double)N * floor(x * d.inv_n[a]);
+    int c = (int)floor(x / g.cs[a]);
+    return c < 0 ? 0 : (c >= g.nc[a] ? g.nc[a] - 1 : c);
+}
+__device__ __forceinline__ unsigned cell_hash(const PairCells& g, int cx, int cy, int cz) {
+    return ((unsigned)cx * 73856093u ^ (unsigned)cy * 19349663u ^ (unsigned)cz * 83492791u) & g.mask;
+}
+
+// the buckets of the previous step's sort go back to empty
+__global__ void __launch_bounds__(128) k_pp_clear(int nvert, const uint32_t* __restrict__ prev_keys, int* start,
+                                                   int* end) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nvert) return;
+    start[prev_keys[s]] = 0;
+    end[prev_keys[s]] = 0;
+}
+
+__global__ void __launch_bounds__(128) k_pp_keys(LatticeDesc d, PairCells g, int nvert, const double* __restrict__ pos,
+                                                  uint32_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= nvert) return;
+    const double* p = pos + 3LL * v;
+    keys[v] = cell_hash(g, pair_cell(d, g, 0, p[0]), pair_cell(d, g, 1, p[1]), pair_cell(d, g, 2, p[2]));
+    ids[v] = (uint32_t)v;
+}
+
+__global__ void __launch_bounds__(128) k_pp_bounds(int nvert, const uint32_t* __restrict__ keys, int* start, int* end) {
+    const int s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= nvert) return;
+    const uint32_t k = keys[s];
+    if (s == 0 || keys[s - 1] != k) start[k] = s;
+    if (s == nvert - 1 || keys[s + 1] != k) end[k] = s + 1;
+}
+
+// Arithmetic1D::min_mod_diff (Periodicity.h:27-35, 96-99) on periodic axes
+__device__ __forceinline__ double min_image(const LatticeDesc& d, int a, double dx) {
+    const int per = a == 0 ? d.px : (a == 1 ? d.py : d.pz);
+    if (!per) return dx;
+    const double N = (double)(a == 0 ? d.nx : (a == 1 ? d.ny : d.nz));
+    return dx - floor(dx * d.inv_n[a] + 0.5) * N;
+}
+
+// One thread per vertex: the sum over partners j of other particles within the cutoff of
+// (-phi(d) / d) (x_j - x_i) (CollisionHandler::handle_collision, CollisionForces.h:187-199),
+// added to the vertex's force.  Every pair is evaluated from both ends, so no atomics.
+__global__ void __launch_bounds__(128) k_pp_forces(LatticeDesc d, Interactions I, PairCells g, int nvert,
+                                                    const double* __restrict__ pos, const int* __restrict__ owner,
+                                                    const uint32_t* __restrict__ ids, const int* __restrict__ start,
+                                                    const int* __restrict__ end, double* __restrict__ force) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= nvert) return;
+    const double xi[3] = {pos[3LL * i], pos[3LL * i + 1], pos[3LL * i + 2]};
+    if (!(isfinite(xi[0]) && isfinite(xi[1]) && isfinite(xi[2]))) return;
+    const int oi = owner[i];
+    const int c[3] = {pair_cell(d, g, 0, xi[0]), pair_cell(d, g, 1, xi[1]), pair_cell(d, g, 2, xi[2])};
+    const int per[3] = {d.px, d.py, d.pz};
+    const double cut2 = I.pp_cut * I.pp_cut;
+    double f[3] = {0.0, 0.0, 0.0};
+    unsigned seen[27];
+    int nseen = 0;
+    for (int dz = -1; dz <= 1; ++dz)
+        for (int dy = -1; dy <= 1; ++dy)
+            for (int dx = -1; dx <= 1; ++dx) {
+                int n[3] = {c[0] + dx, c[1] + dy, c[2] + dz};
+                bool ok = true;
+                for (int a = 0; a < 3; ++a) {
+                    if (n[a] < 0 || n[a] >= g.nc[a]) {
+                        if (!per[a]) ok = false;
+                        else n[a] = (n[a] + g.nc[a]) % g.nc[a];
+                    }
+                }
+                if (!ok) continue;
+                const unsigned h = cell_hash(g, n[0], n[1], n[2]);
+                bool dup = false;  // neighbour cells that share a bucket are visited once
+                for (int q = 0; q < nseen; ++q) dup = dup || seen[q] == h;
+                if (dup) continue;
+                seen[nseen++] = h;
+                for (int s = start[h]; s < end[h]; ++s) {
+                    const int j = (int)ids[s];
+                    if (owner[j] == oi) continue;
+                    const double dr[3] = {min_image(d, 0, pos[3LL * j] - xi[0]), min_image(d, 1, pos[3LL * j + 1] - xi[1]),
+                                          min_image(d, 2, pos[3LL * j + 2] - xi[2])};
+                    const double dsq = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+                    if (!(dsq <= cut2)) continue;
+                    const double dist = sqrt(dsq);
+                    for (int k = 0; k < I.npp; ++k) {
+                        if (!(dsq <= I.pp[k].r0 * I.pp[k].r0)) continue;
+                        const double sc = -potential_eval(I.pp[k], dist) / dist;
+                        f[0] += sc * dr[0];
+                        f[1] += sc * dr[1];
+                        f[2] += sc * dr[2];
+                    }
+                }
+            }
+    force[3LL * i] += f[0];
+    force[3LL * i + 1] += f[1];
+    force[3LL * i + 2] += f[2];
+}
+
 }  // namespace
 
 size_t membrane_smem_bytes(int max_nv) { return (size_t)3 * max_nv * sizeof(double); }
@@ -1083,6 +1236,7 @@ IbView single_view(const Lattice& L, int fbuf) {
     v.stats = L.stats;
     v.vbase = 0;
     v.nvert = L.nvert;
+    v.inter = L.inter;
     return v;
 }
 
@@ -1143,12 +1297,38 @@ void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
     if (L.ib.spread_mode == BIB_SPREAD_DETERMINISTIC) {
         const unsigned g = (L.nvert + 127) / 128;
         if (L.storage == BIB_STORAGE_F64)
-            k_membrane_gather<double><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats);
+            k_membrane_gather<double><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats, L.inter);
         else
-            k_membrane_gather<float><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats);
+            k_membrane_gather<float><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats, L.inter);
         return;
     }
     membrane_any<false>(L.storage, L.pdev, np, single_view(L, -1), nullptr, L.membrane_smem, L.membrane_block, s);
+}
+
+size_t pp_sort_temp_bytes(int nvert, int bits) {
+    size_t bytes = 0;
+    cub::DeviceRadixSort::SortPairs((void*)nullptr, bytes, (uint32_t*)nullptr, (uint32_t*)nullptr, (uint32_t*)nullptr,
+                                    (uint32_t*)nullptr, nvert, 0, bits);
+    return bytes;
+}
+
+void launch_pp_forces(const Lattice& L, cudaStream_t s) {
+    if (L.inter.npp == 0 || L.nvert == 0 || !L.pgrid.table) return;
+    const PairGrid& G = L.pgrid;
+    PairCells g;
+    for (int a = 0; a < 3; ++a) {
+        g.nc[a] = G.nc[a];
+        g.cs[a] = G.cs[a];
+    }
+    g.mask = G.table - 1;
+    const unsigned b = (L.nvert + 127) / 128;
+    k_pp_clear<<<b, 128, 0, s>>>(L.nvert, G.keys[1], G.start, G.end);
+    k_pp_keys<<<b, 128, 0, s>>>(L.d, g, L.nvert, L.pos[L.pcur], G.keys[0], G.ids[0]);
+    size_t tb = G.temp_bytes;
+    cub::DeviceRadixSort::SortPairs(G.temp, tb, G.keys[0], G.keys[1], G.ids[0], G.ids[1], L.nvert, 0, G.bits, s);
+    k_pp_bounds<<<b, 128, 0, s>>>(L.nvert, G.keys[1], G.start, G.end);
+    k_pp_forces<<<b, 128, 0, s>>>(L.d, L.inter, g, L.nvert, L.pos[L.pcur], L.vert_particle, G.ids[1], G.start, G.end,
+                                  L.force);
 }
 
 void launch_particle_update(const Lattice& L, cudaStream_t s) {

@@ -200,6 +200,32 @@ bib_status bib_particles_download(bib_ctx* ctx, int32_t h, double* pos, double* 
 bib_status bib_total_vertices(bib_ctx* ctx, int32_t h, int64_t* n);
 /* compute_total_volume, ImmersedBoundaryDynamics.hh:559-568 */
 bib_status bib_total_volume(bib_ctx* ctx, int32_t h, double* v);
+/* ---- interaction forces added to the vertex forces of every IB step (compute_forces,
+ * ImmersedBoundaryDynamics_forces.hh:287-302): wall interactions first (add_force_decorator with
+ * WallInteraction, ForceDecorator.hh:25-32), then the membrane forces, then particle-particle
+ * interactions (add_pp_force with PPPotentialForce, ParticleParticleInteraction.h:24-40, evaluated
+ * as CollisionHandler::handle_collision, CollisionForces.h:187-199).  Potentials (Potentials.h):
+ * Morse 2 beta strength x (x - 1), x = exp(beta (r0 - d)); spring (r0 - d) strength; both act
+ * for d <= r0.  The pair search takes every pair of vertices of different particles within r0
+ * (minimum image on periodic axes); the reference's grid search examines 7 of the 13 forward
+ * neighbour cells and can miss pairs.  Particle-particle cutoffs are limited to the delta
+ * kernel's half support - 1/2, as in the reference (ImmersedBoundaryDynamics_forces.hh:346-349). ---- */
+enum { BIB_POTENTIAL_NONE = 0, BIB_POTENTIAL_MORSE = 1, BIB_POTENTIAL_SPRING = 2 };
+typedef struct {
+    int32_t kind;    /* BIB_POTENTIAL_* */
+    int32_t reserved;
+    double r0;       /* Morse r_min / spring min_dist: the cutoff */
+    double beta;     /* Morse beta (unused by the spring) */
+    double strength; /* Morse strength / spring constant */
+} bib_potential;
+#define BIB_MAX_WALL_INTERACTIONS 4
+#define BIB_MAX_PP_INTERACTIONS 4
+/* WallInteraction with ParallelPlatesBoundary(lo, hi) (Boundary.h:305-365) normal to axis 1 (y,
+ * the reference's plates) or 2 (z): distance to the nearer plate, force -= phi(dist) outward normal */
+bib_status bib_add_wall_interaction(bib_ctx* ctx, int32_t h, int32_t axis, double lo, double hi, const bib_potential* p);
+bib_status bib_add_pp_interaction(bib_ctx* ctx, int32_t h, const bib_potential* p);
+bib_status bib_clear_interactions(bib_ctx* ctx, int32_t h);
+
 /* ImmersedBoundaryDynamics3D::init (ImmersedBoundaryDynamics.hh:404-412): upload the particles
  * and, on a lattice with a phase field, voxelize them into it.  The first step does this by
  * itself; the call makes the moment explicit (and synchronises). */
