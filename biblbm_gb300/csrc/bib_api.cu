@@ -301,6 +301,8 @@ void free_particles(Lattice& L) {
     cudaFree(L.vel);
     cudaFree(L.force);
     cudaFree(L.stats);
+    cudaFree(L.upd_partial);
+    L.upd_partial = nullptr;
     cudaFree(L.pdev);
     cudaFree(L.vert_particle);
     L.vel = L.force = L.stats = nullptr;
@@ -354,6 +356,7 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
     BIB_CUDA(c, cudaMalloc((void**)&L.vel, vb));
     BIB_CUDA(c, cudaMalloc((void**)&L.force, vb));
     BIB_CUDA(c, cudaMalloc((void**)&L.stats, STATS * np * sizeof(double)));
+    BIB_CUDA(c, cudaMalloc((void**)&L.upd_partial, (size_t)np * 64 * 5 * sizeof(double)));
     BIB_CUDA(c, cudaMemcpy(L.pos[0], L.host_pos.data(), vb, cudaMemcpyHostToDevice));
     BIB_CUDA(c, cudaMemcpy(L.pos[1], L.host_pos.data(), vb, cudaMemcpyHostToDevice));
     BIB_CUDA(c, cudaMemset(L.vel, 0, vb));
@@ -362,6 +365,8 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
     L.pcur = 0;
     std::vector<ParticleDev> pd(np);
     L.max_nv = 0;
+    L.max_elems = 0;
+    L.max_nt = 0;
     for (int p = 0; p < np; ++p) {
         const ParticleHost& ph = L.parts[p];
         const ShapeHost& S = *c->shapes[ph.shape];
@@ -391,6 +396,8 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
         d.A0 = S.area;
         for (int k = 0; k < BIB_P_COUNT; ++k) d.prm[k] = ph.prm[k];
         L.max_nv = std::max(L.max_nv, ph.nv);
+        L.max_elems = std::max(L.max_elems, std::max(d.nt, std::max(d.nl, d.np)));
+        L.max_nt = std::max(L.max_nt, d.nt);
     }
     if (L.ib.spread_mode == BIB_SPREAD_DETERMINISTIC) {
         const int sup = L.ib.dirac == BIB_DIRAC_PESKIN ? 4 : 3;

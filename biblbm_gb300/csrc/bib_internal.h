@@ -218,6 +218,9 @@ struct Lattice {
     Interactions inter;                   // wall and particle-particle interactions
     PairGrid pgrid;                       // pair search of the particle-particle interactions
     int max_nv = 0;
+    int max_elems = 0;            // most triangles, links or pairs of one particle
+    int max_nt = 0;               // most triangles of one particle
+    double* upd_partial = nullptr;  // partial sums of the split update (particles x 64 x 5)
     bool particles_dirty = true;  // host copies below are authoritative until uploaded
     std::vector<double> host_pos;    // concatenated vertex positions
     std::vector<double> host_stats;  // STATS per particle

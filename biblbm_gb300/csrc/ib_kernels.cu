@@ -5,6 +5,7 @@
 //
 // Vertices of all particles of a lattice are concatenated: positions (FP64, two
 // buffers swapped every step), velocities and forces (FP64).
+#include <algorithm>
 #include <cfloat>
 
 #include <cub/device/device_radix_sort.cuh>
@@ -719,8 +720,12 @@ __device__ __forceinline__ void membrane_block(const ParticleDev& P, const IbVie
     double* __restrict__ force = V.force;
     const double* st = V.stats + STATS * P.lpid;
     const double area = st[0], volume = st[1];
+    // gridDim.y CTAs share the elements of one particle: each sums its share in shared memory
+    // and adds it to the force array (seeded by k_force_seed) with atomics
+    const int split = gridDim.y;
+    const int e0 = blockIdx.y * blockDim.x + threadIdx.x, es = split * blockDim.x;
     // the force decorators come first (ImmersedBoundaryDynamics_forces.hh:293-296)
-    if (V.inter.nwall > 0) {
+    if (split == 1 && V.inter.nwall > 0) {
         for (int i = threadIdx.x; i < P.nv; i += blockDim.x) {
             double fw[3];
             wall_force(V.inter, pos + 3LL * (P.v0 + i), fw);
@@ -759,7 +764,7 @@ __device__ __forceinline__ void membrane_block(const ParticleDev& P, const IbVie
         // triangle terms (capsule law and RBC area / volume penalties) of one triangle are
         // summed per corner before they reach the shared accumulators
         if (capsule || rbc_terms)
-            for (int t = threadIdx.x; t < P.nt; t += blockDim.x) {
+            for (int t = e0; t < P.nt; t += es) {
                 const V3<M> z = mk3<M>(0, 0, 0);
                 const int4 ti = __ldg(reinterpret_cast<const int4*>(P.tri4) + t);
                 CornerSink<M> cs{{ti.x, ti.y, ti.z}, {z, z, z}};
@@ -768,14 +773,31 @@ __device__ __forceinline__ void membrane_block(const ParticleDev& P, const IbVie
                 for (int c = 0; c < 3; ++c) sk(cs.id[c], cs.f[c]);
             }
         if (P.model == BIB_MODEL_RBC_WLCPOW)
-            for (int l = threadIdx.x; l < P.nl; l += blockDim.x) rbc_link<M>(P, l, ps, sk);
+            for (int l = e0; l < P.nl; l += es) rbc_link<M>(P, l, ps, sk);
         if (rbc_terms)
-            for (int p = threadIdx.x; p < P.np; p += blockDim.x) rbc_pair<M>(P, p, ps, k, sk);
+            for (int p = e0; p < P.np; p += es) rbc_pair<M>(P, p, ps, k, sk);
     };
     if (rel) run(SharedPos<M>{sp});
     else run(GlobalPos<M>{pos + 3LL * P.v0, {0.0, 0.0, 0.0}});
     __syncthreads();
-    for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) force[3LL * P.v0 + i] = (double)sf[i];
+    if (split == 1) {
+        for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x) force[3LL * P.v0 + i] = (double)sf[i];
+    } else {
+        for (int i = threadIdx.x; i < 3 * P.nv; i += blockDim.x)
+            if (sf[i] != M(0)) atomicAdd(force + 3LL * P.v0 + i, (double)sf[i]);
+    }
+}
+
+// The vertex forces before a split membrane launch adds into them: the wall-interaction
+// decorators, or zero.
+__global__ void __launch_bounds__(128) k_force_seed(IbView V) {
+    const int v = blockIdx.x * blockDim.x + threadIdx.x;
+    if (v >= V.nvert) return;
+    double fw[3] = {0.0, 0.0, 0.0};
+    if (V.inter.nwall > 0) wall_force(V.inter, V.pos + 3LL * v, fw);
+    V.force[3LL * v] = fw[0];
+    V.force[3LL * v + 1] = fw[1];
+    V.force[3LL * v + 2] = fw[2];
 }
 
 template <class M, bool BATCH>
@@ -861,16 +883,15 @@ __device__ __forceinline__ void block_sum5(const double v[5], double* red, doubl
     __syncthreads();
 }
 
+// Per-triangle area, signed volume and area-weighted centroid of X_{n+1}, summed over the
+// triangles e0, e0 + es, ... by this CTA into sum[0..4] (shared; valid for every thread).
 template <class M>
-__device__ __forceinline__ void update_block(const ParticleDev& P, const IbView& V, float* sp, double* red,
-                                             double* delta) {
-    __shared__ double sum[5];
-    const LatticeDesc& d = V.d;
-    double* pos_next = V.pos_next;
-    double* st = V.stats + STATS * P.lpid;
+__device__ __forceinline__ void update_sums(const ParticleDev& P, const IbView& V, float* sp, double* red, double* sum,
+                                            int e0, int es) {
+    const double* pv = V.pos_next + 3LL * P.v0;
+    const double* st = V.stats + STATS * P.lpid;
     const bool rel = sizeof(M) < sizeof(double);
     const double c0 = rel ? st[2] : 0.0, c1 = rel ? st[3] : 0.0, c2 = rel ? st[4] : 0.0;
-    const double* pv = pos_next + 3LL * P.v0;
     if (rel) {  // one FP64 subtraction and rounding per vertex coordinate
         for (int i = threadIdx.x; i < P.nv; i += blockDim.x) {
             sp[3 * i] = (float)(pv[3 * i] - c0);
@@ -885,7 +906,7 @@ __device__ __forceinline__ void update_block(const ParticleDev& P, const IbView&
     };
     // per-thread partial sums in M (a few triangles each), block sums in FP64
     M ta = 0, tv = 0, tcx = 0, tcy = 0, tcz = 0;
-    for (int t = threadIdx.x; t < P.nt; t += blockDim.x) {
+    for (int t = e0; t < P.nt; t += es) {
         const int4 ti = __ldg(reinterpret_cast<const int4*>(P.tri4) + t);
         const V3<M> A = vert(ti.x), B = vert(ti.y), Cv = vert(ti.z);
         const M dA = norm3(cross3(B - A, Cv - A)) * M(0.5);
@@ -900,7 +921,18 @@ __device__ __forceinline__ void update_block(const ParticleDev& P, const IbView&
     }
     const double part[5] = {(double)ta, (double)tv, (double)tcx, (double)tcy, (double)tcz};
     block_sum5(part, red, sum);
+}
+
+// A, V and the centre from the sums (relative to the previous centre for M = float), the
+// periodic centre-of-mass remap, and the shift of the vertices by whole periods.
+template <class M>
+__device__ __forceinline__ void update_finish(const ParticleDev& P, const IbView& V, const double* sum, double* delta) {
+    const LatticeDesc& d = V.d;
+    double* pos_next = V.pos_next;
+    double* st = V.stats + STATS * P.lpid;
     if (threadIdx.x == 0) {
+        const bool rel = sizeof(M) < sizeof(double);
+        const double c0 = rel ? st[2] : 0.0, c1 = rel ? st[3] : 0.0, c2 = rel ? st[4] : 0.0;
         const double sa = sum[0], sv = sum[1];
         const double com[3] = {c0 + sum[2] / sa, c1 + sum[3] / sa, c2 + sum[4] / sa};
         const int N[3] = {d.nx, d.ny, d.nz};
@@ -926,6 +958,44 @@ __device__ __forceinline__ void update_block(const ParticleDev& P, const IbView&
             pos_next[g + 2] += delta[2];
         }
     }
+}
+
+template <class M>
+__device__ __forceinline__ void update_block(const ParticleDev& P, const IbView& V, float* sp, double* red,
+                                             double* delta) {
+    __shared__ double sum[5];
+    update_sums<M>(P, V, sp, red, sum, threadIdx.x, blockDim.x);
+    update_finish<M>(P, V, sum, delta);
+}
+
+// Few particles: gridDim.y CTAs per particle write partial sums, one CTA per particle adds
+// them in slice order and finishes the update.
+constexpr int kMaxUpdateSplit = 64;
+
+template <class M>
+__global__ void __launch_bounds__(256) k_update_partial(const ParticleDev* __restrict__ parts, IbView v1,
+                                                         double* __restrict__ partial) {
+    __shared__ double red[5 * 256];
+    __shared__ double sum[5];
+    extern __shared__ __align__(16) float sp[];
+    const ParticleDev& P = parts[blockIdx.x];
+    update_sums<M>(P, v1, sp, red, sum, blockIdx.y * blockDim.x + threadIdx.x, gridDim.y * blockDim.x);
+    if (threadIdx.x < 5) partial[(blockIdx.x * (size_t)gridDim.y + blockIdx.y) * 5 + threadIdx.x] = sum[threadIdx.x];
+}
+
+template <class M>
+__global__ void __launch_bounds__(256) k_update_finish(const ParticleDev* __restrict__ parts, IbView v1,
+                                                        const double* __restrict__ partial, int split) {
+    __shared__ double sum[5];
+    __shared__ double delta[3];
+    const ParticleDev& P = parts[blockIdx.x];
+    if (threadIdx.x < 5) {
+        double a = 0.0;
+        for (int y = 0; y < split; ++y) a += partial[(blockIdx.x * (size_t)split + y) * 5 + threadIdx.x];
+        sum[threadIdx.x] = a;
+    }
+    __syncthreads();
+    update_finish<M>(P, v1, sum, delta);
 }
 
 template <class M, bool BATCH>
@@ -1221,6 +1291,7 @@ void configure_membrane_kernel(size_t smem) {
     // 3 floats per vertex, at most half of the membrane kernel's 3 doubles per vertex
     cudaFuncSetAttribute(k_particle_update<float, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2));
     cudaFuncSetAttribute(k_particle_update<float, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2));
+    cudaFuncSetAttribute(k_update_partial<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)(smem / 2));
 }
 
 IbView single_view(const Lattice& L, int fbuf) {
@@ -1291,6 +1362,22 @@ void launch_interpolate_move(const Lattice& L, cudaStream_t s) {
     interpolate_any<false>(L.storage, L.ib.dirac, single_view(L, -1), nullptr, nullptr, L.nvert, s);
 }
 
+// CTAs per particle of the membrane kernel: enough to give every SM two CTAs, but at least
+// one element per thread
+int membrane_split(int np, int max_elems, int block) {
+    static int sms = 0;
+    if (!sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (sms <= 0) sms = 1;
+    }
+    if (np <= 0 || np >= sms) return 1;
+    const int want = (2 * sms + np - 1) / np;
+    const int most = std::max(1, (max_elems + block - 1) / block);
+    return std::max(1, std::min(want, most));
+}
+
 void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
     const int np = (int)L.parts.size();
     if (np == 0) return;
@@ -1300,6 +1387,16 @@ void launch_membrane_forces(const Lattice& L, cudaStream_t s) {
             k_membrane_gather<double><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats, L.inter);
         else
             k_membrane_gather<float><<<g, 128, 0, s>>>(L.nvert, L.vert_particle, L.pdev, L.pos[L.pcur], L.force, L.stats, L.inter);
+        return;
+    }
+    // few particles: spread each particle's elements over several CTAs so the launch fills the GPU
+    const int split = membrane_split(np, L.max_elems, L.membrane_block);
+    if (split > 1) {
+        const IbView v = single_view(L, -1);
+        k_force_seed<<<(L.nvert + 127) / 128, 128, 0, s>>>(v);
+        const dim3 grid((unsigned)np, (unsigned)split);
+        if (L.storage == BIB_STORAGE_F64) k_membrane<double, false><<<grid, L.membrane_block, L.membrane_smem, s>>>(L.pdev, v, nullptr);
+        else k_membrane<float, false><<<grid, L.membrane_block, L.membrane_smem, s>>>(L.pdev, v, nullptr);
         return;
     }
     membrane_any<false>(L.storage, L.pdev, np, single_view(L, -1), nullptr, L.membrane_smem, L.membrane_block, s);
@@ -1334,6 +1431,22 @@ void launch_pp_forces(const Lattice& L, cudaStream_t s) {
 void launch_particle_update(const Lattice& L, cudaStream_t s) {
     const int np = (int)L.parts.size();
     if (np == 0) return;
+    // the split costs a second launch: worth it for the FP64 sums, and in FP32 for large meshes
+    // (measured: 642-vertex capsule FP32 slower split, 2562-vertex RBC and every FP64 case faster)
+    const bool big = L.storage == BIB_STORAGE_F64 || L.max_nt >= 4096;
+    const int split = big ? std::min(kMaxUpdateSplit, membrane_split(np, L.max_nt, 256)) : 1;
+    if (split > 1 && L.upd_partial) {
+        const IbView v = single_view(L, -1);
+        const size_t sm = L.storage == BIB_STORAGE_F64 ? 0 : 3 * sizeof(float) * L.max_nv;
+        if (L.storage == BIB_STORAGE_F64) {
+            k_update_partial<double><<<dim3(np, split), 256, sm, s>>>(L.pdev, v, L.upd_partial);
+            k_update_finish<double><<<np, 256, 0, s>>>(L.pdev, v, L.upd_partial, split);
+        } else {
+            k_update_partial<float><<<dim3(np, split), 256, sm, s>>>(L.pdev, v, L.upd_partial);
+            k_update_finish<float><<<np, 256, 0, s>>>(L.pdev, v, L.upd_partial, split);
+        }
+        return;
+    }
     update_any<false>(L.storage, L.pdev, np, single_view(L, -1), nullptr, L.max_nv, s);
 }
 

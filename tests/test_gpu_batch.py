@@ -65,11 +65,13 @@ def test_batch_equals_individual_steps(ctx, storage):
     batch.step(4)
     for lat, fsi, pid in solo:
         fsi.step(9)
-    tol_p, tol_f = (1e-13, 1e-15) if storage == "f64" else (2e-6, 2e-7)
+    # single lattices with few particles split the membrane and update kernels over several
+    # CTAs per particle: the same sums, grouped differently (FP32 partial sums in FP32 storage)
+    tol_p, tol_f, tol_v = (1e-13, 1e-15, 1e-9) if storage == "f64" else (2e-6, 2e-7, 1e-7)
     for (ls, fs, ps), (lg, fg, pg) in zip(solo, grouped):
         a, b = fs.get_particle(ps), fg.get_particle(pg)
         assert rel(b["pos"], a["pos"]) < tol_p
-        assert abs(b["volume"] - a["volume"]) < 1e-9 * a["volume"]
+        assert abs(b["volume"] - a["volume"]) < tol_v * a["volume"]
         assert np.abs(lg.receive() - ls.receive()).max() < tol_f
     batch.close()
 
