@@ -479,6 +479,28 @@ __device__ __forceinline__ StagedGeom view_geom(const CollideView& v, int ns) {
     return g;
 }
 
+// Shared memory of the batched kernel after its stages: the producer's and the consumers'
+// copies of the current lattice view (the view table outgrows L1 next to the stages, and its
+// fields would otherwise be L2 round trips on every tile) and the first tile of every view.
+constexpr int kMaxCachedViews = 512;
+__host__ __device__ constexpr size_t batch_extra_smem() {
+    return 2 * sizeof(CollideView) + kMaxCachedViews * sizeof(int64_t);
+}
+
+// View of `tile`: tiles of a CTA only grow, so step forward from the previous one
+__device__ __forceinline__ int next_view(const int64_t* tile0, int n, int vi, int64_t tile) {
+    while (vi + 1 < n && tile0[vi + 1] <= tile) ++vi;
+    return vi;
+}
+
+// Copy a view into shared memory with `nthreads` threads starting at thread `t`.
+__device__ __forceinline__ void copy_view(CollideView* dst, const CollideView* src, int t, int nthreads) {
+    static_assert(sizeof(CollideView) % 16 == 0, "views copy as 16-byte words");
+    const uint4* s4 = reinterpret_cast<const uint4*>(src);
+    uint4* d4 = reinterpret_cast<uint4*>(dst);
+    for (int k = t; k < (int)(sizeof(CollideView) / 16); k += nthreads) d4[k] = s4[k];
+}
+
 template <class T, int COLL>
 __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ctas_per_sm<T>())
     k_collide_stream_staged_batch(const CollideView* __restrict__ views, int nviews, int64_t ntiles, int NS,
@@ -490,6 +512,10 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);
     uint64_t* empty = full + kMaxStages;
     unsigned char* stages = smem + 256;
+    CollideView* pview = reinterpret_cast<CollideView*>(stages + (size_t)NS * L::BYTES);
+    CollideView* cview = pview + 1;
+    int64_t* tile0 = reinterpret_cast<int64_t*>(cview + 1);
+    const bool cached = nviews <= kMaxCachedViews;
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
     if ((int64_t)blockIdx.x >= ntiles) return;
     if (tid == 0) {
@@ -499,10 +525,12 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
         }
         mbar_init_fence();
     }
+    if (cached)
+        for (int k = tid; k < nviews; k += blockDim.x) tile0[k] = views[k].tile0;
     __syncthreads();
     if (warp == 0) {
         const PopLane pl = pop_lane(lane);
-        int it = 0;
+        int it = 0, vi = 0, have = -1;
         for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
             const int s = it % NS, use = it / NS;
             if (use > 0) {
@@ -512,7 +540,13 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
                     break;
                 }
             }
-            const CollideView& V = views[find_view(views, nviews, tile)];
+            vi = cached ? next_view(tile0, nviews, vi, tile) : find_view(views, nviews, tile);
+            if (vi != have) {
+                copy_view(pview, views + vi, lane, 32);
+                __syncwarp();
+                have = vi;
+            }
+            const CollideView& V = *pview;
             load_tile<T, true, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES, &full[s],
                                      static_cast<const T*>(V.fin), static_cast<const T*>(V.wall),
                                      static_cast<const FT*>(V.Fcol), static_cast<const FT*>(V.Fprev), lane, pl);
@@ -524,7 +558,7 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
         }
         return;
     }
-    int it = 0, cur_view = -1;
+    int it = 0, cur_view = -1, vi = 0;
     TileCell cell{};
     for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++it) {
         const int s = it % NS;
@@ -533,12 +567,17 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
             if (lane == 0) atomicExch(wait_err, 1);
             return;
         }
-        const int vi = find_view(views, nviews, tile);
-        const CollideView& V = views[vi];
-        if (vi != cur_view) {  // the cell of this thread depends on the lattice's row length
-            cell = tile_cell(V.d, V.Ct, tid - 32);
+        vi = cached ? next_view(tile0, nviews, vi, tile) : find_view(views, nviews, tile);
+        if (vi != cur_view) {
+            // every consumer is done with the previous view before it is replaced (named
+            // barrier 1 spans the consumer warps only; they all visit the same tiles)
+            asm volatile("bar.sync 1, %0;" ::"r"(L::CONSUMERS * 32) : "memory");
+            copy_view(cview, views + vi, tid - 32, L::CONSUMERS * 32);
+            asm volatile("bar.sync 1, %0;" ::"r"(L::CONSUMERS * 32) : "memory");
+            cell = tile_cell(cview->d, cview->Ct, tid - 32);  // depends on the lattice's row length
             cur_view = vi;
         }
+        const CollideView& V = *cview;
         consume_tile<T, true, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES,
                                     *reinterpret_cast<const CollideParams<C>*>(V.cp), static_cast<T*>(V.fout),
                                     static_cast<FT*>(V.Fprev), static_cast<FT*>(V.u), V.phase, V.celltype, cell,
@@ -691,7 +730,7 @@ template <class T, int COLL>
 bool batch_inst(const BatchLaunch& B, cudaStream_t s) {
     using LY = StageLayout<T, true, COLL>;
     const int ns = B.stages >= 2 ? B.stages : staged_stages<T, true, COLL>(Lattice{});
-    const size_t smem = staged_smem<T, true, COLL>(ns);
+    const size_t smem = staged_smem<T, true, COLL>(ns) + batch_extra_smem();
     if (smem + 1024 > (size_t)optin_smem()) return false;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -768,7 +807,7 @@ bool collide_batch_fits(int storage, int collision, int stages) {
         if (collision == BIB_COLLISION_BGK_GUO_VOF) smem = staged_smem<T, true, BIB_COLLISION_BGK_GUO_VOF>(ns);
         else if (collision == BIB_COLLISION_BGK) smem = staged_smem<T, true, BIB_COLLISION_BGK>(ns);
         else smem = staged_smem<T, true, BIB_COLLISION_TRT>(ns);
-        return ns <= 4 && smem + 1024 <= (size_t)optin_smem();
+        return ns <= 4 && smem + batch_extra_smem() + 1024 <= (size_t)optin_smem();
     };
     if (storage == BIB_STORAGE_F64) return fits(double{});
     if (storage == BIB_STORAGE_F32) return fits(float{});
