@@ -179,9 +179,12 @@ struct TileRef {
     int64_t row0;  // first cell of the tile
 };
 __device__ __forceinline__ TileRef tile_ref(const LatticeDesc& d, const StagedGeom& g, int64_t tile) {
+    // tile indices of one lattice fit 32 bits (checked on the host): a 32-bit division is a
+    // fraction of the 64-bit sequence, and every consumer thread evaluates it per tile
+    const unsigned ti = (unsigned)tile, ty = (unsigned)g.tiles_y;
     TileRef t;
-    t.z = (int)(tile / g.tiles_y);
-    t.y0 = (int)(tile - (int64_t)t.z * g.tiles_y) * g.R;
+    t.z = (int)(ti / ty);
+    t.y0 = (int)(ti - (unsigned)t.z * ty) * g.R;
     t.row0 = ((int64_t)t.y0 + (int64_t)d.ny * t.z) * d.nx;
     return t;
 }
@@ -705,7 +708,9 @@ bool staged_coll(const Lattice& L, int target, cudaStream_t s) {
 
 template <class T>
 bool shape_ok(const Lattice& L) {
-    return L.d.nx % 2 == 0 && (L.d.nx * sizeof(T)) % 16 == 0 && L.d.nx <= TileOf<T>::value;
+    // tiles are whole x-rows; their count per lattice (at most ny * nz) must fit 31 bits
+    return L.d.nx % 2 == 0 && (L.d.nx * sizeof(T)) % 16 == 0 && L.d.nx <= TileOf<T>::value &&
+           (int64_t)L.d.ny * L.d.nz < ((int64_t)1 << 31);
 }
 
 int default_tile_cells(const Lattice& L) {
