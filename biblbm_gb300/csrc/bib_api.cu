@@ -1237,6 +1237,26 @@ bib_status bib_lattice_set_cell_types(bib_ctx* c, int32_t h, const uint8_t* type
     return BIB_OK;
 }
 
+bib_status bib_lattice_set_pipe_walls(bib_ctx* c, int32_t h, double y0, double z0, double radius) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    if (!(radius > 0) || !std::isfinite(y0) || !std::isfinite(z0)) return fail(c, BIB_EINVAL, "bad pipe geometry");
+    const int64_t nx = L->d.nx, ny = L->d.ny, nz = L->d.nz;
+    std::vector<uint8_t> types((size_t)L->d.n);
+    // PipeBoundary::contains (fsi/Boundary.h:149-152) with margins 0 and -(plint)sqrt(2)
+    const double margin = -(double)(int64_t)std::sqrt(2.0);
+    for (int64_t z = 0; z < nz; ++z)
+        for (int64_t y = 0; y < ny; ++y) {
+            const double dy = (double)y - y0, dz = (double)z - z0;
+            const double r2 = dy * dy + dz * dz;
+            uint8_t t = BIB_CELL_FLUID;
+            if (!(r2 < radius * radius)) t = BIB_CELL_BOUNCE_BACK;
+            if (!(r2 < (radius - margin) * (radius - margin))) t = BIB_CELL_NO_DYNAMICS;
+            std::fill(types.begin() + (size_t)(nx * (y + ny * z)), types.begin() + (size_t)(nx * (y + ny * z) + nx), t);
+        }
+    return bib_lattice_set_cell_types(c, h, types.data());
+}
+
 bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     Lattice* L = get_lattice(c, h);
     if (!L || !t) return fail(c, BIB_EINVAL, "invalid lattice handle or tuning");

@@ -897,6 +897,25 @@ void orc_membrane_forces(int32_t model, const double* prm, int64_t nv, const dou
                         area, volume, force);
 }
 
+/* ------------------------------------------------------------------ pipe walls */
+/* The first-order pipe walls of progs/rbc_in_pipe/rbc_in_pipe.cpp:306-318 on PipeBoundary (axis
+ * along x through (y0, z0), fsi/Boundary.h:132-160): BounceBack where the node is not contained
+ * ((y - y0)^2 + (z - z0)^2 < radius^2 fails), NoDynamics where it is not contained in the pipe
+ * widened by the margin (plint)sqrt(2) = 1. */
+void orc_pipe_celltypes(int64_t nx, int64_t ny, int64_t nz, double y0, double z0, double radius, uint8_t* types) {
+    const double margin = -(double)(int64_t)sqrt(2.0);
+    for (int64_t z = 0; z < nz; ++z)
+        for (int64_t y = 0; y < ny; ++y)
+            for (int64_t x = 0; x < nx; ++x) {
+                const double dy = (double)y - y0, dz = (double)z - z0;
+                const double r2 = dy * dy + dz * dz;
+                uint8_t t = ORC_CELL_FLUID;
+                if (!(r2 < radius * radius)) t = ORC_CELL_BOUNCE_BACK;
+                if (!(r2 < (radius - margin) * (radius - margin))) t = ORC_CELL_NO_DYNAMICS;
+                types[x + nx * (y + ny * z)] = t;
+            }
+}
+
 /* ------------------------------------------------------------------ interaction forces */
 /* MorsePotential::eval and SpringPotential::operator() (fsi/Potentials.h:29-71): the force
  * magnitude at distance d, positive = repulsive; both are cut off at r0 (get_cutoff_distance). */

@@ -91,6 +91,9 @@ void orc_spread(const orc_lattice* L, int32_t dirac, double offset, int64_t n, c
 int32_t orc_threads(void);
 
 /* ---- coupled system (mirrors the product's C ABI) ---- */
+/* BounceBack / NoDynamics cells of the reference's first-order pipe walls (pipe along x) */
+void orc_pipe_celltypes(int64_t nx, int64_t ny, int64_t nz, double y0, double z0, double radius, uint8_t* types);
+
 /* interaction potentials (fsi/Potentials.h): kind, cutoff r0 (Morse r_min / spring min_dist), Morse beta, strength */
 enum { ORC_POTENTIAL_NONE = 0, ORC_POTENTIAL_MORSE = 1, ORC_POTENTIAL_SPRING = 2 };
 typedef struct {

@@ -14,6 +14,9 @@
 //           (ImmersedBoundaryDynamics_interpolation.hh, ImmersedBoundaryDynamics_forces.hh)
 //   shape   ParticleShape rest geometry and connectivity (ParticleShape.hh:21-212)
 //   inertia DeformableParticle3D::compute_moment_of_intertia (DeformableParticle3D.hh:173-272)
+//   pipe    body-force flow in a pipe along x with the first-order walls of
+//           progs/rbc_in_pipe/rbc_in_pipe.cpp:306-318 (BounceBack outside PipeBoundary,
+//           NoDynamics beyond radius + 1), in a periodic box
 //   interact the vertex forces of one IB step with a particle-particle interaction
 //           (add_pp_force, CollisionForces.h) and a wall interaction decorator
 //           (add_force_decorator, ForceDecorator.hh) on parallel plates (Boundary.h:305-365)
@@ -192,6 +195,48 @@ static int run_lbm(const Bundle& in, const char* out) {
             dump_velocity(w, "1", lattice);
         }
     }
+    dump_lattice(w, "end", lattice);
+    dump_velocity(w, "end", lattice);
+    return 0;
+}
+
+// Cells outside the pipe get BounceBack; cells outside the pipe widened by (plint)sqrt(2) = 1
+// get NoDynamics, the two defineDynamics calls of rbc_in_pipe.cpp:306-318 (domain functionals
+// BoundarySurface and BoundaryOutside evaluated on PipeBoundary::contains).
+static int run_pipe(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    const std::vector<double> g = recio::need(in, "pipe").d;  // y0, z0, radius
+    const T omega = recio::num(in, "omega");
+    const long long steps = recio::inum(in, "steps");
+    const std::vector<double> body = recio::need(in, "body").d;
+    PipeBoundary<T> pipe(g[0], g[1], g[2], (T)(nx - 1));
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(omega, omega));
+    lattice.toggleInternalStatistics(false);
+    lattice.periodicity().toggleAll(true);
+    std::vector<long long> mask((size_t)nx * ny * nz, 0);
+    const plint margin = (plint)std::sqrt(2.0);
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x) {
+                const Array<T, 3> p((T)x, (T)y, (T)z);
+                if (!pipe.contains(p)) mask[lidx(x, y, z, nx, ny)] = 1;
+                if (!pipe.contains(p, (T)-margin)) mask[lidx(x, y, z, nx, ny)] = 2;
+            }
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x) {
+                const long long t = mask[lidx(x, y, z, nx, ny)];
+                if (t == 1) defineDynamics(lattice, Box3D(x, x, y, y, z, z), new BounceBack<T, DESCRIPTOR>());
+                else if (t == 2) defineDynamics(lattice, Box3D(x, x, y, y, z, z), new NoDynamics<T, DESCRIPTOR>());
+            }
+    const Box3D domain = lattice.getBoundingBox();
+    setExternalVector(lattice, domain, DESCRIPTOR<T>::ExternalField::forceBeginsAt, Array<T, 3>(body[0], body[1], body[2]));
+    initializeAtEquilibrium(lattice, domain, (T)1, Array<T, 3>(0., 0., 0.));
+    lattice.initialize();
+    for (long long it = 0; it < steps; ++it) lattice.collideAndStream();
+    recio::Writer w(out);
+    w.i("mask", shp(nz, ny, nx), mask);
     dump_lattice(w, "end", lattice);
     dump_velocity(w, "end", lattice);
     return 0;
@@ -620,6 +665,7 @@ int main(int argc, char** argv) {
     if (c == "shape") return run_shape(in, argv[3]);
     if (c == "inertia") return run_inertia(in, argv[3]);
     if (c == "interact") return run_interact(in, argv[3]);
+    if (c == "pipe") return run_pipe(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

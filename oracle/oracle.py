@@ -91,6 +91,8 @@ def lib():
             "orc_sys_step": (None, [C.c_void_p, C.c_int64]),
             "orc_sys_lattice_only_step": (None, [C.c_void_p, C.c_int64]),
             "orc_sys_get_particle": (None, [C.c_void_p, C.c_int32, dp, dp, dp, dp]),
+            "orc_pipe_celltypes": (None, [C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double,
+                                          C.c_void_p]),
             "orc_potential_eval": (C.c_double, [C.POINTER(Potential), C.c_double]),
             "orc_wall_forces": (None, [C.POINTER(Potential), C.c_int32, C.c_double, C.c_double, C.c_int64, dp, dp]),
             "orc_pp_forces_grid": (None, [Lp, C.POINTER(Potential), C.c_int64, dp, i32p, dp]),
@@ -375,3 +377,11 @@ def pp_forces(L, pot: Potential, pos, owner, force=None, grid=False):
     fn = lib().orc_pp_forces_grid if grid else lib().orc_pp_forces
     fn(C.byref(L), C.byref(pot), pos.shape[0], _d(pos), _i32(own), _d(out))
     return out
+
+
+def pipe_celltypes(dims, y0, z0, radius):
+    """(nz, ny, nx) uint8 cell types of the reference's first-order pipe walls."""
+    nx, ny, nz = dims
+    t = np.zeros((nz, ny, nx), dtype=np.uint8)
+    lib().orc_pipe_celltypes(nx, ny, nz, float(y0), float(z0), float(radius), t.ctypes.data)
+    return t

@@ -339,8 +339,16 @@ def case_interact():
         save(name, inp, {"force_a": out["force_a"], "force_b": out["force_b"]})
 
 
+def case_lbm_pipe():
+    """Body-force flow in a pipe along x with the reference's first-order pipe walls
+    (BounceBack outside PipeBoundary, NoDynamics beyond radius + 1), periodic box."""
+    inp = dict(dims=[12, 21, 21], pipe=[10.0, 10.2, 7.3], omega=1.0 / 0.8, body=[1e-4, 0.0, 0.0], steps=40)
+    out = run("pipe", inp)
+    save("lbm_pipe", inp, {"mask": out["mask"], "fbar_end": out["fbar_end"], "u_end": out["u_end"]})
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
-         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact]
+         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):

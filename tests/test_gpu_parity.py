@@ -503,3 +503,24 @@ def test_nan_is_detected(ctx):
     with pytest.raises(bib.BibError) as e:
         lat.check_health()
     assert e.value.status == -4
+
+
+@pytest.mark.parametrize("kernel,storage,tol", [("staged", "f64", 1e-15), ("rows", "f64", 1e-15), ("staged", "f32", 1e-7)])
+def test_pipe_walls_match_reference(ctx, kernel, storage, tol):
+    """First-order pipe walls (rbc_in_pipe.cpp: BounceBack outside the pipe, NoDynamics beyond
+    radius + 1) with a body force, against the reference's populations after 40 steps."""
+    d = golden("lbm_pipe")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    y0, z0, R = d["in_pipe"]
+    om = float(d["in_omega"])
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=om, storage=storage)
+    lat.set_tuning(kernel)
+    lat.set_pipe_walls(y0, z0, R)
+    lat.initialize_at_equilibrium(None, np.zeros((3, nz, ny, nx)))
+    lat.set_external_force(np.asarray(d["in_body"])[:, None, None, None])
+    lat.collide_and_stream(int(d["in_steps"]))
+    f = lat.receive()
+    assert np.abs(f - d["out_fbar_end"]).max() <= tol
+    fluid = d["out_mask"] == 0
+    u = lat.compute_velocity()
+    assert np.abs(u[:, fluid] - d["out_u_end"][:, fluid]).max() <= 10 * tol

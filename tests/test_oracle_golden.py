@@ -221,3 +221,21 @@ def test_grid_search_misses_diagonal_pairs():
     d = np.linalg.norm(pos[1] - pos[0])
     expect = -(0.8 - d) / d * (pos[1] - pos[0])
     assert np.allclose(f[0], expect, rtol=1e-14) and np.array_equal(f[1], -f[0])
+
+
+def test_pipe_first_order_walls():
+    """rbc_in_pipe.cpp's first-order pipe walls (BounceBack outside PipeBoundary, NoDynamics
+    beyond radius + 1) with a body force: the cell types and the flow after 40 steps."""
+    d = golden("lbm_pipe")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    y0, z0, R = d["in_pipe"]
+    types = O.pipe_celltypes((nx, ny, nz), y0, z0, R)
+    assert np.array_equal(types, d["out_mask"])
+    om = float(d["in_omega"])
+    L = O.lattice((nx, ny, nz), (1, 1, 1), "bgk_guo_vof", om, om, celltype=types)
+    n = nx * ny * nz
+    F = np.broadcast_to(np.asarray(d["in_body"])[:, None, None, None], (3, nz, ny, nx))
+    f = O.collide_stream(L, np.zeros((19, nz, ny, nx)), F, np.zeros((nz, ny, nx)), int(d["in_steps"]))
+    assert np.array_equal(f, d["out_fbar_end"])
+    assert np.array_equal(O.compute_velocity(L, f, F), d["out_u_end"])
+    assert n > 0 and d["out_u_end"][0].max() > 1e-3
