@@ -467,6 +467,7 @@ void orc_collide_stream(const orc_lattice* L, double* f, double* ftmp, const dou
             }
     memcpy(f, ftmp, sizeof(double) * Q * n);
     orc_apply_fd_walls(L, f, F);
+    if (L->guo) orc_apply_guo(L, f);
 }
 
 void orc_compute_velocity(const orc_lattice* L, const double* f, const double* F, double* u) {
@@ -914,6 +915,120 @@ void orc_pipe_celltypes(int64_t nx, int64_t ny, int64_t nz, double y0, double z0
                 if (!(r2 < (radius - margin) * (radius - margin))) t = ORC_CELL_NO_DYNAMICS;
                 types[x + nx * (y + ny * z)] = t;
             }
+}
+
+/* PipeBoundary::trace_ray (fsi/Boundary.h:164-187): crossing parameter t in [0, 1] of the
+ * segment x0 -> x1 with the cylinder around the x axis through (y0, z0) */
+static int pipe_trace_ray(double py0, double pz0, double radius, const double* x0, const double* x1, double* t) {
+    const double y1 = x0[1] - py0, y2 = x1[1] - py0, z1 = x0[2] - pz0, z2 = x1[2] - pz0;
+    const double a = (y2 - y1) * (y2 - y1) + (z2 - z1) * (z2 - z1);
+    const double b = y1 * (y2 - y1) + z1 * (z2 - z1);
+    const double c = y1 * y1 + z1 * z1 - radius * radius;
+    const double disc = b * b - c * a;
+    if (disc < 0. || fabs(a) < 10 * DBL_EPSILON) return 0;
+    const double bOverA = -b / a;
+    const double sqrtDisc = sqrt(disc) / a;
+    *t = bOverA - sqrtDisc;
+    if (*t >= 0. && *t <= 1.) return 1;
+    *t = bOverA + sqrtDisc;
+    if (*t >= 0. && *t <= 1.) return 1;
+    return 0;
+}
+
+/* GuoRigidWallBoundaryInstantiator::process (fsi/GuoBoundaryCondition.hh:62-130) on a
+ * PipeBoundary: every node outside the pipe with a lattice vector that crosses the wall becomes a
+ * wall node; among its crossing vectors it keeps the one whose normalised direction has the
+ * smallest cosine with the outward normal at pos + dir/|dir| * t, with delta = 1 - t.  Then
+ * rbc_in_pipe.cpp:313-318 gives NoDynamics to the nodes outside radius + (plint)sqrt(2). */
+int64_t orc_pipe_guo_nodes(int64_t nx, int64_t ny, int64_t nz, double y0, double z0, double radius,
+                           orc_guo_node* nodes, uint8_t* types) {
+    init_weights();
+    const double margin = -(double)(int64_t)sqrt(2.0);
+    int64_t count = 0;
+    for (int64_t x = 0; x < nx; ++x)
+        for (int64_t y = 0; y < ny; ++y)
+            for (int64_t z = 0; z < nz; ++z) {
+                const double pos[3] = {(double)x, (double)y, (double)z};
+                const double dy = pos[1] - y0, dz = pos[2] - z0;
+                const int nodyn = !((dy * dy + dz * dz) < (radius - margin) * (radius - margin));
+                if (types) types[x + nx * (y + ny * z)] = nodyn ? ORC_CELL_NO_DYNAMICS : ORC_CELL_FLUID;
+                if ((dy * dy + dz * dz) < radius * radius) continue;
+                double cos_min = 2, delta_min = -1;
+                int dir_min = 0, found = 0;
+                for (int i = 1; i < Q; ++i) {
+                    const double c[3] = {(double)CX[i], (double)CY[i], (double)CZ[i]};
+                    const double p2[3] = {pos[0] + c[0], pos[1] + c[1], pos[2] + c[2]};
+                    double t = -1;
+                    if (!pipe_trace_ray(y0, z0, radius, pos, p2, &t)) continue;
+                    const double cn = sqrt((double)(CX[i] * CX[i] + CY[i] * CY[i] + CZ[i] * CZ[i]));
+                    const double d2[3] = {c[0] / cn, c[1] / cn, c[2] / cn};
+                    const double w[3] = {pos[0] + d2[0] * t, pos[1] + d2[1] * t, pos[2] + d2[2] * t};
+                    /* PipeBoundary::get_normal (Boundary.h:245-249) */
+                    const double nv[3] = {0, w[1] - y0, w[2] - z0};
+                    const double nn = sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+                    const double nu[3] = {nv[0] / nn, nv[1] / nn, nv[2] / nn};
+                    const double cosang = nu[0] * d2[0] + nu[1] * d2[1] + nu[2] * d2[2];
+                    if (cosang < cos_min) {
+                        dir_min = i;
+                        cos_min = cosang;
+                        delta_min = 1 - t;
+                    }
+                    found = 1;
+                }
+                if (!found) continue;
+                if (nodes) {
+                    orc_guo_node* g = &nodes[count];
+                    g->x = x, g->y = y, g->z = z;
+                    g->dir = dir_min;
+                    g->nodyn = nodyn;
+                    g->delta = delta_min;
+                    g->u[0] = g->u[1] = g->u[2] = 0.0;
+                }
+                ++count;
+            }
+    return count;
+}
+
+/* GuoRigidWallBoundaryFunctional::process with depth 2 (GuoBoundaryCondition.hh:133-187): the
+ * wall node's populations become the equilibrium of the extrapolated wall momentum (with the
+ * density of the first fluid node) plus the extrapolated non-equilibrium part of the two fluid
+ * nodes along the chosen lattice vector.  A NoDynamics node's equilibrium is 0. */
+void orc_apply_guo(const orc_lattice* L, double* f) {
+    init_weights();
+    const int64_t nx = L->nx, ny = L->ny, nz = L->nz, n = nx * ny * nz;
+    for (int64_t g = 0; g < L->nguo; ++g) {
+        const orc_guo_node* w = &L->guo[g];
+        const int d = w->dir;
+        double fc[2][Q], rb[2], j[2][3], fneq[2][Q];
+        for (int m = 0; m < 2; ++m) {
+            int64_t xs = w->x + (m + 1) * CX[d], ys = w->y + (m + 1) * CY[d], zs = w->z + (m + 1) * CZ[d];
+            xs = wrap(xs, nx), ys = wrap(ys, ny), zs = wrap(zs, nz);
+            const int64_t k = cell_index(L, xs, ys, zs);
+            for (int i = 0; i < Q; ++i) fc[m][i] = f[i * n + k];
+            get_rhoBar_j(fc[m], &rb[m], j[m]);
+            const double jsq = j[m][0] * j[m][0] + j[m][1] * j[m][1] + j[m][2] * j[m][2];
+            const double invRho = (double)1 / (rb[m] + (double)1);
+            for (int i = 0; i < Q; ++i) fneq[m][i] = fc[m][i] - bgk_ma2_equilibrium(i, rb[m], invRho, j[m], jsq);
+        }
+        const double rbw = rb[0];
+        double wj[3], jw[3], fw[Q];
+        for (int c = 0; c < 3; ++c) wj[c] = (rbw + (double)1) * w->u[c];
+        const double dl = w->delta;
+        if (dl < (double)0.75) {
+            for (int c = 0; c < 3; ++c)
+                jw[c] = wj[c] + (dl - (double)1.) * j[0][c] +
+                        ((double)1. - dl) / ((double)1. + dl) * ((double)2. * wj[c] + (dl - (double)1.) * j[1][c]);
+            for (int i = 0; i < Q; ++i) fw[i] = dl * fneq[0][i] + ((double)1. - dl) * fneq[1][i];
+        } else {
+            for (int c = 0; c < 3; ++c) jw[c] = (double)1. / dl * (wj[c] + (dl - (double)1.) * j[0][c]);
+            for (int i = 0; i < Q; ++i) fw[i] = fneq[0][i];
+        }
+        const double jsq = jw[0] * jw[0] + jw[1] * jw[1] + jw[2] * jw[2];
+        const double invRho = (double)1 / (rbw + (double)1);
+        const int64_t k = cell_index(L, w->x, w->y, w->z);
+        for (int i = 0; i < Q; ++i)
+            f[i * n + k] = (w->nodyn ? 0.0 : bgk_ma2_equilibrium(i, rbw, invRho, jw, jsq)) + fw[i];
+    }
 }
 
 /* ------------------------------------------------------------------ interaction forces */

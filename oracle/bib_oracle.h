@@ -42,6 +42,15 @@ enum {
     ORC_P_K_AREA_LOCAL, ORC_P_K_VOLUME, ORC_P_VOL_DESIRED, ORC_P_K_BEND, ORC_P_THETA0, ORC_P_COUNT
 };
 
+/* a node of GuoRigidWallBoundary (fsi/GuoBoundaryCondition.h:19-26) */
+typedef struct {
+    int64_t x, y, z;  /* the wall node (outside the boundary) */
+    int32_t dir;      /* population index of the lattice vector towards the fluid */
+    int32_t nodyn;    /* the node carries NoDynamics: its equilibrium is 0 */
+    double delta;     /* 1 - t of the boundary crossing along that vector */
+    double u[3];      /* wall velocity */
+} orc_guo_node;
+
 typedef struct {
     int64_t nx, ny, nz;
     int32_t periodic[3];
@@ -52,6 +61,8 @@ typedef struct {
     double wall_u[4][3];        /* velocity of the y-, y+, z-, z+ walls */
     int32_t envelope_swap;      /* reproduce the reference's periodic-envelope omega swap (see .c) */
     const uint8_t* celltype;    /* NULL or per cell: 0 the lattice's dynamics, 1 BounceBack, 2 NoDynamics */
+    const orc_guo_node* guo;    /* second-order rigid-wall nodes, rebuilt after every collide-and-stream */
+    int64_t nguo;
 } orc_lattice;
 
 enum { ORC_CELL_FLUID = 0, ORC_CELL_BOUNCE_BACK = 1, ORC_CELL_NO_DYNAMICS = 2 };
@@ -93,6 +104,12 @@ int32_t orc_threads(void);
 /* ---- coupled system (mirrors the product's C ABI) ---- */
 /* BounceBack / NoDynamics cells of the reference's first-order pipe walls (pipe along x) */
 void orc_pipe_celltypes(int64_t nx, int64_t ny, int64_t nz, double y0, double z0, double radius, uint8_t* types);
+/* the second-order pipe walls: GuoRigidWallBoundary nodes (returns their count; `nodes` may be NULL to
+ * count) and the NoDynamics cells beyond radius + 1 (types, 0 elsewhere) */
+int64_t orc_pipe_guo_nodes(int64_t nx, int64_t ny, int64_t nz, double y0, double z0, double radius,
+                           orc_guo_node* nodes, uint8_t* types);
+/* GuoRigidWallBoundaryFunctional::process on a post-streaming state */
+void orc_apply_guo(const orc_lattice* L, double* f);
 
 /* interaction potentials (fsi/Potentials.h): kind, cutoff r0 (Morse r_min / spring min_dist), Morse beta, strength */
 enum { ORC_POTENTIAL_NONE = 0, ORC_POTENTIAL_MORSE = 1, ORC_POTENTIAL_SPRING = 2 };

@@ -17,6 +17,8 @@
 //   pipe    body-force flow in a pipe along x with the first-order walls of
 //           progs/rbc_in_pipe/rbc_in_pipe.cpp:306-318 (BounceBack outside PipeBoundary,
 //           NoDynamics beyond radius + 1), in a periodic box
+//   pipe_guo the same flow with the second-order walls: GuoRigidWallBoundary on the pipe
+//           (rbc_in_pipe.cpp:303-305, fsi/GuoBoundaryCondition.hh) and NoDynamics beyond radius + 1
 //   interact the vertex forces of one IB step with a particle-particle interaction
 //           (add_pp_force, CollisionForces.h) and a wall interaction decorator
 //           (add_force_decorator, ForceDecorator.hh) on parallel plates (Boundary.h:305-365)
@@ -27,6 +29,8 @@
 #include "palabos3D.hh"
 #include "fsi/headers.h"
 #include "fsi/headers.hh"
+#include "fsi/GuoBoundaryCondition.h"
+#include "fsi/GuoBoundaryCondition.hh"
 
 #include <string>
 #include <vector>
@@ -237,6 +241,51 @@ static int run_pipe(const Bundle& in, const char* out) {
     for (long long it = 0; it < steps; ++it) lattice.collideAndStream();
     recio::Writer w(out);
     w.i("mask", shp(nz, ny, nx), mask);
+    dump_lattice(w, "end", lattice);
+    dump_velocity(w, "end", lattice);
+    return 0;
+}
+
+static int run_pipe_guo(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    const std::vector<double> g = recio::need(in, "pipe").d;  // y0, z0, radius
+    const T omega = recio::num(in, "omega");
+    const long long steps = recio::inum(in, "steps");
+    const std::vector<double> body = recio::need(in, "body").d;
+    PipeBoundary<T> pipe(g[0], g[1], g[2], (T)(nx - 1));
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(omega, omega));
+    lattice.toggleInternalStatistics(false);
+    lattice.periodicity().toggleAll(true);
+    GuoRigidWallBoundary<T, DESCRIPTOR> walls(pipe, lattice);
+    walls.insert();
+    const plint margin = (plint)std::sqrt(2.0);
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x)
+                if (!pipe.contains(Array<T, 3>((T)x, (T)y, (T)z), (T)-margin))
+                    defineDynamics(lattice, Box3D(x, x, y, y, z, z), new NoDynamics<T, DESCRIPTOR>());
+    const Box3D domain = lattice.getBoundingBox();
+    setExternalVector(lattice, domain, DESCRIPTOR<T>::ExternalField::forceBeginsAt, Array<T, 3>(body[0], body[1], body[2]));
+    initializeAtEquilibrium(lattice, domain, (T)1, Array<T, 3>(0., 0., 0.));
+    lattice.initialize();
+    recio::Writer w(out);
+    dump_lattice(w, "0", lattice);
+    std::vector<long long> loc, dir;
+    std::vector<double> delta;
+    for (GuoRigidWallBoundary<T, DESCRIPTOR>::iterator it = walls.begin(); it != walls.end(); ++it) {
+        loc.push_back(it->location.x), loc.push_back(it->location.y), loc.push_back(it->location.z);
+        dir.push_back(it->direction.x), dir.push_back(it->direction.y), dir.push_back(it->direction.z);
+        delta.push_back(it->delta);
+    }
+    const long long nw = (long long)delta.size();
+    w.i("wall_loc", shp(nw, 3), loc);
+    w.i("wall_dir", shp(nw, 3), dir);
+    w.d("wall_delta", shp(nw), delta);
+    for (long long it = 0; it < steps; ++it) {
+        lattice.collideAndStream();
+        if (it == 0) dump_lattice(w, "1", lattice);
+    }
     dump_lattice(w, "end", lattice);
     dump_velocity(w, "end", lattice);
     return 0;
@@ -666,6 +715,7 @@ int main(int argc, char** argv) {
     if (c == "inertia") return run_inertia(in, argv[3]);
     if (c == "interact") return run_interact(in, argv[3]);
     if (c == "pipe") return run_pipe(in, argv[3]);
+    if (c == "pipe_guo") return run_pipe_guo(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

@@ -23,6 +23,11 @@ PARAM_KEYS = ["G", "C", "nu_s", "kb", "shear_modulus", "L0", "k_area_global", "k
               "k_volume", "vol_desired", "k_bend", "theta0"]
 
 
+class GuoNode(C.Structure):
+    _fields_ = [("x", C.c_int64), ("y", C.c_int64), ("z", C.c_int64), ("dir", C.c_int32), ("nodyn", C.c_int32),
+                ("delta", C.c_double), ("u", C.c_double * 3)]
+
+
 class Lattice(C.Structure):
     _fields_ = [
         ("nx", C.c_int64), ("ny", C.c_int64), ("nz", C.c_int64),
@@ -33,6 +38,8 @@ class Lattice(C.Structure):
         ("wall_u", (C.c_double * 3) * 4),
         ("envelope_swap", C.c_int32),
         ("celltype", C.c_void_p),
+        ("guo", C.c_void_p),
+        ("nguo", C.c_int64),
     ]
 
 
@@ -93,6 +100,9 @@ def lib():
             "orc_sys_get_particle": (None, [C.c_void_p, C.c_int32, dp, dp, dp, dp]),
             "orc_pipe_celltypes": (None, [C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double,
                                           C.c_void_p]),
+            "orc_pipe_guo_nodes": (C.c_int64, [C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double,
+                                               C.c_void_p, C.c_void_p]),
+            "orc_apply_guo": (None, [Lp, dp]),
             "orc_potential_eval": (C.c_double, [C.POINTER(Potential), C.c_double]),
             "orc_wall_forces": (None, [C.POINTER(Potential), C.c_int32, C.c_double, C.c_double, C.c_int64, dp, dp]),
             "orc_pp_forces_grid": (None, [Lp, C.POINTER(Potential), C.c_int64, dp, i32p, dp]),
@@ -385,3 +395,27 @@ def pipe_celltypes(dims, y0, z0, radius):
     t = np.zeros((nz, ny, nx), dtype=np.uint8)
     lib().orc_pipe_celltypes(nx, ny, nz, float(y0), float(z0), float(radius), t.ctypes.data)
     return t
+
+
+def pipe_guo_nodes(dims, y0, z0, radius):
+    """GuoRigidWallBoundary nodes of a pipe along x and the NoDynamics cells beyond radius + 1:
+    (ctypes array of GuoNode, (nz, ny, nx) uint8 cell types)."""
+    nx, ny, nz = dims
+    cnt = lib().orc_pipe_guo_nodes(nx, ny, nz, float(y0), float(z0), float(radius), None, None)
+    nodes = (GuoNode * max(cnt, 1))()
+    t = np.zeros((nz, ny, nx), dtype=np.uint8)
+    lib().orc_pipe_guo_nodes(nx, ny, nz, float(y0), float(z0), float(radius), C.cast(nodes, C.c_void_p), t.ctypes.data)
+    return nodes, int(cnt), t
+
+
+def set_guo(L, nodes, count):
+    """Attach Guo wall nodes to a lattice (the caller keeps `nodes` alive)."""
+    L.guo = C.cast(nodes, C.c_void_p)
+    L.nguo = count
+    return L
+
+
+def apply_guo(L, f):
+    out = f64(f).copy()
+    lib().orc_apply_guo(C.byref(L), _d(out))
+    return out

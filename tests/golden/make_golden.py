@@ -347,8 +347,16 @@ def case_lbm_pipe():
     save("lbm_pipe", inp, {"mask": out["mask"], "fbar_end": out["fbar_end"], "u_end": out["u_end"]})
 
 
+def case_lbm_pipe_guo():
+    """The same pipe flow with the reference's second-order walls (GuoRigidWallBoundary)."""
+    inp = dict(dims=[12, 21, 21], pipe=[10.0, 10.2, 7.3], omega=1.0 / 0.8, body=[1e-4, 0.0, 0.0], steps=40)
+    out = run("pipe_guo", inp)
+    save("lbm_pipe_guo", inp, {k: out[k] for k in ("wall_loc", "wall_dir", "wall_delta", "fbar_0", "fbar_1",
+                                                     "fbar_end", "u_end")})
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
-         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe]
+         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):

@@ -239,3 +239,31 @@ def test_pipe_first_order_walls():
     assert np.array_equal(f, d["out_fbar_end"])
     assert np.array_equal(O.compute_velocity(L, f, F), d["out_u_end"])
     assert n > 0 and d["out_u_end"][0].max() > 1e-3
+
+
+def test_pipe_second_order_walls():
+    """GuoRigidWallBoundary on the pipe (rbc_in_pipe.cpp's second-order walls): the wall nodes
+    with their lattice vectors and distances, the state after initialize(), after one step and
+    after 40 steps of body-force flow."""
+    d = golden("lbm_pipe_guo")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    y0, z0, R = d["in_pipe"]
+    nodes, cnt, types = O.pipe_guo_nodes((nx, ny, nz), y0, z0, R)
+    assert cnt == d["out_wall_loc"].shape[0]
+    C = np.array([[0, 0, 0], [-1, 0, 0], [0, -1, 0], [0, 0, -1], [-1, -1, 0], [-1, 1, 0], [-1, 0, -1], [-1, 0, 1],
+                  [0, -1, -1], [0, -1, 1], [1, 0, 0], [0, 1, 0], [0, 0, 1], [1, 1, 0], [1, -1, 0], [1, 0, 1],
+                  [1, 0, -1], [0, 1, 1], [0, 1, -1]])
+    loc = np.array([[nodes[k].x, nodes[k].y, nodes[k].z] for k in range(cnt)])
+    assert np.array_equal(loc, d["out_wall_loc"])
+    assert np.array_equal(C[[nodes[k].dir for k in range(cnt)]], d["out_wall_dir"])
+    assert np.array_equal(np.array([nodes[k].delta for k in range(cnt)]), d["out_wall_delta"])
+    om = float(d["in_omega"])
+    L = O.set_guo(O.lattice((nx, ny, nz), (1, 1, 1), "bgk_guo_vof", om, om, celltype=types), nodes, cnt)
+    f0 = O.apply_guo(L, np.zeros((19, nz, ny, nx)))  # initializeAtEquilibrium + initialize()
+    assert np.array_equal(f0, d["out_fbar_0"])
+    F = np.broadcast_to(np.asarray(d["in_body"])[:, None, None, None], (3, nz, ny, nx))
+    f1 = O.collide_stream(L, f0, F, np.zeros((nz, ny, nx)), 1)
+    assert np.array_equal(f1, d["out_fbar_1"])
+    fe = O.collide_stream(L, f0, F, np.zeros((nz, ny, nx)), int(d["in_steps"]))
+    assert np.array_equal(fe, d["out_fbar_end"])
+    assert np.array_equal(O.compute_velocity(L, fe, F), d["out_u_end"])
