@@ -229,9 +229,11 @@ class Lattice:
         t = np.ascontiguousarray(np.broadcast_to(types, self.shape), dtype=np.uint8)
         self.ctx.check(self.ctx.lib.bib_lattice_set_cell_types(self.ctx.h, self.h, t.ctypes.data))
 
-    def set_pipe_walls(self, y0, z0, radius):
-        """First-order walls of a pipe along x (rbc_in_pipe.cpp: BounceBack outside, NoDynamics beyond R + 1)."""
-        self.ctx.check(self.ctx.lib.bib_lattice_set_pipe_walls(self.ctx.h, self.h, float(y0), float(z0), float(radius)))
+    def set_pipe_walls(self, y0, z0, radius, second_order=False):
+        """Walls of a pipe along x as rbc_in_pipe.cpp sets them: BounceBack outside (first order) or
+        GuoRigidWallBoundary (second order), NoDynamics beyond radius + 1."""
+        self.ctx.check(self.ctx.lib.bib_lattice_set_pipe_walls(self.ctx.h, self.h, float(y0), float(z0), float(radius),
+                                                               int(bool(second_order))))
 
     def set_tuning(self, kernel="auto", tile_cells=0, stages=0, membrane_block=0):
         """Collide-and-stream kernel ("auto", "rows" or "staged"), staged tile size in cells,

@@ -777,6 +777,9 @@ bib_status build_batch(bib_ctx* c, Batch& B) {
         if (L.inter.npp > 0)
             return fail(c, BIB_EUNSUPPORTED, "batched steps do not evaluate particle-particle interactions (lattice %d)",
                         B.handles[i]);
+        if (L.nguo > 0)
+            return fail(c, BIB_EUNSUPPORTED, "batched steps do not apply second-order rigid walls (lattice %d)",
+                        B.handles[i]);
         B.versions[i] = L.version;
         B.state0[i] = lattice_state(L);
         for (int p = 0; p < 2; ++p) {
@@ -1032,6 +1035,7 @@ void bib_destroy(bib_ctx* c) {
         cudaFree(Lp->wall);
         cudaFree(Lp->phase);
         cudaFree(Lp->celltype);
+        cudaFree(Lp->guo);
     }
     for (auto& S : c->shapes) {
         cudaFree(S->dev.rest);
@@ -1216,7 +1220,7 @@ bib_status bib_spread_forces_noalloc(bib_ctx* c, int32_t h, const double* pos, c
     return BIB_OK;
 }
 
-bib_status bib_lattice_set_cell_types(bib_ctx* c, int32_t h, const uint8_t* types) {
+static bib_status set_cell_types_impl(bib_ctx* c, int32_t h, const uint8_t* types) {
     Lattice* L = get_lattice(c, h);
     if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
@@ -1237,24 +1241,120 @@ bib_status bib_lattice_set_cell_types(bib_ctx* c, int32_t h, const uint8_t* type
     return BIB_OK;
 }
 
-bib_status bib_lattice_set_pipe_walls(bib_ctx* c, int32_t h, double y0, double z0, double radius) {
+bib_status bib_lattice_set_cell_types(bib_ctx* c, int32_t h, const uint8_t* types) {
     Lattice* L = get_lattice(c, h);
     if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
-    if (!(radius > 0) || !std::isfinite(y0) || !std::isfinite(z0)) return fail(c, BIB_EINVAL, "bad pipe geometry");
+    // explicit cell types replace second-order pipe walls
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(L->guo);
+    L->guo = nullptr;
+    L->nguo = 0;
+    return set_cell_types_impl(c, h, types);
+}
+
+// PipeBoundary::trace_ray (fsi/Boundary.h:164-187): crossing parameter t in [0, 1] of the
+// segment p0 -> p1 with the cylinder of `radius` around the x axis through (y0, z0)
+static bool pipe_trace_ray(double py0, double pz0, double radius, const double* p0, const double* p1, double& t) {
+    const double y1 = p0[1] - py0, y2 = p1[1] - py0, z1 = p0[2] - pz0, z2 = p1[2] - pz0;
+    const double a = (y2 - y1) * (y2 - y1) + (z2 - z1) * (z2 - z1);
+    const double b = y1 * (y2 - y1) + z1 * (z2 - z1);
+    const double c = y1 * y1 + z1 * z1 - radius * radius;
+    const double disc = b * b - c * a;
+    if (disc < 0. || std::fabs(a) < 10 * 2.220446049250313e-16) return false;
+    const double bOverA = -b / a;
+    const double sqrtDisc = std::sqrt(disc) / a;
+    t = bOverA - sqrtDisc;
+    if (t >= 0. && t <= 1.) return true;
+    t = bOverA + sqrtDisc;
+    return t >= 0. && t <= 1.;
+}
+
+bib_status bib_lattice_set_pipe_walls(bib_ctx* c, int32_t h, double y0, double z0, double radius, int32_t second_order) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    if (!(radius > 0) || !std::isfinite(y0) || !std::isfinite(z0) || second_order < 0 || second_order > 1)
+        return fail(c, BIB_EINVAL, "bad pipe geometry");
     const int64_t nx = L->d.nx, ny = L->d.ny, nz = L->d.nz;
     std::vector<uint8_t> types((size_t)L->d.n);
     // PipeBoundary::contains (fsi/Boundary.h:149-152) with margins 0 and -(plint)sqrt(2)
     const double margin = -(double)(int64_t)std::sqrt(2.0);
+    auto r2_of = [&](int64_t y, int64_t z) {
+        const double dy = (double)y - y0, dz = (double)z - z0;
+        return dy * dy + dz * dz;
+    };
     for (int64_t z = 0; z < nz; ++z)
         for (int64_t y = 0; y < ny; ++y) {
-            const double dy = (double)y - y0, dz = (double)z - z0;
-            const double r2 = dy * dy + dz * dz;
+            const double r2 = r2_of(y, z);
             uint8_t t = BIB_CELL_FLUID;
-            if (!(r2 < radius * radius)) t = BIB_CELL_BOUNCE_BACK;
+            if (!second_order && !(r2 < radius * radius)) t = BIB_CELL_BOUNCE_BACK;
             if (!(r2 < (radius - margin) * (radius - margin))) t = BIB_CELL_NO_DYNAMICS;
             std::fill(types.begin() + (size_t)(nx * (y + ny * z)), types.begin() + (size_t)(nx * (y + ny * z) + nx), t);
         }
-    return bib_lattice_set_cell_types(c, h, types.data());
+    std::vector<GuoNode> nodes;
+    if (second_order) {
+        // GuoRigidWallBoundaryInstantiator::process (fsi/GuoBoundaryCondition.hh:62-130): nodes
+        // outside the pipe with a lattice vector crossing the wall; among the crossing vectors the
+        // one whose direction has the smallest cosine with the outward normal at the crossing
+        static const int CX[Q] = {0, -1, 0, 0, -1, -1, -1, -1, 0, 0, 1, 0, 0, 1, 1, 1, 1, 0, 0};
+        static const int CY[Q] = {0, 0, -1, 0, -1, 1, 0, 0, -1, -1, 0, 1, 0, 1, -1, 0, 0, 1, 1};
+        static const int CZ[Q] = {0, 0, 0, -1, 0, 0, -1, 1, -1, 1, 0, 0, 1, 0, 0, 1, -1, 1, -1};
+        std::vector<int> is_wall((size_t)L->d.n, 0);
+        for (int64_t x = 0; x < nx; ++x)
+            for (int64_t y = 0; y < ny; ++y)
+                for (int64_t z = 0; z < nz; ++z) {
+                    const double pos[3] = {(double)x, (double)y, (double)z};
+                    if (r2_of(y, z) < radius * radius) continue;
+                    double cos_min = 2, delta_min = -1;
+                    int dir_min = 0;
+                    bool found = false;
+                    for (int i = 1; i < Q; ++i) {
+                        const double cv[3] = {(double)CX[i], (double)CY[i], (double)CZ[i]};
+                        const double p2[3] = {pos[0] + cv[0], pos[1] + cv[1], pos[2] + cv[2]};
+                        double t = -1;
+                        if (!pipe_trace_ray(y0, z0, radius, pos, p2, t)) continue;
+                        const double cn = std::sqrt((double)(CX[i] * CX[i] + CY[i] * CY[i] + CZ[i] * CZ[i]));
+                        const double d2[3] = {cv[0] / cn, cv[1] / cn, cv[2] / cn};
+                        const double w[3] = {pos[0] + d2[0] * t, pos[1] + d2[1] * t, pos[2] + d2[2] * t};
+                        const double nv[3] = {0, w[1] - y0, w[2] - z0};  // PipeBoundary::get_normal
+                        const double nn = std::sqrt(nv[0] * nv[0] + nv[1] * nv[1] + nv[2] * nv[2]);
+                        const double cosang = nv[0] / nn * d2[0] + nv[1] / nn * d2[1] + nv[2] / nn * d2[2];
+                        if (cosang < cos_min) {
+                            dir_min = i;
+                            cos_min = cosang;
+                            delta_min = 1 - t;
+                        }
+                        found = true;
+                    }
+                    if (!found) continue;
+                    GuoNode g{};
+                    g.x = (int)x, g.y = (int)y, g.z = (int)z;
+                    g.dir = dir_min;
+                    g.delta = delta_min;
+                    g.nodyn = types[(size_t)(x + nx * (y + ny * z))] == BIB_CELL_NO_DYNAMICS;
+                    nodes.push_back(g);
+                    is_wall[(size_t)(x + nx * (y + ny * z))] = 1;
+                }
+        // the reconstruction reads two fluid nodes per wall node: they must be neither wall nodes nor
+        // NoDynamics nodes (a pipe a few nodes wide would violate this)
+        for (const GuoNode& g : nodes)
+            for (int m = 1; m <= 2; ++m) {
+                const int64_t xs = ((g.x + m * CX[g.dir]) % nx + nx) % nx, ys = ((g.y + m * CY[g.dir]) % ny + ny) % ny,
+                              zs = ((g.z + m * CZ[g.dir]) % nz + nz) % nz;
+                const size_t k = (size_t)(xs + nx * (ys + ny * zs));
+                if (is_wall[k] || types[k] != BIB_CELL_FLUID)
+                    return fail(c, BIB_EUNSUPPORTED, "pipe too narrow for the second-order walls");
+            }
+    }
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(L->guo);
+    L->guo = nullptr;
+    L->nguo = 0;
+    if (!nodes.empty()) {
+        BIB_CUDA(c, cudaMalloc((void**)&L->guo, nodes.size() * sizeof(GuoNode)));
+        BIB_CUDA(c, cudaMemcpy(L->guo, nodes.data(), nodes.size() * sizeof(GuoNode), cudaMemcpyHostToDevice));
+        L->nguo = (int)nodes.size();
+    }
+    return set_cell_types_impl(c, h, types.data());
 }
 
 bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {

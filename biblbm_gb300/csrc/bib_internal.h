@@ -86,6 +86,18 @@ struct ParticleDev {
 // Per-particle state kept on the device: {area, volume, com[3]}.
 constexpr int STATS = 5;
 
+// A node of the second-order rigid wall (GuoRigidWallBoundary::NodeInfo,
+// fsi/GuoBoundaryCondition.h:19-26): the wall node, the population index of its lattice vector
+// towards the fluid, 1 - t of the wall crossing, the wall velocity, and whether it carries
+// NoDynamics (equilibrium 0).
+struct GuoNode {
+    int x, y, z;
+    int dir;
+    int nodyn;
+    double delta;
+    double u[3];
+};
+
 // Interaction potentials and the wall / particle-particle interactions of a lattice.
 struct PotentialDev {
     int kind;  // BIB_POTENTIAL_*
@@ -204,6 +216,8 @@ struct Lattice {
     void* u = nullptr;                // velocity field, (ux, uy, uz, 0) per cell (double for F64 storage, float otherwise)
     uint8_t* phase = nullptr;
     uint8_t* celltype = nullptr;      // BIB_CELL_* per cell, or nullptr: every cell has the lattice's dynamics
+    GuoNode* guo = nullptr;           // second-order rigid-wall nodes, rebuilt after every collide-and-stream
+    int nguo = 0;
     // immersed boundary
     std::vector<ParticleHost> parts;
     int nvert = 0;

@@ -281,6 +281,55 @@ template <class T>
 __device__ __forceinline__ void fd_wall_cell(const LatticeDesc& d, const T* __restrict__ f, T* __restrict__ wall,
                                              const typename Store<T>::F* __restrict__ F, int x, int z, int side);
 
+// GuoRigidWallBoundaryFunctional::process with depth 2 (fsi/GuoBoundaryCondition.hh:133-187),
+// one thread per wall node after collide-and-stream: the post-streaming states of the two fluid
+// nodes along the node's lattice vector give density, momentum and non-equilibrium parts; the
+// node's new state, the equilibrium of the extrapolated wall momentum (0 for a NoDynamics node)
+// plus the extrapolated non-equilibrium part, is scattered into the post-collision slots it
+// gathers from.  Each slot f*_i(x) is read by the node x + c_i alone, and no wall node's fluid
+// nodes are wall nodes (checked on the host), so the threads never touch each other's data.
+template <class T>
+__global__ void __launch_bounds__(128) k_guo_walls(LatticeDesc d, T* __restrict__ f, const T* __restrict__ wall,
+                                                    const GuoNode* __restrict__ nodes, int n) {
+    using C = typename Store<T>::C;
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= n) return;
+    const GuoNode w = nodes[g];
+    C fc[2][Q], rb[2], j[2][3], fneq[2][Q];
+#pragma unroll
+    for (int m = 0; m < 2; ++m) {
+        const int xs = (int)wrap_index(w.x + (m + 1) * cx(w.dir), d.nx);
+        const int ys = (int)wrap_index(w.y + (m + 1) * cy(w.dir), d.ny);
+        const int zs = (int)wrap_index(w.z + (m + 1) * cz(w.dir), d.nz);
+        gather<T>(d, f, wall, xs, ys, zs, xs + (int64_t)d.nx * (ys + (int64_t)d.ny * zs), fc[m]);
+        rho_bar_j<C>(fc[m], rb[m], j[m]);
+        const C jsq = j[m][0] * j[m][0] + j[m][1] * j[m][1] + j[m][2] * j[m][2];
+        const C invRho = C(1) / (rb[m] + C(1));
+#pragma unroll
+        for (int i = 0; i < Q; ++i) fneq[m][i] = fc[m][i] - bgk_equilibrium<C>(i, rb[m], invRho, j[m], jsq);
+    }
+    const C rbw = rb[0], dl = (C)w.delta;
+    C wj[3], jw[3], fw[Q];
+    for (int c = 0; c < 3; ++c) wj[c] = (rbw + C(1)) * (C)w.u[c];
+    if (dl < C(0.75)) {
+        for (int c = 0; c < 3; ++c)
+            jw[c] = wj[c] + (dl - C(1)) * j[0][c] + (C(1) - dl) / (C(1) + dl) * (C(2) * wj[c] + (dl - C(1)) * j[1][c]);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) fw[i] = dl * fneq[0][i] + (C(1) - dl) * fneq[1][i];
+    } else {
+        for (int c = 0; c < 3; ++c) jw[c] = C(1) / dl * (wj[c] + (dl - C(1)) * j[0][c]);
+#pragma unroll
+        for (int i = 0; i < Q; ++i) fw[i] = fneq[0][i];
+    }
+    const C jsq = jw[0] * jw[0] + jw[1] * jw[1] + jw[2] * jw[2];
+    const C invRho = C(1) / (rbw + C(1));
+    const int64_t k = w.x + (int64_t)d.nx * (w.y + (int64_t)d.ny * w.z);
+#pragma unroll
+    for (int i = 0; i < Q; ++i)
+        scatter_canonical<T>(d, f, const_cast<T*>(wall), i, w.x, w.y, w.z, k,
+                             (double)((w.nodyn ? C(0) : bgk_equilibrium<C>(i, rbw, invRho, jw, jsq)) + fw[i]));
+}
+
 template <class T>
 __global__ void k_fd_walls(LatticeDesc d, const T* __restrict__ f, T* __restrict__ wall,
                            const typename Store<T>::F* __restrict__ F) {
@@ -586,9 +635,16 @@ void launch_fd_walls_batch(const BatchLaunch& B, cudaStream_t s) {
     BIB_DISPATCH(B.storage, fd_walls_batch_t, B, s);
 }
 
+template <class T>
+void guo_walls_t(const Lattice& L, int buf, cudaStream_t s) {
+    k_guo_walls<T><<<(L.nguo + 127) / 128, 128, 0, s>>>(L.d, (T*)L.f[buf], (const T*)L.wall, L.guo, L.nguo);
+}
+
+// The wall processors after a collide-and-stream: finite-difference velocity walls, then the
+// second-order rigid walls (the latter integrated at processor level 1, after the former)
 void launch_fd_walls(const Lattice& L, int buf, int fbuf, cudaStream_t s) {
-    if (!L.d.fd_walls) return;
-    BIB_DISPATCH(L.storage, fd_walls_t, L, buf, fbuf, s);
+    if (L.d.fd_walls) BIB_DISPATCH(L.storage, fd_walls_t, L, buf, fbuf, s);
+    if (L.nguo > 0) BIB_DISPATCH(L.storage, guo_walls_t, L, buf, s);
 }
 
 void launch_velocity_field(const Lattice& L, cudaStream_t s) { BIB_DISPATCH(L.storage, velocity_field_t, L, s); }

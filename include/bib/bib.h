@@ -156,10 +156,13 @@ bib_status bib_lattice_add_domain(bib_ctx* ctx, int64_t nx, int64_t ny, int64_t 
  * colliding, NoDynamics nodes keep theirs; both report zero velocity.  NULL restores the lattice's
  * dynamics everywhere. */
 bib_status bib_lattice_set_cell_types(bib_ctx* ctx, int32_t h, const uint8_t* types);
-/* The first-order pipe walls of progs/rbc_in_pipe/rbc_in_pipe.cpp:306-318 for a PipeBoundary along x
- * through (y0, z0) (fsi/Boundary.h:132-160): BounceBack on the nodes outside the pipe, NoDynamics on
- * those outside radius + 1 (BoundaryOutside with margin (plint)sqrt(2)); replaces the cell types */
-bib_status bib_lattice_set_pipe_walls(bib_ctx* ctx, int32_t h, double y0, double z0, double radius);
+/* The pipe walls of progs/rbc_in_pipe/rbc_in_pipe.cpp:300-318 for a PipeBoundary along x through
+ * (y0, z0) (fsi/Boundary.h:132-249).  second_order = 0: BounceBack on the nodes outside the pipe;
+ * second_order = 1: GuoRigidWallBoundary (fsi/GuoBoundaryCondition.hh): the outside nodes with a
+ * lattice vector crossing the wall are rebuilt after every collide-and-stream from the two fluid
+ * nodes along their best-aligned vector (BIB_EUNSUPPORTED if a pipe is too narrow for that).  Both:
+ * NoDynamics beyond radius + 1.  Replaces the cell types; bib_lattice_set_cell_types removes them. */
+bib_status bib_lattice_set_pipe_walls(bib_ctx* ctx, int32_t h, double y0, double z0, double radius, int32_t second_order);
 /* CoProcessor3D::send, coProcessor3D.h:75-91: whole-domain populations from the host in one of
  * the BIB_LAYOUT_* orders (the PALABOS layout also sets the force and phase scalars). */
 bib_status bib_lattice_send(bib_ctx* ctx, int32_t h, const void* buf, size_t bytes, int32_t layout);

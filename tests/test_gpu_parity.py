@@ -524,3 +524,34 @@ def test_pipe_walls_match_reference(ctx, kernel, storage, tol):
     fluid = d["out_mask"] == 0
     u = lat.compute_velocity()
     assert np.abs(u[:, fluid] - d["out_u_end"][:, fluid]).max() <= 10 * tol
+
+
+# 12-cell rows: FP16 rows (24 bytes) do not fit the staged tile's 16-byte copies
+@pytest.mark.parametrize("kernel,storage,tol", [("staged", "f64", 1e-15), ("rows", "f64", 1e-15), ("staged", "f32", 1e-7),
+                                                ("rows", "f16", 2e-4)])
+def test_second_order_pipe_walls_match_reference(ctx, kernel, storage, tol):
+    """GuoRigidWallBoundary on a pipe (rbc_in_pipe.cpp's second-order walls): the state after
+    initialize(), one step and 40 steps of body-force flow, against the reference."""
+    d = golden("lbm_pipe_guo")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    y0, z0, R = d["in_pipe"]
+    om = float(d["in_omega"])
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=om, storage=storage)
+    lat.set_tuning(kernel)
+    lat.set_pipe_walls(y0, z0, R, second_order=True)
+    lat.initialize_at_equilibrium(None, np.zeros((3, nz, ny, nx)))
+    assert np.abs(lat.receive() - d["out_fbar_0"]).max() <= tol
+    lat.set_external_force(np.asarray(d["in_body"])[:, None, None, None])
+    lat.collide_and_stream(1)
+    assert np.abs(lat.receive() - d["out_fbar_1"]).max() <= tol
+    lat.collide_and_stream(int(d["in_steps"]) - 1)
+    assert np.abs(lat.receive() - d["out_fbar_end"]).max() <= tol
+    u = lat.compute_velocity()
+    assert np.abs(u - d["out_u_end"]).max() <= 10 * tol
+
+
+def test_pipe_too_narrow_for_second_order_walls(ctx):
+    lat = ctx.add_domain(8, 9, 9, periodic=(1, 1, 1), omega=1.0)
+    with pytest.raises(bib.BibError, match="narrow"):
+        lat.set_pipe_walls(4.0, 4.0, 1.2, second_order=True)
+    lat.set_pipe_walls(4.0, 4.0, 1.2)  # first order works at any size
