@@ -1202,13 +1202,16 @@ void orc_pp_forces(const orc_lattice* L, const orc_potential* p, int64_t nv, con
 /* ------------------------------------------------------------------ immersed boundary */
 /* RomaDirac<T,3>::eval and PeskinDirac<T,3>::eval(x), fsi/Dirac.h:27-31 and 78-83 */
 double orc_dirac(int32_t dirac, double x) {
+    if (dirac == ORC_DIRAC_TOPHAT) return 1. - fabs(x); /* TopHatDirac<T,3>::eval, Dirac.h:55-58 */
     const double dx = fabs(x);
     if (dirac == ORC_DIRAC_PESKIN)
         return 0.125 * (dx <= 1 ? (3 - 2 * dx + sqrt(1 + 4 * dx * (1 - dx))) : (5 - 2 * dx - sqrt(-7 + 4 * dx * (3 - dx))));
     return (1.0 / 6.0) * (dx > 0.5 ? (5.0 - 3 * dx - sqrt(-3 * (1 - dx) * (1 - dx) + 1)) : 2.0 * (1 + sqrt(1 - 3 * dx * dx)));
 }
-static double half_support(int32_t dirac) { return dirac == ORC_DIRAC_PESKIN ? 2.0 : 1.5; }
-static int support(int32_t dirac) { return dirac == ORC_DIRAC_PESKIN ? 4 : 3; }
+static double half_support(int32_t dirac) {
+    return dirac == ORC_DIRAC_PESKIN ? 2.0 : (dirac == ORC_DIRAC_TOPHAT ? 1.0 : 1.5);
+}
+static int support(int32_t dirac) { return dirac == ORC_DIRAC_PESKIN ? 4 : (dirac == ORC_DIRAC_TOPHAT ? 2 : 3); }
 
 /* Arithmetic1D::min_mod_diff for a periodic axis, fsi/Periodicity.h:26-34,93-96 */
 static double axis_dist(const orc_lattice* L, int d, double a, double b) {
@@ -1230,7 +1233,18 @@ static int rect_contains(const orc_lattice* L, const double* lo, const double* h
 /* Node classification of a single-block domain, ImmersedBoundaryDynamics.hh:46-66 and
  * 351-363: 1 = bulk (fast path without range checks), 2 = envelope (general path),
  * 0 = outside the domain and its envelope (no interpolation, no spreading). */
+static void classify_pipe(const orc_lattice* L, int32_t dirac, int64_t n, const double* pos, int32_t* cls,
+                          const double* pipe);
+
 void orc_classify(const orc_lattice* L, int32_t dirac, int64_t n, const double* pos, int32_t* cls) {
+    classify_pipe(L, dirac, n, pos, cls, NULL);
+}
+
+/* Node classes (create_nodes_from_particle, ImmersedBoundaryDynamics.hh:345-356): 0 outside the
+ * IB envelope, 3 near a pipe boundary (distance_to_boundary_less_than(pos, h + 1), Boundary.h:
+ * 154-157), 1 bulk, 2 envelope.  `pipe` = {y0, z0, radius} or NULL. */
+static void classify_pipe(const orc_lattice* L, int32_t dirac, int64_t n, const double* pos, int32_t* cls,
+                          const double* pipe) {
     const double h = half_support(dirac);
     const double N[3] = {(double)(L->nx - 1), (double)(L->ny - 1), (double)(L->nz - 1)};
     double elo[3], ehi[3], blo[3], bhi[3];
@@ -1244,6 +1258,9 @@ void orc_classify(const orc_lattice* L, int32_t dirac, int64_t n, const double* 
     for (int64_t i = 0; i < n; ++i) {
         const double* p = pos + 3 * i;
         if (!rect_contains(L, elo, ehi, p)) cls[i] = 0;
+        else if (pipe && (p[1] - pipe[0]) * (p[1] - pipe[0]) + (p[2] - pipe[1]) * (p[2] - pipe[1]) >
+                             (pipe[2] - (h + 1.)) * (pipe[2] - (h + 1.)))
+            cls[i] = 3;
         else if (rect_contains(L, blo, bhi, p)) cls[i] = 1;
         else cls[i] = 2;
     }
@@ -1257,6 +1274,108 @@ static int64_t remap_index(const orc_lattice* L, int d, int64_t i, int64_t offse
     return val < 0 ? val + N : val;
 }
 
+static int64_t remap_index(const orc_lattice* L, int d, int64_t i, int64_t offset);
+
+/* GeneralInterpolator::interpolate_node (ImmersedBoundaryDynamics_interpolation.hh:43-78) with
+ * any delta kernel: out += sum of the kernel weights times u over the support, nodes outside the
+ * lattice skipped */
+static void interp_general(const orc_lattice* L, int32_t dirac, int64_t off, const double* u, const double* pr,
+                           double* out) {
+    const int64_t nn = L->nx * L->ny * L->nz;
+    const int64_t nmax[3] = {L->nx, L->ny, L->nz};
+    const int s = support(dirac);
+    int64_t lo[3];
+    for (int d = 0; d < 3; ++d) lo[d] = (int64_t)ceil(pr[d] - half_support(dirac));
+    for (int64_t i = lo[0]; i <= lo[0] + s - 1; ++i) {
+        const int64_t i2 = remap_index(L, 0, i, off) + off;
+        if (i2 < 0 || i2 > nmax[0] - 1) continue;
+        const double dxw = orc_dirac(dirac, (double)i - pr[0]);
+        for (int64_t j = lo[1]; j <= lo[1] + s - 1; ++j) {
+            const int64_t j2 = remap_index(L, 1, j, off) + off;
+            if (j2 < 0 || j2 > nmax[1] - 1) continue;
+            const double dxy = dxw * orc_dirac(dirac, (double)j - pr[1]);
+            for (int64_t kk = lo[2]; kk <= lo[2] + s - 1; ++kk) {
+                const int64_t k2 = remap_index(L, 2, kk, off) + off;
+                if (k2 < 0 || k2 > nmax[2] - 1) continue;
+                const double dxyz = dxy * orc_dirac(dirac, (double)kk - pr[2]);
+                const int64_t c = i2 + L->nx * (j2 + L->ny * k2);
+                for (int d = 0; d < 3; ++d) out[d] += dxyz * u[d * nn + c];
+            }
+        }
+    }
+}
+
+/* GeneralSpreading::spread (ImmersedBoundaryDynamics_forces.hh:52-85) with any delta kernel */
+static void spread_general(const orc_lattice* L, int32_t dirac, int64_t off, const double* pr, const double* fv,
+                           double* F) {
+    const int64_t nn = L->nx * L->ny * L->nz;
+    const int64_t nmax[3] = {L->nx, L->ny, L->nz};
+    const int s = support(dirac);
+    int64_t lo[3];
+    for (int d = 0; d < 3; ++d) lo[d] = (int64_t)ceil(pr[d] - half_support(dirac));
+    for (int64_t i = lo[0]; i <= lo[0] + s - 1; ++i) {
+        const int64_t i2 = remap_index(L, 0, i, off) + off;
+        if (i2 < 0 || i2 > nmax[0] - 1) continue;
+        const double dxw = orc_dirac(dirac, (double)i - pr[0]);
+        for (int64_t j = lo[1]; j <= lo[1] + s - 1; ++j) {
+            const int64_t j2 = remap_index(L, 1, j, off) + off;
+            if (j2 < 0 || j2 > nmax[1] - 1) continue;
+            const double dxy = dxw * orc_dirac(dirac, (double)j - pr[1]);
+            for (int64_t kk = lo[2]; kk <= lo[2] + s - 1; ++kk) {
+                const int64_t k2 = remap_index(L, 2, kk, off) + off;
+                if (k2 < 0 || k2 > nmax[2] - 1) continue;
+                const double dxyz = dxy * orc_dirac(dirac, (double)kk - pr[2]);
+                const int64_t c = i2 + L->nx * (j2 + L->ny * k2);
+                for (int d = 0; d < 3; ++d) F[d * nn + c] += dxyz * fv[d];
+            }
+        }
+    }
+}
+
+/* PipeBoundary::distance_to_boundary (Boundary.h:158-161) minus the kernel's half support: the
+ * weight of the supplied kernel against the TopHat near the wall */
+static double pipe_weight(const double* pipe, const double* p, double h) {
+    return pipe[2] - sqrt((p[1] - pipe[0]) * (p[1] - pipe[0]) + (p[2] - pipe[1]) * (p[2] - pipe[1])) - h;
+}
+
+/* interpolate_near_boundary (ImmersedBoundaryDynamics_interpolation.hh:181-230): the supplied
+ * kernel from h + 1 off the wall on, the TopHat within h, linear in between */
+static void interp_near_boundary(const orc_lattice* L, int32_t dirac, double offset, const double* u, const double* p,
+                                 const double* pipe, double* out) {
+    const double pr[3] = {p[0] - offset, p[1] - offset, p[2] - offset};
+    const int64_t off = (int64_t)offset;
+    const double weight = pipe_weight(pipe, p, half_support(dirac));
+    out[0] = out[1] = out[2] = 0.0;
+    if (weight >= 1) {
+        interp_general(L, dirac, off, u, pr, out);
+    } else if (weight <= 0) {
+        interp_general(L, ORC_DIRAC_TOPHAT, off, u, pr, out);
+    } else {
+        double a[3] = {0.0, 0.0, 0.0};
+        interp_general(L, dirac, off, u, pr, a);
+        interp_general(L, ORC_DIRAC_TOPHAT, off, u, pr, out);
+        for (int d = 0; d < 3; ++d) out[d] = (1. - weight) * out[d] + weight * a[d];
+    }
+}
+
+/* spread_forces_near_boundary (ImmersedBoundaryDynamics_forces.hh:192-237) */
+static void spread_near_boundary(const orc_lattice* L, int32_t dirac, double offset, const double* p, const double* fv,
+                                 const double* pipe, double* F) {
+    const double pr[3] = {p[0] - offset, p[1] - offset, p[2] - offset};
+    const int64_t off = (int64_t)offset;
+    const double weight = pipe_weight(pipe, p, half_support(dirac));
+    if (weight >= 1) {
+        spread_general(L, dirac, off, pr, fv, F);
+    } else if (weight <= 0) {
+        spread_general(L, ORC_DIRAC_TOPHAT, off, pr, fv, F);
+    } else {
+        const double fa[3] = {fv[0] * weight, fv[1] * weight, fv[2] * weight};
+        const double fb[3] = {fv[0] * (1. - weight), fv[1] * (1. - weight), fv[2] * (1. - weight)};
+        spread_general(L, dirac, off, pr, fa, F);
+        spread_general(L, ORC_DIRAC_TOPHAT, off, pr, fb, F);
+    }
+}
+
 /* Interpolation with the data-processor offset convention of the reference: node
  * positions are taken relative to the field's location `offset` (all three axes) and
  * indices are local (global + (-offset)).  In the IB step the velocity field has a
@@ -1264,8 +1383,8 @@ static int64_t remap_index(const orc_lattice* L, int d, int64_t i, int64_t offse
  * Bulk nodes: BulkInterpolator (Roma-specialised formula for Roma, generic loop else),
  * ImmersedBoundaryDynamics_interpolation.hh:84-153; envelope nodes: GeneralInterpolator
  * :43-78.  u is a (3, nz, ny, nx) field. */
-void orc_interpolate(const orc_lattice* L, int32_t dirac, double offset, const double* u, int64_t n,
-                     const double* pos, const int32_t* cls, double* vel) {
+static void interpolate_impl(const orc_lattice* L, int32_t dirac, double offset, const double* u, int64_t n,
+                             const double* pos, const int32_t* cls, double* vel, const double* pipe) {
     const int64_t nn = L->nx * L->ny * L->nz;
     const double h = half_support(dirac);
     const int s = support(dirac);
@@ -1275,6 +1394,10 @@ void orc_interpolate(const orc_lattice* L, int32_t dirac, double offset, const d
         double* out = vel + 3 * k;
         out[0] = out[1] = out[2] = 0.0;
         if (cls[k] == 0) continue;
+        if (cls[k] == 3) {
+            interp_near_boundary(L, dirac, offset, u, pos + 3 * k, pipe, out);
+            continue;
+        }
         const double pr[3] = {pos[3 * k] - offset, pos[3 * k + 1] - offset, pos[3 * k + 2] - offset};
         int64_t lo[3];
         for (int d = 0; d < 3; ++d) lo[d] = (int64_t)ceil(pr[d] - h);
@@ -1328,8 +1451,13 @@ void orc_interpolate(const orc_lattice* L, int32_t dirac, double offset, const d
 /* Spreading: bulk nodes first (BulkSpreading, Roma-specialised for Roma), then the
  * envelope nodes (GeneralSpreading), as compute_and_spread_forces orders them,
  * ImmersedBoundaryDynamics_forces.hh:22-163 and 243-284.  F is (3, nz, ny, nx). */
-void orc_spread(const orc_lattice* L, int32_t dirac, double offset, int64_t n, const double* pos,
-                const double* force, const int32_t* cls, double* F) {
+void orc_interpolate(const orc_lattice* L, int32_t dirac, double offset, const double* u, int64_t n,
+                     const double* pos, const int32_t* cls, double* vel) {
+    interpolate_impl(L, dirac, offset, u, n, pos, cls, vel, NULL);
+}
+
+static void spread_impl(const orc_lattice* L, int32_t dirac, double offset, int64_t n, const double* pos,
+                        const double* force, const int32_t* cls, double* F, const double* pipe) {
     const int64_t nn = L->nx * L->ny * L->nz;
     const double h = half_support(dirac);
     const int s = support(dirac);
@@ -1380,7 +1508,14 @@ void orc_spread(const orc_lattice* L, int32_t dirac, double offset, int64_t n, c
                 }
             }
         }
-    }
+    }    /* the nodes near a boundary last (compute_and_spread_forces, _forces.hh:277-282) */
+    for (int64_t k = 0; k < n; ++k)
+        if (cls[k] == 3) spread_near_boundary(L, dirac, offset, pos + 3 * k, force + 3 * k, pipe, F);
+}
+
+void orc_spread(const orc_lattice* L, int32_t dirac, double offset, int64_t n, const double* pos,
+                const double* force, const int32_t* cls, double* F) {
+    spread_impl(L, dirac, offset, n, pos, force, cls, F, NULL);
 }
 
 int32_t orc_threads(void) {
@@ -1427,6 +1562,8 @@ struct orc_sys {
     int32_t npp;
     orc_potential pp_pot[8];
     int32_t pp_grid;  /* 1: the reference's grid search, 0: every pair within the cutoff */
+    int32_t has_pipe; /* a PipeBoundary set with set_boundary */
+    double pipe[3];   /* y0, z0, radius */
 };
 
 orc_sys* orc_sys_create(const orc_lattice* L, int32_t dirac, double ib_offset) {
@@ -1563,6 +1700,31 @@ int32_t orc_sys_add_wall_interaction(orc_sys* s, const orc_potential* p, int32_t
     return s->nwalls++;
 }
 
+/* DeformableParticle3D::move_vertices (DeformableParticle3D.hh:26-51): explicit Euler; with a
+ * pipe boundary a step that crosses the wall is reflected about the normal at the crossing */
+void orc_move_vertices(int64_t nv, double* pos, const double* vel, const double* pipe) {
+    for (int64_t v = 0; v < nv; ++v) {
+        double* x = pos + 3 * v;
+        const double* u = vel + 3 * v;
+        const double old[3] = {x[0], x[1], x[2]};
+        for (int d = 0; d < 3; ++d) x[d] += u[d];
+        double t;
+        if (pipe && pipe_trace_ray(pipe[0], pipe[1], pipe[2], old, x, &t)) {
+            for (int d = 0; d < 3; ++d) x[d] = old[d] + t * u[d];
+            const double nv0[3] = {0, x[1] - pipe[0], x[2] - pipe[1]};
+            const double nn = sqrt(nv0[0] * nv0[0] + nv0[1] * nv0[1] + nv0[2] * nv0[2]);
+            const double nrm_[3] = {nv0[0] / nn, nv0[1] / nn, nv0[2] / nn};
+            const double dt2 = 2. * (u[0] * nrm_[0] + u[1] * nrm_[1] + u[2] * nrm_[2]);
+            for (int d = 0; d < 3; ++d) x[d] += (u[d] - dt2 * nrm_[d]) * (1. - t);
+        }
+    }
+}
+
+void orc_sys_set_pipe(orc_sys* s, double y0, double z0, double radius) {
+    s->has_pipe = 1;
+    s->pipe[0] = y0, s->pipe[1] = z0, s->pipe[2] = radius;
+}
+
 int32_t orc_sys_add_pp_interaction(orc_sys* s, const orc_potential* p, int32_t grid) {
     if (s->npp >= 8) return -1;
     s->pp_pot[s->npp] = *p;
@@ -1606,8 +1768,9 @@ static void sys_step(orc_sys* s) {
         int32_t* cls = (int32_t*)malloc(sizeof(int32_t) * (size_t)(nvt > 0 ? nvt : 1));
         double* vel = (double*)malloc(sizeof(double) * 3 * (nvt > 0 ? nvt : 1));
         double* frc = (double*)malloc(sizeof(double) * 3 * (nvt > 0 ? nvt : 1));
-        orc_classify(L, s->dirac, nvt, pos, cls);
-        orc_interpolate(L, s->dirac, s->offset, s->u, nvt, pos, cls, vel);
+        const double* pipe = s->has_pipe ? s->pipe : NULL;
+        classify_pipe(L, s->dirac, nvt, pos, cls, pipe);
+        interpolate_impl(L, s->dirac, s->offset, s->u, nvt, pos, cls, vel, pipe);
         int64_t o = 0;
         for (int32_t i = 0; i < s->nparts; ++i) {
             orc_particle* p = &s->parts[i];
@@ -1641,11 +1804,11 @@ static void sys_step(orc_sys* s) {
             }
             free(owner);
         }
-        orc_spread(L, s->dirac, s->offset, nvt, pos, frc, cls, s->F);
+        spread_impl(L, s->dirac, s->offset, nvt, pos, frc, cls, s->F, pipe);
         for (int32_t i = 0; i < s->nparts; ++i) {
             orc_particle* p = &s->parts[i];
             const orc_shape* sh = &s->shapes[p->shape];
-            for (int64_t k = 0; k < 3 * sh->nv; ++k) p->pos[k] += p->vel[k];
+            orc_move_vertices(sh->nv, p->pos, p->vel, pipe);
             particle_refresh(s, p);
             remap_com(s, p);
         }

@@ -28,7 +28,7 @@ extern "C" {
 
 enum { ORC_COLLISION_BGK_GUO_VOF = 0, ORC_COLLISION_BGK = 1, ORC_COLLISION_TRT = 2 };
 enum { ORC_WALL_NONE = 0, ORC_WALL_FD_VELOCITY = 1, ORC_WALL_HALFWAY_BB = 2 };
-enum { ORC_DIRAC_ROMA = 0, ORC_DIRAC_PESKIN = 1 };
+enum { ORC_DIRAC_ROMA = 0, ORC_DIRAC_PESKIN = 1, ORC_DIRAC_TOPHAT = 2 };
 enum {
     ORC_MODEL_CAPSULE_NEOHOOKEAN = 0,
     ORC_MODEL_CAPSULE_SKALAK = 1,
@@ -141,6 +141,11 @@ void orc_sys_set_voxelize(orc_sys* s, int32_t on);  /* revoxelize after every mo
 int32_t orc_sys_add_wall_interaction(orc_sys* s, const orc_potential* p, int32_t axis, double lo, double hi);
 /* add_pp_force(PPPotentialForce(p)); grid = 1 evaluates it with the reference's grid search */
 int32_t orc_sys_add_pp_interaction(orc_sys* s, const orc_potential* p, int32_t grid);
+/* ImmersedBoundaryDynamics3D::set_boundary with a PipeBoundary along x through (y0, z0): near-wall
+ * TopHat blending of interpolation and spreading, wall reflection of the move */
+void orc_sys_set_pipe(orc_sys* s, double y0, double z0, double radius);
+/* move_vertices: pos += vel, reflected at a pipe wall when pipe = {y0, z0, radius} is given */
+void orc_move_vertices(int64_t nv, double* pos, const double* vel, const double* pipe);
 void orc_sys_lattice_only_step(orc_sys* s, int64_t nsteps);
 void orc_sys_get_particle(orc_sys* s, int32_t pid, double* pos, double* vel, double* force, double* stats5);
 void orc_sys_velocity(orc_sys* s, double* u);

@@ -19,6 +19,11 @@
 //           NoDynamics beyond radius + 1), in a periodic box
 //   pipe_guo the same flow with the second-order walls: GuoRigidWallBoundary on the pipe
 //           (rbc_in_pipe.cpp:303-305, fsi/GuoBoundaryCondition.hh) and NoDynamics beyond radius + 1
+//   ibm_pipe coupled IB-LBM steps of a capsule near the wall of a pipe with second-order walls:
+//           ImmersedBoundaryDynamics3D::set_boundary, i.e. the TopHat near-wall blend of the
+//           interpolation and spreading (_interpolation.hh:181-230, _forces.hh:192-237) and the
+//           ray-traced wall reflection of the move (DeformableParticle3D.hh:26-51)
+//   reflect  DeformableParticle3D::move_vertices(boundary) of given positions and velocities
 //   interact the vertex forces of one IB step with a particle-particle interaction
 //           (add_pp_force, CollisionForces.h) and a wall interaction decorator
 //           (add_force_decorator, ForceDecorator.hh) on parallel plates (Boundary.h:305-365)
@@ -686,6 +691,91 @@ static int run_interact_impl(const Bundle& in, const char* out, const PP& ppot, 
     return 0;
 }
 
+static int run_ibm_pipe(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    const std::vector<double> g = recio::need(in, "pipe").d;  // y0, z0, radius
+    const T omega = 1. / recio::num(in, "tau");
+    const long long steps = recio::inum(in, "steps");
+    const std::vector<double> body = recio::need(in, "body").d;
+    PipeBoundary<T> pipe(g[0], g[1], g[2], (T)(nx - 1));
+    ParticleShapeLibrary<T> lib;
+    store_shape(in, lib, "rest");
+    const ParticleShape<T>* shape = lib.get_by_tag("shape");
+    ParticleBase3D<T>* proto = make_particle(shape, read_spec(in));
+    set_positions(*proto, recio::need(in, "pos"));
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(omega, omega));
+    lattice.toggleInternalStatistics(false);
+    lattice.periodicity().toggleAll(true);
+    GuoRigidWallBoundary<T, DESCRIPTOR> walls(pipe, lattice);
+    walls.insert();
+    const plint margin = (plint)std::sqrt(2.0);
+    for (plint z = 0; z < nz; ++z)
+        for (plint y = 0; y < ny; ++y)
+            for (plint x = 0; x < nx; ++x)
+                if (!pipe.contains(Array<T, 3>((T)x, (T)y, (T)z), (T)-margin))
+                    defineDynamics(lattice, Box3D(x, x, y, y, z, z), new NoDynamics<T, DESCRIPTOR>());
+    const Box3D domain = lattice.getBoundingBox();
+    initializeAtEquilibrium(lattice, domain, (T)1, Array<T, 3>(0., 0., 0.));
+    lattice.initialize();
+    ImmersedBoundaryDynamics3D<T, DESCRIPTOR, Periodicity3D<T, true, true, true> > fsi(lattice, lib);
+    fsi.set_boundary(&pipe);
+    std::auto_ptr<MultiTensorField3D<T, 3> > velocity = generateMultiTensorField<T, 3>(domain);
+    fsi.add_particle(proto);
+    fsi.init();
+    const plint nv = proto->count_nodes();
+    std::vector<double> pos((steps + 1) * nv * 3), vel(steps * nv * 3), frc(steps * nv * 3);
+    for (long long it = 0; it <= steps; ++it) {
+        ParticleBase3D<T>* p = 0;
+        fsi.get_particle(0, p);
+        for (plint i = 0; i < nv; ++i)
+            for (int d = 0; d < 3; ++d) pos[(it * nv + i) * 3 + d] = p->get_node(i).pos[d];
+        if (it == steps) break;
+        computeVelocity(lattice, *velocity, domain);
+        setExternalVector(lattice, domain, DESCRIPTOR<T>::ExternalField::forceBeginsAt, Array<T, 3>(body[0], body[1], body[2]));
+        applyProcessingFunctional(wrap_ibm_dynamics3D(fsi), domain, lattice, *velocity);
+        fsi.get_particle(0, p);
+        for (plint i = 0; i < nv; ++i)
+            for (int d = 0; d < 3; ++d) {
+                vel[(it * nv + i) * 3 + d] = p->get_node(i).vel[d];
+                frc[(it * nv + i) * 3 + d] = p->get_node(i).force[d];
+            }
+        if (it == 0) {
+            recio::Writer w0((std::string(out) + ".step0").c_str());
+            dump_lattice(w0, "spread", lattice);
+        }
+        lattice.collideAndStream();
+    }
+    recio::Writer w(out);
+    w.d("pos", shp(steps + 1, nv, 3), pos);
+    w.d("vel", shp(steps, nv, 3), vel);
+    w.d("force", shp(steps, nv, 3), frc);
+    dump_lattice(w, "end", lattice);
+    dump_velocity(w, "end", lattice);
+    delete proto;
+    return 0;
+}
+
+static int run_reflect(const Bundle& in, const char* out) {
+    const std::vector<double> g = recio::need(in, "pipe").d;
+    PipeBoundary<T> pipe(g[0], g[1], g[2], (T)100);
+    ParticleShapeLibrary<T> lib;
+    store_shape(in, lib, "rest");
+    ParticleBase3D<T>* p = make_particle(lib.get_by_tag("shape"), read_spec(in));
+    set_positions(*p, recio::need(in, "pos"));
+    const recio::Array& v = recio::need(in, "vel");
+    const plint nv = p->count_nodes();
+    for (plint i = 0; i < nv; ++i) p->get_node(i).vel = Array<T, 3>(v.d[3 * i], v.d[3 * i + 1], v.d[3 * i + 2]);
+    dynamic_cast<DeformableParticle3D<T>*>(p)->move_vertices(&pipe);
+    std::vector<double> P(3 * nv);
+    for (plint i = 0; i < nv; ++i)
+        for (int d = 0; d < 3; ++d) P[3 * i + d] = p->get_node(i).pos[d];
+    recio::Writer w(out);
+    w.d("pos", shp(nv, 3), P);
+    delete p;
+    return 0;
+}
+
 static int run_interact(const Bundle& in, const char* out) {
     const long long ppk = recio::inum(in, "pp_kind"), wk = recio::inum(in, "wall_kind");
     const std::vector<double> a = recio::need(in, "pp_params").d, b = recio::need(in, "wall_params").d;
@@ -716,6 +806,8 @@ int main(int argc, char** argv) {
     if (c == "interact") return run_interact(in, argv[3]);
     if (c == "pipe") return run_pipe(in, argv[3]);
     if (c == "pipe_guo") return run_pipe_guo(in, argv[3]);
+    if (c == "ibm_pipe") return run_ibm_pipe(in, argv[3]);
+    if (c == "reflect") return run_reflect(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

@@ -103,6 +103,8 @@ def lib():
             "orc_pipe_guo_nodes": (C.c_int64, [C.c_int64, C.c_int64, C.c_int64, C.c_double, C.c_double, C.c_double,
                                                C.c_void_p, C.c_void_p]),
             "orc_apply_guo": (None, [Lp, dp]),
+            "orc_sys_set_pipe": (None, [C.c_void_p, C.c_double, C.c_double, C.c_double]),
+            "orc_move_vertices": (None, [C.c_int64, dp, dp, C.c_void_p]),
             "orc_potential_eval": (C.c_double, [C.POINTER(Potential), C.c_double]),
             "orc_wall_forces": (None, [C.POINTER(Potential), C.c_int32, C.c_double, C.c_double, C.c_int64, dp, dp]),
             "orc_pp_forces_grid": (None, [Lp, C.POINTER(Potential), C.c_int64, dp, i32p, dp]),
@@ -341,6 +343,10 @@ class System:
         """add_pp_force(PPPotentialForce(pot)); grid=True searches pairs as the reference does."""
         assert lib().orc_sys_add_pp_interaction(self.h, C.byref(pot), int(bool(grid))) >= 0
 
+    def set_pipe(self, y0, z0, radius):
+        """set_boundary(PipeBoundary(y0, z0, radius)): near-wall TopHat blend and wall reflection."""
+        lib().orc_sys_set_pipe(self.h, float(y0), float(z0), float(radius))
+
     def init(self):
         """ImmersedBoundaryDynamics3D::init: voxelize the initial positions (when enabled)."""
         lib().orc_sys_init(self.h)
@@ -418,4 +424,13 @@ def set_guo(L, nodes, count):
 def apply_guo(L, f):
     out = f64(f).copy()
     lib().orc_apply_guo(C.byref(L), _d(out))
+    return out
+
+
+def move_vertices(pos, vel, pipe=None):
+    """DeformableParticle3D::move_vertices, reflected at the wall of pipe = (y0, z0, radius)."""
+    out = f64(pos).copy()
+    v = f64(vel)
+    pp = None if pipe is None else f64(pipe)
+    lib().orc_move_vertices(out.shape[0], _d(out), _d(v), None if pp is None else pp.ctypes.data)
     return out

@@ -355,8 +355,42 @@ def case_lbm_pipe_guo():
                                                      "fbar_end", "u_end")})
 
 
+def case_ibm_pipe():
+    """A prestressed capsule next to the wall of a pipe with second-order walls and body-force
+    flow: the near-wall TopHat blend of interpolation and spreading, 8 coupled steps."""
+    n, R = 21, 8.3
+    rng = np.random.default_rng(606)
+    xyz, tri = meshes.icosphere(2, 2.6)
+    pos = meshes.place(deform(rng, xyz, 0.04), meshes.random_rotation(rng), (7.5, 10.0 + 5.0, 10.2 + 0.3))
+    inp = dict(dims=[16, n, n], pipe=[10.0, 10.2, R], tau=1.0, body=[2e-5, 0.0, 0.0], steps=8, rest=xyz, tri=tri,
+               pos=pos, model=1, params=particle_params(1, G=2e-3, C=1.0))
+    out = run("ibm_pipe", inp)
+    keep = {k: out[k] for k in ("pos", "vel", "force")}
+    keep["fbar_end_planes"] = out["fbar_end"][:, :, :, [0, 7]]
+    keep["fbar_end_sum"] = out["fbar_end"].sum(axis=(1, 2, 3))
+    keep["force_spread"] = out["force_spread"][:, :, :, 4:12]  # the capsule's x range
+    save("ibm_pipe", inp, keep)
+
+
+def case_reflect():
+    """DeformableParticle3D::move_vertices with a pipe boundary: vertices whose step crosses
+    the wall are reflected about the wall normal at the crossing."""
+    rng = np.random.default_rng(707)
+    xyz, tri = meshes.icosphere(1, 2.0)
+    pos = meshes.place(xyz, None, (5.0, 10.0 + 5.9, 10.2 + 0.4))
+    vel = np.array([0.05, 1.0, 0.1]) + 0.05 * rng.standard_normal(pos.shape)
+    inp = dict(pipe=[10.0, 10.2, 8.3], rest=xyz, tri=tri, pos=pos, vel=vel, model=1,
+               params=particle_params(1, G=1e-3, C=1.0))
+    out = run("reflect", inp)
+    r_new = np.hypot(out["pos"][:, 1] - 10.0, out["pos"][:, 2] - 10.2)
+    r_free = np.hypot(pos[:, 1] + vel[:, 1] - 10.0, pos[:, 2] + vel[:, 2] - 10.2)
+    assert (r_free > 8.3).sum() >= 3 and r_new.max() <= 8.3 + 1e-12
+    save("reflect_pipe", inp, {"pos": out["pos"]})
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
-         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo]
+         case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo, case_ibm_pipe,
+         case_reflect]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):

@@ -267,3 +267,44 @@ def test_pipe_second_order_walls():
     fe = O.collide_stream(L, f0, F, np.zeros((nz, ny, nx)), int(d["in_steps"]))
     assert np.array_equal(fe, d["out_fbar_end"])
     assert np.array_equal(O.compute_velocity(L, fe, F), d["out_u_end"])
+
+
+def test_move_vertices_reflects_at_pipe_wall():
+    d = golden("reflect_pipe")
+    assert np.array_equal(O.move_vertices(d["in_pos"], d["in_vel"], d["in_pipe"]), d["out_pos"])
+    free = O.move_vertices(d["in_pos"], d["in_vel"])
+    assert np.array_equal(free, d["in_pos"] + d["in_vel"]) and not np.array_equal(free, d["out_pos"])
+
+
+def pipe_ibm_system(d):
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    y0, z0, R = d["in_pipe"]
+    om = 1.0 / float(d["in_tau"])
+    nodes, cnt, types = O.pipe_guo_nodes((nx, ny, nz), y0, z0, R)
+    L = O.set_guo(O.lattice((nx, ny, nz), (1, 1, 1), "bgk_guo_vof", om, om, celltype=types), nodes, cnt)
+    S = O.System(L, "roma", -1.0)
+    S._keep = (nodes, types)
+    S.f[...] = O.apply_guo(L, np.zeros((19, nz, ny, nx)))
+    S.set_body_force(d["in_body"])
+    S.set_pipe(y0, z0, R)
+    pid = S.add_particle(S.add_shape(d["in_rest"], d["in_tri"]), int(d["in_model"]), d["in_params"], d["in_pos"])
+    S.init()
+    return S, pid
+
+
+def test_capsule_near_pipe_wall():
+    """A capsule next to the wall of a pipe with second-order walls: the near-wall TopHat
+    blend of interpolation and spreading (set_boundary), step by step against the reference."""
+    d = golden("ibm_pipe")
+    S, pid = pipe_ibm_system(d)
+    for it in range(int(d["in_steps"])):
+        assert np.array_equal(S.particle(pid)["pos"], d["out_pos"][it])
+        S.step(1)
+        p = S.particle(pid)
+        assert np.array_equal(p["vel"], d["out_vel"][it]), it
+        assert np.array_equal(p["force"], d["out_force"][it]), it
+        if it == 0:
+            assert np.array_equal(S.force[:, :, :, 4:12], d["out_force_spread"])
+    assert np.array_equal(S.particle(pid)["pos"], d["out_pos"][-1])
+    assert np.array_equal(S.f[:, :, :, [0, 7]], d["out_fbar_end_planes"])
+    assert np.array_equal(S.f.sum(axis=(1, 2, 3)), d["out_fbar_end_sum"])
