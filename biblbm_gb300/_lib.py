@@ -91,6 +91,7 @@ SIGNATURES = {
     "bib_total_volume": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_ibm_step": (C.c_int32, [_vp, C.c_int32]),
     "bib_ibm_init": (C.c_int32, [_vp, C.c_int32]),
+    "bib_ib_set_pipe_boundary": (C.c_int32, [_vp, C.c_int32, C.c_double, C.c_double, C.c_double]),
     "bib_lattice_set_pipe_walls": (C.c_int32, [_vp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32]),
     "bib_add_wall_interaction": (C.c_int32, [_vp, C.c_int32, C.c_int32, C.c_double, C.c_double, C.POINTER(Potential)]),
     "bib_add_pp_interaction": (C.c_int32, [_vp, C.c_int32, C.POINTER(Potential)]),

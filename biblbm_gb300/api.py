@@ -303,6 +303,12 @@ class ImmersedBoundaryDynamics3D:
         self.nv.append(self.shapes.info(shape)["n_vertices"])
         return pid.value
 
+    def set_boundary(self, y0, z0, radius):
+        """set_boundary(PipeBoundary): near-wall TopHat blending and wall reflection for a pipe
+        along x through (y0, z0); radius <= 0 removes it."""
+        self.ctx.check(self.ctx.lib.bib_ib_set_pipe_boundary(self.ctx.h, self.lattice.h, float(y0), float(z0),
+                                                             float(radius)))
+
     def add_wall_interaction(self, potential: Potential, axis: int, lo: float, hi: float):
         """add_force_decorator(WallInteraction(ParallelPlatesBoundary(lo, hi), potential)); the
         plates are normal to `axis` (1 = y as in the reference, 2 = z)."""

@@ -1698,6 +1698,8 @@ bib_status bib_ib_configure(bib_ctx* c, int32_t h, const bib_ib_params* p) {
         return fail(c, BIB_EINVAL, "bad spread mode");
     if (L->d.n >= (int64_t)0xffffffff) return fail(c, BIB_EUNSUPPORTED, "lattice too large for 32-bit cell keys");
     if (p->field_offset != std::floor(p->field_offset)) return fail(c, BIB_EINVAL, "field offset must be integral");
+    if (L->ib.has_pipe && p->spread_mode == BIB_SPREAD_DETERMINISTIC)
+        return fail(c, BIB_EUNSUPPORTED, "deterministic spreading does not blend kernels near a pipe boundary");
     L->ib.dirac = p->dirac;
     L->ib.spread_mode = p->spread_mode;
     L->ib.offset = p->field_offset;
@@ -1709,6 +1711,27 @@ bib_status bib_ib_configure(bib_ctx* c, int32_t h, const bib_ib_params* p) {
     return BIB_OK;
 }
 
+// Interaction changes alter kernel arguments captured in graphs and batch tables
+static void interactions_changed(bib_ctx* c, int32_t h) {
+    drop_graphs(c, h);
+    for (auto& B : c->batches)
+        if (B) B->free_tables();
+}
+
+bib_status bib_ib_set_pipe_boundary(bib_ctx* c, int32_t h, double y0, double z0, double radius) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    if (!std::isfinite(y0) || !std::isfinite(z0) || !std::isfinite(radius)) return fail(c, BIB_EINVAL, "bad pipe geometry");
+    if (radius > 0 && L->ib.spread_mode == BIB_SPREAD_DETERMINISTIC)
+        return fail(c, BIB_EUNSUPPORTED, "deterministic spreading does not blend kernels near a pipe boundary");
+    L->ib.has_pipe = radius > 0;
+    L->ib.pipe_y0 = y0;
+    L->ib.pipe_z0 = z0;
+    L->ib.pipe_r = radius > 0 ? radius : 0.0;
+    interactions_changed(c, h);  // the IB description is captured by graphs and batch tables
+    return BIB_OK;
+}
+
 static bib_status check_potential(bib_ctx* c, const bib_potential* p) {
     if (!p) return fail(c, BIB_EINVAL, "null potential");
     if (p->kind != BIB_POTENTIAL_MORSE && p->kind != BIB_POTENTIAL_SPRING) return fail(c, BIB_EINVAL, "bad potential kind");
@@ -1717,12 +1740,6 @@ static bib_status check_potential(bib_ctx* c, const bib_potential* p) {
     return BIB_OK;
 }
 
-// Interaction changes alter kernel arguments captured in graphs and batch tables
-static void interactions_changed(bib_ctx* c, int32_t h) {
-    drop_graphs(c, h);
-    for (auto& B : c->batches)
-        if (B) B->free_tables();
-}
 
 bib_status bib_add_wall_interaction(bib_ctx* c, int32_t h, int32_t axis, double lo, double hi, const bib_potential* p) {
     Lattice* L = get_lattice(c, h);

@@ -37,6 +37,10 @@ struct IbDesc {
     int dirac;
     int spread_mode;
     double offset;
+    // ImmersedBoundaryDynamics3D::set_boundary with a PipeBoundary along x: near-wall TopHat
+    // blend of interpolation and spreading, wall reflection of the move (has_pipe = 0: none)
+    int has_pipe = 0;
+    double pipe_y0 = 0.0, pipe_z0 = 0.0, pipe_r = 0.0;
 };
 
 // Geometry of one reference shape, device resident.

@@ -146,6 +146,103 @@ __device__ __forceinline__ U3<double> load_u(const double* u, int64_t k) {
     return U3<double>{a.x, a.y, b.x};
 }
 
+// ---------------------------------------------------------------- pipe boundary
+// PipeBoundary::distance_to_boundary (fsi/Boundary.h:158-161) minus the kernel's half support:
+// the weight of the supplied kernel against the 2-point TopHat near the wall (>= 1: the
+// supplied kernel alone, <= 0: the TopHat alone, _interpolation.hh:181-230, _forces.hh:192-237)
+__device__ __forceinline__ double pipe_weight(const IbDesc& ib, const double* p, double h) {
+    const double dy = p[1] - ib.pipe_y0, dz = p[2] - ib.pipe_z0;
+    return ib.pipe_r - sqrt(dy * dy + dz * dz) - h;
+}
+
+// TopHatDirac<T,3> (Dirac.h:47-64): support 2, weight 1 - |x| per axis; the 2 x 2 x 2 nodes
+// in GeneralInterpolator / GeneralSpreading order.  mode 0 gathers u into acc, mode 1 adds
+// w * fv into the force field.
+template <class C, class UT>
+__device__ __forceinline__ void tophat_interp(const LatticeDesc& d, const IbDesc& ib, const double* p, const UT* u, C* acc) {
+    const int off = (int)ib.offset;
+    int64_t lo[3];
+    C w[3][2];
+    for (int a = 0; a < 3; ++a) {
+        const double x = p[a] - ib.offset;
+        lo[a] = (int64_t)ceil(x - 1.0);
+        w[a][0] = (C)(1. - fabs((double)lo[a] - x));
+        w[a][1] = (C)(1. - fabs((double)(lo[a] + 1) - x));
+    }
+    for (int a = 0; a < 2; ++a) {
+        const int gx = remap_global(d.px, d.nx, lo[0] + a, off);
+        if (gx < 0) continue;
+        for (int b = 0; b < 2; ++b) {
+            const int gy = remap_global(d.py, d.ny, lo[1] + b, off);
+            if (gy < 0) continue;
+            const C wxy = w[0][a] * w[1][b];
+            for (int c = 0; c < 2; ++c) {
+                const int gz = remap_global(d.pz, d.nz, lo[2] + c, off);
+                if (gz < 0) continue;
+                const C wt = wxy * w[2][c];
+                const U3<C> uc = load_u(u, gx + (int64_t)d.nx * (gy + (int64_t)d.ny * gz));
+                acc[0] += wt * uc.x;
+                acc[1] += wt * uc.y;
+                acc[2] += wt * uc.z;
+            }
+        }
+    }
+}
+template <class FT>
+__device__ __forceinline__ void tophat_spread(const LatticeDesc& d, const IbDesc& ib, const double* p, const FT* fv, FT* F) {
+    const int off = (int)ib.offset;
+    int64_t lo[3];
+    FT w[3][2];
+    for (int a = 0; a < 3; ++a) {
+        const double x = p[a] - ib.offset;
+        lo[a] = (int64_t)ceil(x - 1.0);
+        w[a][0] = (FT)(1. - fabs((double)lo[a] - x));
+        w[a][1] = (FT)(1. - fabs((double)(lo[a] + 1) - x));
+    }
+    for (int a = 0; a < 2; ++a) {
+        const int gx = remap_global(d.px, d.nx, lo[0] + a, off);
+        if (gx < 0) continue;
+        for (int b = 0; b < 2; ++b) {
+            const int gy = remap_global(d.py, d.ny, lo[1] + b, off);
+            if (gy < 0) continue;
+            const FT wxy = w[0][a] * w[1][b];
+            for (int c = 0; c < 2; ++c) {
+                const int gz = remap_global(d.pz, d.nz, lo[2] + c, off);
+                if (gz < 0) continue;
+                const FT wt = wxy * w[2][c];
+                FT* q = F + gx + (int64_t)d.nx * (gy + (int64_t)d.ny * gz);
+                atomicAdd(q, wt * fv[0]);
+                atomicAdd(q + d.stride, wt * fv[1]);
+                atomicAdd(q + 2 * d.stride, wt * fv[2]);
+            }
+        }
+    }
+}
+
+// DeformableParticle3D::move_vertices(boundary) (DeformableParticle3D.hh:26-51) with
+// PipeBoundary::trace_ray / get_normal (Boundary.h:164-187, 245-249): a step that crosses the
+// wall is reflected about the normal at the crossing.
+__device__ __forceinline__ void pipe_move(const IbDesc& ib, const double* old, const double* v, double* x) {
+    const double y1 = old[1] - ib.pipe_y0, y2 = x[1] - ib.pipe_y0, z1 = old[2] - ib.pipe_z0, z2 = x[2] - ib.pipe_z0;
+    const double a = (y2 - y1) * (y2 - y1) + (z2 - z1) * (z2 - z1);
+    const double b = y1 * (y2 - y1) + z1 * (z2 - z1);
+    const double c = y1 * y1 + z1 * z1 - ib.pipe_r * ib.pipe_r;
+    const double disc = b * b - c * a;
+    if (disc < 0. || fabs(a) < 10 * DBL_EPSILON) return;
+    const double bOverA = -b / a, sqrtDisc = sqrt(disc) / a;
+    double t = bOverA - sqrtDisc;
+    if (!(t >= 0. && t <= 1.)) {
+        t = bOverA + sqrtDisc;
+        if (!(t >= 0. && t <= 1.)) return;
+    }
+    for (int k = 0; k < 3; ++k) x[k] = old[k] + t * v[k];
+    const double ny_ = x[1] - ib.pipe_y0, nz_ = x[2] - ib.pipe_z0;
+    const double nn = sqrt(0.0 * 0.0 + ny_ * ny_ + nz_ * nz_);
+    const double n[3] = {0.0 / nn, ny_ / nn, nz_ / nn};
+    const double s2 = 2. * (v[0] * n[0] + v[1] * n[1] + v[2] * n[2]);
+    for (int k = 0; k < 3; ++k) x[k] += (v[k] - s2 * n[k]) * (1. - t);
+}
+
 // ---------------------------------------------------------------- interpolation
 // Interpolation of the velocity field (written by the collide-and-stream kernel or the
 // velocity kernel) to every vertex, followed by the explicit Euler move
@@ -209,12 +306,22 @@ __device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) 
         out[1] = (double)acc[1];
         out[2] = (double)acc[2];
     }
+    if (ib.has_pipe && inside_envelope(d, ib.dirac, p)) {
+        const double w = pipe_weight(ib, p, S == 4 ? 2.0 : 1.5);
+        if (w < 1) {  // near the wall: blend with (or switch to) the TopHat kernel
+            C t[3] = {C(0), C(0), C(0)};
+            tophat_interp<C, UT>(d, ib, p, u, t);
+            for (int k = 0; k < 3; ++k) out[k] = w <= 0 ? (double)t[k] : (1. - w) * (double)t[k] + w * out[k];
+        }
+    }
     vel[3 * v] = out[0];
     vel[3 * v + 1] = out[1];
     vel[3 * v + 2] = out[2];
-    pos_next[3 * v] = p[0] + out[0];
-    pos_next[3 * v + 1] = p[1] + out[1];
-    pos_next[3 * v + 2] = p[2] + out[2];
+    double xn[3] = {p[0] + out[0], p[1] + out[1], p[2] + out[2]};
+    if (ib.has_pipe) pipe_move(ib, p, out, xn);
+    pos_next[3 * v] = xn[0];
+    pos_next[3 * v + 1] = xn[1];
+    pos_next[3 * v + 2] = xn[2];
 }
 
 template <class UT, int S, bool BATCH>
@@ -239,6 +346,19 @@ __device__ __forceinline__ void spread_vertex(const IbView& V, int v) {
     if (!inside_envelope(d, ib.dirac, p)) return;
     const int off = (int)ib.offset;
     constexpr int s = S;
+    FT fscale = FT(1);
+    if (ib.has_pipe) {
+        const double wp = pipe_weight(ib, p, S == 4 ? 2.0 : 1.5);
+        if (wp < 1) {  // near the wall: the TopHat takes the share 1 - w of the force
+            FT* Fw = static_cast<FT*>(V.F);
+            const FT ft[3] = {(FT)(force[3 * v] * (wp <= 0 ? 1.0 : 1. - wp)),
+                              (FT)(force[3 * v + 1] * (wp <= 0 ? 1.0 : 1. - wp)),
+                              (FT)(force[3 * v + 2] * (wp <= 0 ? 1.0 : 1. - wp))};
+            tophat_spread<FT>(d, ib, p, ft, Fw);
+            if (wp <= 0) return;
+            fscale = (FT)wp;
+        }
+    }
     int64_t lo[3];
     FT w[3][4];
     for (int a = 0; a < 3; ++a) lo[a] = axis_weights<FT, S>(p[a] - ib.offset, w[a]);
@@ -255,7 +375,9 @@ __device__ __forceinline__ void spread_vertex(const IbView& V, int v) {
         yo[m] = (int64_t)gy[m] * d.nx;
         zo[m] = (int64_t)gz[m] * d.ny * d.nx;
     }
-    const FT fv[3] = {(FT)force[3 * v], (FT)force[3 * v + 1], (FT)force[3 * v + 2]};
+    const FT fv[3] = {fscale == FT(1) ? (FT)force[3 * v] : (FT)(force[3 * v] * (double)fscale),
+                      fscale == FT(1) ? (FT)force[3 * v + 1] : (FT)(force[3 * v + 1] * (double)fscale),
+                      fscale == FT(1) ? (FT)force[3 * v + 2] : (FT)(force[3 * v + 2] * (double)fscale)};
     if (sizeof(FT) == sizeof(float) && gx[s - 1] == gx[0] + s - 1) {
         // FP32 field and no periodic wrap along x inside the support: each (y, z) row of
         // each component receives one window of s values through one or two float4 atomics

@@ -83,6 +83,10 @@ bib_status spread_noalloc(const Lattice& L, int device, cudaStream_t s, const do
               " vertices with this kernel)";
         return BIB_EINVAL;
     }
+    if (L.ib.has_pipe) {
+        msg = "the spreading scratch path does not blend kernels near a pipe boundary";
+        return BIB_EUNSUPPORTED;
+    }
     if (L.d.n >= (int64_t)0xffffffff) {
         msg = "lattice too large for 32-bit cell keys";
         return BIB_EUNSUPPORTED;

@@ -192,6 +192,13 @@ bib_status bib_shape_info(bib_ctx* ctx, int32_t shape, double* out);
 
 /* ---- immersed boundary: ImmersedBoundaryDynamics3D ---- */
 bib_status bib_ib_configure(bib_ctx* ctx, int32_t h, const bib_ib_params* p);
+/* ImmersedBoundaryDynamics3D::set_boundary with a PipeBoundary along x through (y0, z0): vertices
+ * within the kernel's half support + 1 of the wall interpolate and spread with a blend of the
+ * kernel and the 2-point TopHat (interpolate_near_boundary / spread_forces_near_boundary,
+ * ImmersedBoundaryDynamics_interpolation.hh:181-230, _forces.hh:192-237), and a move that crosses
+ * the wall is reflected (DeformableParticle3D.hh:26-51).  radius <= 0 removes it.  Atomic
+ * spreading only. */
+bib_status bib_ib_set_pipe_boundary(bib_ctx* ctx, int32_t h, double y0, double z0, double radius);
 /* add_particle (ImmersedBoundaryDynamics.hh:500-525): xyz NULL = the rest shape */
 bib_status bib_particle_add(bib_ctx* ctx, int32_t h, int32_t shape, int32_t model, const double* params,
                             const double* xyz, int32_t* pid);

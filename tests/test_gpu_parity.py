@@ -555,3 +555,72 @@ def test_pipe_too_narrow_for_second_order_walls(ctx):
     with pytest.raises(bib.BibError, match="narrow"):
         lat.set_pipe_walls(4.0, 4.0, 1.2, second_order=True)
     lat.set_pipe_walls(4.0, 4.0, 1.2)  # first order works at any size
+
+
+def pipe_capsule_gpu(ctx, d, u0=None):
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    y0, z0, R = d["in_pipe"]
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=1.0 / float(d["in_tau"]), body_force=d["in_body"])
+    lat.set_pipe_walls(y0, z0, R, second_order=True)
+    lat.initialize_at_equilibrium(None, np.zeros((3, nz, ny, nx)) if u0 is None else u0)
+    shapes = bib.ParticleShapeLibrary(ctx)
+    fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes)
+    fsi.set_boundary(y0, z0, R)
+    pid = fsi.add_particle(shapes.store_mesh(d["in_rest"], d["in_tri"], "c"), "capsule_skalak", d["in_params"], d["in_pos"])
+    ctx.set_graph_mode(False)
+    return lat, fsi, pid
+
+
+def test_capsule_near_pipe_wall_matches_reference(ctx):
+    """set_boundary(PipeBoundary): the TopHat near-wall blend of interpolation and spreading,
+    with the second-order pipe walls, step by step against the reference."""
+    d = golden("ibm_pipe")
+    lat, fsi, pid = pipe_capsule_gpu(ctx, d)
+    fscale = np.abs(d["out_force"]).max()
+    for it in range(int(d["in_steps"])):
+        fsi.step(1)
+        p = fsi.get_particle(pid)
+        assert rel(p["pos"], d["out_pos"][it + 1]) < 1e-13, it
+        assert np.abs(p["vel"] - d["out_vel"][it]).max() < 1e-11 * max(np.abs(d["out_vel"][it]).max(), 1e-30), it
+        assert np.abs(p["force"] - d["out_force"][it]).max() < 1e-10 * fscale, it
+        if it == 0:
+            F = lat.get_external_force()[:, :, :, 4:12]
+            assert np.abs(F - d["out_force_spread"]).max() < 1e-15
+    f = lat.receive()
+    assert np.abs(f[:, :, :, [0, 7]] - d["out_fbar_end_planes"]).max() < 1e-14
+    ctx.set_graph_mode(True)
+
+
+def test_wall_reflection_against_oracle(ctx):
+    """A capsule against the wall in a strong outward flow: vertices whose step crosses the
+    wall are reflected (DeformableParticle3D::move_vertices), as the oracle does."""
+    d = golden("ibm_pipe")
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    y0, z0, R = d["in_pipe"]
+    Y, Z = np.meshgrid(np.arange(ny) - y0, np.arange(nz) - z0, indexing="ij")
+    r = np.hypot(Y, Z) + 1e-30
+    u0 = np.zeros((3, nz, ny, nx))
+    inside = (r < R)[..., None]
+    u0[1] = np.where(inside, (0.25 * Y / r)[..., None], 0.0).transpose(1, 0, 2)
+    u0[2] = np.where(inside, (0.25 * Z / r)[..., None], 0.0).transpose(1, 0, 2)
+    pos = d["in_pos"] + np.array([0.0, 0.55, 0.0])  # outermost vertices 0.2 from the wall
+    dd = dict(d)
+    dd["in_pos"] = pos
+    lat, fsi, pid = pipe_capsule_gpu(ctx, dd, u0)
+    nodes, cnt, types = O.pipe_guo_nodes((nx, ny, nz), y0, z0, R)
+    L = O.set_guo(O.lattice((nx, ny, nz), (1, 1, 1), "bgk_guo_vof", 1.0, 1.0, celltype=types), nodes, cnt)
+    S = O.System(L, "roma", -1.0)
+    S.f[...] = O.apply_guo(L, O.init_equilibrium(L, None, u0))
+    S.set_body_force(d["in_body"])
+    S.set_pipe(y0, z0, R)
+    opid = S.add_particle(S.add_shape(d["in_rest"], d["in_tri"]), "capsule_skalak", d["in_params"], pos)
+    S.init()
+    S.step(1)
+    fsi.step(1)
+    g, o = fsi.get_particle(pid), S.particle(opid)
+    free = pos + o["vel"]
+    crossed = np.hypot(free[:, 1] - y0, free[:, 2] - z0) > R
+    assert crossed.sum() >= 3  # the step pushes some vertices through the wall
+    assert np.hypot(o["pos"][:, 1] - y0, o["pos"][:, 2] - z0).max() <= R
+    assert np.abs(g["pos"] - o["pos"]).max() < 1e-12
+    ctx.set_graph_mode(True)
