@@ -80,6 +80,7 @@ SIGNATURES = {
     "bib_lattice_get_velocity": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_shape_store": (C.c_int32, [_vp, _dp, _ip, C.c_int64, C.c_int64, _i32p]),
     "bib_shape_info": (C.c_int32, [_vp, C.c_int32, _dp]),
+    "bib_shape_set_tag": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),
     "bib_ib_configure": (C.c_int32, [_vp, C.c_int32, C.POINTER(IbParams)]),
     "bib_particle_add": (C.c_int32, [_vp, C.c_int32, C.c_int32, C.c_int32, _dp, _dp, _i32p]),
     "bib_particle_count": (C.c_int32, [_vp, C.c_int32, _i32p]),
@@ -99,6 +100,11 @@ SIGNATURES = {
     "bib_particle_info": (C.c_int32, [_vp, C.c_int32, C.c_int32, _i32p]),
     "bib_lattice_iteration": (C.c_int32, [_vp, C.c_int32, _ip]),
     "bib_checkpoint_save": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),
+    "bib_particles_save_plb": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_char_p]),
+    "bib_particles_load_plb": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_char_p]),
+    "bib_particles_write_vtu": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_uint64]),
+    "bib_particle_write_vtu": (C.c_int32, [_vp, C.c_int32, C.c_int32, C.c_char_p]),
+    "bib_particles_write_lightweight": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_uint64]),
     "bib_checkpoint_load": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),
     "bib_step": (C.c_int32, [_vp, C.c_int32, C.c_int64]),
     "bib_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),

@@ -260,6 +260,7 @@ class ParticleShapeLibrary:
         sid = C.c_int32()
         self.ctx.check(self.ctx.lib.bib_shape_store(self.ctx.h, _d(xyz), tri.ctypes.data_as(C.POINTER(C.c_int64)),
                                                     xyz.shape[0], tri.shape[0], C.byref(sid)))
+        self.ctx.check(self.ctx.lib.bib_shape_set_tag(self.ctx.h, sid.value, str(tag).encode()))
         self.by_tag[tag] = sid.value
         self.meshes[sid.value] = (xyz, tri)
         return sid.value
@@ -335,6 +336,37 @@ class ImmersedBoundaryDynamics3D:
         """Restore a checkpoint into this lattice; its particles replace the current ones.  The
         shapes must be stored in the same order as in the run that saved it."""
         self.ctx.check(self.ctx.lib.bib_checkpoint_load(self.ctx.h, self.lattice.h, os.fsencode(path)))
+        self._refresh_particles()
+
+    def save_particle_checkpoint(self, name, folder=""):
+        """The reference's save_checkpoint (ImmersedBoundaryDynamics_io.hh:17-73): the particles in
+        its .plb format, header <folder>/<name>.plb and data <folder>/<name>/0.plb."""
+        self.ctx.check(self.ctx.lib.bib_particles_save_plb(self.ctx.h, self.lattice.h, os.fsencode(folder),
+                                                           os.fsencode(name)))
+
+    def load_particle_checkpoint(self, name, folder=""):
+        """The reference's load_checkpoint (ImmersedBoundaryDynamics_io.hh:75-159) of a .plb particle
+        checkpoint, written by either library; the particles replace the current ones."""
+        self.ctx.check(self.ctx.lib.bib_particles_load_plb(self.ctx.h, self.lattice.h, os.fsencode(folder),
+                                                           os.fsencode(name)))
+        self._refresh_particles()
+
+    def write_particles_as_vtk(self, iteration, folder=""):
+        """One <folder>/obj<id>-<iteration>.vtu per particle (ImmersedBoundaryDynamics_io.hh:161-176)."""
+        self.ctx.check(self.ctx.lib.bib_particles_write_vtu(self.ctx.h, self.lattice.h, os.fsencode(folder),
+                                                            int(iteration)))
+
+    def write_particle_vtk(self, pid, path):
+        """ParticleBase3D::write_vtk of one particle (ParticleBase.hh:270-390)."""
+        self.ctx.check(self.ctx.lib.bib_particle_write_vtu(self.ctx.h, self.lattice.h, int(pid), os.fsencode(path)))
+
+    def write_lightweight_particle_data(self, iteration, folder=""):
+        """<folder>/objsP0-<iteration>.txt: centre, gyration tensor and volume per particle
+        (ImmersedBoundaryDynamics_io.hh:178-199)."""
+        self.ctx.check(self.ctx.lib.bib_particles_write_lightweight(self.ctx.h, self.lattice.h, os.fsencode(folder),
+                                                                    int(iteration)))
+
+    def _refresh_particles(self):
         n = C.c_int32()
         self.ctx.check(self.ctx.lib.bib_particle_count(self.ctx.h, self.lattice.h, C.byref(n)))
         info = np.zeros(3, dtype=np.int32)

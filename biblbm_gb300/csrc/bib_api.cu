@@ -35,7 +35,7 @@ struct bib_ctx {
     double prof[5] = {0, 0, 0, 0, 0};  // membrane, spread, collide+stream, walls, interpolate+update
     cudaEvent_t ev[6] = {};
     int* d_flag = nullptr;
-    std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, parity) -> two-step graph
+    std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, steps and parity) -> step graph
     double* stage = nullptr;  // device staging area of the host <-> device population transfers
     size_t stage_count = 0;   // its size in doubles
     std::vector<std::unique_ptr<Batch>> batches;
@@ -578,41 +578,66 @@ bib_status accumulate_profile(bib_ctx* c) {
     return BIB_OK;
 }
 
+// The instantiated graph of `steps` (1 or 2) coupled steps from the lattice's current parity
+// state, captured on first use.  Capturing leaves the host-side state as it was.
+bib_status step_graph(bib_ctx* c, Lattice& L, int steps, cudaGraphExec_t* out) {
+    const std::pair<int, int> key(L.handle, (steps - 1) * 8 + L.cur * 4 + L.pcur * 2 + L.fe);
+    GraphEntry& ge = c->graphs[key];
+    if (!ge.exec) {
+        const int cur0 = L.cur, pcur0 = L.pcur, fe0 = L.fe;
+        const bool clean0 = L.target_clean;
+        cudaGraph_t g = nullptr;
+        BIB_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < steps; ++k) enqueue_step(c, L, true, true);
+        cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+        L.cur = cur0;
+        L.pcur = pcur0;
+        L.fe = fe0;
+        L.target_clean = clean0;
+        if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        e = cudaGraphInstantiate(&ge.exec, g, 0);
+        cudaGraphDestroy(g);
+        if (e != cudaSuccess) {
+            ge.exec = nullptr;
+            return fail(c, BIB_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+        }
+    }
+    *out = ge.exec;
+    return BIB_OK;
+}
+
 bib_status run_steps(bib_ctx* c, int32_t h, int64_t nsteps, bool with_ib, bool with_lbm) {
     Lattice* L = get_lattice(c, h);
     if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle %d", h);
     if (nsteps < 0) return fail(c, BIB_EINVAL, "negative step count");
     bib_status st = sync_particles(c, *L);
     if (st) return st;
-    const bool use_graph = c->graph_mode && !c->profiling && with_ib && with_lbm && nsteps >= 2;
+    const bool use_graph = c->graph_mode && !c->profiling && with_ib && with_lbm && nsteps >= 1;
     int64_t done = 0;
     if (use_graph) {
-        if (!L->target_clean) {  // the graph assumes a clean spreading target on entry
+        if (!L->target_clean) {  // the graphs assume a clean spreading target on entry
             enqueue_step(c, *L, true, true);
             BIB_CHECK_LAUNCH(c);
             ++done;
         }
-        const std::pair<int, int> key(h, L->cur * 4 + L->pcur * 2 + L->fe);
-        GraphEntry& ge = c->graphs[key];
-        if (!ge.exec) {
-            const int cur0 = L->cur, pcur0 = L->pcur, fe0 = L->fe;
-            const bool clean0 = L->target_clean;
-            cudaGraph_t g = nullptr;
-            BIB_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            enqueue_step(c, *L, true, true);
-            enqueue_step(c, *L, true, true);
-            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-            L->cur = cur0;
-            L->pcur = pcur0;
-            L->fe = fe0;
-            L->target_clean = clean0;
-            if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
-            e = cudaGraphInstantiate(&ge.exec, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph instantiation failed: %s", cudaGetErrorString(e));
+        // a two-step graph leaves every parity unchanged; a one-step graph (the step-then-read
+        // loop) exists per parity state and flips all three
+        if (done + 2 <= nsteps) {
+            cudaGraphExec_t g2 = nullptr;
+            st = step_graph(c, *L, 2, &g2);
+            if (st) return st;
+            for (; done + 2 <= nsteps; done += 2) BIB_CUDA(c, cudaGraphLaunch(g2, c->stream));
         }
-        for (; done + 2 <= nsteps; done += 2) BIB_CUDA(c, cudaGraphLaunch(ge.exec, c->stream));
-        // two steps leave every parity unchanged
+        if (done < nsteps) {
+            cudaGraphExec_t g1 = nullptr;
+            st = step_graph(c, *L, 1, &g1);
+            if (st) return st;
+            BIB_CUDA(c, cudaGraphLaunch(g1, c->stream));
+            L->cur = 1 - L->cur;
+            L->pcur = 1 - L->pcur;
+            L->fe = 1 - L->fe;
+            ++done;
+        }
     }
     for (; done < nsteps; ++done) {
         enqueue_step(c, *L, with_ib, with_lbm);
@@ -2269,6 +2294,269 @@ bib_status bib_checkpoint_load(bib_ctx* c, int32_t h, const char* path) {
     }
     drop_graphs(c, h);
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BIB_OK;
+}
+
+}  // extern "C"
+
+// ---- the reference's particle files: .plb checkpoints, VTU and lightweight text output ----
+namespace {
+
+// the folder part that FileName::setPath gives an output call: "<dir>/", or nothing
+std::string folder_prefix(const char* dir) {
+    std::string d = dir ? dir : "";
+    if (!d.empty() && d.back() != '/') d += '/';
+    return d;
+}
+
+// FileName of save_checkpoint / load_checkpoint (io/plbFiles.cpp:37-58): the base name
+// without folder and extension; the folder and ".plb" come from the call
+std::string checkpoint_name(const char* name) {
+    std::string n = name ? name : "";
+    const size_t sep = n.find_last_of("\\/");
+    if (sep != std::string::npos) n = n.substr(sep + 1);
+    const size_t dot = n.find_last_of('.');
+    if (dot != std::string::npos) n = n.substr(0, dot);
+    return n;
+}
+
+// positions, velocities, forces (3 per vertex) and STATS per particle on the host
+bib_status particle_state(bib_ctx* c, Lattice& L, std::vector<double>& pos, std::vector<double>& vel,
+                          std::vector<double>& frc, std::vector<double>& stats) {
+    if (L.particles_dirty) {
+        pos = L.host_pos;
+        vel.assign(pos.size(), 0.0);
+        frc.assign(pos.size(), 0.0);
+        stats = L.host_stats;
+        return BIB_OK;
+    }
+    const size_t n3 = 3 * (size_t)L.nvert;
+    pos.resize(n3);
+    vel.resize(n3);
+    frc.resize(n3);
+    stats.resize(STATS * L.parts.size());
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (n3) {
+        BIB_CUDA(c, cudaMemcpy(pos.data(), L.pos[L.pcur], n3 * 8, cudaMemcpyDeviceToHost));
+        BIB_CUDA(c, cudaMemcpy(vel.data(), L.vel, n3 * 8, cudaMemcpyDeviceToHost));
+        BIB_CUDA(c, cudaMemcpy(frc.data(), L.force, n3 * 8, cudaMemcpyDeviceToHost));
+    }
+    if (!stats.empty())
+        BIB_CUDA(c, cudaMemcpy(stats.data(), L.stats, stats.size() * 8, cudaMemcpyDeviceToHost));
+    return BIB_OK;
+}
+
+bool write_file(const std::string& path, const std::string& bytes, bool binary) {
+    FILE* f = fopen(path.c_str(), binary ? "wb" : "w");
+    if (!f) return false;
+    const bool ok = fwrite(bytes.data(), 1, bytes.size(), f) == bytes.size();
+    return fclose(f) == 0 && ok;
+}
+
+bool read_file(const std::string& path, std::string& bytes) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    bytes.clear();
+    char buf[1 << 16];
+    size_t n;
+    while ((n = fread(buf, 1, sizeof(buf), f)) > 0) bytes.append(buf, n);
+    const bool ok = !ferror(f);
+    fclose(f);
+    return ok;
+}
+
+}  // namespace
+
+extern "C" {
+
+bib_status bib_shape_set_tag(bib_ctx* c, int32_t shape, const char* tag) {
+    if (!c || !tag || shape < 0 || shape >= (int32_t)c->shapes.size()) return fail(c, BIB_EINVAL, "invalid shape or tag");
+    c->shapes[shape]->tag = tag;
+    return BIB_OK;
+}
+
+bib_status bib_particles_save_plb(bib_ctx* c, int32_t h, const char* dir, const char* name) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    const std::string base = folder_prefix(dir), nm = checkpoint_name(name);
+    if (nm.empty()) return fail(c, BIB_EINVAL, "empty checkpoint name");
+    std::vector<double> pos, vel, frc, stats;
+    bib_status st = particle_state(c, *L, pos, vel, frc, stats);
+    if (st) return st;
+    // pack everything first: a particle without a reference type leaves no files behind
+    std::string body;
+    const int64_t np = (int64_t)L->parts.size();
+    body.append(reinterpret_cast<const char*>(&np), sizeof(np));
+    std::string err;
+    for (int64_t p = 0; p < np; ++p) {
+        const ParticleHost& ph = L->parts[p];
+        PlbParticle pp;
+        pp.shape = ph.shape;
+        pp.id = p;
+        pp.model = ph.model;
+        const size_t o = 3 * (size_t)ph.v0, n = 3 * (size_t)ph.nv;
+        pp.pos.assign(pos.begin() + o, pos.begin() + o + n);
+        pp.vel.assign(vel.begin() + o, vel.begin() + o + n);
+        pp.force.assign(frc.begin() + o, frc.begin() + o + n);
+        for (int k = 0; k < BIB_P_COUNT; ++k) pp.prm[k] = ph.prm[k];
+        if (!plb_pack(body, pp, err)) return fail(c, BIB_EUNSUPPORTED, "particle %lld: %s", (long long)p, err.c_str());
+    }
+    if (!mkdir_p(base + nm)) return fail(c, BIB_EINVAL, "cannot create the folder %s%s", base.c_str(), nm.c_str());
+    const std::string header = std::to_string(np) + "\n1\n" + nm + "/0.plb\n";
+    if (!write_file(base + nm + ".plb", header, false))
+        return fail(c, BIB_EINVAL, "cannot write the checkpoint header %s%s.plb", base.c_str(), nm.c_str());
+    if (!write_file(base + nm + "/0.plb", body, true))
+        return fail(c, BIB_EINVAL, "cannot write %s%s/0.plb", base.c_str(), nm.c_str());
+    return BIB_OK;
+}
+
+bib_status bib_particles_load_plb(bib_ctx* c, int32_t h, const char* dir, const char* name) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    const std::string base = folder_prefix(dir), nm = checkpoint_name(name);
+    std::string text;
+    if (nm.empty() || !read_file(base + nm + ".plb", text))
+        return fail(c, BIB_EINVAL, "cannot read the checkpoint header %s%s.plb", base.c_str(), nm.c_str());
+    // header: particle count, file count, then one file name per line (relative to the folder)
+    std::vector<std::string> lines;
+    {
+        size_t at = 0;
+        while (at < text.size()) {
+            size_t e = text.find('\n', at);
+            if (e == std::string::npos) e = text.size();
+            lines.push_back(text.substr(at, e - at));
+            at = e + 1;
+        }
+    }
+    long long num_particles = -1, num_files = -1;
+    if (lines.size() < 2 || sscanf(lines[0].c_str(), "%lld", &num_particles) != 1 ||
+        sscanf(lines[1].c_str(), "%lld", &num_files) != 1 || num_particles < 0 || num_files < 0 ||
+        (long long)lines.size() < 2 + num_files)
+        return fail(c, BIB_EINVAL, "malformed checkpoint header %s%s.plb", base.c_str(), nm.c_str());
+    std::vector<int> shape_nv(c->shapes.size());
+    for (size_t s = 0; s < c->shapes.size(); ++s) shape_nv[s] = (int)(c->shapes[s]->rest.size() / 3);
+    std::vector<PlbParticle> got;
+    std::string bytes, err;
+    for (long long k = 0; k < num_files; ++k) {
+        const std::string path = base + lines[2 + k];
+        if (!read_file(path, bytes)) return fail(c, BIB_EINVAL, "cannot read %s", path.c_str());
+        const char* it = bytes.data();
+        const char* end = it + bytes.size();
+        int64_t count = 0;
+        if (end - it < 8) return fail(c, BIB_EINVAL, "%s is truncated", path.c_str());
+        std::memcpy(&count, it, 8);
+        it += 8;
+        if (count < 0) return fail(c, BIB_EINVAL, "%s: negative particle count", path.c_str());
+        for (int64_t j = 0; j < count; ++j) {
+            PlbParticle p;
+            if (!plb_unpack(it, end, shape_nv, p, err)) return fail(c, BIB_EINVAL, "%s: %s", path.c_str(), err.c_str());
+            got.push_back(std::move(p));
+        }
+    }
+    // this library numbers particles 0 .. n-1: the ids must be exactly those
+    const int64_t n = (int64_t)got.size();
+    if (num_particles != n)
+        return fail(c, BIB_EUNSUPPORTED, "checkpoint holds %lld particles but ids up to %lld", (long long)n, num_particles);
+    std::vector<int64_t> slot(n, -1);
+    for (int64_t j = 0; j < n; ++j) {
+        const int64_t id = got[j].id;
+        if (id < 0 || id >= n || slot[id] >= 0)
+            return fail(c, BIB_EUNSUPPORTED, "particle ids of the checkpoint are not 0 .. %lld", (long long)(n - 1));
+        slot[id] = j;
+    }
+    std::vector<ParticleHost> parts(n);
+    std::vector<double> pos, vel, frc, stats(STATS * (size_t)n);
+    int64_t v0 = 0;
+    for (int64_t id = 0; id < n; ++id) {
+        PlbParticle& p = got[slot[id]];
+        if (p.model == BIB_MODEL_RBC_WLCPOW && !(p.prm[BIB_P_VOL_DESIRED] != 0))
+            return fail(c, BIB_EINVAL, "particle %lld: vol_desired must be non-zero", (long long)id);
+        ParticleHost& ph = parts[id];
+        ph.shape = (int)p.shape;
+        ph.model = p.model;
+        ph.v0 = (int)v0;
+        ph.nv = shape_nv[p.shape];
+        ph.prm.assign(p.prm, p.prm + BIB_P_COUNT);
+        // add_particle maps the centre of mass to the periodic grid (ImmersedBoundaryDynamics.hh:508-525)
+        double* s = stats.data() + STATS * id;
+        particle_update(*c->shapes[ph.shape], p.pos.data(), s);
+        remap_com(L->d, p.pos.data(), ph.nv, s);
+        pos.insert(pos.end(), p.pos.begin(), p.pos.end());
+        vel.insert(vel.end(), p.vel.begin(), p.vel.end());
+        frc.insert(frc.end(), p.force.begin(), p.force.end());
+        v0 += ph.nv;
+    }
+    if (v0 >= ((int64_t)1 << 31)) return fail(c, BIB_EUNSUPPORTED, "too many vertices");
+    for (auto& B : c->batches)  // batch tables hold the particle set
+        if (B) B->free_tables();
+    L->parts = std::move(parts);
+    L->host_pos = std::move(pos);
+    L->host_stats = std::move(stats);
+    L->particles_dirty = true;
+    free_particles(*L);
+    L->nvert = 0;
+    bib_status st = sync_particles(c, *L);
+    if (st) return st;
+    if (L->nvert) {
+        const size_t vb = 3 * (size_t)L->nvert * sizeof(double);
+        BIB_CUDA(c, cudaMemcpy(L->vel, vel.data(), vb, cudaMemcpyHostToDevice));
+        BIB_CUDA(c, cudaMemcpy(L->force, frc.data(), vb, cudaMemcpyHostToDevice));
+    }
+    drop_graphs(c, h);
+    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BIB_OK;
+}
+
+bib_status bib_particle_write_vtu(bib_ctx* c, int32_t h, int32_t pid, const char* path) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !path || pid < 0 || pid >= (int32_t)L->parts.size()) return fail(c, BIB_EINVAL, "invalid particle or path");
+    std::vector<double> pos, vel, frc, stats;
+    bib_status st = particle_state(c, *L, pos, vel, frc, stats);
+    if (st) return st;
+    const ParticleHost& ph = L->parts[pid];
+    const ShapeHost& S = *c->shapes[ph.shape];
+    const size_t o = 3 * (size_t)ph.v0;
+    if (!write_file(path, vtu_bytes(pos.data() + o, frc.data() + o, ph.nv, S.tri.data(), (int)S.tri_area.size()), true))
+        return fail(c, BIB_EINVAL, "cannot write %s", path);
+    return BIB_OK;
+}
+
+bib_status bib_particles_write_vtu(bib_ctx* c, int32_t h, const char* dir, uint64_t iter) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    std::vector<double> pos, vel, frc, stats;
+    bib_status st = particle_state(c, *L, pos, vel, frc, stats);
+    if (st) return st;
+    const std::string base = folder_prefix(dir);
+    if (!base.empty() && !mkdir_p(base)) return fail(c, BIB_EINVAL, "cannot create the folder %s", base.c_str());
+    for (size_t p = 0; p < L->parts.size(); ++p) {
+        const ParticleHost& ph = L->parts[p];
+        const ShapeHost& S = *c->shapes[ph.shape];
+        const size_t o = 3 * (size_t)ph.v0;
+        const std::string path = base + "obj" + std::to_string(p) + "-" + std::to_string(iter) + ".vtu";
+        if (!write_file(path, vtu_bytes(pos.data() + o, frc.data() + o, ph.nv, S.tri.data(), (int)S.tri_area.size()), true))
+            return fail(c, BIB_EINVAL, "cannot write %s", path.c_str());
+    }
+    return BIB_OK;
+}
+
+bib_status bib_particles_write_lightweight(bib_ctx* c, int32_t h, const char* dir, uint64_t iter) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    std::vector<double> pos, vel, frc, stats;
+    bib_status st = particle_state(c, *L, pos, vel, frc, stats);
+    if (st) return st;
+    const std::string base = folder_prefix(dir);
+    if (!base.empty() && !mkdir_p(base)) return fail(c, BIB_EINVAL, "cannot create the folder %s", base.c_str());
+    std::string text = "iteration:" + std::to_string(iter) + "\n";
+    for (size_t p = 0; p < L->parts.size(); ++p) {
+        const ParticleHost& ph = L->parts[p];
+        const double* s = stats.data() + STATS * p;
+        text += lightweight_line(c->shapes[ph.shape]->tag, (int64_t)p, pos.data() + 3 * (size_t)ph.v0, ph.nv, s + 2, s[1]);
+        text += "\n";
+    }
+    const std::string path = base + "objsP0-" + std::to_string(iter) + ".txt";
+    if (!write_file(path, text, false)) return fail(c, BIB_EINVAL, "cannot write %s", path.c_str());
     return BIB_OK;
 }
 

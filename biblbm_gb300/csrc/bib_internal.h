@@ -185,6 +185,7 @@ struct ShapeHost {
     std::vector<int> tri, tri4, links, pairs, inc_off, inc;
     std::vector<float> tri_rest_f, tri_area_f, pair_cs_f;
     double area = 0, volume = 0;
+    std::string tag;  // ParticleShape tag (ParticleShape.h:64), the shape's name in text output
     ShapeDev dev{};
 };
 
@@ -341,5 +342,27 @@ bool staged_collide_view(const Lattice& L, int tile_cells, CollideView& v);
 // ---- spreading without device allocation (noalloc.cu) ----
 bib_status spread_noalloc(const Lattice& L, int device, cudaStream_t s, const double* pos, const double* force,
                           int64_t nvert, void* field, std::string& msg);
+
+// ---- the reference's particle file formats (particle_io.cu) ----
+// Particle type ids of the reference's particle factory (ParticleFactory.hh:63-66): registration
+// order of the particle classes in a program that includes fsi/headers.hh
+constexpr int64_t kPlbTypeCapsule = 0;  // DeformableCapsuleParticle, DeformableCapsule.hh:43
+constexpr int64_t kPlbTypeRbc = 1;      // RBCParticle, RBCParticle.hh:123
+struct PlbParticle {
+    int64_t shape = 0, id = 0;
+    int model = 0;  // BIB_MODEL_*
+    bool voxelize = true;
+    std::vector<double> pos, vel, force;  // 3 per vertex
+    double prm[BIB_P_COUNT] = {};
+};
+// append one particle's pack; false (err set) for a model without a reference particle type
+bool plb_pack(std::string& out, const PlbParticle& p, std::string& err);
+// read one particle's pack at it (advanced past it); shape_nv: vertex count per shape id
+bool plb_unpack(const char*& it, const char* end, const std::vector<int>& shape_nv, PlbParticle& p,
+                std::string& err);
+std::string vtu_bytes(const double* pos, const double* force, int nv, const int* tri, int nt);
+std::string lightweight_line(const std::string& tag, int64_t id, const double* pos, int nv, const double* com,
+                             double volume);
+bool mkdir_p(const std::string& dir);
 
 }  // namespace bib

@@ -189,6 +189,8 @@ bib_status bib_lattice_cells(bib_ctx* ctx, int32_t h, int64_t* n);
 bib_status bib_shape_store(bib_ctx* ctx, const double* xyz, const int64_t* tri, int64_t nv, int64_t nt, int32_t* shape);
 /* out[6] = {area, volume, n_links, n_pairs, n_vertices, n_triangles} */
 bib_status bib_shape_info(bib_ctx* ctx, int32_t shape, double* out);
+/* the shape's tag (ParticleShape::get_tag, ParticleShape.h:64), written by the lightweight output */
+bib_status bib_shape_set_tag(bib_ctx* ctx, int32_t shape, const char* tag);
 
 /* ---- immersed boundary: ImmersedBoundaryDynamics3D ---- */
 bib_status bib_ib_configure(bib_ctx* ctx, int32_t h, const bib_ib_params* p);
@@ -261,6 +263,32 @@ bib_status bib_lattice_iteration(bib_ctx* ctx, int32_t h, int64_t* iteration);
  * is being read. ---- */
 bib_status bib_checkpoint_save(bib_ctx* ctx, int32_t h, const char* path);
 bib_status bib_checkpoint_load(bib_ctx* ctx, int32_t h, const char* path);
+
+/* ---- the reference's own particle files.  `dir` is the folder of the reference's FileName
+ * (global::directories() output / input folder; NULL or "" = the working directory); missing
+ * folders are created.
+ * bib_particles_save_plb / _load_plb: ImmersedBoundaryDynamics3D::save_checkpoint /
+ * load_checkpoint (ImmersedBoundaryDynamics_io.hh:17-159).  `name` is taken without folder and
+ * extension, as FileName does.  Save writes the text header <dir>/<name>.plb (particle count, file
+ * count 1, "<name>/0.plb") and the binary <dir>/<name>/0.plb: an int64 particle count, then each
+ * particle's pack (ParticleBase.hh:218-224, DeformableParticle3D.hh:277-287, DeformableCapsule.hh:
+ * 217-223, RBCParticle.hh:344-350) with its positions, vertex velocities and vertex forces.
+ * Capsules (either shear law) and RBCs only: another model gives BIB_EUNSUPPORTED and no file.
+ * Load reads every file the header lists (any rank count), maps each centre of mass to the
+ * periodic grid as add_particle does, and replaces the lattice's particles; the ids must be
+ * 0 .. n-1 (BIB_EUNSUPPORTED otherwise) and the shapes must be stored under the same ids.
+ * bib_particles_write_vtu: write_particles_as_vtk (ImmersedBoundaryDynamics_io.hh:161-176), one
+ * file <dir>/obj<id>-<iter>.vtu per particle in ParticleBase3D::write_vtk's layout
+ * (ParticleBase.hh:270-390): Float32 positions and vertex forces, Int32 triangles, raw appended data.
+ * bib_particle_write_vtu: ParticleBase3D::write_vtk of one particle to `path`.
+ * bib_particles_write_lightweight: write_lightweight_particle_data (ImmersedBoundaryDynamics_io.hh:
+ * 178-199): <dir>/objsP0-<iter>.txt, "iteration:<iter>" then per particle
+ * tag:id:centre:gyration tensor (xx xy xz yy yz zz):volume (DeformableParticle3D.hh:318-333). ---- */
+bib_status bib_particles_save_plb(bib_ctx* ctx, int32_t h, const char* dir, const char* name);
+bib_status bib_particles_load_plb(bib_ctx* ctx, int32_t h, const char* dir, const char* name);
+bib_status bib_particles_write_vtu(bib_ctx* ctx, int32_t h, const char* dir, uint64_t iter);
+bib_status bib_particle_write_vtu(bib_ctx* ctx, int32_t h, int32_t pid, const char* path);
+bib_status bib_particles_write_lightweight(bib_ctx* ctx, int32_t h, const char* dir, uint64_t iter);
 
 /* ---- coupled step: computeVelocity -> setExternalVector -> IB step -> collideAndStream ---- */
 bib_status bib_step(bib_ctx* ctx, int32_t h, int64_t nsteps);

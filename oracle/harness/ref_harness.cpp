@@ -27,6 +27,11 @@
 //   interact the vertex forces of one IB step with a particle-particle interaction
 //           (add_pp_force, CollisionForces.h) and a wall interaction decorator
 //           (add_force_decorator, ForceDecorator.hh) on parallel plates (Boundary.h:305-365)
+//   plb     the particle output formats of particles with given positions, velocities and
+//           forces: save_checkpoint (ImmersedBoundaryDynamics_io.hh:17-73),
+//           write_particles_as_vtk (_io.hh:161-176, ParticleBase.hh:270-390) and
+//           write_lightweight_particle_data (_io.hh:178-199, DeformableParticle3D.hh:318-333),
+//           written under out/ of the working directory, plus the registered particle type ids
 //
 // Array conventions: lattice fields are (components, nz, ny, nx) with x fastest.
 #define FSI_PROFILE
@@ -39,6 +44,7 @@
 
 #include <string>
 #include <vector>
+#include <sys/stat.h>
 #include "rec_io.h"
 
 using namespace plb;
@@ -789,6 +795,79 @@ static int run_interact(const Bundle& in, const char* out) {
     return 2;
 }
 
+static void store_shape_as(const Bundle& in, ParticleShapeLibrary<T>& lib, const char* xyz_name,
+                           const char* tri_name, const char* tag) {
+    const recio::Array& xyz = recio::need(in, xyz_name);
+    const recio::Array& tri = recio::need(in, tri_name);
+    const unsigned nv = (unsigned)xyz.shape[0], nt = (unsigned)tri.shape[0];
+    std::vector<Array<T, 3> > v(nv);
+    for (unsigned i = 0; i < nv; ++i) v[i] = Array<T, 3>(xyz.d[3 * i], xyz.d[3 * i + 1], xyz.d[3 * i + 2]);
+    std::vector<unsigned> idx(3 * nt);
+    for (unsigned i = 0; i < 3 * nt; ++i) idx[i] = (unsigned)tri.i[i];
+    lib.store_mesh(&v[0], &idx[0], nv, nt, tag);
+}
+
+static int run_plb(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    ParticleShapeLibrary<T> lib;
+    store_shape_as(in, lib, "rest", "tri", "shape");
+    store_shape_as(in, lib, "rest_b", "tri_b", "shape_b");
+    const recio::Array& models = recio::need(in, "models");
+    const recio::Array& shapes = recio::need(in, "shapes");
+    const recio::Array& params = recio::need(in, "params");
+    const recio::Array& pos = recio::need(in, "pos");
+    const recio::Array& vel = recio::need(in, "vel");
+    const recio::Array& frc = recio::need(in, "force");
+    const long long iter = recio::inum(in, "iter");
+    const size_t np = (size_t)models.shape[0];
+
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(1.0, 1.0));
+    lattice.toggleInternalStatistics(false);
+    lattice.periodicity().toggleAll(true);
+    initializeAtEquilibrium(lattice, lattice.getBoundingBox(), (T)1, Array<T, 3>(0., 0., 0.));
+    lattice.initialize();
+    ImmersedBoundaryDynamics3D<T, DESCRIPTOR, Periodicity3D<T, true, true, true> > fsi(lattice, lib);
+    size_t off = 0;
+    for (size_t k = 0; k < np; ++k) {
+        ParticleSpec spec;
+        spec.model = models.i[k];
+        spec.prm.assign(params.d.begin() + 12 * k, params.d.begin() + 12 * (k + 1));
+        const ParticleShapeLibrary<T>& clib = lib;  // the non-const get_by_id does not compile
+        ParticleBase3D<T>* proto = make_particle(clib.get_by_id(shapes.i[k]), spec);
+        for (plint i = 0; i < proto->count_nodes(); ++i)
+            proto->get_node(i).pos = Array<T, 3>(pos.d[off + 3 * i], pos.d[off + 3 * i + 1], pos.d[off + 3 * i + 2]);
+        proto->update();
+        off += 3 * (size_t)proto->count_nodes();
+        fsi.add_particle(proto);
+        delete proto;
+    }
+    off = 0;
+    for (size_t k = 0; k < np; ++k) {
+        ParticleBase3D<T>* p = 0;
+        fsi.get_particle((plint)k, p);
+        for (plint i = 0; i < p->count_nodes(); ++i) {
+            p->get_node(i).vel = Array<T, 3>(vel.d[off + 3 * i], vel.d[off + 3 * i + 1], vel.d[off + 3 * i + 2]);
+            p->get_node(i).force = Array<T, 3>(frc.d[off + 3 * i], frc.d[off + 3 * i + 1], frc.d[off + 3 * i + 2]);
+        }
+        off += 3 * (size_t)p->count_nodes();
+    }
+    ::mkdir("out", 0777);
+    global::directories().setOutputDir("out/");
+    fsi.save_checkpoint(FileName("ckpt"));
+    fsi.write_particles_as_vtk((pluint)iter);
+    fsi.write_lightweight_particle_data((pluint)iter);
+    recio::Writer w(out);
+    std::vector<long long> ids;
+    const ParticleShapeLibrary<T>& clib = lib;
+    DeformableCapsuleParticle<T> capsule(clib.get_by_id(0), CapsuleParameters<T>());
+    RBCParticle<T> rbc(clib.get_by_id(0));
+    ids.push_back(capsule.get_type_id());
+    ids.push_back(rbc.get_type_id());
+    w.i("type_ids", shp(2), ids);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) {
         std::fprintf(stderr, "usage: ref_harness <lbm|ibm|forces|interp|shape|inertia> in.rec out.rec\n");
@@ -808,6 +887,7 @@ int main(int argc, char** argv) {
     if (c == "pipe_guo") return run_pipe_guo(in, argv[3]);
     if (c == "ibm_pipe") return run_ibm_pipe(in, argv[3]);
     if (c == "reflect") return run_reflect(in, argv[3]);
+    if (c == "plb") return run_plb(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

@@ -434,3 +434,133 @@ def move_vertices(pos, vel, pipe=None):
     pp = None if pipe is None else f64(pipe)
     lib().orc_move_vertices(out.shape[0], _d(out), _d(v), None if pp is None else pp.ctypes.data)
     return out
+
+
+# ---------------------------------------------------------------- the reference's particle files
+# Particle type ids of the reference's particle factory (ParticleFactory.hh:63-66): the order in
+# which a program including fsi/headers.hh registers DeformableCapsuleParticle and RBCParticle.
+PLB_TYPE_CAPSULE, PLB_TYPE_RBC = 0, 1
+SHEAR_SKALAK, SHEAR_NEOHOOKEAN = 0, 1  # enum ShearModel, DeformableCapsule.h:39
+CAPSULE_PACK = ["C", "kb", "nu_s", "G"]  # CapsuleParameters::pack, DeformableCapsule.hh:21-29
+RBC_PACK = ["L0", "shear_modulus", "k_area_global", "k_area_local", "k_bend", "k_volume", "theta0",
+            "vol_desired"]  # RBCParameters::pack, RBCParticle.hh:93-105
+
+
+def plb_pack(model, shape, pid, pos, vel, force, prm, voxelize=True) -> bytes:
+    """One particle's pack: ParticleBase3D::pack (ParticleBase.hh:218-224) type id, shape id,
+    particle id, should_voxelize; DeformableParticle3D::pack (DeformableParticle3D.hh:277-287) pos,
+    vel, force per vertex; then DeformableCapsuleParticle::pack (shear law + CapsuleParameters,
+    DeformableCapsule.hh:217-223) or RBCParticle::pack (RBCParameters, RBCParticle.hh:344-350)."""
+    import struct
+
+    prm = dict(zip(PARAM_KEYS, np.asarray(prm, dtype=np.float64)))
+    capsule = model in (MODEL["capsule_neohookean"], MODEL["capsule_skalak"])
+    if not capsule and model != MODEL["rbc_wlcpow"]:
+        raise ValueError("model %d has no particle type in the reference's format" % model)
+    out = [struct.pack("<qqq?", PLB_TYPE_CAPSULE if capsule else PLB_TYPE_RBC, shape, pid, voxelize)]
+    verts = np.concatenate([f64(pos), f64(vel), f64(force)], axis=1)  # (nv, 9): pos, vel, force
+    out.append(verts.astype("<f8").tobytes())
+    if capsule:
+        law = SHEAR_SKALAK if model == MODEL["capsule_skalak"] else SHEAR_NEOHOOKEAN
+        out.append(struct.pack("<i4d", law, *[prm[k] for k in CAPSULE_PACK]))
+    else:
+        out.append(struct.pack("<8d", *[prm[k] for k in RBC_PACK]))
+    return b"".join(out)
+
+
+def plb_unpack(buf: bytes, at: int, shape_nv):
+    """Inverse of plb_pack at byte offset `at`: (particle dict, offset after it)."""
+    import struct
+
+    type_id, shape, pid, vox = struct.unpack_from("<qqq?", buf, at)
+    at += 25
+    nv = shape_nv[shape]
+    verts = np.frombuffer(buf, dtype="<f8", count=9 * nv, offset=at).reshape(nv, 9)
+    at += 72 * nv
+    prm = dict.fromkeys(PARAM_KEYS, 0.0)
+    if type_id == PLB_TYPE_CAPSULE:
+        law, *vals = struct.unpack_from("<i4d", buf, at)
+        at += 36
+        model = MODEL["capsule_skalak"] if law == SHEAR_SKALAK else MODEL["capsule_neohookean"]
+        prm.update(zip(CAPSULE_PACK, vals))
+    elif type_id == PLB_TYPE_RBC:
+        vals = struct.unpack_from("<8d", buf, at)
+        at += 64
+        model = MODEL["rbc_wlcpow"]
+        prm.update(zip(RBC_PACK, vals))
+    else:
+        raise ValueError("unknown particle type %d" % type_id)
+    p = dict(model=model, shape=shape, id=pid, voxelize=vox, pos=verts[:, 0:3].copy(), vel=verts[:, 3:6].copy(),
+             force=verts[:, 6:9].copy(), params=np.array([prm[k] for k in PARAM_KEYS]))
+    return p, at
+
+
+def plb_files(name, particles):
+    """ImmersedBoundaryDynamics3D::save_checkpoint (ImmersedBoundaryDynamics_io.hh:17-73) on one
+    rank: (header text, bytes of <name>/0.plb).  particles: dicts as plb_unpack returns them."""
+    import struct
+
+    header = "%d\n1\n%s/0.plb\n" % (len(particles), name)
+    body = struct.pack("<q", len(particles)) + b"".join(
+        plb_pack(p["model"], p["shape"], p["id"], p["pos"], p["vel"], p["force"], p["params"], p.get("voxelize", True))
+        for p in particles)
+    return header, body
+
+
+def vtu_bytes(pos, force, tri) -> bytes:
+    """ParticleBase3D::write_vtk (ParticleBase.hh:270-390): XML UnstructuredGrid with raw appended
+    data, UInt32 block sizes, Float32 positions and forces, Int32 connectivity, offsets, types."""
+    import struct
+
+    pos, force, tri = f64(pos), f64(force), np.asarray(tri, dtype=np.int64)
+    nv, nt = pos.shape[0], tri.shape[0]
+    sizes = [12 * nv, 12 * nv, 12 * nt, 4 * nt, 4 * nt]
+    offs = [0]
+    for s in sizes[:-1]:
+        offs.append(offs[-1] + 4 + s)
+    head = ('<?xml version="1.0"?>\n'
+            '<VTKFile type="UnstructuredGrid" version="0.1" byte_order="LittleEndian" header_type="UInt32" >\n'
+            '  <UnstructuredGrid>\n'
+            '    <Piece NumberOfPoints="%d" NumberOfCells="%d" >\n'
+            '      <Points>\n'
+            '        <DataArray type="Float32" NumberOfComponents="3" format="appended" offset="%d" />\n'
+            '      </Points>\n'
+            '      <PointData>\n'
+            '        <DataArray type="Float32" NumberOfComponents="3" Name="force_tot" format="appended" offset="%d" />\n'
+            '      </PointData>\n'
+            '      <Cells>\n'
+            '        <DataArray type="Int32" Name="connectivity" format="appended" offset="%d" />\n'
+            '        <DataArray type="Int32" Name="offsets" format="appended" offset="%d" />\n'
+            '        <DataArray type="Int32" Name="types" format="appended" offset="%d" />\n'
+            '      </Cells>\n'
+            '    </Piece>\n'
+            '  </UnstructuredGrid>\n'
+            '  <AppendedData encoding="raw">\n'
+            '_') % (nv, nt, *offs)
+    blocks = [pos.astype("<f4"), force.astype("<f4"), tri.astype("<i4"), 3 * np.arange(1, nt + 1, dtype="<i4"),
+              np.full(nt, 5, dtype="<i4")]
+    data = b"".join(struct.pack("<I", s) + b.tobytes() for s, b in zip(sizes, blocks))
+    return head.encode() + data + b"\n  </AppendedData>\n</VTKFile>\n"
+
+
+def _stream_double(x: float) -> str:
+    """A double as std::ostream writes it with default flags (%g, 6 significant digits)."""
+    return "%g" % x
+
+
+def lightweight_text(iteration, rows) -> str:
+    """write_lightweight_particle_data (ImmersedBoundaryDynamics_io.hh:178-199) with
+    DeformableParticle3D::write_lightweight (DeformableParticle3D.hh:318-333) per particle.
+    rows: (tag, id, positions, centre, volume) per particle; the gyration tensor follows
+    compute_tensor_of_gyration (DeformableParticle3D.hh:111-125)."""
+    lines = ["iteration:%d" % iteration]
+    for tag, pid, pos, com, vol in rows:
+        pos, com = f64(pos), f64(com)
+        g = np.zeros((3, 3))
+        for v in range(pos.shape[0]):
+            for i in range(3):
+                for j in range(i, 3):
+                    g[i, j] += (pos[v, i] - com[i]) * (pos[v, j] - com[j])
+        vals = list(com) + [g[i, j] / pos.shape[0] for i in range(3) for j in range(i, 3)] + [vol]
+        lines.append("%s:%d:" % (tag, pid) + ":".join(_stream_double(float(v)) for v in vals))
+    return "\n".join(lines) + "\n"

@@ -81,6 +81,20 @@ def run(case, inputs):
         return out
 
 
+def run_with_files(case, inputs, files):
+    """run() plus the bytes of the files the harness wrote (paths relative to its working
+    directory), as uint8 arrays keyed by the given names."""
+    with tempfile.TemporaryDirectory() as d:
+        fin, fout = os.path.join(d, "in.rec"), os.path.join(d, "out.rec")
+        write_rec(fin, inputs)
+        subprocess.run([HARNESS, case, fin, fout], check=True, cwd=d, stdout=subprocess.DEVNULL)
+        out = read_rec(fout)
+        for key, rel in files.items():
+            with open(os.path.join(d, rel), "rb") as f:
+                out[key] = np.frombuffer(f.read(), dtype=np.uint8).copy()
+        return out
+
+
 def save(name, inputs, outputs, **extra):
     path = os.path.join(HERE, name + ".npz")
     payload = {"in_" + k: np.asarray(v) for k, v in inputs.items()}
@@ -388,9 +402,41 @@ def case_reflect():
     save("reflect_pipe", inp, {"pos": out["pos"]})
 
 
+def case_plb():
+    """The reference's particle output formats: save_checkpoint (a text header naming one
+    binary file per rank holding each particle's pack), write_particles_as_vtk (one VTU file
+    per particle, appended raw data) and write_lightweight_particle_data (text), for two
+    capsules of either shear law and a red blood cell on a second shape."""
+    rng = np.random.default_rng(808)
+    ico, ico_t = meshes.icosphere(1, 3.0)
+    ef, ef_t = meshes.evans_fung(1, 4.0)
+    shape_out = run("shape", dict(rest=ef, tri=ef_t))
+    V_ef = float(shape_out["volume"][0])
+    lmean = float(shape_out["link_length"].mean())
+    specs = [(0, 0, particle_params(0, G=0.01, C=1.0, kb=0.002, nu_s=0.3), (6.2, 7.1, 8.3)),
+             (1, 0, particle_params(1, G=0.02, C=2.5), (14.5, 6.0, 12.2)),
+             (2, 1, particle_params(2, shear_modulus=0.01, L0=lmean, k_area_global=0.5, k_area_local=0.2,
+                                    k_volume=0.7, vol_desired=V_ef, k_bend=0.05, theta0=0.1), (9.0, 15.0, 7.0))]
+    pos, vel, frc = [], [], []
+    for model, shape, prm, centre in specs:
+        rest = ico if shape == 0 else ef
+        p = meshes.place(deform(rng, rest, 0.05), meshes.random_rotation(rng), centre)
+        pos.append(p)
+        vel.append(1e-3 * rng.standard_normal(p.shape))
+        frc.append(1e-4 * rng.standard_normal(p.shape))
+    inp = dict(dims=np.array([24, 24, 24]), rest=ico, tri=ico_t, rest_b=ef, tri_b=ef_t,
+               models=np.array([s[0] for s in specs]), shapes=np.array([s[1] for s in specs]),
+               params=np.stack([s[2] for s in specs]), pos=np.concatenate(pos), vel=np.concatenate(vel),
+               force=np.concatenate(frc), iter=1234)
+    files = {"file_header": "out/ckpt.plb", "file_rank0": "out/ckpt/0.plb", "file_light": "out/objsP0-1234.txt"}
+    files.update({"file_vtu%d" % k: "out/obj%d-1234.vtu" % k for k in range(len(specs))})
+    out = run_with_files("plb", inp, files)
+    save("plb_particles", inp, out)
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
          case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo, case_ibm_pipe,
-         case_reflect]
+         case_reflect, case_plb]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):

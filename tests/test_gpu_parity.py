@@ -401,6 +401,14 @@ def test_graph_replay_equals_plain_launches(ctx):
     ctx.set_graph_mode(True)
     assert rel(fsi_b.get_particle(pb)["pos"], fsi_a.get_particle(pa)["pos"]) < 1e-14
     assert np.abs(lat_b.receive() - lat_a.receive()).max() < 1e-15
+    # one step at a time with a read after each: one-step graphs of every parity state
+    lat_c, fsi_c, pc = run_coupled_gpu(ctx, d, graph=True)
+    for _ in range(6):
+        fsi_c.step(1)
+        fsi_c.get_particle(pc)
+    assert rel(fsi_c.get_particle(pc)["pos"], fsi_a.get_particle(pa)["pos"]) < 1e-14
+    assert np.abs(lat_c.receive() - lat_a.receive()).max() < 1e-15
+    assert lat_c.iteration() == lat_a.iteration()
 
 
 def oracle_capsule_system(n, U, xyz, tri, pos, prm, dirac="roma", steps=0):
