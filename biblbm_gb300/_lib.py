@@ -105,6 +105,8 @@ SIGNATURES = {
     "bib_particles_write_vtu": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_uint64]),
     "bib_particle_write_vtu": (C.c_int32, [_vp, C.c_int32, C.c_int32, C.c_char_p]),
     "bib_particles_write_lightweight": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_uint64]),
+    "bib_lattice_save_plb": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_char_p]),
+    "bib_lattice_load_plb": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_char_p]),
     "bib_checkpoint_load": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),
     "bib_step": (C.c_int32, [_vp, C.c_int32, C.c_int64]),
     "bib_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),

@@ -216,6 +216,16 @@ class Lattice:
     def load_checkpoint(self, path):
         self.ctx.check(self.ctx.lib.bib_checkpoint_load(self.ctx.h, self.h, os.fsencode(path)))
 
+    def save_plb(self, name, folder=""):
+        """parallelIO::save(lattice, name, false): Palabos' static-content checkpoint, XML spec
+        <folder>/<name>.plb and raw cells <folder>/<name>.dat (io/multiBlockWriter3D.cpp:201-213)."""
+        self.ctx.check(self.ctx.lib.bib_lattice_save_plb(self.ctx.h, self.h, os.fsencode(folder), os.fsencode(name)))
+
+    def load_plb(self, name, folder=""):
+        """parallelIO::load(name, lattice, false) of a checkpoint written by either library, of any
+        block decomposition (io/multiBlockReader3D.cpp:214-268)."""
+        self.ctx.check(self.ctx.lib.bib_lattice_load_plb(self.ctx.h, self.h, os.fsencode(folder), os.fsencode(name)))
+
     def iteration(self) -> int:
         it = C.c_int64()
         self.ctx.check(self.ctx.lib.bib_lattice_iteration(self.ctx.h, self.h, C.byref(it)))

@@ -1568,6 +1568,11 @@ bib_status bib_lattice_receive(bib_ctx* c, int32_t h, void* buf, size_t bytes, i
     launch_force_export(*L, L->fe, d, c->stream);
     BIB_CHECK_LAUNCH(c);
     BIB_CUDA(c, cudaMemcpyAsync(host.data() + Q * n, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
+    std::vector<uint8_t> phase;  // the phase external (0 without a phase field)
+    if (per == 23 && L->phase) {
+        phase.resize((size_t)n);
+        BIB_CUDA(c, cudaMemcpyAsync(phase.data(), L->phase, phase.size(), cudaMemcpyDeviceToHost, c->stream));
+    }
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(d);
     double* dst = (double*)buf;
@@ -1580,7 +1585,7 @@ bib_status bib_lattice_receive(bib_ctx* c, int32_t h, void* buf, size_t bytes, i
                 for (int i = 0; i < Q; ++i) dst[per * w + i] = host[i * n + k];
                 if (per == 23) {
                     for (int a = 0; a < 3; ++a) dst[per * w + Q + a] = host[(Q + a) * n + k];
-                    dst[per * w + 22] = 0.0;
+                    dst[per * w + 22] = phase.empty() ? 0.0 : (phase[k] ? 1.0 : 0.0);
                 }
             }
     return BIB_OK;
@@ -2558,6 +2563,93 @@ bib_status bib_particles_write_lightweight(bib_ctx* c, int32_t h, const char* di
     const std::string path = base + "objsP0-" + std::to_string(iter) + ".txt";
     if (!write_file(path, text, false)) return fail(c, BIB_EINVAL, "cannot write %s", path.c_str());
     return BIB_OK;
+}
+
+bib_status bib_lattice_save_plb(bib_ctx* c, int32_t h, const char* dir, const char* name) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    const std::string base = folder_prefix(dir), nm = checkpoint_name(name);
+    if (nm.empty()) return fail(c, BIB_EINVAL, "empty checkpoint name");
+    const int64_t n = L->d.n;
+    std::vector<double> wire((size_t)23 * n);
+    bib_status st = bib_lattice_receive(c, h, wire.data(), wire.size() * sizeof(double), BIB_LAYOUT_PALABOS_F64);
+    if (st) return st;
+    const int64_t bytes = (int64_t)wire.size() * (int64_t)sizeof(double);
+    if (!base.empty() && !mkdir_p(base)) return fail(c, BIB_EINVAL, "cannot create the folder %s", base.c_str());
+    const std::string xml = plb_lattice_xml(nm + ".dat", L->d.nx, L->d.ny, L->d.nz,
+                                            L->d.collision == BIB_COLLISION_BGK_GUO_VOF, bytes);
+    if (!write_file(base + nm + ".plb", xml, false))
+        return fail(c, BIB_EINVAL, "cannot write %s%s.plb", base.c_str(), nm.c_str());
+    if (!write_file(base + nm + ".dat", std::string((const char*)wire.data(), (size_t)bytes), true))
+        return fail(c, BIB_EINVAL, "cannot write %s%s.dat", base.c_str(), nm.c_str());
+    return BIB_OK;
+}
+
+bib_status bib_lattice_load_plb(bib_ctx* c, int32_t h, const char* dir, const char* name) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    const std::string base = folder_prefix(dir), nm = checkpoint_name(name);
+    std::string xml, err;
+    if (nm.empty() || !read_file(base + nm + ".plb", xml))
+        return fail(c, BIB_EINVAL, "cannot read %s%s.plb", base.c_str(), nm.c_str());
+    PlbLatticeSpec spec;
+    if (!plb_lattice_parse(xml, spec, err)) return fail(c, BIB_EINVAL, "%s%s.plb: %s", base.c_str(), nm.c_str(), err.c_str());
+    if (spec.dynamic) return fail(c, BIB_EUNSUPPORTED, "checkpoints with dynamic content are not read");
+    if (spec.datatype != "double") return fail(c, BIB_EUNSUPPORTED, "data type %s", spec.datatype.c_str());
+    if (spec.cell_dim != 22 && spec.cell_dim != 23)
+        return fail(c, BIB_EUNSUPPORTED, "cell dimension %d (ForcedD3Q19: 22, ForcedPhaseD3Q19: 23)", spec.cell_dim);
+    if (!spec.ordering.empty() && spec.ordering != "zIsFastest")
+        return fail(c, BIB_EUNSUPPORTED, "index ordering %s", spec.ordering.c_str());
+    const LatticeDesc& d = L->d;
+    if (spec.box[0] != 0 || spec.box[1] != d.nx - 1 || spec.box[2] != 0 || spec.box[3] != d.ny - 1 || spec.box[4] != 0 ||
+        spec.box[5] != d.nz - 1)
+        return fail(c, BIB_EINVAL, "checkpoint lattice is %lld x %lld x %lld", (long long)(spec.box[1] - spec.box[0] + 1),
+                    (long long)(spec.box[3] - spec.box[2] + 1), (long long)(spec.box[5] - spec.box[4] + 1));
+    // the raw data next to the spec unless its name has a folder; ".dat" unless it has an extension
+    std::string dat = spec.file;
+    const size_t sep = dat.find_last_of("\\/");
+    if (sep == std::string::npos) dat = base + dat;
+    if (dat.find('.', sep == std::string::npos ? 0 : sep + 1) == std::string::npos) dat += ".dat";
+    std::string raw;
+    if (!read_file(dat, raw)) return fail(c, BIB_EINVAL, "cannot read %s", dat.c_str());
+    const int per = spec.cell_dim;
+    const int64_t n = d.n;
+    std::vector<double> wire((size_t)23 * n, 0.0);
+    std::vector<uint8_t> seen((size_t)n, 0);
+    if (per == 22 && L->phase) {  // no phase in the file: keep the lattice's own
+        std::vector<double> ph((size_t)n);
+        bib_status st = bib_lattice_get_phase(c, h, ph.data());
+        if (st) return st;
+        for (int x = 0; x < d.nx; ++x)
+            for (int y = 0; y < d.ny; ++y)
+                for (int z = 0; z < d.nz; ++z)
+                    wire[23 * ((size_t)z + d.nz * ((size_t)y + (size_t)d.ny * x)) + 22] =
+                        ph[x + (size_t)d.nx * (y + (size_t)d.ny * z)];
+    }
+    int64_t start = 0;
+    for (size_t b = 0; b < spec.comps.size(); ++b) {
+        const std::array<int64_t, 6>& bx = spec.comps[b];
+        if (bx[0] < 0 || bx[1] >= d.nx || bx[2] < 0 || bx[3] >= d.ny || bx[4] < 0 || bx[5] >= d.nz || bx[1] < bx[0] ||
+            bx[3] < bx[2] || bx[5] < bx[4])
+            return fail(c, BIB_EINVAL, "component %zu lies outside the lattice", b);
+        const int64_t cells = (bx[1] - bx[0] + 1) * (bx[3] - bx[2] + 1) * (bx[5] - bx[4] + 1);
+        const int64_t end = spec.offsets[b];
+        if (end - start != cells * per * 8 || end > (int64_t)raw.size())
+            return fail(c, BIB_EINVAL, "component %zu: %lld bytes for %lld cells", b, (long long)(end - start), (long long)cells);
+        const char* src = raw.data() + start;
+        for (int64_t x = bx[0]; x <= bx[1]; ++x)
+            for (int64_t y = bx[2]; y <= bx[3]; ++y)
+                for (int64_t z = bx[4]; z <= bx[5]; ++z) {
+                    const size_t w = (size_t)z + d.nz * ((size_t)y + (size_t)d.ny * x);
+                    std::memcpy(&wire[23 * w], src, (size_t)per * 8);
+                    src += (size_t)per * 8;
+                    seen[w] = 1;
+                }
+        start = end;
+    }
+    for (uint8_t v : seen)
+        if (!v) return fail(c, BIB_EINVAL, "the components do not cover the lattice");
+    return bib_lattice_send(c, h, wire.data(), wire.size() * sizeof(double), BIB_LAYOUT_PALABOS_F64);
 }
 
 }  // extern "C"

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <array>
 #include <string>
 #include <vector>
 
@@ -343,7 +344,7 @@ bool staged_collide_view(const Lattice& L, int tile_cells, CollideView& v);
 bib_status spread_noalloc(const Lattice& L, int device, cudaStream_t s, const double* pos, const double* force,
                           int64_t nvert, void* field, std::string& msg);
 
-// ---- the reference's particle file formats (particle_io.cu) ----
+// ---- the reference's particle file formats (reference_files.cu) ----
 // Particle type ids of the reference's particle factory (ParticleFactory.hh:63-66): registration
 // order of the particle classes in a program that includes fsi/headers.hh
 constexpr int64_t kPlbTypeCapsule = 0;  // DeformableCapsuleParticle, DeformableCapsule.hh:43
@@ -364,5 +365,16 @@ std::string vtu_bytes(const double* pos, const double* force, int nv, const int*
 std::string lightweight_line(const std::string& tag, int64_t id, const double* pos, int nv, const double* com,
                              double volume);
 bool mkdir_p(const std::string& dir);
+// parallelIO XML spec of a one-block ForcedPhaseD3Q19 lattice with static content of `bytes` bytes
+std::string plb_lattice_xml(const std::string& dat_file, int nx, int ny, int nz, bool vof, int64_t bytes);
+struct PlbLatticeSpec {
+    int cell_dim = 0;
+    bool dynamic = false;
+    std::string datatype, file, ordering;
+    int64_t box[6] = {};                      // x0 x1 y0 y1 z0 z1, inclusive
+    std::vector<std::array<int64_t, 6>> comps;  // block boxes
+    std::vector<int64_t> offsets;             // end offset of each block's bytes
+};
+bool plb_lattice_parse(const std::string& xml, PlbLatticeSpec& s, std::string& err);
 
 }  // namespace bib

@@ -22,6 +22,13 @@
 //   lightweight text output   DeformableParticle3D::write_lightweight (DeformableParticle3D.hh:
 //                             318-333): tag:id:centre:gyration tensor (upper triangle):volume,
 //                             default stream formatting.
+//   lattice checkpoint        parallelIO::save / load with static content (io/multiBlockWriter3D.cpp:
+//                             53-137, 201-213, 273-310; io/multiBlockReader3D.cpp:135-268): an XML
+//                             spec <name>.plb listing the lattice's blocks ("components", inclusive
+//                             boxes) and the end offset of each block's bytes in the raw file
+//                             <name>.dat; a block's bytes are its cells x-major with z fastest, each
+//                             cell its 19 populations f-bar then its external scalars
+//                             (BlockLattice3D::send, blockLattice3D.hh:671-689), as doubles.
 #include "bib_internal.h"
 
 #include <sys/stat.h>
@@ -198,6 +205,114 @@ std::string lightweight_line(const std::string& tag, int64_t id, const double* p
         for (int j = i; j < 3; ++j) o << ":" << g[i][j] / nv;
     o << ":" << volume;
     return o.str();
+}
+
+std::string plb_lattice_xml(const std::string& dat_file, int nx, int ny, int nz, bool vof, int64_t bytes) {
+    // XMLwriter::print layout: four spaces per level, "<tag> value </tag>"
+    std::ostringstream o;
+    const std::string box = "0 " + std::to_string(nx - 1) + " 0 " + std::to_string(ny - 1) + " 0 " + std::to_string(nz - 1);
+    o << "<?xml version=\"1.0\" ?>\n"
+      << "<Block3D>\n"
+      << "    <General>\n"
+      << "        <Family> BlockLattice3D </Family>\n"
+      << "        <Datatype> double </Datatype>\n"
+      << "        <Descriptor> ForcedPhaseD3Q19 </Descriptor>\n"
+      << "        <cellDim> 23 </cellDim>\n"
+      << "        <dynamicContent> False </dynamicContent>\n"
+      << "        <globalId> 0 </globalId>\n"
+      << "    </General>\n"
+      << "    <Structure>\n"
+      << "        <BoundingBox> " << box << " </BoundingBox>\n"
+      << "        <EnvelopeWidth> 1 </EnvelopeWidth>\n"
+      << "        <GridLevel> 0 </GridLevel>\n"
+      << "        <NumComponents> 1 </NumComponents>\n"
+      << "    </Structure>\n"
+      << "    <Data>\n"
+      << "        <File> " << dat_file << " </File>\n"
+      << "        <Component> " << box << " </Component>\n"
+      << "        <Offsets> " << bytes << " </Offsets>\n";
+    if (vof)  // the registered name of GuoExternalForceVOFDynamics and its id in the reference's programs
+        o << "        <DynamicsDict>\n"
+          << "            <Guo_VOF_dynamics> 3 </Guo_VOF_dynamics>\n"
+          << "        </DynamicsDict>\n";
+    o << "    </Data>\n"
+      << "</Block3D>\n";
+    return o.str();
+}
+
+namespace {
+
+// text of every leaf element <tag ...> text </tag> of an XML document, in order
+std::vector<std::string> xml_leaves(const std::string& xml, const std::string& tag) {
+    std::vector<std::string> out;
+    const std::string open = "<" + tag, close = "</" + tag + ">";
+    size_t at = 0;
+    while ((at = xml.find(open, at)) != std::string::npos) {
+        const size_t after = at + open.size();
+        if (after >= xml.size() || (xml[after] != '>' && xml[after] != ' ' && xml[after] != '\t')) {
+            at = after;
+            continue;
+        }
+        const size_t gt = xml.find('>', after);
+        if (gt == std::string::npos) break;
+        const size_t end = xml.find(close, gt);
+        if (end == std::string::npos) break;
+        out.push_back(xml.substr(gt + 1, end - gt - 1));
+        at = end + close.size();
+    }
+    return out;
+}
+
+std::string trim(const std::string& s) {
+    const size_t a = s.find_first_not_of(" \t\r\n"), b = s.find_last_not_of(" \t\r\n");
+    return a == std::string::npos ? std::string() : s.substr(a, b - a + 1);
+}
+
+bool ints(const std::string& s, std::vector<int64_t>& v) {
+    std::istringstream in(s);
+    v.clear();
+    long long x;
+    while (in >> x) v.push_back(x);
+    return in.eof();
+}
+
+bool one(const std::string& xml, const std::string& tag, std::string& v) {
+    std::vector<std::string> l = xml_leaves(xml, tag);
+    if (l.size() != 1) return false;
+    v = trim(l[0]);
+    return true;
+}
+
+}  // namespace
+
+bool plb_lattice_parse(const std::string& xml, PlbLatticeSpec& s, std::string& err) {
+    std::string v;
+    std::vector<int64_t> iv;
+    if (!one(xml, "cellDim", v) || !ints(v, iv) || iv.size() != 1) return err = "no cellDim", false;
+    s.cell_dim = (int)iv[0];
+    if (!one(xml, "dynamicContent", v)) return err = "no dynamicContent", false;
+    s.dynamic = !(v == "False" || v == "false" || v == "0");
+    if (!one(xml, "Datatype", v)) return err = "no Datatype", false;
+    s.datatype = v;
+    if (!one(xml, "BoundingBox", v) || !ints(v, iv) || iv.size() != 6) return err = "no BoundingBox", false;
+    for (int k = 0; k < 6; ++k) s.box[k] = iv[k];
+    if (!one(xml, "NumComponents", v) || !ints(v, iv) || iv.size() != 1) return err = "no NumComponents", false;
+    const int64_t ncomp = iv[0];
+    if (!one(xml, "Offsets", v) || !ints(v, s.offsets)) return err = "no Offsets", false;
+    if (!one(xml, "File", v) || v.empty()) return err = "no File", false;
+    s.file = v;
+    s.ordering.clear();
+    one(xml, "IndexOrdering", s.ordering);
+    s.comps.clear();
+    for (const std::string& c : xml_leaves(xml, "Component")) {
+        if (!ints(trim(c), iv) || iv.size() != 6) return err = "malformed Component", false;
+        std::array<int64_t, 6> b;
+        for (int k = 0; k < 6; ++k) b[k] = iv[k];
+        s.comps.push_back(b);
+    }
+    if ((int64_t)s.comps.size() != ncomp || (int64_t)s.offsets.size() != ncomp)
+        return err = "component and offset counts differ from NumComponents", false;
+    return true;
 }
 
 bool mkdir_p(const std::string& dir) {

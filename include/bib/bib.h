@@ -84,7 +84,7 @@ enum { BIB_SPREAD_ATOMIC = 0, BIB_SPREAD_DETERMINISTIC = 1 };
 /* host layouts of bib_lattice_send / _receive:
  *  SOA_F64         19 arrays of n doubles, x fastest (this library's order)
  *  PALABOS_F64     Palabos static-cell wire order: x-major, z fastest, 23 doubles per cell
- *                  (19 f-bar + 4 external scalars), blockLattice3D.hh:671-689
+ *                  (19 f-bar + 4 external scalars: force, phase), blockLattice3D.hh:671-689
  *  COPROCESSOR_F64 CoProcessor3D::send order: x-major, z fastest, 19 f-bar per cell
  *                  (coProcessor3D.h:80-91) */
 /* per-cell dynamics, defineDynamics(lattice, domain, new BounceBack / NoDynamics), core/dynamics.h:559-600 */
@@ -289,6 +289,15 @@ bib_status bib_particles_load_plb(bib_ctx* ctx, int32_t h, const char* dir, cons
 bib_status bib_particles_write_vtu(bib_ctx* ctx, int32_t h, const char* dir, uint64_t iter);
 bib_status bib_particle_write_vtu(bib_ctx* ctx, int32_t h, int32_t pid, const char* path);
 bib_status bib_particles_write_lightweight(bib_ctx* ctx, int32_t h, const char* dir, uint64_t iter);
+/* parallelIO::save(lattice, name, false) / parallelIO::load(name, lattice, false) (io/multiBlockWriter3D.cpp:
+ * 53-137, 201-213; io/multiBlockReader3D.cpp:135-268): the lattice in Palabos' static-content checkpoint,
+ * an XML spec <dir>/<name>.plb and the raw cells <dir>/<name>.dat (x-major, z fastest; per cell 19
+ * f-bar, the force and the phase as doubles, BIB_LAYOUT_PALABOS_F64).  Save writes one block of
+ * descriptor ForcedPhaseD3Q19.  Load reads any block decomposition (a checkpoint of a multi-rank run)
+ * of ForcedPhaseD3Q19 or ForcedD3Q19 (then the phase field is kept) into a lattice of the same size,
+ * as bib_lattice_send does; dynamic content gives BIB_EUNSUPPORTED. */
+bib_status bib_lattice_save_plb(bib_ctx* ctx, int32_t h, const char* dir, const char* name);
+bib_status bib_lattice_load_plb(bib_ctx* ctx, int32_t h, const char* dir, const char* name);
 
 /* ---- coupled step: computeVelocity -> setExternalVector -> IB step -> collideAndStream ---- */
 bib_status bib_step(bib_ctx* ctx, int32_t h, int64_t nsteps);

@@ -32,6 +32,12 @@
 //           write_particles_as_vtk (_io.hh:161-176, ParticleBase.hh:270-390) and
 //           write_lightweight_particle_data (_io.hh:178-199, DeformableParticle3D.hh:318-333),
 //           written under out/ of the working directory, plus the registered particle type ids
+//   lattice_save  parallelIO::save(lattice, name, false) (io/multiBlockWriter3D.cpp:53-137, 201-213)
+//           of a lattice with given populations, forces and phase: out/ckpt.plb + out/ckpt.dat
+//           for the default one-block lattice, out/blocks.plb + .dat for the same data on a
+//           lattice of bx x by x bz blocks
+//   lattice_load  parallelIO::load(name, lattice, false) (io/multiBlockReader3D.cpp:135-268) of
+//           in/ckpt.plb into a fresh lattice; dumps its populations, forces and phase
 //
 // Array conventions: lattice fields are (components, nz, ny, nx) with x fastest.
 #define FSI_PROFILE
@@ -868,6 +874,46 @@ static int run_plb(const Bundle& in, const char* out) {
     return 0;
 }
 
+static int run_lattice_save(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    const std::vector<long long> nb = recio::need(in, "blocks").i;
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(1.0, 1.0));
+    lattice.toggleInternalStatistics(false);
+    load_lattice(in, lattice, true);
+    ::mkdir("out", 0777);
+    global::directories().setOutputDir("out/");
+    parallelIO::save(lattice, "ckpt", false);
+    // the same data on a lattice of several blocks, all on this rank
+    SparseBlockStructure3D blocks = createRegularDistribution3D(nx, ny, nz, nb[0], nb[1], nb[2]);
+    ExplicitThreadAttribution* threads = new ExplicitThreadAttribution;
+    for (plint b = 0; b < (plint)(nb[0] * nb[1] * nb[2]); ++b) threads->addBlock(b, 0);
+    MultiBlockLattice3D<T, DESCRIPTOR> multi(MultiBlockManagement3D(blocks, threads, 1),
+                                             defaultMultiBlockPolicy3D().getBlockCommunicator(),
+                                             defaultMultiBlockPolicy3D().getCombinedStatistics(),
+                                             defaultMultiBlockPolicy3D().getMultiCellAccess<T, DESCRIPTOR>(),
+                                             new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(1.0, 1.0));
+    multi.toggleInternalStatistics(false);
+    copy_generic(lattice, lattice.getBoundingBox(), multi, multi.getBoundingBox(), modif::staticVariables);
+    parallelIO::save(multi, "blocks", false);
+    recio::Writer w(out);
+    w.i("nblocks", shp(1), std::vector<long long>(1, (long long)multi.getMultiBlockManagement().getSparseBlockStructure().getBulks().size()));
+    return 0;
+}
+
+static int run_lattice_load(const Bundle& in, const char* out) {
+    const recio::Array& dims = recio::need(in, "dims");
+    const plint nx = dims.i[0], ny = dims.i[1], nz = dims.i[2];
+    Lattice lattice(nx, ny, nz, new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(1.0, 1.0));
+    lattice.toggleInternalStatistics(false);
+    global::directories().setInputDir("in/");
+    parallelIO::load("ckpt", lattice, false);
+    recio::Writer w(out);
+    dump_lattice(w, "loaded", lattice);
+    dump_phase(w, "loaded", lattice);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) {
         std::fprintf(stderr, "usage: ref_harness <lbm|ibm|forces|interp|shape|inertia> in.rec out.rec\n");
@@ -888,6 +934,8 @@ int main(int argc, char** argv) {
     if (c == "ibm_pipe") return run_ibm_pipe(in, argv[3]);
     if (c == "reflect") return run_reflect(in, argv[3]);
     if (c == "plb") return run_plb(in, argv[3]);
+    if (c == "lattice_save") return run_lattice_save(in, argv[3]);
+    if (c == "lattice_load") return run_lattice_load(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

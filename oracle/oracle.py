@@ -564,3 +564,56 @@ def lightweight_text(iteration, rows) -> str:
         vals = list(com) + [g[i, j] / pos.shape[0] for i in range(3) for j in range(i, 3)] + [vol]
         lines.append("%s:%d:" % (tag, pid) + ":".join(_stream_double(float(v)) for v in vals))
     return "\n".join(lines) + "\n"
+
+
+def plb_lattice_files(name, fbar, force, phase, vof=True):
+    """parallelIO::save(lattice, name, false) of a one-block ForcedPhaseD3Q19 lattice
+    (io/multiBlockWriter3D.cpp:53-137, 201-213): (XML spec text, raw .dat bytes).  fbar (19, nz,
+    ny, nx), force (3, nz, ny, nx), phase (nz, ny, nx); cells x-major with z fastest, 23 doubles
+    each (BlockLattice3D::send, blockLattice3D.hh:671-689)."""
+    fbar, force, phase = f64(fbar), f64(force), f64(phase)
+    nz, ny, nx = phase.shape
+    cells = np.concatenate([fbar, force, phase[None]], axis=0)  # (23, nz, ny, nx)
+    dat = np.ascontiguousarray(np.transpose(cells, (3, 2, 1, 0))).astype("<f8").tobytes()
+    box = "0 %d 0 %d 0 %d" % (nx - 1, ny - 1, nz - 1)
+    lines = ['<?xml version="1.0" ?>', "<Block3D>", "    <General>",
+             "        <Family> BlockLattice3D </Family>", "        <Datatype> double </Datatype>",
+             "        <Descriptor> ForcedPhaseD3Q19 </Descriptor>", "        <cellDim> 23 </cellDim>",
+             "        <dynamicContent> False </dynamicContent>", "        <globalId> 0 </globalId>",
+             "    </General>", "    <Structure>", "        <BoundingBox> %s </BoundingBox>" % box,
+             "        <EnvelopeWidth> 1 </EnvelopeWidth>", "        <GridLevel> 0 </GridLevel>",
+             "        <NumComponents> 1 </NumComponents>", "    </Structure>", "    <Data>",
+             "        <File> %s.dat </File>" % name, "        <Component> %s </Component>" % box,
+             "        <Offsets> %d </Offsets>" % len(dat)]
+    if vof:
+        lines += ["        <DynamicsDict>", "            <Guo_VOF_dynamics> 3 </Guo_VOF_dynamics>",
+                  "        </DynamicsDict>"]
+    lines += ["    </Data>", "</Block3D>"]
+    return "\n".join(lines) + "\n", dat
+
+
+def plb_lattice_read(xml: str, dat: bytes):
+    """parallelIO::load's reading of a static-content checkpoint (io/multiBlockReader3D.cpp:135-268)
+    of any block decomposition: (fbar, force, phase) on the whole bounding box; phase is None for
+    22 values per cell (ForcedD3Q19)."""
+    import re
+
+    def leaves(tag):
+        return [m.group(1) for m in re.finditer(r"<%s(?:\s[^>]*)?>(.*?)</%s>" % (tag, tag), xml, re.S)]
+
+    def ints(text):
+        return [int(v) for v in text.split()]
+
+    per = ints(leaves("cellDim")[0])[0]
+    x0, x1, y0, y1, z0, z1 = ints(leaves("BoundingBox")[0])
+    nx, ny, nz = x1 - x0 + 1, y1 - y0 + 1, z1 - z0 + 1
+    cells = np.zeros((nx, ny, nz, per))
+    offsets = ints(leaves("Offsets")[0])
+    start = 0
+    for comp, end in zip(leaves("Component"), offsets):
+        a0, a1, b0, b1, c0, c1 = ints(comp)
+        block = np.frombuffer(dat[start:end], dtype="<f8").reshape(a1 - a0 + 1, b1 - b0 + 1, c1 - c0 + 1, per)
+        cells[a0 - x0:a1 - x0 + 1, b0 - y0:b1 - y0 + 1, c0 - z0:c1 - z0 + 1] = block
+        start = end
+    cells = np.transpose(cells, (3, 2, 1, 0))
+    return cells[:19].copy(), cells[19:22].copy(), (cells[22].copy() if per == 23 else None)

@@ -434,9 +434,41 @@ def case_plb():
     save("plb_particles", inp, out)
 
 
+def case_lattice_plb():
+    """parallelIO::save of a lattice with random populations, forces and phase: the default
+    one-block lattice and the same data on 3 x 2 x 1 blocks (a multi-rank run's layout).  The
+    reference's parallelIO::load reads the oracle's restatement of the one-block files back."""
+    from oracle import oracle as O
+
+    rng = np.random.default_rng(909)
+    nx, ny, nz = 7, 5, 4
+    f = random_state(rng, nx, ny, nz)
+    F = 1e-4 * rng.standard_normal((3, nz, ny, nx))
+    ph = (rng.uniform(size=(nz, ny, nx)) > 0.5).astype(np.float64)
+    inp = dict(dims=np.array([nx, ny, nz]), fbar=f, force=F, phase=ph, blocks=np.array([3, 2, 1]))
+    out = run_with_files("lattice_save", inp, {"file_xml": "out/ckpt.plb", "file_dat": "out/ckpt.dat",
+                                               "file_blocks_xml": "out/blocks.plb", "file_blocks_dat": "out/blocks.dat"})
+    assert int(out["nblocks"][0]) == 6
+    # the reference reads the oracle's files
+    xml, dat = O.plb_lattice_files("ckpt", f, F, ph)
+    with tempfile.TemporaryDirectory() as d:
+        os.makedirs(os.path.join(d, "in"))
+        with open(os.path.join(d, "in", "ckpt.plb"), "w") as fh:
+            fh.write(xml)
+        with open(os.path.join(d, "in", "ckpt.dat"), "wb") as fh:
+            fh.write(dat)
+        fin, fout = os.path.join(d, "in.rec"), os.path.join(d, "out.rec")
+        write_rec(fin, dict(dims=np.array([nx, ny, nz])))
+        subprocess.run([HARNESS, "lattice_load", fin, fout], check=True, cwd=d, stdout=subprocess.DEVNULL)
+        back = read_rec(fout)
+    assert np.array_equal(back["fbar_loaded"], f) and np.array_equal(back["force_loaded"], F)
+    assert np.array_equal(back["phase_loaded"], ph)
+    save("lattice_plb", inp, out)
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
          case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo, case_ibm_pipe,
-         case_reflect, case_plb]
+         case_reflect, case_plb, case_lattice_plb]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):

@@ -1,11 +1,14 @@
-"""The reference's particle files through the C ABI (bib_particles_save_plb / _load_plb,
-bib_particles_write_vtu, bib_particles_write_lightweight).
+"""The reference's own files through the C ABI: particle files (bib_particles_save_plb / _load_plb,
+bib_particles_write_vtu, bib_particles_write_lightweight) and Palabos' lattice checkpoint
+(bib_lattice_save_plb / _load_plb).
 
 The files the reference itself wrote (tests/golden/plb_particles.npz) are loaded into a lattice;
 saving that state again reproduces them byte for byte, and so do the VTU and lightweight outputs
 of the loaded state.  A run's particles survive a save / load through the format exactly; a
 checkpoint split over two rank files (a two-rank reference run) loads by particle id; bad input
-is rejected."""
+is rejected.  The lattice checkpoints the reference wrote (one block, and six blocks as a
+multi-rank run writes them) load exactly; saving reproduces the reference's bytes; a coupled run
+saved in both reference formats and resumed continues bit for bit."""
 import os
 
 import numpy as np
@@ -13,7 +16,7 @@ import pytest
 
 from oracle import oracle as O
 from tests.conftest import golden
-from tests.test_particle_files import TAGS, fixture_particles
+from tests.test_reference_files import TAGS, fixture_particles
 
 pytestmark = pytest.mark.gpu
 
@@ -168,3 +171,106 @@ def test_bad_particle_files_are_rejected(ctx, tmp_path):
     # the failed loads left the lattice's particle as it was
     assert fsi.count_particles() == 1
     assert np.array_equal(fsi.get_particle(0)["pos"], parts[2]["pos"])
+
+
+# ---------------------------------------------------------------- lattice checkpoint (parallelIO)
+def lattice_fixture(ctx, d):
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    return ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=1.0, use_phase=True, omega_inner=0.5)
+
+
+def write_lattice_files(d, folder, which=""):
+    name = "blocks" if which else "ckpt"
+    with open(os.path.join(folder, name + ".plb"), "wb") as f:
+        f.write(bytes(d["out_file_%sxml" % which]))
+    with open(os.path.join(folder, name + ".dat"), "wb") as f:
+        f.write(bytes(d["out_file_%sdat" % which]))
+    return name
+
+
+@pytest.mark.parametrize("which", ["", "blocks_"])
+def test_lattice_checkpoint_of_the_reference_loads_exactly(ctx, tmp_path, which):
+    d = golden("lattice_plb")
+    name = write_lattice_files(d, str(tmp_path), which)
+    lat = lattice_fixture(ctx, d)
+    lat.load_plb(name, folder=str(tmp_path))
+    assert np.array_equal(lat.receive(), d["in_fbar"])
+    assert np.array_equal(lat.get_external_force(), d["in_force"])
+    assert np.array_equal(lat.get_phase(), d["in_phase"])
+
+
+def test_lattice_checkpoint_save_reproduces_the_reference(ctx, tmp_path):
+    d = golden("lattice_plb")
+    write_lattice_files(d, str(tmp_path), "blocks_")
+    lat = lattice_fixture(ctx, d)
+    lat.load_plb("blocks", folder=str(tmp_path))
+    lat.save_plb("ckpt", folder=str(tmp_path / "out"))
+    assert read(tmp_path / "out" / "ckpt.plb") == bytes(d["out_file_xml"])
+    assert read(tmp_path / "out" / "ckpt.dat") == bytes(d["out_file_dat"])
+
+
+def test_lattice_checkpoint_without_phase_keeps_the_phase(ctx, tmp_path):
+    """ForcedD3Q19 checkpoints (22 values per cell) load; the lattice's phase field stays."""
+    d = golden("lattice_plb")
+    xml = bytes(d["out_file_xml"]).decode().replace("ForcedPhaseD3Q19", "ForcedD3Q19").replace(
+        "<cellDim> 23 </cellDim>", "<cellDim> 22 </cellDim>")
+    cells = np.frombuffer(bytes(d["out_file_dat"]), dtype="<f8").reshape(-1, 23)[:, :22]
+    xml = xml.replace("<Offsets> %d </Offsets>" % (cells.shape[0] * 184), "<Offsets> %d </Offsets>" % (cells.shape[0] * 176))
+    (tmp_path / "f22.plb").write_text(xml.replace("ckpt.dat", "f22.dat"))
+    (tmp_path / "f22.dat").write_bytes(np.ascontiguousarray(cells).tobytes())
+    lat = lattice_fixture(ctx, d)
+    phase = 1.0 - d["in_phase"]
+    lat.set_phase(phase)
+    lat.load_plb("f22", folder=str(tmp_path))
+    assert np.array_equal(lat.receive(), d["in_fbar"])
+    assert np.array_equal(lat.get_external_force(), d["in_force"])
+    assert np.array_equal(lat.get_phase(), phase)
+
+
+def test_bad_lattice_checkpoints_are_rejected(ctx, tmp_path):
+    d = golden("lattice_plb")
+    write_lattice_files(d, str(tmp_path))
+    xml = bytes(d["out_file_xml"]).decode()
+    lat = lattice_fixture(ctx, d)
+    before = lat.receive()
+    # another lattice size
+    nx, ny, nz = (int(v) for v in d["in_dims"])
+    other = ctx.add_domain(nx + 1, ny, nz, periodic=(1, 1, 1), omega=1.0)
+    with pytest.raises(bib.BibError):
+        other.load_plb("ckpt", folder=str(tmp_path))
+    # dynamic content, a truncated data file, components that leave cells out, no spec
+    (tmp_path / "dyn.plb").write_text(xml.replace("False", "True").replace("ckpt.dat", "ckpt.dat"))
+    (tmp_path / "cut.plb").write_text(xml.replace("ckpt.dat", "cut.dat"))
+    (tmp_path / "cut.dat").write_bytes(bytes(d["out_file_dat"])[:1000])
+    box = "0 %d 0 %d 0 %d" % (nx - 1, ny - 1, nz - 1)
+    small = "0 %d 0 %d 0 %d" % (nx - 1, ny - 1, nz - 2)
+    (tmp_path / "hole.plb").write_text(xml.replace("<Component> %s </Component>" % box, "<Component> %s </Component>" % small)
+                                       .replace("<Offsets> %d </Offsets>" % (nx * ny * nz * 184),
+                                                "<Offsets> %d </Offsets>" % (nx * ny * (nz - 1) * 184)))
+    for name in ("dyn", "cut", "hole", "missing"):
+        with pytest.raises(bib.BibError):
+            lat.load_plb(name, folder=str(tmp_path))
+    assert np.array_equal(lat.receive(), before)
+
+
+@pytest.mark.parametrize("name", ["ibm_capsule_shear", "ibm_capsule_lambda"])
+def test_run_resumed_from_reference_formats_is_bit_identical(ctx, tmp_path, name):
+    """A coupled FP64 run (deterministic spreading) saved in the reference's two formats, the
+    lattice (parallelIO::save) and the particles (save_checkpoint), and resumed in a fresh lattice
+    continues exactly like the uninterrupted run: finite-difference walls, and a voxelized phase
+    field with viscosity ratio 5."""
+    from tests.test_gpu_parity import run_coupled_gpu
+
+    g = golden(name)
+    lat_a, fsi_a, pa = run_coupled_gpu(ctx, g, spread="deterministic")
+    fsi_a.step(3)
+    lat_a.save_plb("lbm", folder=str(tmp_path))
+    fsi_a.save_particle_checkpoint("fsi", folder=str(tmp_path))
+    fsi_a.step(4)
+    lat_b, fsi_b, pb = run_coupled_gpu(ctx, g, spread="deterministic")
+    lat_b.load_plb("lbm", folder=str(tmp_path))
+    fsi_b.load_particle_checkpoint("fsi", folder=str(tmp_path))
+    fsi_b.step(4)
+    assert np.array_equal(lat_b.receive(), lat_a.receive())
+    assert np.array_equal(fsi_b.get_particle(0)["pos"], fsi_a.get_particle(pa)["pos"])
+    ctx.set_graph_mode(True)

@@ -1,8 +1,10 @@
-"""The reference's particle files, CPU side: the oracle's restatement of the .plb particle
+"""The reference's own files, CPU side: the oracle's restatement of the .plb particle
 checkpoint (save_checkpoint, ImmersedBoundaryDynamics_io.hh:17-73), the VTU particle output
 (ParticleBase3D::write_vtk, ParticleBase.hh:270-390) and the lightweight text output
-(DeformableParticle3D::write_lightweight, DeformableParticle3D.hh:318-333) against the files the
-reference itself wrote (tests/golden/plb_particles.npz), byte for byte."""
+(DeformableParticle3D::write_lightweight, DeformableParticle3D.hh:318-333), and of Palabos'
+static-content lattice checkpoint (parallelIO::save / load, io/multiBlockWriter3D.cpp:53-213,
+io/multiBlockReader3D.cpp:135-268), against the files the reference itself wrote
+(tests/golden/plb_particles.npz, tests/golden/lattice_plb.npz), byte for byte."""
 import numpy as np
 import pytest
 
@@ -79,3 +81,20 @@ def test_plb_pack_rejects_a_model_without_reference_type():
     with pytest.raises(ValueError):
         O.plb_pack(O.MODEL["skalak_bending"], 0, 0, np.zeros((4, 3)), np.zeros((4, 3)), np.zeros((4, 3)),
                    np.zeros(12))
+
+
+# ---------------------------------------------------------------- lattice checkpoint (parallelIO)
+def test_lattice_checkpoint_bytes_match_the_reference():
+    d = golden("lattice_plb")
+    xml, dat = O.plb_lattice_files("ckpt", d["in_fbar"], d["in_force"], d["in_phase"])
+    assert xml.encode() == bytes(d["out_file_xml"])
+    assert dat == bytes(d["out_file_dat"])
+
+
+@pytest.mark.parametrize("which", ["", "blocks_"])
+def test_lattice_checkpoint_read_of_any_block_layout(which):
+    """The one-block file and the 3 x 2 x 1 block file the reference wrote both read back to the
+    lattice's data."""
+    d = golden("lattice_plb")
+    f, F, ph = O.plb_lattice_read(bytes(d["out_file_%sxml" % which]).decode(), bytes(d["out_file_%sdat" % which]))
+    assert np.array_equal(f, d["in_fbar"]) and np.array_equal(F, d["in_force"]) and np.array_equal(ph, d["in_phase"])
