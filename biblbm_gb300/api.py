@@ -285,6 +285,60 @@ class ParticleShapeLibrary:
                     n_triangles=int(out[5]))
 
 
+class RBCShapeInitializer:
+    """RBCShapeInitializer (progs/common/calibrate_rbc_shape.h:147-198): an RBC on a stored shape,
+    its parameters (create_rbc_params), the volume shrink to the discocyte (shrink_rbc_volume, on
+    the GPU) with the minor axis turned onto z, and the result stored as a new shape."""
+
+    def __init__(self, shapes: ParticleShapeLibrary, tag: str):
+        self.shapes = shapes
+        self.ctx = shapes.ctx
+        self.shape = shapes.get_by_tag(tag)
+        xyz, tri = shapes.meshes[self.shape]
+        self.pos = np.array(xyz, dtype=np.float64)
+        self.tri = tri
+        self.params = np.zeros(12)
+        self.damping = None
+
+    def compute_rbc_parameters(self, shear_modulus, k_area, k_bend):
+        self.ctx.check(self.ctx.lib.bib_rbc_params(self.ctx.h, self.shape, float(shear_modulus), float(k_area),
+                                                   float(k_bend), _d(self.params)))
+        return self.params
+
+    def shrink_volume(self, vol_frac, n_it, damping=1.e-2):
+        """shrink_rbc_volume to vol_frac of the shape's volume, then the minor axis onto z and
+        vol_desired = the shrunk volume."""
+        vol0 = self.shapes.info(self.shape)["volume"]
+        out = np.empty_like(self.pos)
+        used = C.c_double()
+        self.ctx.check(self.ctx.lib.bib_rbc_shrink_volume(self.ctx.h, self.shape, _d(self.params),
+                                                          float(vol_frac) * vol0, int(n_it), float(damping), _d(out),
+                                                          C.byref(used)))
+        z = np.array([0.0, 0.0, 1.0])
+        self.ctx.check(self.ctx.lib.bib_align_minor_axis(self.ctx.h, self.shape, _d(out), _d(z)))
+        self.pos = out
+        self.damping = used.value
+        # the volume of the relaxed shape, as DeformableParticle3D::update computes it
+        self.params[PARAM_KEYS.index("vol_desired")] = _volume(out, self.tri)
+        return out
+
+    def store_shape(self, tag: str) -> int:
+        """ParticleBase3D::store_shape (ParticleBase.hh:197-212): the current vertices as a new shape."""
+        return self.shapes.store_mesh(self.pos, self.tri, tag)
+
+
+def _volume(pos, tri) -> float:
+    """Signed volume of a closed triangulation, sum over triangles of v0 . (v1 x v2) / 6 in order."""
+    v = 0.0
+    for t in np.asarray(tri):
+        a, b, c = pos[t[0]], pos[t[1]], pos[t[2]]
+        cx = b[1] * c[2] - b[2] * c[1]
+        cy = b[2] * c[0] - b[0] * c[2]
+        cz = b[0] * c[1] - b[1] * c[0]
+        v += (a[0] * cx + a[1] * cy + a[2] * cz) / 6.
+    return v
+
+
 def MorsePotential(r_min, beta, strength) -> Potential:
     """fsi/Potentials.h MorsePotential: 2 beta strength x (x - 1), x = exp(beta (r_min - d)), d <= r_min."""
     return Potential(1, 0, float(r_min), float(beta), float(strength))

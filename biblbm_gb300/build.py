@@ -33,7 +33,7 @@ def sources():
 
 
 def _flags(extra=()):
-    return [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3", "-I", os.path.join(ROOT, "include"),
+    return [*ARCH, "-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC,-O3,-ffp-contract=off", "-I", os.path.join(ROOT, "include"),
             "-I", CSRC, *extra]
 
 

@@ -2653,3 +2653,226 @@ bib_status bib_lattice_load_plb(bib_ctx* c, int32_t h, const char* dir, const ch
 }
 
 }  // extern "C"
+
+// ---- RBC shape calibration (progs/common/calibrate_rbc_shape.h) ----
+namespace {
+
+// Eigen decomposition of a symmetric 3x3 matrix by cyclic Jacobi rotations (the Jacobi method as
+// published by J. Kopp, "Efficient numerical diagonalization of hermitian 3x3 matrices", 2008,
+// which linalg::diagonalize, fsi/linalg.h:21-138, also follows): eigenvalues w, eigenvectors as
+// the columns of Q.  Reads the diagonal and the upper triangle of A and destroys the latter.
+void jacobi3(double A[3][3], double Q[3][3], double w[3]) {
+    for (int i = 0; i < 3; ++i)
+        for (int j = 0; j < 3; ++j) Q[i][j] = i == j ? 1.0 : 0.0;
+    for (int i = 0; i < 3; ++i) w[i] = A[i][i];
+    for (int sweep = 0; sweep < 50; ++sweep) {
+        double off = 0.0;
+        for (int p = 0; p < 3; ++p)
+            for (int q = p + 1; q < 3; ++q) off += std::fabs(A[p][q]);
+        if (off == 0.0) return;
+        const double thresh = sweep < 4 ? 0.2 * off / 9.0 : 0.0;
+        for (int p = 0; p < 3; ++p)
+            for (int q = p + 1; q < 3; ++q) {
+                const double g = 100.0 * std::fabs(A[p][q]);
+                if (sweep > 4 && std::fabs(w[p]) + g == std::fabs(w[p]) && std::fabs(w[q]) + g == std::fabs(w[q])) {
+                    A[p][q] = 0.0;
+                    continue;
+                }
+                if (!(std::fabs(A[p][q]) > thresh)) continue;
+                const double h = w[q] - w[p];
+                double t;
+                if (std::fabs(h) + g == std::fabs(h)) {
+                    t = A[p][q] / h;
+                } else {
+                    const double theta = 0.5 * h / A[p][q];
+                    t = theta < 0.0 ? -1.0 / (std::sqrt(1.0 + theta * theta) - theta)
+                                    : 1.0 / (std::sqrt(1.0 + theta * theta) + theta);
+                }
+                const double cs = 1.0 / std::sqrt(1.0 + t * t), sn = t * cs, z = t * A[p][q];
+                A[p][q] = 0.0;
+                w[p] -= z;
+                w[q] += z;
+                // rotate the remaining upper-triangle entries and the eigenvector columns p, q
+                auto upper = [&](int a, int b) -> double& { return a < b ? A[a][b] : A[b][a]; };
+                for (int r = 0; r < 3; ++r) {
+                    if (r == p || r == q) continue;
+                    const double ap = upper(r, p), aq = upper(r, q);
+                    upper(r, p) = cs * ap - sn * aq;
+                    upper(r, q) = sn * ap + cs * aq;
+                }
+                for (int r = 0; r < 3; ++r) {
+                    const double qp = Q[r][p], qq = Q[r][q];
+                    Q[r][p] = cs * qp - sn * qq;
+                    Q[r][q] = sn * qp + cs * qq;
+                }
+            }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+bib_status bib_rbc_params(bib_ctx* c, int32_t shape, double shear_modulus, double k_area, double k_bend, double* prm) {
+    if (!c || !prm || shape < 0 || shape >= (int32_t)c->shapes.size()) return fail(c, BIB_EINVAL, "invalid shape or output");
+    const ShapeHost& S = *c->shapes[shape];
+    if (S.link_len.empty()) return fail(c, BIB_EINVAL, "shape has no links");
+    double lavg = 0.0;  // average link length
+    for (double l : S.link_len) lavg += l;
+    lavg /= (double)S.link_len.size();
+    for (int k = 0; k < BIB_P_COUNT; ++k) prm[k] = 0.0;
+    prm[BIB_P_SHEAR_MODULUS] = shear_modulus;
+    prm[BIB_P_L0] = lavg;
+    prm[BIB_P_VOL_DESIRED] = S.volume;
+    // area constraints: the bulk modulus K = 2 G + k_area_global + k_area_local is k_area
+    const double dk = k_area - 2 * shear_modulus;
+    prm[BIB_P_K_AREA_GLOBAL] = dk * 0.8;
+    prm[BIB_P_K_AREA_LOCAL] = dk * 0.2;
+    // radius of the smallest sphere around the origin holding the rest vertices
+    // (ParticleShape::compute_bounding_volumes, ParticleShape.hh:361-383)
+    double r2 = 0.0;
+    const size_t nv = S.rest.size() / 3;
+    for (size_t i = 0; i < nv; ++i) {
+        const double d2 = S.rest[3 * i] * S.rest[3 * i] + S.rest[3 * i + 1] * S.rest[3 * i + 1] +
+                          S.rest[3 * i + 2] * S.rest[3 * i + 2];
+        if (d2 > r2) r2 = d2;
+    }
+    prm[BIB_P_K_VOLUME] = 1000. * shear_modulus / std::sqrt(r2);
+    prm[BIB_P_K_BEND] = k_bend;
+    // spontaneous angle of a closed triangulation of nv vertices
+    const double a = std::sqrt(3.) * ((double)nv - 2.);
+    prm[BIB_P_THETA0] = std::acos((a - 5 * M_PI) / (a - 3. * M_PI));
+    return BIB_OK;
+}
+
+bib_status bib_rbc_shrink_volume(bib_ctx* c, int32_t shape, const double* params, double vol_final, int64_t n_it,
+                                 double damping, double* pos_out, double* damping_out) {
+    if (!c || !params || !pos_out || shape < 0 || shape >= (int32_t)c->shapes.size())
+        return fail(c, BIB_EINVAL, "invalid shape or argument");
+    if (n_it < 1 || n_it > ((int64_t)1 << 40) || !(damping > 0) || !std::isfinite(damping) || !(vol_final > 0) ||
+        !std::isfinite(vol_final) || !(params[BIB_P_VOL_DESIRED] != 0))
+        return fail(c, BIB_EINVAL, "need n_it >= 1, damping > 0, vol_final > 0, vol_desired != 0");
+    const ShapeHost& S = *c->shapes[shape];
+    const int nv = (int)(S.rest.size() / 3);
+    // a holder of the one particle: no lattice buffers, no periodic remap
+    Lattice L;
+    L.d.nx = L.d.ny = L.d.nz = 1;
+    L.d.n = 1;
+    L.d.stride = 128;
+    L.storage = BIB_STORAGE_F64;
+    L.ib = IbDesc{BIB_DIRAC_ROMA, BIB_SPREAD_ATOMIC, -1.0};
+    ParticleHost ph;
+    ph.shape = shape;
+    ph.model = BIB_MODEL_RBC_WLCPOW;
+    ph.v0 = 0;
+    ph.nv = nv;
+    ph.prm.assign(params, params + BIB_P_COUNT);
+    L.parts.push_back(ph);
+    long long* iter = nullptr;
+    BIB_CUDA(c, cudaMalloc((void**)&iter, sizeof(long long)));
+    bib_status st = BIB_OK;
+    cudaStream_t s = c->stream;
+    for (int attempt = 0;; ++attempt) {
+        if (attempt == 64) {
+            st = fail(c, BIB_ENAN, "the relaxation diverged up to damping %g", damping);
+            break;
+        }
+        // the particle as constructed on the shape: rest positions, the shape's area and volume,
+        // zero velocities, then its forces (calibrate_rbc_shape.h:20)
+        double st5[STATS];
+        particle_update(S, S.rest.data(), st5);
+        st5[0] = S.area;
+        st5[1] = S.volume;
+        L.host_pos = S.rest;
+        L.host_stats.assign(st5, st5 + STATS);
+        L.particles_dirty = true;
+        if ((st = sync_particles(c, L))) break;
+        if (cudaMemsetAsync(iter, 0, sizeof(long long), s) != cudaSuccess) {
+            st = fail(c, BIB_ECUDA, "memset failed");
+            break;
+        }
+        launch_membrane_forces(L, s);
+        bool diverged = false;
+        for (int64_t it = 0; it <= 2 * n_it; ++it) {
+            launch_rbc_relax(L, damping, iter, n_it, S.volume, vol_final, s);
+            launch_particle_update(L, s);
+            L.pcur = 1 - L.pcur;
+            launch_membrane_forces(L, s);
+            if ((it & 255) == 255 || it == 2 * n_it) {  // NaN persists: checking a chunk's end is enough
+                double area = 0;
+                if (cudaMemcpyAsync(&area, L.stats, sizeof(double), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+                    cudaStreamSynchronize(s) != cudaSuccess) {
+                    st = fail(c, BIB_ECUDA, "calibration step failed: %s", cudaGetErrorString(cudaGetLastError()));
+                    break;
+                }
+                if (area != area) {
+                    diverged = true;
+                    break;
+                }
+            }
+        }
+        if (st) break;
+        if (!diverged) {
+            if (cudaMemcpy(pos_out, L.pos[L.pcur], 3 * (size_t)nv * sizeof(double), cudaMemcpyDeviceToHost) != cudaSuccess)
+                st = fail(c, BIB_ECUDA, "download failed");
+            break;
+        }
+        damping *= 2.;
+    }
+    free_particles(L);
+    cudaFree(iter);
+    if (!st && damping_out) *damping_out = damping;
+    return st;
+}
+
+bib_status bib_align_minor_axis(bib_ctx* c, int32_t shape, double* pos, const double* dir) {
+    if (!c || !pos || !dir || shape < 0 || shape >= (int32_t)c->shapes.size())
+        return fail(c, BIB_EINVAL, "invalid shape or argument");
+    const ShapeHost& S = *c->shapes[shape];
+    const int nv = (int)(S.rest.size() / 3);
+    double st[STATS];
+    particle_update(S, pos, st);
+    const double* com = st + 2;
+    // tensor of gyration (DeformableParticle3D.hh:111-125)
+    double A[3][3] = {{0, 0, 0}, {0, 0, 0}, {0, 0, 0}};
+    for (int v = 0; v < nv; ++v)
+        for (int i = 0; i < 3; ++i)
+            for (int j = i; j < 3; ++j) A[i][j] += (pos[3 * v + i] - com[i]) * (pos[3 * v + j] - com[j]);
+    for (int i = 0; i < 3; ++i)
+        for (int j = i; j < 3; ++j) A[i][j] /= nv;
+    double Q[3][3], w[3];
+    jacobi3(A, Q, w);
+    // minor axis: the eigenvector of the smallest |eigenvalue| (DeformableParticle3D.hh:85-99)
+    const double a0 = std::fabs(w[0]), a1 = std::fabs(w[1]), a2 = std::fabs(w[2]);
+    const int k = (a0 < a1 && a0 < a2) ? 0 : (a1 < a2) ? 1 : 2;
+    double d[3] = {Q[0][k], Q[1][k], Q[2][k]};
+    const double dn = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+    for (double& x : d) x /= dn;
+    // rotate_to_align_vectors (DeformableParticle3D.hh:128-144) about the centre of mass
+    double ax[3] = {d[1] * dir[2] - d[2] * dir[1], d[2] * dir[0] - d[0] * dir[2], d[0] * dir[1] - d[1] * dir[0]};
+    const double an = std::sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2]);
+    const double pn = std::sqrt(dir[0] * dir[0] + dir[1] * dir[1] + dir[2] * dir[2]);
+    if (!(pn > 0)) return fail(c, BIB_EINVAL, "zero direction");
+    if (an == 0.0) return BIB_OK;  // already aligned (the reference divides by zero here)
+    const double angle = std::asin(an / (std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) * pn));
+    for (double& x : ax) x /= an;
+    if (dir[0] * d[0] + dir[1] * d[1] + dir[2] * d[2] < 0)
+        for (double& x : ax) x = -x;
+    const double sh = std::sin(angle / 2), q0 = std::cos(angle / 2), q1 = sh * ax[0], q2 = sh * ax[1], q3 = sh * ax[2];
+    const double R[3][3] = {{1 - 2 * (q2 * q2 + q3 * q3), 2 * (q1 * q2 - q0 * q3), 2 * (q0 * q2 + q1 * q3)},
+                            {2 * (q1 * q2 + q0 * q3), 1 - 2 * (q1 * q1 + q3 * q3), 2 * (q2 * q3 - q0 * q1)},
+                            {2 * (q1 * q3 - q0 * q2), 2 * (q0 * q1 + q2 * q3), 1 - 2 * (q1 * q1 + q2 * q2)}};
+    // Transform: translate(-com), rotate(R), translate(com), applied as a 3 x 4 affine map
+    double m[3][4];
+    for (int i = 0; i < 3; ++i) {
+        for (int j = 0; j < 3; ++j) m[i][j] = R[i][j];
+        m[i][3] = R[i][0] * -com[0] + R[i][1] * -com[1] + R[i][2] * -com[2] + com[i];
+    }
+    for (int v = 0; v < nv; ++v) {
+        const double x = pos[3 * v], y = pos[3 * v + 1], z = pos[3 * v + 2];
+        for (int i = 0; i < 3; ++i) pos[3 * v + i] = x * m[i][0] + y * m[i][1] + z * m[i][2] + m[i][3];
+    }
+    return BIB_OK;
+}
+
+}  // extern "C"

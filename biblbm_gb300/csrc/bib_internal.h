@@ -293,6 +293,9 @@ void launch_particle_update(const Lattice& L, cudaStream_t s);   // area/volume/
 // particle-particle interaction forces at pos[pcur] added to the vertex forces (no-op without)
 void launch_pp_forces(const Lattice& L, cudaStream_t s);
 size_t pp_sort_temp_bytes(int nvert, int bits);
+// one relax_nodes iteration of the shape calibration of the single RBC of L (pos[pcur] -> pos[1-pcur])
+void launch_rbc_relax(const Lattice& L, double damping, long long* iter, long long n_it, double vol_start,
+                      double vol_final, cudaStream_t s);
 constexpr int kVoxelCap = 64;  // membrane crossings one (x, y) column can hold
 void launch_voxelize(const Lattice& L, const double* pos, cudaStream_t s);  // phase field of the membranes at pos
 size_t membrane_smem_bytes(int max_nv);

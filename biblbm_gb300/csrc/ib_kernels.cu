@@ -1621,4 +1621,57 @@ void launch_voxelize(const Lattice& L, const double* pos, cudaStream_t s) {
     k_voxel_fill<<<(unsigned)((ncol + 127) / 128), 128, 0, s>>>(L.d, L.vox_count, L.vox_z, kVoxelCap, L.phase);
 }
 
+// ---- RBC shape calibration: RBCParticle::relax_nodes (RBCParticle.hh:318-342) ----
+// One iteration of shrink_rbc_volume (progs/common/calibrate_rbc_shape.h:25-33) for the single
+// particle of L: vol_desired of iteration it (while it <= n_it) into the particle's parameters,
+// node masses M_i = sum over the triangles at i (in triangle order) of area/3, vel += force/M -
+// damping vel, pos_next = pos + vel.  The forces of pos_next are computed by the membrane
+// kernel afterwards, with the new vol_desired.  Operations are rounded one by one (no
+// contraction) in the reference's order.  One block; *iter counts the iterations.
+__global__ void __launch_bounds__(256) k_rbc_relax(ParticleDev* P, const double* __restrict__ pos,
+                                                   double* __restrict__ pos_next, double* __restrict__ vel,
+                                                   const double* __restrict__ force, int nv, double damping,
+                                                   long long* iter, long long n_it, double vol_start, double vol_final) {
+    const long long it = *iter;
+    const ParticleDev& p = *P;
+    for (int i = threadIdx.x; i < nv; i += blockDim.x) {
+        double M = 0.0;
+        for (int e = p.inc_off[i]; e < p.inc_off[i + 1]; ++e) {
+            const int code = p.inc[e];
+            if ((code >> 29) != 1) continue;  // triangles only
+            const int t = code & ((1 << 29) - 1);
+            const int i0 = p.tri[3 * t], i1 = p.tri[3 * t + 1], i2 = p.tri[3 * t + 2];
+            const double ax = pos[3 * i0], ay = pos[3 * i0 + 1], az = pos[3 * i0 + 2];
+            const double ux = __dsub_rn(pos[3 * i1], ax), uy = __dsub_rn(pos[3 * i1 + 1], ay),
+                         uz = __dsub_rn(pos[3 * i1 + 2], az);
+            const double wx = __dsub_rn(pos[3 * i2], ax), wy = __dsub_rn(pos[3 * i2 + 1], ay),
+                         wz = __dsub_rn(pos[3 * i2 + 2], az);
+            const double cx = __dsub_rn(__dmul_rn(uy, wz), __dmul_rn(uz, wy));
+            const double cy = __dsub_rn(__dmul_rn(uz, wx), __dmul_rn(ux, wz));
+            const double cz = __dsub_rn(__dmul_rn(ux, wy), __dmul_rn(uy, wx));
+            const double n2 = __dadd_rn(__dadd_rn(__dmul_rn(cx, cx), __dmul_rn(cy, cy)), __dmul_rn(cz, cz));
+            M = __dadd_rn(M, __ddiv_rn(__dmul_rn(0.5, __dsqrt_rn(n2)), 3.0));
+        }
+        for (int k = 0; k < 3; ++k) {
+            const double v = vel[3 * i + k];
+            const double nvk = __dadd_rn(v, __dsub_rn(__ddiv_rn(force[3 * i + k], M), __dmul_rn(damping, v)));
+            vel[3 * i + k] = nvk;
+            pos_next[3 * i + k] = __dadd_rn(pos[3 * i + k], nvk);
+        }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        if (it <= n_it)
+            P->prm[BIB_P_VOL_DESIRED] =
+                __dadd_rn(vol_start, __dmul_rn(__ddiv_rn((double)it, (double)n_it), __dsub_rn(vol_final, vol_start)));
+        *iter = it + 1;
+    }
+}
+
+void launch_rbc_relax(const Lattice& L, double damping, long long* iter, long long n_it, double vol_start,
+                      double vol_final, cudaStream_t s) {
+    k_rbc_relax<<<1, 256, 0, s>>>(L.pdev, L.pos[L.pcur], L.pos[1 - L.pcur], L.vel, L.force, L.nvert, damping, iter,
+                                   n_it, vol_start, vol_final);
+}
+
 }  // namespace bib

@@ -192,6 +192,24 @@ bib_status bib_shape_info(bib_ctx* ctx, int32_t shape, double* out);
 /* the shape's tag (ParticleShape::get_tag, ParticleShape.h:64), written by the lightweight output */
 bib_status bib_shape_set_tag(bib_ctx* ctx, int32_t shape, const char* tag);
 
+/* ---- RBC shape calibration (progs/common/calibrate_rbc_shape.h) ----
+ * bib_rbc_params: create_rbc_params (:72-110) for an RBC on `shape`: L0 = mean link length,
+ * vol_desired = the shape's volume, k_area_global / k_area_local = 0.8 / 0.2 of (k_area - 2 G),
+ * k_volume = 1000 G / (radius of the rest vertices around the origin), k_bend, theta0 of a closed
+ * triangulation; prm receives BIB_P_COUNT values (capsule entries 0).
+ * bib_rbc_shrink_volume: shrink_rbc_volume (:12-69) on the GPU: an RBC on `shape` (its rest
+ * vertices) with `params` relaxes by RBCParticle::relax_nodes (RBCParticle.hh:318-342) for
+ * 2 n_it + 1 iterations while vol_desired ramps from the shape's volume to vol_final over the first
+ * n_it; a relaxation whose area turns NaN restarts with the damping doubled (at most 64 times,
+ * then BIB_ENAN).  pos_out receives 3 nv doubles, damping_out (optional) the damping used.
+ * bib_align_minor_axis: DeformableParticle3D::set_minor_axis_orientation (DeformableParticle3D.hh:
+ * 85-144) of the vertices pos (3 nv, in place) of a particle on `shape`: the eigenvector of the
+ * tensor of gyration with the smallest eigenvalue is rotated onto dir about the centre of mass. */
+bib_status bib_rbc_params(bib_ctx* ctx, int32_t shape, double shear_modulus, double k_area, double k_bend, double* prm);
+bib_status bib_rbc_shrink_volume(bib_ctx* ctx, int32_t shape, const double* params, double vol_final, int64_t n_it,
+                                 double damping, double* pos_out, double* damping_out);
+bib_status bib_align_minor_axis(bib_ctx* ctx, int32_t shape, double* pos, const double* dir);
+
 /* ---- immersed boundary: ImmersedBoundaryDynamics3D ---- */
 bib_status bib_ib_configure(bib_ctx* ctx, int32_t h, const bib_ib_params* p);
 /* ImmersedBoundaryDynamics3D::set_boundary with a PipeBoundary along x through (y0, z0): vertices

@@ -1840,3 +1840,71 @@ void orc_sys_get_particle(orc_sys* s, int32_t pid, double* pos, double* vel, dou
 }
 
 void orc_sys_velocity(orc_sys* s, double* u) { orc_compute_velocity(&s->L, s->f, s->F, u); }
+
+/* ------------------------------------------------------------------ RBC shape calibration */
+/* shrink_rbc_volume (progs/common/calibrate_rbc_shape.h:12-69) of an RBCParticle built on a shape
+ * (positions = the shape's vertices, area / volume = the shape's, zero velocities): the forces
+ * are computed once, then each iteration it = 0 .. 2 n_it sets vol_desired = V0 + it/n_it
+ * (vol_final - V0) while it <= n_it and runs RBCParticle::relax_nodes (RBCParticle.hh:318-342):
+ * node masses M_i = sum over the triangles at i of area/3 (in triangle order), vel += force/M -
+ * damping vel, pos += vel, update (area, volume), forces of the new positions.  An area that
+ * turns NaN restarts the whole relaxation with the damping doubled (64 times at most, then -1
+ * is returned: the reference would retry forever).  Returns the damping used;
+ * pos (3 nv) receives the relaxed vertices, vel (3 nv, optional) their velocities. */
+double orc_rbc_shrink_volume(const double* prm_in, int64_t nv, const double* rest, int64_t nt, const int64_t* tri,
+                             const double* tri_area, double A0, double V0, int64_t nl, const int64_t* links,
+                             const double* link_len, int64_t np, const int64_t* pairs, const double* pair_cs,
+                             double vol_final, int64_t n_it, double damping, double* pos, double* vel_out) {
+    double* F0 = (double*)calloc(3 * nv, sizeof(double));
+    double* F = (double*)malloc(sizeof(double) * 3 * nv);
+    double* vel = (double*)malloc(sizeof(double) * 3 * nv);
+    double* M = (double*)malloc(sizeof(double) * nv);
+    double prm[ORC_P_COUNT];
+    orc_membrane_forces(ORC_MODEL_RBC_WLCPOW, prm_in, nv, rest, nt, tri, tri_area, A0, nl, links, link_len, np, pairs,
+                        pair_cs, rest, A0, V0, F0);
+    for (int attempt = 0;; ++attempt) {
+        if (attempt == 64) { /* the reference retries forever; this restatement gives up like the product */
+            damping = -1.0;
+            break;
+        }
+        memcpy(pos, rest, sizeof(double) * 3 * nv);
+        memcpy(F, F0, sizeof(double) * 3 * nv);
+        memset(vel, 0, sizeof(double) * 3 * nv);
+        memcpy(prm, prm_in, sizeof(prm));
+        int success = 1;
+        for (int64_t it = 0;; ++it) {
+            if (it <= n_it) prm[ORC_P_VOL_DESIRED] = V0 + ((double)it / (double)n_it) * (vol_final - V0);
+            for (int64_t i = 0; i < nv; ++i) M[i] = 0.0;
+            for (int64_t t = 0; t < nt; ++t) {
+                const int64_t i0 = tri[3 * t], i1 = tri[3 * t + 1], i2 = tri[3 * t + 2];
+                const v3 a = ld(pos + 3 * i0);
+                const double la = 0.5 * nrm(crs(sub(ld(pos + 3 * i1), a), sub(ld(pos + 3 * i2), a)));
+                M[i0] += la / 3.;
+                M[i1] += la / 3.;
+                M[i2] += la / 3.;
+            }
+            for (int64_t i = 0; i < nv; ++i)
+                for (int k = 0; k < 3; ++k) {
+                    vel[3 * i + k] += F[3 * i + k] / M[i] - damping * vel[3 * i + k];
+                    pos[3 * i + k] += vel[3 * i + k];
+                }
+            double st[5];
+            orc_particle_update(nv, pos, nt, tri, st);
+            orc_membrane_forces(ORC_MODEL_RBC_WLCPOW, prm, nv, rest, nt, tri, tri_area, A0, nl, links, link_len, np,
+                                pairs, pair_cs, pos, st[0], st[1], F);
+            if (st[0] != st[0]) {
+                damping *= 2.;
+                success = 0;
+                break;
+            }
+            if (it == 2 * n_it) break;
+        }
+        if (success) break;
+    }
+    if (vel_out) memcpy(vel_out, vel, sizeof(double) * 3 * nv);
+    free(F0);
+    free(F);
+    free(vel);
+    free(M);
+    return damping;
+}

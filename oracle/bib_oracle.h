@@ -90,6 +90,11 @@ void orc_membrane_forces(int32_t model, const double* prm, int64_t nv, const dou
                          const double* link_len, int64_t np, const int64_t* pairs, const double* pair_cs,
                          const double* pos, double area, double volume, double* force);
 
+double orc_rbc_shrink_volume(const double* prm_in, int64_t nv, const double* rest, int64_t nt, const int64_t* tri,
+                             const double* tri_area, double A0, double V0, int64_t nl, const int64_t* links,
+                             const double* link_len, int64_t np, const int64_t* pairs, const double* pair_cs,
+                             double vol_final, int64_t n_it, double damping, double* pos, double* vel_out);
+
 /* ---- immersed boundary ---- */
 double orc_dirac(int32_t dirac, double r);
 void orc_classify(const orc_lattice* L, int32_t dirac, int64_t n, const double* pos, int32_t* cls);

@@ -36,6 +36,10 @@
 //           of a lattice with given populations, forces and phase: out/ckpt.plb + out/ckpt.dat
 //           for the default one-block lattice, out/blocks.plb + .dat for the same data on a
 //           lattice of bx x by x bz blocks
+//   calibrate  the RBC shape calibration of progs/common/calibrate_rbc_shape.h: create_rbc_params
+//           (:72-110) on a shape, shrink_rbc_volume (:12-69) to a volume fraction, then
+//           set_minor_axis_orientation onto z (DeformableParticle3D.hh:85-144) as
+//           RBCShapeInitializer::shrink_volume (:180-185) does
 //   lattice_load  parallelIO::load(name, lattice, false) (io/multiBlockReader3D.cpp:135-268) of
 //           in/ckpt.plb into a fresh lattice; dumps its populations, forces and phase
 //
@@ -47,6 +51,7 @@
 #include "fsi/headers.hh"
 #include "fsi/GuoBoundaryCondition.h"
 #include "fsi/GuoBoundaryCondition.hh"
+#include "calibrate_rbc_shape.h"
 
 #include <string>
 #include <vector>
@@ -914,6 +919,36 @@ static int run_lattice_load(const Bundle& in, const char* out) {
     return 0;
 }
 
+static int run_calibrate(const Bundle& in, const char* out) {
+    ParticleShapeLibrary<T> lib;
+    store_shape(in, lib, "rest");
+    const ParticleShapeLibrary<T>& clib = lib;
+    const ParticleShape<T>* shape = clib.get_by_id(0);
+    const std::vector<double> k = recio::need(in, "moduli").d;  // shear modulus, K_area, K_bend
+    RBCParameters<T> prm = create_rbc_params(shape, (T)k[0], (T)k[1], (T)k[2]);
+    RBCParticle<T> rbc(shape, prm);
+    const T vol_final = recio::num(in, "vol_frac") * shape->get_volume();
+    shrink_rbc_volume(rbc, vol_final, (int)recio::inum(in, "n_it"), (T)1, (T)recio::num(in, "damping"));
+    const plint nv = rbc.count_nodes();
+    std::vector<double> shrunk(3 * nv), aligned(3 * nv);
+    for (plint i = 0; i < nv; ++i)
+        for (int d = 0; d < 3; ++d) shrunk[3 * i + d] = rbc.get_node(i).pos[d];
+    rbc.set_minor_axis_orientation(Array<T, 3>(0, 0, 1));
+    rbc.params().vol_desired = rbc.volume();
+    for (plint i = 0; i < nv; ++i)
+        for (int d = 0; d < 3; ++d) aligned[3 * i + d] = rbc.get_node(i).pos[d];
+    const RBCParameters<T>& p = prm;
+    double pv[12] = {0, 0, 0, 0, p.shear_modulus, p.L0, p.k_area_global, p.k_area_local, p.k_volume, p.vol_desired,
+                     p.k_bend, p.theta0};
+    recio::Writer w(out);
+    w.d("params", shp(12), std::vector<double>(pv, pv + 12));
+    w.d("shrunk", shp(nv, 3), shrunk);
+    w.d("aligned", shp(nv, 3), aligned);
+    w.d("vol_desired", shp(1), std::vector<double>(1, rbc.params().vol_desired));
+    w.d("area", shp(1), std::vector<double>(1, rbc.area()));
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) {
         std::fprintf(stderr, "usage: ref_harness <lbm|ibm|forces|interp|shape|inertia> in.rec out.rec\n");
@@ -936,6 +971,7 @@ int main(int argc, char** argv) {
     if (c == "plb") return run_plb(in, argv[3]);
     if (c == "lattice_save") return run_lattice_save(in, argv[3]);
     if (c == "lattice_load") return run_lattice_load(in, argv[3]);
+    if (c == "calibrate") return run_calibrate(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

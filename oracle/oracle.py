@@ -79,6 +79,9 @@ def lib():
             "orc_inertia": (None, [dp, C.c_int64, ip, dp]),
             "orc_membrane_forces": (None, [C.c_int32, dp, C.c_int64, dp, C.c_int64, ip, dp, C.c_double, C.c_int64, ip,
                                            dp, C.c_int64, ip, dp, dp, C.c_double, C.c_double, dp]),
+            "orc_rbc_shrink_volume": (C.c_double, [dp, C.c_int64, dp, C.c_int64, ip, dp, C.c_double, C.c_double,
+                                                   C.c_int64, ip, dp, C.c_int64, ip, dp, C.c_double, C.c_int64,
+                                                   C.c_double, dp, dp]),
             "orc_dirac": (C.c_double, [C.c_int32, C.c_double]),
             "orc_threads": (C.c_int32, []),
             "orc_classify": (None, [Lp, C.c_int32, C.c_int64, dp, i32p]),
@@ -617,3 +620,141 @@ def plb_lattice_read(xml: str, dat: bytes):
         start = end
     cells = np.transpose(cells, (3, 2, 1, 0))
     return cells[:19].copy(), cells[19:22].copy(), (cells[22].copy() if per == 23 else None)
+
+
+# ---------------------------------------------------------------- RBC shape calibration
+def rbc_shrink_volume(shape: Shape, prm, vol_final, n_it, damping=1.e-2):
+    """shrink_rbc_volume (progs/common/calibrate_rbc_shape.h:12-69): (relaxed vertices, damping used)."""
+    pos = np.zeros_like(shape.rest)
+    d = lib().orc_rbc_shrink_volume(_d(f64(prm)), shape.rest.shape[0], _d(shape.rest), shape.tri.shape[0], _i(shape.tri),
+                                    _d(shape.tri_area), shape.area, shape.volume, shape.links.shape[0], _i(shape.links),
+                                    _d(shape.link_len), shape.pairs.shape[0], _i(shape.pairs), _d(shape.pair_cs),
+                                    float(vol_final), int(n_it), float(damping), _d(pos), None)
+    return pos, d
+
+
+def rbc_params(shape: Shape, shear_modulus, k_area, k_bend):
+    """create_rbc_params (progs/common/calibrate_rbc_shape.h:72-110) as a BIB_P_* vector."""
+    import math
+
+    lavg = 0.0
+    for l in shape.link_len:
+        lavg += float(l)
+    lavg /= shape.link_len.shape[0]
+    p = dict.fromkeys(PARAM_KEYS, 0.0)
+    p.update(shear_modulus=shear_modulus, L0=lavg, vol_desired=shape.volume)
+    dk = k_area - (2 * shear_modulus + 0.0 + 0.0)  # RBCParameters::K() with both area stiffnesses 0
+    p.update(k_area_global=dk * 0.8, k_area_local=dk * 0.2)
+    r2 = 0.0
+    for x, y, z in shape.rest:
+        d2 = x * x + y * y + z * z
+        if d2 > r2:
+            r2 = d2
+    p["k_volume"] = 1000. * shear_modulus / math.sqrt(r2)
+    p["k_bend"] = k_bend
+    nv = shape.rest.shape[0]
+    p["theta0"] = math.acos((math.sqrt(3.) * (nv - 2.) - 5 * math.pi) / (math.sqrt(3.) * (nv - 2.) - 3. * math.pi))
+    return np.array([p[k] for k in PARAM_KEYS])
+
+
+def _jacobi3(A):
+    """Cyclic Jacobi eigen decomposition of a symmetric 3x3 matrix (J. Kopp, "Efficient numerical
+    diagonalization of hermitian 3x3 matrices", 2008; the method of linalg::diagonalize,
+    fsi/linalg.h:21-138): (eigenvalues, eigenvectors as columns).  Uses the upper triangle."""
+    import math
+
+    A = [list(map(float, r)) for r in A]
+    Q = [[1.0 if i == j else 0.0 for j in range(3)] for i in range(3)]
+    w = [A[i][i] for i in range(3)]
+    for sweep in range(50):
+        so = 0.0
+        for p in range(3):
+            for q in range(p + 1, 3):
+                so += abs(A[p][q])
+        if so == 0.0:
+            break
+        thresh = 0.2 * so / 9 if sweep < 4 else 0.0
+        for p in range(3):
+            for q in range(p + 1, 3):
+                g = 100.0 * abs(A[p][q])
+                if sweep > 4 and abs(w[p]) + g == abs(w[p]) and abs(w[q]) + g == abs(w[q]):
+                    A[p][q] = 0.0
+                    continue
+                if not abs(A[p][q]) > thresh:
+                    continue
+                h = w[q] - w[p]
+                if abs(h) + g == abs(h):
+                    t = A[p][q] / h
+                else:
+                    theta = 0.5 * h / A[p][q]
+                    t = -1.0 / (math.sqrt(1.0 + theta * theta) - theta) if theta < 0.0 else \
+                        1.0 / (math.sqrt(1.0 + theta * theta) + theta)
+                c = 1.0 / math.sqrt(1.0 + t * t)
+                s = t * c
+                z = t * A[p][q]
+                A[p][q] = 0.0
+                w[p] -= z
+                w[q] += z
+                for r in range(p):
+                    t2 = A[r][p]
+                    A[r][p] = c * t2 - s * A[r][q]
+                    A[r][q] = s * t2 + c * A[r][q]
+                for r in range(p + 1, q):
+                    t2 = A[p][r]
+                    A[p][r] = c * t2 - s * A[r][q]
+                    A[r][q] = s * t2 + c * A[r][q]
+                for r in range(q + 1, 3):
+                    t2 = A[p][r]
+                    A[p][r] = c * t2 - s * A[q][r]
+                    A[q][r] = s * t2 + c * A[q][r]
+                for r in range(3):
+                    t2 = Q[r][p]
+                    Q[r][p] = c * t2 - s * Q[r][q]
+                    Q[r][q] = s * t2 + c * Q[r][q]
+    return w, Q
+
+
+def align_minor_axis(pos, tri, pref=(0.0, 0.0, 1.0)):
+    """DeformableParticle3D::set_minor_axis_orientation (DeformableParticle3D.hh:85-144): the
+    eigenvector of the tensor of gyration with the smallest |eigenvalue| rotated onto pref about
+    the centre of mass (Quaternion.h:28-40, 144-155; Transform.hh:36-84)."""
+    import math
+
+    pos = f64(pos).copy()
+    com = particle_update(pos, tri)[2:5]
+    nv = pos.shape[0]
+    A = [[0.0] * 3 for _ in range(3)]
+    for v in range(nv):
+        for i in range(3):
+            for j in range(i, 3):
+                A[i][j] += (pos[v, i] - com[i]) * (pos[v, j] - com[j])
+    for i in range(3):
+        for j in range(i, 3):
+            A[i][j] /= nv
+    w, Q = _jacobi3(A)
+    a = [abs(x) for x in w]
+    k = 0 if (a[0] < a[1] and a[0] < a[2]) else (1 if a[1] < a[2] else 2)
+    d = [Q[0][k], Q[1][k], Q[2][k]]
+    dn = math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2])
+    d = [x / dn for x in d]
+    p = [float(x) for x in pref]
+    ax = [d[1] * p[2] - d[2] * p[1], d[2] * p[0] - d[0] * p[2], d[0] * p[1] - d[1] * p[0]]
+    an = math.sqrt(ax[0] * ax[0] + ax[1] * ax[1] + ax[2] * ax[2])
+    angle = math.asin(an / (math.sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]) *
+                            math.sqrt(p[0] * p[0] + p[1] * p[1] + p[2] * p[2])))
+    ax = [x / an for x in ax]
+    if p[0] * d[0] + p[1] * d[1] + p[2] * d[2] < 0:
+        ax = [-x for x in ax]
+    sh = math.sin(angle / 2)
+    q0, q1, q2, q3 = math.cos(angle / 2), sh * ax[0], sh * ax[1], sh * ax[2]
+    R = [[1 - 2 * (q2 * q2 + q3 * q3), 2 * (q1 * q2 - q0 * q3), 2 * (q0 * q2 + q1 * q3)],
+         [2 * (q1 * q2 + q0 * q3), 1 - 2 * (q1 * q1 + q3 * q3), 2 * (q2 * q3 - q0 * q1)],
+         [2 * (q1 * q3 - q0 * q2), 2 * (q0 * q1 + q2 * q3), 1 - 2 * (q1 * q1 + q2 * q2)]]
+    # Transform::translate(-com).rotate(R).translate(com): columns 0-2 = R, column 3 = R (-com) + com
+    t = [R[i][0] * -com[0] + R[i][1] * -com[1] + R[i][2] * -com[2] + com[i] for i in range(3)]
+    out = np.empty_like(pos)
+    for v in range(nv):
+        x, y, z = pos[v]
+        for i in range(3):
+            out[v, i] = x * R[i][0] + y * R[i][1] + z * R[i][2] + t[i]
+    return out

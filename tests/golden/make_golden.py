@@ -466,9 +466,24 @@ def case_lattice_plb():
     save("lattice_plb", inp, out)
 
 
+def case_calibrate():
+    """RBC shape calibration (progs/common/calibrate_rbc_shape.h): create_rbc_params on a rotated
+    ellipsoid mesh, shrink_rbc_volume to 65 % of its volume (it flattens into a disc), minor axis
+    onto z.  The moduli and damping keep the explicit relaxation contracting, so that rounding
+    differences do not grow over the 801 iterations."""
+    rng = np.random.default_rng(5)
+    xyz, tri = meshes.icosphere(2, 3.9)
+    xyz = (xyz * np.array([1.15, 1.0, 0.85])) @ meshes.random_rotation(rng).T
+    inp = dict(rest=xyz, tri=tri, moduli=np.array([1e-3, 0.1, 4e-4]), vol_frac=0.65, n_it=400, damping=0.05)
+    out = run("calibrate", inp)
+    short = run("calibrate", dict(inp, n_it=5))  # 11 iterations
+    out["short_shrunk"] = short["shrunk"]
+    save("calibrate_rbc", inp, out)
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
          case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo, case_ibm_pipe,
-         case_reflect, case_plb, case_lattice_plb]
+         case_reflect, case_plb, case_lattice_plb, case_calibrate]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
