@@ -308,3 +308,43 @@ def test_capsule_near_pipe_wall():
     assert np.array_equal(S.particle(pid)["pos"], d["out_pos"][-1])
     assert np.array_equal(S.f[:, :, :, [0, 7]], d["out_fbar_end_planes"])
     assert np.array_equal(S.f.sum(axis=(1, 2, 3)), d["out_fbar_end_sum"])
+
+
+def test_bending_force_is_the_gradient_of_the_bending_energy():
+    """progs/bending_angle_test/bending_angle_test.cpp prints the analytic dihedral-angle gradient
+    (tri::grad_angle_between_pair) beside central differences for a human to compare.  Here the
+    comparison is a test: the RBC bending force of a deformed membrane (k_bend alone) equals minus the
+    central-difference gradient of E = sum over pairs k_bend (1 - cos(t) cos(t0) - sin(t) sin(t0)),
+    with cos t, sin t as tri::cos_sin_of_angle_between_pair (TriangleUtils.h:122-136) gives them."""
+    from biblbm_gb300 import meshes
+
+    rng = np.random.default_rng(11)
+    xyz, tri = meshes.evans_fung(1, 4.0)
+    S = O.Shape(xyz, tri)
+    pos = xyz + 0.08 * rng.standard_normal(xyz.shape)
+    kb = 0.05
+    prm = O.params_vector(k_bend=kb, vol_desired=1.0)
+
+    def unit_normal(a, b, c):
+        n = np.cross(b - a, c - a)
+        return n / np.linalg.norm(n)
+
+    def energy(p):
+        e = 0.0
+        for (i0, i1, i2, i3), (c0, s0) in zip(S.pairs, S.pair_cs):
+            n1, n2 = unit_normal(p[i0], p[i1], p[i2]), unit_normal(p[i0], p[i2], p[i3])
+            c = float(n1 @ n2)
+            s = (1.0 if float((n1 - n2) @ (p[i1] - p[i3])) > 0 else -1.0) * float(np.linalg.norm(np.cross(n1, n2)))
+            e += kb * (1 - c * c0 - s * s0)
+        return e
+
+    F = O.membrane_forces("rbc_wlcpow", prm, S, pos)
+    dx = 1e-6
+    fd = np.zeros_like(pos)
+    for i in range(pos.shape[0]):
+        for a in range(3):
+            pp, pm = pos.copy(), pos.copy()
+            pp[i, a] += dx
+            pm[i, a] -= dx
+            fd[i, a] = -(energy(pp) - energy(pm)) / (2 * dx)
+    assert np.abs(F - fd).max() < 1e-6 * np.abs(fd).max()
