@@ -39,6 +39,41 @@ def env_rank():
     return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
 
 
+class Ranks:
+    """The ranks of a torchrun launch: one independent replica of the workload per GPU (the step
+    has no exchange between replicas), a barrier around the timed region and the maximum of the
+    ranks' times.  NCCL on the GPUs; gloo (CPU tensors) where a test runs the ranks on the host."""
+
+    def __init__(self, backend=None):
+        self.rank, self.world, self.local = env_rank()
+        self.dist = None
+        self.device = "cpu"
+        if self.world > 1:
+            import torch
+            import torch.distributed as dist
+
+            backend = backend or "nccl"
+            if backend == "nccl":
+                torch.cuda.set_device(self.local)
+                self.device = "cuda"
+            if not dist.is_initialized():
+                dist.init_process_group(backend)
+            self.dist = dist
+
+    def barrier(self):
+        if self.dist is not None:
+            self.dist.barrier()
+
+    def max(self, v):
+        if self.dist is None:
+            return v
+        import torch
+
+        t = torch.tensor([v], dtype=torch.float64, device=self.device)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+
 class ClockSampler:
     """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
 
@@ -299,28 +334,11 @@ def main():
         run_reference(args, wl)
         return
 
-    rank, world, local = env_rank()
-    dist = None
-    if world > 1:
-        import torch
-        import torch.distributed as dist
-
-        torch.cuda.set_device(local)
-        dist.init_process_group("nccl")
+    ranks = Ranks()
+    rank, world, local = ranks.rank, ranks.world, ranks.local
     import biblbm_gb300 as bib
 
-    def barrier():
-        if dist is not None:
-            dist.barrier()
-
-    def max_over_ranks(v):
-        if dist is None:
-            return v
-        import torch
-
-        t = torch.tensor([v], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+    barrier, max_over_ranks = ranks.barrier, ranks.max
 
     nx, ny, nz = wl["dims"]
     cells = nx * ny * nz
@@ -523,8 +541,8 @@ def main():
         "cpu_baseline": cpu,
     }
     print(json.dumps(line), flush=True)
-    if dist is not None:
-        dist.destroy_process_group()
+    if ranks.dist is not None:
+        ranks.dist.destroy_process_group()
 
 
 if __name__ == "__main__":
