@@ -79,3 +79,24 @@ def test_divergent_calibration_is_an_error(ctx):
     pos = np.empty_like(d["in_rest"])
     st = ctx.lib.bib_rbc_shrink_volume(ctx.h, sid, dp(prm), 0.65 * shapes.info(sid)["volume"], 100, 1e-2, dp(pos), None)
     assert st == -4  # BIB_ENAN after 64 restarts
+
+
+def test_calibration_arguments_are_checked(ctx):
+    d = golden("calibrate_rbc")
+    shapes = bib.ParticleShapeLibrary(ctx)
+    sid = shapes.store_mesh(d["in_rest"], d["in_tri"], "sphere")
+    prm = np.zeros(12)
+    ctx.check(ctx.lib.bib_rbc_params(ctx.h, sid, 1e-3, 0.1, 4e-4, dp(prm)))
+    pos = np.empty_like(d["in_rest"])
+    lib, h = ctx.lib, ctx.h
+    assert lib.bib_rbc_params(h, 999, 1e-3, 0.1, 4e-4, dp(prm)) == -1          # unknown shape
+    assert lib.bib_rbc_shrink_volume(h, sid, dp(prm), 100.0, 0, 0.05, dp(pos), None) == -1      # n_it < 1
+    assert lib.bib_rbc_shrink_volume(h, sid, dp(prm), 100.0, 10, 0.0, dp(pos), None) == -1      # damping <= 0
+    assert lib.bib_rbc_shrink_volume(h, sid, dp(prm), -1.0, 10, 0.05, dp(pos), None) == -1      # vol_final <= 0
+    bad = prm.copy()
+    bad[9] = 0.0
+    assert lib.bib_rbc_shrink_volume(h, sid, dp(bad), 100.0, 10, 0.05, dp(pos), None) == -1     # vol_desired 0
+    assert lib.bib_align_minor_axis(h, sid, dp(pos), dp(np.zeros(3))) == -1                      # zero direction
+    # the context still works
+    ctx.check(lib.bib_rbc_shrink_volume(h, sid, dp(prm), 0.9 * shapes.info(sid)["volume"], 2, 0.05, dp(pos), None))
+    assert np.isfinite(pos).all()
