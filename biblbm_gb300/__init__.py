@@ -6,13 +6,13 @@ The compute path is the CUDA library ``lib/libbib_gb300.so`` behind the C ABI of
 """
 from .api import (COLLISION, DIRAC, MODEL, STORAGE, WALL, Batch, CapsuleParameters, Context,
                   ImmersedBoundaryDynamics3D, Lattice, MorsePotential, ParticleShapeLibrary, RBCParameters,
-                  RBCShapeInitializer,
+                  RBCShapeInitializer, initial_distribution,
                   SpringPotential, lattice_params, membrane_params, taylor_deformation)
 from ._lib import BibError, LIB_PATH
 
 __all__ = [
     "Batch", "BibError", "CapsuleParameters", "COLLISION", "Context", "DIRAC", "ImmersedBoundaryDynamics3D", "Lattice",
     "LIB_PATH", "MODEL", "MorsePotential", "ParticleShapeLibrary", "RBCParameters", "RBCShapeInitializer", "SpringPotential", "STORAGE",
-    "WALL", "lattice_params",
+    "WALL", "initial_distribution", "lattice_params",
     "membrane_params", "taylor_deformation",
 ]

@@ -109,6 +109,8 @@ SIGNATURES = {
     "bib_rbc_params": (C.c_int32, [_vp, C.c_int32, C.c_double, C.c_double, C.c_double, _dp]),
     "bib_rbc_shrink_volume": (C.c_int32, [_vp, C.c_int32, _dp, C.c_double, C.c_int64, C.c_double, _dp, _dp]),
     "bib_align_minor_axis": (C.c_int32, [_vp, C.c_int32, _dp, _dp]),
+    "bib_initial_distribution": (C.c_int32, [C.POINTER(C.c_int64), _dp, C.c_int32, C.POINTER(C.c_int64), _dp,
+                                             C.c_double, C.c_uint32, C.c_int64, _dp, _dp]),
     "bib_lattice_load_plb": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_char_p]),
     "bib_checkpoint_load": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),
     "bib_step": (C.c_int32, [_vp, C.c_int32, C.c_int64]),

@@ -285,6 +285,27 @@ class ParticleShapeLibrary:
                     n_triangles=int(out[5]))
 
 
+def initial_distribution(box, counts, radii, max_radius, seed, pipe=None, max_tries=5_000_000):
+    """The random placement of progs/common/create_particles.h:37-93 (ParticlePositionInitializer
+    and random orientations) with the numbers glibc's rand() gives after srand(seed): counts[t]
+    non-overlapping spheres of radius radii[t] per type in the integer box (x0, x1, y0, y1, z0, z1),
+    inside the pipe (y0, z0, radius) if given.  Returns (positions (n, 3), quaternions (n, 4) as w, x,
+    y, z).  Host code of the CUDA library; no device needed."""
+    lib = _lib.load()
+    box = np.ascontiguousarray(box, dtype=np.int64)
+    counts = np.ascontiguousarray(counts, dtype=np.int64)
+    radii = _f64(radii)
+    n = int(counts.sum())
+    pos, quat = np.zeros((n, 3)), np.zeros((n, 4))
+    pp = None if pipe is None else _f64(pipe)
+    st = lib.bib_initial_distribution(box.ctypes.data_as(C.POINTER(C.c_int64)), _d(pp) if pp is not None else None,
+                                      int(counts.shape[0]), counts.ctypes.data_as(C.POINTER(C.c_int64)), _d(radii),
+                                      float(max_radius), int(seed), int(max_tries), _d(pos), _d(quat))
+    if st != 0:
+        raise BibError(st, "initial_distribution: " + _lib.status_string(st))
+    return pos, quat
+
+
 class RBCShapeInitializer:
     """RBCShapeInitializer (progs/common/calibrate_rbc_shape.h:147-198): an RBC on a stored shape,
     its parameters (create_rbc_params), the volume shrink to the discocyte (shrink_rbc_volume, on

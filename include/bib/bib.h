@@ -210,6 +210,18 @@ bib_status bib_rbc_shrink_volume(bib_ctx* ctx, int32_t shape, const double* para
                                  double damping, double* pos_out, double* damping_out);
 bib_status bib_align_minor_axis(bib_ctx* ctx, int32_t shape, double* pos, const double* dir);
 
+/* ---- random initial placement (progs/common/create_particles.h:37-93 with
+ * ParticlePositionInitializer, src/fsi/ParticlePositionInitializer.hh:17-80), host only ----
+ * counts[t] spheres of radius radii[t] per type t, in type order, at uniform positions in the box
+ * {x0, x1, y0, y1, z0, z1} (integers, shrunk by the radius), inside the pipe {y0, z0, radius} by the
+ * radius when pipe is non-NULL, overlapping no earlier sphere (radii <= max_radius), then one random
+ * orientation quaternion {w, x, y, z} per sphere; drawn from the sequence of glibc's rand() after
+ * srand(seed), so that the reference's driver gets the same numbers.  pos: 3 per sphere, quat: 4.
+ * BIB_EOVERFLOW if a sphere finds no free place within max_tries draws (the reference tries 5e6). */
+bib_status bib_initial_distribution(const int64_t* box, const double* pipe, int32_t ntypes, const int64_t* counts,
+                                    const double* radii, double max_radius, uint32_t seed, int64_t max_tries,
+                                    double* pos, double* quat);
+
 /* ---- immersed boundary: ImmersedBoundaryDynamics3D ---- */
 bib_status bib_ib_configure(bib_ctx* ctx, int32_t h, const bib_ib_params* p);
 /* ImmersedBoundaryDynamics3D::set_boundary with a PipeBoundary along x through (y0, z0): vertices

@@ -40,6 +40,9 @@
 //           (:72-110) on a shape, shrink_rbc_volume (:12-69) to a volume fraction, then
 //           set_minor_axis_orientation onto z (DeformableParticle3D.hh:85-144) as
 //           RBCShapeInitializer::shrink_volume (:180-185) does
+//   initial  the random placement of progs/common/create_particles.h:37-93: srand(seed), then
+//           ParticlePositionInitializer::generate_points per particle type inside a PipeBoundary
+//           and one random orientation quaternion per particle, drawn as the driver draws them
 //   lattice_load  parallelIO::load(name, lattice, false) (io/multiBlockReader3D.cpp:135-268) of
 //           in/ckpt.plb into a fresh lattice; dumps its populations, forces and phase
 //
@@ -52,6 +55,8 @@
 #include "fsi/GuoBoundaryCondition.h"
 #include "fsi/GuoBoundaryCondition.hh"
 #include "calibrate_rbc_shape.h"
+#include "fsi/ParticlePositionInitializer.h"
+#include "fsi/ParticlePositionInitializer.hh"
 
 #include <string>
 #include <vector>
@@ -949,6 +954,40 @@ static int run_calibrate(const Bundle& in, const char* out) {
     return 0;
 }
 
+static int run_initial(const Bundle& in, const char* out) {
+    const std::vector<long long> b = recio::need(in, "box").i;
+    const std::vector<double> pp = recio::need(in, "pipe").d;  // y0, z0, radius
+    const std::vector<long long> counts = recio::need(in, "counts").i;
+    const std::vector<double> radii = recio::need(in, "radii").d;
+    const T max_radius = recio::num(in, "max_radius");
+    std::srand((unsigned)recio::inum(in, "seed"));
+    PipeBoundary<T> pipe(pp[0], pp[1], pp[2], (T)(b[1] - b[0]));
+    ParticlePositionInitializer<T> init(Box3D(b[0], b[1], b[2], b[3], b[4], b[5]), &pipe, max_radius);
+    for (size_t t = 0; t < counts.size(); ++t)
+        if (!init.generate_points((pluint)counts[t], radii[t], (char)t)) return 3;
+    std::vector<double> pos, quat;
+    for (size_t t = 0; t < counts.size(); ++t) {
+        std::vector<Array<T, 3> > pts;
+        init.get_points((char)t, pts);
+        for (size_t i = 0; i < pts.size(); ++i)
+            for (int d = 0; d < 3; ++d) pos.push_back(pts[i][d]);
+    }
+    // one orientation per particle, the axis built from three draws in one constructor call as
+    // the driver does, the angle from a fourth draw unless the axis is zero
+    const size_t n = pos.size() / 3;
+    for (size_t i = 0; i < n; ++i) {
+        Array<T, 3> dir((T)std::rand() / RAND_MAX, (T)std::rand() / RAND_MAX, (T)std::rand() / RAND_MAX);
+        const T dn = norm(dir);
+        Quaternion<T> q;
+        if (dn > std::numeric_limits<T>::epsilon()) q = Quaternion<T>(2. * M_PI * (T)std::rand() / RAND_MAX, dir / dn);
+        for (int k = 0; k < 4; ++k) quat.push_back(q[k]);
+    }
+    recio::Writer w(out);
+    w.d("pos", shp((long long)n, 3), pos);
+    w.d("quat", shp((long long)n, 4), quat);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) {
         std::fprintf(stderr, "usage: ref_harness <lbm|ibm|forces|interp|shape|inertia> in.rec out.rec\n");
@@ -972,6 +1011,7 @@ int main(int argc, char** argv) {
     if (c == "lattice_save") return run_lattice_save(in, argv[3]);
     if (c == "lattice_load") return run_lattice_load(in, argv[3]);
     if (c == "calibrate") return run_calibrate(in, argv[3]);
+    if (c == "initial") return run_initial(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

@@ -758,3 +758,65 @@ def align_minor_axis(pos, tri, pref=(0.0, 0.0, 1.0)):
         for i in range(3):
             out[v, i] = x * R[i][0] + y * R[i][1] + z * R[i][2] + t[i]
     return out
+
+
+# ---------------------------------------------------------------- random initial placement
+class GlibcRand:
+    """glibc's rand() after srand(seed) (TYPE_3): x_i = x_{i-3} + x_{i-31} mod 2^32, output
+    x_i >> 1; x_1 .. x_30 from the Lehmer generator 16807 x mod (2^31 - 1); 310 outputs discarded."""
+
+    def __init__(self, seed):
+        seed = seed or 1
+        r = [seed]
+        for i in range(1, 31):
+            r.append((16807 * r[i - 1]) % 2147483647)
+        r += r[0:3]
+        for i in range(34, 344):
+            r.append((r[i - 31] + r[i - 3]) & 0xFFFFFFFF)
+        self.r = r[-34:]
+
+    def __call__(self):
+        v = (self.r[-31] + self.r[-3]) & 0xFFFFFFFF
+        self.r = self.r[1:] + [v]
+        return v >> 1
+
+
+def initial_distribution(box, counts, radii, seed, pipe=None):
+    """ParticlePositionInitializer::generate_points (ParticlePositionInitializer.hh:17-80) per type
+    and the random orientations of progs/common/create_particles.h:80-93, as the reference draws
+    them from rand(): (positions (n, 3), quaternions (n, 4))."""
+    import math
+
+    rand = GlibcRand(int(seed))
+    RM = 2147483647.0
+    pos, rad = [], []
+    for t, n in enumerate(counts):
+        r = float(radii[t])
+        for _ in range(int(n)):
+            while True:
+                p = [float(box[2 * a]) + r + (rand() / RM) * (float(box[2 * a + 1] - box[2 * a]) - 2 * r) for a in range(3)]
+                if pipe is not None:
+                    dy, dz = p[1] - pipe[0], p[2] - pipe[1]
+                    if not (dy * dy + dz * dz) < (pipe[2] - r) * (pipe[2] - r):
+                        continue
+                ok = True
+                for q, rq in zip(pos, rad):
+                    dx, dy, dz = q[0] - p[0], q[1] - p[1], q[2] - p[2]
+                    if dx * dx + dy * dy + dz * dz < (rq + r) * (rq + r):
+                        ok = False
+                        break
+                if ok:
+                    break
+            pos.append(p)
+            rad.append(r)
+    quats = []
+    for _ in pos:
+        d2, d1, d0 = rand() / RM, rand() / RM, rand() / RM  # g++ evaluates the three arguments last to first
+        dn = math.sqrt(d0 * d0 + d1 * d1 + d2 * d2)
+        if dn > 2.220446049250313e-16:
+            theta = 2. * math.pi * rand() / RM
+            s = math.sin(theta / 2)
+            quats.append([math.cos(theta / 2), s * (d0 / dn), s * (d1 / dn), s * (d2 / dn)])
+        else:
+            quats.append([1.0, 0.0, 0.0, 0.0])
+    return np.array(pos), np.array(quats)

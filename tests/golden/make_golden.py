@@ -481,9 +481,19 @@ def case_calibrate():
     save("calibrate_rbc", inp, out)
 
 
+def case_initial():
+    """The random initial placement of progs/common/create_particles.h: two particle types at 20 %
+    scale (radius 0.2 R + 1) in a pipe of radius 12 (the driver's pipe radius - 1.5), seeded."""
+    inp = dict(box=np.array([0, 79, 0, 29, 0, 29]), pipe=np.array([14.5, 14.5, 12.0]), counts=np.array([60, 25]),
+               radii=np.array([0.2 * 7.8 + 1.0, 0.2 * 4.0 + 1.0]), max_radius=0.2 * 7.8 + 1.0, seed=12345)
+    out = run("initial", inp)
+    assert out["pos"].shape == (85, 3)
+    save("initial_distribution", inp, out)
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
          case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo, case_ibm_pipe,
-         case_reflect, case_plb, case_lattice_plb, case_calibrate]
+         case_reflect, case_plb, case_lattice_plb, case_calibrate, case_initial]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
