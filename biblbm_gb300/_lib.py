@@ -88,6 +88,9 @@ SIGNATURES = {
     "bib_particle_set_positions": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp]),
     "bib_particle_stats": (C.c_int32, [_vp, C.c_int32, C.c_int32, _dp]),
     "bib_particles_download": (C.c_int32, [_vp, C.c_int32, _dp, _dp]),
+    "bib_particles_download_async": (C.c_int32, [_vp, C.c_int32, _dp, _dp, C.c_int32]),
+    "bib_download_wait": (C.c_int32, [_vp, C.c_int32]),
+    "bib_particles_upload": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_total_vertices": (C.c_int32, [_vp, C.c_int32, _ip]),
     "bib_total_volume": (C.c_int32, [_vp, C.c_int32, _dp]),
     "bib_ibm_step": (C.c_int32, [_vp, C.c_int32]),

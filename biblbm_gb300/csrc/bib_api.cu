@@ -34,6 +34,7 @@ struct bib_ctx {
     bool profiling = false;
     double prof[5] = {0, 0, 0, 0, 0};  // membrane, spread, collide+stream, walls, interpolate+update
     cudaEvent_t ev[6] = {};
+    cudaEvent_t dl_ev[8] = {};  // completion of the asynchronous downloads, one per slot
     int* d_flag = nullptr;
     std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, steps and parity) -> step graph
     double* stage = nullptr;  // device staging area of the host <-> device population transfers
@@ -663,13 +664,14 @@ bib_status pull_particles(bib_ctx* c, Lattice& L) {
     return BIB_OK;
 }
 
-// Population transfers stream whole z-planes through a staging area of about 32 MB (at
-// least one plane of all 19 populations), allocated once per context.
+// Population transfers stream whole z-planes through a staging area of about 32 MB (at least
+// one plane of all 19 populations, at most the lattice), allocated once per context.  (512 MB
+// chunks measured no faster on the 512 x 128 x 128 channel.)
 constexpr size_t kStageTarget = (size_t)4 << 20;  // doubles
 
 bib_status plane_chunk(bib_ctx* c, const Lattice& L, int* planes) {
     const size_t plane = (size_t)Q * L.d.nx * L.d.ny;
-    const size_t want = std::max(plane, kStageTarget / plane * plane);
+    const size_t want = plane * std::max<size_t>(1, std::min<size_t>(kStageTarget / plane, (size_t)L.d.nz));
     if (c->stage_count < want) {
         cudaFree(c->stage);
         c->stage = nullptr;
@@ -1031,6 +1033,7 @@ bib_status bib_create(const bib_config* cfg, bib_ctx** out) {
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
+    for (int k = 0; k < 8 && e == cudaSuccess; ++k) e = cudaEventCreateWithFlags(&c->dl_ev[k], cudaEventDisableTiming);
     // d_flag[0]: NaN scan result, d_flag[1]: set by a bounded device wait that gave up,
     // d_flag[2]: set by a voxelization whose column held more crossings than it can store
     if (e == cudaSuccess) e = cudaMalloc((void**)&c->d_flag, 3 * sizeof(int));
@@ -1079,6 +1082,8 @@ void bib_destroy(bib_ctx* c) {
     }
     for (int k = 0; k < 6; ++k)
         if (c->ev[k]) cudaEventDestroy(c->ev[k]);
+    for (int k = 0; k < 8; ++k)
+        if (c->dl_ev[k]) cudaEventDestroy(c->dl_ev[k]);
     cudaFree(c->d_flag);
     cudaFree(c->stage);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -1913,6 +1918,50 @@ bib_status bib_particles_download(bib_ctx* c, int32_t h, double* pos, double* st
     if (stats && !L->parts.empty())
         BIB_CUDA(c, cudaMemcpyAsync(stats, L->stats, STATS * L->parts.size() * 8, cudaMemcpyDeviceToHost, c->stream));
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    return BIB_OK;
+}
+
+bib_status bib_particles_upload(bib_ctx* c, int32_t h, const double* pos) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || !pos) return fail(c, BIB_EINVAL, "invalid lattice handle or positions");
+    if (L->particles_dirty) {  // not uploaded yet: replace the host copies
+        std::memcpy(L->host_pos.data(), pos, L->host_pos.size() * 8);
+        for (size_t p = 0; p < L->parts.size(); ++p) {
+            const ParticleHost& ph = L->parts[p];
+            particle_update(*c->shapes[ph.shape], L->host_pos.data() + 3 * (size_t)ph.v0, L->host_stats.data() + STATS * p);
+        }
+        return BIB_OK;
+    }
+    if (L->nvert == 0) return BIB_OK;
+    // into the move target, then the end of a step: area / volume / centre (and the periodic
+    // remap of the centre) of the new positions, the parity flip, the voxelization
+    BIB_CUDA(c, cudaMemcpyAsync(L->pos[1 - L->pcur], pos, 3 * (size_t)L->nvert * 8, cudaMemcpyHostToDevice, c->stream));
+    launch_particle_update(*L, c->stream);
+    L->pcur = 1 - L->pcur;
+    if (L->phase) launch_voxelize(*L, L->pos[L->pcur], c->stream);
+    BIB_CHECK_LAUNCH(c);
+    return BIB_OK;
+}
+
+bib_status bib_particles_download_async(bib_ctx* c, int32_t h, double* pos, double* stats, int32_t slot) {
+    Lattice* L = get_lattice(c, h);
+    if (!L || slot < 0 || slot >= 8) return fail(c, BIB_EINVAL, "invalid lattice handle or slot");
+    if (L->particles_dirty) {  // not uploaded yet: the host copies are the state
+        if (pos) std::memcpy(pos, L->host_pos.data(), L->host_pos.size() * 8);
+        if (stats) std::memcpy(stats, L->host_stats.data(), L->host_stats.size() * 8);
+    } else {
+        if (pos && L->nvert)
+            BIB_CUDA(c, cudaMemcpyAsync(pos, L->pos[L->pcur], 3 * (size_t)L->nvert * 8, cudaMemcpyDeviceToHost, c->stream));
+        if (stats && !L->parts.empty())
+            BIB_CUDA(c, cudaMemcpyAsync(stats, L->stats, STATS * L->parts.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+    }
+    BIB_CUDA(c, cudaEventRecord(c->dl_ev[slot], c->stream));
+    return BIB_OK;
+}
+
+bib_status bib_download_wait(bib_ctx* c, int32_t slot) {
+    if (!c || slot < 0 || slot >= 8) return fail(c, BIB_EINVAL, "invalid slot");
+    BIB_CUDA(c, cudaEventSynchronize(c->dl_ev[slot]));
     return BIB_OK;
 }
 

@@ -243,6 +243,18 @@ bib_status bib_particle_set_positions(bib_ctx* ctx, int32_t h, int32_t pid, cons
 bib_status bib_particle_stats(bib_ctx* ctx, int32_t h, int32_t pid, double* out);
 /* all vertex positions (3 * total vertices) and per-particle {area, volume, com[3]} (5 per particle) */
 bib_status bib_particles_download(bib_ctx* ctx, int32_t h, double* pos, double* stats);
+/* all vertex positions (3 per vertex, particles in order) into the device state without
+ * re-building it: the area, volume and centre follow as after a step's move (the centre mapped
+ * to the periodic grid, the vertices with it), and a phase field is re-voxelized.  Asynchronous
+ * on the context's stream; the host buffer is read before the call returns only when the
+ * particles have not been uploaded yet. */
+bib_status bib_particles_upload(bib_ctx* ctx, int32_t h, const double* pos);
+/* bib_particles_download without waiting: the copies are queued on the context's stream behind the
+ * work issued so far, and slot (0..7) marks their completion.  The host buffers must stay valid (and
+ * be pinned for the copy to overlap) until bib_download_wait(ctx, slot) returns; a step issued in
+ * between runs while the copy's data are read.  Either pointer may be NULL. */
+bib_status bib_particles_download_async(bib_ctx* ctx, int32_t h, double* pos, double* stats, int32_t slot);
+bib_status bib_download_wait(bib_ctx* ctx, int32_t slot);
 bib_status bib_total_vertices(bib_ctx* ctx, int32_t h, int64_t* n);
 /* compute_total_volume, ImmersedBoundaryDynamics.hh:559-568 */
 bib_status bib_total_volume(bib_ctx* ctx, int32_t h, double* v);

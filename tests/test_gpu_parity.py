@@ -632,3 +632,50 @@ def test_wall_reflection_against_oracle(ctx):
     assert np.hypot(o["pos"][:, 1] - y0, o["pos"][:, 2] - z0).max() <= R
     assert np.abs(g["pos"] - o["pos"]).max() < 1e-12
     ctx.set_graph_mode(True)
+
+
+def test_async_download_equals_sync_download(ctx):
+    """bib_particles_download_async behind each step, waited for one step later, gives the stats
+    of every step as the synchronous download does."""
+    import ctypes as C
+
+    d = golden("ibm_capsule_shear")
+    lat, fsi, pid = run_coupled_gpu(ctx, d, spread="deterministic")
+    lat2, fsi2, pid2 = run_coupled_gpu(ctx, d, spread="deterministic")
+    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
+    bufs = [np.zeros((1, 5)), np.zeros((1, 5))]
+    got, ref = [], []
+    for k in range(6):
+        fsi.step(1)
+        ctx.check(ctx.lib.bib_particles_download_async(ctx.h, lat.h, None, dp(bufs[k % 2]), k % 2))
+        if k:
+            ctx.check(ctx.lib.bib_download_wait(ctx.h, (k - 1) % 2))
+            got.append(bufs[(k - 1) % 2].copy())
+        fsi2.step(1)
+        ref.append(fsi2.download()[1].copy())
+    ctx.check(ctx.lib.bib_download_wait(ctx.h, 1))
+    got.append(bufs[1].copy())
+    for a, b in zip(got, ref):
+        assert np.array_equal(a, b)
+
+
+def test_bulk_position_upload_equals_per_particle_positions(ctx):
+    """bib_particles_upload (all vertices into the live device state) continues like
+    bib_particle_set_positions (which rebuilds the particle state from the host)."""
+    import ctypes as C
+
+    d = golden("ibm_capsule_shear")
+    lat_a, fsi_a, pa = run_coupled_gpu(ctx, d, spread="deterministic")
+    lat_b, fsi_b, pb = run_coupled_gpu(ctx, d, spread="deterministic")
+    fsi_a.step(2)
+    fsi_b.step(2)
+    new = fsi_a.get_particle(pa)["pos"] + np.array([0.3, -0.2, 0.1])
+    fsi_a.set_positions(pa, new)
+    ctx.check(ctx.lib.bib_particles_upload(ctx.h, lat_b.h, np.ascontiguousarray(new).ctypes.data_as(C.POINTER(C.c_double))))
+    pa_b = fsi_b.get_particle(pb)
+    assert np.array_equal(pa_b["pos"], new)
+    assert pa_b["volume"] == pytest.approx(fsi_a.get_particle(pa)["volume"], rel=1e-13)
+    fsi_a.step(3)
+    fsi_b.step(3)
+    assert rel(fsi_b.get_particle(pb)["pos"], fsi_a.get_particle(pa)["pos"]) < 1e-12
+    assert np.abs(lat_b.receive() - lat_a.receive()).max() < 1e-14
