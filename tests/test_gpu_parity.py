@@ -659,12 +659,14 @@ def test_async_download_equals_sync_download(ctx):
         assert np.array_equal(a, b)
 
 
-def test_bulk_position_upload_equals_per_particle_positions(ctx):
+@pytest.mark.parametrize("name", ["ibm_capsule_shear", "ibm_capsule_lambda"])
+def test_bulk_position_upload_equals_per_particle_positions(ctx, name):
     """bib_particles_upload (all vertices into the live device state) continues like
-    bib_particle_set_positions (which rebuilds the particle state from the host)."""
+    bib_particle_set_positions (which rebuilds the particle state from the host), with a
+    re-voxelized phase field where the viscosity ratio needs one."""
     import ctypes as C
 
-    d = golden("ibm_capsule_shear")
+    d = golden(name)
     lat_a, fsi_a, pa = run_coupled_gpu(ctx, d, spread="deterministic")
     lat_b, fsi_b, pb = run_coupled_gpu(ctx, d, spread="deterministic")
     fsi_a.step(2)
@@ -679,3 +681,5 @@ def test_bulk_position_upload_equals_per_particle_positions(ctx):
     fsi_b.step(3)
     assert rel(fsi_b.get_particle(pb)["pos"], fsi_a.get_particle(pa)["pos"]) < 1e-12
     assert np.abs(lat_b.receive() - lat_a.receive()).max() < 1e-14
+    if "lambda" in name:
+        assert np.array_equal(lat_b.get_phase(), lat_a.get_phase())
