@@ -62,3 +62,19 @@ def test_create_fails_cleanly_without_gpu(lib):
     h = ctypes.c_void_p()
     st = L.bib_create(ctypes.byref(_lib.Config(0, 0)), ctypes.byref(h))
     assert st == -3 and not h.value
+
+
+def test_header_compiles_as_c99(tmp_path):
+    """The drop-in boundary is a plain C header: a C99 translation unit (as a C or cgo / ctypes
+    binding would compile) includes it without warnings."""
+    import shutil
+    import subprocess
+
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if cc is None:
+        pytest.skip("no C compiler")
+    src = tmp_path / "use_bib.c"
+    src.write_text('#include "bib/bib.h"\nint main(void) { bib_lattice_params p; (void)p; return 0; }\n')
+    r = subprocess.run([cc, "-std=c99", "-Wall", "-Wextra", "-pedantic", "-Werror", "-I", os.path.join(ROOT, "include"),
+                        "-c", str(src), "-o", str(tmp_path / "use_bib.o")], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
