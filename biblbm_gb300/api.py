@@ -487,6 +487,25 @@ class ImmersedBoundaryDynamics3D:
         self.ctx.check(self.ctx.lib.bib_particles_download(self.ctx.h, self.lattice.h, _d(pos), _d(stats)))
         return pos, stats
 
+    def download_async(self, stats, slot, pos=None):
+        """Queue the copy of the per-particle area / volume / centre (and optionally all vertex
+        positions) behind the steps issued so far; the arrays (C-contiguous float64, pinned for the
+        copy to overlap) hold the values once ``wait_download(slot)`` returns."""
+        for a in (stats, pos):
+            if a is not None and (a.dtype != np.float64 or not a.flags.c_contiguous):
+                raise ValueError("download buffers must be C-contiguous float64 arrays")
+        self.ctx.check(self.ctx.lib.bib_particles_download_async(self.ctx.h, self.lattice.h,
+                                                                 _d(pos) if pos is not None else None,
+                                                                 _d(stats) if stats is not None else None, int(slot)))
+
+    def wait_download(self, slot):
+        self.ctx.check(self.ctx.lib.bib_download_wait(self.ctx.h, int(slot)))
+
+    def upload_positions(self, pos):
+        """All vertex positions (particles in order) into the live device state, no rebuild."""
+        pos = _f64(pos)
+        self.ctx.check(self.ctx.lib.bib_particles_upload(self.ctx.h, self.lattice.h, _d(pos)))
+
     def compute_total_volume(self) -> float:
         v = C.c_double()
         self.ctx.check(self.ctx.lib.bib_total_volume(self.ctx.h, self.lattice.h, C.byref(v)))

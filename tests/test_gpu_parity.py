@@ -637,19 +637,16 @@ def test_wall_reflection_against_oracle(ctx):
 def test_async_download_equals_sync_download(ctx):
     """bib_particles_download_async behind each step, waited for one step later, gives the stats
     of every step as the synchronous download does."""
-    import ctypes as C
-
     d = golden("ibm_capsule_shear")
     lat, fsi, pid = run_coupled_gpu(ctx, d, spread="deterministic")
     lat2, fsi2, pid2 = run_coupled_gpu(ctx, d, spread="deterministic")
-    dp = lambda a: a.ctypes.data_as(C.POINTER(C.c_double))  # noqa: E731
     bufs = [np.zeros((1, 5)), np.zeros((1, 5))]
     got, ref = [], []
     for k in range(6):
         fsi.step(1)
-        ctx.check(ctx.lib.bib_particles_download_async(ctx.h, lat.h, None, dp(bufs[k % 2]), k % 2))
+        fsi.download_async(bufs[k % 2], k % 2)
         if k:
-            ctx.check(ctx.lib.bib_download_wait(ctx.h, (k - 1) % 2))
+            fsi.wait_download((k - 1) % 2)
             got.append(bufs[(k - 1) % 2].copy())
         fsi2.step(1)
         ref.append(fsi2.download()[1].copy())
@@ -664,8 +661,6 @@ def test_bulk_position_upload_equals_per_particle_positions(ctx, name):
     """bib_particles_upload (all vertices into the live device state) continues like
     bib_particle_set_positions (which rebuilds the particle state from the host), with a
     re-voxelized phase field where the viscosity ratio needs one."""
-    import ctypes as C
-
     d = golden(name)
     lat_a, fsi_a, pa = run_coupled_gpu(ctx, d, spread="deterministic")
     lat_b, fsi_b, pb = run_coupled_gpu(ctx, d, spread="deterministic")
@@ -673,7 +668,7 @@ def test_bulk_position_upload_equals_per_particle_positions(ctx, name):
     fsi_b.step(2)
     new = fsi_a.get_particle(pa)["pos"] + np.array([0.3, -0.2, 0.1])
     fsi_a.set_positions(pa, new)
-    ctx.check(ctx.lib.bib_particles_upload(ctx.h, lat_b.h, np.ascontiguousarray(new).ctypes.data_as(C.POINTER(C.c_double))))
+    fsi_b.upload_positions(new)
     pa_b = fsi_b.get_particle(pb)
     assert np.array_equal(pa_b["pos"], new)
     assert pa_b["volume"] == pytest.approx(fsi_a.get_particle(pa)["volume"], rel=1e-13)
