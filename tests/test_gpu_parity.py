@@ -513,7 +513,8 @@ def test_nan_is_detected(ctx):
     assert e.value.status == -4
 
 
-@pytest.mark.parametrize("kernel,storage,tol", [("staged", "f64", 1e-15), ("rows", "f64", 1e-15), ("staged", "f32", 1e-7)])
+@pytest.mark.parametrize("kernel,storage,tol", [("staged", "f64", 1e-15), ("rows", "f64", 1e-15), ("staged", "f32", 1e-7),
+                                                ("rows", "f16", 2e-4)])
 def test_pipe_walls_match_reference(ctx, kernel, storage, tol):
     """First-order pipe walls (rbc_in_pipe.cpp: BounceBack outside the pipe, NoDynamics beyond
     radius + 1) with a body force, against the reference's populations after 40 steps."""
