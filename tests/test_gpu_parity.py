@@ -566,10 +566,11 @@ def test_pipe_too_narrow_for_second_order_walls(ctx):
     lat.set_pipe_walls(4.0, 4.0, 1.2)  # first order works at any size
 
 
-def pipe_capsule_gpu(ctx, d, u0=None):
+def pipe_capsule_gpu(ctx, d, u0=None, storage="f64"):
     nx, ny, nz = (int(v) for v in d["in_dims"])
     y0, z0, R = d["in_pipe"]
-    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=1.0 / float(d["in_tau"]), body_force=d["in_body"])
+    lat = ctx.add_domain(nx, ny, nz, periodic=(1, 1, 1), omega=1.0 / float(d["in_tau"]), body_force=d["in_body"],
+                         storage=storage)
     lat.set_pipe_walls(y0, z0, R, second_order=True)
     lat.initialize_at_equilibrium(None, np.zeros((3, nz, ny, nx)) if u0 is None else u0)
     shapes = bib.ParticleShapeLibrary(ctx)
@@ -598,6 +599,19 @@ def test_capsule_near_pipe_wall_matches_reference(ctx):
     f = lat.receive()
     assert np.abs(f[:, :, :, [0, 7]] - d["out_fbar_end_planes"]).max() < 1e-14
     ctx.set_graph_mode(True)
+
+
+@pytest.mark.parametrize("storage,tol", [("f32", 1e-4), ("f16", 3e-2)])
+def test_capsule_near_pipe_wall_reduced_precision(ctx, storage, tol):
+    """The same capsule with FP32 / FP16 populations: its vertex displacements over the run follow
+    the reference's FP64 ones within the storage's precision."""
+    d = golden("ibm_pipe")
+    lat, fsi, pid = pipe_capsule_gpu(ctx, d, storage=storage)
+    ctx.set_graph_mode(True)
+    fsi.step(int(d["in_steps"]))
+    disp = fsi.get_particle(pid)["pos"] - d["out_pos"][0]
+    ref = d["out_pos"][-1] - d["out_pos"][0]
+    assert np.abs(disp - ref).max() < tol * np.abs(ref).max()
 
 
 def test_wall_reflection_against_oracle(ctx):
