@@ -98,6 +98,8 @@ SIGNATURES = {
     "bib_ib_set_pipe_boundary": (C.c_int32, [_vp, C.c_int32, C.c_double, C.c_double, C.c_double]),
     "bib_lattice_set_pipe_walls": (C.c_int32, [_vp, C.c_int32, C.c_double, C.c_double, C.c_double, C.c_int32]),
     "bib_add_wall_interaction": (C.c_int32, [_vp, C.c_int32, C.c_int32, C.c_double, C.c_double, C.POINTER(Potential)]),
+    "bib_add_pipe_wall_interaction": (C.c_int32, [_vp, C.c_int32, C.c_double, C.c_double, C.c_double,
+                                                  C.POINTER(Potential)]),
     "bib_add_pp_interaction": (C.c_int32, [_vp, C.c_int32, C.POINTER(Potential)]),
     "bib_clear_interactions": (C.c_int32, [_vp, C.c_int32]),
     "bib_particle_info": (C.c_int32, [_vp, C.c_int32, C.c_int32, _i32p]),

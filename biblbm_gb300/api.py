@@ -401,6 +401,12 @@ class ImmersedBoundaryDynamics3D:
         self.ctx.check(self.ctx.lib.bib_add_wall_interaction(self.ctx.h, self.lattice.h, int(axis), float(lo),
                                                              float(hi), C.byref(potential)))
 
+    def add_pipe_wall_interaction(self, potential: Potential, y0: float, z0: float, radius: float):
+        """add_force_decorator(WallInteraction(PipeBoundary(y0, z0, radius), potential)) for a pipe
+        along x (rbc_in_pipe.cpp:154-163)."""
+        self.ctx.check(self.ctx.lib.bib_add_pipe_wall_interaction(self.ctx.h, self.lattice.h, float(y0), float(z0),
+                                                                  float(radius), C.byref(potential)))
+
     def add_pp_force(self, potential: Potential):
         """add_pp_force(PPPotentialForce(potential)): repulsion between vertices of different particles."""
         self.ctx.check(self.ctx.lib.bib_add_pp_interaction(self.ctx.h, self.lattice.h, C.byref(potential)))

@@ -1792,6 +1792,24 @@ bib_status bib_add_wall_interaction(bib_ctx* c, int32_t h, int32_t axis, double 
     return BIB_OK;
 }
 
+bib_status bib_add_pipe_wall_interaction(bib_ctx* c, int32_t h, double y0, double z0, double radius,
+                                         const bib_potential* p) {
+    Lattice* L = get_lattice(c, h);
+    if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
+    bib_status st = check_potential(c, p);
+    if (st) return st;
+    if (!(radius > 0) || !std::isfinite(y0) || !std::isfinite(z0)) return fail(c, BIB_EINVAL, "bad pipe");
+    if (L->inter.nwall >= BIB_MAX_WALL_INTERACTIONS) return fail(c, BIB_EINVAL, "too many wall interactions");
+    const int w = L->inter.nwall++;
+    L->inter.wall_axis[w] = 3;
+    L->inter.wall_lo[w] = y0;
+    L->inter.wall_hi[w] = z0;
+    L->inter.wall_r[w] = radius;
+    L->inter.wall[w] = PotentialDev{p->kind, p->r0, p->beta, p->strength};
+    interactions_changed(c, h);
+    return BIB_OK;
+}
+
 bib_status bib_add_pp_interaction(bib_ctx* c, int32_t h, const bib_potential* p) {
     Lattice* L = get_lattice(c, h);
     if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");

@@ -112,6 +112,8 @@ struct Interactions {
     int nwall = 0;
     int wall_axis[BIB_MAX_WALL_INTERACTIONS] = {};
     double wall_lo[BIB_MAX_WALL_INTERACTIONS] = {}, wall_hi[BIB_MAX_WALL_INTERACTIONS] = {};
+    // wall_axis 3: a PipeBoundary along x through (wall_lo, wall_hi) = (y0, z0) of radius wall_r
+    double wall_r[BIB_MAX_WALL_INTERACTIONS] = {};
     PotentialDev wall[BIB_MAX_WALL_INTERACTIONS] = {};
     int npp = 0;
     PotentialDev pp[BIB_MAX_PP_INTERACTIONS] = {};

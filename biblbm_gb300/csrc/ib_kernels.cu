@@ -516,6 +516,17 @@ __device__ __forceinline__ void wall_force(const Interactions& I, const double* 
     f[0] = f[1] = f[2] = 0.0;
     for (int w = 0; w < I.nwall; ++w) {
         const int a = I.wall_axis[w];
+        if (a == 3) {  // PipeBoundary: distance_to_boundary and get_normal, Boundary.h:158-161, 245-249
+            const double dy = p[1] - I.wall_lo[w], dz = p[2] - I.wall_hi[w];
+            const double rr = sqrt(dy * dy + dz * dz);
+            const double dist = I.wall_r[w] - rr;
+            if (dist <= I.wall[w].r0) {
+                const double phi = potential_eval(I.wall[w], dist);
+                f[1] -= phi * (dy / rr);
+                f[2] -= phi * (dz / rr);
+            }
+            continue;
+        }
         const double r = p[a], lo = I.wall_lo[w], hi = I.wall_hi[w];
         const bool lower = r < 0.5 * (lo + hi);
         const double dist = lower ? r - lo : hi - r;

@@ -281,6 +281,12 @@ typedef struct {
 /* WallInteraction with ParallelPlatesBoundary(lo, hi) (Boundary.h:305-365) normal to axis 1 (y,
  * the reference's plates) or 2 (z): distance to the nearer plate, force -= phi(dist) outward normal */
 bib_status bib_add_wall_interaction(bib_ctx* ctx, int32_t h, int32_t axis, double lo, double hi, const bib_potential* p);
+/* WallInteraction on a PipeBoundary along x through (y0, z0) (rbc_in_pipe.cpp:154-163,
+ * ForceDecorator.hh:25-32, Boundary.h:158-161, 245-249): a vertex at distance
+ * dist = radius - sqrt((y - y0)^2 + (z - z0)^2) <= r0 from the wall gets force -= phi(dist) n,
+ * n = (0, y - y0, z - z0) / |.| */
+bib_status bib_add_pipe_wall_interaction(bib_ctx* ctx, int32_t h, double y0, double z0, double radius,
+                                         const bib_potential* p);
 bib_status bib_add_pp_interaction(bib_ctx* ctx, int32_t h, const bib_potential* p);
 bib_status bib_clear_interactions(bib_ctx* ctx, int32_t h);
 

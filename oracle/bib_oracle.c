@@ -1062,6 +1062,23 @@ void orc_wall_forces(const orc_potential* p, int32_t axis, double lo, double hi,
     }
 }
 
+/* WallInteraction on a PipeBoundary along x through (y0, z0) of the given radius
+ * (ForceDecorator.hh:25-32; distance_to_boundary and get_normal, Boundary.h:158-161, 245-249):
+ * dist = radius - sqrt((y - y0)^2 + (z - z0)^2), force -= phi(dist) (0, dy, dz) / |(0, dy, dz)| */
+void orc_pipe_wall_forces(const orc_potential* p, double y0, double z0, double radius, int64_t nv, const double* pos,
+                          double* force) {
+    for (int64_t i = 0; i < nv; ++i) {
+        const double dy = pos[3 * i + 1] - y0, dz = pos[3 * i + 2] - z0;
+        const double dist = radius - sqrt(dy * dy + dz * dz);
+        if (dist <= p->r0) {
+            const double f = orc_potential_eval(p, dist);
+            const double nn = sqrt(0.0 * 0.0 + dy * dy + dz * dz);
+            const double n[3] = {0.0 / nn, dy / nn, dz / nn};
+            for (int d = 0; d < 3; ++d) force[3 * i + d] -= f * n[d];
+        }
+    }
+}
+
 /* Arithmetic1D::min_mod_diff (Periodicity.h:27-35, 96-99) on periodic axes, x - y otherwise */
 static double axis_diff(const orc_lattice* L, int a, double x, double y) {
     const int64_t N = a == 0 ? L->nx : (a == 1 ? L->ny : L->nz);
@@ -1558,7 +1575,7 @@ struct orc_sys {
     int32_t nwalls;
     orc_potential wall_pot[8];
     int32_t wall_axis[8];
-    double wall_lo[8], wall_hi[8];
+    double wall_lo[8], wall_hi[8], wall_r[8]; /* axis 3: a pipe along x, (lo, hi) = (y0, z0), radius r */
     int32_t npp;
     orc_potential pp_pot[8];
     int32_t pp_grid;  /* 1: the reference's grid search, 0: every pair within the cutoff */
@@ -1691,8 +1708,19 @@ static void sys_voxelize(orc_sys* s) {
 
 void orc_sys_set_voxelize(orc_sys* s, int32_t on) { s->voxelize = on; }
 
+int32_t orc_sys_add_pipe_wall_interaction(orc_sys* s, const orc_potential* p, double y0, double z0, double radius) {
+    if (s->nwalls >= 8 || !(radius > 0)) return -1;
+    s->wall_pot[s->nwalls] = *p;
+    s->wall_axis[s->nwalls] = 3;
+    s->wall_lo[s->nwalls] = y0;
+    s->wall_hi[s->nwalls] = z0;
+    s->wall_r[s->nwalls] = radius;
+    return s->nwalls++;
+}
+
 int32_t orc_sys_add_wall_interaction(orc_sys* s, const orc_potential* p, int32_t axis, double lo, double hi) {
     if (s->nwalls >= 8 || axis < 0 || axis > 2) return -1;
+    s->wall_r[s->nwalls] = 0.0;
     s->wall_pot[s->nwalls] = *p;
     s->wall_axis[s->nwalls] = axis;
     s->wall_lo[s->nwalls] = lo;
@@ -1778,8 +1806,14 @@ static void sys_step(orc_sys* s) {
             /* ImmersedBoundaryDynamics3D::compute_forces (ImmersedBoundaryDynamics_forces.hh:287-302):
              * zero, the force decorators, then the particle's own forces */
             memset(p->force, 0, sizeof(double) * 3 * sh->nv);
-            for (int32_t w = 0; w < s->nwalls; ++w)
-                orc_wall_forces(&s->wall_pot[w], s->wall_axis[w], s->wall_lo[w], s->wall_hi[w], sh->nv, p->pos, p->force);
+            for (int32_t w = 0; w < s->nwalls; ++w) {
+                if (s->wall_axis[w] == 3)
+                    orc_pipe_wall_forces(&s->wall_pot[w], s->wall_lo[w], s->wall_hi[w], s->wall_r[w], sh->nv, p->pos,
+                                         p->force);
+                else
+                    orc_wall_forces(&s->wall_pot[w], s->wall_axis[w], s->wall_lo[w], s->wall_hi[w], sh->nv, p->pos,
+                                    p->force);
+            }
             membrane_forces_acc(p->model, p->prm, sh->nv, sh->rest, sh->nt, sh->tri, sh->tri_area, sh->area, sh->nl,
                                 sh->links, sh->link_len, sh->np, sh->pairs, sh->pair_cs, p->pos, p->area, p->volume,
                                 p->force);

@@ -143,6 +143,7 @@ void orc_sys_init(orc_sys* s);
 void orc_sys_step(orc_sys* s, int64_t nsteps);
 void orc_sys_set_voxelize(orc_sys* s, int32_t on);  /* revoxelize after every move (and at init) */
 /* add_force_decorator(WallInteraction(ParallelPlatesBoundary(lo, hi) normal to `axis`, p)) */
+int32_t orc_sys_add_pipe_wall_interaction(orc_sys* s, const orc_potential* p, double y0, double z0, double radius);
 int32_t orc_sys_add_wall_interaction(orc_sys* s, const orc_potential* p, int32_t axis, double lo, double hi);
 /* add_pp_force(PPPotentialForce(p)); grid = 1 evaluates it with the reference's grid search */
 int32_t orc_sys_add_pp_interaction(orc_sys* s, const orc_potential* p, int32_t grid);

@@ -686,7 +686,12 @@ static int run_interact_impl(const Bundle& in, const char* out, const PP& ppot, 
     ImmersedBoundaryDynamics3D<T, DESCRIPTOR, Periodicity3D<T, true, true, true> > fsi(lattice, lib);
     const std::vector<double> wy = recio::need(in, "wall_y").d;
     ParallelPlatesBoundary<T> plates(wy[0], wy[1]);
-    WallInteraction<T, WP> wall(plates, wpot);
+    // a pipe along x instead of the plates when given (y0, z0, radius), as rbc_in_pipe.cpp:154-163
+    std::vector<double> pp_geo = recio::has(in, "pipe") ? recio::need(in, "pipe").d : std::vector<double>(3, 0.0);
+    PipeBoundary<T> pipe(pp_geo[0], pp_geo[1], pp_geo[2], (T)nx);
+    const Boundary<T>& bnd = recio::has(in, "pipe") ? static_cast<const Boundary<T>&>(pipe)
+                                                     : static_cast<const Boundary<T>&>(plates);
+    WallInteraction<T, WP> wall(bnd, wpot);
     PPPotentialForce<T, PP> pp(ppot);
     fsi.add_force_decorator(&wall);
     fsi.add_pp_force(&pp);

@@ -115,6 +115,8 @@ def lib():
             "orc_sys_add_wall_interaction": (C.c_int32, [C.c_void_p, C.POINTER(Potential), C.c_int32, C.c_double,
                                                          C.c_double]),
             "orc_sys_add_pp_interaction": (C.c_int32, [C.c_void_p, C.POINTER(Potential), C.c_int32]),
+            "orc_sys_add_pipe_wall_interaction": (C.c_int32, [C.c_void_p, C.POINTER(Potential), C.c_double,
+                                                              C.c_double, C.c_double]),
             "orc_sys_velocity": (None, [C.c_void_p, dp]),
         }
         for name, (res, args) in sig.items():
@@ -341,6 +343,10 @@ class System:
     def add_wall_interaction(self, pot: Potential, axis: int, lo: float, hi: float):
         """add_force_decorator(WallInteraction(ParallelPlatesBoundary(lo, hi) normal to axis, pot))."""
         assert lib().orc_sys_add_wall_interaction(self.h, C.byref(pot), int(axis), float(lo), float(hi)) >= 0
+
+    def add_pipe_wall_interaction(self, pot: Potential, y0: float, z0: float, radius: float):
+        """add_force_decorator(WallInteraction(PipeBoundary along x through (y0, z0), pot))."""
+        assert lib().orc_sys_add_pipe_wall_interaction(self.h, C.byref(pot), float(y0), float(z0), float(radius)) >= 0
 
     def add_pp_interaction(self, pot: Potential, grid: bool = False):
         """add_pp_force(PPPotentialForce(pot)); grid=True searches pairs as the reference does."""

@@ -351,6 +351,15 @@ def case_interact():
         out = run("interact", inp)
         assert np.abs(out["force_a"]).max() > 1e-4 and np.abs(out["force_b"]).max() > 1e-4
         save(name, inp, {"force_a": out["force_a"], "force_b": out["force_b"]})
+    # the wall interaction on a pipe along x (rbc_in_pipe.cpp:154-163) through the capsules' axis,
+    # its wall just outside the outermost vertices
+    y0, z0 = 10.2, 11.6
+    rmax = max(np.hypot(a[:, 1] - y0, a[:, 2] - z0).max(), np.hypot(b[:, 1] - y0, b[:, 2] - z0).max())
+    inp = dict(dims=[n, n, n], rest=xyz, tri=tri, pos_a=a, pos_b=b, model=1, params=prm, pp_kind=1,
+               pp_params=[0.6, 3.0, 2e-3], wall_kind=2, wall_params=[0.5, 0.0, 1e-2], wall_y=list(wy),
+               pipe=[y0, z0, rmax + 0.3])
+    out = run("interact", inp)
+    save("interact_pipe_wall", inp, {"force_a": out["force_a"], "force_b": out["force_b"]})
 
 
 def case_lbm_pipe():

@@ -28,7 +28,7 @@ def potential(kind, q):
     return bib.MorsePotential(q[0], q[1], q[2]) if int(kind) == 1 else bib.SpringPotential(q[0], q[2])
 
 
-@pytest.mark.parametrize("name", ["interact_morse_spring", "interact_spring_morse"])
+@pytest.mark.parametrize("name", ["interact_morse_spring", "interact_spring_morse", "interact_pipe_wall"])
 @pytest.mark.parametrize("spread,storage", [("atomic", "f64"), ("deterministic", "f64"), ("atomic", "f32")])
 def test_interaction_forces_match_reference(ctx, name, spread, storage):
     d = golden(name)
@@ -39,8 +39,11 @@ def test_interaction_forces_match_reference(ctx, name, spread, storage):
     fsi = bib.ImmersedBoundaryDynamics3D(lat, shapes, spread=spread)
     pa = fsi.add_particle(sid, "capsule_skalak", d["in_params"], d["in_pos_a"])
     pb = fsi.add_particle(sid, "capsule_skalak", d["in_params"], d["in_pos_b"])
-    lo, hi = d["in_wall_y"]
-    fsi.add_wall_interaction(potential(d["in_wall_kind"], d["in_wall_params"]), 1, lo, hi)
+    if "in_pipe" in d.files:  # WallInteraction on a PipeBoundary along x
+        fsi.add_pipe_wall_interaction(potential(d["in_wall_kind"], d["in_wall_params"]), *d["in_pipe"])
+    else:
+        lo, hi = d["in_wall_y"]
+        fsi.add_wall_interaction(potential(d["in_wall_kind"], d["in_wall_params"]), 1, lo, hi)
     fsi.add_pp_force(potential(d["in_pp_kind"], d["in_pp_params"]))
     fsi.ibm_step()
     fa, fb = fsi.get_particle(pa)["force"], fsi.get_particle(pb)["force"]

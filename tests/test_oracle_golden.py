@@ -183,15 +183,18 @@ def interact_system(d, grid):
     pa = S.add_particle(sid, int(d["in_model"]), d["in_params"], d["in_pos_a"])
     pb = S.add_particle(sid, int(d["in_model"]), d["in_params"], d["in_pos_b"])
     wq, pq = d["in_wall_params"], d["in_pp_params"]
-    lo, hi = d["in_wall_y"]
-    S.add_wall_interaction(O.potential(int(d["in_wall_kind"]), wq[0], wq[1], wq[2]), 1, lo, hi)
+    if "in_pipe" in d.files:  # WallInteraction on a PipeBoundary along x
+        S.add_pipe_wall_interaction(O.potential(int(d["in_wall_kind"]), wq[0], wq[1], wq[2]), *d["in_pipe"])
+    else:
+        lo, hi = d["in_wall_y"]
+        S.add_wall_interaction(O.potential(int(d["in_wall_kind"]), wq[0], wq[1], wq[2]), 1, lo, hi)
     S.add_pp_interaction(O.potential(int(d["in_pp_kind"]), pq[0], pq[1], pq[2]), grid=grid)
     S.init()
     S.step(1)
     return S.particle(pa)["force"], S.particle(pb)["force"]
 
 
-@pytest.mark.parametrize("name", ["interact_morse_spring", "interact_spring_morse"])
+@pytest.mark.parametrize("name", ["interact_morse_spring", "interact_spring_morse", "interact_pipe_wall"])
 def test_interaction_forces(name):
     """Wall decorator + particle-particle forces of one IB step: the reference's grid search
     bit for bit, and the all-pairs search (what the CUDA path evaluates) to the summation
@@ -199,10 +202,11 @@ def test_interaction_forces(name):
     d = golden(name)
     fa, fb = interact_system(d, grid=True)
     assert np.array_equal(fa, d["out_force_a"]) and np.array_equal(fb, d["out_force_b"])
-    # both particles feel the pair force, particle a also the lower plate
+    # both particles feel the pair force, particle a also the lower plate (b the pipe wall)
     near = np.abs(d["out_force_a"][:, 0]) > 0
     assert near.any() and (np.abs(d["out_force_b"][:, 0]) > 0).any()
-    assert (d["out_force_a"][:, 1] > 1e-6).any()
+    if "in_pipe" not in d.files:
+        assert (d["out_force_a"][:, 1] > 1e-6).any()
     ga, gb = interact_system(d, grid=False)
     scale = max(np.abs(d["out_force_a"]).max(), np.abs(d["out_force_b"]).max())
     assert np.abs(ga - d["out_force_a"]).max() <= 1e-15 * scale
