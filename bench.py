@@ -30,9 +30,13 @@ ROOT = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, ROOT)
 
 METRIC = "MLUPS (coupled IB-LBM step) + membrane vertex-updates/s, FP16/FP32 storage vs FP64, 1 GB300"
-# algorithmic bytes per lattice update of the coupled collide-and-stream kernel: populations
-# read + written, spread force read, previous force read + reset, velocity field written
-BYTES_PER_LU = {"f64": 19 * 8 * 2 + 4 * 3 * 8, "f32": 19 * 4 * 2 + 4 * 3 * 4, "f16": 19 * 2 * 2 + 4 * 3 * 4}
+# Algorithmic bytes per lattice update of the coupled collide-and-stream (the roofline's
+# `achieved`): 19 populations read and written, the spread force read, the velocity field
+# written (FP32 fields for FP32 / FP16 storage, FP64 for FP64); no phase byte at viscosity
+# ratio 1.
+BYTES_PER_LU = {"f64": 19 * 8 * 2 + 2 * 3 * 8, "f32": 19 * 4 * 2 + 2 * 3 * 4, "f16": 19 * 2 * 2 + 2 * 3 * 4}
+# Steps of the precision comparison: the run lengths of the benchmark configurations
+COMPARE_STEPS = {"channel": 2000, "capsule": 2000, "rbc": 5000}
 
 
 def env_rank():
@@ -74,8 +78,64 @@ class Ranks:
         return float(t.item())
 
 
+class _Nvml:
+    """Read-only NVML queries through ctypes (the SM clock, its maximum and the active clock
+    event reasons); nothing is set.  None when the library is absent."""
+
+    # nvmlClocksEventReason* bits
+    REASONS = {0x4: "sw_power_cap", 0x8: "hw_slowdown", 0x20: "sw_thermal_slowdown", 0x40: "hw_thermal_slowdown",
+               0x80: "hw_power_brake_slowdown"}
+
+    def __init__(self, index):
+        import ctypes as C
+
+        self.C = C
+        self.lib = C.CDLL("libnvidia-ml.so.1")
+        if self.lib.nvmlInit_v2() != 0:
+            raise OSError("nvmlInit failed")
+        self.h = C.c_void_p()
+        uuid = _cuda_uuid(index)
+        if not (uuid and self.lib.nvmlDeviceGetHandleByUUID(uuid.encode(), C.byref(self.h)) == 0):
+            if self.lib.nvmlDeviceGetHandleByIndex_v2(C.c_uint(_nvml_index(index)), C.byref(self.h)) != 0:
+                raise OSError("no NVML device for CUDA device %d" % index)
+        reasons = getattr(self.lib, "nvmlDeviceGetCurrentClocksEventReasons", None)
+        self._reasons = reasons or self.lib.nvmlDeviceGetCurrentClocksThrottleReasons
+        v = C.c_uint()
+        self.max_mhz = float(v.value) if self.lib.nvmlDeviceGetMaxClockInfo(self.h, 1, C.byref(v)) == 0 else None
+
+    def sample(self):
+        C = self.C
+        mhz, bits = C.c_uint(), C.c_ulonglong()
+        if self.lib.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) != 0:  # NVML_CLOCK_SM
+            return None
+        if self._reasons(self.h, C.byref(bits)) != 0:
+            bits.value = 0
+        return float(mhz.value), int(bits.value)
+
+
+def _cuda_uuid(device):
+    """NVML's name ("GPU-<uuid>") of CUDA device `device`, or None."""
+    try:
+        import torch
+
+        u = getattr(torch.cuda.get_device_properties(device), "uuid", None)
+        return None if u is None else "GPU-" + str(u)
+    except Exception:
+        return None
+
+
+def _nvml_index(device):
+    vis = os.environ.get("CUDA_VISIBLE_DEVICES", "")
+    ids = [v.strip() for v in vis.split(",") if v.strip()]
+    if ids and all(v.isdigit() for v in ids) and device < len(ids):
+        return int(ids[device])
+    return device
+
+
 class ClockSampler:
-    """nvidia-smi clocks / throttle reasons sampled every 100 ms while running."""
+    """SM clock and clock event reasons sampled every 2 ms while running (NVML, read only),
+    with one sample right at the start and one at the end; nvidia-smi every 100 ms where
+    NVML cannot be loaded."""
 
     FIELDS = ["index", "clocks.sm", "clocks.max.sm", "power.draw", "clocks_event_reasons.active",
               "clocks_event_reasons.hw_slowdown", "clocks_event_reasons.hw_thermal_slowdown",
@@ -83,23 +143,49 @@ class ClockSampler:
 
     def __init__(self, device):
         self.device, self.proc, self.lines = device, None, []
+        self.nvml, self.samples, self.stop = None, [], threading.Event()
+        self.source = "unsampled"
 
     def __enter__(self):
+        try:
+            self.nvml = _Nvml(self.device)
+            self.source = "nvml"
+        except (OSError, AttributeError):
+            self.nvml = None
+        if self.nvml is not None:
+            self._take()
+            self.t = threading.Thread(target=self._poll, daemon=True)
+            self.t.start()
+            return self
         try:
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + ",".join(self.FIELDS),
                                           "--format=csv,noheader,nounits", "-lms", "100"], stdout=subprocess.PIPE,
                                          stderr=subprocess.DEVNULL, text=True)
+            self.source = "nvidia-smi"
             self.t = threading.Thread(target=self._read, daemon=True)
             self.t.start()
         except OSError:
             self.proc = None
         return self
 
+    def _take(self):
+        s = self.nvml.sample()
+        if s is not None:
+            self.samples.append(s)
+
+    def _poll(self):
+        while not self.stop.wait(0.002):
+            self._take()
+
     def _read(self):
         for line in self.proc.stdout:
             self.lines.append(line.strip())
 
     def __exit__(self, *exc):
+        if self.nvml is not None:
+            self.stop.set()
+            self.t.join(timeout=2)
+            self._take()
         if self.proc:
             self.proc.terminate()
             try:
@@ -110,6 +196,11 @@ class ClockSampler:
 
     def summary(self):
         sm, mx, reasons = [], [], set()
+        if self.nvml is not None:
+            for mhz, bits in self.samples:
+                sm.append(mhz)
+                reasons.update(nm for b, nm in _Nvml.REASONS.items() if bits & b)
+            mx = [self.nvml.max_mhz] if self.nvml.max_mhz else sm
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
         for ln in self.lines:
             p = [x.strip() for x in ln.split(",")]
@@ -124,9 +215,9 @@ class ClockSampler:
                 if p[5 + k].lower().startswith("active"):
                     reasons.add(nm)
         if not sm:
-            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0, "source": self.source}
         return {"sm_mhz": float(np.median(sm)), "sm_max_mhz": float(max(mx)), "reasons": sorted(reasons),
-                "samples": len(sm)}
+                "samples": len(sm), "source": self.source}
 
 
 def build_instance(bib, ctx, wl, storage):
@@ -149,8 +240,9 @@ def taylor_and_volume(bib, fsi, wl):
     return pos.reshape(-1, nv, 3), stats, V0
 
 
-def cpu_sample(wl, steps):
-    """The oracle (CPU port of the reference's step) on the same instance, all host threads."""
+def cpu_sample(wl, steps, warmup=1):
+    """The oracle (CPU port of the reference's step) on the same instance, all host threads:
+    `warmup` untimed coupled steps, then `steps` timed ones."""
     from oracle import oracle as O
 
     nx, ny, nz = wl["dims"]
@@ -159,12 +251,16 @@ def cpu_sample(wl, steps):
                   wall_y=lp.get("wall_y", "none"), wall_z=lp.get("wall_z", "none"), wall_u=lp.get("wall_u"))
     S = O.System(L, "roma", -1.0)
     if wl.get("initial_velocity") is not None:
-        S.f[...] = O.init_equilibrium(L, None, wl["initial_velocity"])
+        f0 = O.init_equilibrium(L, None, wl["initial_velocity"])
+        if lp.get("wall_y") == "fd_velocity":
+            f0 = O.apply_fd_walls(L, f0, np.zeros((3, nz, ny, nx)))
+        S.f[...] = f0
     S.set_body_force(np.asarray(lp.get("body_force", (0, 0, 0)), dtype=np.float64))
     sid = S.add_shape(wl["rest"], wl["tri"])
     for pos in wl["positions"]:
         S.add_particle(sid, wl["model"], wl["params"], pos)
-    S.step(1)  # warm-up
+    if warmup:
+        S.step(warmup)
     t0 = time.perf_counter()
     S.step(steps)
     dt = time.perf_counter() - t0
@@ -173,22 +269,37 @@ def cpu_sample(wl, steps):
     return dict(mlups=cells * steps / dt / 1e6, vups=nvt * steps / dt, seconds=dt, steps=steps, threads=O.threads())
 
 
+def workload_config(wl, storage, world=1):
+    """The `config` object of a bench line (the same for both arms)."""
+    nx, ny, nz = wl["dims"]
+    cells = nx * ny * nz
+    walls = {"halfway_bb": "halfway bounce-back", "fd_velocity": "finite-difference velocity walls"}
+    lp = wl["lattice"]
+    wall_txt = ", ".join("%s %s" % (walls.get(lp.get(k), lp.get(k)), k[-1]) for k in ("wall_y", "wall_z")
+                         if lp.get(k, "none") not in ("none", None))
+    return {"workload": wl["name"], "cells": cells, "vertices": int(wl["positions"].size // 3), "storage": storage,
+            "collision": "BGK + Guo forcing", "walls": wall_txt or "none", "dirac": "Roma 3-point",
+            "l2": "populations %.0f MB > 129 MB L2, no flush" % (cells * 19 * 2 * {"f16": 2, "f32": 4, "f64": 8}[storage] / 1e6),
+            "parallelism": "replicas" if world > 1 else "1 GPU"}
+
+
 def run_reference(args, wl):
+    """The reference arm: the CPU oracle (the FP64 port of the reference's coupled step) on the
+    same instance, rank 0 only, `--warmup` untimed steps then `--steps` timed ones."""
     rank, world, _ = env_rank()
     if rank != 0:
         return
     t0 = time.perf_counter()
-    for _ in range(args.warmup):
-        pass
-    r = cpu_sample(wl, max(1, args.steps))
+    r = cpu_sample(wl, max(1, args.steps), warmup=args.warmup)
     line = {
         "impl": "reference", "metric": METRIC, "value": r["mlups"], "unit": "MLUPS", "n_gpus": args.gpus,
         "steps": r["steps"], "warmup": args.warmup, "ms_per_step": 1e3 * r["seconds"] / r["steps"],
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": wl["name"], "cells": int(np.prod(wl["dims"])), "vertices": int(wl["positions"].size // 3)},
+        "config": workload_config(wl, args.storage, world),
         "vertex_updates_per_s": r["vups"],
         "cpu_baseline": {"value": r["mlups"], "unit": "MLUPS", "cores": r["threads"], "kind": "port",
-                         "sample": "%d coupled steps of the full workload after 1 warm-up step" % r["steps"]},
+                         "sample": "%d coupled FP64 steps of the full workload after %d warm-up steps"
+                                   % (r["steps"], args.warmup)},
         "e2e": {"value": r["mlups"], "unit": "MLUPS", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "wall_s": time.perf_counter() - t0,
     }
@@ -315,6 +426,8 @@ def main():
                          "rbc: one RBC in shear, 128x64x64; batch: 64 capsule instances stepped as one batch; "
                          "tgv: TRT Taylor-Green bandwidth sweep, 128^3 / 256^3 / 384^3")
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--compare-steps", type=int, default=0,
+                    help="steps of the FP64 / FP32 / FP16 comparison (default: the configuration's run length)")
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
@@ -367,6 +480,7 @@ def main():
     mlups = cells * K * world / (ms * 1e-3) / 1e6
     vups = nvt * K * world / (ms * 1e-3)
     lat.check_health()
+    kernels_per_step = fsi.kernels_per_step()
 
     # ---------------- per-kernel device time over K more steps (events between kernels)
     ctx.set_profiling(True)
@@ -396,26 +510,31 @@ def main():
     ctx.close()
     del lat, fsi
 
-    # ---------------- same-GPU variants and their error against the FP64 path
+    # ---------------- same-GPU variants and their error against the FP64 path, over the run
+    # length of the workload's configuration (independent of --steps)
     variants = {}
     if not args.no_variants:
+        n_cmp = args.compare_steps or COMPARE_STEPS.get(args.workload, 2000)
         for st in ["f64", "f32", "f16"]:
             c2 = bib.Context(0 if world == 1 else local)
             l2, f2 = build_instance(bib, c2, wl, st)
+            mass0 = cells + float(l2.receive().sum())  # rho = 1 + sum of f-bar
             f2.step(W)
             c2.sync()
-            kk = max(3, K // 2) if st == "f64" else K
+            kk = min(max(3, K // 2) if st == "f64" else K, n_cmp - W)
             t = f2.step_timed(kk)
-            f2.step(steps_main - W - kk)  # same number of steps as the main run
+            f2.step(n_cmp - W - kk)
+            l2.check_health()
             variants[st] = {"mlups": cells * kk / (t * 1e-3) / 1e6, "vertex_updates_per_s": nvt * kk / (t * 1e-3),
-                            "ms_per_step": t / kk}
+                            "ms_per_step": t / kk, "timed_steps": kk}
             pos_v, stats_v, _ = taylor_and_volume(bib, f2, wl)
             variants[st]["_u"] = l2.compute_velocity()
             variants[st]["_stats"] = stats_v
+            variants[st]["_mass"] = (mass0, cells + float(l2.receive().sum()))
             I = bib.api.moments_of_inertia(pos_v, wl["tri"])
             variants[st]["_D"] = np.array([bib.taylor_deformation(Ik) for Ik in I])
             c2.close()
-        ref_u, ref_stats = variants["f64"]["_u"], variants["f64"]["_stats"]
+        ref_u, ref_stats, ref_mass = variants["f64"]["_u"], variants["f64"]["_stats"], variants["f64"]["_mass"]
         for st in ["f32", "f16"]:
             u = variants[st]["_u"]
             variants[st]["velocity_rel_l2_vs_f64"] = float(np.linalg.norm(u - ref_u) / np.linalg.norm(ref_u))
@@ -423,14 +542,17 @@ def main():
                 np.abs(variants[st]["_stats"][:, 1] - ref_stats[:, 1]).max() / V0)
             dD = np.abs(variants[st]["_D"] - variants["f64"]["_D"])
             variants[st]["taylor_D_abs_diff_vs_f64"] = {"max": float(dD.max()), "mean": float(dD.mean())}
-        for st in variants:
-            variants[st]["volume_drift_max"] = float(np.abs(variants[st]["_stats"][:, 1] - V0).max() / V0)
-            variants[st]["taylor_D_mean"] = float(variants[st]["_D"].mean())
-            variants[st].pop("_u")
-            variants[st].pop("_stats")
-            variants[st].pop("_D")
-        variants["steps_compared"] = steps_main
+            variants[st]["mass_rel_diff_vs_f64"] = float((variants[st]["_mass"][1] - ref_mass[1]) / ref_mass[0])
+        for st in ["f64", "f32", "f16"]:
+            v = variants[st]
+            v["volume_drift_max"] = float(np.abs(v["_stats"][:, 1] - V0).max() / V0)
+            v["taylor_D_mean"] = float(v["_D"].mean())
+            v["mass_drift_rel"] = float((v["_mass"][1] - v["_mass"][0]) / v["_mass"][0])
+            for key in ("_u", "_stats", "_D", "_mass"):
+                v.pop(key)
+        variants["steps_compared"] = n_cmp
         variants["f64"]["speedup_f16_over_f64"] = variants["f16"]["mlups"] / variants["f64"]["mlups"]
+        variants["f64"]["speedup_f32_over_f64"] = variants["f32"]["mlups"] / variants["f64"]["mlups"]
 
     # ---------------- end to end through the C ABI with host buffers
     e2e = None
@@ -492,8 +614,19 @@ def main():
         dt = max_over_ranks(dt)
         h2d = f_host.nbytes + pos_host.nbytes
         d2h = K * stats_out.nbytes + pos_out.nbytes + f_out.nbytes
+        # the population transfers alone (after the timed region), pinned and pageable
+        tx = {}
+        pageable = np.zeros_like(f_out)
+        for name, buf in (("pinned", f_out), ("pageable", pageable)):
+            t1 = time.perf_counter()
+            c3.check(lib.bib_lattice_send(h, l3.h, buf.ctypes.data, buf.nbytes, 0))
+            t2 = time.perf_counter()
+            c3.check(lib.bib_lattice_receive(h, l3.h, buf.ctypes.data, buf.nbytes, 0))
+            t3 = time.perf_counter()
+            tx["send_gbs_" + name] = buf.nbytes / (t2 - t1) / 1e9
+            tx["receive_gbs_" + name] = buf.nbytes / (t3 - t2) / 1e9
         e2e = {"value": cells * K * world / dt / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": int(h2d // K),
-               "d2h_bytes_per_step": int(d2h // K),
+               "d2h_bytes_per_step": int(d2h // K), "seconds": dt, **tx,
                "what": "bib_lattice_send of the FP64 initial populations + bib_particles_upload of the vertex positions, K x (bib_step + "
                        "bib_particles_download_async of the per-cell area/volume/centre, waited for one step "
                        "later), final download of all "
@@ -527,16 +660,14 @@ def main():
         "vs_baseline": None,
         "dtype": "f32" if args.storage != "f64" else "f64",
         "data": "synthetic (seeded: RBC positions/orientations seed %d)" % wl["seed"],
-        "config": {"workload": wl["name"], "cells": cells, "vertices": nvt, "storage": args.storage,
-                   "collision": "BGK + Guo forcing", "walls": "halfway bounce-back y,z" if args.workload == "channel"
-                   else "finite-difference velocity walls y", "dirac": "Roma 3-point",
-                   "l2": "populations %.0f MB > 129 MB L2, no flush" % (cells * 19 * 2 * {"f16": 2, "f32": 4, "f64": 8}[args.storage] / 1e6),
-                   "parallelism": "replicas" if world > 1 else "1 GPU"},
+        "config": workload_config(wl, args.storage, world),
         "vertex_updates_per_s": vups,
+        # a second pass of K plain (not graph-replayed) steps with events between the kernels
         "kernel_ms_per_step": {k: v / K for k, v in prof.items()},
-        # per coupled step: membrane forces, spreading, collide-and-stream, interpolation + move,
-        # area / volume / centre update, and the finite-difference wall kernel where there are such walls
-        "gpu_launches": int(K * ((4 if nvt else 0) + 1 + (1 if wl["lattice"].get("wall_y") == "fd_velocity" else 0))),
+        "kernel_ms_source": "separate pass of K eager steps, CUDA events between kernels (sums above the graph step)",
+        # kernel nodes of the replayed step graph (the library's count) x K
+        "gpu_launches": int(K * kernels_per_step),
+        "kernels_per_step": kernels_per_step,
         "roofline": {"bound": "hbm", "kernel": kernel[args.storage], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_cell": bytes_lu,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},

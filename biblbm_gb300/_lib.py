@@ -120,6 +120,7 @@ SIGNATURES = {
     "bib_checkpoint_load": (C.c_int32, [_vp, C.c_int32, C.c_char_p]),
     "bib_step": (C.c_int32, [_vp, C.c_int32, C.c_int64]),
     "bib_step_timed": (C.c_int32, [_vp, C.c_int32, C.c_int64, _dp]),
+    "bib_step_kernel_count": (C.c_int32, [_vp, C.c_int32, _i32p]),
     "bib_check_health": (C.c_int32, [_vp, C.c_int32]),
     "bib_lattice_set_tuning": (C.c_int32, [_vp, C.c_int32, C.POINTER(Tuning)]),
     "bib_lattice_set_cell_types": (C.c_int32, [_vp, C.c_int32, _vp]),

@@ -530,6 +530,12 @@ class ImmersedBoundaryDynamics3D:
         self.ctx.check(self.ctx.lib.bib_step_timed(self.ctx.h, self.lattice.h, int(nsteps), C.byref(ms)))
         return ms.value
 
+    def kernels_per_step(self) -> int:
+        """Kernel launches of one coupled step, counted in the step's captured CUDA graph."""
+        n = C.c_int32()
+        self.ctx.check(self.ctx.lib.bib_step_kernel_count(self.ctx.h, self.lattice.h, C.byref(n)))
+        return n.value
+
 
 def moments_of_inertia(pos, tri) -> np.ndarray:
     """Moment-of-inertia tensors of closed meshes, vectorised over particles.

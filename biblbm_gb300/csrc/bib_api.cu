@@ -20,6 +20,7 @@ using namespace bib;
 struct GraphEntry {
     cudaGraphExec_t exec = nullptr;
     int cur = 0, pcur = 0;
+    int kernels = 0;  // kernel nodes of the captured graph
 };
 
 struct Batch;
@@ -37,8 +38,12 @@ struct bib_ctx {
     cudaEvent_t dl_ev[8] = {};  // completion of the asynchronous downloads, one per slot
     int* d_flag = nullptr;
     std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, steps and parity) -> step graph
-    double* stage = nullptr;  // device staging area of the host <-> device population transfers
-    size_t stage_count = 0;   // its size in doubles
+    // population transfers with pageable host buffers: two device staging halves filled and
+    // drained on a copy stream while the import / export kernels work on the other half
+    double* stage = nullptr;
+    size_t stage_count = 0;   // size of both halves in doubles
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t tx_ready[2] = {}, tx_free[2] = {}, tx_start = nullptr;
     std::vector<std::unique_ptr<Batch>> batches;
     ~bib_ctx();
 };
@@ -596,6 +601,17 @@ bib_status step_graph(bib_ctx* c, Lattice& L, int steps, cudaGraphExec_t* out) {
         L.fe = fe0;
         L.target_clean = clean0;
         if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
+        size_t nn = 0;
+        if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
+            std::vector<cudaGraphNode_t> nodes(nn);
+            if (cudaGraphGetNodes(g, nodes.data(), &nn) == cudaSuccess) {
+                ge.kernels = 0;
+                for (size_t k = 0; k < nn; ++k) {
+                    cudaGraphNodeType t;
+                    if (cudaGraphNodeGetType(nodes[k], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++ge.kernels;
+                }
+            }
+        }
         e = cudaGraphInstantiate(&ge.exec, g, 0);
         cudaGraphDestroy(g);
         if (e != cudaSuccess) {
@@ -664,59 +680,168 @@ bib_status pull_particles(bib_ctx* c, Lattice& L) {
     return BIB_OK;
 }
 
-// Population transfers stream whole z-planes through a staging area of about 32 MB (at least
-// one plane of all 19 populations, at most the lattice), allocated once per context.  (512 MB
-// chunks measured no faster on the 512 x 128 x 128 channel.)
-constexpr size_t kStageTarget = (size_t)4 << 20;  // doubles
+// ---- host <-> device population transfers (bib_lattice_send / _receive)
+//
+// Page-locked host buffers (cudaHostAlloc, cudaMallocHost, cudaHostRegister: with unified
+// addressing the device reaches them at an address it is told by cudaPointerGetAttributes) are
+// read and written by the import / export kernels themselves, in one pass over the lattice that
+// streams over the CPU-GPU link.  Pageable buffers go through two device staging halves: the
+// copies of one chunk run on a copy stream while the kernel converts the other chunk.
+//
+// A transfer in wire order: structure of arrays (19 arrays of n doubles, x fastest; chunks of
+// z-planes) or cell-major (`per` doubles per cell, z fastest and x slowest; chunks of x-planes).
+struct Wire {
+    int per;   // 0: structure of arrays; 19 or 23: doubles per cell, cell-major
+};
 
-bib_status plane_chunk(bib_ctx* c, const Lattice& L, int* planes) {
-    const size_t plane = (size_t)Q * L.d.nx * L.d.ny;
-    const size_t want = plane * std::max<size_t>(1, std::min<size_t>(kStageTarget / plane, (size_t)L.d.nz));
-    if (c->stage_count < want) {
+// Device address of the host range [p, p + bytes) if the device can access it directly
+// (page-locked memory mapped into the unified address space, both ends of one mapping), else null.
+const void* device_view_of_host(const void* p, size_t bytes) {
+    if (!p || bytes == 0) return nullptr;
+    cudaPointerAttributes a{}, b{};
+    if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (a.type != cudaMemoryTypeHost || !a.devicePointer) return nullptr;
+    const char* last = static_cast<const char*>(p) + (bytes - 1);
+    if (cudaPointerGetAttributes(&b, last) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    if (b.type != cudaMemoryTypeHost || !b.devicePointer) return nullptr;
+    if (static_cast<const char*>(b.devicePointer) - static_cast<const char*>(a.devicePointer) != (ptrdiff_t)(bytes - 1))
+        return nullptr;
+    return a.devicePointer;
+}
+
+// Staging halves of at least one chunk unit (a z-plane of 19 populations, or an x-plane of
+// cells) and about 32 MB each; the copy stream and its events are made on first use.
+constexpr size_t kStageHalf = (size_t)4 << 20;  // doubles
+
+bib_status transfer_setup(bib_ctx* c, size_t unit, int64_t units, int64_t* per_chunk) {
+    if (!c->copy_stream) {
+        BIB_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream, cudaStreamNonBlocking));
+        for (int k = 0; k < 2; ++k) {
+            BIB_CUDA(c, cudaEventCreateWithFlags(&c->tx_ready[k], cudaEventDisableTiming));
+            BIB_CUDA(c, cudaEventCreateWithFlags(&c->tx_free[k], cudaEventDisableTiming));
+        }
+        BIB_CUDA(c, cudaEventCreateWithFlags(&c->tx_start, cudaEventDisableTiming));
+    }
+    const size_t half = unit * std::max<size_t>(1, std::min<size_t>(kStageHalf / unit, (size_t)units));
+    if (c->stage_count < 2 * half) {
+        BIB_CUDA(c, cudaStreamSynchronize(c->stream));
         cudaFree(c->stage);
         c->stage = nullptr;
         c->stage_count = 0;
-        BIB_CUDA(c, cudaMalloc((void**)&c->stage, want * sizeof(double)));
-        c->stage_count = want;
+        BIB_CUDA(c, cudaMalloc((void**)&c->stage, 2 * half * sizeof(double)));
+        c->stage_count = 2 * half;
     }
-    *planes = (int)std::min<size_t>(c->stage_count / plane, (size_t)L.d.nz);
+    *per_chunk = (int64_t)std::min<size_t>(c->stage_count / 2 / unit, (size_t)units);
     return BIB_OK;
 }
 
-// Host SoA populations (19 arrays of n doubles) -> lattice state, chunk by chunk: 19 copies
-// into the staging area, then the import of those planes, in stream order.
-bib_status import_populations(bib_ctx* c, Lattice& L, const double* src) {
-    int P = 0;
-    bib_status st = plane_chunk(c, L, &P);
-    if (st) return st;
-    const int64_t n = L.d.n, plane = (int64_t)L.d.nx * L.d.ny;
-    for (int z0 = 0; z0 < L.d.nz; z0 += P) {
-        const int nzc = std::min(P, L.d.nz - z0);
-        const int64_t cc = plane * nzc;
-        for (int i = 0; i < Q; ++i)
-            BIB_CUDA(c, cudaMemcpyAsync(c->stage + i * cc, src + i * n + z0 * plane, cc * sizeof(double),
-                                        cudaMemcpyHostToDevice, c->stream));
-        launch_import_planes(L, c->stage, z0, nzc, cc, c->stream);
+// Host populations in wire order -> lattice state (for the Palabos order also the force and
+// the phase), in stream order; returns once the host buffer has been read.
+bib_status import_populations(bib_ctx* c, Lattice& L, const double* src, Wire w) {
+    const LatticeDesc& d = L.d;
+    const int64_t n = d.n, plane = (int64_t)d.nx * d.ny, xplane = (int64_t)d.ny * d.nz;
+    const size_t bytes = (size_t)(w.per ? w.per : Q) * n * sizeof(double);
+    if (const double* m = static_cast<const double*>(device_view_of_host(src, bytes))) {
+        if (w.per) launch_import_aos(L, m, w.per, 0, n, c->stream);
+        else launch_import_planes(L, m, 0, d.nz, n, c->stream);
         BIB_CHECK_LAUNCH(c);
+        BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+        return BIB_OK;
     }
+    int64_t P = 0;
+    const size_t unit = w.per ? (size_t)w.per * xplane : (size_t)Q * plane;
+    bib_status st = transfer_setup(c, unit, w.per ? d.nx : d.nz, &P);
+    if (st) return st;
+    const size_t half = c->stage_count / 2;
+    // the copies must not overtake earlier work of the main stream on the staging area
+    BIB_CUDA(c, cudaEventRecord(c->tx_start, c->stream));
+    BIB_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->tx_start, 0));
+    const int64_t total = w.per ? d.nx : d.nz;
+    int k = 0;
+    for (int64_t a = 0; a < total; a += P, ++k) {
+        const int64_t cnt = std::min<int64_t>(P, total - a);
+        double* buf = c->stage + (size_t)(k & 1) * half;
+        if (k >= 2) BIB_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->tx_free[k & 1], 0));
+        if (w.per) {
+            BIB_CUDA(c, cudaMemcpyAsync(buf, src + (size_t)w.per * a * xplane, (size_t)w.per * cnt * xplane * sizeof(double),
+                                        cudaMemcpyHostToDevice, c->copy_stream));
+        } else {
+            const int64_t cc = plane * cnt;
+            for (int i = 0; i < Q; ++i)
+                BIB_CUDA(c, cudaMemcpyAsync(buf + i * cc, src + i * n + a * plane, cc * sizeof(double),
+                                            cudaMemcpyHostToDevice, c->copy_stream));
+        }
+        BIB_CUDA(c, cudaEventRecord(c->tx_ready[k & 1], c->copy_stream));
+        BIB_CUDA(c, cudaStreamWaitEvent(c->stream, c->tx_ready[k & 1], 0));
+        if (w.per) launch_import_aos(L, buf, w.per, a * xplane, cnt * xplane, c->stream);
+        else launch_import_planes(L, buf, (int)a, (int)cnt, plane * cnt, c->stream);
+        BIB_CHECK_LAUNCH(c);
+        BIB_CUDA(c, cudaEventRecord(c->tx_free[k & 1], c->stream));
+    }
+    BIB_CUDA(c, cudaStreamSynchronize(c->copy_stream));
     return BIB_OK;
 }
 
-// Lattice state -> host SoA populations, chunk by chunk.
-bib_status export_populations(bib_ctx* c, Lattice& L, double* dst) {
-    int P = 0;
-    bib_status st = plane_chunk(c, L, &P);
-    if (st) return st;
-    const int64_t n = L.d.n, plane = (int64_t)L.d.nx * L.d.ny;
-    for (int z0 = 0; z0 < L.d.nz; z0 += P) {
-        const int nzc = std::min(P, L.d.nz - z0);
-        const int64_t cc = plane * nzc;
-        launch_export_planes(L, c->stage, z0, nzc, cc, c->stream);
+// Lattice state -> host populations in wire order (Palabos order: with the force and the
+// phase); returns once the host buffer holds them.
+bib_status export_populations(bib_ctx* c, Lattice& L, double* dst, Wire w) {
+    const LatticeDesc& d = L.d;
+    const int64_t n = d.n, plane = (int64_t)d.nx * d.ny, xplane = (int64_t)d.ny * d.nz;
+    const size_t bytes = (size_t)(w.per ? w.per : Q) * n * sizeof(double);
+    if (double* m = static_cast<double*>(const_cast<void*>(device_view_of_host(dst, bytes)))) {
+        if (w.per) launch_export_aos(L, m, w.per, 0, n, c->stream);
+        else launch_export_planes(L, m, 0, d.nz, n, c->stream);
         BIB_CHECK_LAUNCH(c);
-        for (int i = 0; i < Q; ++i)
-            BIB_CUDA(c, cudaMemcpyAsync(dst + i * n + z0 * plane, c->stage + i * cc, cc * sizeof(double),
-                                        cudaMemcpyDeviceToHost, c->stream));
+        BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+        return BIB_OK;
     }
+    int64_t P = 0;
+    const size_t unit = w.per ? (size_t)w.per * xplane : (size_t)Q * plane;
+    bib_status st = transfer_setup(c, unit, w.per ? d.nx : d.nz, &P);
+    if (st) return st;
+    const size_t half = c->stage_count / 2;
+    const int64_t total = w.per ? d.nx : d.nz;
+    const int nchunks = (int)((total + P - 1) / P);
+    auto convert = [&](int k) -> bib_status {
+        const int64_t a = (int64_t)k * P, cnt = std::min<int64_t>(P, total - a);
+        double* buf = c->stage + (size_t)(k & 1) * half;
+        if (k >= 2) BIB_CUDA(c, cudaStreamWaitEvent(c->stream, c->tx_free[k & 1], 0));
+        if (w.per) launch_export_aos(L, buf, w.per, a * xplane, cnt * xplane, c->stream);
+        else launch_export_planes(L, buf, (int)a, (int)cnt, plane * cnt, c->stream);
+        BIB_CHECK_LAUNCH(c);
+        BIB_CUDA(c, cudaEventRecord(c->tx_ready[k & 1], c->stream));
+        return BIB_OK;
+    };
+    // the kernel of chunk k + 1 is queued before the copies of chunk k: a copy into pageable
+    // memory returns only when it is done, and the kernel runs meanwhile
+    st = convert(0);
+    if (st) return st;
+    for (int k = 0; k < nchunks; ++k) {
+        if (k + 1 < nchunks) {
+            st = convert(k + 1);
+            if (st) return st;
+        }
+        const int64_t a = (int64_t)k * P, cnt = std::min<int64_t>(P, total - a);
+        const double* buf = c->stage + (size_t)(k & 1) * half;
+        BIB_CUDA(c, cudaStreamWaitEvent(c->copy_stream, c->tx_ready[k & 1], 0));
+        if (w.per) {
+            BIB_CUDA(c, cudaMemcpyAsync(dst + (size_t)w.per * a * xplane, buf, (size_t)w.per * cnt * xplane * sizeof(double),
+                                        cudaMemcpyDeviceToHost, c->copy_stream));
+        } else {
+            const int64_t cc = plane * cnt;
+            for (int i = 0; i < Q; ++i)
+                BIB_CUDA(c, cudaMemcpyAsync(dst + i * n + a * plane, buf + i * cc, cc * sizeof(double),
+                                            cudaMemcpyDeviceToHost, c->copy_stream));
+        }
+        BIB_CUDA(c, cudaEventRecord(c->tx_free[k & 1], c->copy_stream));
+    }
+    BIB_CUDA(c, cudaStreamSynchronize(c->copy_stream));
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     return BIB_OK;
 }
@@ -1085,7 +1210,14 @@ void bib_destroy(bib_ctx* c) {
     for (int k = 0; k < 8; ++k)
         if (c->dl_ev[k]) cudaEventDestroy(c->dl_ev[k]);
     cudaFree(c->d_flag);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     cudaFree(c->stage);
+    for (int k = 0; k < 2; ++k) {
+        if (c->tx_ready[k]) cudaEventDestroy(c->tx_ready[k]);
+        if (c->tx_free[k]) cudaEventDestroy(c->tx_free[k]);
+    }
+    if (c->tx_start) cudaEventDestroy(c->tx_start);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1514,43 +1646,15 @@ bib_status bib_lattice_send(bib_ctx* c, int32_t h, const void* buf, size_t bytes
     Lattice* L = get_lattice(c, h);
     if (!L || !buf) return fail(c, BIB_EINVAL, "invalid lattice handle or buffer");
     const int64_t n = L->d.n;
-    std::vector<double> soa;
-    const double* src = (const double*)buf;
-    std::vector<double> ext;
-    if (layout == BIB_LAYOUT_SOA_F64) {
-        if (bytes != (size_t)Q * n * sizeof(double)) return fail(c, BIB_EINVAL, "expected %zu bytes", (size_t)Q * n * 8);
-    } else if (layout == BIB_LAYOUT_PALABOS_F64 || layout == BIB_LAYOUT_COPROCESSOR_F64) {
-        const int per = layout == BIB_LAYOUT_PALABOS_F64 ? 23 : Q;
-        if (bytes != (size_t)per * n * sizeof(double)) return fail(c, BIB_EINVAL, "expected %zu bytes", (size_t)per * n * 8);
-        soa.resize(Q * n);
-        if (per == 23) ext.resize(4 * n);
-        const LatticeDesc& d = L->d;
-        int64_t w = 0;
-        for (int x = 0; x < d.nx; ++x)
-            for (int y = 0; y < d.ny; ++y)
-                for (int z = 0; z < d.nz; ++z, ++w) {
-                    const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
-                    for (int i = 0; i < Q; ++i) soa[i * n + k] = src[per * w + i];
-                    if (per == 23)
-                        for (int a = 0; a < 4; ++a) ext[a * n + k] = src[per * w + Q + a];
-                }
-        src = soa.data();
-    } else {
-        return fail(c, BIB_EINVAL, "unknown layout %d", layout);
-    }
-    bib_status st = import_populations(c, *L, src);
+    Wire w{0};
+    if (layout == BIB_LAYOUT_PALABOS_F64) w.per = Q + 4;
+    else if (layout == BIB_LAYOUT_COPROCESSOR_F64) w.per = Q;
+    else if (layout != BIB_LAYOUT_SOA_F64) return fail(c, BIB_EINVAL, "unknown layout %d", layout);
+    const size_t want = (size_t)(w.per ? w.per : Q) * n * sizeof(double);
+    if (bytes != want) return fail(c, BIB_EINVAL, "expected %zu bytes", want);
+    bib_status st = import_populations(c, *L, static_cast<const double*>(buf), w);
     if (st) return st;
-    if (!ext.empty()) {
-        double* dF = nullptr;
-        st = device_buffer(c, &dF, ext.data(), 4 * n);
-        if (st) return st;
-        launch_force_import(*L, L->fe, dF, c->stream);
-        L->target_clean = false;
-        if (L->phase) launch_phase_import(*L, dF + 3 * n, c->stream);
-        BIB_CUDA(c, cudaStreamSynchronize(c->stream));
-        cudaFree(dF);
-    }
-    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (w.per == Q + 4) L->target_clean = false;  // the force of the cells became the current external force
     return BIB_OK;
 }
 
@@ -1563,37 +1667,7 @@ bib_status bib_lattice_receive(bib_ctx* c, int32_t h, void* buf, size_t bytes, i
     if (layout != BIB_LAYOUT_SOA_F64 && layout != BIB_LAYOUT_PALABOS_F64 && layout != BIB_LAYOUT_COPROCESSOR_F64)
         return fail(c, BIB_EINVAL, "unknown layout");
     if (bytes != want) return fail(c, BIB_EINVAL, "expected %zu bytes", want);
-    if (layout == BIB_LAYOUT_SOA_F64) return export_populations(c, *L, (double*)buf);
-    std::vector<double> host((Q + 3) * n);
-    bib_status st = export_populations(c, *L, host.data());
-    if (st) return st;
-    double* d = nullptr;
-    st = device_buffer(c, &d, nullptr, 3 * n);
-    if (st) return st;
-    launch_force_export(*L, L->fe, d, c->stream);
-    BIB_CHECK_LAUNCH(c);
-    BIB_CUDA(c, cudaMemcpyAsync(host.data() + Q * n, d, 3 * n * sizeof(double), cudaMemcpyDeviceToHost, c->stream));
-    std::vector<uint8_t> phase;  // the phase external (0 without a phase field)
-    if (per == 23 && L->phase) {
-        phase.resize((size_t)n);
-        BIB_CUDA(c, cudaMemcpyAsync(phase.data(), L->phase, phase.size(), cudaMemcpyDeviceToHost, c->stream));
-    }
-    BIB_CUDA(c, cudaStreamSynchronize(c->stream));
-    cudaFree(d);
-    double* dst = (double*)buf;
-    const LatticeDesc& dd = L->d;
-    int64_t w = 0;
-    for (int x = 0; x < dd.nx; ++x)
-        for (int y = 0; y < dd.ny; ++y)
-            for (int z = 0; z < dd.nz; ++z, ++w) {
-                const int64_t k = x + (int64_t)dd.nx * (y + (int64_t)dd.ny * z);
-                for (int i = 0; i < Q; ++i) dst[per * w + i] = host[i * n + k];
-                if (per == 23) {
-                    for (int a = 0; a < 3; ++a) dst[per * w + Q + a] = host[(Q + a) * n + k];
-                    dst[per * w + 22] = phase.empty() ? 0.0 : (phase[k] ? 1.0 : 0.0);
-                }
-            }
-    return BIB_OK;
+    return export_populations(c, *L, static_cast<double*>(buf), Wire{layout == BIB_LAYOUT_SOA_F64 ? 0 : per});
 }
 
 bib_status bib_lattice_collide_and_stream(bib_ctx* c, int32_t h, int64_t nsteps) {
@@ -2036,6 +2110,21 @@ bib_status bib_step_timed(bib_ctx* c, int32_t h, int64_t nsteps, double* ms) {
     cudaEventDestroy(b);
     *ms = f;
     return st;
+}
+
+bib_status bib_step_kernel_count(bib_ctx* c, int32_t h, int32_t* kernels_per_step) {
+    if (!c || !kernels_per_step) return fail(c, BIB_EINVAL, "null argument");
+    if (!get_lattice(c, h)) return fail(c, BIB_EINVAL, "invalid lattice handle %d", h);
+    // two-step graphs hold two steps; one-step graphs one
+    int best = -1;
+    for (const auto& kv : c->graphs)
+        if (kv.first.first == h && kv.second.exec) {
+            const int steps = kv.first.second >= 8 ? 2 : 1;
+            best = std::max(best, (kv.second.kernels + steps - 1) / steps);
+        }
+    if (best < 0) return fail(c, BIB_EINVAL, "lattice %d has no captured step graph yet", h);
+    *kernels_per_step = best;
+    return BIB_OK;
 }
 
 bib_status bib_check_health(bib_ctx* c, int32_t h) {

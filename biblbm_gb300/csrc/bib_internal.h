@@ -281,6 +281,11 @@ void launch_init_equilibrium(const Lattice& L, const double* rho, const double* 
 // populations of planes z0 .. z0 + nzc - 1 from / to FP64 SoA slices of `pitch` cells
 void launch_import_planes(const Lattice& L, const double* src, int z0, int nzc, int64_t pitch, cudaStream_t s);
 void launch_export_planes(const Lattice& L, double* dst, int z0, int nzc, int64_t pitch, cudaStream_t s);
+// cells w0 .. w0 + count - 1 of the cell-major wire order (x slowest, z fastest), `per` doubles
+// per cell: 19 populations (CoProcessor3D) or 19 populations, the force and the phase (Palabos
+// static content; the force goes to / comes from F[fe])
+void launch_import_aos(const Lattice& L, const double* src, int per, int64_t w0, int64_t count, cudaStream_t s);
+void launch_export_aos(const Lattice& L, double* dst, int per, int64_t w0, int64_t count, cudaStream_t s);
 void launch_force_import(const Lattice& L, int buf, const double* src, cudaStream_t s);
 void launch_force_export(const Lattice& L, int buf, double* dst, cudaStream_t s);
 void launch_force_fill(const Lattice& L, int buf, cudaStream_t s);

@@ -482,6 +482,51 @@ __global__ void k_export(LatticeDesc d, const T* __restrict__ f, const T* __rest
     for (int i = 0; i < Q; ++i) dst[i * pitch + j] = (double)fc[i];
 }
 
+// Import / export of the cells w0 .. w0 + count - 1 of the cell-major wire order of Palabos
+// (BlockLattice3D static content, blockLattice3D.hh:644-689: x slowest, z fastest; `per` = 23
+// doubles per cell: 19 f-bar, the force, the phase) and of CoProcessor3D (coProcessor3D.h:84-91:
+// the same order, `per` = 19 populations only).  `src` / `dst` hold cell w0 first.  Consecutive
+// threads take consecutive cells, so a warp reads or writes one contiguous run of the buffer; the
+// strided lattice accesses merge in L2.
+template <class T>
+__global__ void k_import_aos(LatticeDesc d, T* __restrict__ f, T* __restrict__ wall, typename Store<T>::F* __restrict__ F,
+                             uint8_t* __restrict__ phase, const double* __restrict__ src, int per, int64_t w0,
+                             int64_t count) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t w = w0 + t, r = w / d.nz;
+    const int z = (int)(w - r * d.nz), y = (int)(r % d.ny), x = (int)(r / d.ny);
+    const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+    const double* s = src + per * t;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) scatter_canonical<T>(d, f, wall, i, x, y, z, k, s[i]);
+    if (per == Q + 4) {
+        for (int a = 0; a < 3; ++a) F[a * d.stride + k] = (typename Store<T>::F)s[Q + a];
+        if (phase) phase[k] = s[Q + 3] >= 0.5 ? 1 : 0;
+    }
+}
+
+template <class T>
+__global__ void k_export_aos(LatticeDesc d, const T* __restrict__ f, const T* __restrict__ wall,
+                             const typename Store<T>::F* __restrict__ F, const uint8_t* __restrict__ phase,
+                             double* __restrict__ dst, int per, int64_t w0, int64_t count) {
+    using C = typename Store<T>::C;
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= count) return;
+    const int64_t w = w0 + t, r = w / d.nz;
+    const int z = (int)(w - r * d.nz), y = (int)(r % d.ny), x = (int)(r / d.ny);
+    const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
+    C fc[Q];
+    gather<T>(d, f, wall, x, y, z, k, fc);
+    double* o = dst + per * t;
+#pragma unroll
+    for (int i = 0; i < Q; ++i) o[i] = (double)fc[i];
+    if (per == Q + 4) {
+        for (int a = 0; a < 3; ++a) o[Q + a] = (double)F[a * d.stride + k];
+        o[Q + 3] = phase && phase[k] ? 1.0 : 0.0;
+    }
+}
+
 template <class FT>
 __global__ void k_force_import(LatticeDesc d, FT* __restrict__ F, const double* __restrict__ src) {
     const int64_t k = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
@@ -620,6 +665,20 @@ void export_t(const Lattice& L, double* dst, int z0, int nzc, int64_t pitch, cud
 }
 
 template <class T>
+void import_aos_t(const Lattice& L, const double* src, int per, int64_t w0, int64_t count, cudaStream_t s) {
+    using FT = typename Store<T>::F;
+    k_import_aos<T><<<lin_grid(count, 256), 256, 0, s>>>(L.d, (T*)L.f[L.cur], (T*)L.wall, (FT*)L.F[L.fe], L.phase, src,
+                                                         per, w0, count);
+}
+
+template <class T>
+void export_aos_t(const Lattice& L, double* dst, int per, int64_t w0, int64_t count, cudaStream_t s) {
+    using FT = typename Store<T>::F;
+    k_export_aos<T><<<lin_grid(count, 256), 256, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall,
+                                                         (const FT*)L.F[L.fe], L.phase, dst, per, w0, count);
+}
+
+template <class T>
 void nan_scan_t(const Lattice& L, int* flag, cudaStream_t s) {
     k_nan_scan<T><<<lin_grid(L.d.n, 256), 256, 0, s>>>(L.d, (const T*)L.f[L.cur], flag);
 }
@@ -663,6 +722,14 @@ void launch_import_planes(const Lattice& L, const double* src, int z0, int nzc, 
 
 void launch_export_planes(const Lattice& L, double* dst, int z0, int nzc, int64_t pitch, cudaStream_t s) {
     BIB_DISPATCH(L.storage, export_t, L, dst, z0, nzc, pitch, s);
+}
+
+void launch_import_aos(const Lattice& L, const double* src, int per, int64_t w0, int64_t count, cudaStream_t s) {
+    if (count > 0) BIB_DISPATCH(L.storage, import_aos_t, L, src, per, w0, count, s);
+}
+
+void launch_export_aos(const Lattice& L, double* dst, int per, int64_t w0, int64_t count, cudaStream_t s) {
+    if (count > 0) BIB_DISPATCH(L.storage, export_aos_t, L, dst, per, w0, count, s);
 }
 
 void launch_force_import(const Lattice& L, int buf, const double* src, cudaStream_t s) {

@@ -353,6 +353,10 @@ bib_status bib_step(bib_ctx* ctx, int32_t h, int64_t nsteps);
 bib_status bib_step_timed(bib_ctx* ctx, int32_t h, int64_t nsteps, double* ms);
 /* stream the context's work into CUDA-graph replays (1) or plain launches (0) */
 bib_status bib_set_graph_mode(bib_ctx* ctx, int32_t enabled);
+/* kernel launches in one coupled step of lattice h, counted in the CUDA graph that bib_step
+ * replays (its kernel nodes; memset nodes are not counted); BIB_EINVAL before the first
+ * graph-replayed bib_step of the lattice.  No reference counterpart (instrumentation). */
+bib_status bib_step_kernel_count(bib_ctx* ctx, int32_t h, int32_t* kernels_per_step);
 /* scan populations and vertex positions for NaN / Inf: BIB_OK or BIB_ENAN; BIB_ETIMEOUT if a
  * bounded device wait of an earlier step gave up, BIB_EOVERFLOW if an earlier voxelization met a
  * lattice column crossed by more than 64 membrane triangles or a triangle wider than the lattice
