@@ -299,6 +299,18 @@ void moment_of_inertia(const ShapeHost& S, const double* pos, double* I) {
     I[8] = in[4] + in[5] - vol * (c[0] * c[0] + c[1] * c[1]);
 }
 
+// The force fields were written outside the sparse coupled step: neither may be reset by its
+// recorded support nodes any more (the next reset of each is a dense fill).
+void forces_touched(Lattice& L) { L.sparse_ok[0] = L.sparse_ok[1] = false; }
+
+// The coupled step resets the previous force field sparsely (only where the spreading wrote)
+// on reduced-precision lattices whose velocity field near the membranes is j/rho + F/2 at
+// every node: no phase field, cell types, second-order walls or pipe boundary.
+bool sparse_coupling(const Lattice& L) {
+    return !L.dense_reset && L.storage != BIB_STORAGE_F64 && L.nvert > 0 && !L.phase && !L.celltype && L.nguo == 0 &&
+           !L.ib.has_pipe && L.spread_lo[0] && L.spread_lo[1];
+}
+
 void free_particles(Lattice& L) {
     for (int k = 0; k < 2; ++k) {
         cudaFree(L.pos[k]);
@@ -309,6 +321,11 @@ void free_particles(Lattice& L) {
     cudaFree(L.stats);
     cudaFree(L.upd_partial);
     L.upd_partial = nullptr;
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(L.spread_lo[k]);
+        L.spread_lo[k] = nullptr;
+    }
+    forces_touched(L);
     cudaFree(L.pdev);
     cudaFree(L.vert_particle);
     L.vel = L.force = L.stats = nullptr;
@@ -363,6 +380,8 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
     BIB_CUDA(c, cudaMalloc((void**)&L.force, vb));
     BIB_CUDA(c, cudaMalloc((void**)&L.stats, STATS * np * sizeof(double)));
     BIB_CUDA(c, cudaMalloc((void**)&L.upd_partial, (size_t)np * 64 * 5 * sizeof(double)));
+    for (int k = 0; k < 2; ++k) BIB_CUDA(c, cudaMalloc((void**)&L.spread_lo[k], (size_t)L.nvert * sizeof(int4)));
+    forces_touched(L);
     BIB_CUDA(c, cudaMemcpy(L.pos[0], L.host_pos.data(), vb, cudaMemcpyHostToDevice));
     BIB_CUDA(c, cudaMemcpy(L.pos[1], L.host_pos.data(), vb, cudaMemcpyHostToDevice));
     BIB_CUDA(c, cudaMemset(L.vel, 0, vb));
@@ -475,6 +494,7 @@ void record(bib_ctx* c, int idx) {
     if (c->profiling) cudaEventRecord(c->ev[idx], c->stream);
 }
 
+
 // One coupled step.  The reference's driver order (progs/capsule_in_shear/capsule_in_shear.cpp:
 // 187-227) is computeVelocity -> setExternalVector -> [interpolate, compute + spread forces,
 // move] -> collideAndStream -> wall processors.  Forces at X_n do not depend on the velocity,
@@ -504,7 +524,8 @@ void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
         launch_particle_update(L, s);
         L.pcur = 1 - L.pcur;
         launch_voxelize(L, L.pos[L.pcur], s);
-        launch_collide_stream(L, true, s);
+        launch_collide_stream(L, Coupling::kDense, s);
+        forces_touched(L);
         record(c, 3);
         L.cur = 1 - L.cur;
         L.fe = 1 - L.fe;
@@ -515,22 +536,36 @@ void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
         return;
     }
     if (with_ib && with_lbm) {
+        // Sparse coupling: the collision reads only the force spread in this step and writes
+        // the velocity field j/rho + body/2; the interpolation adds the previous force's share
+        // (F[fe] - body)/2 at its support nodes; then F[fe] is reset to the body force at the
+        // nodes its spreading recorded (or everywhere, when those are not known).
+        const bool sparse = ib && sparse_coupling(L);
         if (!L.target_clean) launch_force_fill(L, 1 - L.fe, s);
         record(c, 0);
         if (ib) launch_membrane_forces(L, s);
         if (ib) launch_pp_forces(L, s);
         record(c, 1);
-        if (ib) launch_spread(L, 1 - L.fe, s);
+        if (ib) launch_spread(L, 1 - L.fe, s, sparse);
+        if (sparse) L.sparse_ok[1 - L.fe] = true;  // a clean target plus the recorded nodes
+        else forces_touched(L);
         record(c, 2);
-        launch_collide_stream(L, true, s);  // u of this state, collision with F[1-fe], F[fe] := body
+        // dense: u of this state, collision with F[1-fe], F[fe] := body
+        launch_collide_stream(L, sparse ? Coupling::kSparse : Coupling::kDense, s);
         record(c, 3);
         L.cur = 1 - L.cur;
         L.fe = 1 - L.fe;
-        L.target_clean = true;
+        L.target_clean = !sparse;
         launch_fd_walls(L, L.cur, L.fe, s);
         record(c, 4);
         if (ib) {
-            launch_interpolate_move(L, s);
+            launch_interpolate_move(L, s, sparse ? 1 - L.fe : -1);
+            if (sparse) {
+                if (L.sparse_ok[1 - L.fe]) launch_force_clear(L, 1 - L.fe, s);
+                else launch_force_fill(L, 1 - L.fe, s);
+                L.sparse_ok[1 - L.fe] = true;  // all body force now
+                L.target_clean = true;
+            }
             launch_particle_update(L, s);
             L.pcur = 1 - L.pcur;
         }
@@ -544,6 +579,7 @@ void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
         launch_velocity_field(L, s);
         launch_force_fill(L, L.fe, s);
         L.target_clean = false;
+        forces_touched(L);
         if (ib) launch_membrane_forces(L, s);
         if (ib) launch_pp_forces(L, s);
         record(c, 1);
@@ -565,7 +601,7 @@ void enqueue_step(bib_ctx* c, Lattice& L, bool with_ib, bool with_lbm) {
     record(c, 0);
     record(c, 1);
     record(c, 2);
-    launch_collide_stream(L, false, s);
+    launch_collide_stream(L, Coupling::kNone, s);
     record(c, 3);
     L.cur = 1 - L.cur;
     launch_fd_walls(L, L.cur, L.fe, s);
@@ -587,11 +623,14 @@ bib_status accumulate_profile(bib_ctx* c) {
 // The instantiated graph of `steps` (1 or 2) coupled steps from the lattice's current parity
 // state, captured on first use.  Capturing leaves the host-side state as it was.
 bib_status step_graph(bib_ctx* c, Lattice& L, int steps, cudaGraphExec_t* out) {
-    const std::pair<int, int> key(L.handle, (steps - 1) * 8 + L.cur * 4 + L.pcur * 2 + L.fe);
+    // the captured launches depend on the parities and, for the sparse coupling, on whether
+    // the previous force field can be reset at its recorded nodes
+    const int sparse_key = sparse_coupling(L) ? 1 + (L.sparse_ok[L.fe] ? 1 : 0) : 0;
+    const std::pair<int, int> key(L.handle, sparse_key * 16 + (steps - 1) * 8 + L.cur * 4 + L.pcur * 2 + L.fe);
     GraphEntry& ge = c->graphs[key];
     if (!ge.exec) {
         const int cur0 = L.cur, pcur0 = L.pcur, fe0 = L.fe;
-        const bool clean0 = L.target_clean;
+        const bool clean0 = L.target_clean, ok0 = L.sparse_ok[0], ok1 = L.sparse_ok[1];
         cudaGraph_t g = nullptr;
         BIB_CUDA(c, cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
         for (int k = 0; k < steps; ++k) enqueue_step(c, L, true, true);
@@ -600,6 +639,8 @@ bib_status step_graph(bib_ctx* c, Lattice& L, int steps, cudaGraphExec_t* out) {
         L.pcur = pcur0;
         L.fe = fe0;
         L.target_clean = clean0;
+        L.sparse_ok[0] = ok0;
+        L.sparse_ok[1] = ok1;
         if (e != cudaSuccess) return fail(c, BIB_ECUDA, "graph capture failed: %s", cudaGetErrorString(e));
         size_t nn = 0;
         if (cudaGraphGetNodes(g, nullptr, &nn) == cudaSuccess && nn) {
@@ -632,7 +673,9 @@ bib_status run_steps(bib_ctx* c, int32_t h, int64_t nsteps, bool with_ib, bool w
     const bool use_graph = c->graph_mode && !c->profiling && with_ib && with_lbm && nsteps >= 1;
     int64_t done = 0;
     if (use_graph) {
-        if (!L->target_clean) {  // the graphs assume a clean spreading target on entry
+        // the graphs assume a clean spreading target on entry (and, for the sparse coupling, a
+        // previous force field with known nodes, which one eager step establishes)
+        if (!L->target_clean || (sparse_coupling(*L) && !L->sparse_ok[L->fe])) {
             enqueue_step(c, *L, true, true);
             BIB_CHECK_LAUNCH(c);
             ++done;
@@ -1063,6 +1106,7 @@ bib_status enqueue_batch_step(bib_ctx* c, Batch& B) {
         L.fe ^= 1;
         if (L.nvert) L.pcur ^= 1;
         L.target_clean = true;
+        forces_touched(L);
     }
     B.phase ^= 1;
     return BIB_OK;
@@ -1525,7 +1569,8 @@ bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     const int mb = t->membrane_block;
     if (t->collide_kernel < BIB_KERNEL_AUTO || t->collide_kernel > BIB_KERNEL_STAGED || t->tile_cells < 0 ||
         t->stages < 0 || t->stages == 1 || t->stages > 4 ||
-        (mb != 0 && mb != 64 && mb != 128 && mb != 256 && mb != 512))
+        (mb != 0 && mb != 64 && mb != 128 && mb != 256 && mb != 512) ||
+        (t->force_reset != BIB_FORCE_RESET_AUTO && t->force_reset != BIB_FORCE_RESET_DENSE) || t->wait_limit_us < 0)
         return fail(c, BIB_EINVAL, "invalid tuning values");
     Lattice probe = {};
     probe.d = L->d;
@@ -1539,6 +1584,9 @@ bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     L->tile_cells = t->tile_cells;
     L->stages = t->stages;
     L->membrane_block = mb ? mb : 256;
+    L->dense_reset = t->force_reset == BIB_FORCE_RESET_DENSE;
+    L->wait_ns = t->wait_limit_us ? (uint64_t)t->wait_limit_us * 1000u : kDefaultWaitNs;
+    forces_touched(*L);
     return BIB_OK;
 }
 
@@ -1654,7 +1702,10 @@ bib_status bib_lattice_send(bib_ctx* c, int32_t h, const void* buf, size_t bytes
     if (bytes != want) return fail(c, BIB_EINVAL, "expected %zu bytes", want);
     bib_status st = import_populations(c, *L, static_cast<const double*>(buf), w);
     if (st) return st;
-    if (w.per == Q + 4) L->target_clean = false;  // the force of the cells became the current external force
+    if (w.per == Q + 4) {  // the force of the cells became the current external force
+        L->target_clean = false;
+        forces_touched(*L);
+    }
     return BIB_OK;
 }
 
@@ -1702,6 +1753,7 @@ bib_status bib_lattice_set_force(bib_ctx* c, int32_t h, const double* F) {
     if (st) return st;
     launch_force_import(*L, L->fe, d, c->stream);
     L->target_clean = false;
+    forces_touched(*L);
     BIB_CHECK_LAUNCH(c);
     BIB_CUDA(c, cudaStreamSynchronize(c->stream));
     cudaFree(d);
@@ -2439,6 +2491,7 @@ bib_status bib_checkpoint_load(bib_ctx* c, int32_t h, const char* path) {
     L->cur = hd.cur;
     L->fe = hd.fe;
     L->target_clean = hd.target_clean != 0;
+    forces_touched(*L);
     L->iteration = hd.iteration;
     // particles: replace the lattice's set, upload, then restore velocities, forces and the
     // per-particle area / volume / centre exactly as saved

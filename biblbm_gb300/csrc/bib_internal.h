@@ -14,6 +14,8 @@
 namespace bib {
 
 constexpr int Q = 19;
+// Bound of every device-side wait (the staged kernel's mbarrier waits on its own bulk copies)
+constexpr uint64_t kDefaultWaitNs = 2000000000ull;
 
 // Lattice geometry and physics parameters as the kernels see them (passed by value).
 struct LatticeDesc {
@@ -151,6 +153,12 @@ struct IbView {
     int vbase;           // batch numbering of the lattice's first vertex
     int nvert;
     Interactions inter;  // wall interactions are applied by the membrane kernel
+    // sparse force reset (single lattices, FP32 fields): the spreading records the first
+    // support node of every vertex (x, y, z, 1; w = 0 outside the envelope) in spread_lo, and
+    // the interpolation adds (Fold - body) / 2 of the force field of the previous step to the
+    // velocity field j / rho + body / 2 that the collision wrote.  Null: not used.
+    int4* spread_lo = nullptr;
+    const void* Fold = nullptr;
 };
 
 // Per-launch constants of the collision in the compute type C.
@@ -221,6 +229,15 @@ struct Lattice {
     void* F[2] = {nullptr, nullptr};  // force fields (double for F64 storage, float otherwise)
     int fe = 0;
     bool target_clean = false;        // F[1-fe] holds the body force, ready to receive spreading
+    // Sparse force reset (reduced-precision storage, coupled step, no phase field, cell types or
+    // pipe boundary): the collision reads only the spread force of its step, and the field of
+    // the previous step is reset to the body force only where its spreading wrote (the support
+    // nodes recorded in spread_lo[b] for F[b]).  sparse_ok[b]: F[b] differs from the body force
+    // only at the nodes in spread_lo[b].
+    int4* spread_lo[2] = {nullptr, nullptr};
+    bool sparse_ok[2] = {false, false};
+    bool dense_reset = false;  // tuning: always the dense reset
+    uint64_t wait_ns = kDefaultWaitNs;  // bound of the staged kernel's hand-off waits
     void* u = nullptr;                // velocity field, (ux, uy, uz, 0) per cell (double for F64 storage, float otherwise)
     uint8_t* phase = nullptr;
     uint8_t* celltype = nullptr;      // BIB_CELL_* per cell, or nullptr: every cell has the lattice's dynamics
@@ -268,11 +285,15 @@ struct Lattice {
 };
 
 // ---- kernel launchers (lattice_kernels.cu) ----
-// coupled = true: velocity output, collision with the spread force F[1-fe], F[fe] reset
-// to the body force afterwards.  coupled = false: collision with F[fe], no side outputs.
-void launch_collide_stream(const Lattice& L, bool coupled, cudaStream_t s);
+// How a collide-and-stream treats the force fields and the velocity field.
+enum class Coupling {
+    kNone,    // collision with F[fe], no side outputs
+    kDense,   // velocity j/rho + F[fe]/2 written, collision with F[1-fe], F[fe] reset to the body force
+    kSparse,  // velocity j/rho + body/2 written, collision with F[1-fe]; F[fe] left for the sparse reset
+};
+void launch_collide_stream(const Lattice& L, Coupling mode, cudaStream_t s);
 // shared-memory staged variant (collide_staged.cu); false if the lattice shape does not fit it
-bool launch_collide_stream_staged(const Lattice& L, bool coupled, cudaStream_t s);
+bool launch_collide_stream_staged(const Lattice& L, Coupling mode, cudaStream_t s);
 bool collide_staged_fits(const Lattice& L);  // both step kinds fit the staged kernel
 void launch_fd_walls(const Lattice& L, int buf, int fbuf, cudaStream_t s);
 void launch_velocity_field(const Lattice& L, cudaStream_t s);  // u from the current state and F[fe]
@@ -294,8 +315,13 @@ void launch_nan_scan(const Lattice& L, int* flag, cudaStream_t s);
 
 // ---- kernel launchers (ib_kernels.cu) ----
 void launch_membrane_forces(const Lattice& L, cudaStream_t s);
-void launch_spread(const Lattice& L, int fbuf, cudaStream_t s);
-void launch_interpolate_move(const Lattice& L, cudaStream_t s);  // vel and pos[1-pcur] = pos + vel
+// spreading into F[fbuf]; with `record` the support nodes go to spread_lo[fbuf]
+void launch_spread(const Lattice& L, int fbuf, cudaStream_t s, bool record = false);
+// vel and pos[1-pcur] = pos + vel; fold >= 0: the velocity field is the sparse-reset form and
+// (F[fold] - body) / 2 is added to it at the support nodes
+void launch_interpolate_move(const Lattice& L, cudaStream_t s, int fold = -1);
+// F[fbuf] := body force at the support nodes in spread_lo[fbuf]
+void launch_force_clear(const Lattice& L, int fbuf, cudaStream_t s);
 void launch_particle_update(const Lattice& L, cudaStream_t s);   // area/volume/COM of pos[1-pcur] + remap
 // particle-particle interaction forces at pos[pcur] added to the vertex forces (no-op without)
 void launch_pp_forces(const Lattice& L, cudaStream_t s);

@@ -12,8 +12,8 @@
 // (the +-1 x shift is an index offset, periodic in x), FP32 arithmetic and coalesced stores.
 //
 // Per lattice update the kernel moves exactly the algorithmic bytes: 19 populations read
-// and written once, the spread force read, and (coupled step) the previous force read,
-// reset to the body force and the velocity field written.
+// and written once, the spread force read, the velocity field written (coupled step) and, with
+// the dense coupling only, the previous force read and reset to the body force.
 #include <algorithm>
 #include <cstring>
 #include <mutex>
@@ -53,14 +53,15 @@ __device__ __forceinline__ uint64_t global_ns() {
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
     return t;
 }
-// Bounded wait for one phase of a stage barrier: gives up after about 2 s (a copy of a
-// tile takes microseconds), so that a lost completion can never hang the GPU.
-__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity) {
+// Bounded wait for one phase of a stage barrier: gives up after limit_ns (2 s by default; a
+// copy of a tile takes microseconds) or 2^26 polls, so that a lost completion can never hang
+// the GPU.
+__device__ __forceinline__ bool mbar_wait_bounded(uint64_t* bar, unsigned parity, uint64_t limit_ns = kDefaultWaitNs) {
     if (mbar_try_wait(bar, parity)) return true;
     const uint64_t t0 = global_ns();
     for (uint32_t it = 0; it < (1u << 26); ++it) {
         if (mbar_try_wait(bar, parity)) return true;
-        if ((it & 255u) == 0 && global_ns() - t0 > 2000000000ull) break;
+        if ((it & 255u) == 0 && global_ns() - t0 > limit_ns) break;
     }
     return false;
 }
@@ -147,9 +148,14 @@ struct TileOf {
     static constexpr int value = sizeof(T) == 8 ? 256 : 512;
 };
 
+// Coupling of a staged launch: lattice only; dense (the velocity field with the previous force,
+// which is read and reset to the body force); sparse (the velocity field with the body force,
+// the previous force left to the sparse reset).
+constexpr int kCplNone = 0, kCplDense = 1, kCplSparse = 2;
+
 // Stage layout (compile-time): 19 population rows, the collision force (BGK + Guo) and,
-// for the coupled step, the previous force, each TILE cells long.
-template <class T, bool COUPLED, int COLL>
+// for the dense coupled step, the previous force, each TILE cells long.
+template <class T, int CPL, int COLL>
 struct StageLayout {
     using FT = typename Store<T>::F;
     static constexpr int TILE = TileOf<T>::value;
@@ -160,7 +166,7 @@ struct StageLayout {
     static constexpr unsigned FRC = TILE * sizeof(FT);
     static constexpr unsigned OFF_FCOL = Q * POP;
     static constexpr unsigned OFF_FPREV = OFF_FCOL + (NEED_FCOL ? 3 * FRC : 0);
-    static constexpr unsigned BYTES = ((OFF_FPREV + (COUPLED ? 3 * FRC : 0)) + 127) / 128 * 128;
+    static constexpr unsigned BYTES = ((OFF_FPREV + (CPL == kCplDense ? 3 * FRC : 0)) + 127) / 128 * 128;
 };
 
 constexpr int kMaxStages = 8;
@@ -172,6 +178,7 @@ struct StagedGeom {
     int nstages;      // pipeline depth (2..kMaxStages)
     int64_t ntiles;   // tiles_y * nz
     unsigned tx_bytes;  // bytes copied in per tile
+    uint64_t wait_ns;   // bound of the hand-off waits (full / empty); the final drain keeps the default
 };
 
 struct TileRef {
@@ -207,12 +214,12 @@ __device__ __forceinline__ PopLane pop_lane(int lane) {
 }
 
 // Copies of one tile into one stage, by the producer warp: lane i < 19 moves population i,
-// lanes 19..21 the collision force, lanes 22..24 the previous force.
-template <class T, bool COUPLED, int COLL>
+// lanes 19..21 the collision force, lanes 22..24 the previous force (dense coupling).
+template <class T, int CPL, int COLL>
 __device__ __forceinline__ void load_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, unsigned char* stage,
                                           uint64_t* bar, const T* fin, const T* wall, const typename Store<T>::F* Fcol,
                                           const typename Store<T>::F* Fprev, int lane, const PopLane& pl) {
-    using L = StageLayout<T, COUPLED, COLL>;
+    using L = StageLayout<T, CPL, COLL>;
     using FT = typename Store<T>::F;
     const TileRef t = tile_ref(d, g, tile);
     if (lane == 0) mbar_arrive_expect_tx(bar, g.tx_bytes);
@@ -264,7 +271,7 @@ __device__ __forceinline__ void load_tile(const LatticeDesc& d, const StagedGeom
         if (L::NEED_FCOL && lane < Q + 3) {
             const int c = lane - Q;
             bulk_copy_g2s(stage + L::OFF_FCOL + c * L::FRC, Fcol + c * d.stride + t.row0, fb, bar);
-        } else if (COUPLED && lane >= Q + 3 && lane < Q + 6) {
+        } else if (CPL == kCplDense && lane >= Q + 3 && lane < Q + 6) {
             const int c = lane - Q - 3;
             bulk_copy_g2s(stage + L::OFF_FPREV + c * L::FRC, Fprev + c * d.stride + t.row0, fb, bar);
         }
@@ -289,7 +296,7 @@ __device__ __forceinline__ TileCell tile_cell(const LatticeDesc& d, int Ct, int 
     return c;
 }
 
-template <class T, bool COUPLED, int COLL>
+template <class T, int CPL, int COLL>
 __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, const unsigned char* st,
                                              const CollideParams<typename Store<T>::C>& cp, T* __restrict__ fout,
                                              typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
@@ -297,7 +304,7 @@ __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedG
                                              const TileCell& cell, uint64_t* empty_s, int lane) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
-    using L = StageLayout<T, COUPLED, COLL>;
+    using L = StageLayout<T, CPL, COLL>;
     constexpr int TILE = L::TILE;
     const int r = cell.r, o0 = cell.o0, ol = cell.ol, orr = cell.orr;
     const bool active = cell.active;
@@ -330,9 +337,12 @@ __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedG
 #pragma unroll
             for (int q = 0; q < 3; ++q) F[q] = (C)SFc[q * TILE + o0];
         }
-        if (COUPLED) {
+        if (CPL == kCplDense) {
 #pragma unroll
             for (int q = 0; q < 3; ++q) Fp[q] = (C)SFp[q * TILE + o0];
+        } else if (CPL == kCplSparse) {
+#pragma unroll
+            for (int q = 0; q < 3; ++q) Fp[q] = cp.body[q];
         }
     }
     // the stage has been read into registers: hand it back to the producer
@@ -342,8 +352,8 @@ __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedG
     const int64_t k = t.row0 + o0;
     const int ctype = d.has_types ? celltype[k] : BIB_CELL_FLUID;
     if (ctype != BIB_CELL_FLUID) {  // BounceBack / NoDynamics node: no collision, zero velocity
-        if (COUPLED) {
-            store_u<FT>(u_out, k, FT(0), FT(0), FT(0));
+        if (CPL != kCplNone) store_u<FT>(u_out, k, FT(0), FT(0), FT(0));
+        if (CPL == kCplDense) {
 #pragma unroll
             for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
         }
@@ -357,7 +367,7 @@ __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedG
         return;
     }
     if (COLL == BIB_COLLISION_BGK_GUO_VOF && d.use_phase && phase[k]) om = cp.om1;
-    if (COUPLED) {
+    if (CPL != kCplNone) {
         staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, Fp, fd ? nullptr : u);
         if (fd) {
             const int side = y == 0 ? 0 : 1;
@@ -365,8 +375,10 @@ __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedG
             for (int q = 0; q < 3; ++q) u[q] = cp.wall_u[side][q];
         }
         store_u<FT>(u_out, k, (FT)u[0], (FT)u[1], (FT)u[2]);
+        if (CPL == kCplDense) {
 #pragma unroll
-        for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
+            for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
+        }
     } else {
         staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, nullptr, nullptr);
     }
@@ -390,8 +402,8 @@ constexpr int staged_ctas_per_sm() {
     return sizeof(T) == 2 ? 2 : 1;
 }
 
-template <class T, bool COUPLED, int COLL>
-__global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged_ctas_per_sm<T>())
+template <class T, int CPL, int COLL>
+__global__ void __launch_bounds__(StageLayout<T, CPL, COLL>::THREADS, staged_ctas_per_sm<T>())
     k_collide_stream_staged(
     LatticeDesc d, StagedGeom g, CollideParams<typename Store<T>::C> cp, const T* __restrict__ fin,
     T* __restrict__ fout, const T* __restrict__ wall, const typename Store<T>::F* __restrict__ Fcol,
@@ -399,7 +411,7 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
     const uint8_t* __restrict__ phase, const uint8_t* __restrict__ celltype, int* __restrict__ wait_err) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
-    using L = StageLayout<T, COUPLED, COLL>;
+    using L = StageLayout<T, CPL, COLL>;
     constexpr int TILE = L::TILE;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);
@@ -425,13 +437,13 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
             const int s = it % NS, use = it / NS;
             if (use > 0) {
                 // every lane observes the release, so every lane's copies are ordered after it
-                const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&empty[s], (unsigned)(use - 1) & 1u));
+                const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&empty[s], (unsigned)(use - 1) & 1u, g.wait_ns));
                 if (!ok) {
                     if (lane == 0) atomicExch(wait_err, 1);
                     break;
                 }
             }
-            load_tile<T, COUPLED, COLL>(d, g, tile, stages + s * L::BYTES, &full[s], fin, wall, Fcol, Fprev, lane, pl);
+            load_tile<T, CPL, COLL>(d, g, tile, stages + s * L::BYTES, &full[s], fin, wall, Fcol, Fprev, lane, pl);
         }
         // a copy may still be landing only if the consumers gave up; wait for it so that
         // no bulk copy writes into the shared memory of a retired CTA
@@ -449,12 +461,12 @@ __global__ void __launch_bounds__(StageLayout<T, COUPLED, COLL>::THREADS, staged
     for (int64_t tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x, ++it) {
         const int s = it % NS;
         // every lane waits, so that the landed bytes are visible to every lane
-        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (unsigned)(it / NS) & 1u));
+        const bool ok = __all_sync(0xffffffffu, mbar_wait_bounded(&full[s], (unsigned)(it / NS) & 1u, g.wait_ns));
         if (!ok) {
             if (lane == 0) atomicExch(wait_err, 1);
             return;
         }
-        consume_tile<T, COUPLED, COLL>(d, g, tile, stages + s * L::BYTES, cp, fout, Fprev, u_out, phase, celltype, cell,
+        consume_tile<T, CPL, COLL>(d, g, tile, stages + s * L::BYTES, cp, fout, Fprev, u_out, phase, celltype, cell,
                                         &empty[s], lane);
     }
 }
@@ -479,6 +491,7 @@ __device__ __forceinline__ StagedGeom view_geom(const CollideView& v, int ns) {
     g.nstages = ns;
     g.ntiles = v.ntiles;
     g.tx_bytes = v.tx_bytes;
+    g.wait_ns = kDefaultWaitNs;
     return g;
 }
 
@@ -505,12 +518,12 @@ __device__ __forceinline__ void copy_view(CollideView* dst, const CollideView* s
 }
 
 template <class T, int COLL>
-__global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ctas_per_sm<T>())
+__global__ void __launch_bounds__(StageLayout<T, kCplDense, COLL>::THREADS, staged_ctas_per_sm<T>())
     k_collide_stream_staged_batch(const CollideView* __restrict__ views, int nviews, int64_t ntiles, int NS,
                                   int* __restrict__ wait_err) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
-    using L = StageLayout<T, true, COLL>;
+    using L = StageLayout<T, kCplDense, COLL>;
     extern __shared__ __align__(128) unsigned char smem[];
     uint64_t* full = reinterpret_cast<uint64_t*>(smem);
     uint64_t* empty = full + kMaxStages;
@@ -550,7 +563,7 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
                 have = vi;
             }
             const CollideView& V = *pview;
-            load_tile<T, true, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES, &full[s],
+            load_tile<T, kCplDense, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES, &full[s],
                                      static_cast<const T*>(V.fin), static_cast<const T*>(V.wall),
                                      static_cast<const FT*>(V.Fcol), static_cast<const FT*>(V.Fprev), lane, pl);
         }
@@ -581,7 +594,7 @@ __global__ void __launch_bounds__(StageLayout<T, true, COLL>::THREADS, staged_ct
             cur_view = vi;
         }
         const CollideView& V = *cview;
-        consume_tile<T, true, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES,
+        consume_tile<T, kCplDense, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES,
                                     *reinterpret_cast<const CollideParams<C>*>(V.cp), static_cast<T*>(V.fout),
                                     static_cast<FT*>(V.Fprev), static_cast<FT*>(V.u), V.phase, V.celltype, cell,
                                     &empty[s], lane);
@@ -603,20 +616,20 @@ int optin_smem() {
     return optin;
 }
 
-template <class T, bool COUPLED, int COLL>
+template <class T, int CPL, int COLL>
 size_t staged_smem(int nstages) {
-    return 256 + (size_t)nstages * StageLayout<T, COUPLED, COLL>::BYTES;
+    return 256 + (size_t)nstages * StageLayout<T, CPL, COLL>::BYTES;
 }
 
 // Pipeline depth: the tuning value, else as many stages as fit the resident CTAs of an SM
 // (228 KB of shared memory per SM, 1 KB of it reserved per CTA).
-template <class T, bool COUPLED, int COLL>
+template <class T, int CPL, int COLL>
 int staged_stages(const Lattice& L) {
     if (L.stages >= 2) return L.stages;
     const size_t limit = std::min<size_t>((size_t)optin_smem(), 228 * 1024 / staged_ctas_per_sm<T>()) - 1024;
     int best = 2;
     for (int ns = 2; ns <= kMaxStages; ++ns)
-        if (staged_smem<T, COUPLED, COLL>(ns) <= limit) best = ns;
+        if (staged_smem<T, CPL, COLL>(ns) <= limit) best = ns;
     return best;
 }
 
@@ -643,11 +656,11 @@ CollideParams<C> collide_params(const LatticeDesc& d, int storage) {
     return cp;
 }
 
-template <class T, bool COUPLED, int COLL>
+template <class T, int CPL, int COLL>
 bool staged_inst(const Lattice& L, int target, cudaStream_t s) {
     using FT = typename Store<T>::F;
     using C = typename Store<T>::C;
-    using LY = StageLayout<T, COUPLED, COLL>;
+    using LY = StageLayout<T, CPL, COLL>;
     const LatticeDesc& d = L.d;
     StagedGeom g{};
     g.R = staged_rows(d, std::min(target, LY::TILE));
@@ -655,15 +668,16 @@ bool staged_inst(const Lattice& L, int target, cudaStream_t s) {
     if (g.Ct > LY::TILE) return false;
     g.tiles_y = d.ny / g.R;
     g.ntiles = (int64_t)g.tiles_y * d.nz;
-    g.nstages = staged_stages<T, COUPLED, COLL>(L);
-    g.tx_bytes = (unsigned)(Q * g.Ct * sizeof(T) + ((LY::NEED_FCOL ? 3 : 0) + (COUPLED ? 3 : 0)) * g.Ct * sizeof(FT));
-    const size_t smem = staged_smem<T, COUPLED, COLL>(g.nstages);
+    g.nstages = staged_stages<T, CPL, COLL>(L);
+    g.wait_ns = L.wait_ns;
+    g.tx_bytes = (unsigned)(Q * g.Ct * sizeof(T) + ((LY::NEED_FCOL ? 3 : 0) + (CPL == kCplDense ? 3 : 0)) * g.Ct * sizeof(FT));
+    const size_t smem = staged_smem<T, CPL, COLL>(g.nstages);
     if (smem + 1024 > (size_t)optin_smem()) return false;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
 
-    auto kern = k_collide_stream_staged<T, COUPLED, COLL>;
+    auto kern = k_collide_stream_staged<T, CPL, COLL>;
     // per device: the dynamic shared memory this kernel is allowed (only ever raised) and
     // the resident CTAs per SM for each stage size
     static std::mutex mu;
@@ -689,20 +703,20 @@ bool staged_inst(const Lattice& L, int target, cudaStream_t s) {
     const int64_t grid = std::min<int64_t>(g.ntiles, (int64_t)nb * sms);
     const T* fin = (const T*)L.f[L.cur];
     T* fout = (T*)L.f[1 - L.cur];
-    const FT* Fcol = (const FT*)(COUPLED ? L.F[1 - L.fe] : L.F[L.fe]);
-    FT* Fprev = COUPLED ? (FT*)L.F[L.fe] : nullptr;
+    const FT* Fcol = (const FT*)(CPL != kCplNone ? L.F[1 - L.fe] : L.F[L.fe]);
+    FT* Fprev = CPL == kCplDense ? (FT*)L.F[L.fe] : nullptr;
     kern<<<(unsigned)grid, LY::THREADS, smem, s>>>(d, g, collide_params<C>(d, L.storage), fin, fout,
-                                                       (const T*)L.wall, Fcol, Fprev, COUPLED ? (FT*)L.u : nullptr,
+                                                       (const T*)L.wall, Fcol, Fprev, CPL != kCplNone ? (FT*)L.u : nullptr,
                                                        L.phase, L.celltype, L.wait_err);
     return true;
 }
 
-template <class T, bool COUPLED>
+template <class T, int CPL>
 bool staged_coll(const Lattice& L, int target, cudaStream_t s) {
     switch (L.d.collision) {
-        case BIB_COLLISION_BGK_GUO_VOF: return staged_inst<T, COUPLED, BIB_COLLISION_BGK_GUO_VOF>(L, target, s);
-        case BIB_COLLISION_BGK: return staged_inst<T, COUPLED, BIB_COLLISION_BGK>(L, target, s);
-        default: return staged_inst<T, COUPLED, BIB_COLLISION_TRT>(L, target, s);
+        case BIB_COLLISION_BGK_GUO_VOF: return staged_inst<T, CPL, BIB_COLLISION_BGK_GUO_VOF>(L, target, s);
+        case BIB_COLLISION_BGK: return staged_inst<T, CPL, BIB_COLLISION_BGK>(L, target, s);
+        default: return staged_inst<T, CPL, BIB_COLLISION_TRT>(L, target, s);
     }
 }
 
@@ -718,24 +732,28 @@ int default_tile_cells(const Lattice& L) {
 }
 
 template <class T>
-bool staged_t(const Lattice& L, bool coupled, cudaStream_t s) {
+bool staged_t(const Lattice& L, Coupling mode, cudaStream_t s) {
     if (!shape_ok<T>(L) || !L.wait_err) return false;
     const int target = default_tile_cells(L);
-    return coupled ? staged_coll<T, true>(L, target, s) : staged_coll<T, false>(L, target, s);
+    switch (mode) {
+        case Coupling::kDense: return staged_coll<T, kCplDense>(L, target, s);
+        case Coupling::kSparse: return staged_coll<T, kCplSparse>(L, target, s);
+        default: return staged_coll<T, kCplNone>(L, target, s);
+    }
 }
 
 template <class T>
 bool fits_t(const Lattice& L) {
     if (!shape_ok<T>(L)) return false;
     const int ns = L.stages >= 2 ? L.stages : 2;
-    return ns <= kMaxStages && staged_smem<T, true, BIB_COLLISION_BGK_GUO_VOF>(ns) + 1024 <= (size_t)optin_smem();
+    return ns <= kMaxStages && staged_smem<T, kCplDense, BIB_COLLISION_BGK_GUO_VOF>(ns) + 1024 <= (size_t)optin_smem();
 }
 
 template <class T, int COLL>
 bool batch_inst(const BatchLaunch& B, cudaStream_t s) {
-    using LY = StageLayout<T, true, COLL>;
-    const int ns = B.stages >= 2 ? B.stages : staged_stages<T, true, COLL>(Lattice{});
-    const size_t smem = staged_smem<T, true, COLL>(ns) + batch_extra_smem();
+    using LY = StageLayout<T, kCplDense, COLL>;
+    const int ns = B.stages >= 2 ? B.stages : staged_stages<T, kCplDense, COLL>(Lattice{});
+    const size_t smem = staged_smem<T, kCplDense, COLL>(ns) + batch_extra_smem();
     if (smem + 1024 > (size_t)optin_smem()) return false;
     int dev = 0, sms = 0;
     cudaGetDevice(&dev);
@@ -809,9 +827,9 @@ bool collide_batch_fits(int storage, int collision, int stages) {
         using T = decltype(tag);
         const int ns = stages >= 2 ? stages : 2;
         size_t smem = 0;
-        if (collision == BIB_COLLISION_BGK_GUO_VOF) smem = staged_smem<T, true, BIB_COLLISION_BGK_GUO_VOF>(ns);
-        else if (collision == BIB_COLLISION_BGK) smem = staged_smem<T, true, BIB_COLLISION_BGK>(ns);
-        else smem = staged_smem<T, true, BIB_COLLISION_TRT>(ns);
+        if (collision == BIB_COLLISION_BGK_GUO_VOF) smem = staged_smem<T, kCplDense, BIB_COLLISION_BGK_GUO_VOF>(ns);
+        else if (collision == BIB_COLLISION_BGK) smem = staged_smem<T, kCplDense, BIB_COLLISION_BGK>(ns);
+        else smem = staged_smem<T, kCplDense, BIB_COLLISION_TRT>(ns);
         return ns <= 4 && smem + batch_extra_smem() + 1024 <= (size_t)optin_smem();
     };
     if (storage == BIB_STORAGE_F64) return fits(double{});
@@ -832,10 +850,10 @@ bool collide_staged_fits(const Lattice& L) {
     return fits_t<__half>(L);
 }
 
-bool launch_collide_stream_staged(const Lattice& L, bool coupled, cudaStream_t s) {
-    if (L.storage == BIB_STORAGE_F64) return staged_t<double>(L, coupled, s);
-    if (L.storage == BIB_STORAGE_F32) return staged_t<float>(L, coupled, s);
-    return staged_t<__half>(L, coupled, s);
+bool launch_collide_stream_staged(const Lattice& L, Coupling mode, cudaStream_t s) {
+    if (L.storage == BIB_STORAGE_F64) return staged_t<double>(L, mode, s);
+    if (L.storage == BIB_STORAGE_F32) return staged_t<float>(L, mode, s);
+    return staged_t<__half>(L, mode, s);
 }
 
 }  // namespace bib

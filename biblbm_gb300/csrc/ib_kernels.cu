@@ -10,7 +10,7 @@
 
 #include <cub/device/device_radix_sort.cuh>
 
-#include "d3q19.cuh"
+#include "lattice_common.cuh"
 
 namespace bib {
 
@@ -93,6 +93,13 @@ __device__ __forceinline__ int remap_global(int periodic, int N, int64_t i_local
         g = i_local + off;
     }
     return (g < 0 || g >= N) ? -1 : (int)g;
+}
+
+// First support node of one axis as the spreading records it for the sparse force reset: on a
+// periodic axis reduced to one period (remap_global of lo + m is unchanged), so that it fits 32
+// bits; on a walled axis a vertex inside the envelope is within h + 1 of the domain.
+__device__ __forceinline__ int record_lo(int periodic, int N, int64_t lo, int off) {
+    return periodic ? pmod(lo + off, N) - off : (int)lo;
 }
 
 // Delta weight of support node lo + m on one axis, phi(lo + m - x) with lo = ceil(x - h).
@@ -251,7 +258,11 @@ __device__ __forceinline__ void pipe_move(const IbDesc& ib, const double* old, c
 // interpolators, ImmersedBoundaryDynamics_interpolation.hh:13-153.
 // One thread per vertex.  BATCH: the vertex numbering runs over the lattices of a batch and
 // each thread looks its lattice's view up through vinst; otherwise v1 is the lattice.
-template <class UT, int S>
+// FOLD (sparse force reset): the velocity field holds j/rho + body/2, and the vertex velocity
+// adds the share of the previous step's force, sum of w (Fold - body) / 2 over the support
+// nodes off the finite-difference wall rows (whose velocity is the wall's); the sum of the two
+// is the interpolation of j/rho + Fold/2, the reference's computeVelocity field.
+template <class UT, int S, bool FOLD = false>
 __device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) {
     using C = UT;
     static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
@@ -283,6 +294,9 @@ __device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) 
             zo[m] = (int64_t)gz[m] * d.ny * d.nx;
         }
         C acc[3] = {C(0), C(0), C(0)};
+        C facc[3] = {C(0), C(0), C(0)};
+        const UT* __restrict__ Fo = static_cast<const UT*>(V.Fold);
+        const C body[3] = {(C)d.body[0], (C)d.body[1], (C)d.body[2]};
 #pragma unroll
         for (int a = 0; a < s; ++a) {
             if (gx[a] < 0) continue;
@@ -291,6 +305,7 @@ __device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) 
                 if (gy[b] < 0) continue;
                 const C wxy = w[0][a] * w[1][b];
                 const int64_t col = gx[a] + yo[b];
+                const bool fd_row = FOLD && fd_wall_node(d, gy[b]);
 #pragma unroll
                 for (int c = 0; c < s; ++c) {
                     if (gz[c] < 0) continue;
@@ -299,12 +314,18 @@ __device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) 
                     acc[0] += wt * uc.x;
                     acc[1] += wt * uc.y;
                     acc[2] += wt * uc.z;
+                    if (FOLD && !fd_row) {
+                        const int64_t k = col + zo[c];
+                        facc[0] += wt * (__ldg(Fo + k) - body[0]);
+                        facc[1] += wt * (__ldg(Fo + d.stride + k) - body[1]);
+                        facc[2] += wt * (__ldg(Fo + 2 * d.stride + k) - body[2]);
+                    }
                 }
             }
         }
-        out[0] = (double)acc[0];
-        out[1] = (double)acc[1];
-        out[2] = (double)acc[2];
+        out[0] = (double)(FOLD ? acc[0] + C(0.5) * facc[0] : acc[0]);
+        out[1] = (double)(FOLD ? acc[1] + C(0.5) * facc[1] : acc[1]);
+        out[2] = (double)(FOLD ? acc[2] + C(0.5) * facc[2] : acc[2]);
     }
     if (ib.has_pipe && inside_envelope(d, ib.dirac, p)) {
         const double w = pipe_weight(ib, p, S == 4 ? 2.0 : 1.5);
@@ -324,13 +345,50 @@ __device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) 
     pos_next[3 * v + 2] = xn[2];
 }
 
-template <class UT, int S, bool BATCH>
+template <class UT, int S, bool BATCH, bool FOLD = false>
 __global__ void __launch_bounds__(128) k_interpolate_move(IbView v1, const IbView* __restrict__ views,
                                                            const int* __restrict__ vinst, int nvert) {
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nvert) return;
     const IbView& V = BATCH ? views[vinst[g]] : v1;
-    interpolate_move_vertex<UT, S>(V, BATCH ? g - V.vbase : g);
+    interpolate_move_vertex<UT, S, FOLD>(V, BATCH ? g - V.vbase : g);
+}
+
+// Sparse force reset: F := body force at the support nodes the last spreading into F recorded
+// (one thread per vertex and (y, z) row of its support).  Along x the stores cover the aligned
+// float4 words around the row's s nodes: a cell of such a word outside the support holds the body
+// force already or lies in the support of another vertex, which is reset in the same launch.
+template <int S>
+__global__ void __launch_bounds__(128) k_force_clear(LatticeDesc d, IbDesc ib, int nvert, const int4* __restrict__ lo,
+                                                      float* __restrict__ F) {
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= (int64_t)nvert * S * S) return;
+    const int v = (int)(t / (S * S)), r = (int)(t - (int64_t)v * S * S);
+    const int4 l = lo[v];
+    if (!l.w) return;
+    const int off = (int)ib.offset;
+    const int gy = remap_global(d.py, d.ny, (int64_t)l.y + r / S, off);
+    const int gz = remap_global(d.pz, d.nz, (int64_t)l.z + r % S, off);
+    if (gy < 0 || gz < 0) return;
+    const int64_t row = (int64_t)d.nx * (gy + (int64_t)d.ny * gz);
+    const float b[3] = {(float)d.body[0], (float)d.body[1], (float)d.body[2]};
+    const int gx0 = remap_global(d.px, d.nx, (int64_t)l.x, off);
+    const int gxl = remap_global(d.px, d.nx, (int64_t)l.x + S - 1, off);
+    if (gx0 >= 0 && gxl == gx0 + S - 1) {
+        // the row's nodes are contiguous: the float4 words from gx0 down to 4 to gxl
+        const int64_t k0 = (row + gx0) & ~(int64_t)3, k1 = (row + gxl) & ~(int64_t)3;
+        for (int q = 0; q < 3; ++q) {
+            float4* p = reinterpret_cast<float4*>(F + q * d.stride);
+            for (int64_t k = k0; k <= k1; k += 4) p[k >> 2] = make_float4(b[q], b[q], b[q], b[q]);
+        }
+        return;
+    }
+#pragma unroll
+    for (int m = 0; m < S; ++m) {
+        const int gx = remap_global(d.px, d.nx, (int64_t)l.x + m, off);
+        if (gx < 0) continue;
+        for (int q = 0; q < 3; ++q) F[q * d.stride + row + gx] = b[q];
+    }
 }
 
 // ---------------------------------------------------------------- spreading
@@ -343,9 +401,18 @@ __device__ __forceinline__ void spread_vertex(const IbView& V, int v) {
     const double* __restrict__ force = V.force;
     FT* __restrict__ F = static_cast<FT*>(V.F);
     const double p[3] = {pos[3 * v], pos[3 * v + 1], pos[3 * v + 2]};
-    if (!inside_envelope(d, ib.dirac, p)) return;
+    if (!inside_envelope(d, ib.dirac, p)) {
+        if (V.spread_lo) V.spread_lo[v] = make_int4(0, 0, 0, 0);
+        return;
+    }
     const int off = (int)ib.offset;
     constexpr int s = S;
+    if (V.spread_lo) {
+        constexpr double h = S == 4 ? 2.0 : 1.5;
+        V.spread_lo[v] = make_int4(record_lo(d.px, d.nx, (int64_t)ceil(p[0] - ib.offset - h), off),
+                                   record_lo(d.py, d.ny, (int64_t)ceil(p[1] - ib.offset - h), off),
+                                   record_lo(d.pz, d.nz, (int64_t)ceil(p[2] - ib.offset - h), off), 1);
+    }
     FT fscale = FT(1);
     if (ib.has_pipe) {
         const double wp = pipe_weight(ib, p, S == 4 ? 2.0 : 1.5);
@@ -443,7 +510,8 @@ __host__ __device__ inline int key_bits(int64_t n) {
 }
 
 __global__ void __launch_bounds__(128) k_spread_keys(LatticeDesc d, IbDesc ib, int nvert, const double* __restrict__ pos,
-                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+                                                      uint32_t* __restrict__ keys, uint32_t* __restrict__ ids,
+                                                      int4* __restrict__ lo_out) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvert) return;
     const int s = support(ib.dirac), s3 = s * s * s;
@@ -453,6 +521,10 @@ __global__ void __launch_bounds__(128) k_spread_keys(LatticeDesc d, IbDesc ib, i
     const double h = half_support(ib.dirac);
     int64_t lo[3];
     for (int a = 0; a < 3; ++a) lo[a] = (int64_t)ceil(p[a] - ib.offset - h);
+    if (lo_out)
+        lo_out[v] = inside ? make_int4(record_lo(d.px, d.nx, lo[0], off), record_lo(d.py, d.ny, lo[1], off),
+                                       record_lo(d.pz, d.nz, lo[2], off), 1)
+                           : make_int4(0, 0, 0, 0);
     for (int m = 0; m < s3; ++m) {
         const int a = m / (s * s), b = (m / s) % s, c = m % s;
         const int gx = remap_global(d.px, d.nx, lo[0] + a, off);
@@ -1399,7 +1471,7 @@ cudaError_t launch_spread_sorted(const LatticeDesc& d, const IbDesc& ib, bool f6
                                  uint32_t* ids1, void* temp, size_t temp_bytes, cudaStream_t s) {
     const int sup = ib.dirac == BIB_DIRAC_PESKIN ? 4 : 3;
     const int64_t ne = (int64_t)nvert * sup * sup * sup;
-    k_spread_keys<<<(nvert + 127) / 128, 128, 0, s>>>(d, ib, nvert, pos, keys0, ids0);
+    k_spread_keys<<<(nvert + 127) / 128, 128, 0, s>>>(d, ib, nvert, pos, keys0, ids0, nullptr);
     cub::DoubleBuffer<uint32_t> k(keys0, keys1), v(ids0, ids1);
     size_t tb = temp_bytes;
     cudaError_t e = cub::DeviceRadixSort::SortPairs(temp, tb, k, v, (int)ne, 0, key_bits(d.n), s);
@@ -1490,9 +1562,26 @@ void update_any(int storage, const ParticleDev* parts, int np, const IbView& v1,
 
 }  // namespace
 
-void launch_interpolate_move(const Lattice& L, cudaStream_t s) {
+void launch_interpolate_move(const Lattice& L, cudaStream_t s, int fold) {
     if (L.nvert == 0) return;
-    interpolate_any<false>(L.storage, L.ib.dirac, single_view(L, -1), nullptr, nullptr, L.nvert, s);
+    if (fold < 0 || L.storage == BIB_STORAGE_F64) {
+        interpolate_any<false>(L.storage, L.ib.dirac, single_view(L, -1), nullptr, nullptr, L.nvert, s);
+        return;
+    }
+    IbView v = single_view(L, -1);
+    v.Fold = L.F[fold];
+    const unsigned g = (L.nvert + 127) / 128;
+    if (L.ib.dirac == BIB_DIRAC_PESKIN) k_interpolate_move<float, 4, false, true><<<g, 128, 0, s>>>(v, nullptr, nullptr, L.nvert);
+    else k_interpolate_move<float, 3, false, true><<<g, 128, 0, s>>>(v, nullptr, nullptr, L.nvert);
+}
+
+void launch_force_clear(const Lattice& L, int fbuf, cudaStream_t s) {
+    if (L.nvert == 0 || L.storage == BIB_STORAGE_F64) return;
+    const int sup = L.ib.dirac == BIB_DIRAC_PESKIN ? 4 : 3;
+    const int64_t threads = (int64_t)L.nvert * sup * sup;
+    const unsigned g = (unsigned)((threads + 127) / 128);
+    if (sup == 4) k_force_clear<4><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, L.spread_lo[fbuf], (float*)L.F[fbuf]);
+    else k_force_clear<3><<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, L.spread_lo[fbuf], (float*)L.F[fbuf]);
 }
 
 // CTAs per particle of the membrane kernel: enough to give every SM two CTAs, but at least
@@ -1600,14 +1689,15 @@ void launch_update_batch(const BatchLaunch& B, cudaStream_t s) {
     update_any<true>(B.storage, B.parts, B.nparts, IbView{}, B.views, B.max_nv, s);
 }
 
-void launch_spread(const Lattice& L, int fbuf, cudaStream_t s) {
+void launch_spread(const Lattice& L, int fbuf, cudaStream_t s, bool record) {
     if (L.nvert == 0) return;
     const unsigned g = (L.nvert + 127) / 128;
     const double* pos = L.pos[L.pcur];
+    int4* lo = record ? L.spread_lo[fbuf] : nullptr;
     if (L.ib.spread_mode == BIB_SPREAD_DETERMINISTIC) {
         const int sup = L.ib.dirac == BIB_DIRAC_PESKIN ? 4 : 3;
         const int64_t ne = (int64_t)L.nvert * sup * sup * sup;
-        k_spread_keys<<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.sort_keys[0], L.sort_ids[0]);
+        k_spread_keys<<<g, 128, 0, s>>>(L.d, L.ib, L.nvert, pos, L.sort_keys[0], L.sort_ids[0], lo);
         size_t tb = L.sort_temp_bytes;
         cub::DeviceRadixSort::SortPairs(L.sort_temp, tb, L.sort_keys[0], L.sort_keys[1], L.sort_ids[0], L.sort_ids[1],
                                         (int)ne, 0, key_bits(L.d.n), s);
@@ -1618,7 +1708,9 @@ void launch_spread(const Lattice& L, int fbuf, cudaStream_t s) {
             k_spread_reduce<float><<<ge, 128, 0, s>>>(L.d, L.ib, ne, L.sort_keys[1], L.sort_ids[1], pos, L.force, (float*)L.F[fbuf]);
         return;
     }
-    spread_any<false>(L.storage, L.ib.dirac, single_view(L, fbuf), nullptr, nullptr, L.nvert, s);
+    IbView v = single_view(L, fbuf);
+    v.spread_lo = lo;
+    spread_any<false>(L.storage, L.ib.dirac, v, nullptr, nullptr, L.nvert, s);
 }
 
 // Phase field of the membranes at pos (the positions of the current step's end): z-rays of

@@ -71,7 +71,8 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
     if (ctype != BIB_CELL_FLUID) {  // BounceBack / NoDynamics node: no collision, zero velocity
         if (COUPLED) {
             store_u<FT>(u_out, k, FT(0), FT(0), FT(0));
-            for (int c = 0; c < 3; ++c) Fprev[c * d.stride + k] = (FT)d.body[c];
+            if (Fprev)
+                for (int c = 0; c < 3; ++c) Fprev[c * d.stride + k] = (FT)d.body[c];
         }
         if (ctype == BIB_CELL_BOUNCE_BACK) bounce_back_cell(f);
 #pragma unroll
@@ -82,7 +83,8 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
         // computeVelocity of the current state (externalForceDynamics.hh:59-74; the wall
         // nodes give their imposed velocity, boundaryDynamics.hh:316-322), with the force of
         // the previous collision; that force buffer is then reset to the body force so the
-        // next step can spread into it (setExternalVector).
+        // next step can spread into it (setExternalVector).  Without Fprev (sparse force
+        // reset) the velocity takes the body force and the interpolation adds the rest.
         C u[3];
         if (fd_wall_node(d, y)) {
             const int side = y == 0 ? 0 : 1;
@@ -90,13 +92,20 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
             u[1] = (C)d.wall_u[side][1];
             u[2] = (C)d.wall_u[side][2];
         } else {
-            C Fp[3] = {(C)Fprev[k], (C)Fprev[d.stride + k], (C)Fprev[2 * d.stride + k]};
+            C Fp[3] = {(C)d.body[0], (C)d.body[1], (C)d.body[2]};
+            if (Fprev) {
+                Fp[0] = (C)Fprev[k];
+                Fp[1] = (C)Fprev[d.stride + k];
+                Fp[2] = (C)Fprev[2 * d.stride + k];
+            }
             velocity_with_force(f, Fp, u);
         }
         store_u<FT>(u_out, k, (FT)u[0], (FT)u[1], (FT)u[2]);
-        Fprev[k] = (FT)d.body[0];
-        Fprev[d.stride + k] = (FT)d.body[1];
-        Fprev[2 * d.stride + k] = (FT)d.body[2];
+        if (Fprev) {
+            Fprev[k] = (FT)d.body[0];
+            Fprev[d.stride + k] = (FT)d.body[1];
+            Fprev[2 * d.stride + k] = (FT)d.body[2];
+        }
     }
     C Fc[3] = {(C)__ldg(Fcol + k), (C)__ldg(Fcol + d.stride + k), (C)__ldg(Fcol + 2 * d.stride + k)};
     if (coll == BIB_COLLISION_BGK_GUO_VOF) {
@@ -189,8 +198,13 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
     }
     if (active) {
         for (int c = 0; c < 3; ++c) load2<FT>(Fcol + c * d.stride + k0, fca[c], fcb[c]);
-        if (COUPLED && !wallrow)
-            for (int c = 0; c < 3; ++c) load2<FT>(Fprev + c * d.stride + k0, fpa[c], fpb[c]);
+        if (COUPLED && !wallrow) {
+            if (Fprev) {
+                for (int c = 0; c < 3; ++c) load2<FT>(Fprev + c * d.stride + k0, fpa[c], fpb[c]);
+            } else {  // sparse force reset: the velocity field takes the body force only
+                for (int c = 0; c < 3; ++c) fpa[c] = fpb[c] = (FT)d.body[c];
+            }
+        }
     }
     // ---- phase 2: assemble the gathered populations (x shifts through the warp)
     C f0[Q], f1[Q];
@@ -242,9 +256,8 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
         if (ct1 != BIB_CELL_FLUID) u1[0] = u1[1] = u1[2] = C(0);
         store_u<FT>(u_out, k0, (FT)u0[0], (FT)u0[1], (FT)u0[2]);
         store_u<FT>(u_out, k0 + 1, (FT)u1[0], (FT)u1[1], (FT)u1[2]);
-        for (int c = 0; c < 3; ++c) {
-            store2<FT>(Fprev + c * d.stride + k0, (FT)d.body[c], (FT)d.body[c]);
-        }
+        if (Fprev)
+            for (int c = 0; c < 3; ++c) store2<FT>(Fprev + c * d.stride + k0, (FT)d.body[c], (FT)d.body[c]);
     }
     C Fa[3] = {(C)fca[0], (C)fca[1], (C)fca[2]}, Fb[3] = {(C)fcb[0], (C)fcb[1], (C)fcb[2]};
     C om0 = (C)d.omega, om1 = (C)d.omega, omm = C(0);
@@ -573,9 +586,12 @@ inline dim3 row_grid(const LatticeDesc& d, int bx) { return dim3((d.nx + bx - 1)
 inline unsigned lin_grid(int64_t n, int b) { return (unsigned)((n + b - 1) / b); }
 
 template <class T>
-void collide_stream_t(const Lattice& L, bool coupled, cudaStream_t s) {
+void collide_stream_t(const Lattice& L, Coupling mode, cudaStream_t s) {
     using FT = typename Store<T>::F;
-    if (L.collide_kernel != BIB_KERNEL_ROWS && launch_collide_stream_staged(L, coupled, s)) return;
+    if (L.collide_kernel != BIB_KERNEL_ROWS && launch_collide_stream_staged(L, mode, s)) return;
+    const bool coupled = mode != Coupling::kNone;
+    // the previous force, read for the velocity and reset (dense coupling only)
+    FT* Fprev = mode == Coupling::kDense ? (FT*)L.F[L.fe] : nullptr;
     if (L.d.nx % 2 == 0) {
         const int pairs = L.d.nx / 2;
         const int bx = std::min(256, (pairs + 31) / 32 * 32);
@@ -587,7 +603,7 @@ void collide_stream_t(const Lattice& L, bool coupled, cudaStream_t s) {
         T* fout = (T*)L.f[1 - L.cur];
         if (coupled)
             k_collide_stream_rows<T, true><<<grid, block, 0, s>>>(L.d, fin, fout, (const T*)L.wall, (const FT*)L.F[1 - L.fe],
-                                                                  (FT*)L.F[L.fe], (FT*)L.u, L.phase, L.celltype, L.d.collision);
+                                                                  Fprev, (FT*)L.u, L.phase, L.celltype, L.d.collision);
         else
             k_collide_stream_rows<T, false><<<grid, block, 0, s>>>(L.d, fin, fout, (const T*)L.wall, (const FT*)L.F[L.fe],
                                                                    nullptr, nullptr, L.phase, L.celltype, L.d.collision);
@@ -599,7 +615,7 @@ void collide_stream_t(const Lattice& L, bool coupled, cudaStream_t s) {
     const T* wall = (const T*)L.wall;
     if (coupled) {
         k_collide_stream<T, true><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, fin, fout, wall, (const FT*)L.F[1 - L.fe],
-                                                                    (FT*)L.F[L.fe], (FT*)L.u, L.phase, L.celltype, L.d.collision);
+                                                                    Fprev, (FT*)L.u, L.phase, L.celltype, L.d.collision);
     } else {
         k_collide_stream<T, false><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, fin, fout, wall, (const FT*)L.F[L.fe], nullptr,
                                                                      nullptr, L.phase, L.celltype, L.d.collision);
@@ -685,8 +701,8 @@ void nan_scan_t(const Lattice& L, int* flag, cudaStream_t s) {
 
 }  // namespace
 
-void launch_collide_stream(const Lattice& L, bool coupled, cudaStream_t s) {
-    BIB_DISPATCH(L.storage, collide_stream_t, L, coupled, s);
+void launch_collide_stream(const Lattice& L, Coupling mode, cudaStream_t s) {
+    BIB_DISPATCH(L.storage, collide_stream_t, L, mode, s);
 }
 
 void launch_fd_walls_batch(const BatchLaunch& B, cudaStream_t s) {

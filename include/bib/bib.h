@@ -136,8 +136,16 @@ typedef struct {
     int32_t tile_cells;     /* staged kernel: cells per tile (whole x-rows); 0 = 512 (256 for FP64) */
     int32_t stages;         /* staged kernel: pipeline depth 2..4; 0 = the deepest that keeps the CTAs resident */
     int32_t membrane_block; /* threads per particle of the membrane kernel: 64 .. 512 (power of two), 0 = 256 */
-    int32_t reserved[4];
+    int32_t force_reset;    /* BIB_FORCE_RESET_*: how the coupled step resets the previous force field */
+    int32_t wait_limit_us;  /* staged kernel: bound of each hand-off wait between its warps, in microseconds
+                             * (0 = 2 s).  A wait that runs out makes the launch give up and bib_check_health
+                             * return BIB_ETIMEOUT; the wait for the kernel's own copies in flight keeps 2 s */
+    int32_t reserved[2];
 } bib_tuning;
+/* AUTO: reduced-precision lattices without phase field, cell types, second-order walls or pipe
+ * boundary reset only the nodes the last spreading wrote (the collide-and-stream then neither reads
+ * nor rewrites the previous force field); DENSE: every step reads and resets the whole field */
+enum { BIB_FORCE_RESET_AUTO = 0, BIB_FORCE_RESET_DENSE = 1 };
 
 /* ---- context (src/coProcessors/coProcessor3D.h:57-115 lifetime) ---- */
 bib_status bib_create(const bib_config* cfg, bib_ctx** out);

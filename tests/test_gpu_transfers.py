@@ -45,18 +45,26 @@ def wire(layout, f, F=None, phase=None):
     return np.ascontiguousarray(np.concatenate([cells, ext], axis=1))
 
 
+WALLS = {
+    # finite-difference velocity walls on y (their nodes live in the wall buffer), periodic x and z
+    "fd": dict(periodic=(1, 0, 1), wall_y="fd_velocity", wall_u=[[-0.01, 0, 0], [0.01, 0, 0], [0, 0, 0], [0, 0, 0]]),
+    # halfway bounce-back on y and z (a moving wall on z-), periodic x
+    "bb": dict(periodic=(1, 0, 0), wall_y="halfway_bb", wall_z="halfway_bb",
+               wall_u=[[0, 0, 0], [0, 0, 0], [0.01, 0, 0], [0, 0, 0]]),
+}
+
+
+@pytest.mark.parametrize("walls", ["fd", "bb"])
 @pytest.mark.parametrize("storage", ["f64", "f32", "f16"])
 @pytest.mark.parametrize("layout", ["soa", "palabos", "coprocessor"])
-def test_pinned_and_pageable_transfers_agree(ctx, storage, layout):
+def test_pinned_and_pageable_transfers_agree(ctx, storage, layout, walls):
     # 128 x 64 x 40: 6.2 M doubles of populations, two staging chunks of each order
     nx, ny, nz = 128, 64, 40
     rng = np.random.default_rng(7)
     f = rng.uniform(-0.01, 0.01, (19, nz, ny, nx))
     F = rng.uniform(-1e-4, 1e-4, (3, nz, ny, nx))
     phase = (rng.uniform(size=(nz, ny, nx)) < 0.3).astype(np.float64)
-    U = 0.01
-    kw = dict(periodic=(1, 0, 0), storage=storage, omega=1.0, use_phase=layout == "palabos",
-              wall_y="fd_velocity", wall_z="halfway_bb", wall_u=[[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]])
+    kw = dict(storage=storage, omega=1.0, use_phase=layout == "palabos", **WALLS[walls])
     buf = wire(layout, f, F, phase)
     results = {}
     for kind, host in (("pageable", buf.copy()), ("pinned", pinned_like(buf))):
