@@ -35,6 +35,11 @@ METRIC = "MLUPS (coupled IB-LBM step) + membrane vertex-updates/s, FP16/FP32 sto
 # written (FP32 fields for FP32 / FP16 storage, FP64 for FP64); no phase byte at viscosity
 # ratio 1.
 BYTES_PER_LU = {"f64": 19 * 8 * 2 + 2 * 3 * 8, "f32": 19 * 4 * 2 + 2 * 3 * 4, "f16": 19 * 2 * 2 + 2 * 3 * 4}
+# What the kernel moves per cell with the default (dense) reset of the previous force field:
+# the above plus that field read and rewritten with the body force (the reference's
+# computeVelocity takes the previous force, setExternalVector resets it) and the velocity
+# field's fourth (pad) component.
+KERNEL_BYTES_PER_LU = {st: b + (2 * 3 + 1) * (8 if st == "f64" else 4) for st, b in BYTES_PER_LU.items()}
 # Steps of the precision comparison: the run lengths of the benchmark configurations
 COMPARE_STEPS = {"channel": 2000, "capsule": 2000, "rbc": 5000}
 
@@ -670,6 +675,8 @@ def main():
         "kernels_per_step": kernels_per_step,
         "roofline": {"bound": "hbm", "kernel": kernel[args.storage], "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "traffic": traffic, "algorithmic_bytes_per_cell": bytes_lu,
+                     "kernel_bytes_per_cell": KERNEL_BYTES_PER_LU[args.storage],
+                     "kernel_gbs": KERNEL_BYTES_PER_LU[args.storage] * cells / (coll_ms * 1e-3) / 1e9,
                      "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6800 GB/s"},
         "clocks": clk.summary(),
         "variants": variants,

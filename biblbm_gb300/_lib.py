@@ -69,6 +69,7 @@ SIGNATURES = {
     "bib_set_profiling": (C.c_int32, [_vp, C.c_int32]),
     "bib_profile_read": (C.c_int32, [_vp, _dp, C.c_int32]),
     "bib_lattice_add_domain": (C.c_int32, [_vp, C.c_int64, C.c_int64, C.c_int64, C.POINTER(LatticeParams), _i32p]),
+    "bib_coprocessor_domain_params": (C.c_int32, [C.c_double, C.c_int32, C.c_int32, C.POINTER(LatticeParams)]),
     "bib_lattice_cells": (C.c_int32, [_vp, C.c_int32, _ip]),
     "bib_lattice_send": (C.c_int32, [_vp, C.c_int32, _vp, C.c_size_t, C.c_int32]),
     "bib_lattice_receive": (C.c_int32, [_vp, C.c_int32, _vp, C.c_size_t, C.c_int32]),

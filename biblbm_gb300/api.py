@@ -249,14 +249,14 @@ class Lattice:
                    wait_limit_us=0):
         """Collide-and-stream kernel ("auto", "rows" or "staged"), staged tile size in cells,
         pipeline depth, membrane-kernel block size (0: automatic / default), the reset of the
-        previous force field ("auto": sparse where the lattice allows it, "dense") and the bound
-        of the staged kernel's hand-off waits in microseconds (0: 2 s)."""
+        previous force field ("auto" = "dense", or "sparse" where the lattice allows it) and the
+        bound of the staged kernel's hand-off waits in microseconds (0: 2 s)."""
         t = Tuning()
         t.collide_kernel = KERNEL[kernel]
         t.tile_cells = int(tile_cells)
         t.stages = int(stages)
         t.membrane_block = int(membrane_block)
-        t.force_reset = {"auto": 0, "dense": 1}[force_reset]
+        t.force_reset = {"auto": 0, "dense": 1, "sparse": 2}[force_reset]
         t.wait_limit_us = int(wait_limit_us)
         self.ctx.check(self.ctx.lib.bib_lattice_set_tuning(self.ctx.h, self.h, C.byref(t)))
 

@@ -304,10 +304,11 @@ void moment_of_inertia(const ShapeHost& S, const double* pos, double* I) {
 void forces_touched(Lattice& L) { L.sparse_ok[0] = L.sparse_ok[1] = false; }
 
 // The coupled step resets the previous force field sparsely (only where the spreading wrote)
-// on reduced-precision lattices whose velocity field near the membranes is j/rho + F/2 at
-// every node: no phase field, cell types, second-order walls or pipe boundary.
+// when the tuning asks for it, on reduced-precision lattices whose velocity field near the
+// membranes is j/rho + F/2 at every node: no phase field, cell types, second-order walls or pipe
+// boundary.
 bool sparse_coupling(const Lattice& L) {
-    return !L.dense_reset && L.storage != BIB_STORAGE_F64 && L.nvert > 0 && !L.phase && !L.celltype && L.nguo == 0 &&
+    return L.sparse_reset && L.storage != BIB_STORAGE_F64 && L.nvert > 0 && !L.phase && !L.celltype && L.nguo == 0 &&
            !L.ib.has_pipe && L.spread_lo[0] && L.spread_lo[1];
 }
 
@@ -1570,7 +1571,7 @@ bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     if (t->collide_kernel < BIB_KERNEL_AUTO || t->collide_kernel > BIB_KERNEL_STAGED || t->tile_cells < 0 ||
         t->stages < 0 || t->stages == 1 || t->stages > 4 ||
         (mb != 0 && mb != 64 && mb != 128 && mb != 256 && mb != 512) ||
-        (t->force_reset != BIB_FORCE_RESET_AUTO && t->force_reset != BIB_FORCE_RESET_DENSE) || t->wait_limit_us < 0)
+        (t->force_reset < BIB_FORCE_RESET_AUTO || t->force_reset > BIB_FORCE_RESET_SPARSE) || t->wait_limit_us < 0)
         return fail(c, BIB_EINVAL, "invalid tuning values");
     Lattice probe = {};
     probe.d = L->d;
@@ -1584,7 +1585,7 @@ bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     L->tile_cells = t->tile_cells;
     L->stages = t->stages;
     L->membrane_block = mb ? mb : 256;
-    L->dense_reset = t->force_reset == BIB_FORCE_RESET_DENSE;
+    L->sparse_reset = t->force_reset == BIB_FORCE_RESET_SPARSE;
     L->wait_ns = t->wait_limit_us ? (uint64_t)t->wait_limit_us * 1000u : kDefaultWaitNs;
     forces_touched(*L);
     return BIB_OK;
@@ -2162,6 +2163,20 @@ bib_status bib_step_timed(bib_ctx* c, int32_t h, int64_t nsteps, double* ms) {
     cudaEventDestroy(b);
     *ms = f;
     return st;
+}
+
+bib_status bib_coprocessor_domain_params(double omega, int32_t storage, int32_t collision, bib_lattice_params* p) {
+    if (!p || !(omega > 0.0 && omega < 2.0)) return BIB_EINVAL;
+    if (storage != BIB_STORAGE_F64 && storage != BIB_STORAGE_F32 && storage != BIB_STORAGE_F16) return BIB_EINVAL;
+    if (collision != BIB_COLLISION_BGK && collision != BIB_COLLISION_BGK_GUO_VOF) return BIB_EINVAL;
+    std::memset(p, 0, sizeof(*p));
+    p->periodic[0] = p->periodic[1] = p->periodic[2] = 1;
+    p->collision = collision;
+    p->storage = storage;
+    p->wall_y = p->wall_z = BIB_WALL_NONE;
+    p->omega = p->omega_inner = omega;
+    p->trt_magic = 0.25;
+    return BIB_OK;
 }
 
 bib_status bib_step_kernel_count(bib_ctx* c, int32_t h, int32_t* kernels_per_step) {

@@ -229,14 +229,14 @@ struct Lattice {
     void* F[2] = {nullptr, nullptr};  // force fields (double for F64 storage, float otherwise)
     int fe = 0;
     bool target_clean = false;        // F[1-fe] holds the body force, ready to receive spreading
-    // Sparse force reset (reduced-precision storage, coupled step, no phase field, cell types or
-    // pipe boundary): the collision reads only the spread force of its step, and the field of
+    // Sparse force reset (opt-in; reduced-precision storage, coupled step, no phase field, cell
+    // types or pipe boundary): the collision reads only the spread force of its step, and the field of
     // the previous step is reset to the body force only where its spreading wrote (the support
     // nodes recorded in spread_lo[b] for F[b]).  sparse_ok[b]: F[b] differs from the body force
     // only at the nodes in spread_lo[b].
     int4* spread_lo[2] = {nullptr, nullptr};
     bool sparse_ok[2] = {false, false};
-    bool dense_reset = false;  // tuning: always the dense reset
+    bool sparse_reset = false;  // tuning: the sparse reset where the lattice allows it
     uint64_t wait_ns = kDefaultWaitNs;  // bound of the staged kernel's hand-off waits
     void* u = nullptr;                // velocity field, (ux, uy, uz, 0) per cell (double for F64 storage, float otherwise)
     uint8_t* phase = nullptr;

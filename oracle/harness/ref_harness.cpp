@@ -45,6 +45,8 @@
 //           and one random orientation quaternion per particle, drawn as the driver draws them
 //   lattice_load  parallelIO::load(name, lattice, false) (io/multiBlockReader3D.cpp:135-268) of
 //           in/ckpt.plb into a fresh lattice; dumps its populations, forces and phase
+//   coprocessor  D3Q19ExampleCoProcessor3D (coProcessors/coProcessor3D.hh:34-78): addDomain,
+//           send of given bytes, collideAndStream, receive
 //
 // Array conventions: lattice fields are (components, nz, ny, nx) with x fastest.
 #define FSI_PROFILE
@@ -993,6 +995,33 @@ static int run_initial(const Bundle& in, const char* out) {
     return 0;
 }
 
+// Palabos' example co-processor (coProcessors/coProcessor3D.hh:34-78): addDomain with the given
+// omega, send of the given cell-major bytes (19 f-bar per cell, z fastest), one collideAndStream,
+// receive; dumps the received bytes as doubles.
+static int run_coprocessor(const Bundle& in, const char* out) {
+    const std::vector<long long> dims = recio::need(in, "dims").i;
+    const T omega = recio::num(in, "omega");
+    const std::vector<double> data = recio::need(in, "data").d;
+    const plint nx = dims[0], ny = dims[1], nz = dims[2];
+    D3Q19ExampleCoProcessor3D<T> cp;
+    int handle = -1;
+    if (cp.addDomain(nx, ny, nz, omega, handle) != 1) return 3;
+    const Box3D box(0, nx - 1, 0, ny - 1, 0, nz - 1);
+    std::vector<char> bytes(data.size() * sizeof(double));
+    std::memcpy(&bytes[0], &data[0], bytes.size());
+    if (cp.send(handle, box, bytes) != 1) return 3;
+    const plint steps = recio::inum(in, "steps");
+    for (plint s = 0; s < steps; ++s)
+        if (cp.collideAndStream(handle) != 1) return 3;
+    std::vector<char> back;
+    if (cp.receive(handle, box, back) != 1) return 3;
+    std::vector<double> res(back.size() / sizeof(double));
+    std::memcpy(&res[0], &back[0], back.size());
+    recio::Writer w(out);
+    w.d("data", shp(nx, ny, nz, Q), res);
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) {
         std::fprintf(stderr, "usage: ref_harness <lbm|ibm|forces|interp|shape|inertia> in.rec out.rec\n");
@@ -1017,6 +1046,7 @@ int main(int argc, char** argv) {
     if (c == "lattice_load") return run_lattice_load(in, argv[3]);
     if (c == "calibrate") return run_calibrate(in, argv[3]);
     if (c == "initial") return run_initial(in, argv[3]);
+    if (c == "coprocessor") return run_coprocessor(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

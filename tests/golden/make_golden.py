@@ -500,9 +500,30 @@ def case_initial():
     save("initial_distribution", inp, out)
 
 
+def case_coprocessor():
+    """Palabos' example co-processor (D3Q19ExampleCoProcessor3D, BGK): a seeded 14 x 11 x 9 block
+    of f-bar in the CoProcessor3D byte order (19 populations per cell, z fastest, x slowest)
+    sent, collided and streamed twice, received; the one-cell outer layer is undefined by the
+    interface (coProcessor3D.h:105-107)."""
+    rng = np.random.default_rng(21)
+    nx, ny, nz = 14, 11, 9
+    rho = 1.0 + rng.uniform(-0.02, 0.02, (nx, ny, nz))
+    u = rng.uniform(-0.03, 0.03, (nx, ny, nz, 3))
+    j = rho[..., None] * u
+    jsq = (j * j).sum(-1)
+    fbar = np.empty((nx, ny, nz, 19))
+    for i in range(19):  # BGK equilibrium plus a seeded non-equilibrium part
+        cj = C[i, 0] * j[..., 0] + C[i, 1] * j[..., 1] + C[i, 2] * j[..., 2]
+        fbar[..., i] = W[i] * ((rho - 1.0) + 3 * cj + (4.5 * cj * cj - 1.5 * jsq) / rho)
+    fbar += rng.uniform(-1e-3, 1e-3, fbar.shape) * W[None, None, None, :]
+    inp = dict(dims=np.array([nx, ny, nz]), omega=1.0 / 0.83, steps=2, data=fbar)
+    out = run("coprocessor", inp)
+    save("coprocessor_bgk", inp, out)
+
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
          case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo, case_ibm_pipe,
-         case_reflect, case_plb, case_lattice_plb, case_calibrate, case_initial]
+         case_reflect, case_plb, case_lattice_plb, case_calibrate, case_initial, case_coprocessor]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
