@@ -39,7 +39,7 @@ class IbParams(C.Structure):
 class Tuning(C.Structure):
     _fields_ = [("collide_kernel", C.c_int32), ("tile_cells", C.c_int32), ("stages", C.c_int32),
                 ("membrane_block", C.c_int32), ("force_reset", C.c_int32), ("wait_limit_us", C.c_int32),
-                ("reserved", C.c_int32 * 2)]
+                ("withhold_tile", C.c_int32), ("reserved", C.c_int32 * 1)]
 
 
 class BatchTuning(C.Structure):

@@ -246,7 +246,7 @@ class Lattice:
                                                                int(bool(second_order))))
 
     def set_tuning(self, kernel="auto", tile_cells=0, stages=0, membrane_block=0, force_reset="auto",
-                   wait_limit_us=0):
+                   wait_limit_us=0, withhold_tile=0):
         """Collide-and-stream kernel ("auto", "rows" or "staged"), staged tile size in cells,
         pipeline depth, membrane-kernel block size (0: automatic / default), the reset of the
         previous force field ("auto" = "dense", or "sparse" where the lattice allows it) and the
@@ -258,6 +258,7 @@ class Lattice:
         t.membrane_block = int(membrane_block)
         t.force_reset = {"auto": 0, "dense": 1, "sparse": 2}[force_reset]
         t.wait_limit_us = int(wait_limit_us)
+        t.withhold_tile = int(withhold_tile)  # failure tests only: 1 + a staged tile left uncopied
         self.ctx.check(self.ctx.lib.bib_lattice_set_tuning(self.ctx.h, self.h, C.byref(t)))
 
 

@@ -3,6 +3,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstdarg>
+#include <cstdlib>
 #include <cstdio>
 #include <cstring>
 #include <functional>
@@ -44,6 +45,9 @@ struct bib_ctx {
     size_t stage_count = 0;   // size of both halves in doubles
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t tx_ready[2] = {}, tx_free[2] = {}, tx_start = nullptr;
+    // device allocations made so far, and the index of one that is made to fail (the
+    // environment variable BIB_FAIL_DEVICE_ALLOC at bib_create; -1: none), for failure tests
+    int64_t alloc_count = 0, fail_alloc = -1;
     std::vector<std::unique_ptr<Batch>> batches;
     ~bib_ctx();
 };
@@ -68,6 +72,28 @@ bib_status fail(bib_ctx* c, bib_status s, const char* fmt, ...) {
     } while (0)
 
 #define BIB_CHECK_LAUNCH(ctx) BIB_CUDA(ctx, cudaGetLastError())
+
+// Every device allocation of a context: cudaMalloc, except the one that BIB_FAIL_DEVICE_ALLOC
+// names, which fails as an exhausted device would (cudaErrorMemoryAllocation).
+cudaError_t dev_malloc(bib_ctx* c, void** p, size_t bytes) {
+    const int64_t k = c->alloc_count++;
+    if (k == c->fail_alloc) {
+        *p = nullptr;
+        return cudaErrorMemoryAllocation;
+    }
+    return cudaMalloc(p, bytes);
+}
+
+#define BIB_ALLOC(ctx, ptr, bytes)                                                                        \
+    do {                                                                                                  \
+        const size_t b_ = (bytes);                                                                        \
+        cudaError_t e_ = dev_malloc(ctx, (void**)(ptr), b_);                                              \
+        if (e_ != cudaSuccess) {                                                                          \
+            cudaGetLastError();                                                                           \
+            return fail(ctx, BIB_ENOMEM, "device allocation of %zu bytes failed (%s:%d): %s", b_, __FILE__, \
+                        __LINE__, cudaGetErrorString(e_));                                                \
+        }                                                                                                 \
+    } while (0)
 
 Lattice* get_lattice(bib_ctx* c, int32_t h) {
     if (!c || h < 0 || h >= (int32_t)c->lattices.size() || !c->lattices[h]) return nullptr;
@@ -205,7 +231,7 @@ template <class T>
 bib_status upload(bib_ctx* c, T** dptr, const std::vector<T>& v) {
     *dptr = nullptr;
     if (v.empty()) return BIB_OK;
-    BIB_CUDA(c, cudaMalloc((void**)dptr, v.size() * sizeof(T)));
+    BIB_ALLOC(c, (void**)dptr, v.size() * sizeof(T));
     BIB_CUDA(c, cudaMemcpy(*dptr, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice));
     return BIB_OK;
 }
@@ -376,12 +402,12 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
         return BIB_OK;
     }
     const size_t vb = 3 * (size_t)L.nvert * sizeof(double);
-    for (int k = 0; k < 2; ++k) BIB_CUDA(c, cudaMalloc((void**)&L.pos[k], vb));
-    BIB_CUDA(c, cudaMalloc((void**)&L.vel, vb));
-    BIB_CUDA(c, cudaMalloc((void**)&L.force, vb));
-    BIB_CUDA(c, cudaMalloc((void**)&L.stats, STATS * np * sizeof(double)));
-    BIB_CUDA(c, cudaMalloc((void**)&L.upd_partial, (size_t)np * 64 * 5 * sizeof(double)));
-    for (int k = 0; k < 2; ++k) BIB_CUDA(c, cudaMalloc((void**)&L.spread_lo[k], (size_t)L.nvert * sizeof(int4)));
+    for (int k = 0; k < 2; ++k) BIB_ALLOC(c, (void**)&L.pos[k], vb);
+    BIB_ALLOC(c, (void**)&L.vel, vb);
+    BIB_ALLOC(c, (void**)&L.force, vb);
+    BIB_ALLOC(c, (void**)&L.stats, STATS * np * sizeof(double));
+    BIB_ALLOC(c, (void**)&L.upd_partial, (size_t)np * 64 * 5 * sizeof(double));
+    for (int k = 0; k < 2; ++k) BIB_ALLOC(c, (void**)&L.spread_lo[k], (size_t)L.nvert * sizeof(int4));
     forces_touched(L);
     BIB_CUDA(c, cudaMemcpy(L.pos[0], L.host_pos.data(), vb, cudaMemcpyHostToDevice));
     BIB_CUDA(c, cudaMemcpy(L.pos[1], L.host_pos.data(), vb, cudaMemcpyHostToDevice));
@@ -430,20 +456,20 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
         const int64_t ne = (int64_t)L.nvert * sup * sup * sup;
         if (ne >= (int64_t)1 << 31) return fail(c, BIB_EUNSUPPORTED, "too many spreading entries for the sort");
         for (int k = 0; k < 2; ++k) {
-            BIB_CUDA(c, cudaMalloc((void**)&L.sort_keys[k], ne * sizeof(uint32_t)));
-            BIB_CUDA(c, cudaMalloc((void**)&L.sort_ids[k], ne * sizeof(uint32_t)));
+            BIB_ALLOC(c, (void**)&L.sort_keys[k], ne * sizeof(uint32_t));
+            BIB_ALLOC(c, (void**)&L.sort_ids[k], ne * sizeof(uint32_t));
         }
         L.sort_temp_bytes = spread_sort_temp_bytes(ne);
-        BIB_CUDA(c, cudaMalloc(&L.sort_temp, L.sort_temp_bytes));
+        BIB_ALLOC(c, &L.sort_temp, L.sort_temp_bytes);
     }
     {
         std::vector<int> vp(L.nvert);
         for (int p = 0; p < np; ++p)
             for (int v = 0; v < L.parts[p].nv; ++v) vp[L.parts[p].v0 + v] = p;
-        BIB_CUDA(c, cudaMalloc((void**)&L.vert_particle, L.nvert * sizeof(int)));
+        BIB_ALLOC(c, (void**)&L.vert_particle, L.nvert * sizeof(int));
         BIB_CUDA(c, cudaMemcpy(L.vert_particle, vp.data(), L.nvert * sizeof(int), cudaMemcpyHostToDevice));
     }
-    BIB_CUDA(c, cudaMalloc((void**)&L.pdev, np * sizeof(ParticleDev)));
+    BIB_ALLOC(c, (void**)&L.pdev, np * sizeof(ParticleDev));
     BIB_CUDA(c, cudaMemcpy(L.pdev, pd.data(), np * sizeof(ParticleDev), cudaMemcpyHostToDevice));
     L.pdev_host = pd;
     L.membrane_smem = membrane_smem_bytes(L.max_nv);
@@ -465,24 +491,24 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
         G.bits = 0;
         while ((1u << G.bits) < G.table) ++G.bits;
         for (int k = 0; k < 2; ++k) {
-            BIB_CUDA(c, cudaMalloc((void**)&G.keys[k], L.nvert * sizeof(uint32_t)));
-            BIB_CUDA(c, cudaMalloc((void**)&G.ids[k], L.nvert * sizeof(uint32_t)));
+            BIB_ALLOC(c, (void**)&G.keys[k], L.nvert * sizeof(uint32_t));
+            BIB_ALLOC(c, (void**)&G.ids[k], L.nvert * sizeof(uint32_t));
         }
         BIB_CUDA(c, cudaMemset(G.keys[1], 0, L.nvert * sizeof(uint32_t)));
-        BIB_CUDA(c, cudaMalloc((void**)&G.start, G.table * sizeof(int)));
-        BIB_CUDA(c, cudaMalloc((void**)&G.end, G.table * sizeof(int)));
+        BIB_ALLOC(c, (void**)&G.start, G.table * sizeof(int));
+        BIB_ALLOC(c, (void**)&G.end, G.table * sizeof(int));
         BIB_CUDA(c, cudaMemset(G.start, 0, G.table * sizeof(int)));
         BIB_CUDA(c, cudaMemset(G.end, 0, G.table * sizeof(int)));
         G.temp_bytes = pp_sort_temp_bytes(L.nvert, G.bits);
-        BIB_CUDA(c, cudaMalloc(&G.temp, std::max<size_t>(G.temp_bytes, 16)));
+        BIB_ALLOC(c, &G.temp, std::max<size_t>(G.temp_bytes, 16));
     }
     if (L.phase) {
         // the reference voxelizes the membranes into the phase field when the immersed-boundary
         // functional first runs (ImmersedBoundaryDynamics.hh:404-412) and after every move
         const int64_t ncol = (int64_t)L.d.nx * L.d.ny;
-        BIB_CUDA(c, cudaMalloc((void**)&L.vox_count, ncol * sizeof(int)));
+        BIB_ALLOC(c, (void**)&L.vox_count, ncol * sizeof(int));
         BIB_CUDA(c, cudaMemset(L.vox_count, 0, ncol * sizeof(int)));
-        BIB_CUDA(c, cudaMalloc((void**)&L.vox_z, ncol * kVoxelCap * sizeof(double)));
+        BIB_ALLOC(c, (void**)&L.vox_z, ncol * kVoxelCap * sizeof(double));
         launch_voxelize(L, L.pos[L.pcur], c->stream);
     }
     BIB_CHECK_LAUNCH(c);
@@ -778,7 +804,7 @@ bib_status transfer_setup(bib_ctx* c, size_t unit, int64_t units, int64_t* per_c
         cudaFree(c->stage);
         c->stage = nullptr;
         c->stage_count = 0;
-        BIB_CUDA(c, cudaMalloc((void**)&c->stage, 2 * half * sizeof(double)));
+        BIB_ALLOC(c, (void**)&c->stage, 2 * half * sizeof(double));
         c->stage_count = 2 * half;
     }
     *per_chunk = (int64_t)std::min<size_t>(c->stage_count / 2 / unit, (size_t)units);
@@ -891,7 +917,7 @@ bib_status export_populations(bib_ctx* c, Lattice& L, double* dst, Wire w) {
 }
 
 bib_status device_buffer(bib_ctx* c, double** d, const double* host, size_t count) {
-    BIB_CUDA(c, cudaMalloc((void**)d, count * sizeof(double)));
+    BIB_ALLOC(c, (void**)d, count * sizeof(double));
     if (host) BIB_CUDA(c, cudaMemcpyAsync(*d, host, count * sizeof(double), cudaMemcpyHostToDevice, c->stream));
     return BIB_OK;
 }
@@ -1200,6 +1226,7 @@ bib_status bib_create(const bib_config* cfg, bib_ctx** out) {
     bib_ctx* c = new (std::nothrow) bib_ctx();
     if (!c) return BIB_ENOMEM;
     c->device = cfg ? cfg->device : 0;
+    if (const char* fa = std::getenv("BIB_FAIL_DEVICE_ALLOC")) c->fail_alloc = std::atoll(fa);
     cudaError_t e = cudaSetDevice(c->device);
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
     for (int k = 0; k < 6 && e == cudaSuccess; ++k) e = cudaEventCreate(&c->ev[k]);
@@ -1438,7 +1465,7 @@ static bib_status set_cell_types_impl(bib_ctx* c, int32_t h, const uint8_t* type
     } else {
         for (int64_t k = 0; k < L->d.n; ++k)
             if (types[k] > BIB_CELL_NO_DYNAMICS) return fail(c, BIB_EINVAL, "cell type %d at cell %lld", (int)types[k], (long long)k);
-        if (!L->celltype) BIB_CUDA(c, cudaMalloc((void**)&L->celltype, L->d.n));
+        if (!L->celltype) BIB_ALLOC(c, (void**)&L->celltype, L->d.n);
         BIB_CUDA(c, cudaMemcpy(L->celltype, types, L->d.n, cudaMemcpyHostToDevice));
         L->d.has_types = 1;
     }
@@ -1557,7 +1584,7 @@ bib_status bib_lattice_set_pipe_walls(bib_ctx* c, int32_t h, double y0, double z
     L->guo = nullptr;
     L->nguo = 0;
     if (!nodes.empty()) {
-        BIB_CUDA(c, cudaMalloc((void**)&L->guo, nodes.size() * sizeof(GuoNode)));
+        BIB_ALLOC(c, (void**)&L->guo, nodes.size() * sizeof(GuoNode));
         BIB_CUDA(c, cudaMemcpy(L->guo, nodes.data(), nodes.size() * sizeof(GuoNode), cudaMemcpyHostToDevice));
         L->nguo = (int)nodes.size();
     }
@@ -1571,7 +1598,8 @@ bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     if (t->collide_kernel < BIB_KERNEL_AUTO || t->collide_kernel > BIB_KERNEL_STAGED || t->tile_cells < 0 ||
         t->stages < 0 || t->stages == 1 || t->stages > 4 ||
         (mb != 0 && mb != 64 && mb != 128 && mb != 256 && mb != 512) ||
-        (t->force_reset < BIB_FORCE_RESET_AUTO || t->force_reset > BIB_FORCE_RESET_SPARSE) || t->wait_limit_us < 0)
+        (t->force_reset < BIB_FORCE_RESET_AUTO || t->force_reset > BIB_FORCE_RESET_SPARSE) || t->wait_limit_us < 0 ||
+        t->withhold_tile < 0)
         return fail(c, BIB_EINVAL, "invalid tuning values");
     Lattice probe = {};
     probe.d = L->d;
@@ -1587,6 +1615,7 @@ bib_status bib_lattice_set_tuning(bib_ctx* c, int32_t h, const bib_tuning* t) {
     L->membrane_block = mb ? mb : 256;
     L->sparse_reset = t->force_reset == BIB_FORCE_RESET_SPARSE;
     L->wait_ns = t->wait_limit_us ? (uint64_t)t->wait_limit_us * 1000u : kDefaultWaitNs;
+    L->withhold_tile = (int64_t)t->withhold_tile - 1;
     forces_touched(*L);
     return BIB_OK;
 }
@@ -1618,6 +1647,14 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
     if (!p->periodic[2] && p->wall_z == BIB_WALL_NONE) return fail(c, BIB_EINVAL, "non-periodic z needs a wall type");
     if (!p->periodic[2] && p->wall_z == BIB_WALL_FD_VELOCITY)
         return fail(c, BIB_EUNSUPPORTED, "finite-difference velocity walls are implemented on y planes");
+    for (int a = 0; a < 3; ++a)
+        if (!std::isfinite(p->body_force[a])) return fail(c, BIB_EINVAL, "body force must be finite");
+    for (int f = 0; f < 4; ++f)
+        for (int a = 0; a < 3; ++a)
+            if (!std::isfinite(p->wall_u[f][a])) return fail(c, BIB_EINVAL, "wall velocities must be finite");
+    if (!(std::isfinite(p->trt_magic) && p->trt_magic >= 0)) return fail(c, BIB_EINVAL, "TRT magic parameter must be >= 0");
+    if (!(std::isfinite(p->f16_scale) && p->f16_scale >= 0 && p->f16_scale <= 65504.0))
+        return fail(c, BIB_EINVAL, "FP16 scale must lie in [0, 65504]");
     if (!p->periodic[1] && !p->periodic[2] && p->wall_y == BIB_WALL_FD_VELOCITY)
         return fail(c, BIB_EUNSUPPORTED, "finite-difference y walls need a periodic z axis");
     auto L = std::make_unique<Lattice>();
@@ -1661,15 +1698,20 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
     const size_t sizes[6] = {pb, pb, fb, fb, ub, wb};
     for (int k = 0; k < 6; ++k) {
         if (!sizes[k]) continue;
-        cudaError_t e = cudaMalloc(bufs[k], sizes[k]);
+        cudaError_t e = dev_malloc(c, bufs[k], sizes[k]);
         if (e != cudaSuccess) {
+            cudaGetLastError();
             for (int j = 0; j < k; ++j) cudaFree(*bufs[j]);
             return fail(c, BIB_ENOMEM, "lattice buffer of %zu bytes: %s", sizes[k], cudaGetErrorString(e));
         }
         cudaMemsetAsync(*bufs[k], 0, sizes[k], c->stream);
     }
     if (d.use_phase) {
-        if (cudaMalloc((void**)&L->phase, d.stride) != cudaSuccess) return fail(c, BIB_ENOMEM, "phase field");
+        if (dev_malloc(c, (void**)&L->phase, d.stride) != cudaSuccess) {
+            cudaGetLastError();
+            for (int j = 0; j < 6; ++j) cudaFree(*bufs[j]);
+            return fail(c, BIB_ENOMEM, "phase field of %zu bytes", (size_t)d.stride);
+        }
         cudaMemsetAsync(L->phase, 0, d.stride, c->stream);
     }
     L->target_clean = false;
@@ -1976,6 +2018,11 @@ bib_status bib_particle_add(bib_ctx* c, int32_t h, int32_t shape, int32_t model,
     if (model == BIB_MODEL_RBC_WLCPOW || model == BIB_MODEL_SKALAK_BENDING) {
         if (!(params[BIB_P_VOL_DESIRED] != 0)) return fail(c, BIB_EINVAL, "vol_desired must be non-zero");
     }
+    for (int k = 0; k < BIB_P_COUNT; ++k)
+        if (!std::isfinite(params[k])) return fail(c, BIB_EINVAL, "membrane parameter %d is not finite", k);
+    if (xyz)
+        for (int k = 0; k < 3 * nv; ++k)
+            if (!std::isfinite(xyz[k])) return fail(c, BIB_EINVAL, "vertex coordinate %d is not finite", k);
     bib_status pst = pull_particles(c, *L);
     if (pst) return pst;
     ParticleHost ph;
@@ -2493,7 +2540,7 @@ bib_status bib_checkpoint_load(bib_ctx* c, int32_t h, const char* path) {
         if (!F.get(types.data(), types.size())) return fail(c, BIB_EINVAL, "checkpoint file is truncated");
         for (uint8_t t : types)
             if (t > BIB_CELL_NO_DYNAMICS) return fail(c, BIB_EINVAL, "corrupt checkpoint: cell type %d", (int)t);
-        if (!L->celltype) BIB_CUDA(c, cudaMalloc((void**)&L->celltype, (size_t)L->d.n));
+        if (!L->celltype) BIB_ALLOC(c, (void**)&L->celltype, (size_t)L->d.n);
         BIB_CUDA(c, cudaMemcpy(L->celltype, types.data(), types.size(), cudaMemcpyHostToDevice));
         L->d.has_types = 1;
     } else if (L->celltype) {
@@ -2993,7 +3040,7 @@ bib_status bib_rbc_shrink_volume(bib_ctx* c, int32_t shape, const double* params
     ph.prm.assign(params, params + BIB_P_COUNT);
     L.parts.push_back(ph);
     long long* iter = nullptr;
-    BIB_CUDA(c, cudaMalloc((void**)&iter, sizeof(long long)));
+    BIB_ALLOC(c, (void**)&iter, sizeof(long long));
     bib_status st = BIB_OK;
     cudaStream_t s = c->stream;
     for (int attempt = 0;; ++attempt) {

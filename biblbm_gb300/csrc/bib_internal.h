@@ -238,6 +238,7 @@ struct Lattice {
     bool sparse_ok[2] = {false, false};
     bool sparse_reset = false;  // tuning: the sparse reset where the lattice allows it
     uint64_t wait_ns = kDefaultWaitNs;  // bound of the staged kernel's hand-off waits
+    int64_t withhold_tile = -1;         // failure testing: a staged tile whose copies are not issued
     void* u = nullptr;                // velocity field, (ux, uy, uz, 0) per cell (double for F64 storage, float otherwise)
     uint8_t* phase = nullptr;
     uint8_t* celltype = nullptr;      // BIB_CELL_* per cell, or nullptr: every cell has the lattice's dynamics

@@ -140,7 +140,9 @@ typedef struct {
     int32_t wait_limit_us;  /* staged kernel: bound of each hand-off wait between its warps, in microseconds
                              * (0 = 2 s).  A wait that runs out makes the launch give up and bib_check_health
                              * return BIB_ETIMEOUT; the wait for the kernel's own copies in flight keeps 2 s */
-    int32_t reserved[2];
+    int32_t withhold_tile;  /* failure testing: 1 + the index of a tile of the staged kernel whose copies its
+                             * producer does not issue, so that the consumers' wait for them runs out (0 = none) */
+    int32_t reserved[1];
 } bib_tuning;
 /* DENSE (AUTO's choice): the collide-and-stream reads the previous force field for the velocity and
  * resets it to the body force, 24 bytes per cell streamed.  SPARSE (reduced-precision lattices

@@ -30,7 +30,27 @@ def small_channel():
     return workloads.channel_suspension(nx=96, ny=40, nz=40, n_cells=16, level=2, hct=0.12, seed=5)
 
 
-def run(ctx, wl, storage, reset, steps, spread="atomic", dirac="roma", graphs=True):
+def spreading_target(path):
+    """The force field the next coupled step spreads into, F[1 - fe], read from a checkpoint of
+    the library (header: magic, version, header size, lattice ints incl. fe at byte 72 and the
+    fd-wall flag at 44, the population stride at 88; then f[cur], the wall buffer when there are
+    finite-difference walls, F[0], F[1]; FP32 force fields for reduced-precision storage)."""
+    import struct
+
+    raw = open(path, "rb").read()
+    (hb,) = struct.unpack_from("<I", raw, 12)
+    nx, ny, nz, storage = struct.unpack_from("<4i", raw, 16)
+    (fd,) = struct.unpack_from("<i", raw, 44)
+    (fe,) = struct.unpack_from("<i", raw, 72)
+    (stride,) = struct.unpack_from("<q", raw, 88)
+    pb = {0: 8, 1: 4, 2: 2}[storage]
+    off = hb + 19 * stride * pb + (19 * 2 * nx * nz * pb if fd else 0)
+    fields = [np.frombuffer(raw, dtype="<f4", count=3 * stride, offset=off + k * 3 * stride * 4).reshape(3, stride)
+              for k in range(2)]
+    return fields[1 - fe][:, : nx * ny * nz]
+
+
+def run(ctx, wl, storage, reset, steps, spread="atomic", dirac="roma", graphs=True, target_check=False):
     nx, ny, nz = wl["dims"]
     lat = ctx.add_domain(nx, ny, nz, storage=storage, **wl["lattice"])
     if wl.get("initial_velocity") is not None:
@@ -47,13 +67,22 @@ def run(ctx, wl, storage, reset, steps, spread="atomic", dirac="roma", graphs=Tr
     lat.check_health()
     pos, stats = fsi.download()
     out = dict(f=lat.receive(), F=lat.get_external_force(), pos=pos, u=lat.compute_velocity())
+    if target_check:
+        import tempfile
+
+        with tempfile.TemporaryDirectory() as d:
+            path = d + "/state.bib"
+            lat.save_checkpoint(path)
+            out["target"] = spreading_target(path)
     del fsi, lat
     return out
 
 
-def compare(a, b, tol_f, tol_pos, rel_F=1e-6):
+def compare(a, b, tol_f, tol_pos, rel_F=1e-3):
     """Populations and positions to absolute bounds; the force field to rel_F of its largest
-    value (a node the sparse reset missed would hold a whole spread force, ~1e-2 .. 1 of it)."""
+    value (a node the sparse reset missed would hold a whole spread force, ~1e-2 .. 1 of it; the
+    rounding differences of the two velocities, amplified through the strained membranes, reach
+    ~4e-5 of it after 30 steps)."""
     assert np.isfinite(a["f"]).all() and np.isfinite(b["f"]).all()
     df = np.abs(a["f"] - b["f"]).max()
     dpos = np.abs(a["pos"] - b["pos"]).max()
@@ -68,7 +97,11 @@ def compare(a, b, tol_f, tol_pos, rel_F=1e-6):
 def test_channel_sparse_equals_dense(ctx, storage, graphs):
     wl = small_channel()
     dense = run(ctx, wl, storage, "dense", 25, graphs=graphs)
-    sparse = run(ctx, wl, storage, "sparse", 25, graphs=graphs)
+    sparse = run(ctx, wl, storage, "sparse", 25, graphs=graphs, target_check=True)
+    # the sparse reset restored the body force at every node the last spreading wrote: the
+    # next spreading target holds exactly the body force everywhere
+    body = np.asarray(wl["lattice"]["body_force"], dtype=np.float32)
+    assert np.array_equal(sparse["target"], np.broadcast_to(body[:, None], sparse["target"].shape))
     # the two resets differ in the last FP32 bits of the interpolated velocity (measured after 25
     # steps: FP32 populations < 1e-8, positions < 1e-7, force field 1e-7 relative; FP16, where a
     # last-bit change of f-bar * 8192 is ~4e-6, positions 5.6e-6)
