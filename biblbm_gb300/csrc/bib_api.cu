@@ -38,6 +38,7 @@ struct bib_ctx {
     cudaEvent_t ev[6] = {};
     cudaEvent_t dl_ev[8] = {};  // completion of the asynchronous downloads, one per slot
     int* d_flag = nullptr;
+    void* spread_scratch = nullptr;  // device address of the no-allocation spreading's static array
     std::map<std::pair<int, int>, GraphEntry> graphs;  // (lattice, steps and parity) -> step graph
     // population transfers with pageable host buffers: two device staging halves filled and
     // drained on a copy stream while the import / export kernels work on the other half
@@ -1239,6 +1240,12 @@ bib_status bib_create(const bib_config* cfg, bib_ctx** out) {
         delete c;
         return BIB_ECUDA;
     }
+    // set-up of bib_spread_forces_noalloc: the static scratch array's address on this device
+    std::string msg;
+    if (spread_scratch_address(&c->spread_scratch, msg) != BIB_OK) {
+        bib_destroy(c);
+        return BIB_ECUDA;
+    }
     *out = c;
     return BIB_OK;
 }
@@ -1449,7 +1456,7 @@ bib_status bib_spread_forces_noalloc(bib_ctx* c, int32_t h, const double* pos, c
     Lattice* L = get_lattice(c, h);
     if (!L) return fail(c, BIB_EINVAL, "invalid lattice handle");
     std::string msg;
-    const bib_status st = spread_noalloc(*L, c->device, c->stream, pos, force, nvert, field, msg);
+    const bib_status st = spread_noalloc(*L, c->device, c->spread_scratch, c->stream, pos, force, nvert, field, msg);
     if (st != BIB_OK) return fail(c, st, "%s", msg.c_str());
     return BIB_OK;
 }

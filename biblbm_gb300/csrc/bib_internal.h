@@ -378,7 +378,9 @@ void launch_fd_walls_batch(const BatchLaunch& B, cudaStream_t s);
 bool staged_collide_view(const Lattice& L, int tile_cells, CollideView& v);
 
 // ---- spreading without device allocation (noalloc.cu) ----
-bib_status spread_noalloc(const Lattice& L, int device, cudaStream_t s, const double* pos, const double* force,
+// device address of the scratch array on the current device (called by bib_create)
+bib_status spread_scratch_address(void** out, std::string& msg);
+bib_status spread_noalloc(const Lattice& L, int device, void* scratch, cudaStream_t s, const double* pos, const double* force,
                           int64_t nvert, void* field, std::string& msg);
 
 // ---- the reference's particle file formats (reference_files.cu) ----

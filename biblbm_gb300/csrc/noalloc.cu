@@ -15,7 +15,13 @@
 // each), then the sort's temporary storage.  Nothing in it has to start at zero: every
 // call writes the keys and ids it sorts, and the sort initialises its own temporaries.
 // All calls share the one array, so calls that overlap in time on one device race on it.
-#include <mutex>
+//
+// The host needs the array's device address to pass it to the kernels: the array's name in
+// host code is a host-side stand-in, not a device address.  bib_create resolves it with
+// cudaGetSymbolAddress while the context's device is current (the set-up step) and keeps it in
+// the context; a context created after a cudaDeviceReset therefore holds the address in the
+// new device context, and the entry point itself makes no runtime query that a stream capture
+// would have to record.
 #include <string>
 
 #include "bib_internal.h"
@@ -29,32 +35,20 @@ static_assert(BIB_SPREAD_NOALLOC_SCRATCH_BYTES > 4 * sizeof(uint32_t) * BIB_SPRE
 
 static __device__ __align__(256) unsigned char g_spread_scratch[BIB_SPREAD_NOALLOC_SCRATCH_BYTES];
 
-namespace {
-
-constexpr int kMaxDevices = 64;
-std::mutex g_scratch_mu;
-void* g_scratch_addr[kMaxDevices] = {};
-
-// Device address of the scratch array on `device` (which is current), resolved once per
-// device: the first call on a device is this set-up step.
-bib_status scratch_address(int device, void** out, std::string& msg) {
-    std::lock_guard<std::mutex> lock(g_scratch_mu);
-    if (device < 0 || device >= kMaxDevices) {
-        msg = "device ordinal out of range";
-        return BIB_EINVAL;
+// Device address of the scratch array on the current device (the set-up step, run by bib_create).
+bib_status spread_scratch_address(void** out, std::string& msg) {
+    void* p = nullptr;
+    const cudaError_t e = cudaGetSymbolAddress(&p, g_spread_scratch);
+    if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        msg = std::string("cudaGetSymbolAddress of the spreading scratch failed: ") + cudaGetErrorString(e);
+        return BIB_ECUDA;
     }
-    if (!g_scratch_addr[device]) {
-        void* p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_spread_scratch);
-        if (e != cudaSuccess || !p) {
-            msg = std::string("cudaGetSymbolAddress of the spreading scratch failed: ") + cudaGetErrorString(e);
-            return BIB_ECUDA;
-        }
-        g_scratch_addr[device] = p;
-    }
-    *out = g_scratch_addr[device];
+    *out = p;
     return BIB_OK;
 }
+
+namespace {
 
 struct DeviceGuard {
     int prev = -1;
@@ -69,8 +63,8 @@ struct DeviceGuard {
 
 }  // namespace
 
-bib_status spread_noalloc(const Lattice& L, int device, cudaStream_t s, const double* pos, const double* force,
-                          int64_t nvert, void* field, std::string& msg) {
+bib_status spread_noalloc(const Lattice& L, int device, void* scratch, cudaStream_t s, const double* pos,
+                          const double* force, int64_t nvert, void* field, std::string& msg) {
     if (nvert < 0) {
         msg = "negative vertex count";
         return BIB_EINVAL;
@@ -103,11 +97,12 @@ bib_status spread_noalloc(const Lattice& L, int device, cudaStream_t s, const do
               std::to_string(kNoallocSortTemp);
         return BIB_EUNSUPPORTED;
     }
+    if (!scratch) {
+        msg = "the context holds no address of the spreading scratch";
+        return BIB_ECUDA;
+    }
     DeviceGuard guard(device);
-    void* base = nullptr;
-    const bib_status st = scratch_address(device, &base, msg);
-    if (st != BIB_OK) return st;
-    uint32_t* words = static_cast<uint32_t*>(base);
+    uint32_t* words = static_cast<uint32_t*>(scratch);
     uint32_t* keys0 = words;
     uint32_t* keys1 = words + kNoallocEntries;
     uint32_t* ids0 = words + 2 * kNoallocEntries;

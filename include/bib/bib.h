@@ -416,10 +416,12 @@ bib_status bib_batch_autotune(bib_ctx* ctx, int32_t batch, int32_t steps, bib_ba
  * BIB_STORAGE_F64 lattice and float otherwise.  The sort scratch is one static device array of the library
  * (BIB_SPREAD_NOALLOC_SCRATCH_BYTES); nvert x support^3 (support 3 for Roma, 4 for Peskin) above
  * BIB_SPREAD_NOALLOC_MAX_ENTRIES is rejected with BIB_EINVAL before any work is queued.
- * The first call on a device resolves the array's device address (a set-up step): make it before any
- * stream capture.  Every call uses the same array, so calls that overlap in time on one device (from two
- * contexts, two threads, or streams not ordered with each other) race on it.  The work is queued on the
- * context's stream; the call returns without synchronising. */
+ * bib_create resolves the array's device address on the context's device (the set-up step), so the
+ * entry point makes no runtime query of its own; after a cudaDeviceReset, which invalidates every
+ * context, create a new context (it resolves the address anew).  Every call uses the same array, so calls
+ * that overlap in time on one device (from two contexts, two threads, or streams not ordered with each
+ * other) race on it.  The work is queued on the context's stream; the call returns without
+ * synchronising. */
 #define BIB_SPREAD_NOALLOC_MAX_ENTRIES (1 << 20)
 #define BIB_SPREAD_NOALLOC_SCRATCH_BYTES (17u << 20)
 bib_status bib_spread_forces_noalloc(bib_ctx* ctx, int32_t h, const double* pos, const double* force, int64_t nvert,

@@ -5,6 +5,8 @@ bib_ibm_step performs with the lattice's own buffers.
 Both run the same key, sort and per-cell reduce kernels in the same order on the same
 inputs, so the fields agree to 1e-15 of the largest force component; two calls in a row
 must give identical fields (the shared scratch carries nothing from one call to the next).
+The fields are also checked against the CPU oracle's spreading (the reference's
+spread_forces_impl, ImmersedBoundaryDynamics_forces.hh:22-163, restated).
 This file is collected last and also passes on its own in a fresh process.
 """
 import numpy as np
@@ -15,6 +17,7 @@ pytestmark = pytest.mark.gpu
 bib = pytest.importorskip("biblbm_gb300")
 torch = pytest.importorskip("torch")
 from biblbm_gb300 import meshes, workloads  # noqa: E402
+from oracle import oracle as O  # noqa: E402
 
 MAX_ENTRIES = 1 << 20  # BIB_SPREAD_NOALLOC_MAX_ENTRIES
 
@@ -51,8 +54,9 @@ def noalloc_spread(ctx, lat, pos_d, force_d, nvert, field_d):
     ctx.sync()
 
 
-@pytest.mark.parametrize("storage,dirac", [("f64", "roma"), ("f64", "peskin"), ("f32", "roma")])
+@pytest.mark.parametrize("storage,dirac", [("f64", "roma"), ("f64", "peskin"), ("f32", "roma"), ("f16", "roma")])
 def test_noalloc_spreading_matches_ibm_step(ctx, storage, dirac):
+    """FP16-storage lattices spread into a float field, as FP32 ones do."""
     lat, pos, forces, body, F_ref = capsule_after_ibm_step(ctx, storage, dirac)
     assert np.abs(forces).max() > 0 and np.abs(F_ref - body[:, None, None, None]).max() > 0
     dev = torch.device("cuda", 0)
@@ -70,6 +74,13 @@ def test_noalloc_spreading_matches_ibm_step(ctx, storage, dirac):
         assert np.abs(out - F_ref).max() <= tol
         outs.append(out)
     assert np.array_equal(outs[0], outs[1])
+    # and against the CPU oracle's spreading of the same forces onto the body force (FP64
+    # weights and sums; the FP32 field of reduced-precision lattices rounds each of them)
+    n = lat.shape[0]
+    L = O.lattice((n, n, n), (1, 1, 1))
+    F_orc = O.spread(L, dirac, pos, forces, offset=-1.0, F=np.broadcast_to(body[:, None, None, None], (3, n, n, n)))
+    rel = np.abs(outs[0] - F_orc).max() / np.abs(F_orc - body[:, None, None, None]).max()
+    assert rel < (1e-13 if storage == "f64" else 1e-5), rel
 
 
 def test_noalloc_spreading_rejects_too_many_entries(ctx):
