@@ -1709,7 +1709,8 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
         if (e != cudaSuccess) {
             cudaGetLastError();
             for (int j = 0; j < k; ++j) cudaFree(*bufs[j]);
-            return fail(c, BIB_ENOMEM, "lattice buffer of %zu bytes: %s", sizes[k], cudaGetErrorString(e));
+            return fail(c, BIB_ENOMEM, "device allocation of %zu bytes for a lattice buffer failed: %s", sizes[k],
+                        cudaGetErrorString(e));
         }
         cudaMemsetAsync(*bufs[k], 0, sizes[k], c->stream);
     }
@@ -1717,7 +1718,7 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
         if (dev_malloc(c, (void**)&L->phase, d.stride) != cudaSuccess) {
             cudaGetLastError();
             for (int j = 0; j < 6; ++j) cudaFree(*bufs[j]);
-            return fail(c, BIB_ENOMEM, "phase field of %zu bytes", (size_t)d.stride);
+            return fail(c, BIB_ENOMEM, "device allocation of %zu bytes for the phase field failed", (size_t)d.stride);
         }
         cudaMemsetAsync(L->phase, 0, d.stride, c->stream);
     }

@@ -163,8 +163,7 @@ template <class T, int CPL, int COLL>
 struct StageLayout {
     using FT = typename Store<T>::F;
     static constexpr int TILE = TileOf<T>::value;
-    static constexpr int CPT = sizeof(T) == 2 ? 2 : 1;  // cells per consumer thread and tile
-    static constexpr int CONSUMERS = TILE / (32 * CPT);  // consumer warps
+    static constexpr int CONSUMERS = TILE / 32;  // consumer warps: one cell per thread and tile
     static constexpr int THREADS = 32 * (CONSUMERS + 1);
     static constexpr bool NEED_FCOL = COLL == BIB_COLLISION_BGK_GUO_VOF;
     static constexpr unsigned POP = TILE * sizeof(T);
@@ -285,21 +284,20 @@ __device__ __forceinline__ void load_tile(const LatticeDesc& d, const StagedGeom
     __syncwarp();
 }
 
-// Consumer side of one tile: the thread's cells of every tile, `cpt` (1 or 2) consecutive cells
-// of one row from o0 on, the left x-neighbour of the first and the right x-neighbour of the last
-// (periodic in x within the row).
+// Consumer side of one tile: the thread's cell of every tile and its x-neighbours (periodic in
+// x within the row).
 struct TileCell {
     bool active;
     int r, o0, ol, orr;
 };
-__device__ __forceinline__ TileCell tile_cell(const LatticeDesc& d, int Ct, int ct, int cpt) {
+__device__ __forceinline__ TileCell tile_cell(const LatticeDesc& d, int Ct, int ct) {
     TileCell c;
-    c.o0 = ct * cpt;
-    c.active = c.o0 < Ct;
-    c.r = c.o0 / d.nx;
-    const int x = c.o0 - c.r * d.nx, xl = x + cpt - 1;
+    c.active = ct < Ct;
+    c.r = ct / d.nx;
+    const int x = ct - c.r * d.nx;
+    c.o0 = ct;
     c.ol = c.r * d.nx + (x == 0 ? d.nx - 1 : x - 1);
-    c.orr = c.r * d.nx + (xl == d.nx - 1 ? 0 : xl + 1);
+    c.orr = c.r * d.nx + (x == d.nx - 1 ? 0 : x + 1);
     return c;
 }
 
@@ -356,18 +354,6 @@ __device__ __forceinline__ void finish_cell(const LatticeDesc& d, const CollideP
         Staged<T>::put(o, f[i]);
         o += d.stride;
     }
-}
-
-// finish_cell out of line, for the rare pairs of the two-cell consumer that hold a
-// BounceBack / NoDynamics cell (inlined, its registers would count against every pair).
-template <class T, int CPL, int COLL>
-__device__ __noinline__ void finish_cell_call(const LatticeDesc& d, const CollideParams<typename Store<T>::C>& cp,
-                                              T* __restrict__ fout, typename Store<T>::F* __restrict__ Fprev,
-                                              typename Store<T>::F* __restrict__ u_out, const uint8_t* __restrict__ phase,
-                                              const uint8_t* __restrict__ celltype, int64_t k, int y, bool fd,
-                                              typename Store<T>::C* f, const typename Store<T>::C* F,
-                                              const typename Store<T>::C* Fp) {
-    finish_cell<T, CPL, COLL>(d, cp, fout, Fprev, u_out, phase, celltype, k, y, fd, f, F, Fp);
 }
 
 // One cell per consumer thread: read the thread's cell from the stage, release the stage,
@@ -427,136 +413,14 @@ __device__ __forceinline__ void consume_cell(const LatticeDesc& d, const StagedG
     finish_cell<T, CPL, COLL>(d, cp, fout, Fprev, u_out, phase, celltype, t.row0 + o0, y, fd, f, F, Fp);
 }
 
-// Two neighbouring cells of one x-row per consumer thread (FP16 storage): the populations with
-// c_x = 0 come out of the stage as one half2 per pair, the collision of both cells runs in packed
-// FP32x2 instructions, and every population is stored as one half2.  Rows next to walls take the
-// per-population face tests of the one-cell path; a pair holding a BounceBack / NoDynamics cell
-// is finished cell by cell.
-template <class T, int CPL, int COLL>
-__device__ __forceinline__ void consume_pair(const LatticeDesc& d, const StagedGeom& g, int64_t tile, const unsigned char* st,
-                                             const CollideParams<float>& cp, T* __restrict__ fout, float* __restrict__ Fprev,
-                                             float* __restrict__ u_out, const uint8_t* __restrict__ phase,
-                                             const uint8_t* __restrict__ celltype, const TileCell& cell, uint64_t* empty_s,
-                                             int lane) {
-    using L = StageLayout<T, CPL, COLL>;
-    constexpr int TILE = L::TILE;
-    const int o0 = cell.o0, ol = cell.ol, orr = cell.orr;
-    const T* P = reinterpret_cast<const T*>(st);
-    const float* SFc = reinterpret_cast<const float*>(st + L::OFF_FCOL);
-    const float* SFp = reinterpret_cast<const float*>(st + L::OFF_FPREV);
-    const TileRef t = tile_ref(d, g, tile);
-    const int y = t.y0 + cell.r;
-    const bool fd = fd_wall_node(d, y);
-    float a[Q], b[Q];
-    float2 F[3] = {bc2(0.0f), bc2(0.0f), bc2(0.0f)}, Fp[3] = {bc2(0.0f), bc2(0.0f), bc2(0.0f)};
-    if (cell.active) {
-        if (!row_special(d, y, t.z)) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                const T* row = P + i * TILE;
-                if (cx(i) == 0) {
-                    Staged<T>::two(row + o0, a[i], b[i]);
-                } else if (cx(i) == 1) {  // from x - 1
-                    a[i] = Staged<T>::one(row + ol);
-                    b[i] = Staged<T>::one(row + o0);
-                } else {  // from x + 1
-                    a[i] = Staged<T>::one(row + o0 + 1);
-                    b[i] = Staged<T>::one(row + orr);
-                }
-            }
-        } else {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) {
-                int face = -1;
-                if (!fd) {
-                    int64_t srow;
-                    face = source_row(d, i, y, t.z, srow);
-                }
-                const T* row = P + i * TILE;
-                if (fd || face >= 0 || cx(i) == 0) {  // no x shift
-                    a[i] = Staged<T>::one(row + o0);
-                    b[i] = Staged<T>::one(row + o0 + 1);
-                } else if (cx(i) == 1) {
-                    a[i] = Staged<T>::one(row + ol);
-                    b[i] = Staged<T>::one(row + o0);
-                } else {
-                    a[i] = Staged<T>::one(row + o0 + 1);
-                    b[i] = Staged<T>::one(row + orr);
-                }
-                if (face >= 0) {
-                    a[i] += cp.mw[face][i];
-                    b[i] += cp.mw[face][i];
-                }
-            }
-        }
-        if (L::NEED_FCOL) {
-#pragma unroll
-            for (int q = 0; q < 3; ++q) F[q] = *reinterpret_cast<const float2*>(SFc + q * TILE + o0);
-        }
-        if (CPL == kCplDense) {
-#pragma unroll
-            for (int q = 0; q < 3; ++q) Fp[q] = *reinterpret_cast<const float2*>(SFp + q * TILE + o0);
-        } else if (CPL == kCplSparse) {
-#pragma unroll
-            for (int q = 0; q < 3; ++q) Fp[q] = bc2(cp.body[q]);
-        }
-    }
-    // the stage has been read into registers: hand it back to the producer
-    __syncwarp();
-    if (lane == 0) mbar_arrive(empty_s);
-    if (!cell.active) return;
-    const int64_t k = t.row0 + o0;
-    if (d.has_types && (celltype[k] != BIB_CELL_FLUID || celltype[k + 1] != BIB_CELL_FLUID)) {
-        const float Fa[3] = {F[0].x, F[1].x, F[2].x}, Fb[3] = {F[0].y, F[1].y, F[2].y};
-        const float Fpa[3] = {Fp[0].x, Fp[1].x, Fp[2].x}, Fpb[3] = {Fp[0].y, Fp[1].y, Fp[2].y};
-        finish_cell_call<T, CPL, COLL>(d, cp, fout, Fprev, u_out, phase, celltype, k, y, fd, a, Fa, Fpa);
-        finish_cell_call<T, CPL, COLL>(d, cp, fout, Fprev, u_out, phase, celltype, k + 1, y, fd, b, Fb, Fpb);
-        return;
-    }
-    float2 f[Q];
-#pragma unroll
-    for (int i = 0; i < Q; ++i) f[i] = make_float2(a[i], b[i]);
-    float2 om = bc2(cp.om0);
-    if (COLL == BIB_COLLISION_BGK_GUO_VOF && d.use_phase) {
-        if (phase[k]) om.x = cp.om1;
-        if (phase[k + 1]) om.y = cp.om1;
-    }
-    if (CPL != kCplNone) {
-        float2 u[3];
-        collide_compact2<COLL>(f, F, om, cp.omm, cp.S, cp.invS, Fp, fd ? nullptr : u);
-        if (fd) {
-            const int side = y == 0 ? 0 : 1;
-#pragma unroll
-            for (int q = 0; q < 3; ++q) u[q] = bc2(cp.wall_u[side][q]);
-        }
-        store_u<float>(u_out, k, u[0].x, u[1].x, u[2].x);
-        store_u<float>(u_out, k + 1, u[0].y, u[1].y, u[2].y);
-        if (CPL == kCplDense) {
-#pragma unroll
-            for (int q = 0; q < 3; ++q) store2<float>(Fprev + q * d.stride + k, cp.body[q], cp.body[q]);
-        }
-    } else {
-        collide_compact2<COLL>(f, F, om, cp.omm, cp.S, cp.invS, nullptr, nullptr);
-    }
-    T* o = fout + k;
-#pragma unroll
-    for (int i = 0; i < Q; ++i) {
-        Staged<T>::store(o, f[i].x, f[i].y);
-        o += d.stride;
-    }
-}
-
-// The consumer of one tile: one or two cells per thread (StageLayout::CPT).
+// The consumer of one tile.
 template <class T, int CPL, int COLL>
 __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, const unsigned char* st,
                                              const CollideParams<typename Store<T>::C>& cp, T* __restrict__ fout,
                                              typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
                                              const uint8_t* __restrict__ phase, const uint8_t* __restrict__ celltype,
                                              const TileCell& cell, uint64_t* empty_s, int lane) {
-    if constexpr (StageLayout<T, CPL, COLL>::CPT == 2)
-        consume_pair<T, CPL, COLL>(d, g, tile, st, cp, fout, Fprev, u_out, phase, celltype, cell, empty_s, lane);
-    else
-        consume_cell<T, CPL, COLL>(d, g, tile, st, cp, fout, Fprev, u_out, phase, celltype, cell, empty_s, lane);
+    consume_cell<T, CPL, COLL>(d, g, tile, st, cp, fout, Fprev, u_out, phase, celltype, cell, empty_s, lane);
 }
 
 // Warp-specialised persistent kernel: warp 0 produces, warps 1..CONSUMERS collide.  Stage
@@ -629,7 +493,7 @@ __global__ void __launch_bounds__(StageLayout<T, CPL, COLL>::THREADS, staged_cta
     }
 
     // ---- consumers: thread `ct` owns cell ct of every tile
-    const TileCell cell = tile_cell(d, g.Ct, tid - 32, L::CPT);
+    const TileCell cell = tile_cell(d, g.Ct, tid - 32);
     int it = 0;
     for (int64_t tile = blockIdx.x; tile < g.ntiles; tile += gridDim.x, ++it) {
         const int s = it % NS;
@@ -764,7 +628,7 @@ __global__ void __launch_bounds__(StageLayout<T, kCplDense, COLL>::THREADS, stag
             asm volatile("bar.sync 1, %0;" ::"r"(L::CONSUMERS * 32) : "memory");
             copy_view(cview, views + vi, tid - 32, L::CONSUMERS * 32);
             asm volatile("bar.sync 1, %0;" ::"r"(L::CONSUMERS * 32) : "memory");
-            cell = tile_cell(cview->d, cview->Ct, tid - 32, L::CPT);  // depends on the lattice's row length
+            cell = tile_cell(cview->d, cview->Ct, tid - 32);  // depends on the lattice's row length
             cur_view = vi;
         }
         const CollideView& V = *cview;

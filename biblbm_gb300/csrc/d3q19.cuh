@@ -272,108 +272,6 @@ __device__ __forceinline__ void collide_compact(float* f, const float* F, float 
     }
 }
 
-// ---------------------------------------------------------------- two cells per thread
-// The compact collision of two cells at once in Blackwell's packed FP32 instructions (FFMA2,
-// FADD2, FMUL2: one instruction for both lanes, each lane rounded as its scalar operation).
-// Lane x is the first cell, lane y the second.
-__device__ __forceinline__ float2 bc2(float s) { return make_float2(s, s); }
-__device__ __forceinline__ float2 add2(float2 a, float2 b) { return __fadd2_rn(a, b); }
-__device__ __forceinline__ float2 sub2(float2 a, float2 b) { return __ffma2_rn(b, bc2(-1.0f), a); }
-__device__ __forceinline__ float2 mul2(float2 a, float2 b) { return __fmul2_rn(a, b); }
-__device__ __forceinline__ float2 fma2(float2 a, float2 b, float2 c) { return __ffma2_rn(a, b, c); }
-
-// c_{i+9} . (a, b, c) for i in 1..9: c_{i+9} = -c_i has no component pair of two minus signs,
-// so every case is one packed addition, subtraction or a copy.
-__device__ __forceinline__ float2 cdot2(int i, float2 a, float2 b, float2 c) {
-    const int j = i + 9;
-    if (cx(j) != 0) {
-        if (cy(j) != 0) return cy(j) > 0 ? add2(a, b) : sub2(a, b);
-        if (cz(j) != 0) return cz(j) > 0 ? add2(a, c) : sub2(a, c);
-        return a;
-    }
-    if (cy(j) != 0) return cz(j) != 0 ? (cz(j) > 0 ? add2(b, c) : sub2(b, c)) : b;
-    return c;
-}
-
-// The operator of collide_compact for two cells.  omega may differ per lane (phase field);
-// with u_prev non-null the velocities j/rho + Fprev/2 of the incoming states are returned.
-template <int COLL>
-__device__ __forceinline__ void collide_compact2(float2* f, const float2* F, float2 omega, float omm, float S,
-                                                 float invS, const float2* Fprev, float2* u_prev) {
-    const float2 sxm = add2(add2(add2(f[1], f[4]), add2(f[5], f[6])), f[7]);
-    const float2 sxp = add2(add2(add2(f[10], f[13]), add2(f[14], f[15])), f[16]);
-    const float2 sym = add2(add2(add2(f[2], f[4]), add2(f[8], f[9])), f[14]);
-    const float2 syp = add2(add2(add2(f[5], f[11]), add2(f[13], f[17])), f[18]);
-    const float2 szm = add2(add2(add2(f[3], f[6]), add2(f[8], f[16])), f[18]);
-    const float2 szp = add2(add2(add2(f[7], f[9]), add2(f[12], f[15])), f[17]);
-    const float2 sx0 = add2(add2(add2(add2(f[0], f[2]), add2(f[3], f[8])), add2(add2(f[9], f[11]), add2(f[12], f[17]))),
-                            f[18]);
-    const float2 iS = bc2(invS);
-    const float2 rb = mul2(add2(add2(sxm, sx0), sxp), iS);
-    const float2 j0 = mul2(sub2(sxp, sxm), iS), j1 = mul2(sub2(syp, sym), iS), j2 = mul2(sub2(szp, szm), iS);
-    const float2 invRho = make_float2(1.0f / (rb.x + 1.0f), 1.0f / (rb.y + 1.0f));
-    const float2 half = bc2(0.5f);
-    if (u_prev) {
-        u_prev[0] = fma2(j0, invRho, mul2(half, Fprev[0]));
-        u_prev[1] = fma2(j1, invRho, mul2(half, Fprev[1]));
-        u_prev[2] = fma2(j2, invRho, mul2(half, Fprev[2]));
-    }
-    const float2 tw0 = bc2(S * weight<float>(0)), tw1 = bc2(S * weight<float>(1)), tw4 = bc2(S * weight<float>(4));
-    if (COLL == BIB_COLLISION_TRT) {
-        // symmetric part relaxes with omega, antisymmetric with omm (scalar forms in collide_compact)
-        const float2 base = sub2(rb, mul2(mul2(bc2(1.5f), invRho),
-                                          fma2(j0, j0, fma2(j1, j1, mul2(j2, j2)))));
-        const float2 h = mul2(bc2(4.5f), invRho);
-        f[0] = fma2(mul2(omega, bc2(-1.0f)), sub2(f[0], mul2(tw0, base)), f[0]);
-        const float2 om_ = bc2(omm);
-#pragma unroll
-        for (int i = 1; i < 10; ++i) {
-            const float2 cj = cdot2(i, j0, j1, j2);  // c_{i+9} . j = -(c_i . j)
-            const float2 tw = i <= 3 ? tw1 : tw4;
-            const float2 ep = mul2(tw, fma2(mul2(h, cj), cj, base));
-            const float2 em = mul2(mul2(tw, bc2(3.0f)), cj);  // feq-(i+9); feq-(i) = -em
-            const float2 dp = mul2(omega, sub2(mul2(half, add2(f[i], f[i + 9])), ep));
-            const float2 dm = mul2(om_, add2(mul2(half, sub2(f[i], f[i + 9])), em));
-            f[i] = sub2(sub2(f[i], dp), dm);
-            f[i + 9] = add2(sub2(f[i + 9], dp), dm);
-        }
-        return;
-    }
-    const bool forced = COLL == BIB_COLLISION_BGK_GUO_VOF;
-    const float2 zero = bc2(0.0f);
-    const float2 F0 = forced ? F[0] : zero, F1 = forced ? F[1] : zero, F2 = forced ? F[2] : zero;
-    const float2 u0 = fma2(j0, invRho, mul2(half, F0)), u1 = fma2(j1, invRho, mul2(half, F1)),
-                 u2 = fma2(j2, invRho, mul2(half, F2));
-    const float2 rho = add2(rb, bc2(1.0f));
-    const float2 mu = fma2(bc2(-0.5f), omega, bc2(1.0f));
-    const float2 wr = mul2(omega, rho);
-    const float2 uu = fma2(u0, u0, fma2(u1, u1, mul2(u2, u2)));
-    const float2 uF = fma2(u0, F0, fma2(u1, F1, mul2(u2, F2)));
-    const float2 A = sub2(sub2(mul2(omega, rb), mul2(mul2(bc2(1.5f), wr), uu)), mul2(mul2(bc2(3.0f), mu), uF));
-    const float2 h3 = mul2(bc2(3.0f), wr), m3 = mul2(bc2(3.0f), mu), g45 = mul2(bc2(4.5f), wr), m9 = mul2(bc2(9.0f), mu);
-    const float2 H0 = fma2(h3, u0, mul2(m3, F0)), H1 = fma2(h3, u1, mul2(m3, F1)), H2 = fma2(h3, u2, mul2(m3, F2));
-    const float2 G0 = fma2(g45, u0, mul2(m9, F0)), G1 = fma2(g45, u1, mul2(m9, F1)), G2 = fma2(g45, u2, mul2(m9, F2));
-    const float2 omo = sub2(bc2(1.0f), omega);
-    f[0] = fma2(omo, f[0], mul2(tw0, A));
-    // the weight of each class folded into A, G and H, one class at a time (fewer live registers)
-#pragma unroll
-    for (int cls = 0; cls < 2; ++cls) {
-        const float2 tw = cls == 0 ? tw1 : tw4;
-        const float2 At = mul2(tw, A);
-        const float2 Gt0 = mul2(tw, G0), Gt1 = mul2(tw, G1), Gt2 = mul2(tw, G2);
-        const float2 Ht0 = mul2(tw, H0), Ht1 = mul2(tw, H1), Ht2 = mul2(tw, H2);
-#pragma unroll
-        for (int i = cls == 0 ? 1 : 4; i < (cls == 0 ? 4 : 10); ++i) {
-            const float2 cu = cdot2(i, u0, u1, u2);     // c_{i+9} . u
-            const float2 cG = cdot2(i, Gt0, Gt1, Gt2);  // t_i (c_{i+9} . G)
-            const float2 Mn = cdot2(i, Ht0, Ht1, Ht2);  // t_i (c_{i+9} . H)
-            const float2 P = fma2(cu, cG, At);
-            f[i] = fma2(omo, f[i], sub2(P, Mn));
-            f[i + 9] = fma2(omo, f[i + 9], add2(P, Mn));
-        }
-    }
-}
-
 __host__ __device__ inline int64_t wrap_index(int64_t i, int64_t n) { return i < 0 ? i + n : (i >= n ? i - n : i); }
 
 }  // namespace bib

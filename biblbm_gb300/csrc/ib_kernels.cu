@@ -593,7 +593,10 @@ __device__ __forceinline__ void wall_force(const Interactions& I, const double* 
             const double rr = sqrt(dy * dy + dz * dz);
             const double dist = I.wall_r[w] - rr;
             if (dist <= I.wall[w].r0) {
+                // the normal (0, dy, dz) / |.| of get_normal: on the axis (rr = 0) every component,
+                // the x one included, is 0/0, as in the reference
                 const double phi = potential_eval(I.wall[w], dist);
+                f[0] -= phi * (0.0 / rr);
                 f[1] -= phi * (dy / rr);
                 f[2] -= phi * (dz / rr);
             }

@@ -268,7 +268,9 @@ bib_status bib_particles_download(bib_ctx* ctx, int32_t h, double* pos, double* 
  * re-building it: the area, volume and centre follow as after a step's move (the centre mapped
  * to the periodic grid, the vertices with it), and a phase field is re-voxelized.  Asynchronous
  * on the context's stream; the host buffer is read before the call returns only when the
- * particles have not been uploaded yet. */
+ * particles have not been uploaded yet.  Otherwise the copy reads it later: keep the buffer
+ * unchanged and allocated until bib_sync (or any call that waits for the stream: receive,
+ * downloads, bib_check_health) has returned. */
 bib_status bib_particles_upload(bib_ctx* ctx, int32_t h, const double* pos);
 /* bib_particles_download without waiting: the copies are queued on the context's stream behind the
  * work issued so far, and slot (0..7) marks their completion.  The host buffers must stay valid (and
