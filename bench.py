@@ -636,6 +636,34 @@ def main():
                        "bib_particles_download_async of the per-cell area/volume/centre, waited for one step "
                        "later), final download of all "
                        "vertex positions and bib_lattice_receive of the populations; pinned host buffers"}
+        # The loop of the reference's own channel driver (rbcs_in_channel.cpp: initializeAtEquilibrium
+        # from a velocity field, then steps; it writes velocity fields and particle data, not
+        # populations): bib_lattice_init_equilibrium from the host velocity field, K x (bib_step +
+        # cell statistics), final vertex positions and bib_lattice_get_velocity.
+        u0 = pinned((3, nz, ny, nx))
+        u0[...] = 0.0 if wl.get("initial_velocity") is None else wl["initial_velocity"]
+        u_out = pinned((3, nz, ny, nx))
+        barrier()
+        t0 = time.perf_counter()
+        c3.check(lib.bib_lattice_init_equilibrium(h, l3.h, None, dpd(u0)))
+        c3.check(lib.bib_particles_upload(h, l3.h, dpd(pos_host)))
+        for k in range(K):
+            c3.check(lib.bib_step(h, l3.h, 1))
+            c3.check(lib.bib_particles_download_async(h, l3.h, None, dpd(stats_buf[k % 2]), k % 2))
+            if k:
+                c3.check(lib.bib_download_wait(h, (k - 1) % 2))
+        c3.check(lib.bib_download_wait(h, (K - 1) % 2))
+        c3.check(lib.bib_particles_download(h, l3.h, dpd(pos_out), None))
+        c3.check(lib.bib_lattice_get_velocity(h, l3.h, dpd(u_out)))
+        dt2 = max_over_ranks(time.perf_counter() - t0)
+        barrier()
+        e2e["driver_loop"] = {
+            "value": cells * K * world / dt2 / 1e6, "unit": "MLUPS", "seconds": dt2,
+            "h2d_bytes_per_step": int((u0.nbytes + pos_host.nbytes) // K),
+            "d2h_bytes_per_step": int((K * stats_out.nbytes + pos_out.nbytes + u_out.nbytes) // K),
+            "what": "bib_lattice_init_equilibrium from the FP64 host velocity field + bib_particles_upload, K x (bib_step "
+                    "+ per-cell area/volume/centre), final vertex positions and bib_lattice_get_velocity (FP64 velocity "
+                    "field); pinned host buffers"}
         c3.close()
 
     # ---------------- CPU baseline (the oracle port) on a bounded sample

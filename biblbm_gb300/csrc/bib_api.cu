@@ -1780,6 +1780,16 @@ bib_status bib_lattice_init_equilibrium(bib_ctx* c, int32_t h, const double* rho
     Lattice* L = get_lattice(c, h);
     if (!L || !u) return fail(c, BIB_EINVAL, "invalid lattice handle or velocity");
     const int64_t n = L->d.n;
+    // page-locked host arrays are read by the kernel directly; others are copied in first
+    const double* mu = static_cast<const double*>(device_view_of_host(u, 3 * n * sizeof(double)));
+    const double* mr = rho ? static_cast<const double*>(device_view_of_host(rho, n * sizeof(double))) : nullptr;
+    if (mu && (!rho || mr)) {
+        launch_init_equilibrium(*L, mr, mu, c->stream);
+        launch_fd_walls(*L, L->cur, L->fe, c->stream);
+        BIB_CHECK_LAUNCH(c);
+        BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+        return BIB_OK;
+    }
     double *dr = nullptr, *du = nullptr;
     bib_status st = device_buffer(c, &du, u, 3 * n);
     if (st) return st;
@@ -1853,6 +1863,12 @@ bib_status bib_lattice_set_phase(bib_ctx* c, int32_t h, const double* phase) {
 bib_status bib_lattice_get_velocity(bib_ctx* c, int32_t h, double* u) {
     Lattice* L = get_lattice(c, h);
     if (!L || !u) return fail(c, BIB_EINVAL, "invalid lattice handle or velocity");
+    if (double* m = static_cast<double*>(const_cast<void*>(device_view_of_host(u, 3 * L->d.n * sizeof(double))))) {
+        launch_velocity_export(*L, m, c->stream);  // page-locked: written by the kernel directly
+        BIB_CHECK_LAUNCH(c);
+        BIB_CUDA(c, cudaStreamSynchronize(c->stream));
+        return BIB_OK;
+    }
     double* d = nullptr;
     bib_status st = device_buffer(c, &d, nullptr, 3 * L->d.n);
     if (st) return st;

@@ -6,6 +6,8 @@ pageable buffers go through the double-buffered staging pipeline.  Both must giv
 lattice state and the same bytes back, in every wire layout, on lattices large enough for several
 staging chunks, with finite-difference wall rows (their own buffer) and halfway bounce-back faces.
 """
+import ctypes
+
 import numpy as np
 import pytest
 
@@ -15,6 +17,7 @@ bib = pytest.importorskip("biblbm_gb300")
 torch = pytest.importorskip("torch")
 
 LAYOUT = {"soa": 0, "palabos": 1, "coprocessor": 2}
+_dp = ctypes.POINTER(ctypes.c_double)
 PER = {"soa": 19, "palabos": 23, "coprocessor": 19}
 
 
@@ -104,3 +107,25 @@ def test_pinned_round_trip_is_exact_where_storage_is(ctx, storage):
     out = pinned_like(np.zeros_like(f))
     ctx.check(ctx.lib.bib_lattice_receive(ctx.h, lat.h, out.ctypes.data, out.nbytes, 0))
     assert np.array_equal(out, f)
+
+
+@pytest.mark.parametrize("storage", ["f64", "f16"])
+def test_equilibrium_and_velocity_through_pinned_buffers(ctx, storage):
+    """bib_lattice_init_equilibrium and bib_lattice_get_velocity read / write page-locked host
+    arrays directly; the result must equal the staged path's for pageable arrays."""
+    nx, ny, nz = 48, 20, 12
+    rng = np.random.default_rng(5)
+    u = rng.uniform(-0.02, 0.02, (3, nz, ny, nx))
+    rho = 1.0 + rng.uniform(-0.01, 0.01, (nz, ny, nx))
+    outs = []
+    for kind in ("pageable", "pinned"):
+        lat = ctx.add_domain(nx, ny, nz, storage=storage, **WALLS["fd"])
+        uu, rr = (u.copy(), rho.copy()) if kind == "pageable" else (pinned_like(u), pinned_like(rho))
+        ctx.check(ctx.lib.bib_lattice_init_equilibrium(ctx.h, lat.h, rr.ctypes.data_as(_dp), uu.ctypes.data_as(_dp)))
+        lat.collide_and_stream(2)
+        vel = np.zeros_like(u) if kind == "pageable" else pinned_like(np.zeros_like(u))
+        ctx.check(ctx.lib.bib_lattice_get_velocity(ctx.h, lat.h, vel.ctypes.data_as(_dp)))
+        outs.append((lat.receive(), np.array(vel)))
+        del lat
+    assert np.array_equal(outs[0][0], outs[1][0]) and np.array_equal(outs[0][1], outs[1][1])
+    assert np.abs(outs[1][1]).max() > 1e-3
