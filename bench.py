@@ -426,8 +426,9 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", default="native", choices=["native", "reference"])
     ap.add_argument("--storage", default="f16", choices=["f16", "f32", "f64"])
-    ap.add_argument("--workload", default="channel", choices=["channel", "capsule", "rbc", "batch", "tgv"],
-                    help="channel: 400 RBCs in 512x128x128 (the headline); capsule: one capsule in shear, 64^3; "
+    ap.add_argument("--workload", default="channel", choices=["channel", "channel_small", "capsule", "rbc", "batch", "tgv"],
+                    help="channel: 400 RBCs in 512x128x128 (the headline); channel_small: the same density and rows, "
+                         "200 RBCs in 512x128x64 (profiling captures); capsule: one capsule in shear, 64^3; "
                          "rbc: one RBC in shear, 128x64x64; batch: 64 capsule instances stepped as one batch; "
                          "tgv: TRT Taylor-Green bandwidth sweep, 128^3 / 256^3 / 384^3")
     ap.add_argument("--cpu-steps", type=int, default=2)
@@ -445,7 +446,9 @@ def main():
 
     if args.workload in ("batch", "tgv") and args.impl == "native":
         return run_batch(args) if args.workload == "batch" else run_tgv(args)
-    wl = {"channel": workloads.channel_suspension, "capsule": workloads.capsule_shear, "rbc": workloads.rbc_shear,
+    wl = {"channel": workloads.channel_suspension,
+          "channel_small": lambda: workloads.channel_suspension(nx=512, ny=128, nz=64, n_cells=200),
+          "capsule": workloads.capsule_shear, "rbc": workloads.rbc_shear,
           "batch": lambda: workloads.batched_capsules()["instances"][0],
           "tgv": workloads.capsule_shear}[args.workload]()
     if args.impl == "reference":
