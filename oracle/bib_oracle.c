@@ -1104,23 +1104,74 @@ static void pp_pair(const orc_lattice* L, const orc_potential* p, double c2, con
     }
 }
 
+/* The domain of a collision grid: the integer bounding box of the lattice (x0..x1 per axis) and
+ * its periodic axes (Periodicity3D's arithmetic on that box). */
+typedef struct {
+    int64_t lo[3], N[3];
+    int32_t per[3];
+} grid_box;
+
+/* Arithmetic1D::min_mod_diff (Periodicity.h:27-35, 96-99) on periodic axes, x - y otherwise */
+static double box_diff(const grid_box* B, int a, double x, double y) {
+    const double d = x - y;
+    if (!B->per[a]) return d;
+    const double Ld = (double)B->N[a], Linv = 1.0 / Ld;
+    return d - floor(d * Linv + 0.5) * Ld;
+}
+
+/* CollisionHandler::handle_collision (CollisionForces.h:187-199) on a grid box */
+static void box_pair(const grid_box* B, const orc_potential* p, double c2, const double* xa, const double* xb,
+                     double* fa, double* fb) {
+    const double dr[3] = {box_diff(B, 0, xb[0], xa[0]), box_diff(B, 1, xb[1], xa[1]), box_diff(B, 2, xb[2], xa[2])};
+    const double dsq = dr[0] * dr[0] + dr[1] * dr[1] + dr[2] * dr[2];
+    if (dsq <= c2) {
+        const double dist = sqrt(dsq);
+        const double s = -orc_potential_eval(p, dist) / dist;
+        for (int d = 0; d < 3; ++d) {
+            const double df = s * dr[d];
+            fa[d] += df;
+            fb[d] -= df;
+        }
+    }
+}
+
+/* geo::clamp (fsi/geometry.h:20-27) */
+static double gclamp(double v, double lo, double hi) { return v >= hi ? hi : (v <= lo ? lo : v); }
+
+/* PipeBoundary::contains(pos, margin) (Boundary.h:148-151) on the (y, z) of a point */
+static int pipe_contains(const double* w, double y, double z, double margin) {
+    const double dy = y - w[0], dz = z - w[1], r = w[2] - margin;
+    return dy * dy + dz * dz < r * r;
+}
+
+/* PipeBoundary::does_intersect(rect, width) (Boundary.h:227-243) for a rect's y and z ranges */
+static int pipe_does_intersect(const double* w, double ry0, double ry1, double rz0, double rz1, double width) {
+    const double cy = w[0] - gclamp(w[0], ry0, ry1), cz = w[1] - gclamp(w[1], rz0, rz1);
+    const double tmp = cy * cy + cz * cz;
+    if (!(tmp <= w[2] * w[2])) return 0;
+    return !(pipe_contains(w, ry0, rz0, width) && pipe_contains(w, ry0, rz1, width) &&
+             pipe_contains(w, ry1, rz0, width) && pipe_contains(w, ry1, rz1, width));
+}
+
 /* Particle-particle forces as the reference evaluates them
  * (compute_particle_particle_interaction_impl, ImmersedBoundaryDynamics_forces.hh:330-375, with
  * CollisionHandler::compute_collision_forces, CollisionForces.h:63-164, and Grid, Grid.hh):
- * nodes inside the lattice box enlarged by 1/2 + cutoff go into a grid of ~unit cells over the
- * box in particle / vertex order; every bulk cell pairs its nodes among themselves and with the
- * nodes of 7 neighbour cells (+y, +y+z, +z, +x, +x+y, +x+y+z, +x+z), then the first and last
- * bulk layers of each periodic axis are paired.  Pairs whose cells sit at other offsets (e.g.
- * +x-y) are not examined: orc_pp_forces below takes every pair within the cutoff. */
-void orc_pp_forces_grid(const orc_lattice* L, const orc_potential* p, int64_t nv, const double* pos,
-                        const int32_t* owner, double* force) {
-    const int64_t N[3] = {L->nx, L->ny, L->nz};
+ * nodes inside the box enlarged by 1/2 + cutoff go into a grid of ~unit cells over the box in
+ * particle / vertex order; every bulk cell pairs its nodes among themselves and with the nodes
+ * of 7 neighbour cells (+y, +y+z, +z, +x, +x+y, +x+y+z, +x+z), then the first and last bulk
+ * layers of each periodic axis are paired.  Pairs whose cells sit at other offsets (e.g. +x-y)
+ * are not examined.  With a pipe wall w = {y0, z0, radius} the wall pass follows
+ * (CollisionHandler::compute_wall_collision_forces, CollisionForces.h:166-184): every node of a
+ * bulk cell the wall intersects (within the cutoff) at distance dist <= cutoff from the wall gets
+ * force -= phi(dist) * n, n the outward normal (Boundary.h:158-161, 245-249). */
+static void grid_forces(const grid_box* B, const orc_potential* p, int64_t nv, const double* pos,
+                        const int32_t* owner, double* force, const double* wall) {
     const double cut = p->r0, c2 = cut * cut;
     double b0[3], b1[3], cs[3], g0[3];
     int64_t nc[3];
     for (int a = 0; a < 3; ++a) {
-        b0[a] = 0 - 0.5;
-        b1[a] = (double)(N[a] - 1) + 0.5 - DBL_EPSILON;
+        b0[a] = (double)B->lo[a] - 0.5;
+        b1[a] = (double)(B->lo[a] + B->N[a] - 1) + 0.5 - DBL_EPSILON;
         nc[a] = (int64_t)floor((b1[a] - b0[a]) / 1.0);
         cs[a] = (b1[a] - b0[a]) / (double)nc[a];
         nc[a] += 2;
@@ -1150,7 +1201,7 @@ void orc_pp_forces_grid(const orc_lattice* L, const orc_potential* p, int64_t nv
 #define PAIR(u, v)                                                                                     \
     do {                                                                                               \
         const int64_t a_ = (u), b_ = (v);                                                              \
-        if (owner[a_] != owner[b_]) pp_pair(L, p, c2, pos + 3 * a_, pos + 3 * b_, force + 3 * a_, force + 3 * b_); \
+        if (owner[a_] != owner[b_]) box_pair(B, p, c2, pos + 3 * a_, pos + 3 * b_, force + 3 * a_, force + 3 * b_); \
     } while (0)
     for (int64_t i = 1; i <= nc[0] - 2; ++i)
         for (int64_t j = 1; j <= nc[1] - 2; ++j)
@@ -1166,28 +1217,49 @@ void orc_pp_forces_grid(const orc_lattice* L, const orc_potential* p, int64_t nv
             }
     /* collide_all_in_cells of the first and last bulk layers of periodic axes (CollisionForces.h:119-163) */
     const int64_t x0 = 1, x1 = nc[0] - 2, y0 = 1, y1 = nc[1] - 2, z0 = 1, z1 = nc[2] - 2;
+    const int32_t* per = B->per;
 #define ALL(ca, cb)                                                                 \
     do {                                                                            \
         const int64_t p_ = (ca), q_ = (cb);                                         \
         for (int64_t l = count[p_]; l < count[p_ + 1]; ++l)                         \
             for (int64_t m = count[q_]; m < count[q_ + 1]; ++m) PAIR(node[l], node[m]); \
     } while (0)
-    if (L->periodic[0])
+    if (per[0])
         for (int64_t j = y0; j <= y1; ++j)
             for (int64_t k = z0; k <= z1; ++k) ALL(CELL(x0, j, k), CELL(x1, j, k));
-    if (L->periodic[1])
+    if (per[1])
         for (int64_t i = x0; i <= x1; ++i)
             for (int64_t k = z0; k <= z1; ++k) ALL(CELL(i, y0, k), CELL(i, y1, k));
-    if (L->periodic[2])
+    if (per[2])
         for (int64_t i = x0; i <= x1; ++i)
             for (int64_t j = y0; j <= y1; ++j) ALL(CELL(i, j, z0), CELL(i, j, z1));
-    if (L->periodic[0] && L->periodic[1])
+    if (per[0] && per[1])
         for (int64_t k = z0; k <= z1; ++k) ALL(CELL(x0, y0, k), CELL(x1, y1, k));
-    if (L->periodic[0] && L->periodic[2])
+    if (per[0] && per[2])
         for (int64_t j = y0; j <= y1; ++j) ALL(CELL(x0, j, z0), CELL(x1, j, z1));
-    if (L->periodic[1] && L->periodic[2])
+    if (per[1] && per[2])
         for (int64_t i = x0; i <= x1; ++i) ALL(CELL(i, y0, z0), CELL(i, y1, z1));
-    if (L->periodic[0] && L->periodic[1] && L->periodic[2]) ALL(CELL(x0, y0, z0), CELL(x1, y1, z1));
+    if (per[0] && per[1] && per[2]) ALL(CELL(x0, y0, z0), CELL(x1, y1, z1));
+    if (wall)
+        for (int64_t i = x0; i <= x1; ++i)
+            for (int64_t j = y0; j <= y1; ++j)
+                for (int64_t k = z0; k <= z1; ++k) {
+                    /* the cell's rect: Grid::repartition, Grid.hh:46-58 */
+                    const double ry0 = b0[1] + (double)(j - 1) * cs[1], rz0 = b0[2] + (double)(k - 1) * cs[2];
+                    if (!pipe_does_intersect(wall, ry0, ry0 + cs[1], rz0, rz0 + cs[2], cut)) continue;
+                    const int64_t c = CELL(i, j, k);
+                    for (int64_t l = count[c]; l < count[c + 1]; ++l) {
+                        const double* x = pos + 3 * node[l];
+                        double* f = force + 3 * node[l];
+                        const double dy = x[1] - wall[0], dz = x[2] - wall[1];
+                        const double dist = wall[2] - sqrt(dy * dy + dz * dz);
+                        if (!(dist <= cut)) continue;
+                        const double nn = sqrt(0.0 * 0.0 + dy * dy + dz * dz);
+                        const double n[3] = {0.0 / nn, dy / nn, dz / nn};
+                        const double phi = orc_potential_eval(p, dist);
+                        for (int d = 0; d < 3; ++d) f[d] -= phi * n[d];
+                    }
+                }
 #undef ALL
 #undef PAIR
 #undef CELL
@@ -1195,6 +1267,12 @@ void orc_pp_forces_grid(const orc_lattice* L, const orc_potential* p, int64_t nv
     free(cell_of);
     free(fill);
     free(node);
+}
+
+void orc_pp_forces_grid(const orc_lattice* L, const orc_potential* p, int64_t nv, const double* pos,
+                        const int32_t* owner, double* force) {
+    const grid_box B = {{0, 0, 0}, {L->nx, L->ny, L->nz}, {L->periodic[0], L->periodic[1], L->periodic[2]}};
+    grid_forces(&B, p, nv, pos, owner, force, NULL);
 }
 
 /* Every pair of vertices of different particles within the cutoff (minimum image on periodic
@@ -1214,6 +1292,239 @@ void orc_pp_forces(const orc_lattice* L, const orc_potential* p, int64_t nv, con
     }
     for (int64_t i = 0; i < 3 * nv; ++i) force[i] += acc[i];
     free(acc);
+}
+
+/* ------------------------------------------------------------------ growth of the initial distribution */
+/* ParticleShape::compute_properties' moment of inertia about the origin (ParticleShape.hh:254-356)
+ * and the shape volume, the sum of tri::signed_volume (ParticleShape.hh:21-57, TriangleUtils.h:106-110) */
+static void shape_mass_props(int64_t nt, const int64_t* tri, const double* v, double* volume, double* I) {
+    double in[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    double vol = 0.0;
+    for (int64_t t = 0; t < nt; ++t) {
+        const double* v0 = v + 3 * tri[3 * t];
+        const double* v1 = v + 3 * tri[3 * t + 1];
+        const double* v2 = v + 3 * tri[3 * t + 2];
+        const v3 c12 = crs(ld(v1), ld(v2));
+        vol += (v0[0] * c12.v[0] + v0[1] * c12.v[1] + v0[2] * c12.v[2]) / 6.;
+        const v3 N = crs(sub(ld(v1), ld(v0)), sub(ld(v2), ld(v0)));
+        double f1[3], f2[3], f3[3], g0[3], g1[3], g2[3];
+        for (int d = 0; d < 3; ++d) {
+            const double tmp0 = v0[d] + v1[d];
+            f1[d] = tmp0 + v2[d];
+            const double tmp1 = v0[d] * v0[d];
+            const double tmp2 = tmp1 + v1[d] * tmp0;
+            f2[d] = tmp2 + v2[d] * f1[d];
+            f3[d] = v0[d] * tmp1 + v1[d] * tmp2 + v2[d] * f2[d];
+            g0[d] = f2[d] + v0[d] * (f1[d] + v0[d]);
+            g1[d] = f2[d] + v1[d] * (f1[d] + v1[d]);
+            g2[d] = f2[d] + v2[d] * (f1[d] + v2[d]);
+        }
+        in[0] += N.v[0] * f1[0];
+        in[1] += N.v[0] * f2[0];
+        in[2] += N.v[1] * f2[1];
+        in[3] += N.v[2] * f2[2];
+        in[4] += N.v[0] * f3[0];
+        in[5] += N.v[1] * f3[1];
+        in[6] += N.v[2] * f3[2];
+        in[7] += N.v[0] * (v0[1] * g0[0] + v1[1] * g1[0] + v2[1] * g2[0]);
+        in[8] += N.v[1] * (v0[2] * g0[1] + v1[2] * g1[1] + v2[2] * g2[1]);
+        in[9] += N.v[2] * (v0[0] * g0[2] + v1[0] * g1[2] + v2[0] * g2[2]);
+    }
+    const double oneDiv60 = (double)(1.0 / 60.0), oneDiv120 = (double)(1.0 / 120.0);
+    for (int k = 4; k <= 6; ++k) in[k] *= oneDiv60;
+    for (int k = 7; k <= 9; ++k) in[k] *= oneDiv120;
+    I[0] = in[5] + in[6];
+    I[1] = -in[7];
+    I[2] = -in[9];
+    I[3] = I[1];
+    I[4] = in[4] + in[6];
+    I[5] = -in[8];
+    I[6] = I[2];
+    I[7] = I[5];
+    I[8] = in[4] + in[5];
+    *volume = vol;
+}
+
+void orc_shape_mass_props(int64_t nt, const int64_t* tri, const double* xyz, double* volume, double* inertia9) {
+    shape_mass_props(nt, tri, xyz, volume, inertia9);
+}
+
+/* Quaternion::apply_rotation / apply_inv_rotation (fsi/Quaternion.h:102-146) */
+static void q_rotate(const double* q, const double* v, double* r) {
+    r[0] = (1 - 2 * (q[2] * q[2] + q[3] * q[3])) * v[0] + 2 * (q[1] * q[2] - q[0] * q[3]) * v[1] +
+           2 * (q[0] * q[2] + q[1] * q[3]) * v[2];
+    r[1] = 2 * (q[1] * q[2] + q[0] * q[3]) * v[0] + (1 - 2 * (q[1] * q[1] + q[3] * q[3])) * v[1] +
+           2 * (q[2] * q[3] - q[0] * q[1]) * v[2];
+    r[2] = 2 * (q[1] * q[3] - q[0] * q[2]) * v[0] + 2 * (q[0] * q[1] + q[2] * q[3]) * v[1] +
+           (1 - 2 * (q[1] * q[1] + q[2] * q[2])) * v[2];
+}
+static void q_rotate_inv(const double* q, const double* v, double* r) {
+    r[0] = (1 - 2 * (q[2] * q[2] + q[3] * q[3])) * v[0] + 2 * (q[1] * q[2] + q[0] * q[3]) * v[1] +
+           2 * (q[1] * q[3] - q[0] * q[2]) * v[2];
+    r[1] = 2 * (q[1] * q[2] - q[0] * q[3]) * v[0] + (1 - 2 * (q[1] * q[1] + q[3] * q[3])) * v[1] +
+           2 * (q[0] * q[1] + q[2] * q[3]) * v[2];
+    r[2] = 2 * (q[0] * q[2] + q[1] * q[3]) * v[0] + 2 * (q[2] * q[3] - q[0] * q[1]) * v[1] +
+           (1 - 2 * (q[1] * q[1] + q[2] * q[2])) * v[2];
+}
+/* Quaternion::to_rot_matrix (Quaternion.h:148-159) */
+static void q_matrix(const double* q, double* R) {
+    R[0] = 1 - 2 * (q[2] * q[2] + q[3] * q[3]);
+    R[1] = 2 * (q[1] * q[2] - q[0] * q[3]);
+    R[2] = 2 * (q[0] * q[2] + q[1] * q[3]);
+    R[3] = 2 * (q[1] * q[2] + q[0] * q[3]);
+    R[4] = 1 - 2 * (q[1] * q[1] + q[3] * q[3]);
+    R[5] = 2 * (q[2] * q[3] - q[0] * q[1]);
+    R[6] = 2 * (q[1] * q[3] - q[0] * q[2]);
+    R[7] = 2 * (q[0] * q[1] + q[2] * q[3]);
+    R[8] = 1 - 2 * (q[1] * q[1] + q[2] * q[2]);
+}
+
+/* RigidParticle3D::update (RigidParticle.hh:27-36): vertex i at com + R (scale v_i) */
+static void rigid_nodes(const double* com, const double* q, double scale, int64_t nv, const double* v, double* pos) {
+    double R[9];
+    q_matrix(q, R);
+    for (int64_t i = 0; i < nv; ++i) {
+        const double w[3] = {scale * v[3 * i], scale * v[3 * i + 1], scale * v[3 * i + 2]};
+        for (int d = 0; d < 3; ++d) pos[3 * i + d] = com[d] + (R[3 * d] * w[0] + R[3 * d + 1] * w[1] + R[3 * d + 2] * w[2]);
+    }
+}
+
+/* The growth stage of create_particles (progs/common/create_particles.h:105-161): rigid copies of
+ * the shapes (RigidParticle3D, RigidParticle.hh) start at com / quat, every rescale_every
+ * iterations are rescaled to initial_scale + (1 - initial_scale) it / n_it, feel
+ * compute_collision_forces(SpringPotential(min_dist, strength), &wall) (the collision grid
+ * above, the pipe wall when has_wall) and move by RigidParticle3D::move_vertices
+ * (RigidParticle.hh:55-101) with the periodic remap of the centre of mass
+ * (ImmersedBoundaryDynamics.hh:486-493).  Runs iterations 0 .. it_end - 1 and returns the centres
+ * and orientations; pos_out / force_out (optional) receive the vertex positions after the last
+ * iteration and the vertex forces of its collision step.  Returns 0, or -1 on bad input. */
+int32_t orc_grow_particles(const orc_growth* g, int32_t nshape, const int64_t* nv, const double* verts,
+                           const int64_t* nt, const int64_t* tri, int32_t np, const int32_t* shape, double* com,
+                           double* quat, double* pos_out, double* force_out) {
+    if (nshape < 1 || np < 0 || g->n_it < 1 || g->rescale_every < 1) return -1;
+    int64_t* voff = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nshape + 1));
+    int64_t* toff = (int64_t*)malloc(sizeof(int64_t) * (size_t)(nshape + 1));
+    voff[0] = toff[0] = 0;
+    for (int32_t s = 0; s < nshape; ++s) {
+        voff[s + 1] = voff[s] + nv[s];
+        toff[s + 1] = toff[s] + nt[s];
+    }
+    double* vol = (double*)malloc(sizeof(double) * (size_t)nshape);
+    double* inertia = (double*)malloc(sizeof(double) * 9 * (size_t)nshape);
+    for (int32_t s = 0; s < nshape; ++s)
+        shape_mass_props(nt[s], tri + 3 * toff[s], verts + 3 * voff[s], &vol[s], inertia + 9 * s);
+    int64_t* poff = (int64_t*)malloc(sizeof(int64_t) * (size_t)(np + 1));
+    poff[0] = 0;
+    for (int32_t p = 0; p < np; ++p) poff[p + 1] = poff[p] + nv[shape[p]];
+    const int64_t ntot = poff[np];
+    double* pos = (double*)calloc((size_t)(3 * (ntot > 0 ? ntot : 1)), sizeof(double));
+    double* frc = (double*)calloc((size_t)(3 * (ntot > 0 ? ntot : 1)), sizeof(double));
+    int32_t* owner = (int32_t*)malloc(sizeof(int32_t) * (size_t)(ntot > 0 ? ntot : 1));
+    double* vel = (double*)calloc((size_t)(3 * (np > 0 ? np : 1)), sizeof(double));
+    double* om = (double*)calloc((size_t)(3 * (np > 0 ? np : 1)), sizeof(double));
+    for (int32_t p = 0; p < np; ++p)
+        for (int64_t i = poff[p]; i < poff[p + 1]; ++i) owner[i] = p;
+    grid_box B;
+    for (int a = 0; a < 3; ++a) {
+        B.lo[a] = g->box[2 * a];
+        B.N[a] = g->box[2 * a + 1] - g->box[2 * a] + 1;
+        B.per[a] = g->periodic[a];
+    }
+    const orc_potential pot = {ORC_POTENTIAL_SPRING, g->min_dist, 0.0, g->strength};
+    double scale = g->initial_scale;
+    for (int32_t p = 0; p < np; ++p)
+        rigid_nodes(com + 3 * p, quat + 4 * p, scale, nv[shape[p]], verts + 3 * voff[shape[p]], pos + 3 * poff[p]);
+    for (int64_t it = 0; it < g->it_end; ++it) {
+        if (it % g->rescale_every == 0) {
+            const double fraction = (double)it / (double)g->n_it;
+            scale = g->initial_scale + (1. - g->initial_scale) * fraction;
+            for (int32_t p = 0; p < np; ++p)
+                rigid_nodes(com + 3 * p, quat + 4 * p, scale, nv[shape[p]], verts + 3 * voff[shape[p]],
+                            pos + 3 * poff[p]);
+        }
+        memset(frc, 0, sizeof(double) * 3 * (size_t)ntot);
+        grid_forces(&B, &pot, ntot, pos, owner, frc, g->has_wall ? g->wall : NULL);
+        for (int32_t p = 0; p < np; ++p) {
+            const int32_t s = shape[p];
+            double* c = com + 3 * p;
+            double* q = quat + 4 * p;
+            double* v = vel + 3 * p;
+            double* w = om + 3 * p;
+            double F[3] = {0, 0, 0}, Tq[3] = {0, 0, 0};
+            for (int64_t i = poff[p]; i < poff[p + 1]; ++i) {
+                const double* x = pos + 3 * i;
+                const double* f = frc + 3 * i;
+                const double r[3] = {x[0] - c[0], x[1] - c[1], x[2] - c[2]};
+                const double cr[3] = {r[1] * f[2] - r[2] * f[1], r[2] * f[0] - r[0] * f[2], r[0] * f[1] - r[1] * f[0]};
+                for (int d = 0; d < 3; ++d) {
+                    F[d] += f[d];
+                    Tq[d] += cr[d];
+                }
+            }
+            double wb[3], Ib[9];
+            q_rotate_inv(q, w, wb);
+            /* std::pow(T, int) of the reference's C++98 build is __builtin_powi, which g++ expands
+             * into the multiplications x^2 = x x, x^3 = x x^2, x^5 = x^2 x^3 */
+            const double s2 = scale * scale, s3 = scale * s2, s5 = s2 * s3;
+            const double fac = g->density * s5;
+            for (int k = 0; k < 9; ++k) Ib[k] = fac * inertia[9 * s + k];
+            const double mass = (scale * scale * scale) * vol[s] * g->density;
+            double vdot[3];
+            for (int d = 0; d < 3; ++d) vdot[d] = F[d] / mass - g->damping * v[d];
+            const double Iw[3] = {Ib[0] * wb[0] + Ib[1] * wb[1] + Ib[2] * wb[2], Ib[3] * wb[0] + Ib[4] * wb[1] + Ib[5] * wb[2],
+                                  Ib[6] * wb[0] + Ib[7] * wb[1] + Ib[8] * wb[2]};
+            const double cw[3] = {wb[1] * Iw[2] - wb[2] * Iw[1], wb[2] * Iw[0] - wb[0] * Iw[2], wb[0] * Iw[1] - wb[1] * Iw[0]};
+            double tb[3], rhs[3], sol[3], rw[3];
+            q_rotate_inv(q, Tq, tb);
+            for (int d = 0; d < 3; ++d) rhs[d] = tb[d] - cw[d];
+            /* Matrix<T, 3>::solve (fsi/Matrix3.h:129-144), Cramer's rule */
+            const double* m = Ib;
+            const double det = m[0] * m[4] * m[8] - m[0] * m[5] * m[7] - m[1] * m[3] * m[8] + m[1] * m[5] * m[6] +
+                               m[2] * m[3] * m[7] - m[2] * m[4] * m[6];
+            sol[0] = (rhs[2] * (m[1] * m[5] - m[2] * m[4]) + rhs[1] * (m[2] * m[7] - m[1] * m[8]) +
+                      rhs[0] * (m[4] * m[8] - m[5] * m[7])) / det;
+            sol[1] = (rhs[2] * (m[2] * m[3] - m[0] * m[5]) + rhs[1] * (m[0] * m[8] - m[2] * m[6]) +
+                      rhs[0] * (m[5] * m[6] - m[3] * m[8])) / det;
+            sol[2] = (rhs[2] * (m[0] * m[4] - m[1] * m[3]) + rhs[1] * (m[1] * m[6] - m[0] * m[7]) +
+                      rhs[0] * (m[3] * m[7] - m[4] * m[6])) / det;
+            q_rotate(q, sol, rw);
+            for (int d = 0; d < 3; ++d) {
+                v[d] += vdot[d];
+                w[d] += rw[d] - g->damping * w[d];
+            }
+            for (int d = 0; d < 3; ++d) c[d] += v[d];
+            /* unit-norm exponential map (RigidParticle.hh:90-94) */
+            const double wn = sqrt(w[0] * w[0] + w[1] * w[1] + w[2] * w[2]);
+            if (wn >= (double)10 * DBL_EPSILON) {
+                const double ax[3] = {w[0] / wn, w[1] / wn, w[2] / wn};
+                const double sh = sin(wn / 2);
+                const double r[4] = {cos(wn / 2), sh * ax[0], sh * ax[1], sh * ax[2]};
+                const double qn[4] = {r[0] * q[0] - (r[1] * q[1] + r[2] * q[2] + r[3] * q[3]),
+                                      r[0] * q[1] + q[0] * r[1] + r[2] * q[3] - r[3] * q[2],
+                                      r[0] * q[2] + q[0] * r[2] + r[3] * q[1] - r[1] * q[3],
+                                      r[0] * q[3] + q[0] * r[3] + r[1] * q[2] - r[2] * q[1]};
+                memcpy(q, qn, sizeof(qn));
+            }
+            double* px = pos + 3 * poff[p];
+            rigid_nodes(c, q, scale, nv[s], verts + 3 * voff[s], px);
+            /* map_center_of_mass_to_periodic_grid (ParticleBase.hh:111-136) */
+            double np_[3] = {c[0], c[1], c[2]};
+            for (int d = 0; d < 3; ++d) {
+                if (!B.per[d]) continue;
+                const double x0 = (double)B.lo[d] - 0.5, Lf = (double)B.N[d], Linv = 1. / Lf;
+                np_[d] = np_[d] - Lf * floor((np_[d] - x0) * Linv);
+            }
+            const double delta[3] = {np_[0] - c[0], np_[1] - c[1], np_[2] - c[2]};
+            for (int64_t i = 0; i < nv[s]; ++i)
+                for (int d = 0; d < 3; ++d) px[3 * i + d] += delta[d];
+            for (int d = 0; d < 3; ++d) c[d] = np_[d];
+        }
+    }
+    if (pos_out) memcpy(pos_out, pos, sizeof(double) * 3 * (size_t)ntot);
+    if (force_out) memcpy(force_out, frc, sizeof(double) * 3 * (size_t)ntot);
+    free(voff); free(toff); free(vol); free(inertia); free(poff);
+    free(pos); free(frc); free(owner); free(vel); free(om);
+    return 0;
 }
 
 /* ------------------------------------------------------------------ immersed boundary */

@@ -130,6 +130,23 @@ void orc_pp_forces_grid(const orc_lattice* L, const orc_potential* p, int64_t nv
 void orc_pp_forces(const orc_lattice* L, const orc_potential* p, int64_t nv, const double* pos, const int32_t* owner,
                    double* force);
 
+/* growth of the initial distribution (progs/common/create_particles.h:105-161), see the .c */
+typedef struct {
+    int64_t box[6];            /* x0, x1, y0, y1, z0, z1: the lattice's bounding box */
+    int32_t periodic[3];
+    int32_t has_wall;
+    double wall[3];            /* PipeBoundary y0, z0, radius the collisions keep the vertices inside */
+    double min_dist, strength; /* SpringPotential(min_dist, strength), fsi/Potentials.h:58-71 */
+    double initial_scale, density, damping;
+    int64_t n_it;              /* the scale reaches 1 at iteration n_it */
+    int64_t rescale_every;
+    int64_t it_end;            /* iterations 0 .. it_end - 1 are run (n_it + 1: the whole growth) */
+} orc_growth;
+void orc_shape_mass_props(int64_t nt, const int64_t* tri, const double* xyz, double* volume, double* inertia9);
+int32_t orc_grow_particles(const orc_growth* g, int32_t nshape, const int64_t* nv, const double* verts,
+                           const int64_t* nt, const int64_t* tri, int32_t np, const int32_t* shape, double* com,
+                           double* quat, double* pos_out, double* force_out);
+
 typedef struct orc_sys orc_sys;
 orc_sys* orc_sys_create(const orc_lattice* L, int32_t dirac, double ib_offset);
 void orc_sys_destroy(orc_sys* s);

@@ -47,6 +47,12 @@
 //           in/ckpt.plb into a fresh lattice; dumps its populations, forces and phase
 //   coprocessor  D3Q19ExampleCoProcessor3D (coProcessors/coProcessor3D.hh:34-78): addDomain,
 //           send of given bytes, collideAndStream, receive
+//   create  the reference's own create_particles (progs/common/create_particles.h) for capsule
+//           templates of given shapes in a pipe along x: random placement at 20 % scale, growth of
+//           rigid copies over its 40000 iterations, deformable particles placed at the result
+//   grow    the growth loop of create_particles (:127-161) from given centres and orientations,
+//           with a given iteration count, dumping centres, orientations, vertex positions and
+//           vertex forces after chosen iterations
 //
 // Array conventions: lattice fields are (components, nz, ny, nx) with x fastest.
 #define FSI_PROFILE
@@ -73,6 +79,19 @@ using recio::shp;
 #define DESCRIPTOR descriptors::ForcedPhaseD3Q19Descriptor
 typedef double T;
 typedef MultiBlockLattice3D<T, DESCRIPTOR> Lattice;
+
+// The globals progs/common/create_particles.h reads, declared as its driver declares them
+// (progs/rbc_in_pipe_distribution/rbc_in_pipe.cpp:19, 31, 39, 47-52).
+typedef Periodicity3D<double, true, false, false> Periodicity;
+struct ParticleTmp {
+    ParticleBase3D<double>* particle;
+    std::string name;
+    double numParticles;
+};
+std::vector<ParticleTmp> particleTypes;
+PipeBoundary<double> pipe_boundary;
+bool load_checkpoint = false;
+#include "create_particles.h"
 
 static const int Q = 19;
 
@@ -1022,6 +1041,166 @@ static int run_coprocessor(const Bundle& in, const char* out) {
     return 0;
 }
 
+
+// create_particles on a lattice over `box` (x0, x1, y0, y1, z0, z1; periodic in x as the pipe
+// drivers), pipe = (y0, z0, radius, length), capsule templates of the shapes rest<t> / tri<t>
+// with counts[t] particles each, srand(seed).  Dumps the vertex positions of the particles it
+// adds, in id order.
+static Lattice* pipe_lattice(const std::vector<long long>& b) {
+    Lattice* lattice = generateMultiBlockLattice<T, DESCRIPTOR>(Box3D(b[0], b[1], b[2], b[3], b[4], b[5]),
+                                                               new GuoExternalForceVOFDynamics<T, DESCRIPTOR>(1.0, 1.0), 1)
+                           .release();
+    lattice->periodicity().toggle(0, Periodicity::get_x());
+    lattice->periodicity().toggle(1, Periodicity::get_y());
+    lattice->periodicity().toggle(2, Periodicity::get_z());
+    lattice->toggleInternalStatistics(false);
+    return lattice;
+}
+
+static void store_typed_shapes(const Bundle& in, ParticleShapeLibrary<T>& lib, long long ntypes) {
+    for (long long t = 0; t < ntypes; ++t) {
+        char xn[32], tn[32], tag[32];
+        std::sprintf(xn, "rest%lld", t);
+        std::sprintf(tn, "tri%lld", t);
+        std::sprintf(tag, "type%lld", t);
+        store_shape_as(in, lib, xn, tn, tag);
+    }
+}
+
+static int run_create(const Bundle& in, const char* out) {
+    const std::vector<long long> b = recio::need(in, "box").i;
+    const std::vector<double> pp = recio::need(in, "pipe").d;
+    const std::vector<long long> counts = recio::need(in, "counts").i;
+    Lattice* lattice = pipe_lattice(b);
+    pipe_boundary = PipeBoundary<T>(pp[0], pp[1], pp[2], pp[3]);
+    ParticleShapeLibrary<T> lib;
+    store_typed_shapes(in, lib, (long long)counts.size());
+    particleTypes.clear();
+    for (size_t t = 0; t < counts.size(); ++t) {
+        char tag[32];
+        std::sprintf(tag, "type%d", (int)t);
+        ParticleTmp pt;
+        pt.particle = new DeformableCapsuleParticle<T>(lib.get_by_tag(tag), CapsuleParameters<T>());
+        pt.name = std::string("rigid_") + tag;
+        pt.numParticles = (double)counts[t];
+        particleTypes.push_back(pt);
+    }
+    ImmersedBoundaryDynamics3D<T, DESCRIPTOR, Periodicity> fsi(*lattice, lib);
+    global::directories().setOutputDir("out/");
+    io::mkdir("out/");
+    std::srand((unsigned)recio::inum(in, "seed"));
+    create_particles<T>(fsi, *lattice);
+    std::vector<double> pos;
+    plint n = 0;
+    for (plint id = 0;; ++id) {
+        ParticleBase3D<T>* p = 0;
+        if (!fsi.get_particle(id, p)) break;
+        for (plint i = 0; i < p->count_nodes(); ++i)
+            for (int d = 0; d < 3; ++d) pos.push_back(p->get_node(i).pos[d]);
+        ++n;
+    }
+    recio::Writer w(out);
+    w.d("pos", shp((long long)(pos.size() / 3), 3), pos);
+    w.d("count", shp(1), std::vector<double>(1, (double)n));
+    for (size_t t = 0; t < particleTypes.size(); ++t) delete particleTypes[t].particle;
+    particleTypes.clear();
+    delete lattice;
+    return 0;
+}
+
+// The body of create_particles' growth loop (create_particles.h:127-161) on rigid copies of the
+// shapes rest<t> / tri<t>: particle k on shape[k] starts at com[k] / quat[k], the wall is
+// PipeBoundary(wall[0], wall[1], wall[2], box length), the potential SpringPotential(pot[0],
+// pot[1]); growth = (initial_scale, density, damping), n_it the iteration the scale reaches 1.
+// After the iterations listed in `dump` (counts of iterations run) the centres, orientations,
+// vertex positions and vertex forces are written with the count as suffix.
+static int run_grow(const Bundle& in, const char* out) {
+    const std::vector<long long> b = recio::need(in, "box").i;
+    const std::vector<double> wall = recio::need(in, "wall").d;
+    const std::vector<double> pot = recio::need(in, "pot").d;
+    const std::vector<double> gr = recio::need(in, "growth").d;
+    const std::vector<long long> shape = recio::need(in, "shape").i;
+    const std::vector<double> com = recio::need(in, "com").d;
+    const std::vector<double> quat = recio::need(in, "quat").d;
+    const std::vector<long long> dump = recio::need(in, "dump").i;
+    const plint Nit = (plint)recio::inum(in, "n_it");
+    const long long ntypes = recio::inum(in, "ntypes");
+    Lattice* lattice = pipe_lattice(b);
+    ParticleShapeLibrary<T> lib;
+    store_typed_shapes(in, lib, ntypes);
+    ImmersedBoundaryDynamics3D<T, DESCRIPTOR, Periodicity> fsi2(*lattice, lib);
+    PipeBoundary<T> boundary2(wall[0], wall[1], wall[2], (T)(b[1] - b[0]));
+    std::vector<RigidParticle3D<T>*> rigid;
+    for (long long t = 0; t < ntypes; ++t) {
+        char tag[32];
+        std::sprintf(tag, "type%lld", t);
+        RigidParticle3D<T>* r = new RigidParticle3D<T>(lib.get_by_tag(tag));
+        r->scale() = gr[0];
+        r->density() = gr[1];
+        r->damping() = gr[2];
+        r->update();
+        rigid.push_back(r);
+    }
+    for (size_t k = 0; k < shape.size(); ++k) {
+        RigidParticle3D<T>* p = rigid[shape[k]];
+        p->scale() = gr[0];
+        p->set_center_of_mass(Array<T, 3>(com[3 * k], com[3 * k + 1], com[3 * k + 2]));
+        p->orientation() = fsi::Quaternion<T>(quat[4 * k], quat[4 * k + 1], quat[4 * k + 2], quat[4 * k + 3]);
+        p->update();
+        fsi2.add_particle(p);
+    }
+    fsi2.init();
+    SpringPotential<T> potential(pot[0], pot[1]);
+    recio::Writer w(out);
+    size_t next = 0;
+    T scale;
+    for (plint it = 0; next < dump.size(); ++it) {
+        if ((it % 10) == 0) {
+            T fraction = (T)it / (T)Nit;
+            scale = gr[0] + (1. - gr[0]) * fraction;
+            for (ImmersedBoundaryDynamics3D<T, DESCRIPTOR, Periodicity>::ObjMapIterator iter = fsi2.particles_begin();
+                 iter != fsi2.particles_end(); ++iter) {
+                RigidParticle3D<T>* p = dynamic_cast<RigidParticle3D<T>*>(iter->second);
+                if (p) {
+                    p->scale() = scale;
+                    p->update();
+                }
+            }
+            fsi2.synchronize_particle_states();
+        }
+        fsi2.compute_collision_forces(potential, &boundary2);
+        fsi2.move_vertices();
+        if (it + 1 == dump[next]) {
+            std::vector<double> c, q, x, f;
+            for (plint id = 0; id < (plint)shape.size(); ++id) {
+                ParticleBase3D<T>* pb = 0;
+                fsi2.get_particle(id, pb);
+                RigidParticle3D<T>* p = dynamic_cast<RigidParticle3D<T>*>(pb);
+                for (int d = 0; d < 3; ++d) c.push_back(p->center_of_mass()[d]);
+                for (int d = 0; d < 4; ++d) q.push_back(p->orientation()[d]);
+                for (plint i = 0; i < p->count_nodes(); ++i)
+                    for (int d = 0; d < 3; ++d) {
+                        x.push_back(p->get_node(i).pos[d]);
+                        f.push_back(p->get_node(i).force[d]);
+                    }
+            }
+            char tc[32], tq[32], tx[32], tf[32];
+            std::sprintf(tc, "com_%lld", dump[next]);
+            std::sprintf(tq, "quat_%lld", dump[next]);
+            std::sprintf(tx, "pos_%lld", dump[next]);
+            std::sprintf(tf, "force_%lld", dump[next]);
+            w.d(tc, shp((long long)shape.size(), 3), c);
+            w.d(tq, shp((long long)shape.size(), 4), q);
+            w.d(tx, shp((long long)(x.size() / 3), 3), x);
+            w.d(tf, shp((long long)(f.size() / 3), 3), f);
+            ++next;
+        }
+    }
+    for (size_t t = 0; t < rigid.size(); ++t) delete rigid[t];
+    delete lattice;
+    return 0;
+}
+
 int main(int argc, char** argv) {
     if (argc < 4) {
         std::fprintf(stderr, "usage: ref_harness <lbm|ibm|forces|interp|shape|inertia> in.rec out.rec\n");
@@ -1047,6 +1226,8 @@ int main(int argc, char** argv) {
     if (c == "calibrate") return run_calibrate(in, argv[3]);
     if (c == "initial") return run_initial(in, argv[3]);
     if (c == "coprocessor") return run_coprocessor(in, argv[3]);
+    if (c == "create") return run_create(in, argv[3]);
+    if (c == "grow") return run_grow(in, argv[3]);
     std::fprintf(stderr, "unknown case %s\n", argv[1]);
     return 2;
 }

@@ -47,6 +47,15 @@ class Potential(C.Structure):
     _fields_ = [("kind", C.c_int32), ("r0", C.c_double), ("beta", C.c_double), ("strength", C.c_double)]
 
 
+class Growth(C.Structure):
+    _fields_ = [
+        ("box", C.c_int64 * 6), ("periodic", C.c_int32 * 3), ("has_wall", C.c_int32), ("wall", C.c_double * 3),
+        ("min_dist", C.c_double), ("strength", C.c_double),
+        ("initial_scale", C.c_double), ("density", C.c_double), ("damping", C.c_double),
+        ("n_it", C.c_int64), ("rescale_every", C.c_int64), ("it_end", C.c_int64),
+    ]
+
+
 def potential(kind, r0, beta=0.0, strength=0.0) -> Potential:
     """MorsePotential(r_min = r0, beta, strength) or SpringPotential(min_dist = r0, strength)."""
     return Potential(POTENTIAL[kind] if isinstance(kind, str) else int(kind), float(r0), float(beta), float(strength))
@@ -118,6 +127,9 @@ def lib():
             "orc_sys_add_pipe_wall_interaction": (C.c_int32, [C.c_void_p, C.POINTER(Potential), C.c_double,
                                                               C.c_double, C.c_double]),
             "orc_sys_velocity": (None, [C.c_void_p, dp]),
+            "orc_shape_mass_props": (None, [C.c_int64, ip, dp, dp, dp]),
+            "orc_grow_particles": (C.c_int32, [C.POINTER(Growth), C.c_int32, ip, dp, ip, ip, C.c_int32, i32p, dp, dp,
+                                               dp, dp]),
         }
         for name, (res, args) in sig.items():
             fn = getattr(L, name)
@@ -826,3 +838,84 @@ def initial_distribution(box, counts, radii, seed, pipe=None):
         else:
             quats.append([1.0, 0.0, 0.0, 0.0])
     return np.array(pos), np.array(quats)
+
+
+def growth(box, wall=None, periodic=(1, 0, 0), pot=(1.0, 5e-2), initial_scale=0.2, density=1.0, damping=0.1,
+           n_it=40000, it_end=None, rescale_every=10) -> Growth:
+    """Parameters of create_particles' growth stage (progs/common/create_particles.h:105-161)."""
+    g = Growth()
+    for k in range(6):
+        g.box[k] = int(box[k])
+    for a in range(3):
+        g.periodic[a] = int(periodic[a])
+    g.has_wall = 0 if wall is None else 1
+    if wall is not None:
+        for k in range(3):
+            g.wall[k] = float(wall[k])
+    g.min_dist, g.strength = float(pot[0]), float(pot[1])
+    g.initial_scale, g.density, g.damping = float(initial_scale), float(density), float(damping)
+    g.n_it, g.rescale_every = int(n_it), int(rescale_every)
+    g.it_end = int(n_it + 1 if it_end is None else it_end)
+    return g
+
+
+def grow_particles(g: Growth, shapes, shape_of, com, quat):
+    """The growth stage on rigid copies of shapes [(xyz, tri), ...]: particle k on shape_of[k]
+    from com[k], quat[k].  Returns (com, quat, vertex positions, vertex forces of the last
+    collision step)."""
+    nv = np.array([len(x) for x, _ in shapes], dtype=np.int64)
+    nt = np.array([len(t) for _, t in shapes], dtype=np.int64)
+    verts = f64(np.concatenate([np.asarray(x, dtype=np.float64) for x, _ in shapes]))
+    tris = i64(np.concatenate([np.asarray(t, dtype=np.int64) for _, t in shapes]))
+    sh = np.ascontiguousarray(shape_of, dtype=np.int32)
+    com, quat = f64(com).copy(), f64(quat).copy()
+    ntot = int(nv[sh].sum())
+    pos, frc = np.zeros((ntot, 3)), np.zeros((ntot, 3))
+    st = lib().orc_grow_particles(C.byref(g), len(shapes), _i(nv), _d(verts), _i(nt), _i(tris), len(sh), _i32(sh),
+                                  _d(com), _d(quat), _d(pos), _d(frc))
+    if st != 0:
+        raise ValueError("orc_grow_particles: bad input")
+    return com, quat, pos, frc
+
+
+def shape_radius(xyz):
+    """ParticleShape::compute_bounding_volumes (ParticleShape.hh:361-383): the largest vertex
+    distance from the origin."""
+    r = 0.0
+    for v in np.asarray(xyz, dtype=np.float64):
+        d = v[0] * v[0] + v[1] * v[1] + v[2] * v[2]
+        if d > r:
+            r = d
+    return float(np.sqrt(r))
+
+
+def place_particle(xyz, tri, pos, quat):
+    """The final placement of create_particles (:193-199): the template's vertices moved by
+    Transform().translate(-com).rotate(quat).translate(pos) (Transform.hh:28-85), com the
+    template's centre (DeformableParticle3D::update)."""
+    xyz = f64(xyz)
+    c = particle_update(xyz, tri)[2:5]
+    q = [float(v) for v in quat]
+    R = [[1 - 2 * (q[2] * q[2] + q[3] * q[3]), 2 * (q[1] * q[2] - q[0] * q[3]), 2 * (q[0] * q[2] + q[1] * q[3])],
+         [2 * (q[1] * q[2] + q[0] * q[3]), 1 - 2 * (q[1] * q[1] + q[3] * q[3]), 2 * (q[2] * q[3] - q[0] * q[1])],
+         [2 * (q[1] * q[3] - q[0] * q[2]), 2 * (q[0] * q[1] + q[2] * q[3]), 1 - 2 * (q[1] * q[1] + q[2] * q[2])]]
+    m3 = [R[i][0] * -c[0] + R[i][1] * -c[1] + R[i][2] * -c[2] + float(pos[i]) for i in range(3)]
+    out = np.empty_like(xyz)
+    for i in range(3):
+        out[:, i] = xyz[:, 0] * R[i][0] + xyz[:, 1] * R[i][1] + xyz[:, 2] * R[i][2] + m3[i]
+    return out
+
+
+def create_particles(box, pipe, types, seed, n_it=40000, periodic=(1, 0, 0)):
+    """create_particles (progs/common/create_particles.h:9-212) for capsule templates: types =
+    [(xyz, tri, count), ...], pipe = (y0, z0, radius); srand(seed) placement at 20 % scale inside
+    the pipe shrunk by 1.5, growth, placement of the templates.  Returns the vertex positions of
+    all particles in order."""
+    shapes = [(x, t) for x, t, _ in types]
+    counts = [int(n) for _, _, n in types]
+    radii = np.array([0.2 * shape_radius(x) + 1.0 for x, _ in shapes])
+    wall = (float(pipe[0]), float(pipe[1]), float(pipe[2]) - 1.5)
+    com, quat = initial_distribution(box, counts, radii, seed, pipe=wall)
+    shape_of = np.repeat(np.arange(len(shapes)), counts)
+    com, quat, _, _ = grow_particles(growth(box, wall, periodic, n_it=n_it), shapes, shape_of, com, quat)
+    return [place_particle(shapes[s][0], shapes[s][1], com[k], quat[k]) for k, s in enumerate(shape_of)]

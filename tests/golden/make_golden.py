@@ -521,9 +521,64 @@ def case_coprocessor():
     save("coprocessor_bgk", inp, out)
 
 
+
+# ---------------------------------------------------------------- growth of the initial distribution
+# A pipe along x through (0, 0) of radius 7.5 and length 24 on the lattice of
+# PipeBoundary::get_bounding_box(2) (Boundary.h:141-146), as progs/rbc_in_pipe_distribution sets it up.
+GROW_BOX = np.array([0, 24, -9, 9, -9, 9])
+GROW_PIPE = np.array([0.0, 0.0, 7.5, 24.0])
+
+
+def growth_shapes():
+    """Two particle types: a sphere of radius 2.5 and an oblate ellipsoid (162 vertices each)."""
+    s0 = meshes.icosphere(2, 2.5)
+    x1, t1 = meshes.icosphere(2, 2.8)
+    return [s0, (x1 * np.array([1.25, 1.25, 0.6]), t1)]
+
+
+def shape_radius(xyz):
+    """ParticleShape::compute_bounding_volumes (ParticleShape.hh:361-383)."""
+    r = 0.0
+    for v in xyz:
+        d = v[0] * v[0] + v[1] * v[1] + v[2] * v[2]
+        if d > r:
+            r = d
+    return float(np.sqrt(r))
+
+
+def case_create():
+    """The reference's own create_particles (progs/common/create_particles.h) for 8 spheres and 3
+    ellipsoids in the pipe: placement at 20 % scale, 40001 growth iterations of rigid copies
+    under spring collisions with the pipe wall at radius 6, capsules placed at the result."""
+    inp = dict(box=GROW_BOX, pipe=GROW_PIPE, counts=np.array([8, 3]), seed=7)
+    for t, (x, tri) in enumerate(growth_shapes()):
+        inp["rest%d" % t], inp["tri%d" % t] = x, tri
+    out = run("create", inp)
+    assert int(out["count"][0]) == 11
+    save("create_particles_pipe", inp, out)
+
+
+def case_grow():
+    """The growth loop of create_particles from the reference's own random placement of the same
+    call (seed 7), the scale reaching 1 after 300 iterations: states after 1, 2, 11 and 301
+    iterations."""
+    shapes = growth_shapes()
+    radii = np.array([0.2 * shape_radius(x) + 1.0 for x, _ in shapes])
+    counts = np.array([8, 3])
+    init = run("initial", dict(box=GROW_BOX, pipe=np.array([0.0, 0.0, 6.0]), counts=counts, radii=radii,
+                               max_radius=radii.max(), seed=7))
+    inp = dict(box=GROW_BOX, wall=np.array([0.0, 0.0, 6.0]), pot=np.array([1.0, 5e-2]), growth=np.array([0.2, 1.0, 0.1]),
+               n_it=300, ntypes=2, shape=np.repeat(np.arange(2), counts), com=init["pos"], quat=init["quat"],
+               dump=np.array([1, 2, 11, 301]))
+    for t, (x, tri) in enumerate(shapes):
+        inp["rest%d" % t], inp["tri%d" % t] = x, tri
+    out = run("grow", inp)
+    save("grow_pipe", inp, out)
+
 CASES = [case_lbm_periodic, case_lbm_shear, case_lbm_bounceback, case_interp, case_shape, case_forces, case_inertia,
          case_ibm_capsule_shear, case_ibm_rbc_periodic, case_ibm_capsule_lambda, case_interact, case_lbm_pipe, case_lbm_pipe_guo, case_ibm_pipe,
-         case_reflect, case_plb, case_lattice_plb, case_calibrate, case_initial, case_coprocessor]
+         case_reflect, case_plb, case_lattice_plb, case_calibrate, case_initial, case_coprocessor,
+         case_create, case_grow]
 
 if __name__ == "__main__":
     if not os.path.exists(HARNESS):
