@@ -48,8 +48,15 @@ class BatchTuning(C.Structure):
 
 
 class Potential(C.Structure):
-    _fields_ = [("kind", C.c_int32), ("reserved", C.c_int32), ("r0", C.c_double), ("beta", C.c_double),
+    _fields_ = [("kind", C.c_int32), ("search", C.c_int32), ("r0", C.c_double), ("beta", C.c_double),
                 ("strength", C.c_double)]
+
+
+class Growth(C.Structure):
+    _fields_ = [("box", C.c_int64 * 6), ("periodic", C.c_int32 * 3), ("has_wall", C.c_int32),
+                ("wall", C.c_double * 3), ("min_dist", C.c_double), ("strength", C.c_double),
+                ("initial_scale", C.c_double), ("density", C.c_double), ("damping", C.c_double),
+                ("n_it", C.c_int64), ("rescale_every", C.c_int64), ("it_end", C.c_int64)]
 
 
 class Config(C.Structure):
@@ -116,6 +123,8 @@ SIGNATURES = {
     "bib_rbc_params": (C.c_int32, [_vp, C.c_int32, C.c_double, C.c_double, C.c_double, _dp]),
     "bib_rbc_shrink_volume": (C.c_int32, [_vp, C.c_int32, _dp, C.c_double, C.c_int64, C.c_double, _dp, _dp]),
     "bib_align_minor_axis": (C.c_int32, [_vp, C.c_int32, _dp, _dp]),
+    "bib_grow_particles": (C.c_int32, [_vp, C.POINTER(Growth), C.c_int32, _i32p, _dp, _dp, _dp, _dp]),
+    "bib_place_particle": (C.c_int32, [_vp, C.c_int32, _dp, _dp, _dp, _dp]),
     "bib_initial_distribution": (C.c_int32, [C.POINTER(C.c_int64), _dp, C.c_int32, C.POINTER(C.c_int64), _dp,
                                              C.c_double, C.c_uint32, C.c_int64, _dp, _dp]),
     "bib_lattice_load_plb": (C.c_int32, [_vp, C.c_int32, C.c_char_p, C.c_char_p]),

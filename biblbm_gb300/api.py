@@ -17,7 +17,7 @@ from dataclasses import dataclass, field
 import numpy as np
 
 from . import _lib
-from ._lib import BatchTuning, BibError, IbParams, LatticeParams, Potential, Tuning
+from ._lib import BatchTuning, BibError, Growth, IbParams, LatticeParams, Potential, Tuning
 
 STORAGE = {"f64": 0, "f32": 1, "f16": 2}
 COLLISION = {"bgk_guo_vof": 0, "bgk": 1, "trt": 2}
@@ -366,14 +366,91 @@ def _volume(pos, tri) -> float:
     return v
 
 
-def MorsePotential(r_min, beta, strength) -> Potential:
-    """fsi/Potentials.h MorsePotential: 2 beta strength x (x - 1), x = exp(beta (r_min - d)), d <= r_min."""
-    return Potential(1, 0, float(r_min), float(beta), float(strength))
+def MorsePotential(r_min, beta, strength, grid=False) -> Potential:
+    """fsi/Potentials.h MorsePotential: 2 beta strength x (x - 1), x = exp(beta (r_min - d)), d <= r_min.
+    grid: as a particle-particle force, searched with the reference's collision grid
+    (CollisionForces.h) instead of every pair within the cutoff."""
+    return Potential(1, 1 if grid else 0, float(r_min), float(beta), float(strength))
 
 
-def SpringPotential(min_dist, strength) -> Potential:
-    """fsi/Potentials.h SpringPotential: (min_dist - d) strength, d <= min_dist."""
-    return Potential(2, 0, float(min_dist), 0.0, float(strength))
+def SpringPotential(min_dist, strength, grid=False) -> Potential:
+    """fsi/Potentials.h SpringPotential: (min_dist - d) strength, d <= min_dist (grid: see MorsePotential)."""
+    return Potential(2, 1 if grid else 0, float(min_dist), 0.0, float(strength))
+
+
+def _shape_nv(ctx: "Context", shape: int) -> int:
+    out = np.zeros(6)
+    ctx.check(ctx.lib.bib_shape_info(ctx.h, int(shape), _d(out)))
+    return int(out[4])
+
+
+def grow_particles(ctx: "Context", shapes, com, quat, box, wall=None, periodic=(1, 0, 0), min_dist=1.0,
+                   strength=5e-2, initial_scale=0.2, density=1.0, damping=0.1, n_it=40000, rescale_every=10,
+                   it_end=None, vertices=False):
+    """The growth stage of create_particles (progs/common/create_particles.h:105-161) on the GPU:
+    rigid copies of the stored shapes `shapes[k]` at com[k] / quat[k] (w, x, y, z) grow from
+    initial_scale to 1 over n_it iterations under spring collision forces (the reference's
+    collision grid) and a pipe wall (y0, z0, radius).  Returns (com, quat), plus the vertex positions
+    and the last collision forces when `vertices`."""
+    sh = np.ascontiguousarray(shapes, dtype=np.int32)
+    com, quat = _f64(com).copy(), _f64(quat).copy()
+    g = Growth()
+    for k in range(6):
+        g.box[k] = int(box[k])
+    for a in range(3):
+        g.periodic[a] = int(periodic[a])
+    g.has_wall = 0 if wall is None else 1
+    if wall is not None:
+        for k in range(3):
+            g.wall[k] = float(wall[k])
+    g.min_dist, g.strength = float(min_dist), float(strength)
+    g.initial_scale, g.density, g.damping = float(initial_scale), float(density), float(damping)
+    g.n_it, g.rescale_every = int(n_it), int(rescale_every)
+    g.it_end = int(n_it + 1 if it_end is None else it_end)
+    nvert = sum(_shape_nv(ctx, int(s)) for s in sh) if vertices else 0
+    pos = np.zeros((nvert, 3)) if vertices else None
+    frc = np.zeros((nvert, 3)) if vertices else None
+    ctx.check(ctx.lib.bib_grow_particles(ctx.h, C.byref(g), len(sh), sh.ctypes.data_as(C.POINTER(C.c_int32)),
+                                         _d(com), _d(quat), _d(pos) if vertices else None,
+                                         _d(frc) if vertices else None))
+    return (com, quat, pos, frc) if vertices else (com, quat)
+
+
+def place_particle(ctx: "Context", shape: int, com, quat, xyz=None) -> np.ndarray:
+    """create_particles' final placement (:193-199): the vertices (default: the shape's rest
+    vertices) moved by translate(-centre of mass), rotate(quat), translate(com)."""
+    n = _shape_nv(ctx, int(shape))
+    v = None if xyz is None else _f64(xyz)
+    out = np.zeros((n, 3))
+    ctx.check(ctx.lib.bib_place_particle(ctx.h, int(shape), _d(v) if v is not None else None, _d(_f64(com)),
+                                         _d(_f64(quat)), _d(out)))
+    return out
+
+
+def create_particles(shapes: ParticleShapeLibrary, types, box, pipe, seed, periodic=(1, 0, 0), n_it=40000,
+                     initial_scale=0.2):
+    """create_particles (progs/common/create_particles.h:9-212) for particle templates on stored
+    shapes: types = [(shape, count), ...], pipe = (y0, z0, radius), srand(seed).  Places the
+    particles at initial_scale inside the pipe shrunk by 1.5 (bib_initial_distribution), grows
+    rigid copies to full size on the GPU and returns [(shape, vertex positions), ...] of the
+    particles at the result, in order, for ImmersedBoundaryDynamics3D.add_particle."""
+    ctx = shapes.ctx
+    sids = [int(s) for s, _ in types]
+    counts = [int(n) for _, n in types]
+    radii = []
+    for s in sids:
+        xyz = shapes.meshes[s][0]
+        r = 0.0
+        for v in xyz:  # ParticleShape::compute_bounding_volumes (ParticleShape.hh:361-383)
+            d = v[0] * v[0] + v[1] * v[1] + v[2] * v[2]
+            r = d if d > r else r
+        radii.append(initial_scale * float(np.sqrt(r)) + 1.)
+    wall = (float(pipe[0]), float(pipe[1]), float(pipe[2]) - 1.5)
+    com, quat = initial_distribution(box, counts, radii, max(radii), seed, pipe=wall)
+    shape_of = np.repeat(np.array(sids, dtype=np.int32), counts)
+    com, quat = grow_particles(ctx, shape_of, com, quat, box, wall=wall, periodic=periodic, n_it=n_it,
+                               initial_scale=initial_scale)
+    return [(int(s), place_particle(ctx, int(s), com[k], quat[k])) for k, s in enumerate(shape_of)]
 
 
 class ImmersedBoundaryDynamics3D:

@@ -375,6 +375,14 @@ void free_particles(Lattice& L) {
     cudaFree(L.pgrid.end);
     cudaFree(L.pgrid.temp);
     L.pgrid = PairGrid{};
+    for (int k = 0; k < 2; ++k) {
+        cudaFree(L.rgrid.keys[k]);
+        cudaFree(L.rgrid.ids[k]);
+    }
+    cudaFree(L.rgrid.start);
+    cudaFree(L.rgrid.end);
+    cudaFree(L.rgrid.temp);
+    L.rgrid = RefGridBuffers{};
     cudaFree(L.vox_count);
     cudaFree(L.vox_z);
     L.vox_count = nullptr;
@@ -479,7 +487,27 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
     if (L.membrane_smem + 1024 > (size_t)dev_max)
         return fail(c, BIB_EUNSUPPORTED, "mesh with %d vertices exceeds the membrane kernel's shared memory", L.max_nv);
     configure_membrane_kernel(L.membrane_smem);
-    if (L.inter.npp > 0) {
+    if (L.inter.npp > 0 && L.inter.pp_search == BIB_PAIR_SEARCH_GRID) {
+        // the reference's collision grid over the lattice box: a dense table of its cells
+        const int64_t box[6] = {0, L.d.nx - 1, 0, L.d.ny - 1, 0, L.d.nz - 1};
+        const int per[3] = {L.d.px, L.d.py, L.d.pz};
+        if (ref_grid_cells(box) > kMaxRefGridCells)
+            return fail(c, BIB_EUNSUPPORTED, "lattice too large for the reference's collision grid");
+        const RefGrid g = ref_grid(box, per, L.inter.pp_cut, L.nvert);
+        RefGridBuffers& R = L.rgrid;
+        R.bits = ref_grid_bits(g.ncell);
+        for (int k = 0; k < 2; ++k) {
+            BIB_ALLOC(c, (void**)&R.keys[k], L.nvert * sizeof(uint32_t));
+            BIB_ALLOC(c, (void**)&R.ids[k], L.nvert * sizeof(uint32_t));
+        }
+        BIB_CUDA(c, cudaMemset(R.keys[1], 0, L.nvert * sizeof(uint32_t)));
+        BIB_ALLOC(c, (void**)&R.start, ((size_t)g.ncell + 1) * sizeof(int));
+        BIB_ALLOC(c, (void**)&R.end, ((size_t)g.ncell + 1) * sizeof(int));
+        BIB_CUDA(c, cudaMemset(R.start, 0, ((size_t)g.ncell + 1) * sizeof(int)));
+        BIB_CUDA(c, cudaMemset(R.end, 0, ((size_t)g.ncell + 1) * sizeof(int)));
+        R.temp_bytes = ref_grid_temp_bytes(L.nvert, R.bits);
+        BIB_ALLOC(c, &R.temp, std::max<size_t>(R.temp_bytes, 16));
+    } else if (L.inter.npp > 0) {
         // pair search: cells of at least the cutoff, hashed into >= 2 buckets per vertex
         PairGrid& G = L.pgrid;
         const int N[3] = {L.d.nx, L.d.ny, L.d.nz};
@@ -2009,11 +2037,15 @@ bib_status bib_add_pp_interaction(bib_ctx* c, int32_t h, const bib_potential* p)
     bib_status st = check_potential(c, p);
     if (st) return st;
     if (L->inter.npp >= BIB_MAX_PP_INTERACTIONS) return fail(c, BIB_EINVAL, "too many particle-particle interactions");
+    if (p->search != BIB_PAIR_SEARCH_ALL && p->search != BIB_PAIR_SEARCH_GRID) return fail(c, BIB_EINVAL, "bad pair search");
+    if (L->inter.npp > 0 && p->search != L->inter.pp_search)
+        return fail(c, BIB_EINVAL, "the particle-particle interactions of a lattice use one pair search");
     // the reference limits the cutoff to the delta kernel's half support - 1/2
     // (ImmersedBoundaryDynamics_forces.hh:346-349)
     const double limit = (L->ib.dirac == BIB_DIRAC_PESKIN ? 2.0 : 1.5) - 0.5;
     if (p->r0 > limit) return fail(c, BIB_EINVAL, "interaction cutoff %g exceeds %g", p->r0, limit);
     L->inter.pp[L->inter.npp++] = PotentialDev{p->kind, p->r0, p->beta, p->strength};
+    L->inter.pp_search = p->search;
     L->inter.pp_cut = std::max(L->inter.pp_cut, p->r0);
     // the pair search buffers are sized with the particles: re-upload them on the next step
     st = pull_particles(c, *L);
@@ -3166,6 +3198,236 @@ bib_status bib_align_minor_axis(bib_ctx* c, int32_t shape, double* pos, const do
     for (int v = 0; v < nv; ++v) {
         const double x = pos[3 * v], y = pos[3 * v + 1], z = pos[3 * v + 2];
         for (int i = 0; i < 3; ++i) pos[3 * v + i] = x * m[i][0] + y * m[i][1] + z * m[i][2] + m[i][3];
+    }
+    return BIB_OK;
+}
+
+}  // extern "C"
+
+// ParticleShape::compute_properties' moment of inertia about the origin (ParticleShape.hh:254-356)
+static void shape_inertia_origin(const ShapeHost& S, double* I) {
+    double in[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+    const int nt = (int)(S.tri.size() / 3);
+    const double* pos = S.rest.data();
+    for (int t = 0; t < nt; ++t) {
+        const double* v0 = pos + 3 * S.tri[3 * t];
+        const double* v1 = pos + 3 * S.tri[3 * t + 1];
+        const double* v2 = pos + 3 * S.tri[3 * t + 2];
+        const V3d N = crs(V3d{v1[0] - v0[0], v1[1] - v0[1], v1[2] - v0[2]}, V3d{v2[0] - v0[0], v2[1] - v0[1], v2[2] - v0[2]});
+        double f2[3], f3[3], g0[3], g1[3], g2[3];
+        for (int d = 0; d < 3; ++d) {
+            const double tmp0 = v0[d] + v1[d];
+            const double f1 = tmp0 + v2[d];
+            const double tmp1 = v0[d] * v0[d];
+            const double tmp2 = tmp1 + v1[d] * tmp0;
+            f2[d] = tmp2 + v2[d] * f1;
+            f3[d] = v0[d] * tmp1 + v1[d] * tmp2 + v2[d] * f2[d];
+            g0[d] = f2[d] + v0[d] * (f1 + v0[d]);
+            g1[d] = f2[d] + v1[d] * (f1 + v1[d]);
+            g2[d] = f2[d] + v2[d] * (f1 + v2[d]);
+        }
+        in[4] += N.x * f3[0];
+        in[5] += N.y * f3[1];
+        in[6] += N.z * f3[2];
+        in[7] += N.x * (v0[1] * g0[0] + v1[1] * g1[0] + v2[1] * g2[0]);
+        in[8] += N.y * (v0[2] * g0[1] + v1[2] * g1[1] + v2[2] * g2[1]);
+        in[9] += N.z * (v0[0] * g0[2] + v1[0] * g1[2] + v2[0] * g2[2]);
+    }
+    for (int k = 4; k <= 6; ++k) in[k] *= (double)(1.0 / 60.0);
+    for (int k = 7; k <= 9; ++k) in[k] *= (double)(1.0 / 120.0);
+    I[0] = in[5] + in[6];
+    I[1] = -in[7];
+    I[2] = -in[9];
+    I[3] = I[1];
+    I[4] = in[4] + in[6];
+    I[5] = -in[8];
+    I[6] = I[2];
+    I[7] = I[5];
+    I[8] = in[4] + in[5];
+}
+
+// Device buffers of one call, freed when it returns.
+struct CallBuffers {
+    std::vector<void*> p;
+    ~CallBuffers() {
+        for (void* q : p) cudaFree(q);
+    }
+    bool get(bib_ctx* c, void** out, size_t bytes) {
+        if (dev_malloc(c, out, std::max<size_t>(bytes, 16)) != cudaSuccess) {
+            cudaGetLastError();
+            *out = nullptr;
+            return false;
+        }
+        p.push_back(*out);
+        return true;
+    }
+};
+
+extern "C" {
+
+bib_status bib_grow_particles(bib_ctx* c, const bib_growth* g, int32_t n, const int32_t* shape, double* com,
+                              double* quat, double* pos_out, double* force_out) {
+    if (!c || !g || n < 0 || (n > 0 && (!shape || !com || !quat))) return fail(c, BIB_EINVAL, "invalid argument");
+    for (int a = 0; a < 3; ++a)
+        if (g->box[2 * a + 1] - g->box[2 * a] < 1 || g->box[2 * a + 1] - g->box[2 * a] > (1 << 20))
+            return fail(c, BIB_EINVAL, "box extents must be in [2, 2^20 + 1]");
+    const double vals[] = {g->min_dist, g->strength, g->initial_scale, g->density, g->damping,
+                           g->wall[0], g->wall[1], g->wall[2]};
+    for (double v : vals)
+        if (!std::isfinite(v)) return fail(c, BIB_EINVAL, "growth parameters must be finite");
+    if (!(g->min_dist > 0 && g->min_dist <= 1.0)) return fail(c, BIB_EINVAL, "min_dist must be in (0, 1]");
+    if (!(g->initial_scale > 0) || !(g->density > 0) || g->n_it < 1 || g->rescale_every < 1 || g->it_end < 0 ||
+        g->it_end > g->n_it + 1 || (g->has_wall && !(g->wall[2] > 0)))
+        return fail(c, BIB_EINVAL, "need initial_scale, density > 0, n_it, rescale_every >= 1, 0 <= it_end <= n_it + 1");
+    // the shapes in use and the vertex ranges of the particles
+    std::vector<int> local(c->shapes.size(), -1), used;
+    std::vector<int> pshape(n), pv0(n);
+    int64_t nvert = 0;
+    for (int k = 0; k < n; ++k) {
+        if (shape[k] < 0 || shape[k] >= (int32_t)c->shapes.size()) return fail(c, BIB_EINVAL, "invalid shape %d", shape[k]);
+        if (local[shape[k]] < 0) {
+            local[shape[k]] = (int)used.size();
+            used.push_back(shape[k]);
+        }
+        pshape[k] = local[shape[k]];
+        pv0[k] = (int)nvert;
+        nvert += (int64_t)(c->shapes[shape[k]]->rest.size() / 3);
+        for (int d = 0; d < 3; ++d)
+            if (!std::isfinite(com[3 * k + d])) return fail(c, BIB_EINVAL, "non-finite centre");
+        for (int d = 0; d < 4; ++d)
+            if (!std::isfinite(quat[4 * k + d])) return fail(c, BIB_EINVAL, "non-finite orientation");
+    }
+    if (nvert > (1 << 28)) return fail(c, BIB_EINVAL, "too many vertices");
+    const int ns = (int)used.size();
+    std::vector<int> snv(ns), sv0(ns);
+    std::vector<double> verts, vol(ns), inertia(9 * (size_t)ns);
+    for (int s = 0; s < ns; ++s) {
+        const ShapeHost& S = *c->shapes[used[s]];
+        snv[s] = (int)(S.rest.size() / 3);
+        sv0[s] = (int)(verts.size() / 3);
+        verts.insert(verts.end(), S.rest.begin(), S.rest.end());
+        vol[s] = S.volume;
+        shape_inertia_origin(S, &inertia[9 * (size_t)s]);
+    }
+    std::vector<int> owner((size_t)nvert);
+    for (int k = 0; k < n; ++k)
+        for (int i = 0; i < snv[pshape[k]]; ++i) owner[(size_t)pv0[k] + i] = k;
+    const int per[3] = {g->periodic[0] ? 1 : 0, g->periodic[1] ? 1 : 0, g->periodic[2] ? 1 : 0};
+    if (ref_grid_cells(g->box) > kMaxRefGridCells) return fail(c, BIB_EINVAL, "box too large for the collision grid");
+    const RefGrid grid = ref_grid(g->box, per, g->min_dist, (int)nvert);
+    CallBuffers B;
+    GrowthView G;
+    RefGridBuffers R;
+    R.bits = ref_grid_bits(grid.ncell);
+    R.temp_bytes = ref_grid_temp_bytes((int)nvert, R.bits);
+    int *d_shape, *d_pv0, *d_snv, *d_sv0, *d_owner;
+    double *d_verts, *d_vol, *d_inertia, *d_state, *d_pos, *d_force, *d_torque;
+    const size_t np = (size_t)std::max(n, 1);
+    const bool ok = B.get(c, (void**)&d_shape, np * sizeof(int)) && B.get(c, (void**)&d_pv0, np * sizeof(int)) &&
+                    B.get(c, (void**)&d_snv, ns * sizeof(int)) && B.get(c, (void**)&d_sv0, ns * sizeof(int)) &&
+                    B.get(c, (void**)&d_owner, nvert * sizeof(int)) &&
+                    B.get(c, (void**)&d_verts, verts.size() * sizeof(double)) &&
+                    B.get(c, (void**)&d_vol, ns * sizeof(double)) &&
+                    B.get(c, (void**)&d_inertia, 9 * ns * sizeof(double)) &&
+                    B.get(c, (void**)&d_state, 13 * np * sizeof(double)) &&
+                    B.get(c, (void**)&d_pos, 3 * nvert * sizeof(double)) &&
+                    B.get(c, (void**)&d_force, 3 * nvert * sizeof(double)) &&
+                    B.get(c, (void**)&d_torque, 3 * nvert * sizeof(double)) &&
+                    B.get(c, (void**)&R.keys[0], nvert * sizeof(uint32_t)) &&
+                    B.get(c, (void**)&R.keys[1], nvert * sizeof(uint32_t)) &&
+                    B.get(c, (void**)&R.ids[0], nvert * sizeof(uint32_t)) &&
+                    B.get(c, (void**)&R.ids[1], nvert * sizeof(uint32_t)) &&
+                    B.get(c, (void**)&R.start, ((size_t)grid.ncell + 1) * sizeof(int)) &&
+                    B.get(c, (void**)&R.end, ((size_t)grid.ncell + 1) * sizeof(int)) && B.get(c, &R.temp, R.temp_bytes);
+    if (!ok) return fail(c, BIB_ENOMEM, "device allocation for the growth stage failed");
+    std::vector<double> state(13 * np, 0.0);  // com, quat, vel, omega
+    for (int k = 0; k < n; ++k) {
+        for (int d = 0; d < 3; ++d) state[3 * (size_t)k + d] = com[3 * k + d];
+        for (int d = 0; d < 4; ++d) state[3 * np + 4 * (size_t)k + d] = quat[4 * k + d];
+    }
+    cudaStream_t st = c->stream;
+    BIB_CUDA(c, cudaMemcpyAsync(d_shape, pshape.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_pv0, pv0.data(), n * sizeof(int), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_snv, snv.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_sv0, sv0.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_owner, owner.data(), nvert * sizeof(int), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_verts, verts.data(), verts.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_vol, vol.data(), ns * sizeof(double), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_inertia, inertia.data(), 9 * ns * sizeof(double), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_state, state.data(), 13 * np * sizeof(double), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemsetAsync(d_force, 0, 3 * nvert * sizeof(double), st));
+    BIB_CUDA(c, cudaMemsetAsync(R.keys[1], 0, nvert * sizeof(uint32_t), st));
+    BIB_CUDA(c, cudaMemsetAsync(R.start, 0, ((size_t)grid.ncell + 1) * sizeof(int), st));
+    BIB_CUDA(c, cudaMemsetAsync(R.end, 0, ((size_t)grid.ncell + 1) * sizeof(int), st));
+    G.np = n;
+    G.shape = d_shape;
+    G.part_v0 = d_pv0;
+    G.shape_nv = d_snv;
+    G.shape_v0 = d_sv0;
+    G.verts = d_verts;
+    G.volume = d_vol;
+    G.inertia = d_inertia;
+    G.com = d_state;
+    G.quat = d_state + 3 * np;
+    G.vel = d_state + 7 * np;
+    G.omega = d_state + 10 * np;
+    G.pos = d_pos;
+    G.force = d_force;
+    G.torque = d_torque;
+    G.density = g->density;
+    G.damping = g->damping;
+    for (int a = 0; a < 3; ++a) {
+        G.per[a] = per[a];
+        G.x0[a] = (double)g->box[2 * a] - 0.5;
+        G.L[a] = (double)(g->box[2 * a + 1] - g->box[2 * a] + 1);
+        G.Linv[a] = 1. / G.L[a];
+    }
+    const PotentialDev pot{BIB_POTENTIAL_SPRING, g->min_dist, 0.0, g->strength};
+    const double wall[3] = {g->wall[0], g->wall[1], g->wall[2]};
+    double scale = g->initial_scale;
+    launch_rigid_nodes(G, scale, st);
+    for (int64_t it = 0; it < g->it_end; ++it) {
+        if (it % g->rescale_every == 0) {
+            const double fraction = (double)it / (double)g->n_it;
+            scale = g->initial_scale + (1. - g->initial_scale) * fraction;
+            launch_rigid_nodes(G, scale, st);
+        }
+        launch_ref_grid_forces(grid, R, pot, d_pos, d_owner, d_force, true, g->has_wall ? wall : nullptr, st);
+        launch_rigid_move(G, scale, st);
+        if ((it & 1023) == 1023) BIB_CHECK_LAUNCH(c);
+    }
+    BIB_CHECK_LAUNCH(c);
+    BIB_CUDA(c, cudaMemcpyAsync(state.data(), d_state, 7 * np * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (pos_out) BIB_CUDA(c, cudaMemcpyAsync(pos_out, d_pos, 3 * nvert * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (force_out) BIB_CUDA(c, cudaMemcpyAsync(force_out, d_force, 3 * nvert * sizeof(double), cudaMemcpyDeviceToHost, st));
+    BIB_CUDA(c, cudaStreamSynchronize(st));
+    for (int k = 0; k < n; ++k) {
+        for (int d = 0; d < 3; ++d) com[3 * k + d] = state[3 * (size_t)k + d];
+        for (int d = 0; d < 4; ++d) quat[4 * k + d] = state[3 * np + 4 * (size_t)k + d];
+    }
+    return BIB_OK;
+}
+
+bib_status bib_place_particle(bib_ctx* c, int32_t shape, const double* xyz, const double* com, const double* quat,
+                              double* out) {
+    if (!c || !com || !quat || !out || shape < 0 || shape >= (int32_t)c->shapes.size())
+        return fail(c, BIB_EINVAL, "invalid shape or argument");
+    const ShapeHost& S = *c->shapes[shape];
+    const int nv = (int)(S.rest.size() / 3);
+    const double* v = xyz ? xyz : S.rest.data();
+    double st[STATS];
+    particle_update(S, v, st);
+    const double* cm = st + 2;
+    const double* q = quat;
+    const double R[3][3] = {{1 - 2 * (q[2] * q[2] + q[3] * q[3]), 2 * (q[1] * q[2] - q[0] * q[3]), 2 * (q[0] * q[2] + q[1] * q[3])},
+                            {2 * (q[1] * q[2] + q[0] * q[3]), 1 - 2 * (q[1] * q[1] + q[3] * q[3]), 2 * (q[2] * q[3] - q[0] * q[1])},
+                            {2 * (q[1] * q[3] - q[0] * q[2]), 2 * (q[0] * q[1] + q[2] * q[3]), 1 - 2 * (q[1] * q[1] + q[2] * q[2])}};
+    // Transform().translate(-c).rotate(R).translate(com) as the 3 x 4 map it builds
+    double m3[3];
+    for (int i = 0; i < 3; ++i) m3[i] = R[i][0] * -cm[0] + R[i][1] * -cm[1] + R[i][2] * -cm[2] + com[i];
+    for (int k = 0; k < nv; ++k) {
+        const double x = v[3 * k], y = v[3 * k + 1], z = v[3 * k + 2];
+        for (int i = 0; i < 3; ++i) out[3 * k + i] = x * R[i][0] + y * R[i][1] + z * R[i][2] + m3[i];
     }
     return BIB_OK;
 }

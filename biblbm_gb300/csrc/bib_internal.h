@@ -120,6 +120,7 @@ struct Interactions {
     int npp = 0;
     PotentialDev pp[BIB_MAX_PP_INTERACTIONS] = {};
     double pp_cut = 0.0;  // largest particle-particle cutoff
+    int pp_search = 0;    // BIB_PAIR_SEARCH_*
 };
 
 // Hashed cell list of the pair search: cells of at least the cutoff (nc per axis, size cs),
@@ -136,6 +137,62 @@ struct PairGrid {
     void* temp = nullptr;
     size_t temp_bytes = 0;
 };
+
+// The reference's collision grid (fsi/Grid.hh over the box [lo - 1/2, hi + 1/2 - eps] per axis,
+// one envelope layer; CollisionForces.h): nc cells per axis of size cs, cell 0 at g0; vertices
+// strictly inside (lo_, hi_) (the box enlarged by the cutoff) are keyed by their cell.
+struct RefGrid {
+    int nc[3];
+    int per[3];
+    int ncell;
+    int nvert;
+    double cs[3], g0[3], b0[3];
+    double lo[3], hi[3];
+    double L[3], Linv[3];  // periodic arithmetic of the box
+};
+struct RefGridBuffers {
+    uint32_t* keys[2] = {nullptr, nullptr};
+    uint32_t* ids[2] = {nullptr, nullptr};
+    int* start = nullptr;  // ncell + 1 entries each, zero between uses
+    int* end = nullptr;
+    void* temp = nullptr;
+    size_t temp_bytes = 0;
+    int bits = 0;
+};
+int64_t ref_grid_cells(const int64_t* box);  // cells of the grid over box (envelope included)
+constexpr int64_t kMaxRefGridCells = (int64_t)1 << 30;
+RefGrid ref_grid(const int64_t* box, const int* periodic, double cut, int nvert);
+int ref_grid_bits(int64_t ncell);
+size_t ref_grid_temp_bytes(int nvert, int bits);
+// forces of one potential by the reference's grid search; zero: start from zero forces (and
+// write the vertices outside the grid), else add in place; wall {y0, z0, radius} or null: the
+// growth stage's pipe wall pass
+void launch_ref_grid_forces(const RefGrid& g, const RefGridBuffers& B, const PotentialDev& pot, const double* pos,
+                            const int* owner, double* force, bool zero, const double* wall, cudaStream_t s);
+
+// Rigid copies of shapes in the growth stage of the initial distribution (device pointers).
+struct GrowthView {
+    int np = 0;
+    const int* shape = nullptr;     // per particle
+    const int* part_v0 = nullptr;   // first vertex of each particle
+    const int* shape_nv = nullptr;  // per shape
+    const int* shape_v0 = nullptr;  // first vertex of each shape in verts
+    const double* verts = nullptr;  // the shapes' vertices
+    const double* volume = nullptr; // per shape
+    const double* inertia = nullptr;  // 9 per shape, about the origin
+    double* com = nullptr;
+    double* quat = nullptr;
+    double* vel = nullptr;
+    double* omega = nullptr;
+    double* pos = nullptr;
+    const double* force = nullptr;
+    double* torque = nullptr;  // 3 per vertex, scratch
+    double density = 1.0, damping = 0.0;
+    int per[3] = {0, 0, 0};
+    double x0[3] = {0, 0, 0}, L[3] = {1, 1, 1}, Linv[3] = {1, 1, 1};
+};
+void launch_rigid_nodes(const GrowthView& G, double scale, cudaStream_t s);
+void launch_rigid_move(const GrowthView& G, double scale, cudaStream_t s);
 
 // What the immersed-boundary kernels need of one lattice for one step (buffer parities
 // resolved).  A single lattice passes one view by value; a batch passes a device table of
@@ -257,6 +314,7 @@ struct Lattice {
     int* vert_particle = nullptr;         // global vertex -> particle
     Interactions inter;                   // wall and particle-particle interactions
     PairGrid pgrid;                       // pair search of the particle-particle interactions
+    RefGridBuffers rgrid;                 // ... when they use the reference's collision grid
     int max_nv = 0;
     int max_elems = 0;            // most triangles, links or pairs of one particle
     int max_nt = 0;               // most triangles of one particle

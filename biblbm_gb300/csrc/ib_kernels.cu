@@ -1635,7 +1635,18 @@ size_t pp_sort_temp_bytes(int nvert, int bits) {
 }
 
 void launch_pp_forces(const Lattice& L, cudaStream_t s) {
-    if (L.inter.npp == 0 || L.nvert == 0 || !L.pgrid.table) return;
+    if (L.inter.npp == 0 || L.nvert == 0) return;
+    if (L.inter.pp_search == BIB_PAIR_SEARCH_GRID) {
+        // one CollisionHandler per potential, in order (ImmersedBoundaryDynamics_forces.hh:299-301)
+        if (!L.rgrid.start) return;
+        const int64_t box[6] = {0, L.d.nx - 1, 0, L.d.ny - 1, 0, L.d.nz - 1};
+        const int per[3] = {L.d.px, L.d.py, L.d.pz};
+        for (int k = 0; k < L.inter.npp; ++k)
+            launch_ref_grid_forces(ref_grid(box, per, L.inter.pp[k].r0, L.nvert), L.rgrid, L.inter.pp[k],
+                                   L.pos[L.pcur], L.vert_particle, L.force, false, nullptr, s);
+        return;
+    }
+    if (!L.pgrid.table) return;
     const PairGrid& G = L.pgrid;
     PairCells g;
     for (int a = 0; a < 3; ++a) {

@@ -243,6 +243,40 @@ bib_status bib_initial_distribution(const int64_t* box, const double* pipe, int3
                                     const double* radii, double max_radius, uint32_t seed, int64_t max_tries,
                                     double* pos, double* quat);
 
+/* ---- growth of the initial distribution (progs/common/create_particles.h:105-212) ----
+ * bib_grow_particles: rigid copies (RigidParticle3D, RigidParticle.hh) of the stored shapes
+ * shape[k], centred at com[k] with orientation quat[k] ({w, x, y, z}), grow from initial_scale:
+ * every rescale_every iterations the scale becomes initial_scale + (1 - initial_scale) it / n_it;
+ * each iteration the vertices feel SpringPotential(min_dist, strength) collision forces between
+ * particles and, with has_wall, against the PipeBoundary wall (compute_collision_forces with the
+ * reference's grid search and wall pass, CollisionForces.h:63-184), and every particle moves as a
+ * damped rigid body (RigidParticle3D::move_vertices, RigidParticle.hh:55-101) with the periodic
+ * remap of its centre.  The box is the lattice's bounding box (each extent >= 2).  Iterations
+ * 0 .. it_end - 1 run on the GPU (n_it + 1 of them: the whole growth); com and quat are updated in
+ * place; pos_out / force_out (optional, 3 doubles per vertex in particle order) receive the
+ * vertex positions after the last iteration and the collision forces of its force step.  The
+ * force and move arithmetic follows the reference's operation order (the forces bit for bit; the
+ * rotation's sin / cos are CUDA's).
+ * bib_place_particle: the final placement of create_particles (:193-199): the vertices xyz of a
+ * particle on `shape` (NULL: the shape's rest vertices) moved by translate(-c), rotate(quat),
+ * translate(com) (Transform.hh:28-85), c their centre of mass (DeformableParticle3D::update);
+ * host only. */
+typedef struct {
+    int64_t box[6];            /* x0, x1, y0, y1, z0, z1 */
+    int32_t periodic[3];
+    int32_t has_wall;
+    double wall[3];            /* y0, z0, radius of the pipe (the drivers pass the pipe radius - 1.5) */
+    double min_dist, strength; /* SpringPotential: cutoff min_dist in (0, 1] */
+    double initial_scale, density, damping;
+    int64_t n_it;              /* the scale reaches 1 at iteration n_it (the reference's drivers: 40000) */
+    int64_t rescale_every;     /* the reference's drivers: 10 */
+    int64_t it_end;            /* in [0, n_it + 1] */
+} bib_growth;
+bib_status bib_grow_particles(bib_ctx* ctx, const bib_growth* g, int32_t n, const int32_t* shape, double* com,
+                              double* quat, double* pos_out, double* force_out);
+bib_status bib_place_particle(bib_ctx* ctx, int32_t shape, const double* xyz, const double* com, const double* quat,
+                              double* out);
+
 /* ---- immersed boundary: ImmersedBoundaryDynamics3D ---- */
 bib_status bib_ib_configure(bib_ctx* ctx, int32_t h, const bib_ib_params* p);
 /* ImmersedBoundaryDynamics3D::set_boundary with a PipeBoundary along x through (y0, z0): vertices
@@ -287,14 +321,19 @@ bib_status bib_total_volume(bib_ctx* ctx, int32_t h, double* v);
  * interactions (add_pp_force with PPPotentialForce, ParticleParticleInteraction.h:24-40, evaluated
  * as CollisionHandler::handle_collision, CollisionForces.h:187-199).  Potentials (Potentials.h):
  * Morse 2 beta strength x (x - 1), x = exp(beta (r0 - d)); spring (r0 - d) strength; both act
- * for d <= r0.  The pair search takes every pair of vertices of different particles within r0
- * (minimum image on periodic axes); the reference's grid search examines 7 of the 13 forward
- * neighbour cells and can miss pairs.  Particle-particle cutoffs are limited to the delta
+ * for d <= r0.  Pair search BIB_PAIR_SEARCH_ALL takes every pair of vertices of different
+ * particles within r0 (minimum image on periodic axes).  BIB_PAIR_SEARCH_GRID is the reference's
+ * own search (CollisionHandler over a Grid of ~unit cells, CollisionForces.h:63-164, Grid.hh): a
+ * cell pairs with 7 of its 13 forward neighbours, so pairs in cells offset by e.g. (+1, -1, 0) are
+ * missed; only vertices inside the lattice box enlarged by 1/2 + r0 take part; the terms are
+ * accumulated in the reference's order, one potential after the other.  All particle-particle
+ * interactions of a lattice use one search.  Particle-particle cutoffs are limited to the delta
  * kernel's half support - 1/2, as in the reference (ImmersedBoundaryDynamics_forces.hh:346-349). ---- */
 enum { BIB_POTENTIAL_NONE = 0, BIB_POTENTIAL_MORSE = 1, BIB_POTENTIAL_SPRING = 2 };
+enum { BIB_PAIR_SEARCH_ALL = 0, BIB_PAIR_SEARCH_GRID = 1 };
 typedef struct {
     int32_t kind;    /* BIB_POTENTIAL_* */
-    int32_t reserved;
+    int32_t search;  /* BIB_PAIR_SEARCH_* (particle-particle interactions; ignored for walls) */
     double r0;       /* Morse r_min / spring min_dist: the cutoff */
     double beta;     /* Morse beta (unused by the spring) */
     double strength; /* Morse strength / spring constant */
