@@ -126,6 +126,9 @@ class Context:
 def lattice_params(periodic=(1, 1, 1), collision="bgk_guo_vof", storage="f64", omega=1.0, omega_inner=None,
                    trt_magic=0.25, wall_y="none", wall_z="none", wall_u=None, body_force=(0, 0, 0), use_phase=False,
                    f16_scale=0.0) -> LatticeParams:
+    """Lattice description of bib_lattice_add_domain.  storage: "f64" (the reference's arithmetic),
+    "f32" or "f16" (FP32 collision; "f16" halves the population bytes and pays on lattices of
+    millions of cells; below ~1 M cells "f32" is as fast and two orders more accurate)."""
     p = LatticeParams()
     for k in range(3):
         p.periodic[k] = int(bool(periodic[k]))

@@ -14,6 +14,8 @@
 #include <utility>
 #include <vector>
 
+#include <nvtx3/nvToolsExt.h>
+
 #include "bib_internal.h"
 
 using namespace bib;
@@ -546,8 +548,17 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
     return BIB_OK;
 }
 
+// Phase boundaries of a step.  With profiling on: an event on the stream for the per-phase device
+// times, and an NVTX range per phase named after the reference's Profile timers
+// (fsi/Profile.h:26-97; the drivers time "compute_forces", "spread_forces", "lbm" around
+// collideAndStream and its wall processors, "interpolate" and "move") for nsys / ncu timelines.
 void record(bib_ctx* c, int idx) {
-    if (c->profiling) cudaEventRecord(c->ev[idx], c->stream);
+    if (!c->profiling) return;
+    cudaEventRecord(c->ev[idx], c->stream);
+    static const char* const kPhase[5] = {"compute_forces", "spread_forces", "lbm", "lbm (wall processors)",
+                                          "interpolate + move"};
+    if (idx > 0) nvtxRangePop();
+    if (idx < 5) nvtxRangePushA(kPhase[idx]);
 }
 
 

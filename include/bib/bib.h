@@ -59,7 +59,13 @@ enum {
     BIB_EOVERFLOW = -8     /* a fixed-capacity device buffer overflowed (see bib_check_health) */
 };
 
-/* population storage on the device */
+/* population storage on the device.  F64 keeps the reference's arithmetic (the parity path; its
+ * collision is FP64-bound on this part, ~1/20 of the F16 step's rate).  F32 collides in FP32 at
+ * twice F16's bytes.  F16 stores f-bar times a scale (f16_scale) and collides in FP32: it pays on
+ * large lattices, whose step is bound by moving the populations (the 8.4 M-cell channel: FP16 1.27x
+ * FP32); on lattices below ~1 M cells the step is bound by its launches and the immersed boundary,
+ * FP16 is no faster than FP32 there and its error is two orders larger (64^3 capsule: Taylor
+ * deformation error 4.5e-4 against 2.4e-6), so F32 is the better choice there. */
 enum { BIB_STORAGE_F64 = 0, BIB_STORAGE_F32 = 1, BIB_STORAGE_F16 = 2 };
 /* collision operator */
 enum {
@@ -471,7 +477,10 @@ bib_status bib_spread_forces_noalloc(bib_ctx* ctx, int32_t h, const double* pos,
 /* ---- timing: per-kernel-group device time (ms) of the last bib_step call when profiling is on ---- */
 bib_status bib_set_profiling(bib_ctx* ctx, int32_t enabled);
 /* out[5] = {membrane forces, spreading, collide+stream, walls, interpolation+move+update};
- * cumulative device milliseconds since profiling was enabled */
+ * cumulative device milliseconds since profiling was enabled.  The groups are the reference's
+ * Profile timers (fsi/Profile.h:26-97): compute_forces, spread_forces, lbm (collideAndStream and,
+ * as out[3], its wall processors), interpolate + move; with profiling on, each step also opens
+ * NVTX ranges of those names around its phases (steps run eagerly, not as graphs). */
 bib_status bib_profile_read(bib_ctx* ctx, double* out, int32_t n);
 
 #ifdef __cplusplus
