@@ -635,7 +635,7 @@ def main():
             t3 = time.perf_counter()
             tx["send_gbs_" + name] = buf.nbytes / (t2 - t1) / 1e9
             tx["receive_gbs_" + name] = buf.nbytes / (t3 - t2) / 1e9
-        e2e = {"value": cells * K * world / dt / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": int(h2d // K),
+        rt = {"value": cells * K * world / dt / 1e6, "unit": "MLUPS", "h2d_bytes_per_step": int(h2d // K),
                "d2h_bytes_per_step": int(d2h // K), "seconds": dt, **tx,
                "what": "bib_lattice_send of the FP64 initial populations + bib_particles_upload of the vertex positions, K x (bib_step + "
                        "bib_particles_download_async of the per-cell area/volume/centre, waited for one step "
@@ -662,13 +662,17 @@ def main():
         c3.check(lib.bib_lattice_get_velocity(h, l3.h, dpd(u_out)))
         dt2 = max_over_ranks(time.perf_counter() - t0)
         barrier()
-        e2e["driver_loop"] = {
+        # the headline: the reference's own driver loop; the population round trip of the
+        # CoProcessor3D boundary (bound by the CPU-GPU link for few steps) beside it
+        e2e = {
             "value": cells * K * world / dt2 / 1e6, "unit": "MLUPS", "seconds": dt2,
             "h2d_bytes_per_step": int((u0.nbytes + pos_host.nbytes) // K),
             "d2h_bytes_per_step": int((K * stats_out.nbytes + pos_out.nbytes + u_out.nbytes) // K),
-            "what": "bib_lattice_init_equilibrium from the FP64 host velocity field + bib_particles_upload, K x (bib_step "
-                    "+ per-cell area/volume/centre), final vertex positions and bib_lattice_get_velocity (FP64 velocity "
-                    "field); pinned host buffers"}
+            "what": "the loop of the reference's channel driver (rbcs_in_channel.cpp): bib_lattice_init_equilibrium "
+                    "from the FP64 host velocity field + bib_particles_upload of the vertex positions, K x (bib_step + "
+                    "bib_particles_download_async of the per-cell area/volume/centre, waited for one step later), final "
+                    "vertex positions and bib_lattice_get_velocity (FP64 velocity field); pinned host buffers",
+            "coprocessor_round_trip": rt}
         c3.close()
 
     # ---------------- CPU baseline (the oracle port) on a bounded sample

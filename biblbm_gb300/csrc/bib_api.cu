@@ -979,6 +979,7 @@ struct Batch {
     size_t membrane_smem = 0;
     int64_t ntiles = 0;
     int any_fd = 0, nx_max = 0, nz_max = 0;
+    int any_phase = 0;                  // a lattice voxelizes its particles into a phase field
     int tile_cells = 0, stages = 0, membrane_block = 256;
     int phase = 0;                      // parity of the next step relative to the tables
     std::vector<uint64_t> versions;     // lattice versions the tables were built for
@@ -1027,15 +1028,13 @@ bib_status build_batch(bib_ctx* c, Batch& B) {
     B.max_nv = 0;
     B.ntiles = 0;
     B.any_fd = 0;
+    B.any_phase = 0;
     B.nx_max = B.nz_max = 0;
     int vbase = 0;
     for (int i = 0; i < n; ++i) {
         Lattice& L = *get_lattice(c, B.handles[i]);
         bib_status st = sync_particles(c, L);
         if (st) return st;
-        if (L.phase && L.nvert)
-            return fail(c, BIB_EUNSUPPORTED, "batched steps do not voxelize membranes into a phase field (lattice %d)",
-                        B.handles[i]);
         if (L.inter.npp > 0)
             return fail(c, BIB_EUNSUPPORTED, "batched steps do not evaluate particle-particle interactions (lattice %d)",
                         B.handles[i]);
@@ -1076,6 +1075,7 @@ bib_status build_batch(bib_ctx* c, Batch& B) {
         }
         B.ntiles += cv[0].back().ntiles;
         B.any_fd |= L.d.fd_walls;
+        B.any_phase |= (L.phase && L.nvert) ? 1 : 0;
         B.nx_max = std::max(B.nx_max, L.d.nx);
         B.nz_max = std::max(B.nz_max, L.d.nz);
         for (size_t k = 0; k < L.pdev_host.size(); ++k) {
@@ -1157,16 +1157,35 @@ BatchLaunch batch_launch(bib_ctx* c, const Batch& B, int phase) {
     return bl;
 }
 
-// One coupled step of every lattice of the batch (the order of enqueue_step).
+// One coupled step of every lattice of the batch (the order of enqueue_step).  With a phase field
+// the collision needs the phase of the moved membranes: the move comes first (velocity field of
+// the current state per lattice, interpolation and move, update, voxelization per lattice of the
+// moved membranes), then collide-and-stream.  The interpolated velocity is the same either way.
 bib_status enqueue_batch_step(bib_ctx* c, Batch& B) {
     const BatchLaunch bl = batch_launch(c, B, B.phase);
     launch_membrane_batch(bl, B.membrane_block, c->stream);
     launch_spread_batch(bl, c->stream);
-    if (!launch_collide_batch(bl, c->stream))
-        return fail(c, BIB_EUNSUPPORTED, "batched collide-and-stream could not be launched (shared memory)");
-    launch_fd_walls_batch(bl, c->stream);
-    launch_interpolate_batch(bl, c->stream);
-    launch_update_batch(bl, c->stream);
+    if (B.any_phase) {
+        for (int32_t h : B.handles) {
+            Lattice& L = *get_lattice(c, h);
+            if (L.nvert) launch_velocity_field(L, c->stream);
+        }
+        launch_interpolate_batch(bl, c->stream);
+        launch_update_batch(bl, c->stream);
+        for (int32_t h : B.handles) {
+            Lattice& L = *get_lattice(c, h);
+            if (L.phase && L.nvert) launch_voxelize(L, L.pos[1 - L.pcur], c->stream);
+        }
+        if (!launch_collide_batch(bl, c->stream))
+            return fail(c, BIB_EUNSUPPORTED, "batched collide-and-stream could not be launched (shared memory)");
+        launch_fd_walls_batch(bl, c->stream);
+    } else {
+        if (!launch_collide_batch(bl, c->stream))
+            return fail(c, BIB_EUNSUPPORTED, "batched collide-and-stream could not be launched (shared memory)");
+        launch_fd_walls_batch(bl, c->stream);
+        launch_interpolate_batch(bl, c->stream);
+        launch_update_batch(bl, c->stream);
+    }
     for (int32_t h : B.handles) {
         Lattice& L = *get_lattice(c, h);
         L.cur ^= 1;

@@ -24,20 +24,23 @@ def rel(a, b):
     return np.abs(np.asarray(a) - np.asarray(b)).max() / max(np.abs(np.asarray(b)).max(), 1e-300)
 
 
-def capsule_instance(ctx, n, level, storage="f64", Ca=0.1, seed=0, fd=True):
-    """Capsule in shear (periodic x, z; FD velocity walls on y) of edge n, radius n/6."""
+def capsule_instance(ctx, n, level, storage="f64", Ca=0.1, seed=0, fd=True, lam=1.0):
+    """Capsule in shear (periodic x, z; FD velocity walls on y) of edge n, radius n/6; lam != 1: a
+    viscosity ratio, with the membranes voxelized into the phase field every step."""
     U = 0.01
     radius = n / 6.0
     wall_u = [[-U, 0, 0], [U, 0, 0], [0, 0, 0], [0, 0, 0]]
+    phase_kw = {} if lam == 1.0 else dict(use_phase=True, omega_inner=1.0 / (0.5 + lam * 0.5))
     if fd:
         lat = ctx.add_domain(n, n, n, periodic=(1, 0, 1), omega=1.0, wall_y="fd_velocity", wall_u=wall_u,
-                             storage=storage)
+                             storage=storage, **phase_kw)
         y = np.arange(n)
         u0 = np.zeros((3, n, n, n))
         u0[0] = (U * (2.0 * y / (n - 1) - 1))[None, :, None]
         lat.initialize_at_equilibrium(None, u0)
     else:
-        lat = ctx.add_domain(n, n, n, periodic=(1, 1, 1), omega=1.0, storage=storage, body_force=(1e-5, 0, 0))
+        lat = ctx.add_domain(n, n, n, periodic=(1, 1, 1), omega=1.0, storage=storage, body_force=(1e-5, 0, 0),
+                             **phase_kw)
     rest, tri = meshes.icosphere(level, radius)
     rng = np.random.default_rng(seed)
     c = 0.5 * (n - 1) + rng.uniform(-0.5, 0.5, 3)
@@ -73,6 +76,30 @@ def test_batch_equals_individual_steps(ctx, storage):
         assert rel(b["pos"], a["pos"]) < tol_p
         assert abs(b["volume"] - a["volume"]) < tol_v * a["volume"]
         assert np.abs(lg.receive() - ls.receive()).max() < tol_f
+    batch.close()
+
+
+@pytest.mark.parametrize("storage", ["f64", "f32"])
+def test_batch_with_phase_fields_equals_individual_steps(ctx, storage):
+    """Capsules with viscosity ratios 3 and 5 (GuoExternalForceVOFDynamics with the membranes
+    voxelized into the phase field after every move) and one lattice without: the batch moves
+    first, voxelizes per lattice, then collides, as a single lattice does."""
+    specs = [(32, 2, 0.1, True, 3.0), (40, 2, 0.5, False, 5.0), (32, 2, 0.1, True, 1.0)]
+    solo = [capsule_instance(ctx, n, l, storage, Ca, seed=i, fd=fd, lam=lam) for i, (n, l, Ca, fd, lam) in enumerate(specs)]
+    grouped = [capsule_instance(ctx, n, l, storage, Ca, seed=i, fd=fd, lam=lam)
+               for i, (n, l, Ca, fd, lam) in enumerate(specs)]
+    batch = bib.Batch(ctx, [g[0] for g in grouped])
+    batch.step(5)
+    batch.step(4)
+    for lat, fsi, pid in solo:
+        fsi.step(9)
+    tol_p, tol_f = (1e-13, 1e-15) if storage == "f64" else (2e-6, 2e-7)
+    for k, ((ls, fs, ps), (lg, fg, pg)) in enumerate(zip(solo, grouped)):
+        assert rel(fg.get_particle(pg)["pos"], fs.get_particle(ps)["pos"]) < tol_p
+        assert np.abs(lg.receive() - ls.receive()).max() < tol_f
+        if specs[k][4] != 1.0:
+            ph = lg.get_phase()
+            assert np.array_equal(ph, ls.get_phase()) and ph.sum() > 100  # the capsule's interior
     batch.close()
 
 
