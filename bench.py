@@ -36,10 +36,12 @@ METRIC = "MLUPS (coupled IB-LBM step) + membrane vertex-updates/s, FP16/FP32 sto
 # ratio 1.
 BYTES_PER_LU = {"f64": 19 * 8 * 2 + 2 * 3 * 8, "f32": 19 * 4 * 2 + 2 * 3 * 4, "f16": 19 * 2 * 2 + 2 * 3 * 4}
 # What the kernel moves per cell with the default (dense) reset of the previous force field:
-# the above plus that field read and rewritten with the body force (the reference's
-# computeVelocity takes the previous force, setExternalVector resets it) and the velocity
-# field's fourth (pad) component.
-KERNEL_BYTES_PER_LU = {st: b + (2 * 3 + 1) * (8 if st == "f64" else 4) for st, b in BYTES_PER_LU.items()}
+# 19 populations read and written, the spread force read, that previous field read and rewritten
+# with the body force (the reference's computeVelocity takes the previous force,
+# setExternalVector resets it) and the velocity field written as four values per cell (FP64 /
+# FP32 / FP16: FP16 storage keeps the velocity field in FP16, 8 bytes per cell).
+KERNEL_BYTES_PER_LU = {st: 19 * s * 2 + 3 * 3 * fb + 4 * ub
+                       for st, s, fb, ub in (("f64", 8, 8, 8), ("f32", 4, 4, 4), ("f16", 2, 4, 2))}
 # Steps of the precision comparison: the run lengths of the benchmark configurations
 COMPARE_STEPS = {"channel": 2000, "capsule": 2000, "rbc": 5000}
 

@@ -105,6 +105,8 @@ Lattice* get_lattice(bib_ctx* c, int32_t h) {
 
 size_t pop_bytes(int storage) { return storage == BIB_STORAGE_F64 ? 8 : (storage == BIB_STORAGE_F32 ? 4 : 2); }
 size_t force_bytes(int storage) { return storage == BIB_STORAGE_F64 ? 8 : 4; }
+// one value of the velocity field (FP16 for FP16 populations)
+size_t velocity_bytes(int storage) { return storage == BIB_STORAGE_F64 ? 8 : (storage == BIB_STORAGE_F32 ? 4 : 2); }
 
 // ---------------------------------------------------------------- shapes
 // ParticleShape constructor and compute_connectivity, src/fsi/ParticleShape.hh:21-212:
@@ -1758,7 +1760,7 @@ bib_status bib_lattice_add_domain(bib_ctx* c, int64_t nx, int64_t ny, int64_t nz
     const size_t pb = pop_bytes(p->storage) * Q * d.stride;
     const size_t fb = force_bytes(p->storage) * 3 * d.stride;
     const size_t wb = d.fd_walls ? pop_bytes(p->storage) * Q * 2 * (size_t)d.nx * d.nz : 0;
-    const size_t ub = force_bytes(p->storage) * 4 * (size_t)d.n;  // (ux, uy, uz, 0) per cell
+    const size_t ub = velocity_bytes(p->storage) * 4 * (size_t)d.n;  // (ux, uy, uz, 0) per cell
     void** bufs[6] = {&L->f[0], &L->f[1], &L->F[0], &L->F[1], &L->u, &L->wall};
     const size_t sizes[6] = {pb, pb, fb, fb, ub, wb};
     for (int k = 0; k < 6; ++k) {

@@ -202,7 +202,7 @@ struct IbView {
     IbDesc ib;
     const double* pos;   // X_n
     double* pos_next;    // X_{n+1}
-    const void* u;       // velocity field, 4 values per cell (FP64 for FP64 storage, FP32 otherwise)
+    const void* u;       // velocity field, 4 values per cell (FP64 / FP32 / FP16 as the populations)
     double* vel;
     double* force;       // vertex forces
     void* F;             // spreading target (field type as u)

@@ -308,15 +308,16 @@ __device__ __forceinline__ TileCell tile_cell(const LatticeDesc& d, int Ct, int 
 template <class T, int CPL, int COLL>
 __device__ __forceinline__ void finish_cell(const LatticeDesc& d, const CollideParams<typename Store<T>::C>& cp,
                                             T* __restrict__ fout, typename Store<T>::F* __restrict__ Fprev,
-                                            typename Store<T>::F* __restrict__ u_out, const uint8_t* __restrict__ phase,
+                                            typename Store<T>::U* __restrict__ u_out, const uint8_t* __restrict__ phase,
                                             const uint8_t* __restrict__ celltype, int64_t k, int y, bool fd,
                                             typename Store<T>::C* f, const typename Store<T>::C* F,
                                             const typename Store<T>::C* Fp) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
+    using UT = typename Store<T>::U;
     const int ctype = d.has_types ? celltype[k] : BIB_CELL_FLUID;
     if (ctype != BIB_CELL_FLUID) {  // BounceBack / NoDynamics node: no collision, zero velocity
-        if (CPL != kCplNone) store_u<FT>(u_out, k, FT(0), FT(0), FT(0));
+        if (CPL != kCplNone) store_u<UT>(u_out, k, (UT)0.0f, (UT)0.0f, (UT)0.0f);
         if (CPL == kCplDense) {
 #pragma unroll
             for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
@@ -340,7 +341,7 @@ __device__ __forceinline__ void finish_cell(const LatticeDesc& d, const CollideP
 #pragma unroll
             for (int q = 0; q < 3; ++q) u[q] = cp.wall_u[side][q];
         }
-        store_u<FT>(u_out, k, (FT)u[0], (FT)u[1], (FT)u[2]);
+        store_u<UT>(u_out, k, (UT)u[0], (UT)u[1], (UT)u[2]);
         if (CPL == kCplDense) {
 #pragma unroll
             for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
@@ -361,7 +362,7 @@ __device__ __forceinline__ void finish_cell(const LatticeDesc& d, const CollideP
 template <class T, int CPL, int COLL>
 __device__ __forceinline__ void consume_cell(const LatticeDesc& d, const StagedGeom& g, int64_t tile, const unsigned char* st,
                                              const CollideParams<typename Store<T>::C>& cp, T* __restrict__ fout,
-                                             typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
+                                             typename Store<T>::F* __restrict__ Fprev, typename Store<T>::U* __restrict__ u_out,
                                              const uint8_t* __restrict__ phase, const uint8_t* __restrict__ celltype,
                                              const TileCell& cell, uint64_t* empty_s, int lane) {
     using C = typename Store<T>::C;
@@ -417,7 +418,7 @@ __device__ __forceinline__ void consume_cell(const LatticeDesc& d, const StagedG
 template <class T, int CPL, int COLL>
 __device__ __forceinline__ void consume_tile(const LatticeDesc& d, const StagedGeom& g, int64_t tile, const unsigned char* st,
                                              const CollideParams<typename Store<T>::C>& cp, T* __restrict__ fout,
-                                             typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
+                                             typename Store<T>::F* __restrict__ Fprev, typename Store<T>::U* __restrict__ u_out,
                                              const uint8_t* __restrict__ phase, const uint8_t* __restrict__ celltype,
                                              const TileCell& cell, uint64_t* empty_s, int lane) {
     consume_cell<T, CPL, COLL>(d, g, tile, st, cp, fout, Fprev, u_out, phase, celltype, cell, empty_s, lane);
@@ -440,7 +441,7 @@ __global__ void __launch_bounds__(StageLayout<T, CPL, COLL>::THREADS, staged_cta
     k_collide_stream_staged(
     LatticeDesc d, StagedGeom g, CollideParams<typename Store<T>::C> cp, const T* __restrict__ fin,
     T* __restrict__ fout, const T* __restrict__ wall, const typename Store<T>::F* __restrict__ Fcol,
-    typename Store<T>::F* __restrict__ Fprev, typename Store<T>::F* __restrict__ u_out,
+    typename Store<T>::F* __restrict__ Fprev, typename Store<T>::U* __restrict__ u_out,
     const uint8_t* __restrict__ phase, const uint8_t* __restrict__ celltype, int* __restrict__ wait_err) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
@@ -634,7 +635,7 @@ __global__ void __launch_bounds__(StageLayout<T, kCplDense, COLL>::THREADS, stag
         const CollideView& V = *cview;
         consume_tile<T, kCplDense, COLL>(V.d, view_geom(V, NS), tile - V.tile0, stages + s * L::BYTES,
                                     *reinterpret_cast<const CollideParams<C>*>(V.cp), static_cast<T*>(V.fout),
-                                    static_cast<FT*>(V.Fprev), static_cast<FT*>(V.u), V.phase, V.celltype, cell,
+                                    static_cast<FT*>(V.Fprev), static_cast<typename Store<T>::U*>(V.u), V.phase, V.celltype, cell,
                                     &empty[s], lane);
     }
 }
@@ -745,7 +746,7 @@ bool staged_inst(const Lattice& L, int target, cudaStream_t s) {
     const FT* Fcol = (const FT*)(CPL != kCplNone ? L.F[1 - L.fe] : L.F[L.fe]);
     FT* Fprev = CPL == kCplDense ? (FT*)L.F[L.fe] : nullptr;
     kern<<<(unsigned)grid, LY::THREADS, smem, s>>>(d, g, collide_params<C>(d, L.storage), fin, fout,
-                                                       (const T*)L.wall, Fcol, Fprev, CPL != kCplNone ? (FT*)L.u : nullptr,
+                                                       (const T*)L.wall, Fcol, Fprev, CPL != kCplNone ? (typename Store<T>::U*)L.u : nullptr,
                                                        L.phase, L.celltype, L.wait_err);
     return true;
 }

@@ -35,6 +35,7 @@ template <>
 struct Store<double> {
     using C = double;
     using F = double;
+    using U = double;  // velocity field
     static __device__ __forceinline__ double load(const double* p, float) { return __ldg(p); }
     static __device__ __forceinline__ void store(double* p, double v, float) { *p = v; }
 };
@@ -42,6 +43,7 @@ template <>
 struct Store<float> {
     using C = float;
     using F = float;
+    using U = float;
     static __device__ __forceinline__ float load(const float* p, float) { return __ldg(p); }
     static __device__ __forceinline__ void store(float* p, float v, float) { *p = v; }
 };
@@ -49,6 +51,7 @@ template <>
 struct Store<__half> {
     using C = float;
     using F = float;
+    using U = __half;  // the velocity field in FP16 too: it only feeds the interpolation
     static __device__ __forceinline__ float load(const __half* p, float inv_scale) {
         return __half2float(__ldg(p)) * inv_scale;
     }

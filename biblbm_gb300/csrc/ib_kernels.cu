@@ -152,6 +152,20 @@ __device__ __forceinline__ U3<double> load_u(const double* u, int64_t k) {
     const double2 a = __ldg(q), b = __ldg(q + 1);
     return U3<double>{a.x, a.y, b.x};
 }
+__device__ __forceinline__ U3<float> load_u(const __half* u, int64_t k) {  // FP16 population storage
+    const uint2 v = __ldg(reinterpret_cast<const uint2*>(u) + k);
+    const float2 ab = __half22float2(*reinterpret_cast<const __half2*>(&v.x));
+    return U3<float>{ab.x, ab.y, __low2float(*reinterpret_cast<const __half2*>(&v.y))};
+}
+// Compute type of an interpolation from the velocity field's storage type.
+template <class UT>
+struct InterpC {
+    using type = float;
+};
+template <>
+struct InterpC<double> {
+    using type = double;
+};
 
 // ---------------------------------------------------------------- pipe boundary
 // PipeBoundary::distance_to_boundary (fsi/Boundary.h:158-161) minus the kernel's half support:
@@ -264,7 +278,7 @@ __device__ __forceinline__ void pipe_move(const IbDesc& ib, const double* old, c
 // is the interpolation of j/rho + Fold/2, the reference's computeVelocity field.
 template <class UT, int S, bool FOLD = false>
 __device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) {
-    using C = UT;
+    using C = typename InterpC<UT>::type;  // also the force field's type
     static_assert(S == 3 || S == 4, "Roma (3) or Peskin (4) support");
     const LatticeDesc& d = V.d;
     const IbDesc& ib = V.ib;
@@ -295,7 +309,7 @@ __device__ __forceinline__ void interpolate_move_vertex(const IbView& V, int v) 
         }
         C acc[3] = {C(0), C(0), C(0)};
         C facc[3] = {C(0), C(0), C(0)};
-        const UT* __restrict__ Fo = static_cast<const UT*>(V.Fold);
+        const C* __restrict__ Fo = static_cast<const C*>(V.Fold);
         const C body[3] = {(C)d.body[0], (C)d.body[1], (C)d.body[2]};
 #pragma unroll
         for (int a = 0; a < s; ++a) {
@@ -1529,9 +1543,12 @@ void interpolate_any(int storage, int dirac, const IbView& v1, const IbView* vie
     if (storage == BIB_STORAGE_F64) {
         if (peskin) k_interpolate_move<double, 4, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
         else k_interpolate_move<double, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
-    } else {
+    } else if (storage == BIB_STORAGE_F32) {
         if (peskin) k_interpolate_move<float, 4, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
         else k_interpolate_move<float, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+    } else {
+        if (peskin) k_interpolate_move<__half, 4, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+        else k_interpolate_move<__half, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
     }
 }
 
@@ -1574,8 +1591,14 @@ void launch_interpolate_move(const Lattice& L, cudaStream_t s, int fold) {
     IbView v = single_view(L, -1);
     v.Fold = L.F[fold];
     const unsigned g = (L.nvert + 127) / 128;
-    if (L.ib.dirac == BIB_DIRAC_PESKIN) k_interpolate_move<float, 4, false, true><<<g, 128, 0, s>>>(v, nullptr, nullptr, L.nvert);
-    else k_interpolate_move<float, 3, false, true><<<g, 128, 0, s>>>(v, nullptr, nullptr, L.nvert);
+    const bool peskin = L.ib.dirac == BIB_DIRAC_PESKIN;
+    if (L.storage == BIB_STORAGE_F32) {
+        if (peskin) k_interpolate_move<float, 4, false, true><<<g, 128, 0, s>>>(v, nullptr, nullptr, L.nvert);
+        else k_interpolate_move<float, 3, false, true><<<g, 128, 0, s>>>(v, nullptr, nullptr, L.nvert);
+    } else {
+        if (peskin) k_interpolate_move<__half, 4, false, true><<<g, 128, 0, s>>>(v, nullptr, nullptr, L.nvert);
+        else k_interpolate_move<__half, 3, false, true><<<g, 128, 0, s>>>(v, nullptr, nullptr, L.nvert);
+    }
 }
 
 void launch_force_clear(const Lattice& L, int fbuf, cudaStream_t s) {

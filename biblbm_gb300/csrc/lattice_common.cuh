@@ -35,7 +35,8 @@ __device__ __forceinline__ C moving_wall_term(const LatticeDesc& d, int i, int f
 
 
 // The velocity field is stored as four values per cell (ux, uy, uz, 0): one aligned vector
-// access per cell for the interpolation's 27 / 64-node gathers.
+// access per cell for the interpolation's 27 / 64-node gathers (FP64, FP32, or FP16 for FP16
+// population storage).
 template <class FT>
 __device__ __forceinline__ void store_u(FT* u, int64_t k, FT a, FT b, FT c);
 template <>
@@ -47,6 +48,12 @@ __device__ __forceinline__ void store_u<double>(double* u, int64_t k, double a, 
     double2* q = reinterpret_cast<double2*>(u) + 2 * k;
     q[0] = make_double2(a, b);
     q[1] = make_double2(c, 0.0);
+}
+// FP16 storage: four halves (8 bytes) per cell
+template <>
+__device__ __forceinline__ void store_u<__half>(__half* u, int64_t k, __half a, __half b, __half c) {
+    const __half2 ab = __halves2half2(a, b), c0 = __halves2half2(c, __ushort_as_half(0));
+    reinterpret_cast<uint2*>(u)[k] = make_uint2(*reinterpret_cast<const unsigned*>(&ab), *reinterpret_cast<const unsigned*>(&c0));
 }
 
 // BounceBack::collide (core/dynamics.hh:763-770): each population swaps with its opposite.

@@ -56,11 +56,12 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
                                                          const T* __restrict__ wall,
                                                          const typename Store<T>::F* __restrict__ Fcol,
                                                          typename Store<T>::F* __restrict__ Fprev,
-                                                         typename Store<T>::F* __restrict__ u_out,
+                                                         typename Store<T>::U* __restrict__ u_out,
                                                          const uint8_t* __restrict__ phase,
                                                          const uint8_t* __restrict__ celltype, int coll) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
+    using UT = typename Store<T>::U;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= d.nx) return;
@@ -70,7 +71,7 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
     const int ctype = d.has_types ? celltype[k] : BIB_CELL_FLUID;
     if (ctype != BIB_CELL_FLUID) {  // BounceBack / NoDynamics node: no collision, zero velocity
         if (COUPLED) {
-            store_u<FT>(u_out, k, FT(0), FT(0), FT(0));
+            store_u<UT>(u_out, k, (UT)0.0f, (UT)0.0f, (UT)0.0f);
             if (Fprev)
                 for (int c = 0; c < 3; ++c) Fprev[c * d.stride + k] = (FT)d.body[c];
         }
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
             }
             velocity_with_force(f, Fp, u);
         }
-        store_u<FT>(u_out, k, (FT)u[0], (FT)u[1], (FT)u[2]);
+        store_u<UT>(u_out, k, (UT)u[0], (UT)u[1], (UT)u[2]);
         if (Fprev) {
             Fprev[k] = (FT)d.body[0];
             Fprev[d.stride + k] = (FT)d.body[1];
@@ -135,11 +136,12 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
                                                               const T* __restrict__ wall,
                                                               const typename Store<T>::F* __restrict__ Fcol,
                                                               typename Store<T>::F* __restrict__ Fprev,
-                                                              typename Store<T>::F* __restrict__ u_out,
+                                                              typename Store<T>::U* __restrict__ u_out,
                                                               const uint8_t* __restrict__ phase,
                                                               const uint8_t* __restrict__ celltype, int coll) {
     using C = typename Store<T>::C;
     using FT = typename Store<T>::F;
+    using UT = typename Store<T>::U;
     const unsigned FULL = 0xffffffffu;
     const int lane = threadIdx.x & 31;
     // grid.x runs over blocks of rows (ny * nz can exceed the 65535 limit of grid.y)
@@ -254,8 +256,8 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
         }
         if (ct0 != BIB_CELL_FLUID) u0[0] = u0[1] = u0[2] = C(0);
         if (ct1 != BIB_CELL_FLUID) u1[0] = u1[1] = u1[2] = C(0);
-        store_u<FT>(u_out, k0, (FT)u0[0], (FT)u0[1], (FT)u0[2]);
-        store_u<FT>(u_out, k0 + 1, (FT)u1[0], (FT)u1[1], (FT)u1[2]);
+        store_u<UT>(u_out, k0, (UT)u0[0], (UT)u0[1], (UT)u0[2]);
+        store_u<UT>(u_out, k0 + 1, (UT)u1[0], (UT)u1[1], (UT)u1[2]);
         if (Fprev)
             for (int c = 0; c < 3; ++c) store2<FT>(Fprev + c * d.stride + k0, (FT)d.body[c], (FT)d.body[c]);
     }
@@ -447,7 +449,7 @@ __global__ void k_velocity(LatticeDesc d, const T* __restrict__ f, const T* __re
         velocity_with_force(fc, Fc, uc);
     }
     for (int a = 0; a < 3; ++a) u[a * cstride + k * kstride] = (OT)uc[a];
-    if (kstride == 4) u[k * 4 + 3] = OT(0);
+    if (kstride == 4) u[k * 4 + 3] = OT(0.0f);
 }
 
 // iniCellAtEquilibrium, src/core/cell.hh:124-132
@@ -603,7 +605,7 @@ void collide_stream_t(const Lattice& L, Coupling mode, cudaStream_t s) {
         T* fout = (T*)L.f[1 - L.cur];
         if (coupled)
             k_collide_stream_rows<T, true><<<grid, block, 0, s>>>(L.d, fin, fout, (const T*)L.wall, (const FT*)L.F[1 - L.fe],
-                                                                  Fprev, (FT*)L.u, L.phase, L.celltype, L.d.collision);
+                                                                  Fprev, (typename Store<T>::U*)L.u, L.phase, L.celltype, L.d.collision);
         else
             k_collide_stream_rows<T, false><<<grid, block, 0, s>>>(L.d, fin, fout, (const T*)L.wall, (const FT*)L.F[L.fe],
                                                                    nullptr, nullptr, L.phase, L.celltype, L.d.collision);
@@ -615,7 +617,7 @@ void collide_stream_t(const Lattice& L, Coupling mode, cudaStream_t s) {
     const T* wall = (const T*)L.wall;
     if (coupled) {
         k_collide_stream<T, true><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, fin, fout, wall, (const FT*)L.F[1 - L.fe],
-                                                                    Fprev, (FT*)L.u, L.phase, L.celltype, L.d.collision);
+                                                                    Fprev, (typename Store<T>::U*)L.u, L.phase, L.celltype, L.d.collision);
     } else {
         k_collide_stream<T, false><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, fin, fout, wall, (const FT*)L.F[L.fe], nullptr,
                                                                      nullptr, L.phase, L.celltype, L.d.collision);
@@ -647,9 +649,10 @@ void fd_walls_t(const Lattice& L, int buf, int fbuf, cudaStream_t s) {
 template <class T>
 void velocity_field_t(const Lattice& L, cudaStream_t s) {
     using FT = typename Store<T>::F;
+    using UT = typename Store<T>::U;
     const int bx = row_block(L.d);
-    k_velocity<T, FT><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall, (const FT*)L.F[L.fe],
-                                                        (FT*)L.u, 1, 4, L.celltype);
+    k_velocity<T, UT><<<row_grid(L.d, bx), bx, 0, s>>>(L.d, (const T*)L.f[L.cur], (const T*)L.wall, (const FT*)L.F[L.fe],
+                                                        (UT*)L.u, 1, 4, L.celltype);
 }
 
 template <class T>

@@ -35,9 +35,11 @@ TOL = {
     # 5.4e-8 / 8.3e-8 / 2.4e-6 / 7.4e-8: the FP32 round-off forces move vertices by F/2 per step)
     "channel": {"f64": (1e-12, 2e-13, 5e-11, 1e-11), "f32": (3e-7, 5e-7, 1.5e-5, 5e-7),
                 "f16": (3e-7, 5e-7, 1.5e-5, 5e-7)},
-    # the same cells inflated by 2 %, 2 steps
+    # the same cells inflated by 2 %, 2 steps (f16 positions measured 1.1e-5: FP16 storage keeps the
+    # velocity field in FP16 too, 11 significant bits, so a vertex moving at u ~ 0.01 is off by up to
+    # ~5e-6 per step)
     "channel_prestrained": {"f64": (1e-12, 1e-12, 1e-10, 1e-11), "f32": (1e-5, 1e-5, 1e-3, 1e-5),
-                            "f16": (1e-5, 1e-5, 1e-3, 1e-5)},
+                            "f16": (1e-5, 5e-5, 1e-3, 1e-5)},
     # capsule in shear, 20 steps (measured f64 5.5e-18 / 7.1e-15 / 1.2e-12 rel. / 3.1e-15; f32 9.1e-10
     # / 2.4e-8 / 1.7e-4 rel. / 2.9e-8; f16 7.5e-7 / 6.9e-6 / 6.4e-4 rel. / 3.9e-7)
     "capsule": {"f64": (1e-16, 5e-14, 1e-10, 2e-14), "f32": (5e-9, 1.5e-7, 1e-3, 1.5e-7),
