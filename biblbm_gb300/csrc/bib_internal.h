@@ -216,6 +216,7 @@ struct IbView {
     // velocity field j / rho + body / 2 that the collision wrote.  Null: not used.
     int4* spread_lo = nullptr;
     const void* Fold = nullptr;
+    const int* order = nullptr;  // single lattices: the vertex each interpolation thread takes
 };
 
 // Per-launch constants of the collision in the compute type C.
@@ -251,6 +252,7 @@ struct CollideView {
 struct ShapeHost {
     std::vector<double> rest, tri_area, link_len, pair_cs;
     std::vector<int> tri, tri4, links, pairs, inc_off, inc;
+    std::vector<int> order;  // vertices in a spatially clustered order (Morton order of the rest shape)
     std::vector<float> tri_rest_f, tri_area_f, pair_cs_f;
     double area = 0, volume = 0;
     std::string tag;  // ParticleShape tag (ParticleShape.h:64), the shape's name in text output
@@ -312,6 +314,7 @@ struct Lattice {
     ParticleDev* pdev = nullptr;
     std::vector<ParticleDev> pdev_host;  // host copy of pdev (batch tables are built from it)
     int* vert_particle = nullptr;         // global vertex -> particle
+    int* visit_order = nullptr;          // the interpolation's visiting order of the vertices
     Interactions inter;                   // wall and particle-particle interactions
     PairGrid pgrid;                       // pair search of the particle-particle interactions
     RefGridBuffers rgrid;                 // ... when they use the reference's collision grid

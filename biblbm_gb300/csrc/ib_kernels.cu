@@ -365,7 +365,7 @@ __global__ void __launch_bounds__(128) k_interpolate_move(IbView v1, const IbVie
     const int g = blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= nvert) return;
     const IbView& V = BATCH ? views[vinst[g]] : v1;
-    interpolate_move_vertex<UT, S, FOLD>(V, BATCH ? g - V.vbase : g);
+    interpolate_move_vertex<UT, S, FOLD>(V, BATCH ? g - V.vbase : (V.order ? V.order[g] : g));
 }
 
 // Sparse force reset: F := body force at the support nodes the last spreading into F recorded
@@ -1530,6 +1530,7 @@ IbView single_view(const Lattice& L, int fbuf) {
     v.vbase = 0;
     v.nvert = L.nvert;
     v.inter = L.inter;
+    v.order = L.visit_order;
     return v;
 }
 
