@@ -342,7 +342,7 @@ static int run_pipe_guo(const Bundle& in, const char* out) {
 // ---------------------------------------------------------------------------
 // Particles
 
-// Composite membrane used by the spec RBC configurations: the capsule's
+// Composite membrane used by the benchmark's RBC configurations: the capsule's
 // Skalak in-plane law (DeformableCapsule.hh:68-150) plus the RBC model's global /
 // local area, volume and dihedral-bending terms (RBCParticle.hh:175-246).  The RBC
 // part is evaluated by a genuine RBCParticle with zero shear modulus, whose WLC-POW
