@@ -407,6 +407,7 @@ void free_particles(Lattice& L) {
     }
     cudaFree(L.rgrid.start);
     cudaFree(L.rgrid.end);
+    cudaFree(L.rgrid.posf);
     cudaFree(L.rgrid.temp);
     L.rgrid = RefGridBuffers{};
     cudaFree(L.vox_count);
@@ -534,6 +535,7 @@ bib_status sync_particles(bib_ctx* c, Lattice& L) {
             BIB_ALLOC(c, (void**)&R.ids[k], L.nvert * sizeof(uint32_t));
         }
         BIB_CUDA(c, cudaMemset(R.keys[1], 0, L.nvert * sizeof(uint32_t)));
+        BIB_ALLOC(c, (void**)&R.posf, L.nvert * sizeof(float4));
         BIB_ALLOC(c, (void**)&R.start, ((size_t)g.ncell + 1) * sizeof(int));
         BIB_ALLOC(c, (void**)&R.end, ((size_t)g.ncell + 1) * sizeof(int));
         BIB_CUDA(c, cudaMemset(R.start, 0, ((size_t)g.ncell + 1) * sizeof(int)));
@@ -3398,6 +3400,7 @@ bib_status bib_grow_particles(bib_ctx* c, const bib_growth* g, int32_t n, const 
                     B.get(c, (void**)&R.keys[1], nvert * sizeof(uint32_t)) &&
                     B.get(c, (void**)&R.ids[0], nvert * sizeof(uint32_t)) &&
                     B.get(c, (void**)&R.ids[1], nvert * sizeof(uint32_t)) &&
+                    B.get(c, (void**)&R.posf, nvert * sizeof(float4)) &&
                     B.get(c, (void**)&R.start, ((size_t)grid.ncell + 1) * sizeof(int)) &&
                     B.get(c, (void**)&R.end, ((size_t)grid.ncell + 1) * sizeof(int)) && B.get(c, &R.temp, R.temp_bytes);
     if (!ok) return fail(c, BIB_ENOMEM, "device allocation for the growth stage failed");
@@ -3445,18 +3448,52 @@ bib_status bib_grow_particles(bib_ctx* c, const bib_growth* g, int32_t n, const 
     }
     const PotentialDev pot{BIB_POTENTIAL_SPRING, g->min_dist, 0.0, g->strength};
     const double wall[3] = {g->wall[0], g->wall[1], g->wall[2]};
-    double scale = g->initial_scale;
-    launch_rigid_nodes(G, scale, st);
-    for (int64_t it = 0; it < g->it_end; ++it) {
-        if (it % g->rescale_every == 0) {
-            const double fraction = (double)it / (double)g->n_it;
-            scale = g->initial_scale + (1. - g->initial_scale) * fraction;
-            launch_rigid_nodes(G, scale, st);
-        }
-        launch_ref_grid_forces(grid, R, pot, d_pos, d_owner, d_force, true, g->has_wall ? wall : nullptr, st);
-        launch_rigid_move(G, scale, st);
-        if ((it & 1023) == 1023) BIB_CHECK_LAUNCH(c);
+    // the scales of the rescale iterations (create_particles.h:132-147), in the driver's arithmetic
+    std::vector<double> scales((size_t)(g->it_end > 0 ? (g->it_end - 1) / g->rescale_every + 1 : 1));
+    for (size_t r = 0; r < scales.size(); ++r) {
+        const double fraction = (double)((int64_t)r * g->rescale_every) / (double)g->n_it;
+        scales[r] = g->initial_scale + (1. - g->initial_scale) * fraction;
     }
+    double* d_scales;
+    long long* d_it;
+    double* d_scale_now;
+    if (!B.get(c, (void**)&d_scales, scales.size() * sizeof(double)) || !B.get(c, (void**)&d_it, sizeof(long long)) ||
+        !B.get(c, (void**)&d_scale_now, sizeof(double)))
+        return fail(c, BIB_ENOMEM, "device allocation for the growth stage failed");
+    const long long zero = 0;
+    BIB_CUDA(c, cudaMemcpyAsync(d_scales, scales.data(), scales.size() * sizeof(double), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_it, &zero, sizeof(long long), cudaMemcpyHostToDevice, st));
+    BIB_CUDA(c, cudaMemcpyAsync(d_scale_now, &g->initial_scale, sizeof(double), cudaMemcpyHostToDevice, st));
+    G.it = d_it;
+    G.scales = d_scales;
+    G.every = g->rescale_every;
+    G.scale_now = d_scale_now;
+    launch_rigid_nodes(G, g->initial_scale, st);
+    auto iteration = [&]() {
+        launch_rigid_rescale(G, st);
+        launch_ref_grid_forces(grid, R, pot, d_pos, d_owner, d_force, true, g->has_wall ? wall : nullptr, st);
+        launch_rigid_move(G, st);
+    };
+    // a block of iterations captured once and replayed: the schedule lives in device memory
+    constexpr int kBlock = 16;
+    int64_t done = 0;
+    if (g->it_end >= 2 * kBlock) {
+        BIB_CUDA(c, cudaStreamSynchronize(st));
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        BIB_CUDA(c, cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+        for (int k = 0; k < kBlock; ++k) iteration();
+        const cudaError_t ec = cudaStreamEndCapture(st, &graph);
+        if (ec != cudaSuccess) return fail(c, BIB_ECUDA, "growth graph capture failed: %s", cudaGetErrorString(ec));
+        const cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) return fail(c, BIB_ECUDA, "growth graph: %s", cudaGetErrorString(ei));
+        cudaError_t el = cudaSuccess;
+        for (; done + kBlock <= g->it_end && el == cudaSuccess; done += kBlock) el = cudaGraphLaunch(exec, st);
+        cudaGraphExecDestroy(exec);
+        if (el != cudaSuccess) return fail(c, BIB_ECUDA, "growth graph launch: %s", cudaGetErrorString(el));
+    }
+    for (; done < g->it_end; ++done) iteration();
     BIB_CHECK_LAUNCH(c);
     BIB_CUDA(c, cudaMemcpyAsync(state.data(), d_state, 7 * np * sizeof(double), cudaMemcpyDeviceToHost, st));
     if (pos_out) BIB_CUDA(c, cudaMemcpyAsync(pos_out, d_pos, 3 * nvert * sizeof(double), cudaMemcpyDeviceToHost, st));

@@ -155,6 +155,7 @@ struct RefGridBuffers {
     uint32_t* ids[2] = {nullptr, nullptr};
     int* start = nullptr;  // ncell + 1 entries each, zero between uses
     int* end = nullptr;
+    float4* posf = nullptr;  // the vertex positions rounded to FP32 (the pair pre-test)
     void* temp = nullptr;
     size_t temp_bytes = 0;
     int bits = 0;
@@ -188,11 +189,16 @@ struct GrowthView {
     const double* force = nullptr;
     double* torque = nullptr;  // 3 per vertex, scratch
     double density = 1.0, damping = 0.0;
+    long long* it = nullptr;          // the iteration counter
+    const double* scales = nullptr;   // the scale of iteration k * every
+    long long every = 1;
+    double* scale_now = nullptr;      // the current scale
     int per[3] = {0, 0, 0};
     double x0[3] = {0, 0, 0}, L[3] = {1, 1, 1}, Linv[3] = {1, 1, 1};
 };
 void launch_rigid_nodes(const GrowthView& G, double scale, cudaStream_t s);
-void launch_rigid_move(const GrowthView& G, double scale, cudaStream_t s);
+void launch_rigid_rescale(const GrowthView& G, cudaStream_t s);  // at the iteration *G.it
+void launch_rigid_move(const GrowthView& G, cudaStream_t s);     // advances *G.it
 
 // What the immersed-boundary kernels need of one lattice for one step (buffer parities
 // resolved).  A single lattice passes one view by value; a batch passes a device table of

@@ -20,6 +20,7 @@
 #include <cub/device/device_radix_sort.cuh>
 
 #include <cfloat>
+#include <cmath>
 
 #include "bib_internal.h"
 
@@ -48,6 +49,12 @@ struct GridArgs {
     RefGrid g;
     PotentialDev pot;
     double c2;  // cutoff squared
+    // FP32 pre-test: a pair whose FP32 distance (positions rounded to FP32, the minimum image taken
+    // in FP32) exceeds sqrt(pre_c2) is beyond the cutoff for certain (the margin covers the
+    // rounding), so the exact FP64 test, which alone decides, is skipped.  pre_c2 <= 0: off.
+    float pre_c2;
+    float Lf[3], Linvf[3];
+    const float4* posf;
     const double* pos;
     const int* owner;
     const uint32_t* keys;  // sorted cell keys
@@ -65,8 +72,16 @@ __device__ __forceinline__ double grid_diff(const RefGrid& g, int a, double x, d
 
 // handle_collision(node, node2) (CollisionForces.h:187-199) seen from one of its vertices:
 // `first` when the vertex is `node` (force += df), else it is `node2` (force -= df).
-__device__ __forceinline__ void grid_event(const GridArgs& A, int a, const double* xa, int b, bool first, double* f) {
+__device__ __forceinline__ void grid_event(const GridArgs& A, int a, const double* xa, const float4& xaf, int b,
+                                           bool first, double* f) {
     if (A.owner[a] == A.owner[b]) return;
+    if (A.pre_c2 > 0.0f) {
+        const float4 q = A.posf[b];
+        float e[3] = {q.x - xaf.x, q.y - xaf.y, q.z - xaf.z};
+        for (int d = 0; d < 3; ++d)
+            if (A.g.per[d]) e[d] -= A.Lf[d] * rintf(e[d] * A.Linvf[d]);
+        if (e[0] * e[0] + e[1] * e[1] + e[2] * e[2] > A.pre_c2) return;
+    }
     const double* xb = A.pos + 3LL * b;
     double dr[3];
     for (int d = 0; d < 3; ++d) dr[d] = first ? grid_diff(A.g, d, xb[d], xa[d]) : grid_diff(A.g, d, xa[d], xb[d]);
@@ -80,30 +95,33 @@ __device__ __forceinline__ void grid_event(const GridArgs& A, int a, const doubl
 __device__ __forceinline__ int grid_cell(const RefGrid& g, int i, int j, int k) { return k + g.nc[2] * (j + g.nc[1] * i); }
 
 // collide_all_in_cells(c1, c2) (CollisionForces.h:178-184): the events of the vertex at slot s
-__device__ void grid_all_in_cells(const GridArgs& A, int c1, int c2, int c, int s, int a, const double* xa, double* f) {
+__device__ void grid_all_in_cells(const GridArgs& A, int c1, int c2, int c, int s, int a, const double* xa,
+                                  const float4& xaf, double* f) {
     if (c1 == c2) {
         for (int l = A.start[c1]; l < A.end[c1]; ++l) {
             if (l == s) {
                 for (int m = A.start[c2]; m < A.end[c2]; ++m)
-                    if (m != s) grid_event(A, a, xa, (int)A.ids[m], true, f);
+                    if (m != s) grid_event(A, a, xa, xaf, (int)A.ids[m], true, f);
             } else {
-                grid_event(A, a, xa, (int)A.ids[l], false, f);
+                grid_event(A, a, xa, xaf, (int)A.ids[l], false, f);
             }
         }
     } else if (c == c1) {
-        for (int m = A.start[c2]; m < A.end[c2]; ++m) grid_event(A, a, xa, (int)A.ids[m], true, f);
+        for (int m = A.start[c2]; m < A.end[c2]; ++m) grid_event(A, a, xa, xaf, (int)A.ids[m], true, f);
     } else if (c == c2) {
-        for (int l = A.start[c1]; l < A.end[c1]; ++l) grid_event(A, a, xa, (int)A.ids[l], false, f);
+        for (int l = A.start[c1]; l < A.end[c1]; ++l) grid_event(A, a, xa, xaf, (int)A.ids[l], false, f);
     }
 }
 
 // Key of a vertex: its cell (Grid::insert, Grid.hh:74-82) when it lies strictly inside the box
 // enlarged by the cutoff (geo::Rect::contains), else the sentinel ncell.
 __global__ void __launch_bounds__(128) k_grid_keys(RefGrid g, int nvert, const double* __restrict__ pos,
-                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ ids) {
+                                                    uint32_t* __restrict__ keys, uint32_t* __restrict__ ids,
+                                                    float4* __restrict__ posf) {
     const int v = blockIdx.x * blockDim.x + threadIdx.x;
     if (v >= nvert) return;
     const double* x = pos + 3LL * v;
+    posf[v] = make_float4((float)x[0], (float)x[1], (float)x[2], 0.0f);
     uint32_t key = (uint32_t)g.ncell;
     bool in = true;
     int ci[3];
@@ -156,6 +174,7 @@ __global__ void __launch_bounds__(128) k_grid_forces(GridArgs A, double wy0, dou
     }
     const RefGrid& g = A.g;
     const double xa[3] = {A.pos[3LL * a], A.pos[3LL * a + 1], A.pos[3LL * a + 2]};
+    const float4 xaf = A.posf[a];
     const int k = c % g.nc[2], j = (c / g.nc[2]) % g.nc[1], i = c / (g.nc[2] * g.nc[1]);
     const int x0 = 1, x1 = g.nc[0] - 2, y0 = 1, y1 = g.nc[1] - 2, z0 = 1, z1 = g.nc[2] - 2;
     auto bulk = [&](int p, int q, int r) { return p >= x0 && p <= x1 && q >= y0 && q <= y1 && r >= z0 && r <= z1; };
@@ -165,28 +184,28 @@ __global__ void __launch_bounds__(128) k_grid_forces(GridArgs A, double wy0, dou
         const int p = i - pre[n][0], q = j - pre[n][1], r = k - pre[n][2];
         if (!bulk(p, q, r)) continue;
         const int cp = grid_cell(g, p, q, r);
-        for (int l = A.start[cp]; l < A.end[cp]; ++l) grid_event(A, a, xa, (int)A.ids[l], false, f);
+        for (int l = A.start[cp]; l < A.end[cp]; ++l) grid_event(A, a, xa, xaf, (int)A.ids[l], false, f);
     }
     if (bulk(i, j, k)) {
-        for (int l = A.start[c]; l < s; ++l) grid_event(A, a, xa, (int)A.ids[l], false, f);
-        for (int m = s + 1; m < A.end[c]; ++m) grid_event(A, a, xa, (int)A.ids[m], true, f);
+        for (int l = A.start[c]; l < s; ++l) grid_event(A, a, xa, xaf, (int)A.ids[l], false, f);
+        for (int m = s + 1; m < A.end[c]; ++m) grid_event(A, a, xa, xaf, (int)A.ids[m], true, f);
         const int nb[7][3] = {{0, 1, 0}, {0, 1, 1}, {0, 0, 1}, {1, 0, 0}, {1, 1, 0}, {1, 1, 1}, {1, 0, 1}};
         for (int n = 0; n < 7; ++n) {
             const int cn = grid_cell(g, i + nb[n][0], j + nb[n][1], k + nb[n][2]);
-            for (int m = A.start[cn]; m < A.end[cn]; ++m) grid_event(A, a, xa, (int)A.ids[m], true, f);
+            for (int m = A.start[cn]; m < A.end[cn]; ++m) grid_event(A, a, xa, xaf, (int)A.ids[m], true, f);
         }
         // the first and last bulk layers of periodic axes (CollisionForces.h:119-163)
-        if (g.per[0] && (i == x0 || i == x1)) grid_all_in_cells(A, grid_cell(g, x0, j, k), grid_cell(g, x1, j, k), c, s, a, xa, f);
-        if (g.per[1] && (j == y0 || j == y1)) grid_all_in_cells(A, grid_cell(g, i, y0, k), grid_cell(g, i, y1, k), c, s, a, xa, f);
-        if (g.per[2] && (k == z0 || k == z1)) grid_all_in_cells(A, grid_cell(g, i, j, z0), grid_cell(g, i, j, z1), c, s, a, xa, f);
+        if (g.per[0] && (i == x0 || i == x1)) grid_all_in_cells(A, grid_cell(g, x0, j, k), grid_cell(g, x1, j, k), c, s, a, xa, xaf, f);
+        if (g.per[1] && (j == y0 || j == y1)) grid_all_in_cells(A, grid_cell(g, i, y0, k), grid_cell(g, i, y1, k), c, s, a, xa, xaf, f);
+        if (g.per[2] && (k == z0 || k == z1)) grid_all_in_cells(A, grid_cell(g, i, j, z0), grid_cell(g, i, j, z1), c, s, a, xa, xaf, f);
         if (g.per[0] && g.per[1] && ((i == x0 && j == y0) || (i == x1 && j == y1)))
-            grid_all_in_cells(A, grid_cell(g, x0, y0, k), grid_cell(g, x1, y1, k), c, s, a, xa, f);
+            grid_all_in_cells(A, grid_cell(g, x0, y0, k), grid_cell(g, x1, y1, k), c, s, a, xa, xaf, f);
         if (g.per[0] && g.per[2] && ((i == x0 && k == z0) || (i == x1 && k == z1)))
-            grid_all_in_cells(A, grid_cell(g, x0, j, z0), grid_cell(g, x1, j, z1), c, s, a, xa, f);
+            grid_all_in_cells(A, grid_cell(g, x0, j, z0), grid_cell(g, x1, j, z1), c, s, a, xa, xaf, f);
         if (g.per[1] && g.per[2] && ((j == y0 && k == z0) || (j == y1 && k == z1)))
-            grid_all_in_cells(A, grid_cell(g, i, y0, z0), grid_cell(g, i, y1, z1), c, s, a, xa, f);
+            grid_all_in_cells(A, grid_cell(g, i, y0, z0), grid_cell(g, i, y1, z1), c, s, a, xa, xaf, f);
         if (g.per[0] && g.per[1] && g.per[2] && ((i == x0 && j == y0 && k == z0) || (i == x1 && j == y1 && k == z1)))
-            grid_all_in_cells(A, grid_cell(g, x0, y0, z0), grid_cell(g, x1, y1, z1), c, s, a, xa, f);
+            grid_all_in_cells(A, grid_cell(g, x0, y0, z0), grid_cell(g, x1, y1, z1), c, s, a, xa, xaf, f);
         if (wr > 0) {
             // PipeBoundary::does_intersect(cell rect, cutoff) (Boundary.h:227-243), the rect of
             // Grid::repartition (Grid.hh:46-58)
@@ -262,10 +281,25 @@ __global__ void __launch_bounds__(256) k_rigid_nodes(GrowthView G, double scale)
     rigid_vertices(G, p, G.com + 3LL * p, R, scale, nullptr);
 }
 
+// The rescale of create_particles.h:132-147 at iterations it = 0, every, 2 every, ...: the
+// iteration counter and the table of scales are in device memory, so a captured sequence of
+// iterations replays unchanged.
+__global__ void __launch_bounds__(256) k_rigid_rescale(GrowthView G) {
+    const long long it = *G.it;
+    if (it % G.every != 0) return;
+    const double scale = G.scales[it / G.every];
+    if (blockIdx.x == 0 && threadIdx.x == 0) *G.scale_now = scale;
+    const int p = blockIdx.x;
+    double R[9];
+    quat_matrix(G.quat + 4LL * p, R);
+    rigid_vertices(G, p, G.com + 3LL * p, R, scale, nullptr);
+}
+
 // RigidParticle3D::move_vertices (RigidParticle.hh:55-101) and the periodic remap of the
 // centre of mass (ParticleBase.hh:111-136).
-__global__ void __launch_bounds__(128) k_rigid_move(GrowthView G, double scale) {
+__global__ void __launch_bounds__(128) k_rigid_move(GrowthView G) {
     const int p = blockIdx.x;
+    const double scale = *G.scale_now;
     __shared__ double sh[3 + 9 + 3];  // com before the remap, R, shift
     __shared__ double sums[6];        // force, torque
     const int s = G.shape[p];
@@ -371,6 +405,7 @@ __global__ void __launch_bounds__(128) k_rigid_move(GrowthView G, double scale) 
     }
     __syncthreads();
     rigid_vertices(G, p, sh, sh + 3, scale, sh + 12);
+    if (p == 0 && threadIdx.x == 0) *G.it += 1;  // no other block reads the counter
 }
 
 }  // namespace
@@ -425,11 +460,33 @@ void launch_ref_grid_forces(const RefGrid& g, const RefGridBuffers& B, const Pot
     if (n <= 0) return;
     const unsigned b = (unsigned)((n + 127) / 128);
     k_grid_clear<<<b, 128, 0, s>>>(n, B.keys[1], B.start, B.end);
-    k_grid_keys<<<b, 128, 0, s>>>(g, n, pos, B.keys[0], B.ids[0]);
+    k_grid_keys<<<b, 128, 0, s>>>(g, n, pos, B.keys[0], B.ids[0], B.posf);
     size_t tb = B.temp_bytes;
     cub::DeviceRadixSort::SortPairs(B.temp, tb, B.keys[0], B.keys[1], B.ids[0], B.ids[1], n, 0, B.bits, s);
     k_grid_bounds<<<b, 128, 0, s>>>(n, B.keys[1], B.start, B.end);
-    GridArgs A{g, pot, pot.r0 * pot.r0, pos, owner, B.keys[1], B.ids[1], B.start, B.end};
+    GridArgs A{};
+    A.g = g;
+    A.pot = pot;
+    A.c2 = pot.r0 * pot.r0;
+    A.pos = pos;
+    A.posf = B.posf;
+    A.owner = owner;
+    A.keys = B.keys[1];
+    A.ids = B.ids[1];
+    A.start = B.start;
+    A.end = B.end;
+    // margin of the FP32 pre-test: the rounding of coordinates up to X (the box and its envelope)
+    // to FP32, twice, with a factor 4 of slack
+    double X = 0.0;
+    bool small_period = false;
+    for (int d = 0; d < 3; ++d) {
+        X = std::max(X, std::max(std::fabs(g.b0[d]), std::fabs(g.b0[d] + g.L[d])) + 4.0);
+        A.Lf[d] = (float)g.L[d];
+        A.Linvf[d] = (float)g.Linv[d];
+        small_period = small_period || (g.per[d] && g.L[d] < 2.0 * pot.r0 + 4.0);
+    }
+    const double margin = 8.0 * X * std::ldexp(1.0, -24) + 1e-4;
+    A.pre_c2 = small_period ? 0.0f : (float)((pot.r0 + margin) * (pot.r0 + margin) * (1.0 + 1e-6));
     const double wy0 = wall ? wall[0] : 0.0, wz0 = wall ? wall[1] : 0.0, wr = wall ? wall[2] : -1.0;
     // FP64-bound threads: with few vertices, one warp per CTA spreads them over more SMs
     const int tpb = n < 152 * 128 ? 32 : 128;
@@ -442,8 +499,12 @@ void launch_rigid_nodes(const GrowthView& G, double scale, cudaStream_t s) {
     if (G.np > 0) k_rigid_nodes<<<G.np, 256, 0, s>>>(G, scale);
 }
 
-void launch_rigid_move(const GrowthView& G, double scale, cudaStream_t s) {
-    if (G.np > 0) k_rigid_move<<<G.np, 128, 0, s>>>(G, scale);
+void launch_rigid_rescale(const GrowthView& G, cudaStream_t s) {
+    if (G.np > 0) k_rigid_rescale<<<G.np, 256, 0, s>>>(G);
+}
+
+void launch_rigid_move(const GrowthView& G, cudaStream_t s) {
+    if (G.np > 0) k_rigid_move<<<G.np, 128, 0, s>>>(G);
 }
 
 }  // namespace bib
