@@ -121,27 +121,15 @@ struct Staged<double> {
     static __device__ __forceinline__ void put(double* p, double a) { *p = a; }
 };
 
-// Collision of one cell in storage units.  FP32 compute uses the compact pairwise forms
-// (BGK + Guo, BGK, TRT); FP64 runs the generic operator of the reference's order.  With u
-// non-null the velocity j/rho + Fp/2 of the incoming state is returned.
+// Collision of one cell in storage units: the compact pairwise forms (BGK + Guo, BGK, TRT) in the
+// compute type.  With u non-null the velocity j/rho + Fp/2 of the incoming state is returned.
 template <class C, int COLL>
 __device__ __forceinline__ void staged_collide(C* f, const C* F, C om, C omm, C S, C invS, const C* Fp, C* u) {
-    if constexpr (sizeof(C) == 4 && COLL == BIB_COLLISION_TRT) {
+    if constexpr (COLL == BIB_COLLISION_TRT) {
         const C Fm[3] = {omm, C(0), C(0)};  // the TRT branch takes omega_minus in F[0]
-        collide_compact<COLL>(f, Fm, om, S, invS, Fp, u);
-    } else if constexpr (sizeof(C) == 4) {
-        collide_compact<COLL>(f, F, om, S, invS, Fp, u);
+        collide_compact<C, COLL>(f, Fm, om, S, invS, Fp, u);
     } else {
-        if (sizeof(C) == 4) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) f[i] *= invS;
-        }
-        if (u) velocity_with_force(f, Fp, u);
-        collide<C, COLL>(f, F, om, omm);
-        if (sizeof(C) == 4) {
-#pragma unroll
-            for (int i = 0; i < Q; ++i) f[i] *= S;
-        }
+        collide_compact<C, COLL>(f, F, om, S, invS, Fp, u);
     }
 }
 

@@ -59,12 +59,7 @@ struct Store<__half> {
 };
 
 // ---------------------------------------------------------------- moments
-// get_rhoBar and get_rhoBar_j (partial sums), src/latticeBoltzmann/momentTemplates3D.h:350-423
-template <class C>
-__device__ __forceinline__ C rho_bar_seq(const C* f) {
-    return f[0] + f[1] + f[2] + f[3] + f[4] + f[5] + f[6] + f[7] + f[8] + f[9] + f[10] + f[11] + f[12] + f[13] + f[14] +
-           f[15] + f[16] + f[17] + f[18];
-}
+// get_rhoBar_j (partial sums), src/latticeBoltzmann/momentTemplates3D.h:350-423
 template <class C>
 __device__ __forceinline__ void rho_bar_j(const C* f, C& rb, C* j) {
     const C sxm = f[1] + f[4] + f[5] + f[6] + f[7];
@@ -97,181 +92,105 @@ __device__ __forceinline__ C bgk_equilibrium(int i, C rhoBar, C invRho, const C*
     return weight<C>(i) * (rhoBar + C(3) * c_j + invRho * (C(4.5) * c_j * c_j - C(1.5) * jSqr));
 }
 
-// bgk_ma2_collision_base, src/latticeBoltzmann/dynamicsTemplates3D.h:770-838
-template <class C>
-__device__ __forceinline__ void bgk_collision(C* f, C rhoBar, const C* j, C omega, C invRho) {
-    const C omo = C(1) - omega;
-    const C t0w = weight<C>(0) * omega, t1w = weight<C>(1) * omega, t4w = weight<C>(4) * omega;
-    const C jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
-    const C kx = C(3) * j[0], ky = C(3) * j[1], kz = C(3) * j[2];
-    const C kxS = invRho / C(2) * kx * kx, kyS = invRho / C(2) * ky * ky, kzS = invRho / C(2) * kz * kz;
-    const C kxky = invRho * kx * ky, kxkz = invRho * kx * kz, kykz = invRho * ky * kz;
-    const C C1 = rhoBar + invRho * C(3) * jSqr;
-    C C2, C3;
-    C3 = -kxS - kyS - kzS;
-    f[0] = f[0] * omo + t0w * (C1 + C3);
-#define BIB_PAIR(a, b, tw)                      \
-    f[a] = f[a] * omo + tw * (C1 + C2 + C3); \
-    f[b] = f[b] * omo + tw * (C1 - C2 + C3);
-    C2 = -kx; C3 = -kyS - kzS; BIB_PAIR(1, 10, t1w)
-    C2 = -ky; C3 = -kxS - kzS; BIB_PAIR(2, 11, t1w)
-    C2 = -kz; C3 = -kxS - kyS; BIB_PAIR(3, 12, t1w)
-    C2 = -kx - ky; C3 = kxky - kzS; BIB_PAIR(4, 13, t4w)
-    C2 = -kx + ky; C3 = -kxky - kzS; BIB_PAIR(5, 14, t4w)
-    C2 = -kx - kz; C3 = kxkz - kyS; BIB_PAIR(6, 15, t4w)
-    C2 = -kx + kz; C3 = -kxkz - kyS; BIB_PAIR(7, 16, t4w)
-    C2 = -ky - kz; C3 = kykz - kxS; BIB_PAIR(8, 17, t4w)
-    C2 = -ky + kz; C3 = -kykz - kxS; BIB_PAIR(9, 18, t4w)
-#undef BIB_PAIR
-}
-
-// Guo forcing for D3Q19, src/fsi/VariableViscosityDynamics.hh:47-129
-template <class C>
-__device__ __forceinline__ void guo_force(C* f, const C* F, const C* u, C omega) {
-    const C mu = C(1) - omega / C(2);
-    const C o6 = C(1) / C(6), o12 = C(1) / C(12);
-    const C F0 = F[0], F1 = F[1], F2 = F[2], u0 = u[0], u1 = u[1], u2 = u[2];
-    f[0] += -mu * (F0 * u0 + F1 * u1 + F2 * u2);
-    f[1] += o6 * mu * (F0 * (C(-1) + 2 * u0) - F1 * u1 - F2 * u2);
-    f[2] += -o6 * mu * (F0 * u0 + F1 * (C(1) - 2 * u1) + F2 * u2);
-    f[3] += -o6 * mu * (F0 * u0 + F1 * u1 + F2 * (C(1) - 2 * u2));
-    f[4] += o12 * mu * (F0 * (C(-1) + 2 * u0 + 3 * u1) + F1 * (C(-1) + 2 * u1 + 3 * u0) - F2 * u2);
-    f[5] += o12 * mu * (F0 * (C(-1) + 2 * u0 - 3 * u1) + F1 * (C(1) + 2 * u1 - 3 * u0) - F2 * u2);
-    f[6] += o12 * mu * (F0 * (C(-1) + 2 * u0 + 3 * u2) - F1 * u1 + F2 * (C(-1) + 2 * u2 + 3 * u0));
-    f[7] += o12 * mu * (F0 * (C(-1) + 2 * u0 - 3 * u2) - F1 * u1 + F2 * (C(1) + 2 * u2 - 3 * u0));
-    f[8] += -o12 * mu * (F0 * u0 + F1 * (C(1) - 2 * u1 - 3 * u2) + F2 * (C(1) - 2 * u2 - 3 * u1));
-    f[9] += -o12 * mu * (F0 * u0 + F1 * (C(1) - 2 * u1 + 3 * u2) + F2 * (C(-1) - 2 * u2 + 3 * u1));
-    f[10] += o6 * mu * (F0 * (C(1) + 2 * u0) - F1 * u1 - F2 * u2);
-    f[11] += -o6 * mu * (F0 * u0 + F1 * (C(-1) - 2 * u1) + F2 * u2);
-    f[12] += -o6 * mu * (F0 * u0 + F1 * u1 + F2 * (C(-1) - 2 * u2));
-    f[13] += o12 * mu * (F0 * (C(1) + 2 * u0 + 3 * u1) + F1 * (C(1) + 2 * u1 + 3 * u0) - F2 * u2);
-    f[14] += o12 * mu * (F0 * (C(1) + 2 * u0 - 3 * u1) + F1 * (C(-1) + 2 * u1 - 3 * u0) - F2 * u2);
-    f[15] += o12 * mu * (F0 * (C(1) + 2 * u0 + 3 * u2) - F1 * u1 + F2 * (C(1) + 2 * u2 + 3 * u0));
-    f[16] += o12 * mu * (F0 * (C(1) + 2 * u0 - 3 * u2) - F1 * u1 + F2 * (C(-1) + 2 * u2 - 3 * u0));
-    f[17] += -o12 * mu * (F0 * u0 + F1 * (C(-1) - 2 * u1 - 3 * u2) + F2 * (C(-1) - 2 * u2 - 3 * u1));
-    f[18] += -o12 * mu * (F0 * u0 + F1 * (C(-1) - 2 * u1 + 3 * u2) + F2 * (C(1) - 2 * u2 + 3 * u1));
-}
-
-// Collision of one cell.  BGK_GUO_VOF follows GuoExternalForceVOFDynamics::collide
-// (src/fsi/VariableViscosityDynamics.hh:151-172); BGK follows BGKdynamics::collide
-// (src/basicDynamics/isoThermalDynamics.hh:329-340); TRT is Ginzburg's two-relaxation-
-// time split around the same equilibrium (no reference counterpart).
-template <class C, int COLL>
-__device__ __forceinline__ void collide(C* f, const C* F, C omega, C omega_minus) {
-    if (COLL == BIB_COLLISION_BGK_GUO_VOF) {
-        const C rhoBar = rho_bar_seq(f);
-        C u[3], j[3];
-        velocity_with_force(f, F, u);
-        const C rho = rhoBar + C(1);
-        j[0] = rho * u[0];
-        j[1] = rho * u[1];
-        j[2] = rho * u[2];
-        bgk_collision(f, rhoBar, j, omega, C(1) / (rhoBar + C(1)));
-        guo_force(f, F, u, omega);
-    } else if (COLL == BIB_COLLISION_BGK) {
-        C rb, j[3];
-        rho_bar_j(f, rb, j);
-        bgk_collision(f, rb, j, omega, C(1) / (rb + C(1)));
-    } else {
-        C rb, j[3];
-        rho_bar_j(f, rb, j);
-        const C invRho = C(1) / (rb + C(1));
-        const C jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
-        f[0] = f[0] - omega * (f[0] - bgk_equilibrium<C>(0, rb, invRho, j, jSqr));
-#pragma unroll
-        for (int i = 1; i < 10; ++i) {
-            const C ei = bgk_equilibrium<C>(i, rb, invRho, j, jSqr);
-            const C eo = bgk_equilibrium<C>(i + 9, rb, invRho, j, jSqr);
-            const C fp = C(0.5) * (f[i] + f[i + 9]), fm = C(0.5) * (f[i] - f[i + 9]);
-            const C dp = omega * (fp - C(0.5) * (ei + eo));
-            const C dm = omega_minus * (fm - C(0.5) * (ei - eo));
-            f[i] = f[i] - dp - dm;
-            f[i + 9] = f[i + 9] - dp + dm;
-        }
-    }
-}
-
-// Compact BGK + Guo collision for the reduced-precision paths.  Algebraically the same
-// operator as collide<C, BGK_GUO_VOF>: with u = j/rho + F/2, rho = rhoBar + 1, the BGK
-// equilibrium of J = rho u plus the Guo term of VariableViscosityDynamics.hh:47-129,
+// Collision of one cell, every kernel and every precision.  BGK_GUO_VOF is
+// GuoExternalForceVOFDynamics::collide (src/fsi/VariableViscosityDynamics.hh:151-172): with
+// u = j/rho + F/2, rho = rhoBar + 1, the BGK equilibrium of J = rho u
+// (bgk_ma2_collision_base, src/latticeBoltzmann/dynamicsTemplates3D.h:770-838) plus the Guo term of
+// VariableViscosityDynamics.hh:47-129,
 // t_i (1 - w/2) [3 (c_i - u).F + 9 (c_i.u)(c_i.F)], collapse to
 //     f_i' = (1 - w) f_i + t_i [A + c_i.H + (c_i.u)(c_i.G)]
 //     A = w rhoBar - 1.5 w rho u.u - 3 mu u.F,  H = 3 w rho u + 3 mu F,  G = 4.5 w rho u + 9 mu F,
 // mu = 1 - w/2, evaluated once per opposite pair (i, i+9) (c_{i+9} = -c_i).  BGK without
-// forcing is the same with F = 0 and u = j/rho.  The populations may carry a common scale S
+// forcing is the same with F = 0 and u = j/rho (BGKdynamics::collide,
+// src/basicDynamics/isoThermalDynamics.hh:329-340); TRT is Ginzburg's two-relaxation-time split
+// around the same equilibrium (no reference counterpart).  The populations may carry a common scale S
 // (FP16 storage keeps f-bar * S): moments are unscaled once, post-collision values come out
 // in scaled units.  With `u_prev` non-null the velocity j/rho + F_prev/2 of the incoming
 // state is returned as well (the reference's computeVelocity).
 // c_i . (a, b, c) with the zero components left out: multiplications by 0 are not removed
 // by the compiler under IEEE semantics (0 * inf is NaN), so they are not written.
-__device__ __forceinline__ float cdot(int i, float a, float b, float c) {
-    const float xa = cx(i) > 0 ? a : -a, yb = cy(i) > 0 ? b : -b, zc = cz(i) > 0 ? c : -c;
+template <class C>
+__device__ __forceinline__ C cdot(int i, C a, C b, C c) {
+    const C xa = cx(i) > 0 ? a : -a, yb = cy(i) > 0 ? b : -b, zc = cz(i) > 0 ? c : -c;
     if (cx(i) != 0) {
         if (cy(i) != 0) return xa + yb;
         if (cz(i) != 0) return xa + zc;
         return xa;
     }
     if (cy(i) != 0) return cz(i) != 0 ? yb + zc : yb;
-    return cz(i) != 0 ? zc : 0.0f;
+    return cz(i) != 0 ? zc : C(0);
 }
+__device__ __forceinline__ float fmac(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fmac(double a, double b, double c) { return fma(a, b, c); }
 
-template <int COLL>
-__device__ __forceinline__ void collide_compact(float* f, const float* F, float omega, float S, float invS,
-                                                const float* Fprev, float* u_prev) {
-    const float sxm = f[1] + f[4] + f[5] + f[6] + f[7];
-    const float sxp = f[10] + f[13] + f[14] + f[15] + f[16];
-    const float sym = f[2] + f[4] + f[8] + f[9] + f[14];
-    const float syp = f[5] + f[11] + f[13] + f[17] + f[18];
-    const float szm = f[3] + f[6] + f[8] + f[16] + f[18];
-    const float szp = f[7] + f[9] + f[12] + f[15] + f[17];
-    const float sx0 = f[0] + f[2] + f[3] + f[8] + f[9] + f[11] + f[12] + f[17] + f[18];
-    const float rb = (sxm + sx0 + sxp) * invS;
-    const float j0 = (sxp - sxm) * invS, j1 = (syp - sym) * invS, j2 = (szp - szm) * invS;
-    const float invRho = 1.0f / (rb + 1.0f);
+template <class C, int COLL>
+__device__ __forceinline__ void collide_compact(C* f, const C* F, C omega, C S, C invS, const C* Fprev, C* u_prev) {
+    const C sxm = f[1] + f[4] + f[5] + f[6] + f[7];
+    const C sxp = f[10] + f[13] + f[14] + f[15] + f[16];
+    const C sym = f[2] + f[4] + f[8] + f[9] + f[14];
+    const C syp = f[5] + f[11] + f[13] + f[17] + f[18];
+    const C szm = f[3] + f[6] + f[8] + f[16] + f[18];
+    const C szp = f[7] + f[9] + f[12] + f[15] + f[17];
+    const C sx0 = f[0] + f[2] + f[3] + f[8] + f[9] + f[11] + f[12] + f[17] + f[18];
+    const C rb = (sxm + sx0 + sxp) * invS;
+    const C j0 = (sxp - sxm) * invS, j1 = (syp - sym) * invS, j2 = (szp - szm) * invS;
+    const C invRho = C(1) / (rb + C(1));
     if (u_prev) {
-        u_prev[0] = fmaf(j0, invRho, 0.5f * Fprev[0]);
-        u_prev[1] = fmaf(j1, invRho, 0.5f * Fprev[1]);
-        u_prev[2] = fmaf(j2, invRho, 0.5f * Fprev[2]);
+        u_prev[0] = fmac(j0, invRho, C(0.5) * Fprev[0]);
+        u_prev[1] = fmac(j1, invRho, C(0.5) * Fprev[1]);
+        u_prev[2] = fmac(j2, invRho, C(0.5) * Fprev[2]);
     }
     if (COLL == BIB_COLLISION_TRT) {
         // Two relaxation times around the BGK equilibrium of j: the symmetric part of each
         // pair (i, i+9) relaxes with omega, the antisymmetric part with omega_minus (passed
         // in F[0]); feq+ = t_i (rhoBar + 4.5 (c.j)^2 / rho - 1.5 j.j / rho), feq- = 3 t_i c.j.
-        const float omm = F[0];
-        const float base = rb - 1.5f * invRho * (j0 * j0 + j1 * j1 + j2 * j2);
-        const float h = 4.5f * invRho;
-        f[0] = fmaf(-omega, f[0] - (S * weight<float>(0)) * base, f[0]);
+        const C omm = F[0];
+        const C base = rb - C(1.5) * invRho * (j0 * j0 + j1 * j1 + j2 * j2);
+        const C h = C(4.5) * invRho;
+        f[0] = fmac(-omega, f[0] - (S * weight<C>(0)) * base, f[0]);
 #pragma unroll
         for (int i = 1; i < 10; ++i) {
-            const float cj = cdot(i, j0, j1, j2);
-            const float tw = S * weight<float>(i);
-            const float ep = tw * fmaf(h * cj, cj, base), em = tw * 3.0f * cj;
-            const float dp = omega * (0.5f * (f[i] + f[i + 9]) - ep);
-            const float dm = omm * (0.5f * (f[i] - f[i + 9]) - em);
+            const C cj = cdot<C>(i, j0, j1, j2);
+            const C tw = S * weight<C>(i);
+            const C ep = tw * fmac(h * cj, cj, base), em = tw * C(3) * cj;
+            const C dp = omega * (C(0.5) * (f[i] + f[i + 9]) - ep);
+            const C dm = omm * (C(0.5) * (f[i] - f[i + 9]) - em);
             f[i] = f[i] - dp - dm;
             f[i + 9] = f[i + 9] - dp + dm;
         }
         return;
     }
     const bool forced = COLL == BIB_COLLISION_BGK_GUO_VOF;
-    const float F0 = forced ? F[0] : 0.0f, F1 = forced ? F[1] : 0.0f, F2 = forced ? F[2] : 0.0f;
-    const float u0 = fmaf(j0, invRho, 0.5f * F0), u1 = fmaf(j1, invRho, 0.5f * F1), u2 = fmaf(j2, invRho, 0.5f * F2);
-    const float rho = rb + 1.0f;
-    const float mu = 1.0f - 0.5f * omega;
-    const float wr = omega * rho;
-    const float A = omega * rb - 1.5f * wr * (u0 * u0 + u1 * u1 + u2 * u2) - 3.0f * mu * (u0 * F0 + u1 * F1 + u2 * F2);
-    const float h3 = 3.0f * wr, m3 = 3.0f * mu, g45 = 4.5f * wr, m9 = 9.0f * mu;
-    const float H0 = fmaf(h3, u0, m3 * F0), H1 = fmaf(h3, u1, m3 * F1), H2 = fmaf(h3, u2, m3 * F2);
-    const float G0 = fmaf(g45, u0, m9 * F0), G1 = fmaf(g45, u1, m9 * F1), G2 = fmaf(g45, u2, m9 * F2);
-    const float omo = 1.0f - omega;
-    f[0] = fmaf(omo, f[0], (S * weight<float>(0)) * A);
+    const C F0 = forced ? F[0] : C(0), F1 = forced ? F[1] : C(0), F2 = forced ? F[2] : C(0);
+    const C u0 = fmac(j0, invRho, C(0.5) * F0), u1 = fmac(j1, invRho, C(0.5) * F1), u2 = fmac(j2, invRho, C(0.5) * F2);
+    const C rho = rb + C(1);
+    const C mu = C(1) - C(0.5) * omega;
+    const C wr = omega * rho;
+    const C A = omega * rb - C(1.5) * wr * (u0 * u0 + u1 * u1 + u2 * u2) - C(3) * mu * (u0 * F0 + u1 * F1 + u2 * F2);
+    const C h3 = C(3) * wr, m3 = C(3) * mu, g45 = C(4.5) * wr, m9 = C(9) * mu;
+    const C H0 = fmac(h3, u0, m3 * F0), H1 = fmac(h3, u1, m3 * F1), H2 = fmac(h3, u2, m3 * F2);
+    const C G0 = fmac(g45, u0, m9 * F0), G1 = fmac(g45, u1, m9 * F1), G2 = fmac(g45, u2, m9 * F2);
+    const C omo = C(1) - omega;
+    f[0] = fmac(omo, f[0], (S * weight<C>(0)) * A);
 #pragma unroll
     for (int i = 1; i < 10; ++i) {
-        const float cu = cdot(i, u0, u1, u2), cG = cdot(i, G0, G1, G2), cH = cdot(i, H0, H1, H2);
-        const float tw = S * weight<float>(i);
-        const float P = tw * fmaf(cu, cG, A), M = tw * cH;
-        f[i] = fmaf(omo, f[i], P + M);
-        f[i + 9] = fmaf(omo, f[i + 9], P - M);
+        const C cu = cdot<C>(i, u0, u1, u2), cG = cdot<C>(i, G0, G1, G2), cH = cdot<C>(i, H0, H1, H2);
+        const C tw = S * weight<C>(i);
+        const C P = tw * fmac(cu, cG, A), M = tw * cH;
+        f[i] = fmac(omo, f[i], P + M);
+        f[i + 9] = fmac(omo, f[i + 9], P - M);
+    }
+}
+
+// The compact operators at unit scale (FP64 / FP32 populations held as f-bar): omega_minus is the
+// TRT rate of the antisymmetric parts, unused otherwise.
+template <class C, int COLL>
+__device__ __forceinline__ void collide_unscaled(C* f, const C* F, C omega, C omega_minus) {
+    if (COLL == BIB_COLLISION_TRT) {
+        const C Fm[3] = {omega_minus, C(0), C(0)};
+        collide_compact<C, COLL>(f, Fm, omega, C(1), C(1), nullptr, nullptr);
+    } else {
+        collide_compact<C, COLL>(f, F, omega, C(1), C(1), nullptr, nullptr);
     }
 }
 

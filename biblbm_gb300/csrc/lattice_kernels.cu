@@ -112,13 +112,13 @@ __global__ void __launch_bounds__(256) k_collide_stream(LatticeDesc d, const T* 
     if (coll == BIB_COLLISION_BGK_GUO_VOF) {
         C omega = (C)d.omega_c0;
         if (d.use_phase && phase[k]) omega = (C)d.omega_c1;
-        collide<C, BIB_COLLISION_BGK_GUO_VOF>(f, Fc, omega, C(0));
+        collide_unscaled<C, BIB_COLLISION_BGK_GUO_VOF>(f, Fc, omega, C(0));
     } else if (coll == BIB_COLLISION_BGK) {
-        collide<C, BIB_COLLISION_BGK>(f, Fc, (C)d.omega, C(0));
+        collide_unscaled<C, BIB_COLLISION_BGK>(f, Fc, (C)d.omega, C(0));
     } else {
         const C om = (C)d.omega;
         const C omm = C(1) / ((C)d.trt_magic / (C(1) / om - C(0.5)) + C(0.5));
-        collide<C, BIB_COLLISION_TRT>(f, Fc, om, omm);
+        collide_unscaled<C, BIB_COLLISION_TRT>(f, Fc, om, omm);
     }
 #pragma unroll
     for (int i = 0; i < Q; ++i) Store<T>::store(fout + i * d.stride + k, f[i], d.scale);
@@ -273,9 +273,9 @@ __global__ void __launch_bounds__(256) k_collide_stream_rows(LatticeDesc d, cons
         omm = C(1) / ((C)d.trt_magic / (C(1) / om0 - C(0.5)) + C(0.5));
     }
     auto collide_one = [&](C* f, const C* Fx, C om) {
-        if (coll == BIB_COLLISION_BGK_GUO_VOF) collide<C, BIB_COLLISION_BGK_GUO_VOF>(f, Fx, om, C(0));
-        else if (coll == BIB_COLLISION_BGK) collide<C, BIB_COLLISION_BGK>(f, Fx, om, C(0));
-        else collide<C, BIB_COLLISION_TRT>(f, Fx, om, omm);
+        if (coll == BIB_COLLISION_BGK_GUO_VOF) collide_unscaled<C, BIB_COLLISION_BGK_GUO_VOF>(f, Fx, om, C(0));
+        else if (coll == BIB_COLLISION_BGK) collide_unscaled<C, BIB_COLLISION_BGK>(f, Fx, om, C(0));
+        else collide_unscaled<C, BIB_COLLISION_TRT>(f, Fx, om, omm);
     };
     // BounceBack nodes swap their incoming populations, NoDynamics nodes keep them
     if (ct0 == BIB_CELL_FLUID) collide_one(f0, Fa, om0);
