@@ -124,12 +124,12 @@ struct Staged<double> {
 // Collision of one cell in storage units: the compact pairwise forms (BGK + Guo, BGK, TRT) in the
 // compute type.  With u non-null the velocity j/rho + Fp/2 of the incoming state is returned.
 template <class C, int COLL>
-__device__ __forceinline__ void staged_collide(C* f, const C* F, C om, C omm, C S, C invS, const C* Fp, C* u) {
+__device__ __forceinline__ void staged_relax(C* f, const C* F, C om, C omm, C S, const CellMoments<C>& m) {
     if constexpr (COLL == BIB_COLLISION_TRT) {
         const C Fm[3] = {omm, C(0), C(0)};  // the TRT branch takes omega_minus in F[0]
-        collide_compact<C, COLL>(f, Fm, om, S, invS, Fp, u);
+        relax_compact<C, COLL>(f, Fm, om, S, m);
     } else {
-        collide_compact<C, COLL>(f, F, om, S, invS, Fp, u);
+        relax_compact<C, COLL>(f, F, om, S, m);
     }
 }
 
@@ -321,22 +321,25 @@ __device__ __forceinline__ void finish_cell(const LatticeDesc& d, const CollideP
     }
     C om = cp.om0;
     if (COLL == BIB_COLLISION_BGK_GUO_VOF && d.use_phase && phase[k]) om = cp.om1;
+    const CellMoments<C> m = moments_compact<C>(f, cp.invS);
     if (CPL != kCplNone) {
+        // the velocity and the force reset are stored before the relaxation, so that the
+        // previous force is dead while the relaxation runs
         C u[3];
-        staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, Fp, fd ? nullptr : u);
         if (fd) {
             const int side = y == 0 ? 0 : 1;
 #pragma unroll
             for (int q = 0; q < 3; ++q) u[q] = cp.wall_u[side][q];
+        } else {
+            velocity_compact<C>(m, Fp, u);
         }
         store_u<UT>(u_out, k, (UT)u[0], (UT)u[1], (UT)u[2]);
         if (CPL == kCplDense) {
 #pragma unroll
             for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
         }
-    } else {
-        staged_collide<C, COLL>(f, F, om, cp.omm, cp.S, cp.invS, nullptr, nullptr);
     }
+    staged_relax<C, COLL>(f, F, om, cp.omm, cp.S, m);
     T* o = fout + k;
 #pragma unroll
     for (int i = 0; i < Q; ++i) {

@@ -123,8 +123,13 @@ __device__ __forceinline__ C cdot(int i, C a, C b, C c) {
 __device__ __forceinline__ float fmac(float a, float b, float c) { return fmaf(a, b, c); }
 __device__ __forceinline__ double fmac(double a, double b, double c) { return fma(a, b, c); }
 
-template <class C, int COLL>
-__device__ __forceinline__ void collide_compact(C* f, const C* F, C omega, C S, C invS, const C* Fprev, C* u_prev) {
+// Moments of the incoming state: rhoBar, j and 1/rho, unscaled.
+template <class C>
+struct CellMoments {
+    C rb, j0, j1, j2, invRho;
+};
+template <class C>
+__device__ __forceinline__ CellMoments<C> moments_compact(const C* f, C invS) {
     const C sxm = f[1] + f[4] + f[5] + f[6] + f[7];
     const C sxp = f[10] + f[13] + f[14] + f[15] + f[16];
     const C sym = f[2] + f[4] + f[8] + f[9] + f[14];
@@ -132,14 +137,27 @@ __device__ __forceinline__ void collide_compact(C* f, const C* F, C omega, C S, 
     const C szm = f[3] + f[6] + f[8] + f[16] + f[18];
     const C szp = f[7] + f[9] + f[12] + f[15] + f[17];
     const C sx0 = f[0] + f[2] + f[3] + f[8] + f[9] + f[11] + f[12] + f[17] + f[18];
-    const C rb = (sxm + sx0 + sxp) * invS;
-    const C j0 = (sxp - sxm) * invS, j1 = (syp - sym) * invS, j2 = (szp - szm) * invS;
-    const C invRho = C(1) / (rb + C(1));
-    if (u_prev) {
-        u_prev[0] = fmac(j0, invRho, C(0.5) * Fprev[0]);
-        u_prev[1] = fmac(j1, invRho, C(0.5) * Fprev[1]);
-        u_prev[2] = fmac(j2, invRho, C(0.5) * Fprev[2]);
-    }
+    CellMoments<C> m;
+    m.rb = (sxm + sx0 + sxp) * invS;
+    m.j0 = (sxp - sxm) * invS;
+    m.j1 = (syp - sym) * invS;
+    m.j2 = (szp - szm) * invS;
+    m.invRho = C(1) / (m.rb + C(1));
+    return m;
+}
+
+// The velocity j/rho + F_prev/2 of the incoming state (the reference's computeVelocity).
+template <class C>
+__device__ __forceinline__ void velocity_compact(const CellMoments<C>& m, const C* Fprev, C* u) {
+    u[0] = fmac(m.j0, m.invRho, C(0.5) * Fprev[0]);
+    u[1] = fmac(m.j1, m.invRho, C(0.5) * Fprev[1]);
+    u[2] = fmac(m.j2, m.invRho, C(0.5) * Fprev[2]);
+}
+
+// Relaxation of one cell from its moments (scaled populations in, scaled populations out).
+template <class C, int COLL>
+__device__ __forceinline__ void relax_compact(C* f, const C* F, C omega, C S, const CellMoments<C>& m) {
+    const C rb = m.rb, j0 = m.j0, j1 = m.j1, j2 = m.j2, invRho = m.invRho;
     if (COLL == BIB_COLLISION_TRT) {
         // Two relaxation times around the BGK equilibrium of j: the symmetric part of each
         // pair (i, i+9) relaxes with omega, the antisymmetric part with omega_minus (passed
@@ -180,6 +198,13 @@ __device__ __forceinline__ void collide_compact(C* f, const C* F, C omega, C S, 
         f[i] = fmac(omo, f[i], P + M);
         f[i + 9] = fmac(omo, f[i + 9], P - M);
     }
+}
+
+template <class C, int COLL>
+__device__ __forceinline__ void collide_compact(C* f, const C* F, C omega, C S, C invS, const C* Fprev, C* u_prev) {
+    const CellMoments<C> m = moments_compact<C>(f, invS);
+    if (u_prev) velocity_compact<C>(m, Fprev, u_prev);
+    relax_compact<C, COLL>(f, F, omega, S, m);
 }
 
 // The compact operators at unit scale (FP64 / FP32 populations held as f-bar): omega_minus is the
