@@ -39,16 +39,16 @@ __device__ __forceinline__ void gather(const LatticeDesc& d, const T* __restrict
 // state has to be stored so that the next gather returns it.
 template <class T>
 __device__ __forceinline__ void scatter_canonical(const LatticeDesc& d, T* __restrict__ f, T* __restrict__ wall, int i, int x,
-                                                  int y, int z, int64_t k, double v) {
+                                                  int y, int z, int64_t k, typename Store<T>::C v) {
     using C = typename Store<T>::C;
     if (fd_wall_node(d, y)) {
-        Store<T>::store(wall + i * wall_stride(d) + wall_index(d, y == 0 ? 0 : 1, x, z), (C)v, d.scale);
+        Store<T>::store(wall + i * wall_stride(d) + wall_index(d, y == 0 ? 0 : 1, x, z), v, d.scale);
         return;
     }
     int face;
     const int64_t s = source_cell(d, i, x, y, z, face);
-    if (s >= 0) Store<T>::store(f + i * d.stride + s, (C)v, d.scale);
-    else Store<T>::store(f + opposite(i) * d.stride + k, (C)v - moving_wall_term<C>(d, i, face), d.scale);
+    if (s >= 0) Store<T>::store(f + i * d.stride + s, v, d.scale);
+    else Store<T>::store(f + opposite(i) * d.stride + k, v - moving_wall_term<C>(d, i, face), d.scale);
 }
 
 template <class T, bool COUPLED>
@@ -342,7 +342,7 @@ __global__ void __launch_bounds__(128) k_guo_walls(LatticeDesc d, T* __restrict_
 #pragma unroll
     for (int i = 0; i < Q; ++i)
         scatter_canonical<T>(d, f, const_cast<T*>(wall), i, w.x, w.y, w.z, k,
-                             (double)((w.nodyn ? C(0) : bgk_equilibrium<C>(i, rbw, invRho, jw, jsq)) + fw[i]));
+                             (w.nodyn ? C(0) : bgk_equilibrium<C>(i, rbw, invRho, jw, jsq)) + fw[i]);
 }
 
 template <class T>
@@ -452,21 +452,24 @@ __global__ void k_velocity(LatticeDesc d, const T* __restrict__ f, const T* __re
     if (kstride == 4) u[k * 4 + 3] = OT(0.0f);
 }
 
-// iniCellAtEquilibrium, src/core/cell.hh:124-132
+// iniCellAtEquilibrium, src/core/cell.hh:124-132, in the storage's compute type (FP64 for FP64
+// storage; FP32 otherwise: the FP64 pipe of this part would make the 19 equilibria per cell
+// slower than reading the host velocity field over the CPU-GPU link).
 template <class T>
 __global__ void k_init_eq(LatticeDesc d, T* __restrict__ f, T* __restrict__ wall, const double* __restrict__ rho,
                           const double* __restrict__ u) {
+    using C = typename Store<T>::C;
     const int x = blockIdx.x * blockDim.x + threadIdx.x;
     const int y = blockIdx.y, z = blockIdx.z;
     if (x >= d.nx) return;
     const int64_t k = x + (int64_t)d.nx * (y + (int64_t)d.ny * z);
     const double r = rho ? rho[k] : 1.0;
-    double j[3] = {u[k] * r, u[d.n + k] * r, u[2 * d.n + k] * r};
-    const double jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
-    const double rhoBar = r - 1.0;
-    const double invRho = 1.0 / (rhoBar + 1.0);
+    const C j[3] = {(C)(u[k] * r), (C)(u[d.n + k] * r), (C)(u[2 * d.n + k] * r)};
+    const C jSqr = j[0] * j[0] + j[1] * j[1] + j[2] * j[2];
+    const double rb = r - 1.0;
+    const C rhoBar = (C)rb, invRho = (C)(1.0 / (rb + 1.0));
 #pragma unroll
-    for (int i = 0; i < Q; ++i) scatter_canonical<T>(d, f, wall, i, x, y, z, k, bgk_equilibrium<double>(i, rhoBar, invRho, j, jSqr));
+    for (int i = 0; i < Q; ++i) scatter_canonical<T>(d, f, wall, i, x, y, z, k, bgk_equilibrium<C>(i, rhoBar, invRho, j, jSqr));
 }
 
 // Import / export of the planes z0 .. z0 + gridDim.z - 1 from / to a buffer holding, per
