@@ -44,6 +44,8 @@ KERNEL_BYTES_PER_LU = {st: 19 * s * 2 + 3 * 3 * fb + 4 * ub
                        for st, s, fb, ub in (("f64", 8, 8, 8), ("f32", 4, 4, 4), ("f16", 2, 4, 2))}
 # Steps of the precision comparison: the run lengths of the benchmark configurations
 COMPARE_STEPS = {"channel": 2000, "capsule": 2000, "rbc": 5000}
+# complete runs of the end-to-end driver loop; the median is reported
+E2E_RUNS = 3
 
 
 def env_rank():
@@ -650,24 +652,32 @@ def main():
         u0 = pinned((3, nz, ny, nx))
         u0[...] = 0.0 if wl.get("initial_velocity") is None else wl["initial_velocity"]
         u_out = pinned((3, nz, ny, nx))
-        barrier()
-        t0 = time.perf_counter()
-        c3.check(lib.bib_lattice_init_equilibrium(h, l3.h, None, dpd(u0)))
-        c3.check(lib.bib_particles_upload(h, l3.h, dpd(pos_host)))
-        for k in range(K):
-            c3.check(lib.bib_step(h, l3.h, 1))
-            c3.check(lib.bib_particles_download_async(h, l3.h, None, dpd(stats_buf[k % 2]), k % 2))
-            if k:
-                c3.check(lib.bib_download_wait(h, (k - 1) % 2))
-        c3.check(lib.bib_download_wait(h, (K - 1) % 2))
-        c3.check(lib.bib_particles_download(h, l3.h, dpd(pos_out), None))
-        c3.check(lib.bib_lattice_get_velocity(h, l3.h, dpd(u_out)))
-        dt2 = max_over_ranks(time.perf_counter() - t0)
+
+        def driver_loop():
+            barrier()
+            t0 = time.perf_counter()
+            c3.check(lib.bib_lattice_init_equilibrium(h, l3.h, None, dpd(u0)))
+            c3.check(lib.bib_particles_upload(h, l3.h, dpd(pos_host)))
+            for k in range(K):
+                c3.check(lib.bib_step(h, l3.h, 1))
+                c3.check(lib.bib_particles_download_async(h, l3.h, None, dpd(stats_buf[k % 2]), k % 2))
+                if k:
+                    c3.check(lib.bib_download_wait(h, (k - 1) % 2))
+            c3.check(lib.bib_download_wait(h, (K - 1) % 2))
+            c3.check(lib.bib_particles_download(h, l3.h, dpd(pos_out), None))
+            c3.check(lib.bib_lattice_get_velocity(h, l3.h, dpd(u_out)))
+            return max_over_ranks(time.perf_counter() - t0)
+
+        # three complete runs of the loop (each from the host velocity field to the host results);
+        # the median is reported: one run of a few milliseconds varies with host scheduling
+        runs = [driver_loop() for _ in range(E2E_RUNS)]
+        dt2 = float(np.median(runs))
         barrier()
         # the headline: the reference's own driver loop; the population round trip of the
         # CoProcessor3D boundary (bound by the CPU-GPU link for few steps) beside it
         e2e = {
             "value": cells * K * world / dt2 / 1e6, "unit": "MLUPS", "seconds": dt2,
+            "runs": len(runs), "seconds_each": runs,
             "h2d_bytes_per_step": int((u0.nbytes + pos_host.nbytes) // K),
             "d2h_bytes_per_step": int((K * stats_out.nbytes + pos_out.nbytes + u_out.nbytes) // K),
             "what": "the loop of the reference's channel driver (rbcs_in_channel.cpp): bib_lattice_init_equilibrium "
