@@ -513,6 +513,73 @@ __global__ void __launch_bounds__(128) k_spread(IbView v1, const IbView* __restr
     spread_vertex<FT, S>(V, BATCH ? g - V.vbase : g);
 }
 
+// Two lanes per vertex (FP32 field, Roma support, no pipe, no wrap along x inside the support):
+// the lanes of a pair add the two float4 words of a window that straddles a 16-byte boundary in
+// the same instruction, so that both words go out in one request when they share a 128-byte line
+// (the spreading is bound by the count of its requests: 0.0950 -> 0.0835 ms on the 400-cell
+// channel against one lane issuing both words).  Same products as spread_vertex.
+__device__ __forceinline__ void spread_vertex_pair(const IbView& V, int v, int half) {
+    const LatticeDesc& d = V.d;
+    const IbDesc& ib = V.ib;
+    const double p[3] = {V.pos[3 * v], V.pos[3 * v + 1], V.pos[3 * v + 2]};
+    if (!inside_envelope(d, ib.dirac, p)) {
+        if (V.spread_lo && half == 0) V.spread_lo[v] = make_int4(0, 0, 0, 0);
+        return;
+    }
+    const int off = (int)ib.offset;
+    int64_t lo[3];
+    float w[3][4];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) lo[a] = axis_weights<float, 3>(p[a] - ib.offset, w[a]);
+    int gx[3], gy[3], gz[3];
+#pragma unroll
+    for (int m = 0; m < 3; ++m) {
+        gx[m] = remap_global(d.px, d.nx, lo[0] + m, off);
+        gy[m] = remap_global(d.py, d.ny, lo[1] + m, off);
+        gz[m] = remap_global(d.pz, d.nz, lo[2] + m, off);
+    }
+    if (ib.has_pipe || gx[2] != gx[0] + 2) {
+        if (half == 0) spread_vertex<float, 3>(V, v);
+        return;
+    }
+    if (V.spread_lo && half == 0)
+        V.spread_lo[v] = make_int4(record_lo(d.px, d.nx, (int64_t)ceil(p[0] - ib.offset - 1.5), off),
+                                   record_lo(d.py, d.ny, (int64_t)ceil(p[1] - ib.offset - 1.5), off),
+                                   record_lo(d.pz, d.nz, (int64_t)ceil(p[2] - ib.offset - 1.5), off), 1);
+    const float fv[3] = {(float)V.force[3 * v], (float)V.force[3 * v + 1], (float)V.force[3 * v + 2]};
+    float* F = static_cast<float*>(V.F);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+        if (gy[b] < 0) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+            if (gz[c] < 0) continue;
+            const float wyz = w[1][b] * w[2][c];
+            const int64_t k0 = gx[0] + (int64_t)gy[b] * d.nx + (int64_t)gz[c] * d.ny * d.nx;
+            const int64_t kq = k0 & ~(int64_t)3;
+            const int o = (int)(k0 - kq);
+            const bool go = half == 0 || o + 3 > 4;
+#pragma unroll
+            for (int q = 0; q < 3; ++q) {
+                float vals[4];
+#pragma unroll
+                for (int m = 0; m < 4; ++m) vals[m] = m < 3 ? (float)((w[0][m] * wyz) * fv[q]) : 0.0f;
+                const int j = half * 4;
+                const float4 val = make_float4(window_select(vals, j, o, 3), window_select(vals, j + 1, o, 3),
+                                               window_select(vals, j + 2, o, 3), window_select(vals, j + 3, o, 3));
+                if (go) atomicAdd(reinterpret_cast<float4*>(F + q * d.stride + kq) + half, val);
+            }
+        }
+    }
+}
+
+__global__ void __launch_bounds__(128) k_spread_pairs(IbView v1, int nvert) {
+    const int g = blockIdx.x * blockDim.x + threadIdx.x;
+    const int v = g >> 1;
+    if (v >= nvert) return;
+    spread_vertex_pair(v1, v, g & 1);
+}
+
 // Deterministic spreading.  Every (vertex, stencil node) pair becomes an entry keyed by its
 // target cell; a stable radix sort groups the entries of a cell in vertex order, and one
 // thread per cell sums its contributions in that order onto the body force already in F.
@@ -1565,6 +1632,7 @@ void spread_any(int storage, int dirac, const IbView& v1, const IbView* views, c
         else k_spread<double, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
     } else {
         if (peskin) k_spread<float, 4, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
+        else if (!BATCH) k_spread_pairs<<<(unsigned)((2LL * nvert + 127) / 128), 128, 0, s>>>(v1, nvert);
         else k_spread<float, 3, BATCH><<<g, 128, 0, s>>>(v1, views, vinst, nvert);
     }
 }
