@@ -2263,8 +2263,17 @@ bib_status bib_particles_download_async(bib_ctx* c, int32_t h, double* pos, doub
     } else {
         if (pos && L->nvert)
             BIB_CUDA(c, cudaMemcpyAsync(pos, L->pos[L->pcur], 3 * (size_t)L->nvert * 8, cudaMemcpyDeviceToHost, c->stream));
-        if (stats && !L->parts.empty())
-            BIB_CUDA(c, cudaMemcpyAsync(stats, L->stats, STATS * L->parts.size() * 8, cudaMemcpyDeviceToHost, c->stream));
+        if (stats && !L->parts.empty()) {
+            // a page-locked buffer is written by a small kernel over the link: no copy-engine
+            // hand-over between the step graphs of a step-then-read loop
+            const size_t n = STATS * L->parts.size();
+            if (double* m = static_cast<double*>(const_cast<void*>(device_view_of_host(stats, n * 8)))) {
+                launch_copy_f64(m, L->stats, n, c->stream);
+                BIB_CHECK_LAUNCH(c);
+            } else {
+                BIB_CUDA(c, cudaMemcpyAsync(stats, L->stats, n * 8, cudaMemcpyDeviceToHost, c->stream));
+            }
+        }
     }
     BIB_CUDA(c, cudaEventRecord(c->dl_ev[slot], c->stream));
     return BIB_OK;

@@ -380,6 +380,8 @@ void launch_force_export(const Lattice& L, int buf, double* dst, cudaStream_t s)
 void launch_force_fill(const Lattice& L, int buf, cudaStream_t s);
 void launch_phase_import(const Lattice& L, const double* src, cudaStream_t s);
 void launch_nan_scan(const Lattice& L, int* flag, cudaStream_t s);
+// dst[i] = src[i] for i < n (dst may be page-locked host memory mapped for the device)
+void launch_copy_f64(double* dst, const double* src, size_t n, cudaStream_t s);
 
 // ---- kernel launchers (ib_kernels.cu) ----
 void launch_membrane_forces(const Lattice& L, cudaStream_t s);

@@ -728,6 +728,18 @@ void launch_fd_walls(const Lattice& L, int buf, int fbuf, cudaStream_t s) {
     if (L.nguo > 0) BIB_DISPATCH(L.storage, guo_walls_t, L, buf, s);
 }
 
+namespace {
+__global__ void __launch_bounds__(256) k_copy_f64(double* __restrict__ dst, const double* __restrict__ src, size_t n) {
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) dst[i] = src[i];
+}
+}  // namespace
+
+void launch_copy_f64(double* dst, const double* src, size_t n, cudaStream_t s) {
+    if (n == 0) return;
+    const unsigned g = (unsigned)std::min<size_t>((n + 255) / 256, 1024);
+    k_copy_f64<<<g, 256, 0, s>>>(dst, src, n);
+}
+
 void launch_velocity_field(const Lattice& L, cudaStream_t s) { BIB_DISPATCH(L.storage, velocity_field_t, L, s); }
 
 void launch_velocity_export(const Lattice& L, double* u, cudaStream_t s) {
