@@ -315,7 +315,9 @@ bib_status bib_particles_upload(bib_ctx* ctx, int32_t h, const double* pos);
 /* bib_particles_download without waiting: the copies are queued on the context's stream behind the
  * work issued so far, and slot (0..7) marks their completion.  The host buffers must stay valid (and
  * be pinned for the copy to overlap) until bib_download_wait(ctx, slot) returns; a step issued in
- * between runs while the copy's data are read.  Either pointer may be NULL. */
+ * between runs while the copy's data are read.  Either pointer may be NULL.  A page-locked stats
+ * buffer is written by a small kernel through its mapped address (no copy-engine hand-over between
+ * the steps of a step-then-read loop). */
 bib_status bib_particles_download_async(bib_ctx* ctx, int32_t h, double* pos, double* stats, int32_t slot);
 bib_status bib_download_wait(bib_ctx* ctx, int32_t slot);
 bib_status bib_total_vertices(bib_ctx* ctx, int32_t h, int64_t* n);
