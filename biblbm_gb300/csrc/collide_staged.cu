@@ -351,7 +351,7 @@ __device__ __forceinline__ void finish_cell(const LatticeDesc& d, const CollideP
         } else {
             velocity_compact<C>(m, Fp, u);
         }
-        store_u<UT>(u_out, k, (UT)u[0], (UT)u[1], (UT)u[2]);
+        store_u_from<UT, C>(u_out, k, u[0], u[1], u[2]);
         if (CPL == kCplDense) {
 #pragma unroll
             for (int q = 0; q < 3; ++q) Fprev[q * d.stride + k] = (FT)cp.body[q];

@@ -56,6 +56,17 @@ __device__ __forceinline__ void store_u<__half>(__half* u, int64_t k, __half a, 
     reinterpret_cast<uint2*>(u)[k] = make_uint2(*reinterpret_cast<const unsigned*>(&ab), *reinterpret_cast<const unsigned*>(&c0));
 }
 
+// The velocity from the compute type: FP16 converts two components per instruction.
+template <class UT, class C>
+__device__ __forceinline__ void store_u_from(UT* u, int64_t k, C a, C b, C c) {
+    store_u<UT>(u, k, (UT)a, (UT)b, (UT)c);
+}
+template <>
+__device__ __forceinline__ void store_u_from<__half, float>(__half* u, int64_t k, float a, float b, float c) {
+    const __half2 ab = __floats2half2_rn(a, b), c0 = __floats2half2_rn(c, 0.0f);
+    reinterpret_cast<uint2*>(u)[k] = make_uint2(*reinterpret_cast<const unsigned*>(&ab), *reinterpret_cast<const unsigned*>(&c0));
+}
+
 // BounceBack::collide (core/dynamics.hh:763-770): each population swaps with its opposite.
 template <class C>
 __device__ __forceinline__ void bounce_back_cell(C* f) {
