@@ -6,10 +6,11 @@
 // bounce-back wall, the tile's own rows of the opposite population, or the wall buffer on
 // finite-difference wall rows.  One warp per CTA moves these runs, and the tile's force
 // rows, into shared memory with bulk asynchronous copies (cp.async.bulk) that complete on
-// an mbarrier; the CTA is persistent and double-buffered, so the copies of tile t+1 are in
-// flight while tile t is collided.  The whole memory-level parallelism sits in the copy
-// engine instead of in registers, and every thread is left with shared-memory reads
-// (the +-1 x shift is an index offset, periodic in x), FP32 arithmetic and coalesced stores.
+// an mbarrier; the CTA is persistent with a ring of 2..8 stages (3 for FP16, two CTAs per SM;
+// 4 for FP32 / FP64), so the copies of the next tiles are in flight while a tile is collided.
+// The memory-level parallelism sits in the bulk-copy engine instead of in registers, and every
+// thread is left with shared-memory reads (the +-1 x shift is an index offset, periodic in x),
+// FP32 arithmetic and coalesced stores.
 //
 // Per lattice update the kernel moves exactly the algorithmic bytes: 19 populations read
 // and written once, the spread force read, the velocity field written (coupled step) and, with
