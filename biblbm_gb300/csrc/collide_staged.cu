@@ -10,7 +10,7 @@
 // 4 for FP32 / FP64), so the copies of the next tiles are in flight while a tile is collided.
 // The memory-level parallelism sits in the bulk-copy engine instead of in registers, and every
 // thread is left with shared-memory reads (the +-1 x shift is an index offset, periodic in x),
-// FP32 arithmetic and coalesced stores.
+// arithmetic in FP32 (FP64 for FP64 storage) and coalesced stores.
 //
 // Per lattice update the kernel moves exactly the algorithmic bytes: 19 populations read
 // and written once, the spread force read, the velocity field written (coupled step) and, with
