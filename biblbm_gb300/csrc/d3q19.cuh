@@ -162,19 +162,21 @@ __device__ __forceinline__ void relax_compact(C* f, const C* F, C omega, C S, co
         // Two relaxation times around the BGK equilibrium of j: the symmetric part of each
         // pair (i, i+9) relaxes with omega, the antisymmetric part with omega_minus (passed
         // in F[0]); feq+ = t_i (rhoBar + 4.5 (c.j)^2 / rho - 1.5 j.j / rho), feq- = 3 t_i c.j.
+        // Collected per pair: f_i' = a f_i + b f_i+9 + (w feq+ + w- feq-) and f_i+9' = a f_i+9 +
+        // b f_i + (w feq+ - w- feq-), with a = 1 - (w + w-)/2 and b = (w- - w)/2.
         const C omm = F[0];
         const C base = rb - C(1.5) * invRho * (j0 * j0 + j1 * j1 + j2 * j2);
         const C h = C(4.5) * invRho;
-        f[0] = fmac(-omega, f[0] - (S * weight<C>(0)) * base, f[0]);
+        const C a = C(1) - C(0.5) * (omega + omm), b = C(0.5) * (omm - omega);
+        const C oS = omega * S, mS3 = C(3) * omm * S;
+        f[0] = fmac(C(1) - omega, f[0], (oS * weight<C>(0)) * base);
 #pragma unroll
         for (int i = 1; i < 10; ++i) {
             const C cj = cdot<C>(i, j0, j1, j2);
-            const C tw = S * weight<C>(i);
-            const C ep = tw * fmac(h * cj, cj, base), em = tw * C(3) * cj;
-            const C dp = omega * (C(0.5) * (f[i] + f[i + 9]) - ep);
-            const C dm = omm * (C(0.5) * (f[i] - f[i + 9]) - em);
-            f[i] = f[i] - dp - dm;
-            f[i + 9] = f[i + 9] - dp + dm;
+            const C P = (oS * weight<C>(i)) * fmac(h * cj, cj, base), M = (mS3 * weight<C>(i)) * cj;
+            const C fi = f[i], fo = f[i + 9];
+            f[i] = fmac(a, fi, fmac(b, fo, P + M));
+            f[i + 9] = fmac(a, fo, fmac(b, fi, P - M));
         }
         return;
     }
